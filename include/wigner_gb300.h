@@ -1,0 +1,147 @@
+/*
+ * wigner_gb300.h - C ABI of the GB300-native Wigner-transport solve.
+ *
+ * Drop-in boundary for the 1D phase-space (x, xi->k) Wigner solve of the
+ * reference MATLAB simulator jonasneu1207/real_space_DG.  One handle owns the
+ * device state of a BATCH of problems that share the discretisation shape
+ * (N_el, N_K, Nk, N_xi, L_xi) but carry their own potential, masses, contact
+ * Fermi levels and device length.  Valleys x modes of one
+ * solve_transport_DG_2D call, bias points of a sweep or gate voltages map to
+ * batch entries.
+ *
+ * Conventions
+ *  - Plain C types only.  Complex vectors are interleaved (re, im) doubles,
+ *    the layout of MATLAB's interleaved-complex MEX API.
+ *  - State vector order (permute_shell = true, DG_code/core/get_Diff.m:66-84):
+ *    k fastest, then the local DG node, then the x element:
+ *    idx = (e*N_K + a)*Nk + j.  A batch stores problem b at offset b*N.
+ *  - Every call returns an int status (WG_OK ...).  The library never calls
+ *    exit/abort; wg_last_error(h) describes the last failure on a handle.
+ *  - A handle is thread-compatible: one host thread per handle at a time.
+ *
+ * Reference interfaces replaced (file:line in the reference project):
+ *  - solve_transport_DG_2D(mat,Esub,Vsub,EfL,EfR)   DG_code/solve_transport_DG_2D.m:1
+ *    -> wg_problem_create + wg_set_potential + wg_solve + wg_get_observables
+ *  - [A,rhs] = get_SysM(mat,p,EM)                    DG_code/core/get_SysM.m:1
+ *    -> wg_set_potential (operator data resident on the device) + wg_apply / wg_get_rhs
+ *  - rho = A\rhs                                     DG_code/solve_transport_DG_2D.m:101
+ *    -> wg_solve (restarted right-preconditioned GMRES + k-line preconditioner)
+ *  - preconditioner.apply(r)                         DG_code/core/get_LineTransversePreconditioner_full2D.m:199
+ *    -> wg_precondition
+ *  - DG.info.solve.{flag,relres,iterations,...}      DG_code/solve_transport_DG_full2D.m:279-334
+ *    -> wg_solve_info
+ *  - Gummel loop of RTD/solve2D_rtd_self_consistent.m:88-205 with the Poisson
+ *    step of RTD/solve_Poisson2D_rtd.m:56-186 (1D, Ny = 1)
+ *    -> wg_gummel_create / wg_gummel_run
+ *  - RK4 loop of DG_code/solve_transport_DG_2D_transient_SC_new.m:124-212
+ *    (Crank-Nicolson replaces RK4)                   -> wg_transient_step
+ */
+#ifndef WIGNER_GB300_H
+#define WIGNER_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes (error identifiers of the reference: DG:Full2D:*, RTD:*). */
+enum {
+  WG_OK = 0,
+  WG_NOT_CONVERGED = 1,   /* iterative solve stopped above tolerance: a status, not an error */
+  WG_ERR_ARG = 2,         /* invalid argument or size */
+  WG_ERR_OOM = 3,         /* device memory budget exceeded (DG:Full2D:GmresMemoryLimit) */
+  WG_ERR_TIMEOUT = 4,     /* bounded device wait ran out */
+  WG_ERR_CUDA = 5,        /* CUDA runtime error */
+  WG_ERR_NUMERIC = 6      /* NaN/Inf met in a reduction */
+};
+
+enum { WG_PREC_FP64 = 0, WG_PREC_MIXED = 1 };
+
+/* Discretisation shared by all problems of a handle (initParams.m:58-221). */
+typedef struct {
+  int n_el;          /* N_chi: x elements                          (initParams.m:59)  */
+  int n_local;       /* N_K_chi: DG nodes per element, 2..4        (initParams.m:58)  */
+  int nk;            /* Nk = mat.dg.params.N: k points             (initParams.m:62)  */
+  int n_xi;          /* N_xi: FV xi cells, >= nk                   (initParams.m:60)  */
+  double l_xi;       /* Ly: xi interval length [m]                 (initParams.m:110) */
+  double m_diff;     /* mass in Q_diff = hbar/m [kg]; <= 0 selects the reference's 0.041*m0 (initParams.m:102) */
+  double mpc;        /* MPC prefactor of A and rhs (solve_transport_DG_2D.m:95-98); 0 -> 1 */
+  int precision;     /* WG_PREC_FP64 (drop-in) or WG_PREC_MIXED */
+  int restart;       /* GMRES restart length m (basis m+1 vectors); 0 -> 50 */
+  double mem_budget_bytes; /* admission budget for this handle; 0 -> no limit */
+} wg_params;
+
+/* One problem's device/material data on the material grid (mat.x, nm). */
+typedef struct {
+  int nx;              /* mat.Nx = n_el*(n_local-1)+1 */
+  const double* x_nm;  /* [nx] material grid in nm, x_nm[0] = 0, x_nm[nx-1] = L_x */
+  const double* m_kg;  /* [nx] effective mass along x [kg] (mat.me_x(IV,:,mid)*m0) */
+  double me_z;         /* transverse mass, units of m0 (mat.me_z_ch) */
+  double temp;         /* mat.Temp [K] */
+} wg_device;
+
+typedef struct {
+  double tol;          /* relative residual target; 0 -> 1e-10 */
+  int maxit;           /* restart cycles; 0 -> 50 */
+  int use_rho0;        /* 1: warm start from the rho0 argument / the resident state */
+} wg_solve_opts;
+
+typedef struct {
+  int flag;            /* 0 converged, 1 not converged (iterativeStatus) */
+  int iterations;      /* inner Krylov iterations (all cycles) */
+  int cycles;          /* restart cycles run */
+  int refinements;     /* outer FP64 refinement steps (mixed form; 0 for FP64) */
+  double relres;       /* true relative residual |b - A x| / |b| in FP64 */
+  double initial_relres; /* |b - A x0| / |b| (1 without warm start) */
+  double rhs_norm;     /* |b| */
+} wg_solve_info;
+
+typedef struct wg_problem wg_problem;
+
+/* Create a handle for `batch` problems.  Allocates all device memory. */
+int wg_problem_create(const wg_params* prm, int batch, wg_problem** out);
+int wg_problem_destroy(wg_problem* h);
+const char* wg_last_error(const wg_problem* h);
+/* Library-level last error (for failures before a handle exists). */
+const char* wg_global_error(void);
+
+/* Sizes: N per problem (complex entries), batch, bytes of device memory held. */
+int wg_problem_sizes(const wg_problem* h, long long* n_per_problem, int* batch, double* device_bytes);
+
+/* Set problem b's potential (Esub [eV] on the material grid), masses and the
+ * contact Fermi levels.  Rebuilds on the device: the Wigner-potential kernel
+ * data Vw(x,k) (get_Drift_accel_trial_permutedShell.m:64-147), the contact
+ * inflow (verteilung.m:118-170, get_Diff.m:77-83) and the line factors. */
+int wg_set_potential(wg_problem* h, int b, const wg_device* dev, const double* esub_ev,
+                     double ef_l, double ef_r);
+
+/* Solve A rho = rhs for every problem of the batch.  rho0 (nullable, batch*N
+ * complex) is a physical warm start; with opts->use_rho0 and rho0 == NULL the
+ * resident solution of the previous solve is the warm start.  info has batch
+ * entries.  Returns WG_OK when every problem converged, WG_NOT_CONVERGED when
+ * at least one did not (see info[b].flag). */
+int wg_solve(wg_problem* h, const wg_solve_opts* opts, const double* rho0, wg_solve_info* info);
+
+/* Copy problem b's solution (N complex) to the host. */
+int wg_get_rho(wg_problem* h, int b, double* rho);
+
+/* Problem b's charge and current density at the DG nodes (n_el*n_local each):
+ * n_dg = Re of the centre-xi value of Phi*rho, j = q hbar/m Im(d rho_u/d xi)
+ * (solve_transport_DG_2D.m:114-156). */
+int wg_get_observables(wg_problem* h, int b, double* n_dg, double* j);
+
+/* Problem b's Wigner function on the xi grid, rho_u = Phi * rho per DG node
+ * (solve_transport_DG_2D.m:118, DG.RHO(IV,IM,:,:)): n_el*n_local rows of
+ * n_xi complex values (row = DG node, xi fastest). */
+int wg_get_rho_xi(wg_problem* h, int b, double* rho_u);
+
+/* y = A x for the whole batch (host buffers, batch*N complex each). */
+int wg_apply(wg_problem* h, const double* x, double* y);
+/* z = M^-1 r with the k-line preconditioner (host buffers). */
+int wg_precondition(wg_problem* h, const double* r, double* z);
+/* The batch's right-hand sides (batch*N complex). */
+int wg_get_rhs(wg_problem* h, double* rhs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WIGNER_GB300_H */

@@ -1,0 +1,100 @@
+"""ctypes binding of libwigner_gb300.so (the C ABI of include/wigner_gb300.h).
+
+The library is built in-tree by real_space_dg_gb300/build.py.  Loading fails
+loudly when it is missing: there is no CPU fallback for the product path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libwigner_gb300.so")
+
+WG_OK, WG_NOT_CONVERGED, WG_ERR_ARG, WG_ERR_OOM, WG_ERR_TIMEOUT, WG_ERR_CUDA, WG_ERR_NUMERIC = range(7)
+WG_PREC_FP64, WG_PREC_MIXED = 0, 1
+STATUS_NAMES = {0: "WG_OK", 1: "WG_NOT_CONVERGED", 2: "WG_ERR_ARG", 3: "WG_ERR_OOM", 4: "WG_ERR_TIMEOUT",
+                5: "WG_ERR_CUDA", 6: "WG_ERR_NUMERIC"}
+# Error identifiers of the reference (DG:Full2D:*), by status.
+ERROR_IDS = {WG_ERR_ARG: "DG:Full2D:InvalidArgument", WG_ERR_OOM: "DG:Full2D:GmresMemoryLimit",
+             WG_ERR_TIMEOUT: "DG:Full2D:Timeout", WG_ERR_CUDA: "DG:Full2D:CUDA",
+             WG_ERR_NUMERIC: "DG:Full2D:NonFinite"}
+
+
+class WgParams(C.Structure):
+    _fields_ = [("n_el", C.c_int), ("n_local", C.c_int), ("nk", C.c_int), ("n_xi", C.c_int),
+                ("l_xi", C.c_double), ("m_diff", C.c_double), ("mpc", C.c_double), ("precision", C.c_int),
+                ("restart", C.c_int), ("mem_budget_bytes", C.c_double)]
+
+
+class WgDevice(C.Structure):
+    _fields_ = [("nx", C.c_int), ("x_nm", C.POINTER(C.c_double)), ("m_kg", C.POINTER(C.c_double)),
+                ("me_z", C.c_double), ("temp", C.c_double)]
+
+
+class WgSolveOpts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("use_rho0", C.c_int)]
+
+
+class WgSolveInfo(C.Structure):
+    _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("cycles", C.c_int), ("refinements", C.c_int),
+                ("relres", C.c_double), ("initial_relres", C.c_double), ("rhs_norm", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+# Every symbol the header declares, with its ctypes signature.
+_H = C.c_void_p
+_D = C.POINTER(C.c_double)
+SIGNATURES = {
+    "wg_problem_create": ([C.POINTER(WgParams), C.c_int, C.POINTER(_H)], C.c_int),
+    "wg_problem_destroy": ([_H], C.c_int),
+    "wg_last_error": ([_H], C.c_char_p),
+    "wg_global_error": ([], C.c_char_p),
+    "wg_problem_sizes": ([_H, C.POINTER(C.c_longlong), C.POINTER(C.c_int), _D], C.c_int),
+    "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),
+    "wg_solve": ([_H, C.POINTER(WgSolveOpts), _D, C.POINTER(WgSolveInfo)], C.c_int),
+    "wg_get_rho": ([_H, C.c_int, _D], C.c_int),
+    "wg_get_observables": ([_H, C.c_int, _D, _D], C.c_int),
+    "wg_get_rho_xi": ([_H, C.c_int, _D], C.c_int),
+    "wg_apply": ([_H, _D, _D], C.c_int),
+    "wg_precondition": ([_H, _D, _D], C.c_int),
+    "wg_get_rhs": ([_H, _D], C.c_int),
+}
+
+_lib = None
+
+
+class WignerError(RuntimeError):
+    """Raised for every non-OK status except WG_NOT_CONVERGED (which is a status)."""
+
+    def __init__(self, status, message):
+        self.status = status
+        self.identifier = ERROR_IDS.get(status, "DG:Full2D:Error")
+        super().__init__("%s (%s): %s" % (self.identifier, STATUS_NAMES.get(status, status), message))
+
+
+def load(path=LIB_PATH):
+    """Load the library and bind every declared symbol (no GPU call is made)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libwigner_gb300.so is not built (%s); run real_space_dg_gb300.build.build() "
+                          "or __graft_entry__.build(). There is no CPU fallback." % path)
+    lib = C.CDLL(path)
+    for name, (argtypes, restype) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = restype
+    _lib = lib
+    return lib
+
+
+def dptr(a):
+    return a.ctypes.data_as(_D)
+
+
+def as_c128(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)

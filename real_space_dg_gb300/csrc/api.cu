@@ -1,0 +1,395 @@
+// C ABI entry points of the Wigner-transport library (see include/wigner_gb300.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "problem.h"
+
+struct wg_problem {
+  wg::Problem P;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(wg::Problem* P, int code, const std::string& msg) {
+  if (P) P->err = msg;
+  g_err = msg;
+  return code;
+}
+
+#define API_CK(P, expr)                                                                    \
+  do {                                                                                     \
+    cudaError_t e_ = (expr);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(P, WG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #expr); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count, double& bytes) {
+  bytes += (double)sizeof(T) * (double)count;
+  return cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(count, 1));
+}
+
+void free_all(wg::Problem& P) {
+  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.qd, P.beta, P.xq, P.pot_x,
+                  P.pot_v, P.m_nodes, P.rhs, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
+                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.target, P.active, P.kused, P.any_active,
+                  P.mx.phi16, P.mx.xin16, P.mx.V, P.mx.w, P.mx.z, P.mx.xh, P.mx.yh, P.mx.beta};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (P.stream) cudaStreamDestroy(P.stream);
+  P.stream = nullptr;
+}
+
+// Small dense inverse (row-major) for the k-line factors.
+bool inv_small(const double* A, double* out, int n) {
+  double a[wg::kMaxLocal * wg::kMaxLocal];
+  std::memcpy(a, A, sizeof(double) * n * n);
+  for (int i = 0; i < n * n; ++i) out[i] = 0;
+  for (int i = 0; i < n; ++i) out[i * n + i] = 1;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r)
+      if (std::fabs(a[r * n + c]) > std::fabs(a[piv * n + c])) piv = r;
+    if (a[piv * n + c] == 0.0) return false;
+    if (piv != c)
+      for (int k = 0; k < n; ++k) {
+        std::swap(a[c * n + k], a[piv * n + k]);
+        std::swap(out[c * n + k], out[piv * n + k]);
+      }
+    const double d = a[c * n + c];
+    for (int k = 0; k < n; ++k) { a[c * n + k] /= d; out[c * n + k] /= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = a[r * n + c];
+      for (int k = 0; k < n; ++k) { a[r * n + k] -= f * a[c * n + k]; out[r * n + k] -= f * out[c * n + k]; }
+    }
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* wg_global_error(void) { return g_err.c_str(); }
+
+const char* wg_last_error(const wg_problem* h) { return h ? h->P.err.c_str() : g_err.c_str(); }
+
+int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
+  if (!prm || !out || batch < 1) return fail(nullptr, WG_ERR_ARG, "wg_problem_create: null argument or batch < 1");
+  *out = nullptr;
+  wg_problem* h = new (std::nothrow) wg_problem();
+  if (!h) return fail(nullptr, WG_ERR_OOM, "host allocation failed");
+  wg::Problem& P = h->P;
+  std::string e = wg::build_shape(P.s, prm->n_el, prm->n_local, prm->nk, prm->n_xi, prm->l_xi, prm->m_diff, prm->mpc);
+  if (!e.empty()) {
+    delete h;
+    return fail(nullptr, WG_ERR_ARG, "wg_problem_create: " + e);
+  }
+  if (prm->precision != WG_PREC_FP64 && prm->precision != WG_PREC_MIXED) {
+    delete h;
+    return fail(nullptr, WG_ERR_ARG, "wg_problem_create: unknown precision");
+  }
+  P.batch = batch;
+  P.precision = prm->precision;
+  P.restart = prm->restart > 0 ? prm->restart : 50;
+  P.mem_budget = prm->mem_budget_bytes;
+  const wg::Shape& s = P.s;
+  const int nK = s.nK;
+  P.N = (long long)s.n_el * nK * s.nk;
+  P.ncols = (long long)batch * s.n_el * nK;
+  P.nx = s.n_el * (nK - 1) + 1;
+  P.nchunk = (int)std::min<long long>(128, std::max<long long>(1, (P.N + 2047) / 2048));
+  const long long BN = P.N * batch;
+  const int mp1 = P.restart + 1;
+  // memory estimate before allocating (GmresMemoryLimit analogue)
+  double est = 16.0 * BN * (5 + mp1) + 16.0 * 2 * s.nxi * P.ncols +
+               8.0 * batch * s.n_el * nK * nK * (s.nxi + 1) + 16.0 * s.nxi * s.nk;
+  if (P.mem_budget > 0 && est > P.mem_budget) {
+    delete h;
+    return fail(nullptr, WG_ERR_OOM,
+                "wg_problem_create: estimated device memory " + std::to_string(est / 1073741824.0) +
+                    " GiB exceeds the admission budget");
+  }
+  P.fb.nK = nK;
+  for (int i = 0; i < nK * nK; ++i) {
+    P.fb.K1[i] = s.K1[i];
+    P.fb.K2[i] = s.K2[i];
+    P.fb.K3[i] = s.K3[i];
+    P.fb.K5[i] = s.K5[i];
+  }
+  double bytes = 0;
+  cudaError_t ce = cudaSuccess;
+  auto A = [&](cudaError_t r) {
+    if (ce == cudaSuccess) ce = r;
+  };
+  A(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
+  A(dalloc(&P.phi, (size_t)s.nxi * s.nk, bytes));
+  A(dalloc(&P.kvec, s.nk, bytes));
+  A(dalloc(&P.xi_edge, s.nxi + 1, bytes));
+  A(dalloc(&P.kap, (size_t)nK * nK * wg::kNqx, bytes));
+  A(dalloc(&P.betai, (size_t)nK * nK * (s.nxi + 1), bytes));
+  A(dalloc(&P.pre_dinv, (size_t)s.nk * nK * nK, bytes));
+  A(dalloc(&P.pre_h, (size_t)s.nk * nK, bytes));
+  A(dalloc(&P.qd, batch, bytes));
+  A(dalloc(&P.beta, (size_t)batch * s.n_el * nK * nK * (s.nxi + 1), bytes));
+  A(dalloc(&P.xq, (size_t)batch * s.n_el * wg::kNqx, bytes));
+  A(dalloc(&P.pot_x, (size_t)batch * P.nx, bytes));
+  A(dalloc(&P.pot_v, (size_t)batch * P.nx, bytes));
+  A(dalloc(&P.m_nodes, (size_t)batch * s.n_el * nK, bytes));
+  A(dalloc(&P.rhs, BN, bytes));
+  A(dalloc(&P.x, BN, bytes));
+  A(dalloc(&P.w, BN, bytes));
+  A(dalloc(&P.z, BN, bytes));
+  A(dalloc(&P.r, BN, bytes));
+  A(dalloc(&P.V, (size_t)BN * mp1, bytes));
+  A(dalloc(&P.xh, (size_t)s.nxi * P.ncols, bytes));
+  A(dalloc(&P.yh, (size_t)s.nxi * P.ncols, bytes));
+  A(dalloc(&P.H, (size_t)batch * mp1 * P.restart, bytes));
+  A(dalloc(&P.cs, (size_t)batch * P.restart, bytes));
+  A(dalloc(&P.sn, (size_t)batch * P.restart, bytes));
+  A(dalloc(&P.g, (size_t)batch * mp1, bytes));
+  A(dalloc(&P.hcol, (size_t)batch * mp1, bytes));
+  A(dalloc(&P.ycoef, (size_t)batch * P.restart, bytes));
+  A(dalloc(&P.partial, (size_t)batch * mp1 * P.nchunk, bytes));
+  A(dalloc(&P.nrm_partial, (size_t)batch * P.nchunk, bytes));
+  A(dalloc(&P.nrm, batch, bytes));
+  A(dalloc(&P.target, batch, bytes));
+  A(dalloc(&P.active, batch, bytes));
+  A(dalloc(&P.kused, batch, bytes));
+  A(dalloc(&P.any_active, 1, bytes));
+  P.device_bytes = bytes;
+  if (ce != cudaSuccess) {
+    std::string msg = std::string("wg_problem_create: device allocation failed: ") + cudaGetErrorString(ce);
+    free_all(P);
+    delete h;
+    cudaGetLastError();
+    return fail(nullptr, ce == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA, msg);
+  }
+  // constant data
+  std::vector<double2> phi((size_t)s.nxi * s.nk);
+  for (size_t i = 0; i < phi.size(); ++i) phi[i] = make_double2(s.phi[i].real(), s.phi[i].imag());
+  std::vector<double> betai((size_t)nK * nK * (s.nxi + 1));
+  for (int ac = 0; ac < nK * nK; ++ac)
+    for (int i = 0; i <= s.nxi; ++i)
+      betai[(size_t)ac * (s.nxi + 1) + i] = -(s.delta_xi / 4 * s.mpc) * s.kap_sum[ac] * s.cap[i];
+  // k-line factors: D0 = k K1 + |k| K2, h = D0^-1 * coupling column
+  std::vector<double> dinv((size_t)s.nk * nK * nK), hv((size_t)s.nk * nK);
+  double kmax = 0;
+  for (double kk : s.k) kmax = std::max(kmax, std::fabs(kk));
+  for (int j = 0; j < s.nk; ++j) {
+    const double k = s.k[j], ak = std::fabs(k);
+    double D[wg::kMaxLocal * wg::kMaxLocal], Di[wg::kMaxLocal * wg::kMaxLocal], g[wg::kMaxLocal];
+    for (int i = 0; i < nK * nK; ++i) D[i] = k * s.K1[i] + ak * s.K2[i];
+    bool ok = k != 0.0 && inv_small(D, Di, nK);
+    if (!ok) {
+      // k = 0 (odd Nk): the flux vanishes; a shifted identity keeps M^-1 regular
+      for (int i = 0; i < nK * nK; ++i) Di[i] = 0;
+      double nrm = 0;
+      for (int i = 0; i < nK * nK; ++i) nrm = std::max(nrm, std::fabs(s.K1[i]) + std::fabs(s.K2[i]));
+      const double sigma = 0.003 * kmax * std::max(nrm, 1e-300);
+      for (int i = 0; i < nK; ++i) Di[i * nK + i] = 1.0 / sigma;
+    }
+    for (int a = 0; a < nK; ++a) g[a] = k > 0 ? (k + ak) * s.K3[a * nK + nK - 1] : (k < 0 ? (k - ak) * s.K5[a * nK + 0] : 0.0);
+    for (int a = 0; a < nK; ++a) {
+      double acc = 0;
+      for (int c = 0; c < nK; ++c) acc += Di[a * nK + c] * g[c];
+      hv[(size_t)j * nK + a] = acc;
+    }
+    for (int i = 0; i < nK * nK; ++i) dinv[(size_t)j * nK * nK + i] = Di[i];
+  }
+  API_CK(&P, cudaMemcpyAsync(P.phi, phi.data(), sizeof(double2) * phi.size(), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.kvec, s.k.data(), sizeof(double) * s.nk, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.xi_edge, s.xi_edge.data(), sizeof(double) * (s.nxi + 1), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.kap, s.kap.data(), sizeof(double) * s.kap.size(), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.betai, betai.data(), sizeof(double) * betai.size(), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.pre_dinv, dinv.data(), sizeof(double) * dinv.size(), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.pre_h, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.rhs, 0, sizeof(double2) * BN, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.x, 0, sizeof(double2) * BN, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.beta, 0, sizeof(double) * batch * s.n_el * nK * nK * (s.nxi + 1), P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  P.hp.resize(batch);
+  P.h_nrm.resize(batch);
+  P.h_active.resize(batch);
+  P.h_kused.resize(batch);
+  *out = h;
+  return WG_OK;
+}
+
+int wg_problem_destroy(wg_problem* h) {
+  if (!h) return WG_OK;
+  if (h->P.stream) cudaStreamSynchronize(h->P.stream);
+  free_all(h->P);
+  delete h;
+  return WG_OK;
+}
+
+int wg_problem_sizes(const wg_problem* h, long long* n_per_problem, int* batch, double* device_bytes) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  if (n_per_problem) *n_per_problem = h->P.N;
+  if (batch) *batch = h->P.batch;
+  if (device_bytes) *device_bytes = h->P.device_bytes;
+  return WG_OK;
+}
+
+int wg_set_potential(wg_problem* h, int b, const wg_device* dev, const double* esub_ev, double ef_l, double ef_r) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_set_potential: batch index out of range");
+  if (!dev || !esub_ev || !dev->x_nm || !dev->m_kg) return fail(&P, WG_ERR_ARG, "wg_set_potential: null argument");
+  if (dev->nx != P.nx)
+    return fail(&P, WG_ERR_ARG, "wg_set_potential: nx must equal n_el*(n_local-1)+1 = " + std::to_string(P.nx));
+  const wg::Shape& s = P.s;
+  const int nK = s.nK, nx = dev->nx;
+  for (int i = 0; i < nx; ++i) {
+    if (!std::isfinite(esub_ev[i]) || !std::isfinite(dev->x_nm[i]) || !std::isfinite(dev->m_kg[i]))
+      return fail(&P, WG_ERR_ARG, "wg_set_potential: non-finite potential, grid or mass");
+    if (i > 0 && !(dev->x_nm[i] > dev->x_nm[i - 1]))
+      return fail(&P, WG_ERR_ARG, "wg_set_potential: x_nm must be strictly increasing");
+  }
+  if (dev->x_nm[0] != 0.0) return fail(&P, WG_ERR_ARG, "wg_set_potential: x_nm[0] must be 0");
+  if (!std::isfinite(ef_l) || !std::isfinite(ef_r)) return fail(&P, WG_ERR_ARG, "wg_set_potential: non-finite Fermi level");
+  wg::HostProblem& hp = P.hp[b];
+  hp.l_chi = dev->x_nm[nx - 1] * 1e-9;
+  const double detJ = hp.l_chi / s.n_el / 2;
+  hp.qd = s.q_diff / detJ * s.mpc;
+  hp.vmin = *std::min_element(esub_ev, esub_ev + nx);
+  std::string e = wg::contact_inflow(s, esub_ev, dev->m_kg, nx, dev->me_z, dev->temp, ef_l, ef_r, hp.fnl, hp.fnr);
+  if (!e.empty()) return fail(&P, WG_ERR_ARG, "wg_set_potential: " + e);
+  hp.m_nodes.resize((size_t)s.n_el * nK);
+  for (int el = 0; el < s.n_el; ++el)
+    for (int a = 0; a < nK; ++a) hp.m_nodes[(size_t)el * nK + a] = dev->m_kg[el * (nK - 1) + a];
+  std::vector<double> xq, xg(nx);
+  wg::quad_points(s, hp.l_chi, xq);
+  for (int i = 0; i < nx; ++i) xg[i] = dev->x_nm[i] * 1e-9;
+  // contact inflow blocks: first element (k > 0) and last element (k < 0), get_Diff.m:77-83
+  std::vector<double2> rfirst((size_t)nK * s.nk), rlast((size_t)nK * s.nk);
+  for (int a = 0; a < nK; ++a)
+    for (int j = 0; j < s.nk; ++j) {
+      const double k = s.k[j], ak = std::fabs(k);
+      const double q1 = s.invM[a * nK + 0] / detJ, q2 = s.invM[a * nK + nK - 1] / detJ;
+      const wg::cplx vl = (k > 0 ? 1.0 : 0.0) * (ak * hp.fnl[j]);
+      const wg::cplx vr = (k < 0 ? 1.0 : 0.0) * (ak * hp.fnr[j]);
+      const wg::cplx tl = s.mpc * (s.q_diff * (q1 * vl));
+      const wg::cplx tr = s.mpc * (s.q_diff * (q2 * vr));
+      rfirst[(size_t)a * s.nk + j] = make_double2(tl.real(), tl.imag());
+      rlast[(size_t)a * s.nk + j] = make_double2(tr.real(), tr.imag());
+    }
+  const size_t blk = (size_t)nK * s.nk;
+  double2* rb = P.rhs + (long long)b * P.N;
+  API_CK(&P, cudaMemcpyAsync(rb, rfirst.data(), sizeof(double2) * blk, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(rb + (long long)(s.n_el - 1) * blk, rlast.data(), sizeof(double2) * blk,
+                             cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.xq + (long long)b * s.n_el * wg::kNqx, xq.data(), sizeof(double) * xq.size(),
+                             cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.pot_x + (long long)b * nx, xg.data(), sizeof(double) * nx, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.pot_v + (long long)b * nx, esub_ev, sizeof(double) * nx, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.m_nodes + (long long)b * s.n_el * nK, hp.m_nodes.data(), sizeof(double) * hp.m_nodes.size(),
+                             cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.qd + b, &hp.qd, sizeof(double), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, wg::launch_vw_rebuild(P, b));
+  // host vectors above go out of scope: wait for the copies
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  hp.ready = true;
+  return WG_OK;
+}
+
+int wg_solve(wg_problem* h, const wg_solve_opts* opts, const double* rho0, wg_solve_info* info) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (!info) return fail(&P, WG_ERR_ARG, "wg_solve: info must hold batch entries");
+  for (int b = 0; b < P.batch; ++b)
+    if (!P.hp[b].ready) return fail(&P, WG_ERR_ARG, "wg_solve: wg_set_potential not called for problem " + std::to_string(b));
+  wg_solve_opts o{};
+  if (opts) o = *opts;
+  if (o.tol < 0 || !std::isfinite(o.tol)) return fail(&P, WG_ERR_ARG, "wg_solve: tol must be >= 0 and finite");
+  bool warm = false;
+  if (rho0) {
+    const long long n = P.N * P.batch;
+    for (long long i = 0; i < 2 * n; ++i)
+      if (!std::isfinite(rho0[i])) return fail(&P, WG_ERR_ARG, "wg_solve: rho0 must contain only finite values");
+    API_CK(&P, cudaMemcpyAsync(P.x, rho0, sizeof(double2) * n, cudaMemcpyHostToDevice, P.stream));
+    warm = true;
+  } else if (o.use_rho0) {
+    warm = true;
+  }
+  std::memset(info, 0, sizeof(wg_solve_info) * P.batch);
+  int rc = wg::gmres_solve_fp64(P, o, warm, info);
+  if (rc == WG_ERR_CUDA || rc == WG_ERR_NUMERIC) fail(&P, rc, P.err);
+  return rc;
+}
+
+int wg_get_rho(wg_problem* h, int b, double* rho) {
+  if (!h || !rho) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_get_rho: null argument");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_get_rho: batch index out of range");
+  API_CK(&P, cudaMemcpyAsync(rho, P.x + (long long)b * P.N, sizeof(double2) * P.N, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_get_observables(wg_problem* h, int b, double* n_dg, double* j) {
+  if (!h || !n_dg || !j) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_get_observables: null argument");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_get_observables: batch index out of range");
+  const int ncol = P.s.n_el * P.s.nK;
+  // two small outputs: reuse the norm-partial scratch when it is large enough, else the xh buffer
+  double* dn = reinterpret_cast<double*>(P.xh);
+  API_CK(&P, wg::launch_observables(P, b, dn, dn + ncol));
+  API_CK(&P, cudaMemcpyAsync(n_dg, dn, sizeof(double) * ncol, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaMemcpyAsync(j, dn + ncol, sizeof(double) * ncol, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_get_rho_xi(wg_problem* h, int b, double* rho_u) {
+  if (!h || !rho_u) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_get_rho_xi: null argument");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_get_rho_xi: batch index out of range");
+  const long long n = (long long)P.s.n_el * P.s.nK * P.s.nxi;
+  API_CK(&P, wg::launch_rho_xi(P, b, P.yh));
+  API_CK(&P, cudaMemcpyAsync(rho_u, P.yh, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_apply(wg_problem* h, const double* x, double* y) {
+  if (!h || !x || !y) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_apply: null argument");
+  wg::Problem& P = h->P;
+  const long long n = P.N * P.batch;
+  API_CK(&P, cudaMemcpyAsync(P.z, x, sizeof(double2) * n, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, wg::launch_apply(P, P.z, P.w));
+  API_CK(&P, cudaMemcpyAsync(y, P.w, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_precondition(wg_problem* h, const double* r, double* z) {
+  if (!h || !r || !z) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_precondition: null argument");
+  wg::Problem& P = h->P;
+  const long long n = P.N * P.batch;
+  API_CK(&P, cudaMemcpyAsync(P.r, r, sizeof(double2) * n, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, wg::launch_precondition(P, P.r, P.N, P.z));
+  API_CK(&P, cudaMemcpyAsync(z, P.z, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_get_rhs(wg_problem* h, double* rhs) {
+  if (!h || !rhs) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_get_rhs: null argument");
+  wg::Problem& P = h->P;
+  API_CK(&P, cudaMemcpyAsync(rhs, P.rhs, sizeof(double2) * P.N * P.batch, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+}  // extern "C"

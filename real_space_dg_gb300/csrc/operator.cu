@@ -1,0 +1,500 @@
+// FP64 operator kernels of the 1D Wigner transport solve (sm_103a).
+//
+// y = A x is applied matrix-free in three parts (the factorised form of
+// get_SysM.m:1-16 = get_Diff.m:66-84 + get_Drift_accel_trial_permutedShell.m:64-333):
+//   1. flux_kernel       upwind x-flux times diag(k): per k a block-bidiagonal
+//                        stencil over elements (HBM-bound streaming kernel)
+//   2. zgemm_kernel      X^ = Phi X over every DG node of the batch (one GEMM),
+//      stencil_kernel    Y^_{e,a} = sum_b T(beta_{e,ab}) X^_{e,b} (xi-tridiagonal),
+//      zgemm_kernel      y += i Phi^H Y^ (second GEMM, accumulating epilogue)
+// plus the k-line preconditioner, the Vw(x,k) rebuild and the observables.
+#include <cuda_runtime.h>
+
+#include "problem.h"
+
+namespace wg {
+
+namespace {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
+
+// ---------------------------------------------------------------------------
+// 1. Upwind flux: y_{e,.,j} = qd_b [ (k K1 + |k| K2) x_e + (k+|k|) K3 x_{e-1}
+//                                   + (k-|k|) K5 x_{e+1} ]_j
+// One thread per (b, e, j); k fastest so every load/store is coalesced.
+// ---------------------------------------------------------------------------
+template <int NK>
+__global__ void __launch_bounds__(256) flux_kernel(const double2* __restrict__ x, double2* __restrict__ y,
+                                                   const double* __restrict__ kvec,
+                                                   const double* __restrict__ qd, FluxBlocks fb, int n_el,
+                                                   int nk, long long total) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int j = (int)(t % nk);
+  const long long be = t / nk;          // b * n_el + e
+  const int e = (int)(be % n_el);
+  const int b = (int)(be / n_el);
+  const double k = kvec[j];
+  const double ak = fabs(k);
+  const double s = qd[b];
+  const double2* xe = x + be * (long long)NK * nk + j;
+  double2 xv[NK];
+#pragma unroll
+  for (int c = 0; c < NK; ++c) xv[c] = xe[(long long)c * nk];
+  double2 acc[NK];
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const double m = k * fb.K1[a * NK + c] + ak * fb.K2[a * NK + c];
+      v.x += m * xv[c].x;
+      v.y += m * xv[c].y;
+    }
+    acc[a] = v;
+  }
+  if (k > 0 && e > 0) {
+    const double2* xl = xe - (long long)NK * nk;
+    double2 xp[NK];
+#pragma unroll
+    for (int c = 0; c < NK; ++c) xp[c] = xl[(long long)c * nk];
+#pragma unroll
+    for (int a = 0; a < NK; ++a)
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        const double m = (k + ak) * fb.K3[a * NK + c];
+        acc[a].x += m * xp[c].x;
+        acc[a].y += m * xp[c].y;
+      }
+  } else if (k < 0 && e < n_el - 1) {
+    const double2* xr = xe + (long long)NK * nk;
+    double2 xp[NK];
+#pragma unroll
+    for (int c = 0; c < NK; ++c) xp[c] = xr[(long long)c * nk];
+#pragma unroll
+    for (int a = 0; a < NK; ++a)
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        const double m = (k - ak) * fb.K5[a * NK + c];
+        acc[a].x += m * xp[c].x;
+        acc[a].y += m * xp[c].y;
+      }
+  }
+  double2* ye = y + be * (long long)NK * nk + j;
+#pragma unroll
+  for (int a = 0; a < NK; ++a) ye[(long long)a * nk] = cscale(s, acc[a]);
+}
+
+// ---------------------------------------------------------------------------
+// 2a. Complex FP64 GEMM  C(M x Ncol) = op(A)(M x K) * B(K x Ncol), column-major
+// B and C with leading dimensions ldb = K, ldc = M.
+//   MODE 0: A(m,k) = phi[m*lda + k]        C  = acc        (X^ = Phi X)
+//   MODE 1: A(m,k) = conj(phi[k*lda + m])  C += i * acc    (y += i Phi^H Y^)
+// 64x64 output tile, 256 threads, 4x4 complex outputs per thread, BK = 8.
+// ---------------------------------------------------------------------------
+constexpr int GBM = 64, GBN = 64, GBK = 8;
+
+template <int MODE>
+__global__ void __launch_bounds__(256) zgemm_kernel(const double2* __restrict__ A, int lda,
+                                                   const double2* __restrict__ Bm, double2* __restrict__ C, int M,
+                                                   int K, long long Ncol) {
+  __shared__ double2 As[2][GBK][GBM];
+  __shared__ double2 Bs[2][GBK][GBN];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = blockIdx.y * GBM;
+  const long long n0 = (long long)blockIdx.x * GBN;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) acc[i][jj] = make_double2(0.0, 0.0);
+
+  auto load = [&](int buf, int k0) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int idx = tid + r * 256;
+      int mm, kk;
+      if (MODE == 0) { mm = idx >> 3; kk = idx & 7; } else { kk = idx >> 6; mm = idx & 63; }
+      const int gm = m0 + mm, gk = k0 + kk;
+      double2 v = make_double2(0.0, 0.0);
+      if (gm < M && gk < K) {
+        if (MODE == 0) {
+          v = A[(long long)gm * lda + gk];
+        } else {
+          v = A[(long long)gk * lda + gm];
+          v.y = -v.y;
+        }
+      }
+      As[buf][kk][mm] = v;
+      const int nn = idx >> 3, kb = idx & 7;
+      const long long gn = n0 + nn;
+      double2 bv = make_double2(0.0, 0.0);
+      if (gn < Ncol && k0 + kb < K) bv = Bm[gn * K + k0 + kb];
+      Bs[buf][kb][nn] = bv;
+    }
+  };
+
+  const int nkt = (K + GBK - 1) / GBK;
+  load(0, 0);
+  __syncthreads();
+  for (int kt = 0; kt < nkt; ++kt) {
+    const int cur = kt & 1;
+    if (kt + 1 < nkt) load(cur ^ 1, (kt + 1) * GBK);
+#pragma unroll
+    for (int kk = 0; kk < GBK; ++kk) {
+      double2 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[cur][kk][tx + 16 * i];
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) b[jj] = Bs[cur][kk][ty + 16 * jj];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          acc[i][jj].x = fma(a[i].x, b[jj].x, fma(-a[i].y, b[jj].y, acc[i][jj].x));
+          acc[i][jj].y = fma(a[i].x, b[jj].y, fma(a[i].y, b[jj].x, acc[i][jj].y));
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int gm = m0 + tx + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const long long gn = n0 + ty + 16 * jj;
+      if (gn >= Ncol) continue;
+      double2* c = C + gn * M + gm;
+      if (MODE == 0) {
+        *c = acc[i][jj];
+      } else {
+        double2 o = *c;
+        o.x -= acc[i][jj].y;
+        o.y += acc[i][jj].x;
+        *c = o;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 2b. xi stencil: Y^_{e,a}(s) = sum_c beta_{ac}(s) (X^_c(s) + X^_c(s-1))
+//                               + beta_{ac}(s+1) (X^_c(s) + X^_c(s+1))
+// beta = betar[b][e][ac][s] + i * betai[ac][s] (potential + CAP parts).
+// One thread per (element of the batch, s); s fastest.
+// ---------------------------------------------------------------------------
+template <int NK>
+__global__ void __launch_bounds__(256) stencil_kernel(const double2* __restrict__ xh, double2* __restrict__ yh,
+                                                      const double* __restrict__ betar,
+                                                      const double* __restrict__ betai, int nxi,
+                                                      long long nelem_batch) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelem_batch * nxi) return;
+  const int s = (int)(t % nxi);
+  const long long be = t / nxi;
+  const int ne = nxi + 1;
+  const double2* X = xh + be * NK * (long long)nxi;
+  double2 sm[NK], sp[NK];
+#pragma unroll
+  for (int c = 0; c < NK; ++c) {
+    const double2 x0 = X[(long long)c * nxi + s];
+    const double2 xm = s > 0 ? X[(long long)c * nxi + s - 1] : make_double2(0.0, 0.0);
+    const double2 xp = s < nxi - 1 ? X[(long long)c * nxi + s + 1] : make_double2(0.0, 0.0);
+    sm[c] = cadd(x0, xm);
+    sp[c] = cadd(x0, xp);
+  }
+  const double* br = betar + be * (long long)NK * NK * ne;
+  double2* Y = yh + be * NK * (long long)nxi;
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const int ac = a * NK + c;
+      const double2 b0 = make_double2(br[(long long)ac * ne + s], betai[ac * ne + s]);
+      const double2 b1 = make_double2(br[(long long)ac * ne + s + 1], betai[ac * ne + s + 1]);
+      v = cadd(v, cadd(cmul(b0, sm[c]), cmul(b1, sp[c])));
+    }
+    Y[(long long)a * nxi + s] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k-line preconditioner: exact inverse of the flux part, per k an upwind
+// block-bidiagonal system over the elements (line operator of
+// get_LineTransversePreconditioner_full2D.m:174-239 in 1D).  The upwind
+// coupling touches one node of the neighbour element, so the sweep carries
+// one complex scalar s_e: s_e = u_e[st] - h[st] s_{e-1}, u_e = D0^-1 r_e / qd.
+// Elements are split into P chunks (one warp each, lanes = k); the affine maps
+// of the chunks are scanned in shared memory, then every chunk re-sweeps.
+// ---------------------------------------------------------------------------
+template <int NK>
+__global__ void precond_kernel(const double2* __restrict__ r, double2* __restrict__ z,
+                               const double* __restrict__ kvec, const double* __restrict__ dinv,
+                               const double* __restrict__ hvec, const double* __restrict__ qd, int n_el, int nk,
+                               long long N, long long r_stride) {
+  extern __shared__ double2 sh[];                 // [2][P][32]
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int P = blockDim.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  const int b = blockIdx.y;
+  const bool valid = j < nk;
+  const int chunk = (n_el + P - 1) / P;
+  const int e_lo = min(n_el, w * chunk), e_hi = min(n_el, (w + 1) * chunk);
+  double D[NK * NK], h[NK];
+  bool fwd = true;
+  double inv_qd = 1.0;
+  if (valid) {
+#pragma unroll
+    for (int i = 0; i < NK * NK; ++i) D[i] = dinv[j * NK * NK + i];
+#pragma unroll
+    for (int i = 0; i < NK; ++i) h[i] = hvec[j * NK + i];
+    fwd = kvec[j] > 0;
+    inv_qd = 1.0 / qd[b];
+  }
+  const int st = fwd ? NK - 1 : 0;
+  const double alpha = valid ? -h[st] : 0.0;
+  const double2* rb = r + (long long)b * r_stride + j;
+  double2* zb = z + (long long)b * N + j;
+  const int len = e_hi - e_lo;
+  // phase 1: chunk map with zero input
+  double2 s = make_double2(0.0, 0.0);
+  double Amul = 1.0;
+  if (valid) {
+    for (int i = 0; i < len; ++i) {
+      const int e = fwd ? e_lo + i : e_hi - 1 - i;
+      const double2* re = rb + (long long)e * NK * nk;
+      double2 u = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        const double2 rv = re[(long long)c * nk];
+        u.x += D[st * NK + c] * rv.x;
+        u.y += D[st * NK + c] * rv.y;
+      }
+      s = make_double2(u.x * inv_qd + alpha * s.x, u.y * inv_qd + alpha * s.y);
+      Amul *= alpha;
+    }
+  }
+  sh[(0 * P + w) * 32 + lane] = make_double2(Amul, 0.0);
+  sh[(1 * P + w) * 32 + lane] = s;
+  __syncthreads();
+  if (w == 0 && valid) {
+    // exclusive scan over chunks in sweep order; overwrite B slot with s_in
+    double2 acc = make_double2(0.0, 0.0);
+    for (int c = 0; c < P; ++c) {
+      const int cc = fwd ? c : P - 1 - c;
+      const double a = sh[(0 * P + cc) * 32 + lane].x;
+      const double2 bb = sh[(1 * P + cc) * 32 + lane];
+      sh[(1 * P + cc) * 32 + lane] = acc;
+      acc = make_double2(a * acc.x + bb.x, a * acc.y + bb.y);
+    }
+  }
+  __syncthreads();
+  if (!valid) return;
+  s = sh[(1 * P + w) * 32 + lane];
+  for (int i = 0; i < len; ++i) {
+    const int e = fwd ? e_lo + i : e_hi - 1 - i;
+    const double2* re = rb + (long long)e * NK * nk;
+    double2 rv[NK];
+#pragma unroll
+    for (int c = 0; c < NK; ++c) rv[c] = re[(long long)c * nk];
+    double2* ze = zb + (long long)e * NK * nk;
+    double2 snew = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      double2 u = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        u.x += D[a * NK + c] * rv[c].x;
+        u.y += D[a * NK + c] * rv[c].y;
+      }
+      const double2 zv = make_double2(u.x * inv_qd - h[a] * s.x, u.y * inv_qd - h[a] * s.y);
+      ze[(long long)a * nk] = zv;
+      if (a == st) snew = zv;
+    }
+    s = snew;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Vw(x,k) rebuild: beta[b][e][ac][s] = (dxi/4) mpc sum_q kap[ac][q]
+//     * (V(x_q + xi_s/2) - V(x_q - xi_s/2))
+// with V the lookup of V_transient.m (linear inside [0,Lx), min(V) beyond Lx,
+// V(1) below 0).  One thread per (e, s).
+// ---------------------------------------------------------------------------
+__device__ double v_lookup(double x, const double* __restrict__ xg, const double* __restrict__ vg, int nx,
+                           double lx, double vmin) {
+  if (x < 0) return vg[0];
+  if (x >= lx) return vmin;
+  int lo = 0, hi = nx - 1;
+  if (x >= xg[hi]) return vg[hi];
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (xg[mid] <= x) lo = mid; else hi = mid;
+  }
+  const double slope = (vg[lo + 1] - vg[lo]) / (xg[lo + 1] - xg[lo]);
+  return slope * (x - xg[lo]) + vg[lo];
+}
+
+template <int NK>
+__global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ xq, const double* __restrict__ xi_edge,
+                          const double* __restrict__ kap, const double* __restrict__ xg, const double* __restrict__ vg,
+                          int nx, double lx, double vmin, int n_el, int nxi, double scale) {
+  const int ne = nxi + 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long long)n_el * ne) return;
+  const int s = (int)(t % ne);
+  const int e = (int)(t / ne);
+  const double xi = xi_edge[s];
+  double dv[kNqx];
+#pragma unroll
+  for (int q = 0; q < kNqx; ++q) {
+    const double x = xq[e * kNqx + q];
+    dv[q] = v_lookup(x + 0.5 * xi, xg, vg, nx, lx, vmin) - v_lookup(x - 0.5 * xi, xg, vg, nx, lx, vmin);
+  }
+  double* be = beta + (long long)e * NK * NK * ne;
+#pragma unroll
+  for (int ac = 0; ac < NK * NK; ++ac) {
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < kNqx; ++q) acc += kap[ac * kNqx + q] * dv[q];
+    be[(long long)ac * ne + s] = acc * scale;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Observables: rho_u(s) = sum_j Phi(s,j) rho_{x,j} at the centre xi rows,
+// n = Re rho_u(centre), j = q hbar / m Im d rho_u / d xi
+// (solve_transport_DG_2D.m:114-156).  One warp per DG node.
+// ---------------------------------------------------------------------------
+__global__ void observables_kernel(const double2* __restrict__ rho, const double2* __restrict__ phi,
+                                   const double* __restrict__ m_nodes, double* __restrict__ n_out,
+                                   double* __restrict__ j_out, int nk, int nxi, int ncol, double delta_xi,
+                                   double pref) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= ncol) return;
+  const bool odd = nxi & 1;
+  const int c1 = odd ? (nxi - 1) / 2 - 1 : nxi / 2 - 1;
+  const int c2 = odd ? (nxi - 1) / 2 + 1 : nxi / 2;
+  const int cm = (nxi - 1) / 2;
+  double2 u1 = make_double2(0, 0), u2 = make_double2(0, 0), um = make_double2(0, 0);
+  const double2* rx = rho + (long long)warp * nk;
+  for (int j = lane; j < nk; j += 32) {
+    const double2 rv = rx[j];
+    u1 = cadd(u1, cmul(phi[(long long)c1 * nk + j], rv));
+    u2 = cadd(u2, cmul(phi[(long long)c2 * nk + j], rv));
+    if (odd) um = cadd(um, cmul(phi[(long long)cm * nk + j], rv));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    u1.x += __shfl_xor_sync(0xffffffffu, u1.x, o);
+    u1.y += __shfl_xor_sync(0xffffffffu, u1.y, o);
+    u2.x += __shfl_xor_sync(0xffffffffu, u2.x, o);
+    u2.y += __shfl_xor_sync(0xffffffffu, u2.y, o);
+    um.x += __shfl_xor_sync(0xffffffffu, um.x, o);
+    um.y += __shfl_xor_sync(0xffffffffu, um.y, o);
+  }
+  if (lane == 0) {
+    const double m = m_nodes[warp];
+    if (odd) {
+      n_out[warp] = um.x;
+      j_out[warp] = pref / m * (u2.y - u1.y) / 2 / delta_xi;
+    } else {
+      n_out[warp] = (u1.x + u2.x) / 2;
+      j_out[warp] = pref / m * (u2.y - u1.y) / delta_xi;
+    }
+  }
+}
+
+template <int NK>
+cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
+  const long long total = (long long)P.batch * P.s.n_el * P.s.nk;
+  flux_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el,
+                                                                          P.s.nk, total);
+  dim3 g1((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nxi + GBM - 1) / GBM);
+  zgemm_kernel<0><<<g1, 256, 0, P.stream>>>(P.phi, P.s.nk, x, P.xh, P.s.nxi, P.s.nk, P.ncols);
+  const long long nelem = (long long)P.batch * P.s.n_el;
+  const long long st = nelem * P.s.nxi;
+  stencil_kernel<NK><<<(unsigned)((st + 255) / 256), 256, 0, P.stream>>>(P.xh, P.yh, P.beta, P.betai, P.s.nxi,
+                                                                          nelem);
+  dim3 g2((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nk + GBM - 1) / GBM);
+  zgemm_kernel<1><<<g2, 256, 0, P.stream>>>(P.phi, P.s.nk, P.yh, y, P.s.nk, P.s.nxi, P.ncols);
+  return cudaGetLastError();
+}
+
+template <int NK>
+cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2* z) {
+  const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
+  dim3 grid((P.s.nk + 31) / 32, P.batch);
+  const size_t shm = sizeof(double2) * 2 * Pw * 32;
+  precond_kernel<NK><<<grid, 32 * Pw, shm, P.stream>>>(r, z, P.kvec, P.pre_dinv, P.pre_h, P.qd, P.s.n_el, P.s.nk,
+                                                        P.N, r_stride);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
+  switch (P.s.nK) {
+    case 2: return apply_nk<2>(P, x, y);
+    case 3: return apply_nk<3>(P, x, y);
+    default: return apply_nk<4>(P, x, y);
+  }
+}
+
+cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z) {
+  switch (P.s.nK) {
+    case 2: return precond_nk<2>(P, r, r_stride, z);
+    case 3: return precond_nk<3>(P, r, r_stride, z);
+    default: return precond_nk<4>(P, r, r_stride, z);
+  }
+}
+
+cudaError_t launch_vw_rebuild(Problem& P, int b) {
+  const HostProblem& hpb = P.hp[b];
+  const int ne = P.s.nxi + 1;
+  const long long total = (long long)P.s.n_el * ne;
+  double* beta = P.beta + (long long)b * P.s.n_el * P.s.nK * P.s.nK * ne;
+  const double* xq = P.xq + (long long)b * P.s.n_el * kNqx;
+  const double* xg = P.pot_x + (long long)b * P.nx;
+  const double* vg = P.pot_v + (long long)b * P.nx;
+  // min(V) for x >= Lx (V_transient.m:6) is computed on the host and passed by value
+  double vmin = hpb.vmin;
+  const double scale = P.s.delta_xi / 4 * P.s.mpc;
+  const unsigned grid = (unsigned)((total + 127) / 128);
+  switch (P.s.nK) {
+    case 2: vw_kernel<2><<<grid, 128, 0, P.stream>>>(beta, xq, P.xi_edge, P.kap, xg, vg, P.nx, hpb.l_chi, vmin,
+                                                     P.s.n_el, P.s.nxi, scale); break;
+    case 3: vw_kernel<3><<<grid, 128, 0, P.stream>>>(beta, xq, P.xi_edge, P.kap, xg, vg, P.nx, hpb.l_chi, vmin,
+                                                     P.s.n_el, P.s.nxi, scale); break;
+    default: vw_kernel<4><<<grid, 128, 0, P.stream>>>(beta, xq, P.xi_edge, P.kap, xg, vg, P.nx, hpb.l_chi, vmin,
+                                                      P.s.n_el, P.s.nxi, scale); break;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rho_xi(Problem& P, int b, double2* out) {
+  const long long ncol = (long long)P.s.n_el * P.s.nK;
+  dim3 g1((unsigned)((ncol + GBN - 1) / GBN), (P.s.nxi + GBM - 1) / GBM);
+  zgemm_kernel<0><<<g1, 256, 0, P.stream>>>(P.phi, P.s.nk, P.x + (long long)b * P.N, out, P.s.nxi, P.s.nk, ncol);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j) {
+  const int ncol = P.s.n_el * P.s.nK;
+  const double pref = kQ * (kHV / 2 / M_PI);
+  const double2* rho = P.x + (long long)b * P.N;
+  const unsigned grid = (unsigned)((ncol * 32 + 255) / 256);
+  observables_kernel<<<grid, 256, 0, P.stream>>>(rho, P.phi, P.m_nodes + (long long)b * ncol, n_dg, j, P.s.nk,
+                                                 P.s.nxi, ncol, P.s.delta_xi, pref);
+  return cudaGetLastError();
+}
+
+}  // namespace wg

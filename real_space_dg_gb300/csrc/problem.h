@@ -1,0 +1,116 @@
+// Device-side state of a wg_problem handle (internal header).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "setup.h"
+#include "wigner_gb300.h"
+
+namespace wg {
+
+// Small constant blocks passed by value to kernels (fits the parameter space).
+struct FluxBlocks {
+  int nK;
+  double K1[kMaxLocal * kMaxLocal];
+  double K2[kMaxLocal * kMaxLocal];
+  double K3[kMaxLocal * kMaxLocal];
+  double K5[kMaxLocal * kMaxLocal];
+};
+
+// Per-problem host copy of the set-up that stays fixed until the next set_potential.
+struct HostProblem {
+  bool ready = false;
+  double l_chi = 0;                 // device length [m]
+  double qd = 0;                    // Q_diff * mpc / detJ
+  double vmin = 0;                  // min(Esub): V(x >= Lx) of V_transient.m:6
+  std::vector<double> m_nodes;      // mass at the DG nodes [kg]
+  std::vector<cplx> fnl, fnr;
+};
+
+// Device buffers of the mixed-precision inner solver (allocated only for WG_PREC_MIXED).
+struct MixedBuffers {
+  void* phi16 = nullptr;     // bf16 operand planes of Phi / Phi^H (layout owned by mixed.cu)
+  void* xin16 = nullptr;     // bf16 staging of the GEMM B operands
+  float* V = nullptr;        // fp32 Krylov basis [B][m+1][2N]
+  float* w = nullptr;        // fp32 work vectors
+  float* z = nullptr;
+  float* xh = nullptr;
+  float* yh = nullptr;
+  float* beta = nullptr;     // fp32 copy of the potential weights
+};
+
+struct Problem {
+  // shape
+  Shape s;
+  int batch = 0;
+  int precision = WG_PREC_FP64;
+  int restart = 50;
+  long long N = 0;          // complex entries per problem
+  long long ncols = 0;      // DG nodes in the batch = batch * n_el * nK
+  double device_bytes = 0;
+  double mem_budget = 0;
+  FluxBlocks fb{};
+  std::string err;
+
+  std::vector<HostProblem> hp;
+
+  cudaStream_t stream = nullptr;
+  // constant device data
+  double2* phi = nullptr;        // nxi x nk row-major
+  double* kvec = nullptr;        // nk
+  double* xi_edge = nullptr;     // nxi + 1
+  double* kap = nullptr;         // nK*nK*10
+  double* betai = nullptr;       // [nK*nK][nxi+1] CAP part of the potential weights (imaginary)
+  double* pre_dinv = nullptr;    // [nk][nK*nK] inverse of k K1 + |k| K2
+  double* pre_h = nullptr;       // [nk][nK] D0^-1 * coupling column
+  // per-problem device data
+  double* qd = nullptr;          // [B]
+  double* beta = nullptr;        // [B][n_el][nK*nK][nxi+1] real potential weights
+  double* xq = nullptr;          // [B][n_el*10] quadrature x [m]
+  double* pot_x = nullptr;       // [B][nx] material grid [m]
+  double* pot_v = nullptr;       // [B][nx] potential [eV]
+  double* m_nodes = nullptr;     // [B][n_el*nK] masses at DG nodes [kg]
+  int nx = 0;
+  // vectors
+  double2* rhs = nullptr;        // [B*N]
+  double2* x = nullptr;          // [B*N] solution (resident across solves)
+  double2* w = nullptr;          // [B*N] work
+  double2* z = nullptr;          // [B*N] work
+  double2* r = nullptr;          // [B*N] work
+  double2* V = nullptr;          // [B][m+1][N] Krylov basis
+  double2* xh = nullptr;         // [nxi][ncols] transformed state
+  double2* yh = nullptr;         // [nxi][ncols]
+  // GMRES small data
+  double2* H = nullptr;          // [B][m+1][m] column-major per problem: H[b][col*(m+1)+row]
+  double2* cs = nullptr;         // [B][m]
+  double2* sn = nullptr;         // [B][m]
+  double2* g = nullptr;          // [B][m+1]
+  double2* hcol = nullptr;       // [B][m+1] current column partial results
+  double2* ycoef = nullptr;      // [B][m]
+  double2* partial = nullptr;    // [B][m+1][nchunk]
+  double* nrm_partial = nullptr; // [B][nchunk]
+  double* nrm = nullptr;         // [B]
+  double* target = nullptr;      // [B] absolute residual targets
+  int* active = nullptr;         // [B] 1 while iterating in this cycle
+  int* kused = nullptr;          // [B] iterations used in this cycle
+  int* any_active = nullptr;     // [1]
+  int nchunk = 0;
+  // host mirrors
+  std::vector<double> h_nrm;
+  std::vector<int> h_active, h_kused;
+
+  MixedBuffers mx;
+};
+
+// Kernel launchers (operator.cu)
+cudaError_t launch_apply(Problem& P, const double2* x, double2* y);
+cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z);
+cudaError_t launch_vw_rebuild(Problem& P, int b);
+cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j);
+cudaError_t launch_rho_xi(Problem& P, int b, double2* out);
+// Krylov (gmres.cu)
+int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
+
+}  // namespace wg
