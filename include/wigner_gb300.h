@@ -141,6 +141,17 @@ int wg_precondition(wg_problem* h, const double* r, double* z);
 /* The batch's right-hand sides (batch*N complex). */
 int wg_get_rhs(wg_problem* h, double* rhs);
 
+/* Kernel-class profiler (the reference's tic/toc solveInfo timings,
+ * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).
+ * Classes: flux, forward GEMM, xi stencil, backward GEMM, k-line
+ * preconditioner, Krylov (Gram-Schmidt + Givens per iteration), other. */
+enum { WG_PROF_FLUX = 0, WG_PROF_GEMM_FWD, WG_PROF_STENCIL, WG_PROF_GEMM_BWD, WG_PROF_PRECOND, WG_PROF_KRYLOV,
+       WG_PROF_OTHER, WG_PROF_N };
+int wg_profile_enable(wg_problem* h, int on);
+/* ms[i]: summed event time of class i; timed[i]: timed launches; launches[i]:
+ * kernel launches of class i since the last reset (always counted). */
+int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, int reset);
+
 #ifdef __cplusplus
 }
 #endif

@@ -104,7 +104,8 @@ def fermi_kz_integral(E_k, Ef, me_z, temp, vmax):
     dkz = kz[1] - kz[0]
     ekz = HB_V ** 2 * kz ** 2 / 2 / M0_V / me_z / Q_V
     arg = Q_V * (E_k[:, None] + ekz[None, :] - Ef) / (KB_V * temp)
-    return 2 / np.pi * dkz * np.sum(1.0 / (1.0 + np.exp(arg)), axis=1)
+    with np.errstate(over="ignore"):
+        return 2 / np.pi * dkz * np.sum(1.0 / (1.0 + np.exp(arg)), axis=1)
 
 
 def verteilung_msa2d(mat, p, V, m, EfL, EfR):

@@ -61,7 +61,10 @@ SIGNATURES = {
     "wg_apply": ([_H, _D, _D], C.c_int),
     "wg_precondition": ([_H, _D, _D], C.c_int),
     "wg_get_rhs": ([_H, _D], C.c_int),
+    "wg_profile_enable": ([_H, C.c_int], C.c_int),
+    "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.c_int], C.c_int),
 }
+PROF_CLASSES = ["flux", "gemm_fwd", "stencil", "gemm_bwd", "precond", "krylov", "other"]
 
 _lib = None
 

@@ -38,6 +38,7 @@ cudaError_t dalloc(T** p, size_t count, double& bytes) {
 }
 
 void free_all(wg::Problem& P) {
+  wg::prof_release(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
                   P.ycoef, P.partial, P.nrm_partial, P.nrm, P.target, P.active, P.kused, P.any_active,
@@ -381,6 +382,30 @@ int wg_precondition(wg_problem* h, const double* r, double* z) {
   API_CK(&P, wg::launch_precondition(P, P.r, P.N, P.z));
   API_CK(&P, cudaMemcpyAsync(z, P.z, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_profile_enable(wg_problem* h, int on) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  h->P.prof.on = on != 0;
+  return WG_OK;
+}
+
+int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, int reset) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  API_CK(&P, wg::prof_collect(P));
+  for (int i = 0; i < wg::PROF_N; ++i) {
+    if (ms) ms[i] = P.prof.ms[i];
+    if (timed) timed[i] = P.prof.timed[i];
+    if (launches) launches[i] = P.prof.launches[i];
+  }
+  if (reset)
+    for (int i = 0; i < wg::PROF_N; ++i) {
+      P.prof.ms[i] = 0;
+      P.prof.timed[i] = 0;
+      P.prof.launches[i] = 0;
+    }
   return WG_OK;
 }
 

@@ -317,6 +317,7 @@ inline unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
 // r = rhs - A x ; nrm[b] = |r_b|
 int true_residual(Problem& P) {
   const long long tot = P.N * P.batch;
+  P.prof.launches[PROF_OTHER] += 3;
   WG_CK(launch_apply(P, P.x, P.w));
   residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot);
   norm_partial_kernel<<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk);
@@ -334,6 +335,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
   const int maxit = o.maxit > 0 ? o.maxit : 50;
   if (!warm) WG_CK(cudaMemsetAsync(P.x, 0, sizeof(double2) * tot, P.stream));
   // |b|
+  P.prof.launches[PROF_OTHER] += 2;
   norm_partial_kernel<<<dim3(P.nchunk, B), 256, 0, P.stream>>>(P.rhs, P.nrm_partial, N, P.nchunk);
   norm_reduce_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, nullptr, P.active, P.nchunk, 0, 0, 0);
   std::vector<double> bnorm(B), initial(B);
@@ -353,6 +355,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
     bool any = false;
     for (int b = 0; b < B; ++b) any |= (res[b] > tgt[b]) && std::isfinite(res[b]);
     if (!any) break;
+    P.prof.launches[PROF_OTHER] += 2;
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, mp1, B);
     // V_0 = r / |r|
     scale_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.r, P.V, P.nrm, P.active, N, (long long)mp1 * N, B);
@@ -361,6 +364,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
       WG_CK(launch_precondition(P, P.V + (long long)k * N, (long long)mp1 * N, P.z));
       WG_CK(launch_apply(P, P.z, P.w));
       const int nv = k + 1;
+      cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 10);
       for (int pass = 0; pass < 2; ++pass) {
         dot_partial_kernel<<<dim3(P.nchunk, nv, B), 256, 0, P.stream>>>(P.V, P.w, P.partial, P.active, N, mp1,
                                                                        P.nchunk);
@@ -374,6 +378,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
                                                             (long long)mp1 * N, k, mp1, m, B);
       givens_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.cs, P.sn, P.g, P.active, P.kused, P.target, k, mp1,
                                                           m, B);
+      prof_end(P, PROF_KRYLOV, ev);
       WG_CK(cudaGetLastError());
       // early exit of the cycle once every problem has met its target
       if ((k & 3) == 3 || k == m - 1) {
@@ -384,6 +389,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
         if (!still) break;
       }
     }
+    P.prof.launches[PROF_OTHER] += 4;
     backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, P.kused, mp1, m, B);
     combine_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.V, P.ycoef, P.kused, P.w, N, mp1, m, B);
     WG_CK(launch_precondition(P, P.w, N, P.z));

@@ -416,16 +416,24 @@ __global__ void observables_kernel(const double2* __restrict__ rho, const double
 template <int NK>
 cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
   const long long total = (long long)P.batch * P.s.n_el * P.s.nk;
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX);
   flux_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el,
                                                                           P.s.nk, total);
+  prof_end(P, PROF_FLUX, ev);
   dim3 g1((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nxi + GBM - 1) / GBM);
+  ev = prof_begin(P, PROF_GEMM_FWD);
   zgemm_kernel<0><<<g1, 256, 0, P.stream>>>(P.phi, P.s.nk, x, P.xh, P.s.nxi, P.s.nk, P.ncols);
+  prof_end(P, PROF_GEMM_FWD, ev);
   const long long nelem = (long long)P.batch * P.s.n_el;
   const long long st = nelem * P.s.nxi;
+  ev = prof_begin(P, PROF_STENCIL);
   stencil_kernel<NK><<<(unsigned)((st + 255) / 256), 256, 0, P.stream>>>(P.xh, P.yh, P.beta, P.betai, P.s.nxi,
                                                                           nelem);
+  prof_end(P, PROF_STENCIL, ev);
   dim3 g2((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nk + GBM - 1) / GBM);
+  ev = prof_begin(P, PROF_GEMM_BWD);
   zgemm_kernel<1><<<g2, 256, 0, P.stream>>>(P.phi, P.s.nk, P.yh, y, P.s.nk, P.s.nxi, P.ncols);
+  prof_end(P, PROF_GEMM_BWD, ev);
   return cudaGetLastError();
 }
 
@@ -434,12 +442,64 @@ cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2
   const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
   dim3 grid((P.s.nk + 31) / 32, P.batch);
   const size_t shm = sizeof(double2) * 2 * Pw * 32;
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND);
   precond_kernel<NK><<<grid, 32 * Pw, shm, P.stream>>>(r, z, P.kvec, P.pre_dinv, P.pre_h, P.qd, P.s.n_el, P.s.nk,
                                                         P.N, r_stride);
+  prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
 
 }  // namespace
+
+cudaEvent_t prof_begin(Problem& P, int cls, int n) {
+  P.prof.launches[cls] += n;
+  if (!P.prof.on) return nullptr;
+  cudaEvent_t a;
+  if (P.prof.pool.empty()) {
+    if (cudaEventCreate(&a) != cudaSuccess) return nullptr;
+  } else {
+    a = P.prof.pool.back();
+    P.prof.pool.pop_back();
+  }
+  cudaEventRecord(a, P.stream);
+  return a;
+}
+
+void prof_end(Problem& P, int cls, cudaEvent_t a) {
+  if (!a) return;
+  cudaEvent_t b;
+  if (P.prof.pool.empty()) {
+    if (cudaEventCreate(&b) != cudaSuccess) { P.prof.pool.push_back(a); return; }
+  } else {
+    b = P.prof.pool.back();
+    P.prof.pool.pop_back();
+  }
+  cudaEventRecord(b, P.stream);
+  P.prof.pending.push_back({cls, a, b});
+  if (P.prof.pending.size() > 8192) prof_collect(P);
+}
+
+cudaError_t prof_collect(Problem& P) {
+  if (P.prof.pending.empty()) return cudaSuccess;
+  cudaError_t e = cudaStreamSynchronize(P.stream);
+  for (auto& r : P.prof.pending) {
+    float ms = 0;
+    if (e == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      P.prof.ms[r.cls] += ms;
+      P.prof.timed[r.cls] += 1;
+    }
+    P.prof.pool.push_back(r.a);
+    P.prof.pool.push_back(r.b);
+  }
+  P.prof.pending.clear();
+  return e;
+}
+
+void prof_release(Problem& P) {
+  prof_collect(P);
+  for (cudaEvent_t e : P.prof.pool) cudaEventDestroy(e);
+  P.prof.pool.clear();
+}
 
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
   switch (P.s.nK) {

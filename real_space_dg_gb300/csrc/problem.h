@@ -41,6 +41,25 @@ struct MixedBuffers {
   float* beta = nullptr;     // fp32 copy of the potential weights
 };
 
+// Kernel classes timed and counted by the profiler.
+enum ProfClass { PROF_FLUX = 0, PROF_GEMM_FWD, PROF_STENCIL, PROF_GEMM_BWD, PROF_PRECOND, PROF_KRYLOV, PROF_OTHER,
+                 PROF_N };
+
+// CUDA-event timing of kernel classes on the handle's stream (off by default;
+// launch counts are kept always).
+struct Profiler {
+  bool on = false;
+  struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+  };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Rec> pending;
+  double ms[PROF_N] = {};
+  long long timed[PROF_N] = {};
+  long long launches[PROF_N] = {};
+};
+
 struct Problem {
   // shape
   Shape s;
@@ -102,7 +121,15 @@ struct Problem {
   std::vector<int> h_active, h_kused;
 
   MixedBuffers mx;
+  Profiler prof;
 };
+
+// Profiler helpers (operator.cu).  prof_begin counts `n` launches of class cls
+// and, when timing is on, records a start event; prof_end records the stop event.
+cudaEvent_t prof_begin(Problem& P, int cls, int n = 1);
+void prof_end(Problem& P, int cls, cudaEvent_t a);
+cudaError_t prof_collect(Problem& P);
+void prof_release(Problem& P);
 
 // Kernel launchers (operator.cu)
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y);

@@ -126,6 +126,16 @@ class Problem1D:
                                              z.view(np.float64).ctypes.data_as(_lib._D)))
         return z
 
+    def profile(self, on=None, reset=False):
+        """Enable/disable kernel timing (on=True/False) and/or read the counters:
+        {class: (ms, timed launches, launches)}."""
+        if on is not None:
+            self._check(self.lib.wg_profile_enable(self.h, 1 if on else 0))
+        n = len(_lib.PROF_CLASSES)
+        ms = np.zeros(n); timed = (C.c_longlong * n)(); launches = (C.c_longlong * n)()
+        self._check(self.lib.wg_profile_read(self.h, _lib.dptr(ms), timed, launches, 1 if reset else 0))
+        return {c: (ms[i], timed[i], launches[i]) for i, c in enumerate(_lib.PROF_CLASSES)}
+
     def rhs(self):
         out = np.empty(self.N * self.batch, dtype=np.complex128)
         self._check(self.lib.wg_get_rhs(self.h, out.view(np.float64).ctypes.data_as(_lib._D)))

@@ -1,0 +1,80 @@
+"""CPU checks of the C ABI: the library loads, exports every declared symbol,
+and its struct layouts agree with the header (no GPU call is made)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "wigner_gb300.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(wg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for required in ("wg_problem_create", "wg_set_potential", "wg_solve", "wg_get_observables",
+                     "wg_problem_destroy", "wg_last_error", "wg_apply", "wg_precondition"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(built_lib)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_every_symbol(built_lib):
+    from real_space_dg_gb300 import _lib
+    assert set(declared_functions()) <= set(_lib.SIGNATURES)
+    _lib.load()
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """Compile a C probe against the header and compare sizeof/offsetof with ctypes."""
+    from real_space_dg_gb300 import _lib
+    src = tmp_path / "probe.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "wigner_gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu\n", sizeof(wg_params), sizeof(wg_device), sizeof(wg_solve_opts), sizeof(wg_solve_info));
+  printf("%zu %zu %zu\n", offsetof(wg_params, l_xi), offsetof(wg_params, precision), offsetof(wg_params, mem_budget_bytes));
+  printf("%zu %zu\n", offsetof(wg_solve_info, relres), offsetof(wg_solve_info, rhs_norm));
+  return 0;
+}''')
+    exe = tmp_path / "probe"
+    r = subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode:
+        pytest.skip("no C compiler: " + r.stderr)
+    out = subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()
+    got = list(map(int, out))
+    want = [C.sizeof(_lib.WgParams), C.sizeof(_lib.WgDevice), C.sizeof(_lib.WgSolveOpts),
+            C.sizeof(_lib.WgSolveInfo), _lib.WgParams.l_xi.offset, _lib.WgParams.precision.offset,
+            _lib.WgParams.mem_budget_bytes.offset, _lib.WgSolveInfo.relres.offset, _lib.WgSolveInfo.rhs_norm.offset]
+    assert got == want
+
+
+def test_errors_without_handle_are_statuses(built_lib):
+    """Argument errors return a status and a message; the library never aborts."""
+    from real_space_dg_gb300 import _lib
+    lib = _lib.load()
+    assert lib.wg_problem_create(None, 1, None) == _lib.WG_ERR_ARG
+    assert b"null" in lib.wg_global_error()
+    prm = _lib.WgParams(1, 3, 16, 16, 30e-9, 0.0, 1.0, 0, 0, 0.0)    # n_el = 1 is invalid
+    h = C.c_void_p()
+    assert lib.wg_problem_create(C.byref(prm), 1, C.byref(h)) == _lib.WG_ERR_ARG
+    assert b"n_el" in lib.wg_global_error()
+    prm = _lib.WgParams(8, 3, 16, 12, 30e-9, 0.0, 1.0, 0, 0, 0.0)    # n_xi < nk
+    assert lib.wg_problem_create(C.byref(prm), 1, C.byref(h)) == _lib.WG_ERR_ARG
+    prm = _lib.WgParams(8, 3, 16, 16, 30e-9, 0.0, 1.0, 0, 0, 1.0)    # 1-byte budget -> OOM status
+    assert lib.wg_problem_create(C.byref(prm), 1, C.byref(h)) == _lib.WG_ERR_OOM
+    assert b"budget" in lib.wg_global_error()
