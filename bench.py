@@ -1,0 +1,329 @@
+#!/usr/bin/env python
+"""Benchmark: converged self-consistent RTD bias points per second on one GB300.
+
+Workload (the configuration the headline metric is quoted on): a self-consistent
+RTD, GaAs, 80 nm device with 20 nm contacts at 1e18 cm^-3, Al0.3Ga0.7As double
+barrier 0.27 eV x 3 nm around a 5 nm well; DG p=3, 240 elements, Nk=256 (245,760
+complex unknowns per bias point); Gummel mixing 0.3, potential tolerance 1e-6 V;
+every transport solve to a 1e-8 relative residual.  One step = one batch of
+`--batch` bias points (0.2 V * (1..B)/B) solved from a cold start to the Gummel
+fixed point, all points advancing together in one handle.
+
+Arms: default (ours, this library on the GPU) and ``--impl reference`` (the CPU
+restatement of the reference algorithm, timed on a bounded sample).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged self-consistent bias points/s at 1e-8 transport residual (C2 RTD, batched)"
+UNIT = "bias_points/s"
+
+SPEC = dict(length_nm=80.0, contact_nm=20.0, barrier_ev=0.27, barrier_nm=3.0, well_nm=5.0, doping_m3=1e24,
+            m_rel=0.067, temp_k=300.0, order=3, n_el=240, nk=256, l_xi_m=30e-9)
+GUMMEL = dict(mixing=0.3, potentialTolerance=1e-6, densityTolerance=5e-4, poissonResidualTolerance=8e-2,
+              maxIterations=200, transportTolerance=1e-8, transportMaxCycles=60)
+# Inner Krylov iterations per converged bias point of this workload, measured on
+# the FP64 GPU path (same algorithm as the CPU restatement); used to extrapolate
+# the CPU sample.  Overwritten by the live measurement when the GPU arm runs.
+ITERS_PER_POINT_FALLBACK = 3000.0
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = [r for r in self.rows if r[0] == "0"] or self.rows
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1])]
+        mx = [num(r[2]) for r in rows if num(r[2])]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip() == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(v, dist):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(v, dist):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def make_workload(batch):
+    from real_space_dg_gb300 import devices
+    spec = devices.RTDSpec(**SPEC)
+    mat = devices.make_mat(spec)
+    mat["dy_norm_nm"] = devices.density_normalisation_nm(mat)
+    biases = 0.2 * np.arange(1, batch + 1) / batch
+    return spec, mat, biases
+
+
+def algorithmic_cost(kind, spec, batch):
+    """Algorithmic bytes or flops of one launch of a kernel class."""
+    nK = spec.order + 1
+    N = spec.n_el * nK * spec.nk
+    ncol = batch * spec.n_el * nK
+    nxi = spec.n_xi or spec.nk
+    if kind in ("gemm_fwd", "gemm_bwd"):
+        return 8.0 * nxi * spec.nk * ncol, "TFLOP/s"
+    if kind == "flux":
+        return 2 * 16.0 * N * batch, "GB/s"
+    if kind == "stencil":
+        return 2 * 16.0 * nxi * ncol + 8.0 * batch * spec.n_el * nK * nK * (nxi + 1), "GB/s"
+    if kind == "precond":
+        return 2 * 16.0 * N * batch, "GB/s"
+    return None, None
+
+
+def run_ours(args, rank, world, dist):
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300 import _lib
+    from real_space_dg_gb300.rtd import RTDSweep, solve_rtd_self_consistent
+
+    spec, mat, biases = make_workload(args.batch)
+    opts = dict(GUMMEL, precision=args.precision, restart=args.restart)
+    S = RTDSweep(mat, args.batch, opts)
+    for b, v in enumerate(biases):
+        S.set(b, v)
+    for _ in range(args.warmup):
+        S.run(restart_from_phi0=True)
+    S.P.profile(on=True, reset=True)
+    clocks = ClockSampler()
+    clocks.start()
+    barrier(dist)
+    lat, pts, its, gummel_its, statuses = [], 0, 0, 0, []
+    total_ms = 0.0
+    for _ in range(args.steps):
+        S.P.event(0)
+        st, info = S.run(restart_from_phi0=True)
+        S.P.event(1)
+        total_ms += S.P.elapsed_ms(0, 1)
+        for i in info:
+            statuses.append(i["status"])
+            if i["status"] == 0:
+                pts += 1
+                lat.append(i["seconds"])
+            its += i["gmres_iterations"]
+            gummel_its += i["iterations"]
+    clk = clocks.stop()
+    prof = S.P.profile(on=False, reset=True)
+    t_max = max_over_ranks(total_ms / 1000.0, dist)
+    pts_all = sum_over_ranks(pts, dist)
+    value = pts_all / t_max if t_max > 0 else 0.0
+    # roofline of the dominant kernel class (largest share of timed kernel time)
+    timed = {k: v for k, v in prof.items() if v[1] > 0}
+    dom = max(timed, key=lambda k: timed[k][0]) if timed else None
+    hbm, bf16, src = read_peaks()
+    roof = None
+    if dom:
+        ms, n_t, _ = timed[dom]
+        cost, unit = algorithmic_cost(dom, spec, args.batch)
+        if cost is not None:
+            per_launch_s = ms / 1000.0 / n_t
+            if unit == "TFLOP/s":
+                achieved = cost / per_launch_s / 1e12
+                if args.precision == "fp64":
+                    peak, bound, psrc = 1.25, "fp64", "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)"
+                else:
+                    peak, bound, psrc = bf16, "tensor", "bf16_tflops of MEASURED_PEAKS.json (%s)" % src
+            else:
+                achieved = cost / per_launch_s / 1e9
+                peak, bound, psrc = hbm, "hbm", "hbm_gbs of MEASURED_PEAKS.json (%s)" % src
+            roof = {"kernel": dom, "bound": bound, "achieved": round(achieved, 3), "peak": peak, "unit": unit,
+                    "frac": round(achieved / peak, 4), "traffic": None, "peak_source": psrc,
+                    "avg_launch_us": round(1000.0 * ms / n_t, 2),
+                    "share": {k: round(v[0] / sum(x[0] for x in timed.values()), 4) for k, v in timed.items()}}
+    launches = sum(v[2] for v in prof.values())
+    # e2e: the public call with host inputs and outputs, every step
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        t0 = time.perf_counter()
+        r = solve_rtd_self_consistent(mat, biases, opts, mode="batched")
+        e2e_s = time.perf_counter() - t0
+        nx = int(mat["Nx"])
+        ncol = spec.n_el * (spec.order + 1)
+        e2e = {"value": round(sum(r["sweep"]["converged"]) / e2e_s, 5), "unit": UNIT,
+               "h2d_bytes_per_step": int(args.batch * 6 * nx * 8),
+               "d2h_bytes_per_step": int(args.batch * (nx + 2 * ncol) * 8),
+               "seconds": round(e2e_s, 3)}
+    S.close()
+    lat_sorted = sorted(lat)
+    p50 = float(np.percentile(lat_sorted, 50)) if lat else None
+    p99 = float(np.percentile(lat_sorted, 99)) if lat else None
+    iters_per_point = its / max(1, len(statuses))
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args, iters_per_point)
+    out = {
+        "metric": METRIC, "value": round(value, 6), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000.0 * t_max / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "bf16/f32 in f64 refinement",
+        "data": "synthetic RTD device of the named shape (seeded, deterministic)",
+        "config": {"workload": "C2 self-consistent RTD 80 nm, p=3, N_el=240, Nk=256, 245760 unknowns/point",
+                   "batch_bias_points": args.batch, "biases_v": [round(float(b), 4) for b in biases],
+                   "precision": args.precision, "gmres_restart": args.restart, "gummel_mixing": 0.3,
+                   "potential_tol_v": 1e-6, "transport_rtol": 1e-8,
+                   "l2": "inputs larger than L2 (Krylov basis %.2f GB)" %
+                         (16.0 * (args.restart + 1) * args.batch * spec.n_el * (spec.order + 1) * spec.nk / 1e9)},
+        "latency_s": {"p50": p50, "p99": p99, "definition": "time from step start to each point's Gummel exit"},
+        "converged_points": int(pts_all), "points_attempted": len(statuses) * world,
+        "gmres_iterations_per_point": round(iters_per_point, 1),
+        "gummel_iterations_per_point": round(gummel_its / max(1, len(statuses)), 2),
+        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+    }
+    return out
+
+
+def cpu_baseline(args, iters_per_point):
+    """Oracle (CPU restatement) GMRES iterations on the same C2 operator, timed on a
+    bounded sample and extrapolated with the measured iterations per bias point."""
+    from oracle import dg1d, krylov
+    from real_space_dg_gb300 import devices
+    spec, mat, biases = make_workload(1)
+    bias = 0.2
+    V = devices.flatband_potential(mat, bias)
+    efl, efr = devices.contact_fermi_levels(mat, bias)
+    m = np.full(mat["Nx"], spec.m_rel * dg1d.M0_V)
+    p = dg1d.init_params(mat, efl, efr, V, m)
+    op = krylov.Operator1D(mat, p, V)
+    pre = krylov.KLinePreconditioner(op, use_drift_diag=False)
+    _, rhs = dg1d.get_diff(p)
+    n_it = args.cpu_iters
+    t0 = time.perf_counter()
+    krylov.gmres_right(op.apply, pre.apply, rhs, restart=n_it, tol=1e-30, maxit=1)
+    dt = time.perf_counter() - t0
+    t_iter = dt / n_it
+    value = 1.0 / (t_iter * iters_per_point)
+    return {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d oracle GMRES(right, k-line) iterations on the C2 operator in %.2f s (%.3f s/iteration, "
+                      "NumPy/BLAS on all host cores), extrapolated with %.0f iterations per converged bias point"
+                      % (n_it, dt, t_iter, iters_per_point)}
+
+
+def run_reference(args, rank, world, dist):
+    if rank != 0:
+        return None
+    # warm-up: import and operator set-up are outside the timed samples
+    vals = []
+    for i in range(args.warmup + args.steps):
+        cpu = cpu_baseline(args, args.iters_per_point)
+        if i >= args.warmup:
+            vals.append(cpu["value"])
+    value = float(np.median(vals))
+    cpu["value"] = value
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic RTD device of the named shape",
+            "config": {"workload": "C2 self-consistent RTD 80 nm, p=3, N_el=240, Nk=256, 245760 unknowns/point",
+                       "sample": cpu["sample"]},
+            "cpu_baseline": cpu, "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--restart", type=int, default=50)
+    ap.add_argument("--cpu-iters", type=int, default=8)
+    ap.add_argument("--iters-per-point", type=float, default=ITERS_PER_POINT_FALLBACK)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, dist = dist_setup()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world, dist)
+    else:
+        out = run_ours(args, rank, world, dist)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -141,6 +141,55 @@ int wg_precondition(wg_problem* h, const double* r, double* z);
 /* The batch's right-hand sides (batch*N complex). */
 int wg_get_rhs(wg_problem* h, double* rhs);
 
+/* ---- Gummel self-consistency (1D RTD, Dirichlet contacts) ----------------
+ * RTD/solve2D_rtd_self_consistent.m:88-205 with the approximate-Newton
+ * Poisson step of RTD/solve_Poisson2D_rtd.m:56-186 and the DG -> control
+ * volume projection of RTD/project_DG_density_RTD.m, for Ny = 1. */
+typedef struct {
+  const double* vc_ev;  /* [nx] conduction band edge (mat.Vc) [eV]; V = Vc - phi */
+  const double* nd_m3;  /* [nx] ionised donors (mat.Nd) [m^-3] */
+  const double* eps_r;  /* [nx] relative permittivity (mat.eps) */
+  const double* phi0;   /* [nx] initial electrostatic potential [V], phi(0)=0, phi(end)=bias */
+  double bias;          /* drain bias [V] */
+  double ef_offset;     /* E_F - Vc at both contacts [eV] (0.05 in solve2D_rtd_self_consistent.m:110) */
+  double dy_nm;         /* density normalisation: n = n_DG |Vsub|^2 / dy (solve_transport_DG_2D.m:204) */
+} wg_rtd_1d;
+
+typedef struct {
+  int max_iterations;          /* 0 -> 100 */
+  double mixing;               /* alpha in (0,1]; 0 -> 0.1 */
+  double potential_tol;        /* max |phi* - phi| [V]; 0 -> 5e-4 */
+  double density_tol;          /* relative density change; 0 -> 5e-4 */
+  double poisson_residual_tol; /* |F|_inf / scale before the step; 0 -> 8e-2 */
+  double transport_tol;        /* GMRES relative residual; 0 -> 1e-8 */
+  int transport_maxit;         /* GMRES restart cycles; 0 -> 50 */
+  int warm_start;              /* 1: first transport solve starts from the resident rho */
+  int restart_from_phi0;       /* 1: reset phi to the phi0 of wg_gummel_set (device copy) */
+} wg_gummel_opts;
+
+enum { WG_GUMMEL_CONVERGED = 0, WG_GUMMEL_ITERATION_LIMIT = 1, WG_GUMMEL_TRANSPORT_FAILED = 2,
+       WG_GUMMEL_POISSON_FAILED = 3 };
+
+typedef struct {
+  int status;                  /* WG_GUMMEL_* (sweep.status of the reference) */
+  int iterations;              /* Gummel iterations run */
+  int gmres_iterations;        /* inner Krylov iterations over all transport solves */
+  double potential_defect;     /* last max |phi* - phi| [V] */
+  double density_change;       /* last relative density change */
+  double poisson_relres;       /* last Poisson residual before the step */
+  double transport_relres;     /* last transport true relative residual */
+  double seconds;              /* wall time from the start of wg_gummel_run to this problem's exit */
+} wg_gummel_info;
+
+/* Problem b: device/material data, RTD electrostatics and initial potential.
+ * Sets the transport data for V = Vc - phi0 (calls wg_set_potential). */
+int wg_gummel_set(wg_problem* h, int b, const wg_device* dev, const wg_rtd_1d* rtd);
+/* Run every problem's Gummel loop to convergence (or a limit).  info has batch entries.
+ * Returns WG_OK when all converged, WG_NOT_CONVERGED otherwise. */
+int wg_gummel_run(wg_problem* h, const wg_gummel_opts* opts, wg_gummel_info* info);
+/* Problem b's potential phi [nx], density n [n_el*n_local] in m^-3 and current density j. */
+int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j);
+
 /* Kernel-class profiler (the reference's tic/toc solveInfo timings,
  * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).
  * Classes: flux, forward GEMM, xi stencil, backward GEMM, k-line
@@ -151,6 +200,11 @@ int wg_profile_enable(wg_problem* h, int on);
 /* ms[i]: summed event time of class i; timed[i]: timed launches; launches[i]:
  * kernel launches of class i since the last reset (always counted). */
 int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, int reset);
+
+/* CUDA events on the handle's stream (16 slots): device-side timing of any
+ * sequence of calls.  wg_event_elapsed waits for slot b. */
+int wg_event_record(wg_problem* h, int slot);
+int wg_event_elapsed(wg_problem* h, int a, int b, double* ms);
 
 #ifdef __cplusplus
 }

@@ -36,6 +36,31 @@ class WgSolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("use_rho0", C.c_int)]
 
 
+class WgRtd1D(C.Structure):
+    _fields_ = [("vc_ev", C.POINTER(C.c_double)), ("nd_m3", C.POINTER(C.c_double)), ("eps_r", C.POINTER(C.c_double)),
+                ("phi0", C.POINTER(C.c_double)), ("bias", C.c_double), ("ef_offset", C.c_double),
+                ("dy_nm", C.c_double)]
+
+
+class WgGummelOpts(C.Structure):
+    _fields_ = [("max_iterations", C.c_int), ("mixing", C.c_double), ("potential_tol", C.c_double),
+                ("density_tol", C.c_double), ("poisson_residual_tol", C.c_double), ("transport_tol", C.c_double),
+                ("transport_maxit", C.c_int), ("warm_start", C.c_int), ("restart_from_phi0", C.c_int)]
+
+
+class WgGummelInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("gmres_iterations", C.c_int),
+                ("potential_defect", C.c_double), ("density_change", C.c_double), ("poisson_relres", C.c_double),
+                ("transport_relres", C.c_double), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+GUMMEL_STATUS = {0: "fixed-point-converged", 1: "iteration-limit", 2: "transport-not-converged",
+                 3: "poisson-not-converged"}
+
+
 class WgSolveInfo(C.Structure):
     _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("cycles", C.c_int), ("refinements", C.c_int),
                 ("relres", C.c_double), ("initial_relres", C.c_double), ("rhs_norm", C.c_double)]
@@ -61,6 +86,11 @@ SIGNATURES = {
     "wg_apply": ([_H, _D, _D], C.c_int),
     "wg_precondition": ([_H, _D, _D], C.c_int),
     "wg_get_rhs": ([_H, _D], C.c_int),
+    "wg_gummel_set": ([_H, C.c_int, C.POINTER(WgDevice), C.POINTER(WgRtd1D)], C.c_int),
+    "wg_gummel_run": ([_H, C.POINTER(WgGummelOpts), C.POINTER(WgGummelInfo)], C.c_int),
+    "wg_gummel_get": ([_H, C.c_int, _D, _D, _D], C.c_int),
+    "wg_event_record": ([_H, C.c_int], C.c_int),
+    "wg_event_elapsed": ([_H, C.c_int, C.c_int, _D], C.c_int),
     "wg_profile_enable": ([_H, C.c_int], C.c_int),
     "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.c_int], C.c_int),
 }

@@ -39,7 +39,13 @@ cudaError_t dalloc(T** p, size_t count, double& bytes) {
 
 void free_all(wg::Problem& P) {
   wg::prof_release(P);
-  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.qd, P.beta, P.xq, P.pot_x,
+  for (cudaEvent_t& e : P.ev)
+    if (e) {
+      cudaEventDestroy(e);
+      e = nullptr;
+    }
+  wg::gummel_free(P);
+  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
                   P.ycoef, P.partial, P.nrm_partial, P.nrm, P.target, P.active, P.kused, P.any_active,
                   P.mx.phi16, P.mx.xin16, P.mx.V, P.mx.w, P.mx.z, P.mx.xh, P.mx.yh, P.mx.beta};
@@ -90,7 +96,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   wg_problem* h = new (std::nothrow) wg_problem();
   if (!h) return fail(nullptr, WG_ERR_OOM, "host allocation failed");
   wg::Problem& P = h->P;
-  std::string e = wg::build_shape(P.s, prm->n_el, prm->n_local, prm->nk, prm->n_xi, prm->l_xi, prm->m_diff, prm->mpc);
+  std::string e = wg::build_shape_cached(P.s, prm->n_el, prm->n_local, prm->nk, prm->n_xi, prm->l_xi, prm->m_diff, prm->mpc);
   if (!e.empty()) {
     delete h;
     return fail(nullptr, WG_ERR_ARG, "wg_problem_create: " + e);
@@ -126,6 +132,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
     P.fb.K2[i] = s.K2[i];
     P.fb.K3[i] = s.K3[i];
     P.fb.K5[i] = s.K5[i];
+    P.fb.invM[i] = s.invM[i];
   }
   double bytes = 0;
   cudaError_t ce = cudaSuccess;
@@ -140,6 +147,10 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.betai, (size_t)nK * nK * (s.nxi + 1), bytes));
   A(dalloc(&P.pre_dinv, (size_t)s.nk * nK * nK, bytes));
   A(dalloc(&P.pre_h, (size_t)s.nk * nK, bytes));
+  A(dalloc(&P.cosm, (size_t)s.nxi * s.nk, bytes));
+  A(dalloc(&P.pinv, (size_t)s.nk * s.nxi, bytes));
+  A(dalloc(&P.pp, (size_t)batch * wg::kPP, bytes));
+  A(dalloc(&P.flr, (size_t)batch * 2 * s.nk, bytes));
   A(dalloc(&P.qd, batch, bytes));
   A(dalloc(&P.beta, (size_t)batch * s.n_el * nK * nK * (s.nxi + 1), bytes));
   A(dalloc(&P.xq, (size_t)batch * s.n_el * wg::kNqx, bytes));
@@ -214,6 +225,13 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   API_CK(&P, cudaMemcpyAsync(P.betai, betai.data(), sizeof(double) * betai.size(), cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.pre_dinv, dinv.data(), sizeof(double) * dinv.size(), cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.pre_h, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaMemcpyAsync(P.cosm, s.cosm.data(), sizeof(double) * s.cosm.size(), cudaMemcpyHostToDevice, P.stream));
+  {
+    std::vector<double2> pinv(s.pinv.size());
+    for (size_t i = 0; i < pinv.size(); ++i) pinv[i] = make_double2(s.pinv[i].real(), s.pinv[i].imag());
+    API_CK(&P, cudaMemcpyAsync(P.pinv, pinv.data(), sizeof(double2) * pinv.size(), cudaMemcpyHostToDevice, P.stream));
+    API_CK(&P, cudaStreamSynchronize(P.stream));
+  }
   API_CK(&P, cudaMemsetAsync(P.rhs, 0, sizeof(double2) * BN, P.stream));
   API_CK(&P, cudaMemsetAsync(P.x, 0, sizeof(double2) * BN, P.stream));
   API_CK(&P, cudaMemsetAsync(P.beta, 0, sizeof(double) * batch * s.n_el * nK * nK * (s.nxi + 1), P.stream));
@@ -263,33 +281,29 @@ int wg_set_potential(wg_problem* h, int b, const wg_device* dev, const double* e
   hp.l_chi = dev->x_nm[nx - 1] * 1e-9;
   const double detJ = hp.l_chi / s.n_el / 2;
   hp.qd = s.q_diff / detJ * s.mpc;
-  hp.vmin = *std::min_element(esub_ev, esub_ev + nx);
-  std::string e = wg::contact_inflow(s, esub_ev, dev->m_kg, nx, dev->me_z, dev->temp, ef_l, ef_r, hp.fnl, hp.fnr);
-  if (!e.empty()) return fail(&P, WG_ERR_ARG, "wg_set_potential: " + e);
+  {
+    double vmax = esub_ev[0];
+    for (int i = 1; i < nx; ++i) vmax = std::max(vmax, esub_ev[i]);
+    if (!(vmax + 0.3 > 0)) return fail(&P, WG_ERR_ARG, "wg_set_potential: max(Esub)+0.3 must be positive (kz range of verteilung.m:140)");
+    if (!(dev->me_z > 0) || !(dev->temp > 0) || !(dev->m_kg[0] > 0) || !(dev->m_kg[nx - 1] > 0))
+      return fail(&P, WG_ERR_ARG, "wg_set_potential: masses and Temp must be positive");
+  }
   hp.m_nodes.resize((size_t)s.n_el * nK);
   for (int el = 0; el < s.n_el; ++el)
     for (int a = 0; a < nK; ++a) hp.m_nodes[(size_t)el * nK + a] = dev->m_kg[el * (nK - 1) + a];
   std::vector<double> xq, xg(nx);
   wg::quad_points(s, hp.l_chi, xq);
   for (int i = 0; i < nx; ++i) xg[i] = dev->x_nm[i] * 1e-9;
-  // contact inflow blocks: first element (k > 0) and last element (k < 0), get_Diff.m:77-83
-  std::vector<double2> rfirst((size_t)nK * s.nk), rlast((size_t)nK * s.nk);
-  for (int a = 0; a < nK; ++a)
-    for (int j = 0; j < s.nk; ++j) {
-      const double k = s.k[j], ak = std::fabs(k);
-      const double q1 = s.invM[a * nK + 0] / detJ, q2 = s.invM[a * nK + nK - 1] / detJ;
-      const wg::cplx vl = (k > 0 ? 1.0 : 0.0) * (ak * hp.fnl[j]);
-      const wg::cplx vr = (k < 0 ? 1.0 : 0.0) * (ak * hp.fnr[j]);
-      const wg::cplx tl = s.mpc * (s.q_diff * (q1 * vl));
-      const wg::cplx tr = s.mpc * (s.q_diff * (q2 * vr));
-      rfirst[(size_t)a * s.nk + j] = make_double2(tl.real(), tl.imag());
-      rlast[(size_t)a * s.nk + j] = make_double2(tr.real(), tr.imag());
-    }
-  const size_t blk = (size_t)nK * s.nk;
-  double2* rb = P.rhs + (long long)b * P.N;
-  API_CK(&P, cudaMemcpyAsync(rb, rfirst.data(), sizeof(double2) * blk, cudaMemcpyHostToDevice, P.stream));
-  API_CK(&P, cudaMemcpyAsync(rb + (long long)(s.n_el - 1) * blk, rlast.data(), sizeof(double2) * blk,
-                             cudaMemcpyHostToDevice, P.stream));
+  double pp[wg::kPP] = {};
+  pp[wg::PP_LX] = hp.l_chi;
+  pp[wg::PP_QD] = hp.qd;
+  pp[wg::PP_M0] = dev->m_kg[0];
+  pp[wg::PP_M1] = dev->m_kg[nx - 1];
+  pp[wg::PP_MEZ] = dev->me_z;
+  pp[wg::PP_TEMP] = dev->temp;
+  pp[wg::PP_EFL] = ef_l;
+  pp[wg::PP_EFR] = ef_r;
+  API_CK(&P, cudaMemcpyAsync(P.pp + (long long)b * wg::kPP, pp, sizeof(pp), cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.xq + (long long)b * s.n_el * wg::kNqx, xq.data(), sizeof(double) * xq.size(),
                              cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.pot_x + (long long)b * nx, xg.data(), sizeof(double) * nx, cudaMemcpyHostToDevice, P.stream));
@@ -297,7 +311,7 @@ int wg_set_potential(wg_problem* h, int b, const wg_device* dev, const double* e
   API_CK(&P, cudaMemcpyAsync(P.m_nodes + (long long)b * s.n_el * nK, hp.m_nodes.data(), sizeof(double) * hp.m_nodes.size(),
                              cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.qd + b, &hp.qd, sizeof(double), cudaMemcpyHostToDevice, P.stream));
-  API_CK(&P, wg::launch_vw_rebuild(P, b));
+  API_CK(&P, wg::launch_potential_update(P, b, b + 1));
   // host vectors above go out of scope: wait for the copies
   API_CK(&P, cudaStreamSynchronize(P.stream));
   hp.ready = true;
@@ -324,7 +338,7 @@ int wg_solve(wg_problem* h, const wg_solve_opts* opts, const double* rho0, wg_so
     warm = true;
   }
   std::memset(info, 0, sizeof(wg_solve_info) * P.batch);
-  int rc = wg::gmres_solve_fp64(P, o, warm, info);
+  int rc = wg::solve_dispatch(P, o, warm, info);
   if (rc == WG_ERR_CUDA || rc == WG_ERR_NUMERIC) fail(&P, rc, P.err);
   return rc;
 }
@@ -382,6 +396,67 @@ int wg_precondition(wg_problem* h, const double* r, double* z) {
   API_CK(&P, wg::launch_precondition(P, P.r, P.N, P.z));
   API_CK(&P, cudaMemcpyAsync(z, P.z, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_gummel_set(wg_problem* h, int b, const wg_device* dev, const wg_rtd_1d* rtd) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_gummel_set: batch index out of range");
+  if (!dev || !rtd || !dev->x_nm || !rtd->vc_ev || !rtd->nd_m3 || !rtd->eps_r || !rtd->phi0)
+    return fail(&P, WG_ERR_ARG, "wg_gummel_set: null argument");
+  if (dev->nx != P.nx) return fail(&P, WG_ERR_ARG, "wg_gummel_set: nx must equal n_el*(n_local-1)+1");
+  if (!std::isfinite(rtd->bias) || !std::isfinite(rtd->ef_offset))
+    return fail(&P, WG_ERR_ARG, "wg_gummel_set: non-finite bias or Fermi offset");
+  // transport data for the initial potential V = Vc - phi0, E_F from the contact band edges
+  std::vector<double> v(P.nx);
+  for (int i = 0; i < P.nx; ++i) v[i] = rtd->vc_ev[i] - rtd->phi0[i];
+  const double efl = rtd->vc_ev[0] + rtd->ef_offset;
+  const double efr = rtd->vc_ev[P.nx - 1] + rtd->ef_offset - rtd->bias;
+  int rc = wg_set_potential(h, b, dev, v.data(), efl, efr);
+  if (rc) return rc;
+  rc = wg::gummel_set(P, b, *dev, *rtd);
+  if (rc) return fail(&P, rc, P.err);
+  return WG_OK;
+}
+
+int wg_gummel_run(wg_problem* h, const wg_gummel_opts* opts, wg_gummel_info* info) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (!info) return fail(&P, WG_ERR_ARG, "wg_gummel_run: info must hold batch entries");
+  wg_gummel_opts o{};
+  if (opts) o = *opts;
+  if (o.mixing < 0 || o.mixing > 1) return fail(&P, WG_ERR_ARG, "wg_gummel_run: mixing must be in (0, 1]");
+  const int rc = wg::gummel_run(P, o, info);
+  if (rc != WG_OK && rc != WG_NOT_CONVERGED) return fail(&P, rc, P.err);
+  return rc;
+}
+
+int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_gummel_get: batch index out of range");
+  const int rc = wg::gummel_get(P, b, phi, n_dg, j);
+  if (rc) return fail(&P, rc, P.err);
+  return WG_OK;
+}
+
+int wg_event_record(wg_problem* h, int slot) {
+  if (!h || slot < 0 || slot >= 16) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_event_record: bad slot");
+  wg::Problem& P = h->P;
+  if (!P.ev[slot]) API_CK(&P, cudaEventCreate(&P.ev[slot]));
+  API_CK(&P, cudaEventRecord(P.ev[slot], P.stream));
+  return WG_OK;
+}
+
+int wg_event_elapsed(wg_problem* h, int a, int b, double* ms) {
+  if (!h || !ms || a < 0 || b < 0 || a >= 16 || b >= 16 || !h->P.ev[a] || !h->P.ev[b])
+    return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_event_elapsed: unrecorded slot");
+  wg::Problem& P = h->P;
+  API_CK(&P, cudaEventSynchronize(P.ev[b]));
+  float f = 0;
+  API_CK(&P, cudaEventElapsedTime(&f, P.ev[a], P.ev[b]));
+  *ms = f;
   return WG_OK;
 }
 

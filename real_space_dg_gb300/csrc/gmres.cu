@@ -426,4 +426,8 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
   return status;
 }
 
+int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info) {
+  return gmres_solve_fp64(P, o, warm, info);
+}
+
 }  // namespace wg

@@ -324,52 +324,6 @@ __global__ void precond_kernel(const double2* __restrict__ r, double2* __restric
 }
 
 // ---------------------------------------------------------------------------
-// Vw(x,k) rebuild: beta[b][e][ac][s] = (dxi/4) mpc sum_q kap[ac][q]
-//     * (V(x_q + xi_s/2) - V(x_q - xi_s/2))
-// with V the lookup of V_transient.m (linear inside [0,Lx), min(V) beyond Lx,
-// V(1) below 0).  One thread per (e, s).
-// ---------------------------------------------------------------------------
-__device__ double v_lookup(double x, const double* __restrict__ xg, const double* __restrict__ vg, int nx,
-                           double lx, double vmin) {
-  if (x < 0) return vg[0];
-  if (x >= lx) return vmin;
-  int lo = 0, hi = nx - 1;
-  if (x >= xg[hi]) return vg[hi];
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (xg[mid] <= x) lo = mid; else hi = mid;
-  }
-  const double slope = (vg[lo + 1] - vg[lo]) / (xg[lo + 1] - xg[lo]);
-  return slope * (x - xg[lo]) + vg[lo];
-}
-
-template <int NK>
-__global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ xq, const double* __restrict__ xi_edge,
-                          const double* __restrict__ kap, const double* __restrict__ xg, const double* __restrict__ vg,
-                          int nx, double lx, double vmin, int n_el, int nxi, double scale) {
-  const int ne = nxi + 1;
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n_el * ne) return;
-  const int s = (int)(t % ne);
-  const int e = (int)(t / ne);
-  const double xi = xi_edge[s];
-  double dv[kNqx];
-#pragma unroll
-  for (int q = 0; q < kNqx; ++q) {
-    const double x = xq[e * kNqx + q];
-    dv[q] = v_lookup(x + 0.5 * xi, xg, vg, nx, lx, vmin) - v_lookup(x - 0.5 * xi, xg, vg, nx, lx, vmin);
-  }
-  double* be = beta + (long long)e * NK * NK * ne;
-#pragma unroll
-  for (int ac = 0; ac < NK * NK; ++ac) {
-    double acc = 0.0;
-#pragma unroll
-    for (int q = 0; q < kNqx; ++q) acc += kap[ac * kNqx + q] * dv[q];
-    be[(long long)ac * ne + s] = acc * scale;
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Observables: rho_u(s) = sum_j Phi(s,j) rho_{x,j} at the centre xi rows,
 // n = Re rho_u(centre), j = q hbar / m Im d rho_u / d xi
 // (solve_transport_DG_2D.m:114-156).  One warp per DG node.
@@ -515,29 +469,6 @@ cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride
     case 3: return precond_nk<3>(P, r, r_stride, z);
     default: return precond_nk<4>(P, r, r_stride, z);
   }
-}
-
-cudaError_t launch_vw_rebuild(Problem& P, int b) {
-  const HostProblem& hpb = P.hp[b];
-  const int ne = P.s.nxi + 1;
-  const long long total = (long long)P.s.n_el * ne;
-  double* beta = P.beta + (long long)b * P.s.n_el * P.s.nK * P.s.nK * ne;
-  const double* xq = P.xq + (long long)b * P.s.n_el * kNqx;
-  const double* xg = P.pot_x + (long long)b * P.nx;
-  const double* vg = P.pot_v + (long long)b * P.nx;
-  // min(V) for x >= Lx (V_transient.m:6) is computed on the host and passed by value
-  double vmin = hpb.vmin;
-  const double scale = P.s.delta_xi / 4 * P.s.mpc;
-  const unsigned grid = (unsigned)((total + 127) / 128);
-  switch (P.s.nK) {
-    case 2: vw_kernel<2><<<grid, 128, 0, P.stream>>>(beta, xq, P.xi_edge, P.kap, xg, vg, P.nx, hpb.l_chi, vmin,
-                                                     P.s.n_el, P.s.nxi, scale); break;
-    case 3: vw_kernel<3><<<grid, 128, 0, P.stream>>>(beta, xq, P.xi_edge, P.kap, xg, vg, P.nx, hpb.l_chi, vmin,
-                                                     P.s.n_el, P.s.nxi, scale); break;
-    default: vw_kernel<4><<<grid, 128, 0, P.stream>>>(beta, xq, P.xi_edge, P.kap, xg, vg, P.nx, hpb.l_chi, vmin,
-                                                      P.s.n_el, P.s.nxi, scale); break;
-  }
-  return cudaGetLastError();
 }
 
 cudaError_t launch_rho_xi(Problem& P, int b, double2* out) {

@@ -17,16 +17,19 @@ struct FluxBlocks {
   double K2[kMaxLocal * kMaxLocal];
   double K3[kMaxLocal * kMaxLocal];
   double K5[kMaxLocal * kMaxLocal];
+  double invM[kMaxLocal * kMaxLocal];
 };
+
+// Per-problem scalar parameters on the device: pp[b * kPP + PP_*].
+constexpr int kPP = 10;
+enum { PP_LX = 0, PP_QD, PP_M0, PP_M1, PP_MEZ, PP_TEMP, PP_EFL, PP_EFR, PP_VMIN, PP_VMAX };
 
 // Per-problem host copy of the set-up that stays fixed until the next set_potential.
 struct HostProblem {
   bool ready = false;
   double l_chi = 0;                 // device length [m]
   double qd = 0;                    // Q_diff * mpc / detJ
-  double vmin = 0;                  // min(Esub): V(x >= Lx) of V_transient.m:6
   std::vector<double> m_nodes;      // mass at the DG nodes [kg]
-  std::vector<cplx> fnl, fnr;
 };
 
 // Device buffers of the mixed-precision inner solver (allocated only for WG_PREC_MIXED).
@@ -60,6 +63,34 @@ struct Profiler {
   long long launches[PROF_N] = {};
 };
 
+// Device arrays of the Gummel loop (allocated on the first wg_gummel_set).
+struct GummelDev {
+  double* vc = nullptr;      // [B][nx] band edge
+  double* nd = nullptr;      // [B][nx] donors
+  double* phi = nullptr;     // [B][nx] electrostatic potential
+  double* phi0 = nullptr;    // [B][nx] initial potential of wg_gummel_set
+  double* cand = nullptr;    // [B][nx] Poisson candidate
+  double* ncv = nullptr;     // [B][nx] control-volume density
+  double* tri = nullptr;     // [B][3][nx] Poisson stencil (lower, diagonal, upper)
+  double* work = nullptr;    // [B][2][nx] Thomas scratch
+  double* projc = nullptr;   // [B][nx][2][kMaxLocal] projection weights
+  int* proje = nullptr;      // [B][nx][2] projection element indices (-1: none)
+  double* ndg = nullptr;     // [B][ncol] density at the DG nodes [m^-3]
+  double* jdg = nullptr;     // [B][ncol] current density at the DG nodes
+  double* nprev = nullptr;   // [B][ncol] previous iteration's density
+  double* diag = nullptr;    // [B][8] Poisson-step diagnostics
+  double* bias = nullptr;    // [B]
+  double* temp = nullptr;    // [B]
+  double* scale = nullptr;   // [B] |Vsub|^2 / dy
+  int* active = nullptr;     // [B]
+  int* mix = nullptr;        // [B]
+};
+
+struct GummelHost {
+  bool ready = false;
+  double bias = 0;
+};
+
 struct Problem {
   // shape
   Shape s;
@@ -84,8 +115,12 @@ struct Problem {
   double* betai = nullptr;       // [nK*nK][nxi+1] CAP part of the potential weights (imaginary)
   double* pre_dinv = nullptr;    // [nk][nK*nK] inverse of k K1 + |k| K2
   double* pre_h = nullptr;       // [nk][nK] D0^-1 * coupling column
+  double* cosm = nullptr;        // [nxi][nk] cos(xi_s k_j)
+  double2* pinv = nullptr;       // [nk][nxi] pseudo-inverse of Phi
   // per-problem device data
   double* qd = nullptr;          // [B]
+  double* pp = nullptr;          // [B][kPP] per-problem scalars
+  double* flr = nullptr;         // [B][2][nk] contact occupations f_L, f_R
   double* beta = nullptr;        // [B][n_el][nK*nK][nxi+1] real potential weights
   double* xq = nullptr;          // [B][n_el*10] quadrature x [m]
   double* pot_x = nullptr;       // [B][nx] material grid [m]
@@ -122,6 +157,9 @@ struct Problem {
 
   MixedBuffers mx;
   Profiler prof;
+  GummelDev gd;
+  std::vector<GummelHost> gh;
+  cudaEvent_t ev[16] = {};       // user event slots (wg_event_record)
 };
 
 // Profiler helpers (operator.cu).  prof_begin counts `n` launches of class cls
@@ -134,10 +172,18 @@ void prof_release(Problem& P);
 // Kernel launchers (operator.cu)
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y);
 cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z);
-cudaError_t launch_vw_rebuild(Problem& P, int b);
+// Rebuild potential-dependent data (Vw weights, contact inflow rhs) of problems [b0, b1).
+cudaError_t launch_potential_update(Problem& P, int b0, int b1);
 cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j);
 cudaError_t launch_rho_xi(Problem& P, int b, double2* out);
 // Krylov (gmres.cu)
 int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
+// FP64 GMRES or the mixed-precision refinement, by P.precision.
+int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
+// Gummel loop (gummel.cu)
+int gummel_set(Problem& P, int b, const wg_device& dev, const wg_rtd_1d& rtd);
+int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info);
+int gummel_get(Problem& P, int b, double* phi, double* n_dg, double* j);
+void gummel_free(Problem& P);
 
 }  // namespace wg

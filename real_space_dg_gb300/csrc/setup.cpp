@@ -12,6 +12,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <memory>
+#include <mutex>
 
 namespace wg {
 
@@ -214,7 +217,8 @@ void householder_qr(std::vector<cplx>& a, std::vector<cplx>& tau, int m, int n) 
 
 }  // namespace
 
-std::string build_shape(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff, double mpc) {
+std::string build_shape_light(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff,
+                              double mpc) {
   if (n_el < 2) return "n_el must be >= 2";
   if (nK < 2 || nK > kMaxLocal) return "n_local must be 2..4 (DG order 1..3)";
   if (nk < 2) return "nk must be >= 2";
@@ -291,8 +295,71 @@ std::string build_shape(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi
       const double th = s.xi_elem[i] * s.k[j];
       s.phi[(size_t)i * nk + j] = cplx(std::cos(th), std::sin(th)) / sc;
     }
+  s.cosm.resize((size_t)nxi * nk);
+  for (int i = 0; i < nxi; ++i)
+    for (int j = 0; j < nk; ++j) s.cosm[(size_t)i * nk + j] = std::cos(s.xi_elem[i] * s.k[j]);
+  return "";
+}
+
+std::string build_shape(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff, double mpc) {
+  std::string e = build_shape_light(s, n_el, nK, nk, nxi, l_xi, m_diff, mpc);
+  if (!e.empty()) return e;
   s.qr = s.phi;
   householder_qr(s.qr, s.tau, nxi, nk);
+  // Phi^+ column by column: z = argmin |Phi z - e_i|
+  s.pinv.assign((size_t)nk * nxi, cplx(0));
+  std::vector<cplx> unit(nxi), z;
+  for (int i = 0; i < nxi; ++i) {
+    std::fill(unit.begin(), unit.end(), cplx(0));
+    unit[i] = 1.0;
+    phi_lstsq(s, unit, z);
+    for (int j = 0; j < nk; ++j) s.pinv[(size_t)j * nxi + i] = z[j];
+  }
+  return "";
+}
+
+std::string build_shape_cached(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff,
+                               double mpc) {
+  // The expensive part (QR and pseudo-inverse of Phi) depends only on (nk, nxi, l_xi).
+  struct Key {
+    int nk, nxi;
+    double l_xi;
+    bool operator<(const Key& o) const {
+      if (nk != o.nk) return nk < o.nk;
+      if (nxi != o.nxi) return nxi < o.nxi;
+      return l_xi < o.l_xi;
+    }
+  };
+  static std::mutex mu;
+  static std::map<Key, std::shared_ptr<const Shape>> cache;
+  const Key key{nk, nxi, l_xi};
+  std::shared_ptr<const Shape> hit;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) hit = it->second;
+  }
+  if (hit && hit->n_el == n_el && hit->nK == nK && hit->m_diff == (m_diff > 0 ? m_diff : kMElektronRef) &&
+      hit->mpc == (mpc != 0 ? mpc : 1.0)) {
+    s = *hit;
+    return "";
+  }
+  if (hit) {
+    // same xi/k basis, different element data: rebuild the cheap part, reuse QR and Phi^+
+    Shape t;
+    std::vector<cplx> qr = hit->qr, tau = hit->tau, pinv = hit->pinv;
+    std::string e = build_shape_light(t, n_el, nK, nk, nxi, l_xi, m_diff, mpc);
+    if (!e.empty()) return e;
+    t.qr = std::move(qr);
+    t.tau = std::move(tau);
+    t.pinv = std::move(pinv);
+    s = t;
+    return "";
+  }
+  std::string e = build_shape(s, n_el, nK, nk, nxi, l_xi, m_diff, mpc);
+  if (!e.empty()) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = std::make_shared<const Shape>(s);
   return "";
 }
 
@@ -324,51 +391,6 @@ void quad_points(const Shape& s, double l_chi, std::vector<double>& xq) {
   xq.resize((size_t)s.n_el * kNqx);
   for (int e = 0; e < s.n_el; ++e)
     for (int q = 0; q < kNqx; ++q) xq[(size_t)e * kNqx + q] = disk[e] + chi_gl[q];
-}
-
-std::string contact_inflow(const Shape& s, const double* esub_ev, const double* m_kg, int nx, double me_z,
-                           double temp, double ef_l, double ef_r, std::vector<cplx>& fnl,
-                           std::vector<cplx>& fnr) {
-  const int nk = s.nk;
-  const double hb = kHV / 2 / M_PI;
-  double vmax = esub_ev[0];
-  for (int i = 1; i < nx; ++i) vmax = std::max(vmax, esub_ev[i]);
-  if (!(vmax + 0.3 > 0)) return "max(Esub)+0.3 must be positive (kz range of verteilung.m:140)";
-  if (!(me_z > 0) || !(temp > 0) || !(m_kg[0] > 0) || !(m_kg[nx - 1] > 0)) return "masses and Temp must be positive";
-  const double kz_max = std::sqrt(2 * 2 * kM0V * me_z * kQV * (vmax + 0.3)) / hb;
-  const double dkz = kz_max / (kNkz - 1);
-  std::vector<double> ekz(kNkz);
-  for (int z = 0; z < kNkz; ++z) {
-    const double kz = (z == kNkz - 1) ? kz_max : z * dkz;
-    ekz[z] = hb * hb * kz * kz / 2 / kM0V / me_z / kQV;
-  }
-  const double dk = std::fabs(s.k[1] - s.k[0]);
-  std::vector<double> fL(nk), fR(nk);
-  for (int j = 0; j < nk; ++j) {
-    const double EL = esub_ev[0] + hb * hb * s.k[j] * s.k[j] / 2 / m_kg[0] / kQV;
-    const double ER = esub_ev[nx - 1] + hb * hb * s.k[j] * s.k[j] / 2 / m_kg[nx - 1] / kQV;
-    double sl = 0, sr = 0;
-    for (int z = 0; z < kNkz; ++z) {
-      sl += 1.0 / (1.0 + std::exp(kQV * (EL + ekz[z] - ef_l) / (kKBV * temp)));
-      sr += 1.0 / (1.0 + std::exp(kQV * (ER + ekz[z] - ef_r) / (kKBV * temp)));
-    }
-    fL[j] = 2 / M_PI * dkz * sl;
-    fR[j] = 2 / M_PI * dkz * sr;
-  }
-  std::vector<cplx> fLn(s.nxi), fRn(s.nxi);
-  for (int i = 0; i < s.nxi; ++i) {
-    double al = 0, ar = 0;
-    for (int j = 0; j < nk; ++j) {
-      const double c = std::cos(s.xi_elem[i] * s.k[j]);
-      al += c * fL[j];
-      ar += c * fR[j];
-    }
-    fLn[i] = al * dk / 2 / M_PI;
-    fRn[i] = ar * dk / 2 / M_PI;
-  }
-  phi_lstsq(s, fLn, fnl);
-  phi_lstsq(s, fRn, fnr);
-  return "";
 }
 
 }  // namespace wg

@@ -42,20 +42,26 @@ struct Shape {
   // Householder QR of Phi for the least-squares contact projection
   std::vector<cplx> qr;                 // nxi x nk packed reflectors + R (row-major)
   std::vector<cplx> tau;
+  std::vector<cplx> pinv;               // nk x nxi: Phi^+ = R^-1 Q^H (row-major)
+  std::vector<double> cosm;             // nxi x nk: cos(xi_s k_j) (verteilung.m:158-161)
 };
+
+// Shape constants are pure functions of (n_el, nK, nk, nxi, l_xi, m_diff, mpc);
+// the QR and pseudo-inverse of Phi are shared through a process-wide cache.
+std::string build_shape_cached(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff,
+                               double mpc);
 
 // Build every shape constant.  Returns an empty string on success.
 std::string build_shape(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff,
                         double mpc);
 
+// The element/xi constants without the QR and pseudo-inverse of Phi.
+std::string build_shape_light(Shape& s, int n_el, int nK, int nk, int nxi, double l_xi, double m_diff,
+                              double mpc);
+
 // Quadrature x coordinates (n_el*10) for an element length delta_chi, built as
 // cumulative GL spacings (get_Drift_accel_trial_permutedShell.m:16-55).
 void quad_points(const Shape& s, double l_chi, std::vector<double>& xq);
-
-// Contact inflow coefficients fnl, fnr (verteilung.m:118-170, DG_MSA_2D, FV).
-std::string contact_inflow(const Shape& s, const double* esub_ev, const double* m_kg, int nx, double me_z,
-                           double temp, double ef_l, double ef_r, std::vector<cplx>& fnl,
-                           std::vector<cplx>& fnr);
 
 // Least-squares solve Phi z = f using the stored QR.
 void phi_lstsq(const Shape& s, const std::vector<cplx>& f, std::vector<cplx>& z);

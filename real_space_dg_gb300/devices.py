@@ -112,6 +112,35 @@ def flatband_potential(mat: dict, bias: float) -> np.ndarray:
     return np.asarray(mat["Vc"]) - bias * np.asarray(mat["ramp"])
 
 
+def density_normalisation_nm(mat: dict, offset_ev: float = 0.05) -> float:
+    """Transverse length dy [nm] that makes the contact's equilibrium density equal N_D.
+
+    The 1D Wigner density is n_DG = sum_k f(k) dk / 2 pi with f the kz-integrated
+    Fermi-Dirac occupation of the contact (verteilung.m:139-152), a sheet density;
+    the volume density is n_DG |Vsub|^2 / dy (solve_transport_DG_2D.m:204).  This
+    picks dy so that the flat-band contact at E_F - Ec = offset carries N_D.
+    """
+    h, m0, q, kb = 6.626e-34, 9.109e-31, 1.602e-19, 1.38e-23
+    hb = h / 2 / np.pi
+    prm = mat["dg"]["params"]
+    nk, lxi = int(prm["N"]), float(prm["Ly"])
+    k = -2 * np.pi / lxi * (np.arange(1, nk + 1) - 0.5 * (nk + 1))
+    dk = abs(k[1] - k[0])
+    m = float(np.asarray(mat["me_x"]).ravel()[0]) * m0
+    me_z = float(mat["me_z_ch"])
+    temp = float(mat["Temp"])
+    vmax = float(np.max(mat["Vc"]))
+    kz_max = np.sqrt(2 * 2 * m0 * me_z * q * (vmax + 0.3)) / hb
+    kz = np.linspace(0.0, kz_max, 1001)
+    ekz = hb ** 2 * kz ** 2 / 2 / m0 / me_z / q
+    e = hb ** 2 * k ** 2 / 2 / m / q - offset_ev
+    with np.errstate(over="ignore"):
+        f = 2 / np.pi * (kz[1] - kz[0]) * np.sum(1 / (1 + np.exp(q * (e[:, None] + ekz[None, :]) / (kb * temp))), 1)
+    n2d = np.sum(f) * dk / 2 / np.pi
+    nd = float(np.max(mat["Nd"]))
+    return n2d / nd / 1e-9
+
+
 def contact_fermi_levels(mat: dict, bias: float, offset_ev: float = 0.05):
     """E_F,L = Vc(1) + offset, E_F,R = Vc(end) + offset - bias
     (RTD/solve2D_rtd_self_consistent.m:110-111 defaults)."""

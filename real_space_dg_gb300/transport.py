@@ -136,6 +136,15 @@ class Problem1D:
         self._check(self.lib.wg_profile_read(self.h, _lib.dptr(ms), timed, launches, 1 if reset else 0))
         return {c: (ms[i], timed[i], launches[i]) for i, c in enumerate(_lib.PROF_CLASSES)}
 
+    def event(self, slot):
+        """Record CUDA event `slot` on this handle's stream."""
+        self._check(self.lib.wg_event_record(self.h, int(slot)))
+
+    def elapsed_ms(self, a, b):
+        ms = C.c_double()
+        self._check(self.lib.wg_event_elapsed(self.h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
     def rhs(self):
         out = np.empty(self.N * self.batch, dtype=np.complex128)
         self._check(self.lib.wg_get_rhs(self.h, out.view(np.float64).ctypes.data_as(_lib._D)))

@@ -1,0 +1,97 @@
+"""Gummel / Poisson self-consistency: CPU pins of the oracle and GPU parity.
+
+GPU tolerances: a fixed number of Gummel iterations reproduces the oracle's
+potential to 1e-9 V and the density to 1e-8 relative (the transport solves
+differ only by the 1e-12 GMRES tolerance); a converged loop reproduces the
+oracle's fixed point to the potential tolerance.
+"""
+import numpy as np
+import pytest
+
+from conftest import small_rtd
+from oracle import dg1d, gummel1d
+
+
+def test_poisson_matrix_is_second_difference():
+    x = np.linspace(0, 10, 41)
+    eps = np.full(41, 12.9)
+    lo, di, up = gummel1d.poisson_matrix(x, eps)
+    phi = 0.3 * x ** 2
+    lap = lo[1:-1] * phi[:-2] + di[1:-1] * phi[1:-1] + up[1:-1] * phi[2:]
+    assert np.allclose(lap, gummel1d.EPS0 * 12.9 * 0.6 * 1e18, rtol=1e-10)
+
+
+def test_poisson_step_keeps_neutral_linear_potential():
+    x = np.linspace(0, 20, 81)
+    tri = gummel1d.poisson_matrix(x, np.full(81, 12.9))
+    nd = np.full(81, 1e24)
+    phi = 0.2 * x / 20
+    cand, info = gummel1d.poisson_step(tri, nd.copy(), nd, phi, 0.2, 300.0)
+    assert info["converged"] and np.abs(cand - phi).max() < 1e-14
+
+
+def test_projection_conserves_the_dg_integral():
+    spec, mat, E, efl, efr, m = small_rtd(n_el=7, nk=16, order=3)
+    p = dg1d.init_params(mat, efl, efr, E, m)
+    T = gummel1d.projection(mat["x"], p)
+    x = mat["x"]
+    widths = np.diff(np.concatenate(([x[0]], (x[:-1] + x[1:]) / 2, [x[-1]])))
+    n = np.cos(np.arange(T.shape[1]))
+    # integral over the control volumes == integral of the DG polynomial (mass row sums)
+    w = np.tile(dg1d.jacobi.jacobi_gl(0, 0, 3)[1], 7) * (x[3] - x[0]) / 2
+    assert abs(widths @ (T @ n) - w @ n) < 1e-12 * abs(w @ n)
+
+
+def _rtd(n_el=12, nk=32, order=2, bias=0.1):
+    from real_space_dg_gb300 import devices
+    spec, mat, E, efl, efr, m = small_rtd(n_el=n_el, nk=nk, order=order, bias=bias)
+    dy = devices.density_normalisation_nm(mat)
+    return spec, mat, dy
+
+
+@pytest.mark.gpu
+def test_gummel_iterates_match_oracle(built_lib):
+    from real_space_dg_gb300.rtd import RTDSweep
+    spec, mat, dy = _rtd()
+    bias = 0.1
+    ref = gummel1d.gummel(mat, bias, bias * mat["ramp"], dy_nm=dy, mixing=0.3, potential_tol=1e-30,
+                          density_tol=1e-30, max_iterations=4)
+    S = RTDSweep(mat, 1, dict(mixing=0.3, potentialTolerance=1e-30, densityTolerance=1e-30, maxIterations=4,
+                              transportTolerance=1e-12, transportMaxCycles=60))
+    S.dy = dy
+    try:
+        S.set(0, bias)
+        st, info = S.run()
+        phi, n, j = S.get(0)
+    finally:
+        S.close()
+    assert info[0]["iterations"] == 4 and info[0]["status"] == 1
+    assert np.abs(phi - ref["phi"]).max() < 1e-9
+    assert np.linalg.norm(n - ref["n"]) < 1e-8 * np.linalg.norm(ref["n"])
+    assert np.linalg.norm(j - ref["j"]) < 1e-7 * np.linalg.norm(ref["j"])
+    assert abs(info[0]["potential_defect"] - ref["history"][-1]["defect"]) < 1e-9
+
+
+@pytest.mark.gpu
+def test_gummel_fixed_point_and_batch_independence(built_lib):
+    from real_space_dg_gb300.rtd import RTDSweep, solve_rtd_self_consistent
+    spec, mat, dy = _rtd(n_el=10, nk=24)
+    opts = dict(mixing=0.5, potentialTolerance=1e-6, densityTolerance=1e-5, maxIterations=120,
+                transportTolerance=1e-11, transportMaxCycles=60)
+    mat = dict(mat, dy_norm_nm=dy)
+    biases = [0.0, 0.1, 0.2]
+    res = solve_rtd_self_consistent(mat, biases, opts, mode="batched")
+    assert res["selfConsistency"]["converged"], res["sweep"]["status"]
+    for ib, bias in enumerate(biases):
+        ref = gummel1d.gummel(mat, bias, bias * mat["ramp"], dy_nm=dy, mixing=0.5, potential_tol=1e-6,
+                              density_tol=1e-5, max_iterations=120)
+        assert ref["status"] == "fixed-point-converged"
+        assert np.abs(res["sweep"]["phi"][:, ib] - ref["phi"]).max() < 2e-5
+        assert np.linalg.norm(res["sweep"]["current"][:, ib] - ref["j"]) <= 1e-3 * np.linalg.norm(ref["j"]) + 1e-30
+    # one bias alone gives the same as inside the batch
+    alone = solve_rtd_self_consistent(mat, [0.1], opts, mode="batched")
+    assert np.abs(alone["sweep"]["phi"][:, 0] - res["sweep"]["phi"][:, 1]).max() < 1e-12
+    # sequential continuation reaches the same fixed points
+    seq = solve_rtd_self_consistent(mat, biases, opts, mode="sequential")
+    assert seq["selfConsistency"]["converged"]
+    assert np.abs(seq["sweep"]["phi"] - res["sweep"]["phi"]).max() < 2e-5
