@@ -68,6 +68,8 @@ typedef struct {
   int precision;     /* WG_PREC_FP64 (drop-in) or WG_PREC_MIXED */
   int restart;       /* GMRES restart length m (basis m+1 vectors); 0 -> 50 */
   double mem_budget_bytes; /* admission budget for this handle; 0 -> no limit */
+  int inner_restart; /* mixed form: inner FP32 GMRES length; 0 -> 40 */
+  double inner_tol;  /* mixed form: floor of the inner relative tolerance; 0 -> 1e-3 */
 } wg_params;
 
 /* One problem's device/material data on the material grid (mat.x, nm). */
@@ -136,6 +138,9 @@ int wg_get_rho_xi(wg_problem* h, int b, double* rho_u);
 
 /* y = A x for the whole batch (host buffers, batch*N complex each). */
 int wg_apply(wg_problem* h, const double* x, double* y);
+/* y = A_lo x with the operator of the mixed form's inner solve (BF16 tensor-core
+ * transforms, FP32 flux and stencil); mixed handles only.  Host FP64 buffers. */
+int wg_apply_lowprec(wg_problem* h, const double* x, double* y);
 /* z = M^-1 r with the k-line preconditioner (host buffers). */
 int wg_precondition(wg_problem* h, const double* r, double* z);
 /* The batch's right-hand sides (batch*N complex). */
@@ -189,6 +194,11 @@ int wg_gummel_set(wg_problem* h, int b, const wg_device* dev, const wg_rtd_1d* r
 int wg_gummel_run(wg_problem* h, const wg_gummel_opts* opts, wg_gummel_info* info);
 /* Problem b's potential phi [nx], density n [n_el*n_local] in m^-3 and current density j. */
 int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j);
+
+/* Diagnostic: C = bf16(A) * bf16(B) on the tcgen05 tensor-core GEMM of the mixed
+ * form, FP32 accumulation.  A row-major M x K, B column-major K x N, C column-major
+ * M x N, host buffers; K >= 64 and K % 8 == 0.  No counterpart in the reference. */
+int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K);
 
 /* Kernel-class profiler (the reference's tic/toc solveInfo timings,
  * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).

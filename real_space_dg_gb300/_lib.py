@@ -24,7 +24,8 @@ ERROR_IDS = {WG_ERR_ARG: "DG:Full2D:InvalidArgument", WG_ERR_OOM: "DG:Full2D:Gmr
 class WgParams(C.Structure):
     _fields_ = [("n_el", C.c_int), ("n_local", C.c_int), ("nk", C.c_int), ("n_xi", C.c_int),
                 ("l_xi", C.c_double), ("m_diff", C.c_double), ("mpc", C.c_double), ("precision", C.c_int),
-                ("restart", C.c_int), ("mem_budget_bytes", C.c_double)]
+                ("restart", C.c_int), ("mem_budget_bytes", C.c_double), ("inner_restart", C.c_int),
+                ("inner_tol", C.c_double)]
 
 
 class WgDevice(C.Structure):
@@ -84,11 +85,14 @@ SIGNATURES = {
     "wg_get_observables": ([_H, C.c_int, _D, _D], C.c_int),
     "wg_get_rho_xi": ([_H, C.c_int, _D], C.c_int),
     "wg_apply": ([_H, _D, _D], C.c_int),
+    "wg_apply_lowprec": ([_H, _D, _D], C.c_int),
     "wg_precondition": ([_H, _D, _D], C.c_int),
     "wg_get_rhs": ([_H, _D], C.c_int),
     "wg_gummel_set": ([_H, C.c_int, C.POINTER(WgDevice), C.POINTER(WgRtd1D)], C.c_int),
     "wg_gummel_run": ([_H, C.POINTER(WgGummelOpts), C.POINTER(WgGummelInfo)], C.c_int),
     "wg_gummel_get": ([_H, C.c_int, _D, _D, _D], C.c_int),
+    "wg_debug_gemm_bf16": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
+                            C.c_int], C.c_int),
     "wg_event_record": ([_H, C.c_int], C.c_int),
     "wg_event_elapsed": ([_H, C.c_int, C.c_int, _D], C.c_int),
     "wg_profile_enable": ([_H, C.c_int], C.c_int),

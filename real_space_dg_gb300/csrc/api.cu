@@ -39,6 +39,7 @@ cudaError_t dalloc(T** p, size_t count, double& bytes) {
 
 void free_all(wg::Problem& P) {
   wg::prof_release(P);
+  wg::mixed_free(P);
   for (cudaEvent_t& e : P.ev)
     if (e) {
       cudaEventDestroy(e);
@@ -47,8 +48,7 @@ void free_all(wg::Problem& P) {
   wg::gummel_free(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
-                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.target, P.active, P.kused, P.any_active,
-                  P.mx.phi16, P.mx.xin16, P.mx.V, P.mx.w, P.mx.z, P.mx.xh, P.mx.yh, P.mx.beta};
+                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.target, P.active, P.kused, P.any_active};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P.stream) cudaStreamDestroy(P.stream);
@@ -108,6 +108,16 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   P.batch = batch;
   P.precision = prm->precision;
   P.restart = prm->restart > 0 ? prm->restart : 50;
+  P.restart_inner = prm->inner_restart > 0 ? prm->inner_restart : 40;
+  P.restart_max = std::max(P.restart, P.restart_inner);
+  P.inner_tol = prm->inner_tol > 0 ? prm->inner_tol : 1e-3;
+  if (P.precision == WG_PREC_MIXED) {
+    const std::string me = wg::mixed_check_shape(P.s);
+    if (!me.empty()) {
+      delete h;
+      return fail(nullptr, WG_ERR_ARG, "wg_problem_create: " + me);
+    }
+  }
   P.mem_budget = prm->mem_budget_bytes;
   const wg::Shape& s = P.s;
   const int nK = s.nK;
@@ -117,9 +127,11 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   P.nchunk = (int)std::min<long long>(128, std::max<long long>(1, (P.N + 2047) / 2048));
   const long long BN = P.N * batch;
   const int mp1 = P.restart + 1;
+  const int pst = P.restart_max + 1;
   // memory estimate before allocating (GmresMemoryLimit analogue)
   double est = 16.0 * BN * (5 + mp1) + 16.0 * 2 * s.nxi * P.ncols +
                8.0 * batch * s.n_el * nK * nK * (s.nxi + 1) + 16.0 * s.nxi * s.nk;
+  if (P.precision == WG_PREC_MIXED) est += wg::mixed_bytes(s, batch, P.restart_inner);
   if (P.mem_budget > 0 && est > P.mem_budget) {
     delete h;
     return fail(nullptr, WG_ERR_OOM,
@@ -165,15 +177,16 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.V, (size_t)BN * mp1, bytes));
   A(dalloc(&P.xh, (size_t)s.nxi * P.ncols, bytes));
   A(dalloc(&P.yh, (size_t)s.nxi * P.ncols, bytes));
-  A(dalloc(&P.H, (size_t)batch * mp1 * P.restart, bytes));
-  A(dalloc(&P.cs, (size_t)batch * P.restart, bytes));
-  A(dalloc(&P.sn, (size_t)batch * P.restart, bytes));
-  A(dalloc(&P.g, (size_t)batch * mp1, bytes));
-  A(dalloc(&P.hcol, (size_t)batch * mp1, bytes));
-  A(dalloc(&P.ycoef, (size_t)batch * P.restart, bytes));
-  A(dalloc(&P.partial, (size_t)batch * mp1 * P.nchunk, bytes));
+  A(dalloc(&P.H, (size_t)batch * pst * P.restart_max, bytes));
+  A(dalloc(&P.cs, (size_t)batch * P.restart_max, bytes));
+  A(dalloc(&P.sn, (size_t)batch * P.restart_max, bytes));
+  A(dalloc(&P.g, (size_t)batch * pst, bytes));
+  A(dalloc(&P.hcol, (size_t)batch * pst, bytes));
+  A(dalloc(&P.ycoef, (size_t)batch * P.restart_max, bytes));
+  A(dalloc(&P.partial, (size_t)batch * pst * P.nchunk, bytes));
   A(dalloc(&P.nrm_partial, (size_t)batch * P.nchunk, bytes));
   A(dalloc(&P.nrm, batch, bytes));
+  A(dalloc(&P.nrm_keep, batch, bytes));
   A(dalloc(&P.target, batch, bytes));
   A(dalloc(&P.active, batch, bytes));
   A(dalloc(&P.kused, batch, bytes));
@@ -236,6 +249,15 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   API_CK(&P, cudaMemsetAsync(P.x, 0, sizeof(double2) * BN, P.stream));
   API_CK(&P, cudaMemsetAsync(P.beta, 0, sizeof(double) * batch * s.n_el * nK * nK * (s.nxi + 1), P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
+  if (P.precision == WG_PREC_MIXED) {
+    const int mr = wg::mixed_alloc(P);
+    if (mr != WG_OK) {
+      std::string msg = "wg_problem_create: " + P.err;
+      free_all(P);
+      delete h;
+      return fail(nullptr, mr, msg);
+    }
+  }
   P.hp.resize(batch);
   P.h_nrm.resize(batch);
   P.h_active.resize(batch);
@@ -388,6 +410,21 @@ int wg_apply(wg_problem* h, const double* x, double* y) {
   return WG_OK;
 }
 
+int wg_apply_lowprec(wg_problem* h, const double* x, double* y) {
+  if (!h || !x || !y) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_apply_lowprec: null argument");
+  wg::Problem& P = h->P;
+  if (P.precision != WG_PREC_MIXED) return fail(&P, WG_ERR_ARG, "wg_apply_lowprec: handle is not mixed precision");
+  const long long n = P.N * P.batch;
+  API_CK(&P, cudaMemcpyAsync(P.z, x, sizeof(double2) * n, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, wg::apply_mixed_f64(P, P.z, P.w));
+  API_CK(&P, cudaMemcpyAsync(y, P.w, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  int herr = 0;
+  API_CK(&P, cudaMemcpy(&herr, P.mx.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) return fail(&P, WG_ERR_TIMEOUT, "wg_apply_lowprec: tensor-core GEMM barrier wait timed out");
+  return WG_OK;
+}
+
 int wg_precondition(wg_problem* h, const double* r, double* z) {
   if (!h || !r || !z) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_precondition: null argument");
   wg::Problem& P = h->P;
@@ -438,6 +475,14 @@ int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j) {
   if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_gummel_get: batch index out of range");
   const int rc = wg::gummel_get(P, b, phi, n_dg, j);
   if (rc) return fail(&P, rc, P.err);
+  return WG_OK;
+}
+
+int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K) {
+  if (!A || !B || !C) return fail(nullptr, WG_ERR_ARG, "wg_debug_gemm_bf16: null argument");
+  std::string err;
+  const int rc = wg::debug_gemm_bf16(A, B, C, M, N, K, err);
+  if (rc) return fail(nullptr, rc, "wg_debug_gemm_bf16: " + err);
   return WG_OK;
 }
 

@@ -1,0 +1,517 @@
+// Mixed-precision operator of the 1D Wigner solve (sm_103a).
+//
+// The complex plane-wave transforms become real BF16 GEMMs on the tensor cores:
+// with real and imaginary parts interleaved along K and M, a complex coefficient
+// c = a + ib acts as the 2x2 block [[a, -b], [b, a]], so the interleaved complex
+// state (column-major, Nk complex per DG node) IS the K-major B operand and the
+// FP32 accumulator, stored column-major, IS the interleaved complex result.
+//   GEMM 1: X^ (2 N_xi x ncols) = Phi'      (2 N_xi x 2 Nk) * x (2 Nk x ncols)
+//   GEMM 2: y  (2 Nk x ncols)  += (i Phi^H)' (2 Nk x 2 N_xi) * Y^ (2 N_xi x ncols)
+// The flux, the xi stencil and the k-line preconditioner run in FP32; the stencil
+// and the preconditioner write the BF16 GEMM operands directly.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "problem.h"
+#include "tc_gemm.cuh"
+
+namespace wg {
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+using bf162 = __nv_bfloat162;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// K-major bf16 operand of `rows` rows and K columns, 64 x box_rows boxes, 128-byte swizzle.
+bool make_map(CUtensorMap* m, const void* base, long long rows, int K, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+  cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)box_rows};
+  cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int EPI>
+cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, float* D, int M, long long Ncol, int K, int* err,
+                        cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc::gemm_bf16_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((M + tc::BM - 1) / tc::BM, (unsigned)((Ncol + tc::BN - 1) / tc::BN));
+  tc::gemm_bf16_kernel<EPI><<<grid, 128, tc::SMEM_BYTES, st>>>(a, b, D, M, Ncol, K, err);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP32 upwind flux (the FP64 flux_kernel in single precision).
+// ---------------------------------------------------------------------------
+template <int NK>
+__global__ void __launch_bounds__(256) flux32_kernel(const float2* __restrict__ x, float2* __restrict__ y,
+                                                     const double* __restrict__ kvec, const double* __restrict__ qd,
+                                                     FluxBlocks fb, int n_el, int nk, long long total) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int j = (int)(t % nk);
+  const long long be = t / nk;
+  const int e = (int)(be % n_el);
+  const int b = (int)(be / n_el);
+  const float k = (float)kvec[j], ak = fabsf(k);
+  const float s = (float)qd[b];
+  const float2* xe = x + be * (long long)NK * nk + j;
+  float2 xv[NK], acc[NK];
+#pragma unroll
+  for (int c = 0; c < NK; ++c) xv[c] = xe[(long long)c * nk];
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const float m = k * (float)fb.K1[a * NK + c] + ak * (float)fb.K2[a * NK + c];
+      v.x = fmaf(m, xv[c].x, v.x);
+      v.y = fmaf(m, xv[c].y, v.y);
+    }
+    acc[a] = v;
+  }
+  if (k > 0 && e > 0) {
+    const float2* xl = xe - (long long)NK * nk;
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const float2 xp = xl[(long long)c * nk];
+#pragma unroll
+      for (int a = 0; a < NK; ++a) {
+        const float m = (k + ak) * (float)fb.K3[a * NK + c];
+        acc[a].x = fmaf(m, xp.x, acc[a].x);
+        acc[a].y = fmaf(m, xp.y, acc[a].y);
+      }
+    }
+  } else if (k < 0 && e < n_el - 1) {
+    const float2* xr = xe + (long long)NK * nk;
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const float2 xp = xr[(long long)c * nk];
+#pragma unroll
+      for (int a = 0; a < NK; ++a) {
+        const float m = (k - ak) * (float)fb.K5[a * NK + c];
+        acc[a].x = fmaf(m, xp.x, acc[a].x);
+        acc[a].y = fmaf(m, xp.y, acc[a].y);
+      }
+    }
+  }
+  float2* ye = y + be * (long long)NK * nk + j;
+#pragma unroll
+  for (int a = 0; a < NK; ++a) ye[(long long)a * nk] = make_float2(s * acc[a].x, s * acc[a].y);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 xi stencil, output as the BF16 B operand of GEMM 2.
+// ---------------------------------------------------------------------------
+template <int NK>
+__global__ void __launch_bounds__(256) stencil32_kernel(const float2* __restrict__ xh, bf162* __restrict__ yh,
+                                                        const float* __restrict__ betar,
+                                                        const float* __restrict__ betai, int nxi,
+                                                        long long nelem_batch) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nelem_batch * nxi) return;
+  const int s = (int)(t % nxi);
+  const long long be = t / nxi;
+  const int ne = nxi + 1;
+  const float2* X = xh + be * NK * (long long)nxi;
+  float2 sm[NK], sp[NK];
+#pragma unroll
+  for (int c = 0; c < NK; ++c) {
+    const float2 x0 = X[(long long)c * nxi + s];
+    const float2 xm = s > 0 ? X[(long long)c * nxi + s - 1] : make_float2(0.f, 0.f);
+    const float2 xp = s < nxi - 1 ? X[(long long)c * nxi + s + 1] : make_float2(0.f, 0.f);
+    sm[c] = make_float2(x0.x + xm.x, x0.y + xm.y);
+    sp[c] = make_float2(x0.x + xp.x, x0.y + xp.y);
+  }
+  const float* br = betar + be * (long long)NK * NK * ne;
+  bf162* Y = yh + be * NK * (long long)nxi;
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    float vx = 0.f, vy = 0.f;
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const int ac = a * NK + c;
+      const float b0r = br[(long long)ac * ne + s], b0i = betai[ac * ne + s];
+      const float b1r = br[(long long)ac * ne + s + 1], b1i = betai[ac * ne + s + 1];
+      vx += b0r * sm[c].x - b0i * sm[c].y + b1r * sp[c].x - b1i * sp[c].y;
+      vy += b0r * sm[c].y + b0i * sm[c].x + b1r * sp[c].y + b1i * sp[c].x;
+    }
+    Y[(long long)a * nxi + s] = __floats2bfloat162_rn(vx, vy);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP32 k-line preconditioner (same chunked affine scan as the FP64 kernel);
+// writes z in FP32 and, optionally, its BF16 copy for GEMM 1.
+// ---------------------------------------------------------------------------
+template <int NK>
+__global__ void precond32_kernel(const float2* __restrict__ r, float2* __restrict__ z, bf162* __restrict__ zb,
+                                 const double* __restrict__ kvec, const double* __restrict__ dinv,
+                                 const double* __restrict__ hvec, const double* __restrict__ qd, int n_el, int nk,
+                                 long long N, long long r_stride) {
+  extern __shared__ float2 shf[];  // [2][P][32]
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int P = blockDim.x >> 5;
+  const int j = blockIdx.x * 32 + lane;
+  const int b = blockIdx.y;
+  const bool valid = j < nk;
+  const int chunk = (n_el + P - 1) / P;
+  const int e_lo = min(n_el, w * chunk), e_hi = min(n_el, (w + 1) * chunk);
+  float D[NK * NK], h[NK];
+  bool fwd = true;
+  float inv_qd = 1.f;
+#pragma unroll
+  for (int i = 0; i < NK * NK; ++i) D[i] = valid ? (float)dinv[j * NK * NK + i] : 0.f;
+#pragma unroll
+  for (int i = 0; i < NK; ++i) h[i] = valid ? (float)hvec[j * NK + i] : 0.f;
+  if (valid) {
+    fwd = kvec[j] > 0;
+    inv_qd = (float)(1.0 / qd[b]);
+  }
+  // row `st` of D and h[st] without dynamic register indexing
+  float Dst[NK];
+  float hst = 0.f;
+#pragma unroll
+  for (int c = 0; c < NK; ++c) Dst[c] = fwd ? D[(NK - 1) * NK + c] : D[c];
+  hst = fwd ? h[NK - 1] : h[0];
+  const float alpha = valid ? -hst : 0.f;
+  const float2* rb = r + (long long)b * r_stride + j;
+  const long long zoff = (long long)b * N + j;
+  const int len = e_hi - e_lo;
+  float2 s = make_float2(0.f, 0.f);
+  float Amul = 1.f;
+  if (valid) {
+    for (int i = 0; i < len; ++i) {
+      const int e = fwd ? e_lo + i : e_hi - 1 - i;
+      const float2* re = rb + (long long)e * NK * nk;
+      float ux = 0.f, uy = 0.f;
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        const float2 rv = re[(long long)c * nk];
+        ux = fmaf(Dst[c], rv.x, ux);
+        uy = fmaf(Dst[c], rv.y, uy);
+      }
+      s = make_float2(ux * inv_qd + alpha * s.x, uy * inv_qd + alpha * s.y);
+      Amul *= alpha;
+    }
+  }
+  shf[(0 * P + w) * 32 + lane] = make_float2(Amul, 0.f);
+  shf[(1 * P + w) * 32 + lane] = s;
+  __syncthreads();
+  if (w == 0 && valid) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < P; ++c) {
+      const int cc = fwd ? c : P - 1 - c;
+      const float a = shf[(0 * P + cc) * 32 + lane].x;
+      const float2 bb = shf[(1 * P + cc) * 32 + lane];
+      shf[(1 * P + cc) * 32 + lane] = acc;
+      acc = make_float2(a * acc.x + bb.x, a * acc.y + bb.y);
+    }
+  }
+  __syncthreads();
+  if (!valid) return;
+  s = shf[(1 * P + w) * 32 + lane];
+  for (int i = 0; i < len; ++i) {
+    const int e = fwd ? e_lo + i : e_hi - 1 - i;
+    const float2* re = rb + (long long)e * NK * nk;
+    float2 rv[NK];
+#pragma unroll
+    for (int c = 0; c < NK; ++c) rv[c] = re[(long long)c * nk];
+    float2 snew = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      float ux = 0.f, uy = 0.f;
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        ux = fmaf(D[a * NK + c], rv[c].x, ux);
+        uy = fmaf(D[a * NK + c], rv[c].y, uy);
+      }
+      const float2 zv = make_float2(ux * inv_qd - h[a] * s.x, uy * inv_qd - h[a] * s.y);
+      const long long o = zoff + (long long)(e * NK + a) * nk;
+      z[o] = zv;
+      if (zb) zb[o] = __floats2bfloat162_rn(zv.x, zv.y);
+      if ((fwd && a == NK - 1) || (!fwd && a == 0)) snew = zv;
+    }
+    s = snew;
+  }
+}
+
+__global__ void to_bf16_kernel(const float2* __restrict__ x, bf162* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) {
+    const float2 v = x[t];
+    y[t] = __floats2bfloat162_rn(v.x, v.y);
+  }
+}
+
+__global__ void c2f_kernel(const double2* __restrict__ x, float2* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = make_float2((float)x[t].x, (float)x[t].y);
+}
+
+__global__ void f2c_kernel(const float2* __restrict__ x, double2* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = make_double2(x[t].x, x[t].y);
+}
+
+__global__ void d2f_kernel(const double* __restrict__ x, float* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = (float)x[t];
+}
+
+template <int NK>
+cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2* y) {
+  MixedBuffers& M = P.mx;
+  if (xb && xb != M.xin16 && xb != M.zb16) return cudaErrorInvalidValue;
+  const Shape& s = P.s;
+  const long long total = (long long)P.batch * s.n_el * s.nk;
+  const long long BN = P.N * P.batch;
+  if (!xb) {
+    to_bf16_kernel<<<(unsigned)((BN + 255) / 256), 256, 0, P.stream>>>(x, M.xin16, BN);
+    xb = M.xin16;
+    P.prof.launches[PROF_OTHER] += 1;
+  }
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX);
+  flux32_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, s.n_el, s.nk,
+                                                                            total);
+  prof_end(P, PROF_FLUX, ev);
+  ev = prof_begin(P, PROF_GEMM_FWD);
+  // GEMM 1 reads its B operand through the tensor map of whichever bf16 buffer holds x
+  cudaError_t e = launch_gemm<0>(M.tmA1, xb == M.xin16 ? M.tmB1 : M.tmB1z, reinterpret_cast<float*>(M.xh), 2 * s.nxi,
+                                 P.ncols, 2 * s.nk, M.err, P.stream);
+  prof_end(P, PROF_GEMM_FWD, ev);
+  if (e != cudaSuccess) return e;
+  const long long nelem = (long long)P.batch * s.n_el;
+  ev = prof_begin(P, PROF_STENCIL);
+  stencil32_kernel<NK><<<(unsigned)((nelem * s.nxi + 255) / 256), 256, 0, P.stream>>>(
+      reinterpret_cast<const float2*>(M.xh), M.yh16, M.beta, M.betai, s.nxi, nelem);
+  prof_end(P, PROF_STENCIL, ev);
+  ev = prof_begin(P, PROF_GEMM_BWD);
+  e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream);
+  prof_end(P, PROF_GEMM_BWD, ev);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+template <int NK>
+cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb) {
+  const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
+  dim3 grid((P.s.nk + 31) / 32, P.batch);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND);
+  precond32_kernel<NK><<<grid, 32 * Pw, sizeof(float2) * 2 * Pw * 32, P.stream>>>(
+      r, z, zb, P.kvec, P.pre_dinv, P.pre_h, P.qd, P.s.n_el, P.s.nk, P.N, r_stride);
+  prof_end(P, PROF_PRECOND, ev);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+std::string mixed_check_shape(const Shape& s) {
+  if (s.nk % 4 || s.nxi % 4) return "the mixed form needs Nk and N_xi divisible by 4 (16-byte TMA rows)";
+  if (s.nk < 32 || s.nxi < 32) return "the mixed form needs Nk, N_xi >= 32 (one 64-wide BF16 K block)";
+  return "";
+}
+
+double mixed_bytes(const Shape& s, int batch, int restart) {
+  const double BN = (double)s.n_el * s.nK * s.nk * batch;
+  const double ncols = (double)batch * s.n_el * s.nK;
+  return 2.0 * 2 * (4.0 * s.nxi * s.nk) + 4.0 * BN + 8.0 * ncols * s.nxi + 4.0 * ncols * s.nxi +
+         8.0 * BN * (restart + 1 + 4) + 4.0 * batch * s.n_el * s.nK * s.nK * (s.nxi + 1);
+}
+
+int mixed_alloc(Problem& P) {
+  MixedBuffers& M = P.mx;
+  const Shape& s = P.s;
+  const long long BN = P.N * P.batch;
+  const int mp1 = P.restart_inner + 1;
+  double bytes = 0;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](cudaError_t r) { if (e == cudaSuccess) e = r; };
+  auto alloc = [&](void** p, size_t n) { bytes += (double)n; A(cudaMalloc(p, n)); };
+  alloc((void**)&M.phi1, sizeof(bf16) * 4 * (size_t)s.nxi * s.nk);
+  alloc((void**)&M.phi2, sizeof(bf16) * 4 * (size_t)s.nxi * s.nk);
+  alloc((void**)&M.xin16, sizeof(bf162) * BN);
+  alloc((void**)&M.zb16, sizeof(bf162) * BN);
+  alloc((void**)&M.yh16, sizeof(bf162) * (size_t)s.nxi * P.ncols);
+  alloc((void**)&M.xh, sizeof(float2) * (size_t)s.nxi * P.ncols);
+  alloc((void**)&M.V, sizeof(float2) * BN * mp1);
+  alloc((void**)&M.w, sizeof(float2) * BN);
+  alloc((void**)&M.z, sizeof(float2) * BN);
+  alloc((void**)&M.r, sizeof(float2) * BN);
+  alloc((void**)&M.d, sizeof(float2) * BN);
+  alloc((void**)&M.beta, sizeof(float) * (size_t)P.batch * s.n_el * s.nK * s.nK * (s.nxi + 1));
+  alloc((void**)&M.betai, sizeof(float) * (size_t)s.nK * s.nK * (s.nxi + 1));
+  alloc((void**)&M.err, sizeof(int));
+  if (e != cudaSuccess) {
+    P.err = std::string("mixed-precision buffers: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
+  }
+  P.device_bytes += bytes;
+  cudaMemsetAsync(M.err, 0, sizeof(int), P.stream);
+  // BF16 real embeddings of Phi (GEMM 1) and i Phi^H (GEMM 2), interleaved (re, im) along both axes
+  const int nxi = s.nxi, nk = s.nk;
+  std::vector<bf16> a1((size_t)4 * nxi * nk), a2((size_t)4 * nxi * nk);
+  for (int si = 0; si < nxi; ++si)
+    for (int j = 0; j < nk; ++j) {
+      const double pr = s.phi[(size_t)si * nk + j].real(), pi = s.phi[(size_t)si * nk + j].imag();
+      // GEMM 1 row 2s+o, column 2j+c: [[pr, -pi], [pi, pr]]
+      const size_t K1 = 2 * (size_t)nk;
+      a1[(2 * si + 0) * K1 + 2 * j + 0] = __float2bfloat16((float)pr);
+      a1[(2 * si + 0) * K1 + 2 * j + 1] = __float2bfloat16((float)-pi);
+      a1[(2 * si + 1) * K1 + 2 * j + 0] = __float2bfloat16((float)pi);
+      a1[(2 * si + 1) * K1 + 2 * j + 1] = __float2bfloat16((float)pr);
+      // GEMM 2: i conj(Phi(s,j)) = pi + i pr -> row 2j+o, column 2s+c: [[pi, -pr], [pr, pi]]
+      const size_t K2 = 2 * (size_t)nxi;
+      a2[(2 * j + 0) * K2 + 2 * si + 0] = __float2bfloat16((float)pi);
+      a2[(2 * j + 0) * K2 + 2 * si + 1] = __float2bfloat16((float)-pr);
+      a2[(2 * j + 1) * K2 + 2 * si + 0] = __float2bfloat16((float)pr);
+      a2[(2 * j + 1) * K2 + 2 * si + 1] = __float2bfloat16((float)pi);
+    }
+  e = cudaMemcpyAsync(M.phi1, a1.data(), sizeof(bf16) * a1.size(), cudaMemcpyHostToDevice, P.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(M.phi2, a2.data(), sizeof(bf16) * a2.size(), cudaMemcpyHostToDevice, P.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P.stream);
+  if (e != cudaSuccess) {
+    P.err = std::string("mixed-precision set-up: ") + cudaGetErrorString(e);
+    return WG_ERR_CUDA;
+  }
+  bool ok = make_map(&M.tmA1, M.phi1, 2 * nxi, 2 * nk, tc::BM) && make_map(&M.tmB1, M.xin16, P.ncols, 2 * nk, tc::BN) &&
+            make_map(&M.tmB1z, M.zb16, P.ncols, 2 * nk, tc::BN) && make_map(&M.tmA2, M.phi2, 2 * nk, 2 * nxi, tc::BM) &&
+            make_map(&M.tmB2, M.yh16, P.ncols, 2 * nxi, tc::BN);
+  if (!ok) {
+    P.err = "cuTensorMapEncodeTiled failed for the BF16 GEMM operands";
+    return WG_ERR_CUDA;
+  }
+  return WG_OK;
+}
+
+void mixed_free(Problem& P) {
+  MixedBuffers& M = P.mx;
+  void* ptrs[] = {M.phi1, M.phi2, M.xin16, M.zb16, M.yh16, M.xh, M.V, M.w, M.z, M.r, M.d, M.beta, M.betai, M.err};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  M = MixedBuffers{};
+}
+
+// FP32 copies of the potential weights after every potential update.
+cudaError_t mixed_sync_weights(Problem& P) {
+  const Shape& s = P.s;
+  const long long nb = (long long)P.batch * s.n_el * s.nK * s.nK * (s.nxi + 1);
+  const long long ni = (long long)s.nK * s.nK * (s.nxi + 1);
+  P.prof.launches[PROF_OTHER] += 2;
+  d2f_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, P.stream>>>(P.beta, P.mx.beta, nb);
+  d2f_kernel<<<(unsigned)((ni + 255) / 256), 256, 0, P.stream>>>(P.betai, P.mx.betai, ni);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y) {
+  switch (P.s.nK) {
+    case 2: return apply_mixed_nk<2>(P, x, xb, y);
+    case 3: return apply_mixed_nk<3>(P, x, xb, y);
+    default: return apply_mixed_nk<4>(P, x, xb, y);
+  }
+}
+
+// y = A_lo x for FP64 device vectors (conversion, mixed apply, conversion back).
+cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y) {
+  const long long n = P.N * P.batch;
+  cudaError_t e = mixed_sync_weights(P);
+  if (e != cudaSuccess) return e;
+  c2f_kernel<<<(unsigned)((n + 255) / 256), 256, 0, P.stream>>>(x, P.mx.z, n);
+  e = launch_apply_mixed(P, P.mx.z, nullptr, P.mx.w);
+  if (e != cudaSuccess) return e;
+  f2c_kernel<<<(unsigned)((n + 255) / 256), 256, 0, P.stream>>>(P.mx.w, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
+                                      __nv_bfloat162* zb) {
+  switch (P.s.nK) {
+    case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb);
+    case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb);
+    default: return precond_mixed_nk<4>(P, r, r_stride, z, zb);
+  }
+}
+
+// Stand-alone BF16 GEMM for diagnostics: C = bf16(A) bf16(B), A row-major M x K,
+// B column-major K x N, C column-major M x N (fp32 host buffers).
+int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err) {
+  if (M < 1 || N < 1 || K < 64 || K % 8) {
+    err = "debug GEMM needs K >= 64 and K % 8 == 0";
+    return WG_ERR_ARG;
+  }
+  std::vector<bf16> ha((size_t)M * K), hb((size_t)N * K);
+  for (size_t i = 0; i < ha.size(); ++i) ha[i] = __float2bfloat16(A[i]);
+  for (size_t i = 0; i < hb.size(); ++i) hb[i] = __float2bfloat16(B[i]);
+  bf16 *da = nullptr, *db = nullptr;
+  float* dc = nullptr;
+  int* derr = nullptr;
+  cudaError_t e = cudaMalloc(&da, ha.size() * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&db, hb.size() * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&dc, (size_t)M * N * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&derr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(da, ha.data(), ha.size() * sizeof(bf16), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(db, hb.data(), hb.size() * sizeof(bf16), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(dc, 0, (size_t)M * N * sizeof(float));
+  CUtensorMap ma, mb;
+  int rc = WG_OK;
+  if (e == cudaSuccess) {
+    if (!make_map(&ma, da, M, K, tc::BM) || !make_map(&mb, db, N, K, tc::BN)) {
+      err = "cuTensorMapEncodeTiled failed";
+      rc = WG_ERR_CUDA;
+    } else {
+      e = launch_gemm<0>(ma, mb, dc, M, N, K, derr, 0);
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      int herr = 0;
+      if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(C, dc, (size_t)M * N * sizeof(float), cudaMemcpyDeviceToHost);
+      if (herr) {
+        err = "GEMM barrier wait timed out";
+        rc = WG_ERR_TIMEOUT;
+      }
+    }
+  }
+  if (e != cudaSuccess) {
+    err = std::string("CUDA: ") + cudaGetErrorString(e);
+    rc = WG_ERR_CUDA;
+  }
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dc);
+  cudaFree(derr);
+  return rc;
+}
+
+}  // namespace wg

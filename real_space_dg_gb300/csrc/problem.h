@@ -1,5 +1,7 @@
 // Device-side state of a wg_problem handle (internal header).
 #pragma once
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -34,14 +36,21 @@ struct HostProblem {
 
 // Device buffers of the mixed-precision inner solver (allocated only for WG_PREC_MIXED).
 struct MixedBuffers {
-  void* phi16 = nullptr;     // bf16 operand planes of Phi / Phi^H (layout owned by mixed.cu)
-  void* xin16 = nullptr;     // bf16 staging of the GEMM B operands
-  float* V = nullptr;        // fp32 Krylov basis [B][m+1][2N]
-  float* w = nullptr;        // fp32 work vectors
-  float* z = nullptr;
-  float* xh = nullptr;
-  float* yh = nullptr;
-  float* beta = nullptr;     // fp32 copy of the potential weights
+  __nv_bfloat16* phi1 = nullptr;     // [2 N_xi][2 Nk]  real embedding of Phi (GEMM 1 A operand)
+  __nv_bfloat16* phi2 = nullptr;     // [2 Nk][2 N_xi]  real embedding of i Phi^H (GEMM 2 A operand)
+  __nv_bfloat162* xin16 = nullptr;   // [B*N] bf16 staging of a GEMM 1 B operand
+  __nv_bfloat162* zb16 = nullptr;    // [B*N] bf16 copy of the preconditioned vector
+  __nv_bfloat162* yh16 = nullptr;    // [ncols][N_xi] bf16 stencil output (GEMM 2 B operand)
+  float2* xh = nullptr;              // [ncols][N_xi] fp32 GEMM 1 output
+  float2* V = nullptr;               // [B][m_inner+1][N] fp32 Krylov basis
+  float2* w = nullptr;               // [B*N]
+  float2* z = nullptr;               // [B*N]
+  float2* r = nullptr;               // [B*N] normalised outer residual
+  float2* d = nullptr;               // [B*N] inner correction
+  float* beta = nullptr;             // fp32 copy of the potential weights
+  float* betai = nullptr;
+  int* err = nullptr;                // raised by a GEMM whose barrier wait timed out
+  CUtensorMap tmA1, tmB1, tmB1z, tmA2, tmB2;
 };
 
 // Kernel classes timed and counted by the profiler.
@@ -97,6 +106,9 @@ struct Problem {
   int batch = 0;
   int precision = WG_PREC_FP64;
   int restart = 50;
+  int restart_inner = 40;   // inner GMRES length of the mixed form
+  int restart_max = 50;     // sizes the Hessenberg storage: max(restart, restart_inner)
+  double inner_tol = 1e-3;  // floor of the inner relative tolerance of the mixed form
   long long N = 0;          // complex entries per problem
   long long ncols = 0;      // DG nodes in the batch = batch * n_el * nK
   double device_bytes = 0;
@@ -146,6 +158,7 @@ struct Problem {
   double2* partial = nullptr;    // [B][m+1][nchunk]
   double* nrm_partial = nullptr; // [B][nchunk]
   double* nrm = nullptr;         // [B]
+  double* nrm_keep = nullptr;    // [B] outer residual norms of the mixed refinement
   double* target = nullptr;      // [B] absolute residual targets
   int* active = nullptr;         // [B] 1 while iterating in this cycle
   int* kused = nullptr;          // [B] iterations used in this cycle
@@ -178,6 +191,18 @@ cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j);
 cudaError_t launch_rho_xi(Problem& P, int b, double2* out);
 // Krylov (gmres.cu)
 int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
+// Mixed form (mixed.cu)
+std::string mixed_check_shape(const Shape& s);
+double mixed_bytes(const Shape& s, int batch, int restart);
+int mixed_alloc(Problem& P);
+void mixed_free(Problem& P);
+cudaError_t mixed_sync_weights(Problem& P);
+cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y);
+cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
+                                      __nv_bfloat162* zb);
+cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);
+int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err);
+int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // FP64 GMRES or the mixed-precision refinement, by P.precision.
 int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // Gummel loop (gummel.cu)

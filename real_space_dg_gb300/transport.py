@@ -28,11 +28,11 @@ class Problem1D:
     """
 
     def __init__(self, n_el, n_local, nk, n_xi=None, l_xi=30e-9, batch=1, precision="fp64", restart=50,
-                 m_diff=0.0, mpc=1.0, mem_budget_bytes=0.0):
+                 m_diff=0.0, mpc=1.0, mem_budget_bytes=0.0, inner_restart=0, inner_tol=0.0):
         self.lib = _lib.load()
         prm = _lib.WgParams(int(n_el), int(n_local), int(nk), int(n_xi or nk), float(l_xi), float(m_diff),
                             float(mpc), PRECISIONS[precision] if isinstance(precision, str) else int(precision),
-                            int(restart), float(mem_budget_bytes))
+                            int(restart), float(mem_budget_bytes), int(inner_restart), float(inner_tol))
         h = C.c_void_p()
         st = self.lib.wg_problem_create(C.byref(prm), int(batch), C.byref(h))
         if st != _lib.WG_OK:
@@ -117,6 +117,14 @@ class Problem1D:
         y = np.empty_like(x)
         self._check(self.lib.wg_apply(self.h, x.view(np.float64).ctypes.data_as(_lib._D),
                                       y.view(np.float64).ctypes.data_as(_lib._D)))
+        return y
+
+    def apply_lowprec(self, x):
+        """The mixed form's inner operator (BF16 tensor-core transforms, FP32 flux)."""
+        x = _lib.as_c128(x).reshape(-1)
+        y = np.empty_like(x)
+        self._check(self.lib.wg_apply_lowprec(self.h, x.view(np.float64).ctypes.data_as(_lib._D),
+                                              y.view(np.float64).ctypes.data_as(_lib._D)))
         return y
 
     def precondition(self, r):
