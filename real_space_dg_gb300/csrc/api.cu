@@ -48,7 +48,7 @@ void free_all(wg::Problem& P) {
   wg::gummel_free(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
-                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.target, P.active, P.kused, P.any_active};
+                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.kused, P.any_active};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P.stream) cudaStreamDestroy(P.stream);
@@ -111,6 +111,10 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   P.restart_inner = prm->inner_restart > 0 ? prm->inner_restart : 40;
   P.restart_max = std::max(P.restart, P.restart_inner);
   P.inner_tol = prm->inner_tol > 0 ? prm->inner_tol : 1e-3;
+  if (P.restart_max > 256) {
+    delete h;
+    return fail(nullptr, WG_ERR_ARG, "wg_problem_create: restart lengths must be <= 256");
+  }
   if (P.precision == WG_PREC_MIXED) {
     const std::string me = wg::mixed_check_shape(P.s);
     if (!me.empty()) {
@@ -124,7 +128,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   P.N = (long long)s.n_el * nK * s.nk;
   P.ncols = (long long)batch * s.n_el * nK;
   P.nx = s.n_el * (nK - 1) + 1;
-  P.nchunk = (int)std::min<long long>(128, std::max<long long>(1, (P.N + 2047) / 2048));
+  P.nchunk = (int)std::max<long long>(1, (P.N + 2047) / 2048);
+  P.nblk = (int)std::max<long long>(1, (P.N + 255) / 256);
   const long long BN = P.N * batch;
   const int mp1 = P.restart + 1;
   const int pst = P.restart_max + 1;
@@ -184,9 +189,10 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.hcol, (size_t)batch * pst, bytes));
   A(dalloc(&P.ycoef, (size_t)batch * P.restart_max, bytes));
   A(dalloc(&P.partial, (size_t)batch * pst * P.nchunk, bytes));
-  A(dalloc(&P.nrm_partial, (size_t)batch * P.nchunk, bytes));
+  A(dalloc(&P.nrm_partial, (size_t)batch * std::max(P.nchunk, P.nblk), bytes));
   A(dalloc(&P.nrm, batch, bytes));
   A(dalloc(&P.nrm_keep, batch, bytes));
+  A(dalloc(&P.inv64, batch, bytes));
   A(dalloc(&P.target, batch, bytes));
   A(dalloc(&P.active, batch, bytes));
   A(dalloc(&P.kused, batch, bytes));

@@ -14,8 +14,8 @@
 //  - gmres_solve_mixed: FP64 iterative refinement.  The outer residual
 //    r = b - A x is FP64; each correction solves A d = r/|r| with one GMRES cycle
 //    whose basis is FP32 and whose operator runs the BF16 tensor-core transforms
-//    and the FP32 flux / preconditioner.  Inner products, norms, Givens rotations
-//    and the Hessenberg solve stay FP64.
+//    and the FP32 flux / preconditioner.  Inner products and norms are combined
+//    in FP64 (see AccF32), Givens rotations and the Hessenberg solve are FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,6 +36,76 @@ __device__ __forceinline__ void st2(float2& d, double2 v) { d = make_float2((flo
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
+
+// Inner-product accumulators.  FP64 vectors accumulate in FP64.  FP32 basis
+// vectors (mixed form) multiply and add in FP32 within a thread's run of kMdE
+// elements (at most 16 terms), then the runs are combined exactly in double-float
+// arithmetic across the warp (TwoSum on the FP32 pipes) and in FP64 across warps,
+// blocks and chunks.  The result carries ~1e-6 relative error with respect to
+// sum |a_i b_i|, below the rounding of the FP32 basis itself; a fully error-free
+// per-element scheme (Dot2) measured at a third of the HBM rate on GB300, whose
+// FP64 rate is too low to accumulate per element.
+struct Acc64 {
+  double2 v = make_double2(0.0, 0.0);
+  __device__ __forceinline__ void add_cdot(const double2& a, const double2& x) {  // += conj(a) x
+    v.x += a.x * x.x + a.y * x.y;
+    v.y += a.x * x.y - a.y * x.x;
+  }
+  __device__ __forceinline__ void add_norm(const double2& a) { v.x += a.x * a.x + a.y * a.y; }
+  __device__ __forceinline__ void warp_reduce() {
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+  }
+  __device__ __forceinline__ double2 get() const { return v; }
+};
+
+struct AccF32 {
+  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;   // (hi, lo) pairs after warp_reduce
+  __device__ __forceinline__ void add_cdot(const float2& a, const float2& x) {
+    rh = fmaf(a.x, x.x, fmaf(a.y, x.y, rh));
+    ih = fmaf(a.x, x.y, fmaf(-a.y, x.x, ih));
+  }
+  __device__ __forceinline__ void add_norm(const float2& a) { rh = fmaf(a.x, a.x, fmaf(a.y, a.y, rh)); }
+  // (hi, lo) += (bh, bl) in double-float arithmetic (TwoSum, then renormalise).
+  __device__ __forceinline__ static void merge(float& hi, float& lo, float bh, float bl) {
+    const float s = __fadd_rn(hi, bh);
+    const float bb = __fsub_rn(s, hi);
+    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
+    e = __fadd_rn(e, __fadd_rn(lo, bl));
+    hi = __fadd_rn(s, e);
+    lo = __fsub_rn(e, __fsub_rn(hi, s));
+  }
+  __device__ __forceinline__ void warp_reduce() {
+    for (int o = 16; o > 0; o >>= 1) {
+      const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
+      const float c = __shfl_xor_sync(0xffffffffu, ih, o), d = __shfl_xor_sync(0xffffffffu, il, o);
+      merge(rh, rl, a, b);
+      merge(ih, il, c, d);
+    }
+  }
+  __device__ __forceinline__ double2 get() const {
+    return make_double2((double)rh + (double)rl, (double)ih + (double)il);
+  }
+};
+
+template <typename T> struct AccFor;
+template <> struct AccFor<double2> { using type = Acc64; };
+template <> struct AccFor<float2> { using type = AccF32; };
+
+// Complex multiply-subtract in the vector's own precision: w -= v h.
+__device__ __forceinline__ void cms(double2& w, const double2& v, const double2& h) {
+  w.x -= v.x * h.x - v.y * h.y;
+  w.y -= v.x * h.y + v.y * h.x;
+}
+__device__ __forceinline__ void cms(float2& w, const float2& v, const float2& h) {
+  w.x = fmaf(-v.x, h.x, fmaf(v.y, h.y, w.x));
+  w.y = fmaf(-v.x, h.y, fmaf(-v.y, h.x, w.y));
+}
+template <typename T> __device__ __forceinline__ T from2(double2 v);
+template <> __device__ __forceinline__ double2 from2<double2>(double2 v) { return v; }
+template <> __device__ __forceinline__ float2 from2<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
@@ -76,29 +146,55 @@ __device__ double block_sum1(double v) {
   return r;
 }
 
-// partial[b][i][c] = sum over chunk c of conj(V_i) . w     grid (nchunk, nv, B)
+// Multi-dot: partial[b][i][c] = sum over chunk c of conj(V_i) . w for every i < nv.
+// One block per (chunk of 256*E elements, problem): w stays in registers, each V_i
+// chunk is read once, warps drop their partial sums in shared memory and the
+// block adds them at the end (no block barrier per coefficient).
+constexpr int kMdE = 8;
 template <typename T>
-__global__ void __launch_bounds__(256) dot_partial_kernel(const T* __restrict__ V, const T* __restrict__ w,
-                                                          double2* __restrict__ partial, const int* __restrict__ active,
-                                                          long long N, int mp1, int pstride, int nchunk) {
-  const int b = blockIdx.z, i = blockIdx.y, c = blockIdx.x;
+__global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, const T* __restrict__ w,
+                                                       double2* __restrict__ partial, const int* __restrict__ active,
+                                                       long long N, int nv, int mp1, int pstride, int nchunk) {
+  extern __shared__ double2 red[];  // [nv][8]
+  const int b = blockIdx.y, c = blockIdx.x;
   if (!active[b]) return;
-  const T* v = V + ((long long)b * mp1 + i) * N;
-  const T* ww = w + (long long)b * N;
-  double2 acc = make_double2(0, 0);
-  for (long long n = (long long)c * 256 + threadIdx.x; n < N; n += (long long)nchunk * 256) {
-    const double2 a = ld2(v[n]), x = ld2(ww[n]);
-    acc.x += a.x * x.x + a.y * x.y;
-    acc.y += a.x * x.y - a.y * x.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long base = (long long)c * 256 * kMdE + threadIdx.x;
+  const T* wb = w + (long long)b * N;
+  T wv[kMdE];
+#pragma unroll
+  for (int j = 0; j < kMdE; ++j) {
+    const long long n = base + (long long)j * 256;
+    if (n < N) wv[j] = wb[n];
+    else { wv[j].x = 0; wv[j].y = 0; }
   }
-  acc = block_sum2(acc);
-  if (threadIdx.x == 0) partial[((long long)b * pstride + i) * nchunk + c] = acc;
+  for (int i = 0; i < nv; ++i) {
+    const T* v = V + ((long long)b * mp1 + i) * N;
+    typename AccFor<T>::type a;
+#pragma unroll
+    for (int j = 0; j < kMdE; ++j) {
+      const long long n = base + (long long)j * 256;
+      if (n < N) a.add_cdot(v[n], wv[j]);
+    }
+    a.warp_reduce();
+    if (lane == 0) red[i * 8 + warp] = a.get();
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+    double2 s = make_double2(0, 0);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      s.x += red[i * 8 + q].x;
+      s.y += red[i * 8 + q].y;
+    }
+    partial[((long long)b * pstride + i) * nchunk + c] = s;
+  }
 }
 
 // hcol[b][i] = sum_c partial; H[b][k][i] (+)= hcol          grid (B), block 256
 __global__ void dot_reduce_kernel(const double2* __restrict__ partial, double2* __restrict__ hcol,
-                                  double2* __restrict__ H, const int* __restrict__ active, int nv, int k, int pstride,
-                                  int m, int nchunk, int first) {
+                                  float2* __restrict__ hcol32, double2* __restrict__ H, const int* __restrict__ active,
+                                  int nv, int k, int pstride, int m, int nchunk, int first) {
   const int b = blockIdx.x;
   if (!active[b]) return;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -113,6 +209,7 @@ __global__ void dot_reduce_kernel(const double2* __restrict__ partial, double2* 
     acc.y = warp_sum(acc.y);
     if (lane == 0) {
       hcol[b * pstride + i] = acc;
+      if (hcol32) hcol32[b * pstride + i] = make_float2((float)acc.x, (float)acc.y);
       double2* h = H + (long long)b * pstride * m + (long long)k * pstride + i;
       if (first) *h = acc;
       else { h->x += acc.x; h->y += acc.y; }
@@ -120,25 +217,36 @@ __global__ void dot_reduce_kernel(const double2* __restrict__ partial, double2* 
   }
 }
 
-// w -= sum_i V_i hcol_i
-template <typename T>
+// w -= sum_i V_i hcol_i; with NORM, also nrm_partial[b][blockIdx.x] = sum |w|^2 of the block.
+// Grid (ceil(N/256), B).
+template <typename T, bool NORM>
 __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V, T* __restrict__ w,
-                                                        const double2* __restrict__ hcol, const int* __restrict__ active,
-                                                        long long N, int nv, int mp1, int pstride, int batch) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= N * batch) return;
-  const int b = (int)(t / N);
+                                                        const T* __restrict__ hcol, const int* __restrict__ active,
+                                                        double* __restrict__ nrm_partial, long long N, int nv, int mp1,
+                                                        int pstride, int nblk) {
+  const int b = blockIdx.y;
   if (!active[b]) return;
-  const long long n = t - (long long)b * N;
-  double2 acc = ld2(w[t]);
-  const T* v = V + (long long)b * mp1 * N + n;
-  for (int i = 0; i < nv; ++i) {
-    const double2 h = hcol[b * pstride + i];
-    const double2 vi = ld2(v[(long long)i * N]);
-    acc.x -= vi.x * h.x - vi.y * h.y;
-    acc.y -= vi.x * h.y + vi.y * h.x;
+  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  typename AccFor<T>::type a;
+  if (n < N) {
+    const long long t = (long long)b * N + n;
+    T acc = w[t];
+    const T* v = V + (long long)b * mp1 * N + n;
+    for (int i = 0; i < nv; ++i) cms(acc, v[(long long)i * N], hcol[b * pstride + i]);
+    w[t] = acc;
+    if (NORM) a.add_norm(acc);
   }
-  st2(w[t], acc);
+  if (NORM) {
+    __shared__ double wsum[8];
+    a.warp_reduce();
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = a.get().x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += wsum[q];
+      nrm_partial[(long long)b * nblk + blockIdx.x] = t;
+    }
+  }
 }
 
 template <typename T>
@@ -146,19 +254,17 @@ __global__ void __launch_bounds__(256) norm_partial_kernel(const T* __restrict__
                                                            long long N, int nchunk) {
   const int b = blockIdx.y, c = blockIdx.x;
   const T* vv = v + (long long)b * N;
-  double acc = 0;
-  for (long long n = (long long)c * 256 + threadIdx.x; n < N; n += (long long)nchunk * 256) {
-    const double2 t = ld2(vv[n]);
-    acc += t.x * t.x + t.y * t.y;
-  }
-  acc = block_sum1(acc);
+  typename AccFor<T>::type a;
+  for (long long n = (long long)c * 256 + threadIdx.x; n < N; n += (long long)nchunk * 256) a.add_norm(vv[n]);
+  const double acc = block_sum1(a.get().x);
   if (threadIdx.x == 0) out[b * nchunk + c] = acc;
 }
 
 // out[b] = sqrt(sum_c partial); optionally H[b][k][k+1] = out[b]
 __global__ void norm_reduce_kernel(const double* __restrict__ partial, double* __restrict__ out,
                                    double2* __restrict__ H, const int* __restrict__ active, int nchunk, int k,
-                                   int pstride, int m) {
+                                   int pstride, int m, double* __restrict__ inv64 = nullptr,
+                                   float* __restrict__ inv32 = nullptr) {
   const int b = blockIdx.x;
   double acc = 0;
   for (int c = threadIdx.x; c < nchunk; c += 32) acc += partial[b * nchunk + c];
@@ -166,11 +272,13 @@ __global__ void norm_reduce_kernel(const double* __restrict__ partial, double* _
   if (threadIdx.x == 0) {
     const double v = sqrt(acc);
     out[b] = v;
+    if (inv64) inv64[b] = v > 0 ? 1.0 / v : 0.0;
+    if (inv32) inv32[b] = v > 0 ? (float)(1.0 / v) : 0.f;
     if (H && active[b]) H[(long long)b * pstride * m + (long long)k * pstride + k + 1] = make_double2(v, 0.0);
   }
 }
 
-// dst = src / nrm[b]
+// dst = src * inv[b]  (inverse norms precomputed per problem)
 template <typename S, typename D>
 __global__ void __launch_bounds__(256) scale_kernel(const S* __restrict__ src, D* __restrict__ dst,
                                                     const double* __restrict__ nrm, const int* __restrict__ active,
@@ -180,26 +288,26 @@ __global__ void __launch_bounds__(256) scale_kernel(const S* __restrict__ src, D
   const int b = (int)(t / N);
   if (!active[b]) return;
   const long long n = t - (long long)b * N;
-  const double s = nrm[b];
-  const double inv = s > 0 ? 1.0 / s : 0.0;
+  const double inv = nrm[b];   // inverse norm
   const double2 v = ld2(src[t]);
   st2(dst[(long long)b * dst_stride + n], make_double2(v.x * inv, v.y * inv));
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) scale_h_kernel(const T* __restrict__ src, T* __restrict__ dst,
-                                                      const double2* __restrict__ H, const int* __restrict__ active,
-                                                      long long N, long long dst_stride, int k, int pstride, int m,
-                                                      int batch) {
+// dst = src * inv[b]  (inverse norm computed once per problem)
+template <typename T, typename S>
+__global__ void __launch_bounds__(256) scale_inv_kernel(const T* __restrict__ src, T* __restrict__ dst,
+                                                        const S* __restrict__ inv, const int* __restrict__ active,
+                                                        long long N, long long dst_stride, int batch) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= N * batch) return;
   const int b = (int)(t / N);
   if (!active[b]) return;
   const long long n = t - (long long)b * N;
-  const double s = H[(long long)b * pstride * m + (long long)k * pstride + k + 1].x;
-  const double inv = s > 0 ? 1.0 / s : 0.0;
-  const double2 v = ld2(src[t]);
-  st2(dst[(long long)b * dst_stride + n], make_double2(v.x * inv, v.y * inv));
+  const S f = inv[b];
+  T v = src[t];
+  v.x *= f;
+  v.y *= f;
+  dst[(long long)b * dst_stride + n] = v;
 }
 
 __global__ void __launch_bounds__(256) residual_kernel(const double2* __restrict__ rhs, const double2* __restrict__ ax,
@@ -234,52 +342,65 @@ __global__ void cycle_init_kernel(const double* __restrict__ nrm, const double* 
   for (int i = 0; i < pstride; ++i) g[b * pstride + i] = make_double2(i == 0 ? beta : 0.0, 0.0);
 }
 
-// Givens rotations of column k, residual estimate, convergence test.  One thread per problem.
+// Givens rotations of column k, residual estimate, convergence test.  One warp per
+// problem: the lanes stage the column and the rotations in shared memory, lane 0
+// applies the k previous rotations sequentially there.
+constexpr int kMaxRestart = 256;
 __global__ void givens_kernel(double2* __restrict__ H, double2* __restrict__ cs, double2* __restrict__ sn,
                               double2* __restrict__ g, int* __restrict__ active, int* __restrict__ kused,
                               const double* __restrict__ target, int k, int pstride, int m, int batch) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double2 col_s[kMaxRestart + 1], c_s[kMaxRestart], s_s[kMaxRestart];
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x;
   if (b >= batch || !active[b]) return;
   double2* col = H + (long long)b * pstride * m + (long long)k * pstride;
   double2* c = cs + b * m;
   double2* s = sn + b * m;
-  double2* gg = g + b * pstride;
-  double2 hi = col[0];
-  for (int i = 0; i < k; ++i) {
-    const double2 hj = col[i + 1];
-    const double2 ci = c[i], si = s[i];
-    const double2 t = make_double2(ci.x * hi.x - ci.y * hi.y + si.x * hj.x - si.y * hj.y,
-                                   ci.x * hi.y + ci.y * hi.x + si.x * hj.y + si.y * hj.x);
-    const double2 u = make_double2(-(si.x * hi.x + si.y * hi.y) + (ci.x * hj.x + ci.y * hj.y),
-                                   -(si.x * hi.y - si.y * hi.x) + (ci.x * hj.y - ci.y * hj.x));
-    col[i] = t;
-    hi = u;
+  for (int i = lane; i <= k + 1; i += 32) col_s[i] = col[i];
+  for (int i = lane; i < k; i += 32) {
+    c_s[i] = c[i];
+    s_s[i] = s[i];
   }
-  const double2 a = hi, bb = col[k + 1];
-  const double den = sqrt(a.x * a.x + a.y * a.y + bb.x * bb.x + bb.y * bb.y);
-  double2 cc, ss;
-  if (den == 0.0) {
-    cc = make_double2(1.0, 0.0);
-    ss = make_double2(0.0, 0.0);
-  } else {
-    cc = make_double2(a.x / den, -a.y / den);
-    ss = make_double2(bb.x / den, -bb.y / den);
+  __syncwarp();
+  if (lane == 0) {
+    double2* gg = g + b * pstride;
+    double2 hi = col_s[0];
+    for (int i = 0; i < k; ++i) {
+      const double2 hj = col_s[i + 1];
+      const double2 ci = c_s[i], si = s_s[i];
+      col_s[i] = make_double2(ci.x * hi.x - ci.y * hi.y + si.x * hj.x - si.y * hj.y,
+                              ci.x * hi.y + ci.y * hi.x + si.x * hj.y + si.y * hj.x);
+      hi = make_double2(-(si.x * hi.x + si.y * hi.y) + (ci.x * hj.x + ci.y * hj.y),
+                        -(si.x * hi.y - si.y * hi.x) + (ci.x * hj.y - ci.y * hj.x));
+    }
+    const double2 a = hi, bb = col_s[k + 1];
+    const double den = sqrt(a.x * a.x + a.y * a.y + bb.x * bb.x + bb.y * bb.y);
+    double2 cc, ss;
+    if (den == 0.0) {
+      cc = make_double2(1.0, 0.0);
+      ss = make_double2(0.0, 0.0);
+    } else {
+      cc = make_double2(a.x / den, -a.y / den);
+      ss = make_double2(bb.x / den, -bb.y / den);
+    }
+    c[k] = cc;
+    s[k] = ss;
+    col_s[k] = make_double2(den, 0.0);
+    col_s[k + 1] = make_double2(0.0, 0.0);
+    const double2 gk = gg[k];
+    gg[k + 1] = make_double2(-(ss.x * gk.x + ss.y * gk.y), -(ss.x * gk.y - ss.y * gk.x));
+    gg[k] = make_double2(cc.x * gk.x - cc.y * gk.y, cc.x * gk.y + cc.y * gk.x);
+    kused[b] = k + 1;
+    const double res = sqrt(gg[k + 1].x * gg[k + 1].x + gg[k + 1].y * gg[k + 1].y);
+    if (!(res > target[b]) || bb.x == 0.0 || !isfinite(res)) active[b] = 0;
   }
-  c[k] = cc;
-  s[k] = ss;
-  col[k] = make_double2(den, 0.0);
-  col[k + 1] = make_double2(0.0, 0.0);
-  const double2 gk = gg[k];
-  gg[k + 1] = make_double2(-(ss.x * gk.x + ss.y * gk.y), -(ss.x * gk.y - ss.y * gk.x));
-  gg[k] = make_double2(cc.x * gk.x - cc.y * gk.y, cc.x * gk.y + cc.y * gk.x);
-  kused[b] = k + 1;
-  const double res = sqrt(gg[k + 1].x * gg[k + 1].x + gg[k + 1].y * gg[k + 1].y);
-  if (!(res > target[b]) || bb.x == 0.0 || !isfinite(res)) active[b] = 0;
+  __syncwarp();
+  for (int i = lane; i <= k + 1; i += 32) col[i] = col_s[i];
 }
 
 __global__ void backsolve_kernel(const double2* __restrict__ H, const double2* __restrict__ g,
-                                 double2* __restrict__ y, const int* __restrict__ kused, int pstride, int m,
-                                 int batch) {
+                                 double2* __restrict__ y, float2* __restrict__ y32, const int* __restrict__ kused,
+                                 int pstride, int m, int batch) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= batch) return;
   const int kk = kused[b];
@@ -298,10 +419,12 @@ __global__ void backsolve_kernel(const double2* __restrict__ H, const double2* _
     yb[i] = dd > 0 ? make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd)
                    : make_double2(0, 0);
   }
+  if (y32)
+    for (int i = 0; i < m; ++i) y32[b * m + i] = make_float2((float)yb[i].x, (float)yb[i].y);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) combine_kernel(const T* __restrict__ V, const double2* __restrict__ y,
+__global__ void __launch_bounds__(256) combine_kernel(const T* __restrict__ V, const T* __restrict__ y,
                                                       const int* __restrict__ kused, T* __restrict__ u, long long N,
                                                       int mp1, int m, int batch) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -309,14 +432,17 @@ __global__ void __launch_bounds__(256) combine_kernel(const T* __restrict__ V, c
   const int b = (int)(t / N);
   const long long n = t - (long long)b * N;
   const int kk = kused[b];
-  double2 acc = make_double2(0, 0);
+  T acc;
+  acc.x = 0;
+  acc.y = 0;
   const T* v = V + (long long)b * mp1 * N + n;
   for (int i = 0; i < kk; ++i) {
-    const double2 t2 = cmul(ld2(v[(long long)i * N]), y[b * m + i]);
-    acc.x += t2.x;
-    acc.y += t2.y;
+    T h = y[b * m + i];
+    h.x = -h.x;
+    h.y = -h.y;
+    cms(acc, v[(long long)i * N], h);   // acc += v y
   }
-  st2(u[t], acc);
+  u[t] = acc;
 }
 
 inline unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
@@ -333,6 +459,13 @@ inline unsigned blocks_for(long long n) { return (unsigned)((n + 255) / 256); }
 // One Arnoldi step k on basis V (stride (m+1) N per problem): z = M^-1 V_k,
 // w = A z, CGS2 against V_0..V_k, V_{k+1} = w / |w|, Givens.  `prec` and `apply`
 // are the operator pair of the basis precision.
+template <typename T> T* coef_col(Problem& P);
+template <> double2* coef_col<double2>(Problem& P) { return P.hcol; }
+template <> float2* coef_col<float2>(Problem& P) { return P.mx.hcol; }
+template <typename T> float2* coef_col32(Problem& P);
+template <> float2* coef_col32<double2>(Problem&) { return nullptr; }
+template <> float2* coef_col32<float2>(Problem& P) { return P.mx.hcol; }
+
 template <typename T, typename Prec, typename Apply>
 int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   const int B = P.batch, mp1 = m + 1, ps = P.restart_max + 1, mm = P.restart_max;
@@ -340,19 +473,31 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   WG_CK(prec(V + (long long)k * N, (long long)mp1 * N));
   WG_CK(apply());
   const int nv = k + 1;
-  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 10);
+  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 9);
+  const dim3 gu((unsigned)((N + 255) / 256), B);
   for (int pass = 0; pass < 2; ++pass) {
-    dot_partial_kernel<T><<<dim3(P.nchunk, nv, B), 256, 0, P.stream>>>(V, w, P.partial, P.active, N, mp1, ps,
-                                                                     P.nchunk);
-    dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, P.H, P.active, nv, k, ps, mm, P.nchunk, pass == 0);
-    gs_update_kernel<T><<<blocks_for(tot), 256, 0, P.stream>>>(V, w, P.hcol, P.active, N, nv, mp1, ps, B);
+    multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double2) * 8 * nv, P.stream>>>(V, w, P.partial, P.active, N, nv,
+                                                                                     mp1, ps, P.nchunk);
+    dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, coef_col32<T>(P), P.H, P.active, nv, k, ps, mm,
+                                               P.nchunk, pass == 0);
+    if (pass == 0)
+      gs_update_kernel<T, false><<<gu, 256, 0, P.stream>>>(V, w, coef_col<T>(P), P.active, nullptr, N, nv, mp1, ps,
+                                                          P.nblk);
+    else
+      gs_update_kernel<T, true><<<gu, 256, 0, P.stream>>>(V, w, coef_col<T>(P), P.active, P.nrm_partial, N, nv, mp1,
+                                                         ps, P.nblk);
   }
-  norm_partial_kernel<T><<<dim3(P.nchunk, B), 256, 0, P.stream>>>(w, P.nrm_partial, N, P.nchunk);
-  norm_reduce_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, P.H, P.active, P.nchunk, k, ps, mm);
-  scale_h_kernel<T><<<blocks_for(tot), 256, 0, P.stream>>>(w, V + (long long)(k + 1) * N, P.H, P.active, N,
-                                                          (long long)mp1 * N, k, ps, mm, B);
-  givens_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.cs, P.sn, P.g, P.active, P.kused, P.target, k, ps, mm,
-                                                      B);
+  norm_reduce_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, P.H, P.active, P.nblk, k, ps, mm, P.inv64,
+                                             P.mx.inv);
+  if (sizeof(T) == sizeof(float2))
+    scale_inv_kernel<float2, float><<<blocks_for(tot), 256, 0, P.stream>>>(
+        reinterpret_cast<const float2*>(w), reinterpret_cast<float2*>(V) + (long long)(k + 1) * N, P.mx.inv,
+        P.active, N, (long long)mp1 * N, B);
+  else
+    scale_inv_kernel<double2, double><<<blocks_for(tot), 256, 0, P.stream>>>(
+        reinterpret_cast<const double2*>(w), reinterpret_cast<double2*>(V) + (long long)(k + 1) * N, P.inv64,
+        P.active, N, (long long)mp1 * N, B);
+  givens_kernel<<<B, 32, 0, P.stream>>>(P.H, P.cs, P.sn, P.g, P.active, P.kused, P.target, k, ps, mm, B);
   prof_end(P, PROF_KRYLOV, ev);
   WG_CK(cudaGetLastError());
   return WG_OK;
@@ -365,7 +510,8 @@ int true_residual(Problem& P) {
   WG_CK(launch_apply(P, P.x, P.w));
   residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot);
   norm_partial_kernel<double2><<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk);
-  norm_reduce_kernel<<<P.batch, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, nullptr, P.active, P.nchunk, 0, 0, 0);
+  norm_reduce_kernel<<<P.batch, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, nullptr, P.active, P.nchunk, 0, 0, 0,
+                                                   P.inv64);
   WG_CK(cudaGetLastError());
   return WG_OK;
 }
@@ -442,7 +588,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
     if (!any) break;
     P.prof.launches[PROF_OTHER] += 2;
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
-    scale_kernel<double2, double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, P.V, P.nrm, P.active, N,
+    scale_kernel<double2, double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, P.V, P.inv64, P.active, N,
                                                                          (long long)mp1 * N, B);
     for (int k = 0; k < m; ++k) {
       rc = arnoldi_step<double2>(P, P.V, P.w, k, m, prec, apply);
@@ -454,7 +600,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
       }
     }
     P.prof.launches[PROF_OTHER] += 3;
-    backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, P.kused, ps, mm, B);
+    backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, nullptr, P.kused, ps, mm, B);
     combine_kernel<double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.V, P.ycoef, P.kused, P.w, N, mp1, mm, B);
     WG_CK(launch_precondition(P, P.w, N, P.z));
     axpy_kernel<double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, P.z, nullptr, N, B);
@@ -502,7 +648,7 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     WG_CK(cudaMemcpyAsync(P.nrm, ones.data(), sizeof(double) * B, cudaMemcpyHostToDevice, P.stream));
     P.prof.launches[PROF_OTHER] += 2;
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
-    scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.V, P.nrm_keep, P.active, N,
+    scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.V, P.inv64, P.active, N,
                                                                         (long long)mp1 * N, B);
     for (int k = 0; k < m; ++k) {
       rc = arnoldi_step<float2>(P, M.V, M.w, k, m, prec, apply);
@@ -515,8 +661,8 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     }
     // d = M^-1 (V y) in FP32, x += |r| d in FP64
     P.prof.launches[PROF_OTHER] += 3;
-    backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, P.kused, ps, mm, B);
-    combine_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(M.V, P.ycoef, P.kused, M.w, N, mp1, mm, B);
+    backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, M.y, P.kused, ps, mm, B);
+    combine_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(M.V, M.y, P.kused, M.w, N, mp1, mm, B);
     WG_CK(launch_precondition_mixed(P, M.w, N, M.d, nullptr));
     axpy_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, M.d, P.nrm_keep, N, B);
     WG_CK(cudaGetLastError());

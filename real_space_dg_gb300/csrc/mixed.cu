@@ -76,16 +76,16 @@ cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, float* D, in
 // ---------------------------------------------------------------------------
 template <int NK>
 __global__ void __launch_bounds__(256) flux32_kernel(const float2* __restrict__ x, float2* __restrict__ y,
-                                                     const double* __restrict__ kvec, const double* __restrict__ qd,
-                                                     FluxBlocks fb, int n_el, int nk, long long total) {
+                                                     const float* __restrict__ kvec, const float* __restrict__ qd,
+                                                     FluxBlocks32 fb, int n_el, int nk, long long total) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= total) return;
   const int j = (int)(t % nk);
   const long long be = t / nk;
   const int e = (int)(be % n_el);
   const int b = (int)(be / n_el);
-  const float k = (float)kvec[j], ak = fabsf(k);
-  const float s = (float)qd[b];
+  const float k = kvec[j], ak = fabsf(k);
+  const float s = qd[b];
   const float2* xe = x + be * (long long)NK * nk + j;
   float2 xv[NK], acc[NK];
 #pragma unroll
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(256) flux32_kernel(const float2* __restrict__ 
     float2 v = make_float2(0.f, 0.f);
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
-      const float m = k * (float)fb.K1[a * NK + c] + ak * (float)fb.K2[a * NK + c];
+      const float m = k * fb.K1[a * NK + c] + ak * fb.K2[a * NK + c];
       v.x = fmaf(m, xv[c].x, v.x);
       v.y = fmaf(m, xv[c].y, v.y);
     }
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(256) flux32_kernel(const float2* __restrict__ 
       const float2 xp = xl[(long long)c * nk];
 #pragma unroll
       for (int a = 0; a < NK; ++a) {
-        const float m = (k + ak) * (float)fb.K3[a * NK + c];
+        const float m = (k + ak) * fb.K3[a * NK + c];
         acc[a].x = fmaf(m, xp.x, acc[a].x);
         acc[a].y = fmaf(m, xp.y, acc[a].y);
       }
@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) flux32_kernel(const float2* __restrict__ 
       const float2 xp = xr[(long long)c * nk];
 #pragma unroll
       for (int a = 0; a < NK; ++a) {
-        const float m = (k - ak) * (float)fb.K5[a * NK + c];
+        const float m = (k - ak) * fb.K5[a * NK + c];
         acc[a].x = fmaf(m, xp.x, acc[a].x);
         acc[a].y = fmaf(m, xp.y, acc[a].y);
       }
@@ -177,8 +177,8 @@ __global__ void __launch_bounds__(256) stencil32_kernel(const float2* __restrict
 // ---------------------------------------------------------------------------
 template <int NK>
 __global__ void precond32_kernel(const float2* __restrict__ r, float2* __restrict__ z, bf162* __restrict__ zb,
-                                 const double* __restrict__ kvec, const double* __restrict__ dinv,
-                                 const double* __restrict__ hvec, const double* __restrict__ qd, int n_el, int nk,
+                                 const float* __restrict__ kvec, const float* __restrict__ dinv,
+                                 const float* __restrict__ hvec, const float* __restrict__ qd, int n_el, int nk,
                                  long long N, long long r_stride) {
   extern __shared__ float2 shf[];  // [2][P][32]
   const int lane = threadIdx.x & 31;
@@ -193,12 +193,12 @@ __global__ void precond32_kernel(const float2* __restrict__ r, float2* __restric
   bool fwd = true;
   float inv_qd = 1.f;
 #pragma unroll
-  for (int i = 0; i < NK * NK; ++i) D[i] = valid ? (float)dinv[j * NK * NK + i] : 0.f;
+  for (int i = 0; i < NK * NK; ++i) D[i] = valid ? dinv[j * NK * NK + i] : 0.f;
 #pragma unroll
-  for (int i = 0; i < NK; ++i) h[i] = valid ? (float)hvec[j * NK + i] : 0.f;
+  for (int i = 0; i < NK; ++i) h[i] = valid ? hvec[j * NK + i] : 0.f;
   if (valid) {
     fwd = kvec[j] > 0;
-    inv_qd = (float)(1.0 / qd[b]);
+    inv_qd = __frcp_rn(qd[b]);
   }
   // row `st` of D and h[st] without dynamic register indexing
   float Dst[NK];
@@ -304,7 +304,7 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
     P.prof.launches[PROF_OTHER] += 1;
   }
   cudaEvent_t ev = prof_begin(P, PROF_FLUX);
-  flux32_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, s.n_el, s.nk,
+  flux32_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, M.kvec, M.qd, M.fb, s.n_el, s.nk,
                                                                             total);
   prof_end(P, PROF_FLUX, ev);
   ev = prof_begin(P, PROF_GEMM_FWD);
@@ -331,7 +331,7 @@ cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, fl
   dim3 grid((P.s.nk + 31) / 32, P.batch);
   cudaEvent_t ev = prof_begin(P, PROF_PRECOND);
   precond32_kernel<NK><<<grid, 32 * Pw, sizeof(float2) * 2 * Pw * 32, P.stream>>>(
-      r, z, zb, P.kvec, P.pre_dinv, P.pre_h, P.qd, P.s.n_el, P.s.nk, P.N, r_stride);
+      r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, P.s.n_el, P.s.nk, P.N, r_stride);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
@@ -374,9 +374,23 @@ int mixed_alloc(Problem& P) {
   alloc((void**)&M.beta, sizeof(float) * (size_t)P.batch * s.n_el * s.nK * s.nK * (s.nxi + 1));
   alloc((void**)&M.betai, sizeof(float) * (size_t)s.nK * s.nK * (s.nxi + 1));
   alloc((void**)&M.err, sizeof(int));
+  alloc((void**)&M.kvec, sizeof(float) * s.nk);
+  alloc((void**)&M.qd, sizeof(float) * P.batch);
+  alloc((void**)&M.dinv, sizeof(float) * (size_t)s.nk * s.nK * s.nK);
+  alloc((void**)&M.h, sizeof(float) * (size_t)s.nk * s.nK);
+  alloc((void**)&M.hcol, sizeof(float2) * (size_t)P.batch * (P.restart_max + 1));
+  alloc((void**)&M.y, sizeof(float2) * (size_t)P.batch * P.restart_max);
+  alloc((void**)&M.inv, sizeof(float) * P.batch);
   if (e != cudaSuccess) {
     P.err = std::string("mixed-precision buffers: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
+  }
+  M.fb.nK = s.nK;
+  for (int i = 0; i < s.nK * s.nK; ++i) {
+    M.fb.K1[i] = (float)s.K1[i];
+    M.fb.K2[i] = (float)s.K2[i];
+    M.fb.K3[i] = (float)s.K3[i];
+    M.fb.K5[i] = (float)s.K5[i];
   }
   P.device_bytes += bytes;
   cudaMemsetAsync(M.err, 0, sizeof(int), P.stream);
@@ -418,7 +432,8 @@ int mixed_alloc(Problem& P) {
 
 void mixed_free(Problem& P) {
   MixedBuffers& M = P.mx;
-  void* ptrs[] = {M.phi1, M.phi2, M.xin16, M.zb16, M.yh16, M.xh, M.V, M.w, M.z, M.r, M.d, M.beta, M.betai, M.err};
+  void* ptrs[] = {M.phi1, M.phi2, M.xin16, M.zb16, M.yh16, M.xh, M.V, M.w, M.z, M.r, M.d, M.beta, M.betai, M.err,
+                  M.kvec, M.qd, M.dinv, M.h, M.hcol, M.y, M.inv};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   M = MixedBuffers{};
@@ -429,9 +444,14 @@ cudaError_t mixed_sync_weights(Problem& P) {
   const Shape& s = P.s;
   const long long nb = (long long)P.batch * s.n_el * s.nK * s.nK * (s.nxi + 1);
   const long long ni = (long long)s.nK * s.nK * (s.nxi + 1);
-  P.prof.launches[PROF_OTHER] += 2;
+  P.prof.launches[PROF_OTHER] += 6;
   d2f_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, P.stream>>>(P.beta, P.mx.beta, nb);
   d2f_kernel<<<(unsigned)((ni + 255) / 256), 256, 0, P.stream>>>(P.betai, P.mx.betai, ni);
+  d2f_kernel<<<1, 256, 0, P.stream>>>(P.qd, P.mx.qd, P.batch);
+  d2f_kernel<<<(unsigned)((s.nk + 255) / 256), 256, 0, P.stream>>>(P.kvec, P.mx.kvec, s.nk);
+  d2f_kernel<<<(unsigned)((s.nk * s.nK * s.nK + 255) / 256), 256, 0, P.stream>>>(P.pre_dinv, P.mx.dinv,
+                                                                                (long long)s.nk * s.nK * s.nK);
+  d2f_kernel<<<(unsigned)((s.nk * s.nK + 255) / 256), 256, 0, P.stream>>>(P.pre_h, P.mx.h, (long long)s.nk * s.nK);
   return cudaGetLastError();
 }
 

@@ -22,6 +22,15 @@ struct FluxBlocks {
   double invM[kMaxLocal * kMaxLocal];
 };
 
+// FP32 copies of the flux blocks for the mixed form (no FP64 instruction per element).
+struct FluxBlocks32 {
+  int nK;
+  float K1[kMaxLocal * kMaxLocal];
+  float K2[kMaxLocal * kMaxLocal];
+  float K3[kMaxLocal * kMaxLocal];
+  float K5[kMaxLocal * kMaxLocal];
+};
+
 // Per-problem scalar parameters on the device: pp[b * kPP + PP_*].
 constexpr int kPP = 10;
 enum { PP_LX = 0, PP_QD, PP_M0, PP_M1, PP_MEZ, PP_TEMP, PP_EFL, PP_EFR, PP_VMIN, PP_VMAX };
@@ -49,6 +58,14 @@ struct MixedBuffers {
   float2* d = nullptr;               // [B*N] inner correction
   float* beta = nullptr;             // fp32 copy of the potential weights
   float* betai = nullptr;
+  float* kvec = nullptr;             // [nk]
+  float* qd = nullptr;               // [B]
+  float* dinv = nullptr;             // [nk][nK*nK]
+  float* h = nullptr;                // [nk][nK]
+  float2* hcol = nullptr;            // [B][m+1] Gram-Schmidt coefficients in FP32
+  float2* y = nullptr;               // [B][m] Hessenberg solution in FP32
+  float* inv = nullptr;              // [B] 1/|w| in FP32
+  FluxBlocks32 fb;
   int* err = nullptr;                // raised by a GEMM whose barrier wait timed out
   CUtensorMap tmA1, tmB1, tmB1z, tmA2, tmB2;
 };
@@ -159,11 +176,13 @@ struct Problem {
   double* nrm_partial = nullptr; // [B][nchunk]
   double* nrm = nullptr;         // [B]
   double* nrm_keep = nullptr;    // [B] outer residual norms of the mixed refinement
+  double* inv64 = nullptr;       // [B] inverse basis-vector norms
   double* target = nullptr;      // [B] absolute residual targets
   int* active = nullptr;         // [B] 1 while iterating in this cycle
   int* kused = nullptr;          // [B] iterations used in this cycle
   int* any_active = nullptr;     // [1]
-  int nchunk = 0;
+  int nchunk = 0;  // 2048-element chunks of one problem vector (multi-dot partials)
+  int nblk = 0;    // 256-element blocks of one problem vector (norm partials)
   // host mirrors
   std::vector<double> h_nrm;
   std::vector<int> h_active, h_kused;

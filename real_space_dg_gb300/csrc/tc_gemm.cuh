@@ -198,15 +198,19 @@ __global__ void __launch_bounds__(128, 1) gemm_bf16_kernel(const __grid_constant
       float v[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, v);
       if (row < M) {
+        float* dst = D + (n0 + cb * 32) * (long long)M + row;
+        const int ncb = (int)min((long long)32, Ncol - (n0 + cb * 32));
+        if (EPI == 1) {
+          // issue all loads before any store so they overlap
+          float old[32];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const long long col = n0 + cb * 32 + i;
-          if (col < Ncol) {
-            float* dst = D + col * (long long)M + row;
-            if (EPI == 0) *dst = v[i];
-            else *dst += v[i];
-          }
+          for (int i = 0; i < 32; ++i) old[i] = i < ncb ? dst[(long long)i * M] : 0.f;
+#pragma unroll
+          for (int i = 0; i < 32; ++i) v[i] += old[i];
         }
+#pragma unroll
+        for (int i = 0; i < 32; ++i)
+          if (i < ncb) dst[(long long)i * M] = v[i];
       }
     }
   }
