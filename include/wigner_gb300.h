@@ -195,6 +195,31 @@ int wg_gummel_run(wg_problem* h, const wg_gummel_opts* opts, wg_gummel_info* inf
 /* Problem b's potential phi [nx], density n [n_el*n_local] in m^-3 and current density j. */
 int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j);
 
+/* ---- Allocation-free operator apply ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * while they call in: applications that own all device memory through their
+ * own allocator (a MEX gateway on gpuArray storage, a framework pool with a
+ * hard budget) and code recording a CUDA graph, where allocation is not
+ * allowed during stream capture.  y = A x (the FP64 operator of wg_apply) on
+ * caller-owned DEVICE buffers; the library allocates nothing.  The transform
+ * scratch is a fixed file-scope device array of 2^20 complex doubles (16 MiB)
+ * that every GPU loading the library keeps until exit; problems with
+ * n_xi*batch*n_el*n_local > 2^19 are rejected with WG_ERR_ARG.  All calls share
+ * that array: calls whose kernels overlap on the GPU race and must be
+ * serialised by the caller.  The first call on a device looks up the array's
+ * device address; make it before any stream capture.  Kernels are enqueued on
+ * `stream` (NULL: the default stream) and the call does not synchronise. */
+typedef struct {
+  int n_el, n_local, nk, n_xi, batch;
+  const double* phi;    /* device: n_xi x nk complex, row-major (xi row s, k column j), exp(i k_j xi_s)/sqrt(Ly) */
+  const double* kvec;   /* device: nk wave numbers */
+  const double* qd;     /* device: batch values Q_diff * MPC / detJ (detJ = L_x / n_el / 2) */
+  const double* beta;   /* device: [batch][n_el][n_local^2][n_xi+1] real xi-stencil weights of the potential */
+  const double* betai;  /* device: [n_local^2][n_xi+1] imaginary (CAP) xi-stencil weights */
+  double K1[16], K2[16], K3[16], K5[16];  /* host: element flux blocks, row-major n_local x n_local */
+} wg_operator_view;
+int wg_apply_noalloc(const wg_operator_view* op, const double* x, double* y, void* stream);
+
 /* Diagnostic: C = bf16(A) * bf16(B) on the tcgen05 tensor-core GEMM of the mixed
  * form, FP32 accumulation.  A row-major M x K, B column-major K x N, C column-major
  * M x N, host buffers; K >= 64 and K % 8 == 0.  No counterpart in the reference. */

@@ -33,6 +33,13 @@ class WgDevice(C.Structure):
                 ("me_z", C.c_double), ("temp", C.c_double)]
 
 
+class WgOperatorView(C.Structure):
+    _fields_ = [("n_el", C.c_int), ("n_local", C.c_int), ("nk", C.c_int), ("n_xi", C.c_int), ("batch", C.c_int),
+                ("phi", C.c_void_p), ("kvec", C.c_void_p), ("qd", C.c_void_p), ("beta", C.c_void_p),
+                ("betai", C.c_void_p), ("K1", C.c_double * 16), ("K2", C.c_double * 16), ("K3", C.c_double * 16),
+                ("K5", C.c_double * 16)]
+
+
 class WgSolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("use_rho0", C.c_int)]
 
@@ -91,6 +98,7 @@ SIGNATURES = {
     "wg_gummel_set": ([_H, C.c_int, C.POINTER(WgDevice), C.POINTER(WgRtd1D)], C.c_int),
     "wg_gummel_run": ([_H, C.POINTER(WgGummelOpts), C.POINTER(WgGummelInfo)], C.c_int),
     "wg_gummel_get": ([_H, C.c_int, _D, _D, _D], C.c_int),
+    "wg_apply_noalloc": ([C.POINTER(WgOperatorView), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "wg_debug_gemm_bf16": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
                             C.c_int], C.c_int),
     "wg_event_record": ([_H, C.c_int], C.c_int),

@@ -484,6 +484,14 @@ int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j) {
   return WG_OK;
 }
 
+int wg_apply_noalloc(const wg_operator_view* op, const double* x, double* y, void* stream) {
+  if (!op) return fail(nullptr, WG_ERR_ARG, "wg_apply_noalloc: null operator view");
+  std::string err;
+  const int rc = wg::apply_noalloc(*op, x, y, stream, err);
+  if (rc) return fail(nullptr, rc, err);
+  return WG_OK;
+}
+
 int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K) {
   if (!A || !B || !C) return fail(nullptr, WG_ERR_ARG, "wg_debug_gemm_bf16: null argument");
   std::string err;

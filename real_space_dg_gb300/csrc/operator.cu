@@ -10,6 +10,9 @@
 // plus the k-line preconditioner, the Vw(x,k) rebuild and the observables.
 #include <cuda_runtime.h>
 
+#include <mutex>
+#include <string>
+
 #include "problem.h"
 
 namespace wg {
@@ -486,6 +489,114 @@ cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j) {
   observables_kernel<<<grid, 256, 0, P.stream>>>(rho, P.phi, P.m_nodes + (long long)b * ncol, n_dg, j, P.s.nk,
                                                  P.s.nxi, ncol, P.s.delta_xi, pref);
   return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free operator apply.
+//
+// For callers that must not allocate device memory while they call in: a host
+// application that owns every device allocation through its own pool (a MATLAB
+// MEX gateway working on gpuArray storage, a framework's caching allocator with
+// a hard budget), or code recording a CUDA graph, where cudaMalloc/cudaFree are
+// not allowed inside stream capture.  The caller passes its own device buffers
+// for the operator data, x and y; the only scratch, the transformed state X^ and
+// the stencil output Y^, lives in the file-scope array below.  Its size is fixed
+// (kNoAllocScratch complex doubles, 16 MiB) and every GPU that loads the library
+// keeps it until the process exits.  All calls share it: two calls whose kernels
+// overlap on the GPU (different streams, or devices shared by threads without
+// ordering) race on it and must be serialised by the caller.  Both halves are
+// fully written before they are read in every call, so nothing is cleared.
+// ---------------------------------------------------------------------------
+constexpr long long kNoAllocScratch = 1ll << 20;      // complex doubles: two halves for X^ and Y^
+static __device__ __align__(256) double2 g_noalloc_scratch[kNoAllocScratch];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double2* g_noalloc_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array for the current device.  The first call on
+// a device looks it up (cudaGetSymbolAddress, which does not allocate); make that
+// first call before any stream capture.
+cudaError_t noalloc_scratch(double2** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_ptr[dev] = static_cast<double2*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return cudaSuccess;
+}
+
+template <int NK>
+cudaError_t apply_noalloc_nk(const wg_operator_view& v, const FluxBlocks& fb, const double2* x, double2* y,
+                             double2* xh, double2* yh, cudaStream_t st) {
+  const long long ncols = (long long)v.batch * v.n_el * NK;
+  const long long total = (long long)v.batch * v.n_el * v.nk;
+  flux_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(x, y, v.kvec, v.qd, fb, v.n_el, v.nk, total);
+  const double2* phi = reinterpret_cast<const double2*>(v.phi);
+  dim3 g1((unsigned)((ncols + GBN - 1) / GBN), (v.n_xi + GBM - 1) / GBM);
+  zgemm_kernel<0><<<g1, 256, 0, st>>>(phi, v.nk, x, xh, v.n_xi, v.nk, ncols);
+  const long long nelem = (long long)v.batch * v.n_el;
+  stencil_kernel<NK><<<(unsigned)((nelem * v.n_xi + 255) / 256), 256, 0, st>>>(xh, yh, v.beta, v.betai, v.n_xi, nelem);
+  dim3 g2((unsigned)((ncols + GBN - 1) / GBN), (v.nk + GBM - 1) / GBM);
+  zgemm_kernel<1><<<g2, 256, 0, st>>>(phi, v.nk, yh, y, v.nk, v.n_xi, ncols);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int apply_noalloc(const wg_operator_view& v, const double* x, double* y, void* stream, std::string& err) {
+  if (v.n_local < 2 || v.n_local > kMaxLocal || v.n_el < 1 || v.nk < 1 || v.n_xi < 1 || v.batch < 1) {
+    err = "wg_apply_noalloc: sizes must be positive and n_local in 2..4";
+    return WG_ERR_ARG;
+  }
+  if (!v.phi || !v.kvec || !v.qd || !v.beta || !v.betai || !x || !y) {
+    err = "wg_apply_noalloc: null device pointer";
+    return WG_ERR_ARG;
+  }
+  const long long need = (long long)v.n_xi * v.batch * v.n_el * v.n_local;
+  if (need > kNoAllocScratch / 2) {
+    err = "wg_apply_noalloc: n_xi*batch*n_el*n_local = " + std::to_string(need) + " exceeds the fixed scratch of " +
+          std::to_string(kNoAllocScratch / 2) + " complex values per transform (use wg_apply on a handle)";
+    return WG_ERR_ARG;
+  }
+  double2* scratch = nullptr;
+  cudaError_t e = noalloc_scratch(&scratch);
+  if (e != cudaSuccess) {
+    err = std::string("wg_apply_noalloc: scratch address: ") + cudaGetErrorString(e);
+    return WG_ERR_CUDA;
+  }
+  FluxBlocks fb{};
+  fb.nK = v.n_local;
+  for (int i = 0; i < v.n_local * v.n_local; ++i) {
+    fb.K1[i] = v.K1[i];
+    fb.K2[i] = v.K2[i];
+    fb.K3[i] = v.K3[i];
+    fb.K5[i] = v.K5[i];
+  }
+  const double2* xx = reinterpret_cast<const double2*>(x);
+  double2* yy = reinterpret_cast<double2*>(y);
+  double2* xh = scratch;
+  double2* yh = scratch + kNoAllocScratch / 2;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  switch (v.n_local) {
+    case 2: e = apply_noalloc_nk<2>(v, fb, xx, yy, xh, yh, st); break;
+    case 3: e = apply_noalloc_nk<3>(v, fb, xx, yy, xh, yh, st); break;
+    default: e = apply_noalloc_nk<4>(v, fb, xx, yy, xh, yh, st); break;
+  }
+  if (e != cudaSuccess) {
+    err = std::string("wg_apply_noalloc: ") + cudaGetErrorString(e);
+    return WG_ERR_CUDA;
+  }
+  return WG_OK;
 }
 
 }  // namespace wg

@@ -208,6 +208,8 @@ cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride
 cudaError_t launch_potential_update(Problem& P, int b0, int b1);
 cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j);
 cudaError_t launch_rho_xi(Problem& P, int b, double2* out);
+// Allocation-free operator apply on caller-owned device buffers (operator.cu).
+int apply_noalloc(const wg_operator_view& v, const double* x, double* y, void* stream, std::string& err);
 // Krylov (gmres.cu)
 int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // Mixed form (mixed.cu)
