@@ -137,21 +137,30 @@ def make_workload(batch):
     return spec, mat, biases
 
 
-def algorithmic_cost(kind, spec, batch):
-    """Algorithmic bytes or flops of one launch of a kernel class."""
-    nK = spec.order + 1
-    N = spec.n_el * nK * spec.nk
-    ncol = batch * spec.n_el * nK
-    nxi = spec.n_xi or spec.nk
-    if kind in ("gemm_fwd", "gemm_bwd"):
-        return 8.0 * nxi * spec.nk * ncol, "TFLOP/s"
-    if kind == "flux":
-        return 2 * 16.0 * N * batch, "GB/s"
-    if kind == "stencil":
-        return 2 * 16.0 * nxi * ncol + 8.0 * batch * spec.n_el * nK * nK * (nxi + 1), "GB/s"
-    if kind == "precond":
-        return 2 * 16.0 * N * batch, "GB/s"
-    return None, None
+def rooflines(prof, precision):
+    """Achieved rate per kernel class from the library's CUDA-event timings and the
+    algorithmic bytes/flops it attributed to each timed launch."""
+    hbm, bf16, src = read_peaks()
+    out = {}
+    total = sum(v[0] for v in prof.values() if v[1] > 0) or 1.0
+    for cls, (ms, n_t, n_l, by, fl) in prof.items():
+        if n_t == 0 or ms <= 0:
+            continue
+        sec = ms / 1000.0
+        if cls == "gemm_bf16":
+            ach, peak, bound, unit, psrc = fl / sec / 1e12, bf16, "tensor", "TFLOP/s", "bf16_tflops (%s)" % src
+        elif cls == "gemm_f64":
+            ach, peak, bound, unit = fl / sec / 1e12, 1.25, "fp64", "TFLOP/s"
+            psrc = "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)"
+        elif by > 0:
+            ach, peak, bound, unit, psrc = by / sec / 1e9, hbm, "hbm", "GB/s", "hbm_gbs (%s)" % src
+        else:
+            continue
+        out[cls] = {"kernel": cls, "bound": bound, "achieved": round(ach, 3), "peak": peak, "unit": unit,
+                    "frac": round(ach / peak, 4), "traffic": None, "peak_source": psrc,
+                    "avg_launch_us": round(1000.0 * ms / n_t, 2), "launches": int(n_t), "share": round(ms / total, 4),
+                    "per_launch": {"bytes": by / n_t, "flops": fl / n_t}}
+    return out
 
 
 def run_ours(args, rank, world, dist):
@@ -161,7 +170,8 @@ def run_ours(args, rank, world, dist):
     from real_space_dg_gb300.rtd import RTDSweep, solve_rtd_self_consistent
 
     spec, mat, biases = make_workload(args.batch)
-    opts = dict(GUMMEL, precision=args.precision, restart=args.restart)
+    opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
+                innerTol=args.inner_tol, inexactFactor=args.inexact)
     S = RTDSweep(mat, args.batch, opts)
     for b, v in enumerate(biases):
         S.set(b, v)
@@ -191,28 +201,8 @@ def run_ours(args, rank, world, dist):
     pts_all = sum_over_ranks(pts, dist)
     value = pts_all / t_max if t_max > 0 else 0.0
     # roofline of the dominant kernel class (largest share of timed kernel time)
-    timed = {k: v for k, v in prof.items() if v[1] > 0}
-    dom = max(timed, key=lambda k: timed[k][0]) if timed else None
-    hbm, bf16, src = read_peaks()
-    roof = None
-    if dom:
-        ms, n_t, _ = timed[dom]
-        cost, unit = algorithmic_cost(dom, spec, args.batch)
-        if cost is not None:
-            per_launch_s = ms / 1000.0 / n_t
-            if unit == "TFLOP/s":
-                achieved = cost / per_launch_s / 1e12
-                if args.precision == "fp64":
-                    peak, bound, psrc = 1.25, "fp64", "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)"
-                else:
-                    peak, bound, psrc = bf16, "tensor", "bf16_tflops of MEASURED_PEAKS.json (%s)" % src
-            else:
-                achieved = cost / per_launch_s / 1e9
-                peak, bound, psrc = hbm, "hbm", "hbm_gbs of MEASURED_PEAKS.json (%s)" % src
-            roof = {"kernel": dom, "bound": bound, "achieved": round(achieved, 3), "peak": peak, "unit": unit,
-                    "frac": round(achieved / peak, 4), "traffic": None, "peak_source": psrc,
-                    "avg_launch_us": round(1000.0 * ms / n_t, 2),
-                    "share": {k: round(v[0] / sum(x[0] for x in timed.values()), 4) for k, v in timed.items()}}
+    roofs = rooflines(prof, args.precision)
+    roof = max(roofs.values(), key=lambda r: r["share"]) if roofs else None
     launches = sum(v[2] for v in prof.values())
     # e2e: the public call with host inputs and outputs, every step
     e2e = None
@@ -241,7 +231,9 @@ def run_ours(args, rank, world, dist):
         "data": "synthetic RTD device of the named shape (seeded, deterministic)",
         "config": {"workload": "C2 self-consistent RTD 80 nm, p=3, N_el=240, Nk=256, 245760 unknowns/point",
                    "batch_bias_points": args.batch, "biases_v": [round(float(b), 4) for b in biases],
-                   "precision": args.precision, "gmres_restart": args.restart, "gummel_mixing": 0.3,
+                   "precision": args.precision, "gmres_restart": args.restart,
+                   "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
+                   "inexact_gummel_factor": args.inexact, "gummel_mixing": 0.3,
                    "potential_tol_v": 1e-6, "transport_rtol": 1e-8,
                    "l2": "inputs larger than L2 (Krylov basis %.2f GB)" %
                          (16.0 * (args.restart + 1) * args.batch * spec.n_el * (spec.order + 1) * spec.nk / 1e9)},
@@ -249,7 +241,7 @@ def run_ours(args, rank, world, dist):
         "converged_points": int(pts_all), "points_attempted": len(statuses) * world,
         "gmres_iterations_per_point": round(iters_per_point, 1),
         "gummel_iterations_per_point": round(gummel_its / max(1, len(statuses)), 2),
-        "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "roofline": roof, "rooflines": roofs, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
     }
     return out
 
@@ -309,6 +301,10 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--restart", type=int, default=50)
+    ap.add_argument("--inner-restart", type=int, default=40)
+    ap.add_argument("--inner-tol", type=float, default=1e-3)
+    ap.add_argument("--inexact", type=float, default=0.0,
+                    help="inexact Gummel factor (transport tol = factor * potential defect); 0 = fixed 1e-8")
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--iters-per-point", type=float, default=ITERS_PER_POINT_FALLBACK)
     ap.add_argument("--no-e2e", action="store_true")

@@ -170,6 +170,10 @@ typedef struct {
   int transport_maxit;         /* GMRES restart cycles; 0 -> 50 */
   int warm_start;              /* 1: first transport solve starts from the resident rho */
   int restart_from_phi0;       /* 1: reset phi to the phi0 of wg_gummel_set (device copy) */
+  double inexact_factor;       /* > 0: inexact Gummel, transport tol = clamp(factor * defect[V], transport_tol,
+                                  inexact_cap) per problem; convergence is only accepted after a solve at
+                                  transport_tol with the same potential.  0: fixed transport_tol (reference) */
+  double inexact_cap;          /* loosest transport tolerance of the inexact mode; 0 -> 1e-4 */
 } wg_gummel_opts;
 
 enum { WG_GUMMEL_CONVERGED = 0, WG_GUMMEL_ITERATION_LIMIT = 1, WG_GUMMEL_TRANSPORT_FAILED = 2,
@@ -227,14 +231,17 @@ int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, i
 
 /* Kernel-class profiler (the reference's tic/toc solveInfo timings,
  * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).
- * Classes: flux, forward GEMM, xi stencil, backward GEMM, k-line
- * preconditioner, Krylov (Gram-Schmidt + Givens per iteration), other. */
-enum { WG_PROF_FLUX = 0, WG_PROF_GEMM_FWD, WG_PROF_STENCIL, WG_PROF_GEMM_BWD, WG_PROF_PRECOND, WG_PROF_KRYLOV,
-       WG_PROF_OTHER, WG_PROF_N };
+ * Classes: upwind flux, FP64 transform GEMMs, BF16 tensor-core GEMMs, xi stencil,
+ * k-line preconditioner, Gram-Schmidt multi-dot, Gram-Schmidt update, small
+ * Krylov kernels (reductions, normalisation, Givens), other. */
+enum { WG_PROF_FLUX = 0, WG_PROF_GEMM_F64, WG_PROF_GEMM_BF16, WG_PROF_STENCIL, WG_PROF_PRECOND, WG_PROF_MULTIDOT,
+       WG_PROF_GSUPDATE, WG_PROF_KRYLOV, WG_PROF_OTHER, WG_PROF_N };
 int wg_profile_enable(wg_problem* h, int on);
 /* ms[i]: summed event time of class i; timed[i]: timed launches; launches[i]:
- * kernel launches of class i since the last reset (always counted). */
-int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, int reset);
+ * kernel launches of class i since the last reset (always counted); bytes[i] and
+ * flops[i]: algorithmic bytes and flops of the timed launches (any may be NULL). */
+int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, double* bytes, double* flops,
+                    int reset);
 
 /* CUDA events on the handle's stream (16 slots): device-side timing of any
  * sequence of calls.  wg_event_elapsed waits for slot b. */

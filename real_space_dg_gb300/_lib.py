@@ -53,7 +53,8 @@ class WgRtd1D(C.Structure):
 class WgGummelOpts(C.Structure):
     _fields_ = [("max_iterations", C.c_int), ("mixing", C.c_double), ("potential_tol", C.c_double),
                 ("density_tol", C.c_double), ("poisson_residual_tol", C.c_double), ("transport_tol", C.c_double),
-                ("transport_maxit", C.c_int), ("warm_start", C.c_int), ("restart_from_phi0", C.c_int)]
+                ("transport_maxit", C.c_int), ("warm_start", C.c_int), ("restart_from_phi0", C.c_int),
+                ("inexact_factor", C.c_double), ("inexact_cap", C.c_double)]
 
 
 class WgGummelInfo(C.Structure):
@@ -104,9 +105,9 @@ SIGNATURES = {
     "wg_event_record": ([_H, C.c_int], C.c_int),
     "wg_event_elapsed": ([_H, C.c_int, C.c_int, _D], C.c_int),
     "wg_profile_enable": ([_H, C.c_int], C.c_int),
-    "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.c_int], C.c_int),
+    "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _D, _D, C.c_int], C.c_int),
 }
-PROF_CLASSES = ["flux", "gemm_fwd", "stencil", "gemm_bwd", "precond", "krylov", "other"]
+PROF_CLASSES = ["flux", "gemm_f64", "gemm_bf16", "stencil", "precond", "multidot", "gs_update", "krylov_small", "other"]
 
 _lib = None
 

@@ -525,7 +525,8 @@ int wg_profile_enable(wg_problem* h, int on) {
   return WG_OK;
 }
 
-int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, int reset) {
+int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, double* bytes, double* flops,
+                    int reset) {
   if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
   wg::Problem& P = h->P;
   API_CK(&P, wg::prof_collect(P));
@@ -533,12 +534,16 @@ int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* laun
     if (ms) ms[i] = P.prof.ms[i];
     if (timed) timed[i] = P.prof.timed[i];
     if (launches) launches[i] = P.prof.launches[i];
+    if (bytes) bytes[i] = P.prof.bytes[i];
+    if (flops) flops[i] = P.prof.flops[i];
   }
   if (reset)
     for (int i = 0; i < wg::PROF_N; ++i) {
       P.prof.ms[i] = 0;
       P.prof.timed[i] = 0;
       P.prof.launches[i] = 0;
+      P.prof.bytes[i] = 0;
+      P.prof.flops[i] = 0;
     }
   return WG_OK;
 }

@@ -473,20 +473,27 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   WG_CK(prec(V + (long long)k * N, (long long)mp1 * N));
   WG_CK(apply());
   const int nv = k + 1;
-  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 9);
+  const double sz = (double)sizeof(T), vec = (double)N * B * sz;
   const dim3 gu((unsigned)((N + 255) / 256), B);
   for (int pass = 0; pass < 2; ++pass) {
+    cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B);
     multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double2) * 8 * nv, P.stream>>>(V, w, P.partial, P.active, N, nv,
                                                                                      mp1, ps, P.nchunk);
+    prof_end(P, PROF_MULTIDOT, ev);
+    ev = prof_begin(P, PROF_KRYLOV);
     dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, coef_col32<T>(P), P.H, P.active, nv, k, ps, mm,
                                                P.nchunk, pass == 0);
+    prof_end(P, PROF_KRYLOV, ev);
+    ev = prof_begin(P, PROF_GSUPDATE, 1, (nv + 2) * vec, 8.0 * nv * N * B);
     if (pass == 0)
       gs_update_kernel<T, false><<<gu, 256, 0, P.stream>>>(V, w, coef_col<T>(P), P.active, nullptr, N, nv, mp1, ps,
                                                           P.nblk);
     else
       gs_update_kernel<T, true><<<gu, 256, 0, P.stream>>>(V, w, coef_col<T>(P), P.active, P.nrm_partial, N, nv, mp1,
                                                          ps, P.nblk);
+    prof_end(P, PROF_GSUPDATE, ev);
   }
+  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 3, 2 * vec);
   norm_reduce_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, P.H, P.active, P.nblk, k, ps, mm, P.inv64,
                                              P.mx.inv);
   if (sizeof(T) == sizeof(float2))
@@ -528,7 +535,7 @@ int solve_begin(Problem& P, double tol, bool warm, std::vector<double>& bnorm, s
   WG_CK(cudaMemcpyAsync(bnorm.data(), P.nrm, sizeof(double) * B, cudaMemcpyDeviceToHost, P.stream));
   WG_CK(cudaStreamSynchronize(P.stream));
   tgt.resize(B);
-  for (int b = 0; b < B; ++b) tgt[b] = tol * bnorm[b];
+  for (int b = 0; b < B; ++b) tgt[b] = (P.tol_pp.empty() ? tol : P.tol_pp[b]) * bnorm[b];
   int rc = true_residual(P);
   if (rc) return rc;
   res.resize(B);

@@ -227,12 +227,12 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
   }
 }
 
-// phi <- phi + alpha (cand - phi); nprev <- n  for problems flagged in mix[b].
+// mix[b] == 1: phi <- phi + alpha (cand - phi) and nprev <- n;  mix[b] == 2: nprev <- n only.
 __global__ void mix_kernel(const GummelDev G, const int* __restrict__ mix, double alpha, int nx, int ncol) {
   const int b = blockIdx.y;
   if (!mix[b]) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < nx) {
+  if (i < nx && mix[b] == 1) {
     const long long o = (long long)b * nx + i;
     G.phi[o] = G.phi[o] + alpha * (G.cand[o] - G.phi[o]);
   }
@@ -415,6 +415,16 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
   wg_solve_opts so{};
   so.tol = o.transport_tol > 0 ? o.transport_tol : 1e-8;
   so.maxit = o.transport_maxit > 0 ? o.transport_maxit : 50;
+  // Inexact Gummel (opt-in): transport tolerance tied to the potential defect,
+  // tol_b = clamp(factor * defect_b, final tol, cap); convergence is accepted only
+  // after a transport solve at the final tolerance with the same potential.
+  const bool inexact = o.inexact_factor > 0;
+  const double cap = o.inexact_cap > 0 ? o.inexact_cap : 1e-4;
+  std::vector<double> tolb(B, inexact ? std::max(cap, so.tol) : so.tol);
+  struct TolGuard {
+    Problem& P;
+    ~TolGuard() { P.tol_pp.clear(); }
+  } guard{P};
   for (int it = 1; it <= maxit; ++it) {
     bool any = false;
     for (int b = 0; b < B; ++b) any |= active[b] != 0;
@@ -424,6 +434,7 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
     potential_from_phi_kernel<<<dim3((nx + 255) / 256, B), 256, 0, P.stream>>>(G.vc, G.phi, P.pot_v, G.active, nx);
     GK(cudaGetLastError());
     GK(launch_potential_update(P, 0, B));
+    P.tol_pp = tolb;
     int rc = solve_dispatch(P, so, /*warm=*/true, sinfo.data());
     if (rc != WG_OK && rc != WG_NOT_CONVERGED) return rc;
     P.prof.launches[PROF_OTHER] += 2;
@@ -456,7 +467,8 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
         active[b] = 0;
         continue;
       }
-      if (in.potential_defect <= tol_v && in.density_change <= tol_n && in.poisson_relres <= tol_p) {
+      const bool conv = in.potential_defect <= tol_v && in.density_change <= tol_n && in.poisson_relres <= tol_p;
+      if (conv && tolb[b] <= so.tol) {
         in.status = WG_GUMMEL_CONVERGED;
         active[b] = 0;
         continue;
@@ -465,6 +477,13 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
         active[b] = 0;  // never hand back a potential newer than the transport state
         continue;
       }
+      if (conv) {
+        // converged on a loose transport solve: re-solve at the final tolerance, same potential
+        tolb[b] = so.tol;
+        mix[b] = 2;
+        continue;
+      }
+      if (inexact) tolb[b] = std::min(cap, std::max(so.tol, o.inexact_factor * in.potential_defect));
       mix[b] = 1;
     }
     GK(cudaMemcpyAsync(G.mix, mix.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));

@@ -303,24 +303,26 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
     xb = M.xin16;
     P.prof.launches[PROF_OTHER] += 1;
   }
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX);
+  const double ncols = (double)P.ncols, nxi = s.nxi, nkd = s.nk;
+  const double gemm_flops = 2.0 * (2 * nxi) * (2 * nkd) * ncols;
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 16.0 * BN);
   flux32_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, M.kvec, M.qd, M.fb, s.n_el, s.nk,
                                                                             total);
   prof_end(P, PROF_FLUX, ev);
-  ev = prof_begin(P, PROF_GEMM_FWD);
+  ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * BN + 8.0 * nxi * ncols, gemm_flops);
   // GEMM 1 reads its B operand through the tensor map of whichever bf16 buffer holds x
   cudaError_t e = launch_gemm<0>(M.tmA1, xb == M.xin16 ? M.tmB1 : M.tmB1z, reinterpret_cast<float*>(M.xh), 2 * s.nxi,
                                  P.ncols, 2 * s.nk, M.err, P.stream);
-  prof_end(P, PROF_GEMM_FWD, ev);
+  prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
   const long long nelem = (long long)P.batch * s.n_el;
-  ev = prof_begin(P, PROF_STENCIL);
+  ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * NK * NK * (nxi + 1));
   stencil32_kernel<NK><<<(unsigned)((nelem * s.nxi + 255) / 256), 256, 0, P.stream>>>(
       reinterpret_cast<const float2*>(M.xh), M.yh16, M.beta, M.betai, s.nxi, nelem);
   prof_end(P, PROF_STENCIL, ev);
-  ev = prof_begin(P, PROF_GEMM_BWD);
+  ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops);
   e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream);
-  prof_end(P, PROF_GEMM_BWD, ev);
+  prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -329,7 +331,7 @@ template <int NK>
 cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb) {
   const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
   dim3 grid((P.s.nk + 31) / 32, P.batch);
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 1, (zb ? 20.0 : 16.0) * P.N * P.batch);
   precond32_kernel<NK><<<grid, 32 * Pw, sizeof(float2) * 2 * Pw * 32, P.stream>>>(
       r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, P.s.n_el, P.s.nk, P.N, r_stride);
   prof_end(P, PROF_PRECOND, ev);

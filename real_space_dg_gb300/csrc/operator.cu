@@ -373,24 +373,26 @@ __global__ void observables_kernel(const double2* __restrict__ rho, const double
 template <int NK>
 cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
   const long long total = (long long)P.batch * P.s.n_el * P.s.nk;
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX);
+  const double BN = (double)P.N * P.batch, ncols = (double)P.ncols, nxi = P.s.nxi, nk = P.s.nk;
+  const double gemm_flops = 8.0 * nxi * nk * ncols;
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * BN);
   flux_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el,
                                                                           P.s.nk, total);
   prof_end(P, PROF_FLUX, ev);
   dim3 g1((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nxi + GBM - 1) / GBM);
-  ev = prof_begin(P, PROF_GEMM_FWD);
+  ev = prof_begin(P, PROF_GEMM_F64, 1, 16.0 * (BN + nxi * ncols), gemm_flops);
   zgemm_kernel<0><<<g1, 256, 0, P.stream>>>(P.phi, P.s.nk, x, P.xh, P.s.nxi, P.s.nk, P.ncols);
-  prof_end(P, PROF_GEMM_FWD, ev);
+  prof_end(P, PROF_GEMM_F64, ev);
   const long long nelem = (long long)P.batch * P.s.n_el;
   const long long st = nelem * P.s.nxi;
-  ev = prof_begin(P, PROF_STENCIL);
+  ev = prof_begin(P, PROF_STENCIL, 1, 32.0 * nxi * ncols + 8.0 * P.batch * P.s.n_el * NK * NK * (nxi + 1));
   stencil_kernel<NK><<<(unsigned)((st + 255) / 256), 256, 0, P.stream>>>(P.xh, P.yh, P.beta, P.betai, P.s.nxi,
                                                                           nelem);
   prof_end(P, PROF_STENCIL, ev);
   dim3 g2((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nk + GBM - 1) / GBM);
-  ev = prof_begin(P, PROF_GEMM_BWD);
+  ev = prof_begin(P, PROF_GEMM_F64, 1, 16.0 * (2 * BN + nxi * ncols), gemm_flops);
   zgemm_kernel<1><<<g2, 256, 0, P.stream>>>(P.phi, P.s.nk, P.yh, y, P.s.nk, P.s.nxi, P.ncols);
-  prof_end(P, PROF_GEMM_BWD, ev);
+  prof_end(P, PROF_GEMM_F64, ev);
   return cudaGetLastError();
 }
 
@@ -399,7 +401,7 @@ cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2
   const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
   dim3 grid((P.s.nk + 31) / 32, P.batch);
   const size_t shm = sizeof(double2) * 2 * Pw * 32;
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 1, 32.0 * P.N * P.batch);
   precond_kernel<NK><<<grid, 32 * Pw, shm, P.stream>>>(r, z, P.kvec, P.pre_dinv, P.pre_h, P.qd, P.s.n_el, P.s.nk,
                                                         P.N, r_stride);
   prof_end(P, PROF_PRECOND, ev);
@@ -408,9 +410,11 @@ cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2
 
 }  // namespace
 
-cudaEvent_t prof_begin(Problem& P, int cls, int n) {
+cudaEvent_t prof_begin(Problem& P, int cls, int n, double bytes, double flops) {
   P.prof.launches[cls] += n;
   if (!P.prof.on) return nullptr;
+  P.prof.pend_bytes.push_back(bytes);
+  P.prof.pend_flops.push_back(flops);
   cudaEvent_t a;
   if (P.prof.pool.empty()) {
     if (cudaEventCreate(&a) != cudaSuccess) return nullptr;
@@ -426,7 +430,12 @@ void prof_end(Problem& P, int cls, cudaEvent_t a) {
   if (!a) return;
   cudaEvent_t b;
   if (P.prof.pool.empty()) {
-    if (cudaEventCreate(&b) != cudaSuccess) { P.prof.pool.push_back(a); return; }
+    if (cudaEventCreate(&b) != cudaSuccess) {
+      P.prof.pool.push_back(a);
+      P.prof.pend_bytes.pop_back();
+      P.prof.pend_flops.pop_back();
+      return;
+    }
   } else {
     b = P.prof.pool.back();
     P.prof.pool.pop_back();
@@ -439,16 +448,21 @@ void prof_end(Problem& P, int cls, cudaEvent_t a) {
 cudaError_t prof_collect(Problem& P) {
   if (P.prof.pending.empty()) return cudaSuccess;
   cudaError_t e = cudaStreamSynchronize(P.stream);
-  for (auto& r : P.prof.pending) {
+  for (size_t i = 0; i < P.prof.pending.size(); ++i) {
+    const auto& r = P.prof.pending[i];
     float ms = 0;
     if (e == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
       P.prof.ms[r.cls] += ms;
       P.prof.timed[r.cls] += 1;
+      P.prof.bytes[r.cls] += P.prof.pend_bytes[i];
+      P.prof.flops[r.cls] += P.prof.pend_flops[i];
     }
     P.prof.pool.push_back(r.a);
     P.prof.pool.push_back(r.b);
   }
   P.prof.pending.clear();
+  P.prof.pend_bytes.clear();
+  P.prof.pend_flops.clear();
   return e;
 }
 

@@ -71,8 +71,8 @@ struct MixedBuffers {
 };
 
 // Kernel classes timed and counted by the profiler.
-enum ProfClass { PROF_FLUX = 0, PROF_GEMM_FWD, PROF_STENCIL, PROF_GEMM_BWD, PROF_PRECOND, PROF_KRYLOV, PROF_OTHER,
-                 PROF_N };
+enum ProfClass { PROF_FLUX = 0, PROF_GEMM_F64, PROF_GEMM_BF16, PROF_STENCIL, PROF_PRECOND, PROF_MULTIDOT,
+                 PROF_GSUPDATE, PROF_KRYLOV, PROF_OTHER, PROF_N };
 
 // CUDA-event timing of kernel classes on the handle's stream (off by default;
 // launch counts are kept always).
@@ -87,6 +87,9 @@ struct Profiler {
   double ms[PROF_N] = {};
   long long timed[PROF_N] = {};
   long long launches[PROF_N] = {};
+  double bytes[PROF_N] = {};   // algorithmic bytes of the timed launches
+  double flops[PROF_N] = {};   // algorithmic flops of the timed launches
+  std::vector<double> pend_bytes, pend_flops;
 };
 
 // Device arrays of the Gummel loop (allocated on the first wg_gummel_set).
@@ -192,11 +195,12 @@ struct Problem {
   GummelDev gd;
   std::vector<GummelHost> gh;
   cudaEvent_t ev[16] = {};       // user event slots (wg_event_record)
+  std::vector<double> tol_pp;    // per-problem relative tolerances for the next solve (empty: opts.tol)
 };
 
 // Profiler helpers (operator.cu).  prof_begin counts `n` launches of class cls
 // and, when timing is on, records a start event; prof_end records the stop event.
-cudaEvent_t prof_begin(Problem& P, int cls, int n = 1);
+cudaEvent_t prof_begin(Problem& P, int cls, int n = 1, double bytes = 0, double flops = 0);
 void prof_end(Problem& P, int cls, cudaEvent_t a);
 cudaError_t prof_collect(Problem& P);
 void prof_release(Problem& P);

@@ -136,13 +136,15 @@ class Problem1D:
 
     def profile(self, on=None, reset=False):
         """Enable/disable kernel timing (on=True/False) and/or read the counters:
-        {class: (ms, timed launches, launches)}."""
+        {class: (ms, timed launches, launches, algorithmic bytes, algorithmic flops)}."""
         if on is not None:
             self._check(self.lib.wg_profile_enable(self.h, 1 if on else 0))
         n = len(_lib.PROF_CLASSES)
         ms = np.zeros(n); timed = (C.c_longlong * n)(); launches = (C.c_longlong * n)()
-        self._check(self.lib.wg_profile_read(self.h, _lib.dptr(ms), timed, launches, 1 if reset else 0))
-        return {c: (ms[i], timed[i], launches[i]) for i, c in enumerate(_lib.PROF_CLASSES)}
+        by = np.zeros(n); fl = np.zeros(n)
+        self._check(self.lib.wg_profile_read(self.h, _lib.dptr(ms), timed, launches, _lib.dptr(by), _lib.dptr(fl),
+                                             1 if reset else 0))
+        return {c: (ms[i], timed[i], launches[i], by[i], fl[i]) for i, c in enumerate(_lib.PROF_CLASSES)}
 
     def event(self, slot):
         """Record CUDA event `slot` on this handle's stream."""

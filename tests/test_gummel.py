@@ -95,3 +95,22 @@ def test_gummel_fixed_point_and_batch_independence(built_lib):
     seq = solve_rtd_self_consistent(mat, biases, opts, mode="sequential")
     assert seq["selfConsistency"]["converged"]
     assert np.abs(seq["sweep"]["phi"] - res["sweep"]["phi"]).max() < 2e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_inexact_gummel_reaches_the_same_fixed_point(built_lib, precision):
+    """Transport tolerance tied to the potential defect (opt-in) converges to the
+    fixed point of the exact loop; the accepted state is solved at 1e-8."""
+    from real_space_dg_gb300 import devices
+    from real_space_dg_gb300.rtd import solve_rtd_self_consistent
+    spec, mat, E, efl, efr, m = small_rtd(n_el=10, nk=32, order=2)
+    mat = dict(mat, dy_norm_nm=devices.density_normalisation_nm(mat))
+    opts = dict(mixing=0.5, potentialTolerance=1e-6, densityTolerance=1e-5, maxIterations=150,
+                transportTolerance=1e-8, transportMaxCycles=60, precision=precision)
+    exact = solve_rtd_self_consistent(mat, [0.05, 0.15], opts)
+    inexact = solve_rtd_self_consistent(mat, [0.05, 0.15], dict(opts, inexactFactor=1e-2, inexactCap=1e-4))
+    assert exact["selfConsistency"]["converged"] and inexact["selfConsistency"]["converged"]
+    assert max(inexact["sweep"]["transport_relres"]) <= 1e-8
+    assert np.abs(inexact["sweep"]["phi"] - exact["sweep"]["phi"]).max() < 1e-5
+    assert sum(inexact["sweep"]["gmres_iterations"]) < sum(exact["sweep"]["gmres_iterations"])
