@@ -7,7 +7,11 @@ barrier 0.27 eV x 3 nm around a 5 nm well; DG p=3, 240 elements, Nk=256 (245,760
 complex unknowns per bias point); Gummel mixing 0.3, potential tolerance 1e-6 V;
 every transport solve to a 1e-8 relative residual.  One step = one batch of
 `--batch` bias points (0.2 V * (1..B)/B) solved from a cold start to the Gummel
-fixed point, all points advancing together in one handle.
+fixed point, all points advancing together in one handle.  Default form: mixed
+precision (BF16 tensor-core transforms inside FP64 refinement) with the inexact
+Gummel schedule (transport tolerance tied to the potential defect, every
+accepted state re-solved at 1e-8); ``--precision fp64 --inexact 0`` is the
+plain drop-in form.
 
 Arms: default (ours, this library on the GPU) and ``--impl reference`` (the CPU
 restatement of the reference algorithm, timed on a bounded sample).
@@ -172,6 +176,8 @@ def run_ours(args, rank, world, dist):
     spec, mat, biases = make_workload(args.batch)
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
                 innerTol=args.inner_tol, inexactFactor=args.inexact)
+    if args.max_gummel:
+        opts["maxIterations"] = args.max_gummel      # profiling runs only: points need not converge
     S = RTDSweep(mat, args.batch, opts)
     for b, v in enumerate(biases):
         S.set(b, v)
@@ -298,12 +304,14 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--restart", type=int, default=50)
     ap.add_argument("--inner-restart", type=int, default=40)
     ap.add_argument("--inner-tol", type=float, default=1e-3)
-    ap.add_argument("--inexact", type=float, default=0.0,
+    ap.add_argument("--max-gummel", type=int, default=0,
+                    help="cap on Gummel iterations for profiling runs (0: run to convergence)")
+    ap.add_argument("--inexact", type=float, default=1e-2,
                     help="inexact Gummel factor (transport tol = factor * potential defect); 0 = fixed 1e-8")
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--iters-per-point", type=float, default=ITERS_PER_POINT_FALLBACK)

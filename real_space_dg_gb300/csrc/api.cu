@@ -410,9 +410,15 @@ int wg_apply(wg_problem* h, const double* x, double* y) {
   wg::Problem& P = h->P;
   const long long n = P.N * P.batch;
   API_CK(&P, cudaMemcpyAsync(P.z, x, sizeof(double2) * n, cudaMemcpyHostToDevice, P.stream));
-  API_CK(&P, wg::launch_apply(P, P.z, P.w));
+  if (P.precision == WG_PREC_MIXED) API_CK(&P, wg::launch_apply_f64_tc(P, P.z, P.w));
+  else API_CK(&P, wg::launch_apply(P, P.z, P.w));
   API_CK(&P, cudaMemcpyAsync(y, P.w, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
+  if (P.precision == WG_PREC_MIXED) {
+    int herr = 0;
+    API_CK(&P, cudaMemcpy(&herr, P.mx.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) return fail(&P, WG_ERR_TIMEOUT, "wg_apply: tensor-core GEMM barrier wait timed out");
+  }
   return WG_OK;
 }
 
@@ -497,6 +503,14 @@ int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, i
   std::string err;
   const int rc = wg::debug_gemm_bf16(A, B, C, M, N, K, err);
   if (rc) return fail(nullptr, rc, "wg_debug_gemm_bf16: " + err);
+  return WG_OK;
+}
+
+int wg_debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K) {
+  if (!A || !B || !C) return fail(nullptr, WG_ERR_ARG, "wg_debug_gemm_f64_tc: null argument");
+  std::string err;
+  const int rc = wg::debug_gemm_f64_tc(A, B, C, M, N, K, err);
+  if (rc) return fail(nullptr, rc, "wg_debug_gemm_f64_tc: " + err);
   return WG_OK;
 }
 

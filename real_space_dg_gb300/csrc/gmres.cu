@@ -59,6 +59,13 @@ struct Acc64 {
     }
   }
   __device__ __forceinline__ double2 get() const { return v; }
+  // block-level staging: one slot of 4 doubles per warp
+  __device__ __forceinline__ void stage(double* slot) const { slot[0] = v.x; slot[1] = v.y; }
+  __device__ __forceinline__ static double2 combine(const double* slots, int n) {
+    double2 r = make_double2(0, 0);
+    for (int q = 0; q < n; ++q) { r.x += slots[4 * q]; r.y += slots[4 * q + 1]; }
+    return r;
+  }
 };
 
 struct AccF32 {
@@ -87,6 +94,21 @@ struct AccF32 {
   }
   __device__ __forceinline__ double2 get() const {
     return make_double2((double)rh + (double)rl, (double)ih + (double)il);
+  }
+  // Block-level staging keeps the double-float pairs in FP32 (no FP64 instruction per warp);
+  // combine() merges the warps' pairs in FP32 and converts once.
+  __device__ __forceinline__ void stage(double* slot) const {
+    float* f = reinterpret_cast<float*>(slot);
+    f[0] = rh; f[1] = rl; f[2] = ih; f[3] = il;
+  }
+  __device__ __forceinline__ static double2 combine(const double* slots, int n) {
+    AccF32 a;
+    for (int q = 0; q < n; ++q) {
+      const float* f = reinterpret_cast<const float*>(slots + 4 * q);
+      merge(a.rh, a.rl, f[0], f[1]);
+      merge(a.ih, a.il, f[2], f[3]);
+    }
+    return a.get();
   }
 };
 
@@ -155,7 +177,7 @@ template <typename T>
 __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, const T* __restrict__ w,
                                                        double2* __restrict__ partial, const int* __restrict__ active,
                                                        long long N, int nv, int mp1, int pstride, int nchunk) {
-  extern __shared__ double2 red[];  // [nv][8]
+  extern __shared__ double red[];  // [nv][8 warps][4 doubles]
   const int b = blockIdx.y, c = blockIdx.x;
   if (!active[b]) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -177,18 +199,11 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
       if (n < N) a.add_cdot(v[n], wv[j]);
     }
     a.warp_reduce();
-    if (lane == 0) red[i * 8 + warp] = a.get();
+    if (lane == 0) a.stage(red + (i * 8 + warp) * 4);
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < nv; i += blockDim.x) {
-    double2 s = make_double2(0, 0);
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      s.x += red[i * 8 + q].x;
-      s.y += red[i * 8 + q].y;
-    }
-    partial[((long long)b * pstride + i) * nchunk + c] = s;
-  }
+  for (int i = threadIdx.x; i < nv; i += blockDim.x)
+    partial[((long long)b * pstride + i) * nchunk + c] = AccFor<T>::type::combine(red + i * 8 * 4, 8);
 }
 
 // hcol[b][i] = sum_c partial; H[b][k][i] (+)= hcol          grid (B), block 256
@@ -237,15 +252,12 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
     if (NORM) a.add_norm(acc);
   }
   if (NORM) {
-    __shared__ double wsum[8];
+    __shared__ double wsum[8 * 4];
     a.warp_reduce();
-    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = a.get().x;
+    if ((threadIdx.x & 31) == 0) a.stage(wsum + (threadIdx.x >> 5) * 4);
     __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0;
-      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += wsum[q];
-      nrm_partial[(long long)b * nblk + blockIdx.x] = t;
-    }
+    if (threadIdx.x == 0)
+      nrm_partial[(long long)b * nblk + blockIdx.x] = AccFor<T>::type::combine(wsum, blockDim.x >> 5).x;
   }
 }
 
@@ -477,8 +489,8 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   const dim3 gu((unsigned)((N + 255) / 256), B);
   for (int pass = 0; pass < 2; ++pass) {
     cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B);
-    multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double2) * 8 * nv, P.stream>>>(V, w, P.partial, P.active, N, nv,
-                                                                                     mp1, ps, P.nchunk);
+    multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, P.active, N,
+                                                                                      nv, mp1, ps, P.nchunk);
     prof_end(P, PROF_MULTIDOT, ev);
     ev = prof_begin(P, PROF_KRYLOV);
     dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, coef_col32<T>(P), P.H, P.active, nv, k, ps, mm,
@@ -514,7 +526,8 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
 int true_residual(Problem& P) {
   const long long tot = P.N * P.batch;
   P.prof.launches[PROF_OTHER] += 3;
-  WG_CK(launch_apply(P, P.x, P.w));
+  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w));
+  else WG_CK(launch_apply(P, P.x, P.w));
   residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot);
   norm_partial_kernel<double2><<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk);
   norm_reduce_kernel<<<P.batch, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, nullptr, P.active, P.nchunk, 0, 0, 0,

@@ -13,10 +13,13 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include "ozaki.cuh"
 #include "problem.h"
 #include "tc_gemm.cuh"
 
@@ -54,6 +57,62 @@ bool make_map(CUtensorMap* m, const void* base, long long rows, int K, int box_r
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// bf16 digit stack [S][rows][K] (K-major), 64 x box_rows x 1 boxes, 128-byte swizzle.
+bool make_map3(CUtensorMap* m, const void* base, long long rows, int K, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)oz::S};
+  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)K * 2 * (cuuint64_t)rows};
+  cuuint32_t box[3] = {(cuuint32_t)oz::BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Digits of the rows of a row-major M x K FP64 matrix (host), the split of
+// slice_columns_kernel: row r with max|a| < 2^m has F = round(a 2^(6S-1-m)) written
+// in balanced base-64 digits, a = 2^e[r] sum_p t_p 2^(-6(p+1)), e[r] = m + 1.
+void slice_rows_host(const std::vector<double>& A, int M, int K, std::vector<bf16>& dig, std::vector<int>& e) {
+  dig.assign((size_t)oz::S * M * K, __float2bfloat16(0.f));
+  e.assign(M, 0);
+  for (int r = 0; r < M; ++r) {
+    double mx = 0;
+    for (int k = 0; k < K; ++k) mx = std::max(mx, std::fabs(A[(size_t)r * K + k]));
+    if (mx == 0) continue;
+    int m;
+    std::frexp(mx, &m);   // mx = f 2^m, 0.5 <= f < 1
+    e[r] = m + 1;
+    for (int k = 0; k < K; ++k) {
+      const double a = A[(size_t)r * K + k];
+      // |a| 2^(6S-1-m) < 2^47: adding one half is exact
+      long long F = (long long)std::floor(std::ldexp(std::fabs(a), oz::BETA * oz::S - 1 - m) + 0.5);
+      if (a < 0) F = -F;
+      for (int p = oz::S - 1; p > 0; --p) {
+        const long long d = ((F + 32) & 63) - 32;
+        dig[((size_t)p * M + r) * K + k] = __float2bfloat16((float)d);
+        F = (F - d) >> oz::BETA;
+      }
+      dig[(size_t)r * K + k] = __float2bfloat16((float)F);
+    }
+  }
+}
+
+template <int EPI>
+cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* ea, const int* eb, double* C, int M,
+                         long long Ncol, int K, int* err, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(oz::gemm_ozaki_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         oz::SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
+  oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err);
+  return cudaGetLastError();
 }
 
 template <int EPI>
@@ -429,13 +488,60 @@ int mixed_alloc(Problem& P) {
     P.err = "cuTensorMapEncodeTiled failed for the BF16 GEMM operands";
     return WG_ERR_CUDA;
   }
+  // FP64 outer residual on the tensor cores when the grouped accumulation stays exact
+  M.ozaki = 2 * nk <= oz::MAX_K && 2 * nxi <= oz::MAX_K;
+  if (M.ozaki) {
+    const int kmax = 2 * std::max(nk, nxi);
+    std::vector<double> A1((size_t)4 * nxi * nk), A2((size_t)4 * nxi * nk);
+    for (int si = 0; si < nxi; ++si)
+      for (int j = 0; j < nk; ++j) {
+        const double pr = s.phi[(size_t)si * nk + j].real(), pi = s.phi[(size_t)si * nk + j].imag();
+        const size_t K1 = 2 * (size_t)nk, K2 = 2 * (size_t)nxi;
+        A1[(2 * si + 0) * K1 + 2 * j + 0] = pr;
+        A1[(2 * si + 0) * K1 + 2 * j + 1] = -pi;
+        A1[(2 * si + 1) * K1 + 2 * j + 0] = pi;
+        A1[(2 * si + 1) * K1 + 2 * j + 1] = pr;
+        A2[(2 * j + 0) * K2 + 2 * si + 0] = pi;
+        A2[(2 * j + 0) * K2 + 2 * si + 1] = -pr;
+        A2[(2 * j + 1) * K2 + 2 * si + 0] = pr;
+        A2[(2 * j + 1) * K2 + 2 * si + 1] = pi;
+      }
+    std::vector<bf16> d1, d2;
+    std::vector<int> e1, e2;
+    slice_rows_host(A1, 2 * nxi, 2 * nk, d1, e1);
+    slice_rows_host(A2, 2 * nk, 2 * nxi, d2, e2);
+    cudaError_t ce = cudaSuccess;
+    auto C2 = [&](cudaError_t r) { if (ce == cudaSuccess) ce = r; };
+    C2(cudaMalloc(&M.oa1, sizeof(bf16) * d1.size()));
+    C2(cudaMalloc(&M.oa2, sizeof(bf16) * d2.size()));
+    C2(cudaMalloc(&M.ea1, sizeof(int) * e1.size()));
+    C2(cudaMalloc(&M.ea2, sizeof(int) * e2.size()));
+    C2(cudaMalloc(&M.ob, sizeof(bf16) * (size_t)oz::S * P.ncols * kmax));
+    C2(cudaMalloc(&M.eb, sizeof(int) * (size_t)P.ncols));
+    C2(cudaMemcpy(M.oa1, d1.data(), sizeof(bf16) * d1.size(), cudaMemcpyHostToDevice));
+    C2(cudaMemcpy(M.oa2, d2.data(), sizeof(bf16) * d2.size(), cudaMemcpyHostToDevice));
+    C2(cudaMemcpy(M.ea1, e1.data(), sizeof(int) * e1.size(), cudaMemcpyHostToDevice));
+    C2(cudaMemcpy(M.ea2, e2.data(), sizeof(int) * e2.size(), cudaMemcpyHostToDevice));
+    if (ce != cudaSuccess) {
+      P.err = std::string("FP64 tensor-core buffers: ") + cudaGetErrorString(ce);
+      return ce == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
+    }
+    P.device_bytes += 2.0 * (d1.size() + d2.size()) + 4.0 * (e1.size() + e2.size()) +
+                      2.0 * oz::S * P.ncols * kmax + 4.0 * P.ncols;
+    ok = make_map3(&M.tmOA1, M.oa1, 2 * nxi, 2 * nk, oz::BM) && make_map3(&M.tmOA2, M.oa2, 2 * nk, 2 * nxi, oz::BM) &&
+         make_map3(&M.tmOB1, M.ob, P.ncols, 2 * nk, oz::BN) && make_map3(&M.tmOB2, M.ob, P.ncols, 2 * nxi, oz::BN);
+    if (!ok) {
+      P.err = "cuTensorMapEncodeTiled failed for the FP64 tensor-core operands";
+      return WG_ERR_CUDA;
+    }
+  }
   return WG_OK;
 }
 
 void mixed_free(Problem& P) {
   MixedBuffers& M = P.mx;
   void* ptrs[] = {M.phi1, M.phi2, M.xin16, M.zb16, M.yh16, M.xh, M.V, M.w, M.z, M.r, M.d, M.beta, M.betai, M.err,
-                  M.kvec, M.qd, M.dinv, M.h, M.hcol, M.y, M.inv};
+                  M.kvec, M.qd, M.dinv, M.h, M.hcol, M.y, M.inv, M.oa1, M.oa2, M.ea1, M.ea2, M.ob, M.eb};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   M = MixedBuffers{};
@@ -532,6 +638,93 @@ int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int 
   cudaFree(da);
   cudaFree(db);
   cudaFree(dc);
+  cudaFree(derr);
+  return rc;
+}
+
+// FP64 operator apply of the mixed form's outer residual: flux and xi stencil in
+// FP64, both transforms as digit-sliced FP64 GEMMs on the tensor cores.
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y) {
+  MixedBuffers& M = P.mx;
+  if (!M.ozaki) return launch_apply(P, x, y);
+  const Shape& s = P.s;
+  const int K1 = 2 * s.nk, K2 = 2 * s.nxi;
+  const double ncols = (double)P.ncols;
+  cudaError_t e = launch_flux_f64(P, x, y);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t ev = prof_begin(P, PROF_GEMM_F64, 2, 8.0 * P.N * P.batch + 16.0 * s.nxi * ncols,
+                              8.0 * s.nxi * s.nk * ncols);
+  oz::slice_columns_kernel<<<(unsigned)P.ncols, 256, 0, P.stream>>>(reinterpret_cast<const double*>(x), K1, P.ncols,
+                                                                    M.ob, M.eb);
+  e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
+                      P.stream);
+  prof_end(P, PROF_GEMM_F64, ev);
+  if (e != cudaSuccess) return e;
+  e = launch_stencil_f64(P, P.xh, P.yh);
+  if (e != cudaSuccess) return e;
+  ev = prof_begin(P, PROF_GEMM_F64, 2, 16.0 * s.nxi * ncols + 16.0 * P.N * P.batch, 8.0 * s.nxi * s.nk * ncols);
+  oz::slice_columns_kernel<<<(unsigned)P.ncols, 256, 0, P.stream>>>(reinterpret_cast<const double*>(P.yh), K2,
+                                                                    P.ncols, M.ob, M.eb);
+  e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream);
+  prof_end(P, PROF_GEMM_F64, ev);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// Stand-alone digit-sliced FP64 GEMM for diagnostics: C = A B with A row-major M x K,
+// B column-major K x N, C column-major M x N (host FP64 buffers), K <= 512, K % 8 == 0.
+int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err) {
+  if (M < 1 || N < 1 || K < 64 || K % 8 || K > oz::MAX_K) {
+    err = "debug FP64 GEMM needs 64 <= K <= 512 and K % 8 == 0";
+    return WG_ERR_ARG;
+  }
+  std::vector<double> a(A, A + (size_t)M * K);
+  std::vector<bf16> da_h;
+  std::vector<int> ea_h;
+  slice_rows_host(a, M, K, da_h, ea_h);
+  bf16 *da = nullptr, *db = nullptr;
+  double *dB = nullptr, *dC = nullptr;
+  int *dea = nullptr, *deb = nullptr, *derr = nullptr;
+  cudaError_t e = cudaMalloc(&da, sizeof(bf16) * da_h.size());
+  if (e == cudaSuccess) e = cudaMalloc(&db, sizeof(bf16) * (size_t)oz::S * N * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dB, sizeof(double) * (size_t)N * K);
+  if (e == cudaSuccess) e = cudaMalloc(&dC, sizeof(double) * (size_t)M * N);
+  if (e == cudaSuccess) e = cudaMalloc(&dea, sizeof(int) * M);
+  if (e == cudaSuccess) e = cudaMalloc(&deb, sizeof(int) * N);
+  if (e == cudaSuccess) e = cudaMalloc(&derr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(da, da_h.data(), sizeof(bf16) * da_h.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dea, ea_h.data(), sizeof(int) * M, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(dB, B, sizeof(double) * (size_t)N * K, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+  int rc = WG_OK;
+  if (e == cudaSuccess) {
+    CUtensorMap ma, mb;
+    if (!make_map3(&ma, da, M, K, oz::BM) || !make_map3(&mb, db, N, K, oz::BN)) {
+      err = "cuTensorMapEncodeTiled failed";
+      rc = WG_ERR_CUDA;
+    } else {
+      oz::slice_columns_kernel<<<N, 256>>>(dB, K, N, db, deb);
+      e = launch_ozaki<0>(ma, mb, dea, deb, dC, M, N, K, derr, 0);
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      int herr = 0;
+      if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+      if (e == cudaSuccess) e = cudaMemcpy(C, dC, sizeof(double) * (size_t)M * N, cudaMemcpyDeviceToHost);
+      if (herr) {
+        err = "FP64 tensor-core GEMM barrier wait timed out";
+        rc = WG_ERR_TIMEOUT;
+      }
+    }
+  }
+  if (e != cudaSuccess) {
+    err = std::string("CUDA: ") + cudaGetErrorString(e);
+    rc = WG_ERR_CUDA;
+  }
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dB);
+  cudaFree(dC);
+  cudaFree(dea);
+  cudaFree(deb);
   cudaFree(derr);
   return rc;
 }

@@ -480,6 +480,34 @@ cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
   }
 }
 
+cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y) {
+  const long long total = (long long)P.batch * P.s.n_el * P.s.nk;
+  const unsigned g = (unsigned)((total + 255) / 256);
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * P.N * P.batch);
+  switch (P.s.nK) {
+    case 2: flux_kernel<2><<<g, 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el, P.s.nk, total); break;
+    case 3: flux_kernel<3><<<g, 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el, P.s.nk, total); break;
+    default: flux_kernel<4><<<g, 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el, P.s.nk, total); break;
+  }
+  prof_end(P, PROF_FLUX, ev);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh) {
+  const long long nelem = (long long)P.batch * P.s.n_el;
+  const unsigned g = (unsigned)((nelem * P.s.nxi + 255) / 256);
+  const int nK = P.s.nK;
+  cudaEvent_t ev = prof_begin(P, PROF_STENCIL, 1,
+                              32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1));
+  switch (nK) {
+    case 2: stencil_kernel<2><<<g, 256, 0, P.stream>>>(xh, yh, P.beta, P.betai, P.s.nxi, nelem); break;
+    case 3: stencil_kernel<3><<<g, 256, 0, P.stream>>>(xh, yh, P.beta, P.betai, P.s.nxi, nelem); break;
+    default: stencil_kernel<4><<<g, 256, 0, P.stream>>>(xh, yh, P.beta, P.betai, P.s.nxi, nelem); break;
+  }
+  prof_end(P, PROF_STENCIL, ev);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z) {
   switch (P.s.nK) {
     case 2: return precond_nk<2>(P, r, r_stride, z);

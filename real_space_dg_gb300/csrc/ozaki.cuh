@@ -1,0 +1,230 @@
+// FP64 GEMM emulated on the BF16 tensor cores (Ozaki splitting), sm_103a.
+//
+//   C (M x Ncol, fp64, column-major)  (=|+=)  A (M x K, fp64)  *  B (K x Ncol, fp64, column-major)
+//
+// Each row of A and each column of B is scaled by a power of two and rounded to
+// an integer F with |F| <= 2^(6S-1), which is written in S balanced base-64
+// digits: a = 2^e sum_p t_p 2^(-6(p+1)), |t_p| <= 32 (|t_0| <= 33).  The digits
+// are exact in BF16 and a digit product summed over K <= 512 stays below 2^20, so
+// every product A^(p) B^(q) is EXACT in the FP32 tensor-core accumulator.
+// Products of equal weight p+q (at most 8 of them) share one TMEM accumulator
+// (< 2^23, still exact); the S groups of a 128 x 64 output tile use 8 x 64 = 512
+// TMEM columns.  Products of weight p+q >= S are dropped.  The epilogue adds the
+// groups in double-float FP32 arithmetic (exact power-of-two scalings, TwoSum),
+// converts once to FP64 and applies the row and column exponents with integer
+// arithmetic.  Error: a few 2^(-6S) (S = 8: ~1e-14) relative to |A| |B|,
+// unbiased (rounded split).
+#pragma once
+#include "tc_gemm.cuh"
+
+namespace wg {
+namespace oz {
+
+constexpr int S = 8;              // digits per operand
+constexpr int BETA = 6;           // bits per digit
+constexpr int BM = 128, BN = 64, BK = 64;
+constexpr int NGROUP = S;         // weights p+q = 2 .. S+1
+constexpr int A_SLICE = BM * BK * 2;      // 16 KiB
+constexpr int B_SLICE = BN * BK * 2;      // 8 KiB
+constexpr int STAGE = S * (A_SLICE + B_SLICE);
+constexpr int SMEM_BYTES = STAGE + 1024 + 256;
+constexpr int MAX_K = 512;        // exactness bound of the grouped accumulation
+
+// Instruction descriptor: D f32, A/B bf16, K-major, M = 128, N = 64.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                            ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(tc::smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(tc::smem_u32(bar))
+      : "memory");
+}
+
+// (hi, lo) += v exactly-rounded in double-float arithmetic.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float v) {
+  const float s = __fadd_rn(hi, v);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+  const float t = __fadd_rn(lo, e);
+  hi = __fadd_rn(s, t);
+  lo = __fsub_rn(t, __fsub_rn(hi, s));
+}
+
+// x * 2^e for a finite double by exponent arithmetic (no FP64 instruction); zero stays zero.
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+  long long bits = __double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  if (ex == 0) return 0.0;
+  const int ne = ex + e;
+  if (ne <= 0) return 0.0;
+  if (ne >= 0x7FF) return x > 0 ? INFINITY : -INFINITY;
+  bits = (bits & ~(0x7FFll << 52)) | ((long long)ne << 52);
+  return __longlong_as_double(bits);
+}
+
+// EPI 0: C = A B.  EPI 1: C += A B.   ea[row], eb[col]: power-of-two exponents of A's rows and B's columns.
+template <int EPI>
+__global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                            const __grid_constant__ CUtensorMap tmB,
+                                                            const int* __restrict__ ea, const int* __restrict__ eb,
+                                                            double* __restrict__ C, int M, long long Ncol, int K,
+                                                            int* __restrict__ err) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sa = smem;                       // [S][BM][BK] bf16
+  uint8_t* sb = smem + S * A_SLICE;         // [S][BN][BK] bf16
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGE);
+  uint64_t* empty = full + 1;
+  uint64_t* done = empty + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * BM;
+  const long long n0 = (long long)blockIdx.y * BN;
+  const int nkb = (K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    tc::mbar_init(full, 1);
+    tc::mbar_init(empty, 1);
+    tc::mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tc::tmem_alloc(tmem_slot, 512);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    for (int kb = 0; kb < nkb; ++kb) {
+      if (kb > 0 && !tc::mbar_wait(empty, (kb - 1) & 1, err)) break;
+      tc::mbar_expect_tx(full, STAGE);
+      for (int p = 0; p < S; ++p) {
+        tma_load_3d(sa + p * A_SLICE, &tmA, kb * BK, m0, p, full);
+        tma_load_3d(sb + p * B_SLICE, &tmB, kb * BK, (int)n0, p, full);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    for (int kb = 0; kb < nkb; ++kb) {
+      if (!tc::mbar_wait(full, kb & 1, err)) break;
+      tc::fence_after();
+      for (int p = 0; p < S; ++p)
+        for (int q = 0; q + p < S; ++q) {        // weight p+q (0-based) <= S-1
+          const int g = p + q;
+          const uint32_t d = tmem + (uint32_t)(g * BN);
+          // group g is first reached with p == 0 (q == g): that product at the first k block
+          // and k step initialises the accumulator, every other one accumulates
+          const uint8_t* a = sa + p * A_SLICE;
+          const uint8_t* b = sb + q * B_SLICE;
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            const uint32_t acc = (kb > 0 || kk > 0 || p > 0) ? 1u : 0u;
+            tc::mma_bf16(d, tc::sdesc_sw128(a + kk * 32), tc::sdesc_sw128(b + kk * 32), kIdesc, acc);
+          }
+        }
+      tc::mma_commit(empty);
+    }
+    tc::mma_commit(done);
+  }
+  __syncwarp();
+  const bool ok = tc::mbar_wait(done, 0, err);
+  tc::fence_after();
+  if (ok && !*(volatile int*)err) {
+    const int row = m0 + warp * 32 + lane;
+    const int er = row < M ? ea[row] : 0;
+#pragma unroll 1
+    for (int cb = 0; cb < BN / 32; ++cb) {
+      float hi[32], lo[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) hi[i] = lo[i] = 0.f;
+      // smallest weights first
+#pragma unroll 1
+      for (int g = NGROUP - 1; g >= 0; --g) {
+        float v[32];
+        tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * BN + cb * 32), v);
+        // weight 2^(-6 (g + 2)) with 1-based digits; exact power-of-two scaling
+        const float w = __int_as_float((127 - BETA * (g + 2)) << 23);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) df_add(hi[i], lo[i], v[i] * w);
+      }
+      if (row < M) {
+        const long long c0 = n0 + cb * 32;
+        const int ncb = (int)min((long long)32, Ncol - c0);
+        double* dst = C + c0 * (long long)M + row;
+        double old[32];
+        if (EPI == 1) {
+#pragma unroll
+          for (int i = 0; i < 32; ++i) old[i] = i < ncb ? dst[(long long)i * M] : 0.0;
+        }
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          if (i < ncb) {
+            const double val = scale_pow2((double)hi[i] + (double)lo[i], er + eb[c0 + i]);
+            dst[(long long)i * M] = EPI == 1 ? old[i] + val : val;
+          }
+        }
+      }
+    }
+  }
+  tc::fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after();
+    tc::tmem_dealloc(tmem, 512);
+  }
+}
+
+// Digits of the columns of a K x Ncol column-major FP64 matrix: for column c with
+// max|x| < 2^m, F = round(x 2^(6S-1-m)) (|F| <= 2^(6S-1)) is split into balanced
+// base-64 digits t_p (p = 0 most significant), x = 2^e sum_p t_p 2^(-6(p+1)) with
+// e = m + 1 written to e_out[c]; t_p goes as bf16 to slices[p][c][k] (K-major).
+// Integer arithmetic on the FP64 bit patterns only.
+__global__ void __launch_bounds__(256) slice_columns_kernel(const double* __restrict__ X, int K, long long Ncol,
+                                                            __nv_bfloat16* __restrict__ slices,
+                                                            int* __restrict__ e_out) {
+  const long long c = blockIdx.x;
+  if (c >= Ncol) return;
+  const double* x = X + c * (long long)K;
+  unsigned long long mx = 0;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    const unsigned long long a = (unsigned long long)__double_as_longlong(x[k]) & 0x7FFFFFFFFFFFFFFFull;
+    mx = a > mx ? a : mx;
+  }
+  __shared__ unsigned long long smx[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = t > mx ? t : mx;
+  }
+  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = smx[w] > mx ? smx[w] : mx;
+  const int emax = (int)((mx >> 52) & 0x7FF);
+  const int m = mx == 0 ? 0 : emax - 1023 + 1;   // max|x| < 2^m
+  if (threadIdx.x == 0) e_out[c] = m + 1;
+  const long long slice_stride = Ncol * (long long)K;
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    const long long bits = __double_as_longlong(x[k]);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    long long F = 0;   // round(|x| 2^(6S-1-m)) <= 2^(6S-1)
+    if (ex != 0 && mx != 0) {
+      const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+      const int rs = m - (ex - 1023 - 52) - (BETA * S - 1);   // >= 6 since |x| < 2^m
+      if (rs < 64) F = (long long)((mant + (1ull << (rs - 1))) >> rs);
+    }
+    if (bits < 0) F = -F;
+    __nv_bfloat16* out = slices + c * (long long)K + k;
+#pragma unroll
+    for (int p = S - 1; p > 0; --p) {
+      const long long d = ((F + 32) & 63) - 32;
+      out[p * slice_stride] = __float2bfloat16_rn((float)d);
+      F = (F - d) >> BETA;
+    }
+    out[0] = __float2bfloat16_rn((float)F);
+  }
+}
+
+}  // namespace oz
+}  // namespace wg

@@ -68,6 +68,15 @@ struct MixedBuffers {
   FluxBlocks32 fb;
   int* err = nullptr;                // raised by a GEMM whose barrier wait timed out
   CUtensorMap tmA1, tmB1, tmB1z, tmA2, tmB2;
+  // FP64 outer residual on the tensor cores (digit slices, see ozaki.cuh)
+  bool ozaki = false;
+  __nv_bfloat16* oa1 = nullptr;      // [S][2 N_xi][2 Nk] digits of Phi'
+  __nv_bfloat16* oa2 = nullptr;      // [S][2 Nk][2 N_xi] digits of (i Phi^H)'
+  int* ea1 = nullptr;                // [2 N_xi] row exponents
+  int* ea2 = nullptr;                // [2 Nk]
+  __nv_bfloat16* ob = nullptr;       // [S][ncols][max(2 Nk, 2 N_xi)] digits of the B operand
+  int* eb = nullptr;                 // [ncols] column exponents
+  CUtensorMap tmOA1, tmOA2, tmOB1, tmOB2;
 };
 
 // Kernel classes timed and counted by the profiler.
@@ -208,6 +217,11 @@ void prof_release(Problem& P);
 // Kernel launchers (operator.cu)
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y);
 cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z);
+cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y);
+cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh);
+// FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y);
+int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err);
 // Rebuild potential-dependent data (Vw weights, contact inflow rhs) of problems [b0, b1).
 cudaError_t launch_potential_update(Problem& P, int b0, int b1);
 cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j);

@@ -1,7 +1,9 @@
 """GPU tests of the mixed-precision form (tcgen05 BF16 transforms in FP64 refinement).
 
 Tolerances: the tensor-core GEMM against a float64 product of the same
-bf16-rounded operands, 1e-5 relative (FP32 accumulation); the low-precision
+bf16-rounded operands, 1e-5 relative (FP32 accumulation); the emulated FP64
+GEMM against numpy FP64, 2e-13 of |A| |B| elementwise, and the mixed handle's
+FP64 operator built on it against the oracle's sparse matrix, 1e-12; the low-precision
 operator against the FP64 operator, 2e-2 relative (BF16 operands); the refined
 solution against the oracle's sparse LU at a 1e-10 residual target: density
 1e-8 and current 1e-7 relative (the mixed form's bar against FP64).
@@ -42,6 +44,28 @@ def test_tcgen05_bf16_gemm(built_lib, M, N, K):
     assert st == 0, lib.wg_global_error()
     ref = bf16_round(B) @ bf16_round(A).T                          # (N x M) = column-major M x N
     assert rel(Cout, ref) < 1e-5
+
+
+@pytest.mark.parametrize("M,N,K", [(256, 300, 512), (200, 150, 512), (128, 64, 64), (40, 37, 72)])
+def test_fp64_emulated_gemm(built_lib, M, N, K):
+    """Digit-sliced FP64 GEMM on the tensor cores against numpy FP64: rows and
+    columns spanning many binades, a zero column and a ragged tile edge; the
+    error is bounded by 2e-13 of |A| |B| elementwise."""
+    from real_space_dg_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(M * N + K)
+    A = rng.standard_normal((M, K)) * np.exp(rng.uniform(-20, 20, (M, 1)))      # row-major M x K
+    Bt = rng.standard_normal((N, K)) * np.exp(rng.uniform(-20, 20, (N, 1)))     # column-major K x N
+    Bt[N // 2] = 0.0
+    Bt[1, ::3] *= 1e-30                                                          # wide range inside a column
+    Cout = np.zeros((N, M))                                                      # column-major M x N
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    st = lib.wg_debug_gemm_f64_tc(dp(A), dp(Bt), dp(Cout), M, N, K)
+    assert st == 0, lib.wg_global_error()
+    ref = Bt @ A.T
+    bound = np.abs(Bt) @ np.abs(A).T
+    assert np.all(np.abs(Cout - ref) <= 2e-13 * bound)
+    assert np.all(Cout[N // 2] == 0.0)
 
 
 def make(spec, precision, batch=1, **kw):
