@@ -141,6 +141,9 @@ def make_workload(batch):
     return spec, mat, biases
 
 
+OZAKI_PRODUCTS = 36      # 8 digits per operand, products of weight < 8 (csrc/ozaki.cuh)
+
+
 def rooflines(prof, precision):
     """Achieved rate per kernel class from the library's CUDA-event timings and the
     algorithmic bytes/flops it attributed to each timed launch."""
@@ -153,6 +156,10 @@ def rooflines(prof, precision):
         sec = ms / 1000.0
         if cls == "gemm_bf16":
             ach, peak, bound, unit, psrc = fl / sec / 1e12, bf16, "tensor", "TFLOP/s", "bf16_tflops (%s)" % src
+        elif cls == "gemm_f64" and precision == "mixed":
+            # FP64 emulated on the BF16 tensor cores: 36 digit-slice products per FP64 GEMM
+            ach, peak, bound, unit = OZAKI_PRODUCTS * fl / sec / 1e12, bf16, "tensor", "TFLOP/s"
+            psrc = "bf16_tflops (%s); achieved counts the %d BF16 slice products" % (src, OZAKI_PRODUCTS)
         elif cls == "gemm_f64":
             ach, peak, bound, unit = fl / sec / 1e12, 1.25, "fp64", "TFLOP/s"
             psrc = "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)"
@@ -183,7 +190,8 @@ def run_ours(args, rank, world, dist):
         S.set(b, v)
     for _ in range(args.warmup):
         S.run(restart_from_phi0=True)
-    S.P.profile(on=True, reset=True)
+    # the timed region runs without the per-launch event profiler (launches are still counted)
+    S.P.profile(on=False, reset=True)
     clocks = ClockSampler()
     clocks.start()
     barrier(dist)
@@ -202,14 +210,17 @@ def run_ours(args, rank, world, dist):
             its += i["gmres_iterations"]
             gummel_its += i["iterations"]
     clk = clocks.stop()
-    prof = S.P.profile(on=False, reset=True)
+    counted = S.P.profile(on=False, reset=True)
+    launches = sum(v[2] for v in counted.values())
     t_max = max_over_ranks(total_ms / 1000.0, dist)
     pts_all = sum_over_ranks(pts, dist)
     value = pts_all / t_max if t_max > 0 else 0.0
-    # roofline of the dominant kernel class (largest share of timed kernel time)
+    # one more step, untimed, with CUDA events around every launch: per-class rooflines
+    S.P.profile(on=True, reset=True)
+    S.run(restart_from_phi0=True)
+    prof = S.P.profile(on=False, reset=True)
     roofs = rooflines(prof, args.precision)
     roof = max(roofs.values(), key=lambda r: r["share"]) if roofs else None
-    launches = sum(v[2] for v in prof.values())
     # e2e: the public call with host inputs and outputs, every step
     e2e = None
     if not args.no_e2e and rank == 0:

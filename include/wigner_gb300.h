@@ -202,6 +202,53 @@ int wg_gummel_run(wg_problem* h, const wg_gummel_opts* opts, wg_gummel_info* inf
 /* Problem b's potential phi [nx], density n [n_el*n_local] in m^-3 and current density j. */
 int wg_gummel_get(wg_problem* h, int b, double* phi, double* n_dg, double* j);
 
+/* ---- Transient self-consistent solve (1D RTD) -------------------------------
+ * DG_code/solve_transport_DG_2D_transient_SC_new.m:124-212 on the state of a
+ * Gummel handle: d rho/dt = scale_rhs * rhs - scale_a * A rho, the operator and
+ * the inflow rebuilt from the potential before step t when (t-1) % E == 0 or
+ * t < F (:131-149), the linear Poisson problem of solve_Poisson2D_transient.m
+ * solved for the current density after step t when t % E == 0 or t < F
+ * (:204-211), n and j after every step (:161-185).  Integrators: the
+ * reference's RK4 (:153-158) or Crank-Nicolson,
+ * (A + s I) rho' = (s I - A) rho + 2 scale_rhs/scale_a rhs with s = 2/(dt scale_a),
+ * one restarted-GMRES solve per step with the shifted k-line preconditioner,
+ * warm-started from the previous step (the plain or the mixed form of the handle). */
+enum { WG_TRANSIENT_CN = 0, WG_TRANSIENT_RK4 = 1 };
+
+typedef struct {
+  double dt;            /* time step [s] (mat.dt) */
+  int nsteps;           /* steps of this call (mat.Nt) */
+  int method;           /* WG_TRANSIENT_CN or WG_TRANSIENT_RK4 */
+  double scale_a;       /* operator scale; 0 -> 2e-10 (solve_transport_DG_2D_transient_SC_new.m:148) */
+  double scale_rhs;     /* inflow scale; 0 -> scale_a, so the stationary state is A^-1 rhs */
+  int refresh_every;    /* E; 0 -> 20; < 0: potential and operator fixed after the first step */
+  int refresh_first;    /* F; 0 -> 50; < 0 -> none */
+  double tol;           /* Crank-Nicolson GMRES relative residual per step; 0 -> 1e-10 */
+  int maxit;            /* restart cycles per step; 0 -> 20 */
+  int record_every;     /* store n and j after every record_every-th step; 0: none */
+} wg_transient_opts;
+
+typedef struct {
+  int status;                  /* 0: every step solved to tol; 1: some step stopped above tol */
+  int steps;                   /* steps taken */
+  long long gmres_iterations;  /* inner Krylov iterations over all steps */
+  double max_relres;           /* largest final relative residual of the step solves */
+  int refreshes;               /* operator and inflow rebuilds */
+  int poisson_solves;          /* potential re-solves (incl. the one of a bias step) */
+  double seconds;              /* wall time of the call */
+} wg_transient_info;
+
+/* Step problem b's drain bias at t = 0 of the next wg_transient_run: the right
+ * contact's Fermi level and the Poisson boundary value change now; the potential
+ * is re-solved for the current density before the first step. */
+int wg_transient_set_bias(wg_problem* h, int b, double bias);
+/* Advance every problem of the handle by nsteps from its resident state (the
+ * Wigner function and the potential of wg_gummel_run or of a previous call).
+ * n_hist, j_hist (either may be NULL): [nsteps / record_every][batch][n_el*n_local],
+ * n in m^-3 as wg_gummel_get.  info has batch entries. */
+int wg_transient_run(wg_problem* h, const wg_transient_opts* opts, double* n_hist, double* j_hist,
+                     wg_transient_info* info);
+
 /* ---- Allocation-free operator apply ----------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * while they call in: applications that own all device memory through their

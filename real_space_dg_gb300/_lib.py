@@ -70,6 +70,24 @@ GUMMEL_STATUS = {0: "fixed-point-converged", 1: "iteration-limit", 2: "transport
                  3: "poisson-not-converged"}
 
 
+class WgTransientOpts(C.Structure):
+    _fields_ = [("dt", C.c_double), ("nsteps", C.c_int), ("method", C.c_int), ("scale_a", C.c_double),
+                ("scale_rhs", C.c_double), ("refresh_every", C.c_int), ("refresh_first", C.c_int),
+                ("tol", C.c_double), ("maxit", C.c_int), ("record_every", C.c_int)]
+
+
+class WgTransientInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("steps", C.c_int), ("gmres_iterations", C.c_longlong),
+                ("max_relres", C.c_double), ("refreshes", C.c_int), ("poisson_solves", C.c_int),
+                ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+TRANSIENT_METHODS = {"cn": 0, "rk4": 1}
+
+
 class WgSolveInfo(C.Structure):
     _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("cycles", C.c_int), ("refinements", C.c_int),
                 ("relres", C.c_double), ("initial_relres", C.c_double), ("rhs_norm", C.c_double)]
@@ -99,6 +117,8 @@ SIGNATURES = {
     "wg_gummel_set": ([_H, C.c_int, C.POINTER(WgDevice), C.POINTER(WgRtd1D)], C.c_int),
     "wg_gummel_run": ([_H, C.POINTER(WgGummelOpts), C.POINTER(WgGummelInfo)], C.c_int),
     "wg_gummel_get": ([_H, C.c_int, _D, _D, _D], C.c_int),
+    "wg_transient_set_bias": ([_H, C.c_int, C.c_double], C.c_int),
+    "wg_transient_run": ([_H, C.POINTER(WgTransientOpts), _D, _D, C.POINTER(WgTransientInfo)], C.c_int),
     "wg_apply_noalloc": ([C.POINTER(WgOperatorView), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "wg_debug_gemm_bf16": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
                             C.c_int], C.c_int),

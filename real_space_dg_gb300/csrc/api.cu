@@ -47,8 +47,8 @@ void free_all(wg::Problem& P) {
     }
   wg::gummel_free(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
-                  P.pot_v, P.m_nodes, P.rhs, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
-                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.kused, P.any_active};
+                  P.pot_v, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
+                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.kused, P.any_active};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P.stream) cudaStreamDestroy(P.stream);
@@ -83,6 +83,75 @@ bool inv_small(const double* A, double* out, int n) {
 }
 
 }  // namespace
+
+namespace wg {
+
+// k-line factors of the flux part of A + sigma I, per problem b and wave number k:
+// D_b(k) = (k K1 + |k| K2 + (sigma / qd_b) I)^-1 and h = D_b(k) * upwind coupling column
+// (the line operator of get_LineTransversePreconditioner_full2D.m:174-197 in 1D; the
+// kernels multiply by 1 / qd_b).  With sigma = 0 and k = 0 (odd Nk) the flux vanishes
+// and the shift 0.003 max|k| |K| of get_LineTransversePreconditioner_full2D.m:50-71
+// keeps the factor regular.
+int set_kline_factors(Problem& P) {
+  const Shape& s = P.s;
+  const int nK = s.nK, B = P.batch;
+  const size_t per_d = (size_t)s.nk * nK * nK, per_h = (size_t)s.nk * nK;
+  std::vector<double> dinv(per_d * B), hv(per_h * B);
+  double kmax = 0;
+  for (double kk : s.k) kmax = std::max(kmax, std::fabs(kk));
+  for (int b = 0; b < B; ++b) {
+    double rel = 0;
+    if (P.shift != 0) {
+      if (!P.hp[b].ready || !(P.hp[b].qd > 0)) {
+        P.err = "shifted k-line factors need wg_set_potential for problem " + std::to_string(b);
+        return WG_ERR_ARG;
+      }
+      rel = P.shift / P.hp[b].qd;
+    } else if (b > 0) {
+      std::copy(dinv.begin(), dinv.begin() + per_d, dinv.begin() + per_d * b);
+      std::copy(hv.begin(), hv.begin() + per_h, hv.begin() + per_h * b);
+      continue;
+    }
+    for (int j = 0; j < s.nk; ++j) {
+      const double k = s.k[j], ak = std::fabs(k);
+      double D[kMaxLocal * kMaxLocal], Di[kMaxLocal * kMaxLocal], g[kMaxLocal];
+      for (int i = 0; i < nK * nK; ++i) D[i] = k * s.K1[i] + ak * s.K2[i];
+      for (int i = 0; i < nK; ++i) D[i * nK + i] += rel;
+      bool ok = (k != 0.0 || rel != 0.0) && inv_small(D, Di, nK);
+      if (!ok) {
+        if (rel != 0.0) {
+          P.err = "singular shifted k-line block";
+          return WG_ERR_NUMERIC;
+        }
+        for (int i = 0; i < nK * nK; ++i) Di[i] = 0;
+        double nrm = 0;
+        for (int i = 0; i < nK * nK; ++i) nrm = std::max(nrm, std::fabs(s.K1[i]) + std::fabs(s.K2[i]));
+        const double sigma = 0.003 * kmax * std::max(nrm, 1e-300);
+        for (int i = 0; i < nK; ++i) Di[i * nK + i] = 1.0 / sigma;
+      }
+      for (int a = 0; a < nK; ++a)
+        g[a] = k > 0 ? (k + ak) * s.K3[a * nK + nK - 1] : (k < 0 ? (k - ak) * s.K5[a * nK + 0] : 0.0);
+      for (int a = 0; a < nK; ++a) {
+        double acc = 0;
+        for (int c = 0; c < nK; ++c) acc += Di[a * nK + c] * g[c];
+        hv[per_h * b + (size_t)j * nK + a] = acc;
+      }
+      for (int i = 0; i < nK * nK; ++i) dinv[per_d * b + (size_t)j * nK * nK + i] = Di[i];
+    }
+  }
+  cudaError_t e = cudaMemcpyAsync(P.pre_dinv, dinv.data(), sizeof(double) * dinv.size(), cudaMemcpyHostToDevice,
+                                  P.stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P.pre_h, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice, P.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P.stream);   // host vectors go out of scope
+  if (e != cudaSuccess) {
+    P.err = std::string("k-line factors: ") + cudaGetErrorString(e);
+    return WG_ERR_CUDA;
+  }
+  return WG_OK;
+}
+
+}  // namespace wg
 
 extern "C" {
 
@@ -162,8 +231,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.xi_edge, s.nxi + 1, bytes));
   A(dalloc(&P.kap, (size_t)nK * nK * wg::kNqx, bytes));
   A(dalloc(&P.betai, (size_t)nK * nK * (s.nxi + 1), bytes));
-  A(dalloc(&P.pre_dinv, (size_t)s.nk * nK * nK, bytes));
-  A(dalloc(&P.pre_h, (size_t)s.nk * nK, bytes));
+  A(dalloc(&P.pre_dinv, (size_t)batch * s.nk * nK * nK, bytes));
+  A(dalloc(&P.pre_h, (size_t)batch * s.nk * nK, bytes));
   A(dalloc(&P.cosm, (size_t)s.nxi * s.nk, bytes));
   A(dalloc(&P.pinv, (size_t)s.nk * s.nxi, bytes));
   A(dalloc(&P.pp, (size_t)batch * wg::kPP, bytes));
@@ -195,6 +264,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.inv64, batch, bytes));
   A(dalloc(&P.target, batch, bytes));
   A(dalloc(&P.active, batch, bytes));
+  A(dalloc(&P.reorth, batch, bytes));
   A(dalloc(&P.kused, batch, bytes));
   A(dalloc(&P.any_active, 1, bytes));
   P.device_bytes = bytes;
@@ -212,38 +282,15 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   for (int ac = 0; ac < nK * nK; ++ac)
     for (int i = 0; i <= s.nxi; ++i)
       betai[(size_t)ac * (s.nxi + 1) + i] = -(s.delta_xi / 4 * s.mpc) * s.kap_sum[ac] * s.cap[i];
-  // k-line factors: D0 = k K1 + |k| K2, h = D0^-1 * coupling column
-  std::vector<double> dinv((size_t)s.nk * nK * nK), hv((size_t)s.nk * nK);
-  double kmax = 0;
-  for (double kk : s.k) kmax = std::max(kmax, std::fabs(kk));
-  for (int j = 0; j < s.nk; ++j) {
-    const double k = s.k[j], ak = std::fabs(k);
-    double D[wg::kMaxLocal * wg::kMaxLocal], Di[wg::kMaxLocal * wg::kMaxLocal], g[wg::kMaxLocal];
-    for (int i = 0; i < nK * nK; ++i) D[i] = k * s.K1[i] + ak * s.K2[i];
-    bool ok = k != 0.0 && inv_small(D, Di, nK);
-    if (!ok) {
-      // k = 0 (odd Nk): the flux vanishes; a shifted identity keeps M^-1 regular
-      for (int i = 0; i < nK * nK; ++i) Di[i] = 0;
-      double nrm = 0;
-      for (int i = 0; i < nK * nK; ++i) nrm = std::max(nrm, std::fabs(s.K1[i]) + std::fabs(s.K2[i]));
-      const double sigma = 0.003 * kmax * std::max(nrm, 1e-300);
-      for (int i = 0; i < nK; ++i) Di[i * nK + i] = 1.0 / sigma;
-    }
-    for (int a = 0; a < nK; ++a) g[a] = k > 0 ? (k + ak) * s.K3[a * nK + nK - 1] : (k < 0 ? (k - ak) * s.K5[a * nK + 0] : 0.0);
-    for (int a = 0; a < nK; ++a) {
-      double acc = 0;
-      for (int c = 0; c < nK; ++c) acc += Di[a * nK + c] * g[c];
-      hv[(size_t)j * nK + a] = acc;
-    }
-    for (int i = 0; i < nK * nK; ++i) dinv[(size_t)j * nK * nK + i] = Di[i];
-  }
   API_CK(&P, cudaMemcpyAsync(P.phi, phi.data(), sizeof(double2) * phi.size(), cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.kvec, s.k.data(), sizeof(double) * s.nk, cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.xi_edge, s.xi_edge.data(), sizeof(double) * (s.nxi + 1), cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.kap, s.kap.data(), sizeof(double) * s.kap.size(), cudaMemcpyHostToDevice, P.stream));
   API_CK(&P, cudaMemcpyAsync(P.betai, betai.data(), sizeof(double) * betai.size(), cudaMemcpyHostToDevice, P.stream));
-  API_CK(&P, cudaMemcpyAsync(P.pre_dinv, dinv.data(), sizeof(double) * dinv.size(), cudaMemcpyHostToDevice, P.stream));
-  API_CK(&P, cudaMemcpyAsync(P.pre_h, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice, P.stream));
+  {
+    const int rc = wg::set_kline_factors(P);
+    if (rc) return fail(&P, rc, P.err);
+  }
   API_CK(&P, cudaMemcpyAsync(P.cosm, s.cosm.data(), sizeof(double) * s.cosm.size(), cudaMemcpyHostToDevice, P.stream));
   {
     std::vector<double2> pinv(s.pinv.size());
@@ -309,6 +356,8 @@ int wg_set_potential(wg_problem* h, int b, const wg_device* dev, const double* e
   hp.l_chi = dev->x_nm[nx - 1] * 1e-9;
   const double detJ = hp.l_chi / s.n_el / 2;
   hp.qd = s.q_diff / detJ * s.mpc;
+  hp.ef_l = ef_l;
+  hp.ef_r = ef_r;
   {
     double vmax = esub_ev[0];
     for (int i = 1; i < nx; ++i) vmax = std::max(vmax, esub_ev[i]);
@@ -477,6 +526,26 @@ int wg_gummel_run(wg_problem* h, const wg_gummel_opts* opts, wg_gummel_info* inf
   if (opts) o = *opts;
   if (o.mixing < 0 || o.mixing > 1) return fail(&P, WG_ERR_ARG, "wg_gummel_run: mixing must be in (0, 1]");
   const int rc = wg::gummel_run(P, o, info);
+  if (rc != WG_OK && rc != WG_NOT_CONVERGED) return fail(&P, rc, P.err);
+  return rc;
+}
+
+int wg_transient_set_bias(wg_problem* h, int b, double bias) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_transient_set_bias: batch index out of range");
+  if (!std::isfinite(bias)) return fail(&P, WG_ERR_ARG, "wg_transient_set_bias: non-finite bias");
+  const int rc = wg::transient_set_bias(P, b, bias);
+  if (rc) return fail(&P, rc, P.err);
+  return WG_OK;
+}
+
+int wg_transient_run(wg_problem* h, const wg_transient_opts* opts, double* n_hist, double* j_hist,
+                     wg_transient_info* info) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (!opts || !info) return fail(&P, WG_ERR_ARG, "wg_transient_run: opts and info (batch entries) are required");
+  const int rc = wg::transient_run(P, *opts, n_hist, j_hist, info);
   if (rc != WG_OK && rc != WG_NOT_CONVERGED) return fail(&P, rc, P.err);
   return rc;
 }

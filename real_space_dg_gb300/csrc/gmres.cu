@@ -21,12 +21,15 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <type_traits>
 
 #include "problem.h"
 
 namespace wg {
 
 namespace {
+
+constexpr int kMaxRestart = 256;   // Krylov length bound of the device Givens / staging buffers
 
 __device__ __forceinline__ double2 ld2(const double2& v) { return v; }
 __device__ __forceinline__ double2 ld2(const float2& v) { return make_double2(v.x, v.y); }
@@ -38,13 +41,12 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 }
 
 // Inner-product accumulators.  FP64 vectors accumulate in FP64.  FP32 basis
-// vectors (mixed form) multiply and add in FP32 within a thread's run of kMdE
-// elements (at most 16 terms), then the runs are combined exactly in double-float
-// arithmetic across the warp (TwoSum on the FP32 pipes) and in FP64 across warps,
-// blocks and chunks.  The result carries ~1e-6 relative error with respect to
-// sum |a_i b_i|, below the rounding of the FP32 basis itself; a fully error-free
-// per-element scheme (Dot2) measured at a third of the HBM rate on GB300, whose
-// FP64 rate is too low to accumulate per element.
+// vectors (mixed form) multiply and add in FP32 within a thread (at most 8
+// complex terms) and across the warp (a 5-level tree), then in FP64 across warps,
+// blocks and chunks.  The error, a few 1e-7 of sum |a_i b_i|, matches the rounding
+// of the FP32 basis itself; the inner GMRES it serves targets 1e-3.  (Error-free
+// FP32 transformations per element measured at a third of the HBM rate, and
+// double-float merges per warp level made the kernels issue-bound.)
 struct Acc64 {
   double2 v = make_double2(0.0, 0.0);
   __device__ __forceinline__ void add_cdot(const double2& a, const double2& x) {  // += conj(a) x
@@ -69,46 +71,32 @@ struct Acc64 {
 };
 
 struct AccF32 {
-  float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;   // (hi, lo) pairs after warp_reduce
-  __device__ __forceinline__ void add_cdot(const float2& a, const float2& x) {
-    rh = fmaf(a.x, x.x, fmaf(a.y, x.y, rh));
-    ih = fmaf(a.x, x.y, fmaf(-a.y, x.x, ih));
+  float re = 0.f, im = 0.f;
+  // two consecutive complex values per float4
+  __device__ __forceinline__ void add_cdot4(const float4& a, const float4& x) {
+    re = fmaf(a.x, x.x, fmaf(a.y, x.y, fmaf(a.z, x.z, fmaf(a.w, x.w, re))));
+    im = fmaf(a.x, x.y, fmaf(-a.y, x.x, fmaf(a.z, x.w, fmaf(-a.w, x.z, im))));
   }
-  __device__ __forceinline__ void add_norm(const float2& a) { rh = fmaf(a.x, a.x, fmaf(a.y, a.y, rh)); }
-  // (hi, lo) += (bh, bl) in double-float arithmetic (TwoSum, then renormalise).
-  __device__ __forceinline__ static void merge(float& hi, float& lo, float bh, float bl) {
-    const float s = __fadd_rn(hi, bh);
-    const float bb = __fsub_rn(s, hi);
-    float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(bh, bb));
-    e = __fadd_rn(e, __fadd_rn(lo, bl));
-    hi = __fadd_rn(s, e);
-    lo = __fsub_rn(e, __fsub_rn(hi, s));
-  }
+  __device__ __forceinline__ void add_norm(const float2& a) { re = fmaf(a.x, a.x, fmaf(a.y, a.y, re)); }
   __device__ __forceinline__ void warp_reduce() {
     for (int o = 16; o > 0; o >>= 1) {
-      const float a = __shfl_xor_sync(0xffffffffu, rh, o), b = __shfl_xor_sync(0xffffffffu, rl, o);
-      const float c = __shfl_xor_sync(0xffffffffu, ih, o), d = __shfl_xor_sync(0xffffffffu, il, o);
-      merge(rh, rl, a, b);
-      merge(ih, il, c, d);
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
     }
   }
-  __device__ __forceinline__ double2 get() const {
-    return make_double2((double)rh + (double)rl, (double)ih + (double)il);
-  }
-  // Block-level staging keeps the double-float pairs in FP32 (no FP64 instruction per warp);
-  // combine() merges the warps' pairs in FP32 and converts once.
   __device__ __forceinline__ void stage(double* slot) const {
     float* f = reinterpret_cast<float*>(slot);
-    f[0] = rh; f[1] = rl; f[2] = ih; f[3] = il;
+    f[0] = re;
+    f[1] = im;
   }
   __device__ __forceinline__ static double2 combine(const double* slots, int n) {
-    AccF32 a;
+    double2 r = make_double2(0, 0);
     for (int q = 0; q < n; ++q) {
       const float* f = reinterpret_cast<const float*>(slots + 4 * q);
-      merge(a.rh, a.rl, f[0], f[1]);
-      merge(a.ih, a.il, f[2], f[3]);
+      r.x += (double)f[0];
+      r.y += (double)f[1];
     }
-    return a.get();
+    return r;
   }
 };
 
@@ -125,32 +113,11 @@ __device__ __forceinline__ void cms(float2& w, const float2& v, const float2& h)
   w.x = fmaf(-v.x, h.x, fmaf(v.y, h.y, w.x));
   w.y = fmaf(-v.x, h.y, fmaf(-v.y, h.x, w.y));
 }
-template <typename T> __device__ __forceinline__ T from2(double2 v);
-template <> __device__ __forceinline__ double2 from2<double2>(double2 v) { return v; }
-template <> __device__ __forceinline__ float2 from2<float2>(double2 v) { return make_float2((float)v.x, (float)v.y); }
 
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
-}
-
-__device__ double2 block_sum2(double2 v) {
-  __shared__ double sx[8], sy[8];
-  v.x = warp_sum(v.x);
-  v.y = warp_sum(v.y);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) { sx[w] = v.x; sy[w] = v.y; }
-  __syncthreads();
-  double2 r = make_double2(0, 0);
-  if (threadIdx.x < 32) {
-    r.x = lane < 8 ? sx[lane] : 0.0;
-    r.y = lane < 8 ? sy[lane] : 0.0;
-    r.x = warp_sum(r.x);
-    r.y = warp_sum(r.y);
-  }
-  __syncthreads();
-  return r;
 }
 
 __device__ double block_sum1(double v) {
@@ -181,25 +148,73 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
   const int b = blockIdx.y, c = blockIdx.x;
   if (!active[b]) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long base = (long long)c * 256 * kMdE + threadIdx.x;
-  const T* wb = w + (long long)b * N;
-  T wv[kMdE];
+  if constexpr (std::is_same<T, float2>::value) {
+    // two complex values per 16-byte load (N is even for the mixed form)
+    constexpr int E4 = kMdE / 2;
+    const long long base4 = (long long)c * 256 * E4 + threadIdx.x, N4 = N / 2;
+    const float4* wb = reinterpret_cast<const float4*>(w + (long long)b * N);
+    float4 wv[E4];
 #pragma unroll
-  for (int j = 0; j < kMdE; ++j) {
-    const long long n = base + (long long)j * 256;
-    if (n < N) wv[j] = wb[n];
-    else { wv[j].x = 0; wv[j].y = 0; }
-  }
-  for (int i = 0; i < nv; ++i) {
-    const T* v = V + ((long long)b * mp1 + i) * N;
-    typename AccFor<T>::type a;
+    for (int j = 0; j < E4; ++j) {
+      const long long n = base4 + (long long)j * 256;
+      wv[j] = n < N4 ? wb[n] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    int i = 0;
+    for (; i + 1 < nv; i += 2) {
+      const float4* v0 = reinterpret_cast<const float4*>(V + ((long long)b * mp1 + i) * N);
+      const float4* v1 = v0 + N4;
+      float4 a0[E4], a1[E4];
+#pragma unroll
+      for (int j = 0; j < E4; ++j) {
+        const long long n = base4 + (long long)j * 256;
+        a0[j] = n < N4 ? v0[n] : make_float4(0.f, 0.f, 0.f, 0.f);
+        a1[j] = n < N4 ? v1[n] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      AccF32 s0, s1;
+#pragma unroll
+      for (int j = 0; j < E4; ++j) {
+        s0.add_cdot4(a0[j], wv[j]);
+        s1.add_cdot4(a1[j], wv[j]);
+      }
+      s0.warp_reduce();
+      s1.warp_reduce();
+      if (lane == 0) {
+        s0.stage(red + (i * 8 + warp) * 4);
+        s1.stage(red + ((i + 1) * 8 + warp) * 4);
+      }
+    }
+    if (i < nv) {
+      const float4* v0 = reinterpret_cast<const float4*>(V + ((long long)b * mp1 + i) * N);
+      AccF32 s0;
+#pragma unroll
+      for (int j = 0; j < E4; ++j) {
+        const long long n = base4 + (long long)j * 256;
+        if (n < N4) s0.add_cdot4(v0[n], wv[j]);
+      }
+      s0.warp_reduce();
+      if (lane == 0) s0.stage(red + (i * 8 + warp) * 4);
+    }
+  } else {
+    const long long base = (long long)c * 256 * kMdE + threadIdx.x;
+    const T* wb = w + (long long)b * N;
+    T wv[kMdE];
 #pragma unroll
     for (int j = 0; j < kMdE; ++j) {
       const long long n = base + (long long)j * 256;
-      if (n < N) a.add_cdot(v[n], wv[j]);
+      if (n < N) wv[j] = wb[n];
+      else { wv[j].x = 0; wv[j].y = 0; }
     }
-    a.warp_reduce();
-    if (lane == 0) a.stage(red + (i * 8 + warp) * 4);
+    for (int i = 0; i < nv; ++i) {
+      const T* v = V + ((long long)b * mp1 + i) * N;
+      typename AccFor<T>::type a;
+#pragma unroll
+      for (int j = 0; j < kMdE; ++j) {
+        const long long n = base + (long long)j * 256;
+        if (n < N) a.add_cdot(v[n], wv[j]);
+      }
+      a.warp_reduce();
+      if (lane == 0) a.stage(red + (i * 8 + warp) * 4);
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nv; i += blockDim.x)
@@ -232,8 +247,28 @@ __global__ void dot_reduce_kernel(const double2* __restrict__ partial, double2* 
   }
 }
 
+// Daniel-Gragg-Kaufman-Stewart test after the first classical Gram-Schmidt pass:
+// problem b is re-orthogonalised only if |w1| < |w| / sqrt(2), where w1 = w - V h
+// and |w|^2 = |w1|^2 + |h|^2 (V orthonormal), i.e. only if |w1|^2 < |h|^2.
+__global__ void reorth_test_kernel(const double* __restrict__ partial, const double2* __restrict__ hcol,
+                                   const int* __restrict__ active, int* __restrict__ reorth, int nblk, int nv,
+                                   int pstride) {
+  const int b = blockIdx.x;
+  double w2 = 0, h2 = 0;
+  for (int c = threadIdx.x; c < nblk; c += 32) w2 += partial[(long long)b * nblk + c];
+  for (int i = threadIdx.x; i < nv; i += 32) {
+    const double2 h = hcol[(long long)b * pstride + i];
+    h2 += h.x * h.x + h.y * h.y;
+  }
+  w2 = warp_sum(w2);
+  h2 = warp_sum(h2);
+  if (threadIdx.x == 0) reorth[b] = (active[b] && w2 < h2) ? 1 : 0;
+}
+
 // w -= sum_i V_i hcol_i; with NORM, also nrm_partial[b][blockIdx.x] = sum |w|^2 of the block.
-// Grid (ceil(N/256), B).
+// Grid (ceil(N/256), B): 256 complex values per block, one per thread for FP64 vectors,
+// two per thread (16-byte accesses, 128 threads) for FP32 vectors.  The coefficients
+// are staged in shared memory.
 template <typename T, bool NORM>
 __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V, T* __restrict__ w,
                                                         const T* __restrict__ hcol, const int* __restrict__ active,
@@ -241,15 +276,43 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
                                                         int pstride, int nblk) {
   const int b = blockIdx.y;
   if (!active[b]) return;
-  const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ T hs[kMaxRestart + 1];
+  for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = hcol[b * pstride + i];
+  __syncthreads();
   typename AccFor<T>::type a;
-  if (n < N) {
-    const long long t = (long long)b * N + n;
-    T acc = w[t];
-    const T* v = V + (long long)b * mp1 * N + n;
-    for (int i = 0; i < nv; ++i) cms(acc, v[(long long)i * N], hcol[b * pstride + i]);
-    w[t] = acc;
-    if (NORM) a.add_norm(acc);
+  if constexpr (std::is_same<T, float2>::value) {
+    const long long N4 = N / 2;
+    const long long n4 = (long long)blockIdx.x * 128 + threadIdx.x;
+    if (n4 < N4) {
+      float4* wp = reinterpret_cast<float4*>(w + (long long)b * N) + n4;
+      float4 acc = *wp;
+      const float4* v = reinterpret_cast<const float4*>(V + (long long)b * mp1 * N) + n4;
+#pragma unroll 4
+      for (int i = 0; i < nv; ++i) {
+        const float4 x = v[(long long)i * N4];
+        const float2 h = hs[i];
+        acc.x = fmaf(-x.x, h.x, fmaf(x.y, h.y, acc.x));
+        acc.y = fmaf(-x.x, h.y, fmaf(-x.y, h.x, acc.y));
+        acc.z = fmaf(-x.z, h.x, fmaf(x.w, h.y, acc.z));
+        acc.w = fmaf(-x.z, h.y, fmaf(-x.w, h.x, acc.w));
+      }
+      *wp = acc;
+      if (NORM) {
+        a.add_norm(make_float2(acc.x, acc.y));
+        a.add_norm(make_float2(acc.z, acc.w));
+      }
+    }
+  } else {
+    const long long n = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n < N) {
+      const long long t = (long long)b * N + n;
+      T acc = w[t];
+      const T* v = V + (long long)b * mp1 * N + n;
+#pragma unroll 4
+      for (int i = 0; i < nv; ++i) cms(acc, v[(long long)i * N], hs[i]);
+      w[t] = acc;
+      if (NORM) a.add_norm(acc);
+    }
   }
   if (NORM) {
     __shared__ double wsum[8 * 4];
@@ -357,7 +420,6 @@ __global__ void cycle_init_kernel(const double* __restrict__ nrm, const double* 
 // Givens rotations of column k, residual estimate, convergence test.  One warp per
 // problem: the lanes stage the column and the rotations in shared memory, lane 0
 // applies the k previous rotations sequentially there.
-constexpr int kMaxRestart = 256;
 __global__ void givens_kernel(double2* __restrict__ H, double2* __restrict__ cs, double2* __restrict__ sn,
                               double2* __restrict__ g, int* __restrict__ active, int* __restrict__ kused,
                               const double* __restrict__ target, int k, int pstride, int m, int batch) {
@@ -487,23 +549,27 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   const int nv = k + 1;
   const double sz = (double)sizeof(T), vec = (double)N * B * sz;
   const dim3 gu((unsigned)((N + 255) / 256), B);
+  // classical Gram-Schmidt; the second pass runs only for the problems that fail the
+  // DGKS test (its kernels see P.reorth as their activity mask)
   for (int pass = 0; pass < 2; ++pass) {
+    const int* mask = pass == 0 ? P.active : P.reorth;
     cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B);
-    multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, P.active, N,
+    multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, mask, N,
                                                                                       nv, mp1, ps, P.nchunk);
     prof_end(P, PROF_MULTIDOT, ev);
     ev = prof_begin(P, PROF_KRYLOV);
-    dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, coef_col32<T>(P), P.H, P.active, nv, k, ps, mm,
+    dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, coef_col32<T>(P), P.H, mask, nv, k, ps, mm,
                                                P.nchunk, pass == 0);
     prof_end(P, PROF_KRYLOV, ev);
     ev = prof_begin(P, PROF_GSUPDATE, 1, (nv + 2) * vec, 8.0 * nv * N * B);
-    if (pass == 0)
-      gs_update_kernel<T, false><<<gu, 256, 0, P.stream>>>(V, w, coef_col<T>(P), P.active, nullptr, N, nv, mp1, ps,
-                                                          P.nblk);
-    else
-      gs_update_kernel<T, true><<<gu, 256, 0, P.stream>>>(V, w, coef_col<T>(P), P.active, P.nrm_partial, N, nv, mp1,
-                                                         ps, P.nblk);
+    gs_update_kernel<T, true><<<gu, sizeof(T) == sizeof(float2) ? 128 : 256, 0, P.stream>>>(
+        V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1, ps, P.nblk);
     prof_end(P, PROF_GSUPDATE, ev);
+    if (pass == 0) {
+      ev = prof_begin(P, PROF_KRYLOV);
+      reorth_test_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.hcol, P.active, P.reorth, P.nblk, nv, ps);
+      prof_end(P, PROF_KRYLOV, ev);
+    }
   }
   cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 3, 2 * vec);
   norm_reduce_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, P.H, P.active, P.nblk, k, ps, mm, P.inv64,

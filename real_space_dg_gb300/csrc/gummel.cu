@@ -114,8 +114,11 @@ __global__ void observables_batched_kernel(const double2* __restrict__ x, const 
 
 // One approximate-Newton Poisson step per problem (block per problem).
 // diag[b][0..7] = {defect, density change, relres before, linear relres, max|delta|, finite, -, -}
+// newton = 1: approximate-Newton step of the Gummel loop; newton = 0: the linear
+// Poisson problem A v = q (n - N_D) of the transient (solve_Poisson2D_transient.m),
+// solved exactly by the same step with J = A.
 __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const int* __restrict__ active, int nx,
-                                                      int ncol, int nK, double temp_default) {
+                                                      int ncol, int nK, double temp_default, double newton) {
   const int b = blockIdx.x;
   if (!active[b]) return;
   const long long ox = (long long)b * nx;
@@ -164,7 +167,7 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
   __syncthreads();
   // 3. Thomas solve of J delta = -F over the free nodes 1..nx-2
   if (threadIdx.x == 0) {
-    const double g = kQP * kQP / (kKBP * temp);
+    const double g = newton * kQP * kQP / (kKBP * temp);
     double cprev = 0, dprev = 0;
     for (int i = 1; i < nx - 1; ++i) {
       const double a = (i > 1) ? lo[i] : 0.0;
@@ -188,7 +191,7 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
     else {
       c = phi[i] + wd[i];
       const double dm = (i > 1) ? wd[i - 1] : 0.0, dp = (i < nx - 2) ? wd[i + 1] : 0.0;
-      const double g = kQP * kQP / (kKBP * temp);
+      const double g = newton * kQP * kQP / (kKBP * temp);
       const double jd = lo[i] * dm + (di[i] - g * ncv[i]) * wd[i] + up[i] * dp;
       const double vm = (i - 1 == 0) ? 0.0 : phi[i - 1];
       const double vp = (i + 1 == nx - 1) ? bias : phi[i + 1];
@@ -248,6 +251,36 @@ double lagrange(const std::vector<double>& r, int a, double x) {
 }
 
 }  // namespace
+
+cudaError_t gummel_observables(Problem& P) {
+  const int ncol = P.s.n_el * P.s.nK;
+  const double pref = kQ * (kHV / 2 / M_PI);
+  P.prof.launches[PROF_OTHER] += 1;
+  observables_batched_kernel<<<dim3((ncol * 32 + 255) / 256, P.batch), 256, 0, P.stream>>>(
+      P.x, P.phi, P.m_nodes, P.gd.scale, P.gd.ndg, P.gd.jdg, P.s.nk, P.s.nxi, ncol, P.N, P.s.delta_xi, pref);
+  return cudaGetLastError();
+}
+
+cudaError_t gummel_poisson(Problem& P, const int* active_dev, bool linear) {
+  P.prof.launches[PROF_OTHER] += 1;
+  poisson_kernel<<<P.batch, 256, 0, P.stream>>>(P.gd, active_dev, P.nx, P.s.n_el * P.s.nK, P.s.nK, 300.0,
+                                                linear ? 0.0 : 1.0);
+  return cudaGetLastError();
+}
+
+cudaError_t gummel_potential(Problem& P, const int* active_dev) {
+  P.prof.launches[PROF_OTHER] += 1;
+  potential_from_phi_kernel<<<dim3((P.nx + 255) / 256, P.batch), 256, 0, P.stream>>>(P.gd.vc, P.gd.phi, P.pot_v,
+                                                                                     active_dev, P.nx);
+  return cudaGetLastError();
+}
+
+cudaError_t gummel_mix(Problem& P, const int* mix_dev, double alpha) {
+  const int nx = P.nx, ncol = P.s.n_el * P.s.nK;
+  P.prof.launches[PROF_OTHER] += 1;
+  mix_kernel<<<dim3((std::max(nx, ncol) + 255) / 256, P.batch), 256, 0, P.stream>>>(P.gd, mix_dev, alpha, nx, ncol);
+  return cudaGetLastError();
+}
 
 int gummel_alloc(Problem& P) {
   if (P.gd.phi) return WG_OK;
@@ -411,7 +444,6 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
   const auto t0 = std::chrono::steady_clock::now();
   auto now_s = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
   if (!o.warm_start) GK(cudaMemsetAsync(P.x, 0, sizeof(double2) * P.N * B, P.stream));
-  const double pref = kQ * (kHV / 2 / M_PI);
   wg_solve_opts so{};
   so.tol = o.transport_tol > 0 ? o.transport_tol : 1e-8;
   so.maxit = o.transport_maxit > 0 ? o.transport_maxit : 50;
@@ -430,18 +462,13 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
     for (int b = 0; b < B; ++b) any |= active[b] != 0;
     if (!any) break;
     GK(cudaMemcpyAsync(G.active, active.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
-    P.prof.launches[PROF_OTHER] += 1;
-    potential_from_phi_kernel<<<dim3((nx + 255) / 256, B), 256, 0, P.stream>>>(G.vc, G.phi, P.pot_v, G.active, nx);
-    GK(cudaGetLastError());
+    GK(gummel_potential(P, G.active));
     GK(launch_potential_update(P, 0, B));
     P.tol_pp = tolb;
     int rc = solve_dispatch(P, so, /*warm=*/true, sinfo.data());
     if (rc != WG_OK && rc != WG_NOT_CONVERGED) return rc;
-    P.prof.launches[PROF_OTHER] += 2;
-    observables_batched_kernel<<<dim3((ncol * 32 + 255) / 256, B), 256, 0, P.stream>>>(
-        P.x, P.phi, P.m_nodes, G.scale, G.ndg, G.jdg, P.s.nk, P.s.nxi, ncol, P.N, P.s.delta_xi, pref);
-    poisson_kernel<<<B, 256, 0, P.stream>>>(G, G.active, nx, ncol, P.s.nK, 300.0);
-    GK(cudaGetLastError());
+    GK(gummel_observables(P));
+    GK(gummel_poisson(P, G.active, false));
     GK(cudaMemcpyAsync(diag.data(), G.diag, sizeof(double) * 8 * B, cudaMemcpyDeviceToHost, P.stream));
     GK(cudaStreamSynchronize(P.stream));
     const double tnow = now_s();
@@ -487,9 +514,7 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
       mix[b] = 1;
     }
     GK(cudaMemcpyAsync(G.mix, mix.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
-    P.prof.launches[PROF_OTHER] += 1;
-    mix_kernel<<<dim3((std::max(nx, ncol) + 255) / 256, B), 256, 0, P.stream>>>(G, G.mix, alpha, nx, ncol);
-    GK(cudaGetLastError());
+    GK(gummel_mix(P, G.mix, alpha));
   }
   GK(cudaStreamSynchronize(P.stream));
   int status = WG_OK;

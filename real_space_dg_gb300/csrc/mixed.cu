@@ -131,102 +131,119 @@ cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, float* D, in
 }
 
 // ---------------------------------------------------------------------------
-// FP32 upwind flux (the FP64 flux_kernel in single precision).
+// FP32 upwind flux (the FP64 flux_kernel in single precision), two k per thread
+// with 16-byte loads and stores.  Grid (batch * n_el, ceil(nk / 256)).  k changes
+// sign only between j = nk/2 - 1 and nk/2, so for nk % 4 == 0 (required by the
+// mixed form) both k of a pair share the upwind side.  xb (optional) receives x in
+// BF16, the B operand of the following GEMM, so no separate conversion pass is needed.
 // ---------------------------------------------------------------------------
+constexpr int kFlux32Threads = 128;
+
 template <int NK>
-__global__ void __launch_bounds__(256) flux32_kernel(const float2* __restrict__ x, float2* __restrict__ y,
-                                                     const float* __restrict__ kvec, const float* __restrict__ qd,
-                                                     FluxBlocks32 fb, int n_el, int nk, long long total) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= total) return;
-  const int j = (int)(t % nk);
-  const long long be = t / nk;
-  const int e = (int)(be % n_el);
-  const int b = (int)(be / n_el);
-  const float k = kvec[j], ak = fabsf(k);
+__global__ void __launch_bounds__(kFlux32Threads) flux32_kernel(const float2* __restrict__ x, float2* __restrict__ y,
+                                                                bf162* __restrict__ xb,
+                                                                const float* __restrict__ kvec,
+                                                                const float* __restrict__ qd, FluxBlocks32 fb,
+                                                                int n_el, int nk, float shift) {
+  const int be = blockIdx.x;
+  const int j = 2 * (blockIdx.y * kFlux32Threads + threadIdx.x);
+  if (j >= nk) return;
+  const int b = be / n_el;
+  const int e = be - b * n_el;
+  const float k0 = kvec[j], k1 = kvec[j + 1];
+  const float ak0 = fabsf(k0), ak1 = fabsf(k1);
   const float s = qd[b];
-  const float2* xe = x + be * (long long)NK * nk + j;
-  float2 xv[NK], acc[NK];
+  const long long base = (long long)be * NK * nk + j;
+  float4 xv[NK];
 #pragma unroll
-  for (int c = 0; c < NK; ++c) xv[c] = xe[(long long)c * nk];
-#pragma unroll
-  for (int a = 0; a < NK; ++a) {
-    float2 v = make_float2(0.f, 0.f);
+  for (int c = 0; c < NK; ++c) xv[c] = *reinterpret_cast<const float4*>(x + base + (long long)c * nk);
+  if (xb) {
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
-      const float m = k * fb.K1[a * NK + c] + ak * fb.K2[a * NK + c];
-      v.x = fmaf(m, xv[c].x, v.x);
-      v.y = fmaf(m, xv[c].y, v.y);
+      bf162 lo = __floats2bfloat162_rn(xv[c].x, xv[c].y), hi = __floats2bfloat162_rn(xv[c].z, xv[c].w);
+      uint2 pk;
+      pk.x = *reinterpret_cast<uint32_t*>(&lo);
+      pk.y = *reinterpret_cast<uint32_t*>(&hi);
+      *reinterpret_cast<uint2*>(xb + base + (long long)c * nk) = pk;
+    }
+  }
+  float4 acc[NK];
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < NK; ++c) {
+      const float m0 = k0 * fb.K1[a * NK + c] + ak0 * fb.K2[a * NK + c];
+      const float m1 = k1 * fb.K1[a * NK + c] + ak1 * fb.K2[a * NK + c];
+      v.x = fmaf(m0, xv[c].x, v.x);
+      v.y = fmaf(m0, xv[c].y, v.y);
+      v.z = fmaf(m1, xv[c].z, v.z);
+      v.w = fmaf(m1, xv[c].w, v.w);
     }
     acc[a] = v;
   }
-  if (k > 0 && e > 0) {
-    const float2* xl = xe - (long long)NK * nk;
+  const bool left = k0 > 0 && e > 0, right = k0 < 0 && e < n_el - 1;
+  if (left || right) {
+    const float* K = left ? fb.K3 : fb.K5;
+    const float w0 = left ? k0 + ak0 : k0 - ak0, w1 = left ? k1 + ak1 : k1 - ak1;
+    const long long nb = base + (left ? -(long long)NK * nk : (long long)NK * nk);
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
-      const float2 xp = xl[(long long)c * nk];
+      const float4 xp = *reinterpret_cast<const float4*>(x + nb + (long long)c * nk);
 #pragma unroll
       for (int a = 0; a < NK; ++a) {
-        const float m = (k + ak) * fb.K3[a * NK + c];
-        acc[a].x = fmaf(m, xp.x, acc[a].x);
-        acc[a].y = fmaf(m, xp.y, acc[a].y);
-      }
-    }
-  } else if (k < 0 && e < n_el - 1) {
-    const float2* xr = xe + (long long)NK * nk;
-#pragma unroll
-    for (int c = 0; c < NK; ++c) {
-      const float2 xp = xr[(long long)c * nk];
-#pragma unroll
-      for (int a = 0; a < NK; ++a) {
-        const float m = (k - ak) * fb.K5[a * NK + c];
-        acc[a].x = fmaf(m, xp.x, acc[a].x);
-        acc[a].y = fmaf(m, xp.y, acc[a].y);
+        const float m0 = w0 * K[a * NK + c], m1 = w1 * K[a * NK + c];
+        acc[a].x = fmaf(m0, xp.x, acc[a].x);
+        acc[a].y = fmaf(m0, xp.y, acc[a].y);
+        acc[a].z = fmaf(m1, xp.z, acc[a].z);
+        acc[a].w = fmaf(m1, xp.w, acc[a].w);
       }
     }
   }
-  float2* ye = y + be * (long long)NK * nk + j;
 #pragma unroll
-  for (int a = 0; a < NK; ++a) ye[(long long)a * nk] = make_float2(s * acc[a].x, s * acc[a].y);
+  for (int a = 0; a < NK; ++a)
+    *reinterpret_cast<float4*>(y + base + (long long)a * nk) =
+        make_float4(fmaf(s, acc[a].x, shift * xv[a].x), fmaf(s, acc[a].y, shift * xv[a].y),
+                    fmaf(s, acc[a].z, shift * xv[a].z), fmaf(s, acc[a].w, shift * xv[a].w));
 }
 
 // ---------------------------------------------------------------------------
 // FP32 xi stencil, output as the BF16 B operand of GEMM 2.
+// Grid (batch * n_el, ceil(nxi / 128)): one block row per element.
 // ---------------------------------------------------------------------------
 template <int NK>
-__global__ void __launch_bounds__(256) stencil32_kernel(const float2* __restrict__ xh, bf162* __restrict__ yh,
-                                                        const float* __restrict__ betar,
-                                                        const float* __restrict__ betai, int nxi,
-                                                        long long nelem_batch) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nelem_batch * nxi) return;
-  const int s = (int)(t % nxi);
-  const long long be = t / nxi;
+__global__ void __launch_bounds__(kFlux32Threads) stencil32_kernel(const float2* __restrict__ xh,
+                                                                   bf162* __restrict__ yh,
+                                                                   const float* __restrict__ betar,
+                                                                   const float* __restrict__ betai, int nxi) {
+  const int be = blockIdx.x;
+  const int s = blockIdx.y * kFlux32Threads + threadIdx.x;
+  if (s >= nxi) return;
   const int ne = nxi + 1;
-  const float2* X = xh + be * NK * (long long)nxi;
+  const float2* X = xh + (long long)be * NK * nxi;
   float2 sm[NK], sp[NK];
 #pragma unroll
   for (int c = 0; c < NK; ++c) {
-    const float2 x0 = X[(long long)c * nxi + s];
-    const float2 xm = s > 0 ? X[(long long)c * nxi + s - 1] : make_float2(0.f, 0.f);
-    const float2 xp = s < nxi - 1 ? X[(long long)c * nxi + s + 1] : make_float2(0.f, 0.f);
+    const float2 x0 = X[c * nxi + s];
+    const float2 xm = s > 0 ? X[c * nxi + s - 1] : make_float2(0.f, 0.f);
+    const float2 xp = s < nxi - 1 ? X[c * nxi + s + 1] : make_float2(0.f, 0.f);
     sm[c] = make_float2(x0.x + xm.x, x0.y + xm.y);
     sp[c] = make_float2(x0.x + xp.x, x0.y + xp.y);
   }
-  const float* br = betar + be * (long long)NK * NK * ne;
-  bf162* Y = yh + be * NK * (long long)nxi;
+  const float* br = betar + (long long)be * NK * NK * ne;
+  bf162* Y = yh + (long long)be * NK * nxi;
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
     float vx = 0.f, vy = 0.f;
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
       const int ac = a * NK + c;
-      const float b0r = br[(long long)ac * ne + s], b0i = betai[ac * ne + s];
-      const float b1r = br[(long long)ac * ne + s + 1], b1i = betai[ac * ne + s + 1];
+      const float b0r = br[ac * ne + s], b0i = betai[ac * ne + s];
+      const float b1r = br[ac * ne + s + 1], b1i = betai[ac * ne + s + 1];
       vx += b0r * sm[c].x - b0i * sm[c].y + b1r * sp[c].x - b1i * sp[c].y;
       vy += b0r * sm[c].y + b0i * sm[c].x + b1r * sp[c].y + b1i * sp[c].x;
     }
-    Y[(long long)a * nxi + s] = __floats2bfloat162_rn(vx, vy);
+    Y[a * nxi + s] = __floats2bfloat162_rn(vx, vy);
   }
 }
 
@@ -251,10 +268,11 @@ __global__ void precond32_kernel(const float2* __restrict__ r, float2* __restric
   float D[NK * NK], h[NK];
   bool fwd = true;
   float inv_qd = 1.f;
+  const long long bj = (long long)b * nk + j;
 #pragma unroll
-  for (int i = 0; i < NK * NK; ++i) D[i] = valid ? dinv[j * NK * NK + i] : 0.f;
+  for (int i = 0; i < NK * NK; ++i) D[i] = valid ? dinv[bj * NK * NK + i] : 0.f;
 #pragma unroll
-  for (int i = 0; i < NK; ++i) h[i] = valid ? hvec[j * NK + i] : 0.f;
+  for (int i = 0; i < NK; ++i) h[i] = valid ? hvec[bj * NK + i] : 0.f;
   if (valid) {
     fwd = kvec[j] > 0;
     inv_qd = __frcp_rn(qd[b]);
@@ -327,14 +345,6 @@ __global__ void precond32_kernel(const float2* __restrict__ r, float2* __restric
   }
 }
 
-__global__ void to_bf16_kernel(const float2* __restrict__ x, bf162* __restrict__ y, long long n) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) {
-    const float2 v = x[t];
-    y[t] = __floats2bfloat162_rn(v.x, v.y);
-  }
-}
-
 __global__ void c2f_kernel(const double2* __restrict__ x, float2* __restrict__ y, long long n) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) y[t] = make_float2((float)x[t].x, (float)x[t].y);
@@ -355,18 +365,16 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
   MixedBuffers& M = P.mx;
   if (xb && xb != M.xin16 && xb != M.zb16) return cudaErrorInvalidValue;
   const Shape& s = P.s;
-  const long long total = (long long)P.batch * s.n_el * s.nk;
   const long long BN = P.N * P.batch;
-  if (!xb) {
-    to_bf16_kernel<<<(unsigned)((BN + 255) / 256), 256, 0, P.stream>>>(x, M.xin16, BN);
-    xb = M.xin16;
-    P.prof.launches[PROF_OTHER] += 1;
-  }
+  // without a BF16 copy of x the flux kernel writes one into xin16
+  bf162* xb_out = xb ? nullptr : M.xin16;
+  if (!xb) xb = M.xin16;
   const double ncols = (double)P.ncols, nxi = s.nxi, nkd = s.nk;
   const double gemm_flops = 2.0 * (2 * nxi) * (2 * nkd) * ncols;
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 16.0 * BN);
-  flux32_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, M.kvec, M.qd, M.fb, s.n_el, s.nk,
-                                                                            total);
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, (xb_out ? 20.0 : 16.0) * BN);
+  const dim3 fgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nk / 2 + kFlux32Threads - 1) / kFlux32Threads));
+  flux32_kernel<NK><<<fgrid, kFlux32Threads, 0, P.stream>>>(x, y, xb_out, M.kvec, M.qd, M.fb, s.n_el, s.nk,
+                                                            (float)P.shift);
   prof_end(P, PROF_FLUX, ev);
   ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * BN + 8.0 * nxi * ncols, gemm_flops);
   // GEMM 1 reads its B operand through the tensor map of whichever bf16 buffer holds x
@@ -374,10 +382,10 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
                                  P.ncols, 2 * s.nk, M.err, P.stream);
   prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
-  const long long nelem = (long long)P.batch * s.n_el;
   ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * NK * NK * (nxi + 1));
-  stencil32_kernel<NK><<<(unsigned)((nelem * s.nxi + 255) / 256), 256, 0, P.stream>>>(
-      reinterpret_cast<const float2*>(M.xh), M.yh16, M.beta, M.betai, s.nxi, nelem);
+  const dim3 sgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nxi + kFlux32Threads - 1) / kFlux32Threads));
+  stencil32_kernel<NK><<<sgrid, kFlux32Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16,
+                                                               M.beta, M.betai, s.nxi);
   prof_end(P, PROF_STENCIL, ev);
   ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops);
   e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream);
@@ -437,8 +445,8 @@ int mixed_alloc(Problem& P) {
   alloc((void**)&M.err, sizeof(int));
   alloc((void**)&M.kvec, sizeof(float) * s.nk);
   alloc((void**)&M.qd, sizeof(float) * P.batch);
-  alloc((void**)&M.dinv, sizeof(float) * (size_t)s.nk * s.nK * s.nK);
-  alloc((void**)&M.h, sizeof(float) * (size_t)s.nk * s.nK);
+  alloc((void**)&M.dinv, sizeof(float) * (size_t)P.batch * s.nk * s.nK * s.nK);
+  alloc((void**)&M.h, sizeof(float) * (size_t)P.batch * s.nk * s.nK);
   alloc((void**)&M.hcol, sizeof(float2) * (size_t)P.batch * (P.restart_max + 1));
   alloc((void**)&M.y, sizeof(float2) * (size_t)P.batch * P.restart_max);
   alloc((void**)&M.inv, sizeof(float) * P.batch);
@@ -557,9 +565,9 @@ cudaError_t mixed_sync_weights(Problem& P) {
   d2f_kernel<<<(unsigned)((ni + 255) / 256), 256, 0, P.stream>>>(P.betai, P.mx.betai, ni);
   d2f_kernel<<<1, 256, 0, P.stream>>>(P.qd, P.mx.qd, P.batch);
   d2f_kernel<<<(unsigned)((s.nk + 255) / 256), 256, 0, P.stream>>>(P.kvec, P.mx.kvec, s.nk);
-  d2f_kernel<<<(unsigned)((s.nk * s.nK * s.nK + 255) / 256), 256, 0, P.stream>>>(P.pre_dinv, P.mx.dinv,
-                                                                                (long long)s.nk * s.nK * s.nK);
-  d2f_kernel<<<(unsigned)((s.nk * s.nK + 255) / 256), 256, 0, P.stream>>>(P.pre_h, P.mx.h, (long long)s.nk * s.nK);
+  const long long nd = (long long)P.batch * s.nk * s.nK * s.nK, nh = (long long)P.batch * s.nk * s.nK;
+  d2f_kernel<<<(unsigned)((nd + 255) / 256), 256, 0, P.stream>>>(P.pre_dinv, P.mx.dinv, nd);
+  d2f_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, P.stream>>>(P.pre_h, P.mx.h, nh);
   return cudaGetLastError();
 }
 

@@ -23,28 +23,30 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ double2 cscale(double s, double2 a) { return make_double2(s * a.x, s * a.y); }
 
 // ---------------------------------------------------------------------------
 // 1. Upwind flux: y_{e,.,j} = qd_b [ (k K1 + |k| K2) x_e + (k+|k|) K3 x_{e-1}
-//                                   + (k-|k|) K5 x_{e+1} ]_j
-// One thread per (b, e, j); k fastest so every load/store is coalesced.
+//                                   + (k-|k|) K5 x_{e+1} ]_j  + shift x_{e,.,j}
+// Grid (batch * n_el, ceil(nk / 128)): one block row per element, one thread per
+// k, k fastest so every load/store is coalesced; no integer division per thread.
+// shift = 0 for the stationary operator, sigma for the shifted (Crank-Nicolson) one.
 // ---------------------------------------------------------------------------
+constexpr int kFluxThreads = 128;
+
 template <int NK>
-__global__ void __launch_bounds__(256) flux_kernel(const double2* __restrict__ x, double2* __restrict__ y,
-                                                   const double* __restrict__ kvec,
-                                                   const double* __restrict__ qd, FluxBlocks fb, int n_el,
-                                                   int nk, long long total) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= total) return;
-  const int j = (int)(t % nk);
-  const long long be = t / nk;          // b * n_el + e
-  const int e = (int)(be % n_el);
-  const int b = (int)(be / n_el);
+__global__ void __launch_bounds__(kFluxThreads) flux_kernel(const double2* __restrict__ x, double2* __restrict__ y,
+                                                            const double* __restrict__ kvec,
+                                                            const double* __restrict__ qd, FluxBlocks fb, int n_el,
+                                                            int nk, double shift) {
+  const int be = blockIdx.x;                  // b * n_el + e
+  const int j = blockIdx.y * kFluxThreads + threadIdx.x;
+  if (j >= nk) return;
+  const int b = be / n_el;
+  const int e = be - b * n_el;
   const double k = kvec[j];
   const double ak = fabs(k);
   const double s = qd[b];
-  const double2* xe = x + be * (long long)NK * nk + j;
+  const double2* xe = x + (long long)be * NK * nk + j;
   double2 xv[NK];
 #pragma unroll
   for (int c = 0; c < NK; ++c) xv[c] = xe[(long long)c * nk];
@@ -87,9 +89,10 @@ __global__ void __launch_bounds__(256) flux_kernel(const double2* __restrict__ x
         acc[a].y += m * xp[c].y;
       }
   }
-  double2* ye = y + be * (long long)NK * nk + j;
+  double2* ye = y + (long long)be * NK * nk + j;
 #pragma unroll
-  for (int a = 0; a < NK; ++a) ye[(long long)a * nk] = cscale(s, acc[a]);
+  for (int a = 0; a < NK; ++a)
+    ye[(long long)a * nk] = make_double2(s * acc[a].x + shift * xv[a].x, s * acc[a].y + shift * xv[a].y);
 }
 
 // ---------------------------------------------------------------------------
@@ -193,38 +196,38 @@ __global__ void __launch_bounds__(256) zgemm_kernel(const double2* __restrict__ 
 // One thread per (element of the batch, s); s fastest.
 // ---------------------------------------------------------------------------
 template <int NK>
-__global__ void __launch_bounds__(256) stencil_kernel(const double2* __restrict__ xh, double2* __restrict__ yh,
-                                                      const double* __restrict__ betar,
-                                                      const double* __restrict__ betai, int nxi,
-                                                      long long nelem_batch) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= nelem_batch * nxi) return;
-  const int s = (int)(t % nxi);
-  const long long be = t / nxi;
+__global__ void __launch_bounds__(kFluxThreads) stencil_kernel(const double2* __restrict__ xh,
+                                                               double2* __restrict__ yh,
+                                                               const double* __restrict__ betar,
+                                                               const double* __restrict__ betai, int nxi) {
+  // grid (batch * n_el, ceil(nxi / 128)): one block row per element, one thread per xi cell
+  const int be = blockIdx.x;
+  const int s = blockIdx.y * kFluxThreads + threadIdx.x;
+  if (s >= nxi) return;
   const int ne = nxi + 1;
-  const double2* X = xh + be * NK * (long long)nxi;
+  const double2* X = xh + (long long)be * NK * nxi;
   double2 sm[NK], sp[NK];
 #pragma unroll
   for (int c = 0; c < NK; ++c) {
-    const double2 x0 = X[(long long)c * nxi + s];
-    const double2 xm = s > 0 ? X[(long long)c * nxi + s - 1] : make_double2(0.0, 0.0);
-    const double2 xp = s < nxi - 1 ? X[(long long)c * nxi + s + 1] : make_double2(0.0, 0.0);
+    const double2 x0 = X[c * nxi + s];
+    const double2 xm = s > 0 ? X[c * nxi + s - 1] : make_double2(0.0, 0.0);
+    const double2 xp = s < nxi - 1 ? X[c * nxi + s + 1] : make_double2(0.0, 0.0);
     sm[c] = cadd(x0, xm);
     sp[c] = cadd(x0, xp);
   }
-  const double* br = betar + be * (long long)NK * NK * ne;
-  double2* Y = yh + be * NK * (long long)nxi;
+  const double* br = betar + (long long)be * NK * NK * ne;
+  double2* Y = yh + (long long)be * NK * nxi;
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
     double2 v = make_double2(0.0, 0.0);
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
       const int ac = a * NK + c;
-      const double2 b0 = make_double2(br[(long long)ac * ne + s], betai[ac * ne + s]);
-      const double2 b1 = make_double2(br[(long long)ac * ne + s + 1], betai[ac * ne + s + 1]);
+      const double2 b0 = make_double2(br[ac * ne + s], betai[ac * ne + s]);
+      const double2 b1 = make_double2(br[ac * ne + s + 1], betai[ac * ne + s + 1]);
       v = cadd(v, cadd(cmul(b0, sm[c]), cmul(b1, sp[c])));
     }
-    Y[(long long)a * nxi + s] = v;
+    Y[a * nxi + s] = v;
   }
 }
 
@@ -255,10 +258,11 @@ __global__ void precond_kernel(const double2* __restrict__ r, double2* __restric
   bool fwd = true;
   double inv_qd = 1.0;
   if (valid) {
+    const long long bj = (long long)b * nk + j;
 #pragma unroll
-    for (int i = 0; i < NK * NK; ++i) D[i] = dinv[j * NK * NK + i];
+    for (int i = 0; i < NK * NK; ++i) D[i] = dinv[bj * NK * NK + i];
 #pragma unroll
-    for (int i = 0; i < NK; ++i) h[i] = hvec[j * NK + i];
+    for (int i = 0; i < NK; ++i) h[i] = hvec[bj * NK + i];
     fwd = kvec[j] > 0;
     inv_qd = 1.0 / qd[b];
   }
@@ -371,23 +375,32 @@ __global__ void observables_kernel(const double2* __restrict__ rho, const double
 }
 
 template <int NK>
+void flux_launch(const double2* x, double2* y, const double* kvec, const double* qd, const FluxBlocks& fb, int batch,
+                 int n_el, int nk, double shift, cudaStream_t st) {
+  const dim3 grid((unsigned)(batch * n_el), (unsigned)((nk + kFluxThreads - 1) / kFluxThreads));
+  flux_kernel<NK><<<grid, kFluxThreads, 0, st>>>(x, y, kvec, qd, fb, n_el, nk, shift);
+}
+
+template <int NK>
+void stencil_launch(const double2* xh, double2* yh, const double* beta, const double* betai, int batch, int n_el,
+                    int nxi, cudaStream_t st) {
+  const dim3 grid((unsigned)(batch * n_el), (unsigned)((nxi + kFluxThreads - 1) / kFluxThreads));
+  stencil_kernel<NK><<<grid, kFluxThreads, 0, st>>>(xh, yh, beta, betai, nxi);
+}
+
+template <int NK>
 cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
-  const long long total = (long long)P.batch * P.s.n_el * P.s.nk;
   const double BN = (double)P.N * P.batch, ncols = (double)P.ncols, nxi = P.s.nxi, nk = P.s.nk;
   const double gemm_flops = 8.0 * nxi * nk * ncols;
   cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * BN);
-  flux_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el,
-                                                                          P.s.nk, total);
+  flux_launch<NK>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream);
   prof_end(P, PROF_FLUX, ev);
   dim3 g1((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nxi + GBM - 1) / GBM);
   ev = prof_begin(P, PROF_GEMM_F64, 1, 16.0 * (BN + nxi * ncols), gemm_flops);
   zgemm_kernel<0><<<g1, 256, 0, P.stream>>>(P.phi, P.s.nk, x, P.xh, P.s.nxi, P.s.nk, P.ncols);
   prof_end(P, PROF_GEMM_F64, ev);
-  const long long nelem = (long long)P.batch * P.s.n_el;
-  const long long st = nelem * P.s.nxi;
   ev = prof_begin(P, PROF_STENCIL, 1, 32.0 * nxi * ncols + 8.0 * P.batch * P.s.n_el * NK * NK * (nxi + 1));
-  stencil_kernel<NK><<<(unsigned)((st + 255) / 256), 256, 0, P.stream>>>(P.xh, P.yh, P.beta, P.betai, P.s.nxi,
-                                                                          nelem);
+  stencil_launch<NK>(P.xh, P.yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream);
   prof_end(P, PROF_STENCIL, ev);
   dim3 g2((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nk + GBM - 1) / GBM);
   ev = prof_begin(P, PROF_GEMM_F64, 1, 16.0 * (2 * BN + nxi * ncols), gemm_flops);
@@ -481,28 +494,24 @@ cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
 }
 
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y) {
-  const long long total = (long long)P.batch * P.s.n_el * P.s.nk;
-  const unsigned g = (unsigned)((total + 255) / 256);
   cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * P.N * P.batch);
   switch (P.s.nK) {
-    case 2: flux_kernel<2><<<g, 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el, P.s.nk, total); break;
-    case 3: flux_kernel<3><<<g, 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el, P.s.nk, total); break;
-    default: flux_kernel<4><<<g, 256, 0, P.stream>>>(x, y, P.kvec, P.qd, P.fb, P.s.n_el, P.s.nk, total); break;
+    case 2: flux_launch<2>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream); break;
+    case 3: flux_launch<3>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream); break;
+    default: flux_launch<4>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream); break;
   }
   prof_end(P, PROF_FLUX, ev);
   return cudaGetLastError();
 }
 
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh) {
-  const long long nelem = (long long)P.batch * P.s.n_el;
-  const unsigned g = (unsigned)((nelem * P.s.nxi + 255) / 256);
   const int nK = P.s.nK;
   cudaEvent_t ev = prof_begin(P, PROF_STENCIL, 1,
                               32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1));
   switch (nK) {
-    case 2: stencil_kernel<2><<<g, 256, 0, P.stream>>>(xh, yh, P.beta, P.betai, P.s.nxi, nelem); break;
-    case 3: stencil_kernel<3><<<g, 256, 0, P.stream>>>(xh, yh, P.beta, P.betai, P.s.nxi, nelem); break;
-    default: stencil_kernel<4><<<g, 256, 0, P.stream>>>(xh, yh, P.beta, P.betai, P.s.nxi, nelem); break;
+    case 2: stencil_launch<2>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream); break;
+    case 3: stencil_launch<3>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream); break;
+    default: stencil_launch<4>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream); break;
   }
   prof_end(P, PROF_STENCIL, ev);
   return cudaGetLastError();
@@ -581,13 +590,11 @@ template <int NK>
 cudaError_t apply_noalloc_nk(const wg_operator_view& v, const FluxBlocks& fb, const double2* x, double2* y,
                              double2* xh, double2* yh, cudaStream_t st) {
   const long long ncols = (long long)v.batch * v.n_el * NK;
-  const long long total = (long long)v.batch * v.n_el * v.nk;
-  flux_kernel<NK><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(x, y, v.kvec, v.qd, fb, v.n_el, v.nk, total);
+  flux_launch<NK>(x, y, v.kvec, v.qd, fb, v.batch, v.n_el, v.nk, 0.0, st);
   const double2* phi = reinterpret_cast<const double2*>(v.phi);
   dim3 g1((unsigned)((ncols + GBN - 1) / GBN), (v.n_xi + GBM - 1) / GBM);
   zgemm_kernel<0><<<g1, 256, 0, st>>>(phi, v.nk, x, xh, v.n_xi, v.nk, ncols);
-  const long long nelem = (long long)v.batch * v.n_el;
-  stencil_kernel<NK><<<(unsigned)((nelem * v.n_xi + 255) / 256), 256, 0, st>>>(xh, yh, v.beta, v.betai, v.n_xi, nelem);
+  stencil_launch<NK>(xh, yh, v.beta, v.betai, v.batch, v.n_el, v.n_xi, st);
   dim3 g2((unsigned)((ncols + GBN - 1) / GBN), (v.nk + GBM - 1) / GBM);
   zgemm_kernel<1><<<g2, 256, 0, st>>>(phi, v.nk, yh, y, v.nk, v.n_xi, ncols);
   return cudaGetLastError();

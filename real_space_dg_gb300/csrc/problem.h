@@ -40,6 +40,7 @@ struct HostProblem {
   bool ready = false;
   double l_chi = 0;                 // device length [m]
   double qd = 0;                    // Q_diff * mpc / detJ
+  double ef_l = 0, ef_r = 0;        // contact Fermi levels [eV]
   std::vector<double> m_nodes;      // mass at the DG nodes [kg]
 };
 
@@ -127,6 +128,7 @@ struct GummelDev {
 struct GummelHost {
   bool ready = false;
   double bias = 0;
+  bool step_pending = false;   // a transient bias step waits for its potential re-solve
 };
 
 struct Problem {
@@ -143,6 +145,7 @@ struct Problem {
   double device_bytes = 0;
   double mem_budget = 0;
   FluxBlocks fb{};
+  double shift = 0;         // sigma of the shifted operator A + sigma I (0: the stationary A)
   std::string err;
 
   std::vector<HostProblem> hp;
@@ -154,8 +157,8 @@ struct Problem {
   double* xi_edge = nullptr;     // nxi + 1
   double* kap = nullptr;         // nK*nK*10
   double* betai = nullptr;       // [nK*nK][nxi+1] CAP part of the potential weights (imaginary)
-  double* pre_dinv = nullptr;    // [nk][nK*nK] inverse of k K1 + |k| K2
-  double* pre_h = nullptr;       // [nk][nK] D0^-1 * coupling column
+  double* pre_dinv = nullptr;    // [B][nk][nK*nK] inverse of k K1 + |k| K2 + shift/qd_b
+  double* pre_h = nullptr;       // [B][nk][nK] that inverse times the coupling column
   double* cosm = nullptr;        // [nxi][nk] cos(xi_s k_j)
   double2* pinv = nullptr;       // [nk][nxi] pseudo-inverse of Phi
   // per-problem device data
@@ -170,6 +173,7 @@ struct Problem {
   int nx = 0;
   // vectors
   double2* rhs = nullptr;        // [B*N]
+  double2* tr_b = nullptr;       // [B*N] Crank-Nicolson right-hand side (allocated by the first transient)
   double2* x = nullptr;          // [B*N] solution (resident across solves)
   double2* w = nullptr;          // [B*N] work
   double2* z = nullptr;          // [B*N] work
@@ -191,6 +195,7 @@ struct Problem {
   double* inv64 = nullptr;       // [B] inverse basis-vector norms
   double* target = nullptr;      // [B] absolute residual targets
   int* active = nullptr;         // [B] 1 while iterating in this cycle
+  int* reorth = nullptr;         // [B] 1 where the current Arnoldi step re-orthogonalises
   int* kused = nullptr;          // [B] iterations used in this cycle
   int* any_active = nullptr;     // [1]
   int nchunk = 0;  // 2048-element chunks of one problem vector (multi-dot partials)
@@ -217,6 +222,8 @@ void prof_release(Problem& P);
 // Kernel launchers (operator.cu)
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y);
 cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z);
+// k-line factors of A + sigma I for every problem (sigma = P.shift), uploaded to pre_dinv / pre_h.
+int set_kline_factors(Problem& P);
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y);
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh);
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
@@ -248,6 +255,12 @@ int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info*
 int gummel_set(Problem& P, int b, const wg_device& dev, const wg_rtd_1d& rtd);
 int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info);
 int gummel_get(Problem& P, int b, double* phi, double* n_dg, double* j);
+cudaError_t gummel_observables(Problem& P);                               // ndg, jdg of every problem from x
+cudaError_t gummel_poisson(Problem& P, const int* active_dev, bool linear);  // cand, diag
+cudaError_t gummel_potential(Problem& P, const int* active_dev);          // pot_v = Vc - phi
+cudaError_t gummel_mix(Problem& P, const int* mix_dev, double alpha);
+int transient_set_bias(Problem& P, int b, double bias);
+int transient_run(Problem& P, const wg_transient_opts& o, double* n_hist, double* j_hist, wg_transient_info* info);
 void gummel_free(Problem& P);
 
 }  // namespace wg

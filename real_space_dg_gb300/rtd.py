@@ -7,6 +7,12 @@ potentialTolerance, densityTolerance, poissonResidualTolerance; results with a
 for the 1D transport of solve_transport_DG_2D.  The Gummel loop, the Poisson
 step and every transport solve run in libwigner_gb300.so.
 
+``solve_transient_self_consistent(mat, bias0, steps, options)`` follows
+DG_code/solve_transport_DG_2D_transient_SC_new.m:1-221: from the stationary
+self-consistent state at bias0 (the reference's INIT) every problem of the
+batch takes a drain-bias step at t = 0 and is integrated in time (RK4 or
+Crank-Nicolson) with the potential re-solved on the reference's schedule.
+
 Two sweep modes:
   * ``sequential``: the reference's bias continuation, one bias after another,
     each seeded by the converged potential and Wigner function of the last;
@@ -85,6 +91,26 @@ class RTDSweep:
         self.P._check(self.lib.wg_gummel_get(self.P.h, int(b), _lib.dptr(phi), _lib.dptr(n), _lib.dptr(j)))
         return phi, n, j
 
+    def step_bias(self, b, bias):
+        """Drain-bias step of problem b at t = 0 of the next transient()."""
+        self.P._check(self.lib.wg_transient_set_bias(self.P.h, int(b), float(bias)))
+
+    def transient(self, dt, nsteps, method="cn", scale_a=0.0, scale_rhs=0.0, refresh_every=0, refresh_first=0,
+                  tol=0.0, maxit=0, record_every=1):
+        """Advance every problem by nsteps; returns (status, info, n [nrec, batch, ncol], j)."""
+        if method not in _lib.TRANSIENT_METHODS:
+            raise WignerError(_lib.WG_ERR_ARG, "unknown transient method %r" % (method,))
+        o = _lib.WgTransientOpts(float(dt), int(nsteps), _lib.TRANSIENT_METHODS[method], float(scale_a),
+                                 float(scale_rhs), int(refresh_every), int(refresh_first), float(tol), int(maxit),
+                                 int(record_every))
+        nrec = nsteps // record_every if record_every > 0 else 0
+        n = np.zeros((nrec, self.P.batch, self.P.ncol))
+        j = np.zeros((nrec, self.P.batch, self.P.ncol))
+        info = (_lib.WgTransientInfo * self.P.batch)()
+        st = self.lib.wg_transient_run(self.P.h, C.byref(o), _lib.dptr(n), _lib.dptr(j), info)
+        self.P._check(st, allow_not_converged=True)
+        return st, [i.as_dict() for i in info], n, j
+
 
 def solve_rtd_self_consistent(mat, biases, options=None, mode="batched"):
     """results = solve2D_rtd_self_consistent('DG', mat, options) for the 1D path.
@@ -134,3 +160,45 @@ def solve_rtd_self_consistent(mat, biases, options=None, mode="batched"):
     return {"sweep": sweep, "Id": Id,
             "selfConsistency": {"converged": bool(all(sweep["converged"]) and len(sweep["converged"]) == nb),
                                 "iterations": sweep["iterations"], "status": sweep["status"]}}
+
+
+TRANSIENT_DEFAULTS = dict(dt=1e-15, steps=100, method="cn", scaleA=2e-10, scaleRhs=0.0, refreshEvery=20,
+                          refreshFirst=50, stepTolerance=1e-10, stepMaxCycles=20, recordEvery=1)
+
+
+def solve_transient_self_consistent(mat, bias0, steps, options=None, transient=None):
+    """DG = solve_transport_DG_2D_transient_SC_new(mat, INIT) for the 1D RTD, batched.
+
+    bias0: the stationary bias of INIT; steps: the bias after the step, one
+    transient per entry, all advanced together.  ``options`` are the Gummel
+    options of the stationary state (solve_rtd_self_consistent); ``transient``
+    overrides TRANSIENT_DEFAULTS.  Returns n_over_t / j_over_t as
+    [n_el*n_local, nrec, n_transients] (DG.n_over_t / DG.j_over_t), the time
+    axis t, the final potential phi and per-transient info.
+    """
+    steps = np.atleast_1d(np.asarray(steps, dtype=float))
+    T = dict(TRANSIENT_DEFAULTS)
+    for k, v in (transient or {}).items():
+        if k not in T:
+            raise WignerError(_lib.WG_ERR_ARG, "unknown transient option %s" % k)
+        T[k] = v
+    S = RTDSweep(mat, len(steps), options)
+    try:
+        for b in range(len(steps)):
+            S.set(b, bias0)
+        st, ginfo = S.run()
+        if st != 0:
+            raise WignerError(st, "stationary state at bias0 did not converge: %s" % [g["status"] for g in ginfo])
+        for b, v in enumerate(steps):
+            S.step_bias(b, v)
+        st, info, n, j = S.transient(T["dt"], int(T["steps"]), T["method"], T["scaleA"], T["scaleRhs"],
+                                     int(T["refreshEvery"]), int(T["refreshFirst"]), T["stepTolerance"],
+                                     int(T["stepMaxCycles"]), int(T["recordEvery"]))
+        phi = np.array([S.get(b)[0] for b in range(len(steps))]).T
+    finally:
+        S.close()
+    rec = int(T["recordEvery"])
+    t = T["dt"] * rec * np.arange(1, n.shape[0] + 1)
+    return {"n_over_t": np.transpose(n, (2, 0, 1)), "j_over_t": np.transpose(j, (2, 0, 1)), "t": t, "phi": phi,
+            "status": st, "info": info, "stationary": ginfo}
+
