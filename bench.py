@@ -182,7 +182,7 @@ def run_ours(args, rank, world, dist):
 
     spec, mat, biases = make_workload(args.batch)
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
-                innerTol=args.inner_tol, inexactFactor=args.inexact)
+                innerTol=args.inner_tol, inexactFactor=args.inexact, reorth=args.reorth, innerReorth=args.inner_reorth)
     if args.max_gummel:
         opts["maxIterations"] = args.max_gummel      # profiling runs only: points need not converge
     S = RTDSweep(mat, args.batch, opts)
@@ -251,6 +251,7 @@ def run_ours(args, rank, world, dist):
                    "precision": args.precision, "gmres_restart": args.restart,
                    "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
                    "inexact_gummel_factor": args.inexact, "gummel_mixing": 0.3,
+                   "reorth": args.reorth, "inner_reorth": args.inner_reorth,
                    "potential_tol_v": 1e-6, "transport_rtol": 1e-8,
                    "l2": "inputs larger than L2 (Krylov basis %.2f GB)" %
                          (16.0 * (args.restart + 1) * args.batch * spec.n_el * (spec.order + 1) * spec.nk / 1e9)},
@@ -309,12 +310,137 @@ def run_reference(args, rank, world, dist):
                                           "d2h_bytes_per_step": 0}}
 
 
+SERVED = dict(devices=12, biases_per_device=8, rate_hz=20.0, budget_bytes=150e9, max_slots=8, seed=2026)
+
+
+def served_requests(seed):
+    """The mixed-shape I-V workload: devices with seeded random barrier height
+    U(0.20, 0.35) eV, barrier width U(2, 4) nm and well width U(4, 6) nm, each on a
+    grid drawn from Nk in {128, 256, 512}, N_el in {120, 240, 480}, p in {1, 2, 3},
+    swept over biases drawn from U(0, 0.6) V; requests arrive as a Poisson process."""
+    from real_space_dg_gb300 import devices
+    rng = np.random.default_rng(seed)
+    jobs, shapes = [], []
+    for d in range(SERVED["devices"]):
+        spec = devices.RTDSpec(**dict(SPEC, barrier_ev=rng.uniform(0.20, 0.35), barrier_nm=rng.uniform(2, 4),
+                                      well_nm=rng.uniform(4, 6), nk=int(rng.choice([128, 256, 512])),
+                                      n_el=int(rng.choice([120, 240, 480])), order=int(rng.choice([1, 2, 3]))))
+        mat = devices.make_mat(spec)
+        mat["dy_norm_nm"] = devices.density_normalisation_nm(mat)
+        shapes.append((spec.n_el, spec.order, spec.nk))
+        for v in rng.uniform(0.0, 0.6, SERVED["biases_per_device"]):
+            jobs.append((mat, float(v), d))
+    order = rng.permutation(len(jobs))
+    jobs = [jobs[i] for i in order]
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVED["rate_hz"], len(jobs)))
+    arrivals -= arrivals[0]
+    return jobs, arrivals, shapes
+
+
+def run_served(args):
+    """Continuous-batching server on the mixed-shape I-V workload: throughput and latency."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300.serve import Server, serve_sweep
+    jobs, arrivals, shapes = served_requests(SERVED["seed"])
+    opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
+                innerTol=args.inner_tol, inexactFactor=args.inexact, reorth=args.reorth, innerReorth=args.inner_reorth)
+    clocks = ClockSampler()
+    clocks.start()
+    with Server(opts, mem_budget_bytes=SERVED["budget_bytes"], max_slots=SERVED["max_slots"], warm_start=True) as S:
+        res, wall = serve_sweep(S, jobs, arrivals)
+        stats = S.stats()
+    clk = clocks.stop()
+    lat = np.array([r["latency"] for r in res if r["state"] == "done"])
+    conv = sum(r["status"] == "fixed-point-converged" for r in res)
+    unknowns = sum(n_el * (p + 1) * nk for (mat, v, d) in jobs for (n_el, p, nk) in [shapes[d]])
+    return {
+        "metric": "served converged bias points/s (mixed-shape I-V sweep, continuous batching)",
+        "value": round(conv / wall, 4), "unit": UNIT, "n_gpus": 1, "higher_is_better": True,
+        "dtype": "f64" if args.precision == "fp64" else "bf16/f32 in f64 refinement",
+        "data": "synthetic RTD devices, seeded random barriers and grids, Poisson arrivals",
+        "config": {"workload": "%d devices x %d biases U(0,0.6) V, Nk {128,256,512}, N_el {120,240,480}, "
+                               "p {1,2,3}, %g req/s, %g GB budget" % (SERVED["devices"], SERVED["biases_per_device"],
+                                                                       SERVED["rate_hz"], SERVED["budget_bytes"] / 1e9),
+                   "shapes": shapes, "precision": args.precision, "inexact_gummel_factor": args.inexact,
+                   "max_slots": SERVED["max_slots"], "unknowns_per_point_mean": unknowns / len(jobs)},
+        "wall_s": round(wall, 3), "requests": len(jobs), "converged_points": int(conv),
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "definition": "request arrival to result"},
+        "warm_started": int(sum(r["warm"] > 0 for r in res)),
+        "gummel_iterations_per_point": float(np.mean([r["info"]["iterations"] for r in res])),
+        "server": stats, "clocks": clk,
+    }
+
+
+TRANSIENT = dict(batch=16, order=2, n_el=240, nk=512, dt=1e-15, seed=2027)
+
+
+def run_transient(args):
+    """Crank-Nicolson bias-step transients of the C5 RTD, batched; every step one
+    shifted GMRES solve per transient and a Poisson re-solve (refresh every step)."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300 import devices
+    from real_space_dg_gb300.rtd import RTDSweep
+    rng = np.random.default_rng(TRANSIENT["seed"])
+    B = TRANSIENT["batch"]
+    widths = rng.uniform(2.0, 4.0, B)
+    steps_v = rng.uniform(0.1, 0.4, B)
+    base = dict(SPEC, order=TRANSIENT["order"], n_el=TRANSIENT["n_el"], nk=TRANSIENT["nk"])
+    opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
+                innerTol=args.inner_tol, inexactFactor=args.inexact, reorth=args.reorth, innerReorth=args.inner_reorth)
+    # one handle; the problems differ in their barrier width (device data per problem)
+    mats = []
+    for w in widths:
+        spec = devices.RTDSpec(**dict(base, barrier_nm=float(w)))
+        mat = devices.make_mat(spec)
+        mat["dy_norm_nm"] = devices.density_normalisation_nm(mat)
+        mats.append(mat)
+    S = RTDSweep(mats[0], B, opts)
+    for b in range(B):
+        S.set(b, 0.0, mat=mats[b])
+    st, info = S.run()                                   # stationary state at 0 V (INIT)
+    for b in range(B):
+        S.step_bias(b, float(steps_v[b]))
+    kw = dict(refresh_every=1, refresh_first=1, tol=1e-8, maxit=20, record_every=0)
+    S.transient(TRANSIENT["dt"], args.warmup, "cn", **kw)          # untimed
+    clocks = ClockSampler()
+    clocks.start()
+    S.P.profile(on=False, reset=True)
+    S.P.event(0)
+    st, tinfo, _, _ = S.transient(TRANSIENT["dt"], args.steps, "cn", **kw)
+    S.P.event(1)
+    ms = S.P.elapsed_ms(0, 1)
+    counted = S.P.profile(on=False, reset=True)
+    clk = clocks.stop()
+    S.close()
+    n = TRANSIENT["n_el"] * (TRANSIENT["order"] + 1) * TRANSIENT["nk"]
+    return {
+        "metric": "Crank-Nicolson transient steps/s (C5 RTD, %d transients batched)" % B,
+        "value": round(B * args.steps / (ms / 1000.0), 3), "unit": "problem_steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "bf16/f32 in f64 refinement",
+        "data": "synthetic RTD devices (seeded barrier widths and bias steps)",
+        "config": {"workload": "C5 transient RTD p=2, N_el=240, Nk=512, %d unknowns per transient, dt=1 fs, "
+                               "Poisson every step" % n, "batch": B, "stationary_status": int(st),
+                   "step_tolerance": 1e-8, "precision": args.precision},
+        "gmres_iterations_per_step": float(np.mean([t["gmres_iterations"] for t in tinfo])) / max(1, args.steps),
+        "max_step_relres": float(max(t["max_relres"] for t in tinfo)),
+        "gpu_launches": int(sum(v[2] for v in counted.values())), "clocks": clk,
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient"],
+                    help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
+                         "transient: batched Crank-Nicolson steps of the C5 RTD")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--restart", type=int, default=50)
@@ -324,6 +450,10 @@ def main():
                     help="cap on Gummel iterations for profiling runs (0: run to convergence)")
     ap.add_argument("--inexact", type=float, default=1e-2,
                     help="inexact Gummel factor (transport tol = factor * potential defect); 0 = fixed 1e-8")
+    ap.add_argument("--reorth", type=float, default=0.0,
+                    help="DGKS re-orthogonalisation threshold of the FP64 Arnoldi (0: 1/sqrt(2), <0 never, >=1 always)")
+    ap.add_argument("--inner-reorth", type=float, default=0.0,
+                    help="the same for the mixed form's inner FP32 Arnoldi (0: never, one classical pass)")
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--iters-per-point", type=float, default=ITERS_PER_POINT_FALLBACK)
     ap.add_argument("--no-e2e", action="store_true")
@@ -332,6 +462,10 @@ def main():
     rank, world, dist = dist_setup()
     if args.impl == "reference":
         out = run_reference(args, rank, world, dist)
+    elif args.workload == "served":
+        out = run_served(args) if rank == 0 else None
+    elif args.workload == "transient":
+        out = run_transient(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

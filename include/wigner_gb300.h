@@ -32,9 +32,11 @@
  *    -> wg_solve_info
  *  - Gummel loop of RTD/solve2D_rtd_self_consistent.m:88-205 with the Poisson
  *    step of RTD/solve_Poisson2D_rtd.m:56-186 (1D, Ny = 1)
- *    -> wg_gummel_create / wg_gummel_run
+ *    -> wg_gummel_set / wg_gummel_run / wg_gummel_get
  *  - RK4 loop of DG_code/solve_transport_DG_2D_transient_SC_new.m:124-212
- *    (Crank-Nicolson replaces RK4)                   -> wg_transient_step
+ *    (RK4 kept, Crank-Nicolson added)                -> wg_transient_set_bias / wg_transient_run
+ *  - the bias loop of RTD/solve2D_rtd_self_consistent.m, served: requests of
+ *    mixed shapes admitted under a device-memory budget -> wg_server_*
  */
 #ifndef WIGNER_GB300_H
 #define WIGNER_GB300_H
@@ -70,6 +72,11 @@ typedef struct {
   double mem_budget_bytes; /* admission budget for this handle; 0 -> no limit */
   int inner_restart; /* mixed form: inner FP32 GMRES length; 0 -> 40 */
   double inner_tol;  /* mixed form: floor of the inner relative tolerance; 0 -> 1e-3 */
+  double reorth;     /* Gram-Schmidt: a second classical pass when |w1| < reorth |w| (Daniel-Gragg-
+                        Kaufman-Stewart test); 0 -> 1/sqrt(2); >= 1: always (CGS2); < 0: never (CGS) */
+  double inner_reorth; /* the same for the mixed form's inner FP32 solve; 0 -> never (one classical pass:
+                          the inner solve only has to reduce the residual by inner_tol, and the FP64
+                          refinement keeps the accuracy; a second pass measured 25% slower, same iterations) */
 } wg_params;
 
 /* One problem's device/material data on the material grid (mat.x, nm). */
@@ -102,6 +109,9 @@ typedef struct wg_problem wg_problem;
 /* Create a handle for `batch` problems.  Allocates all device memory. */
 int wg_problem_create(const wg_params* prm, int batch, wg_problem** out);
 int wg_problem_destroy(wg_problem* h);
+/* Device bytes a handle of `batch` problems would allocate (the admission estimate
+ * of wg_problem_create, GmresMemoryLimit analogue of solve_transport_DG_full2D.m:198). */
+int wg_problem_bytes(const wg_params* prm, int batch, double* bytes);
 const char* wg_last_error(const wg_problem* h);
 /* Library-level last error (for failures before a handle exists). */
 const char* wg_global_error(void);
@@ -248,6 +258,72 @@ int wg_transient_set_bias(wg_problem* h, int b, double bias);
  * n in m^-3 as wg_gummel_get.  info has batch entries. */
 int wg_transient_run(wg_problem* h, const wg_transient_opts* opts, double* n_hist, double* j_hist,
                      wg_transient_info* info);
+
+/* ---- Serving: continuous batching of self-consistent bias points -----------
+ * A request is one point of an I-V sweep (the bias loop of
+ * RTD/solve2D_rtd_self_consistent.m run through wg_gummel_*).  Requests of equal
+ * shape (n_el, n_local, nk, n_xi, l_xi) share a handle of max_slots problems; a
+ * worker thread per handle admits queued requests into free slots between Gummel
+ * iterations while the other slots keep iterating, and retires each slot the
+ * moment its own loop ends.  Handles of different shapes run on their own
+ * streams, so their work overlaps on the device.  A handle is created only when
+ * its estimated bytes fit the device-memory budget next to the live handles, and
+ * released when it has been idle for idle_release_s while others wait for memory.
+ * Warm start: a request is seeded from the nearest finished bias with the same
+ * device_key and shape -- in the same slot when free (Wigner function and
+ * potential resident on the device), else from that bias' potential. */
+typedef struct {
+  double mem_budget_bytes;     /* device bytes for all handles; 0 -> 150e9 */
+  int max_slots;               /* problems per handle; 0 -> 8 */
+  int precision;               /* WG_PREC_FP64 or WG_PREC_MIXED */
+  int restart, inner_restart;  /* 0 -> 50, 40 */
+  double inner_tol;            /* 0 -> 1e-3 */
+  double reorth, inner_reorth; /* Gram-Schmidt thresholds as in wg_params */
+  wg_gummel_opts gummel;       /* loop options of every request (warm_start, restart_from_phi0 unused) */
+  int warm_start;              /* 1: seed requests from neighbouring biases */
+  double idle_release_s;       /* 0 -> 0.5 */
+} wg_server_opts;
+
+typedef struct {
+  int n_el, n_local, nk, n_xi;  /* shape (wg_params) */
+  double l_xi, m_diff, mpc;     /* as in wg_params (0 -> the reference's defaults) */
+  wg_device dev;                /* copied at submission */
+  wg_rtd_1d rtd;                /* copied at submission (phi0 = the cold-start potential) */
+  long long device_key;         /* requests of one device share warm starts */
+} wg_request;
+
+enum { WG_REQ_QUEUED = 0, WG_REQ_RUNNING = 1, WG_REQ_DONE = 2, WG_REQ_FAILED = 3 };
+
+typedef struct {
+  int state;                   /* WG_REQ_* */
+  wg_gummel_info info;         /* the request's Gummel loop (status WG_GUMMEL_*) */
+  double t_submit, t_admit, t_done;  /* seconds since wg_server_create */
+  int handle, slot;            /* where it ran */
+  int warm;                    /* 0 cold, 1 potential seeded, 2 potential and Wigner function resident */
+  char error[192];             /* why a request failed (WG_REQ_FAILED), else empty */
+} wg_request_status;
+
+typedef struct {
+  int handles;                 /* live handles */
+  int queued, running;         /* requests */
+  long long done, failed;
+  double device_bytes, device_bytes_peak;  /* estimated bytes of the live handles */
+} wg_server_stats;
+
+typedef struct wg_server wg_server;
+int wg_server_create(const wg_server_opts* opts, wg_server** out);
+/* Queue a request (all inputs are copied); *id identifies it. */
+int wg_server_submit(wg_server* s, const wg_request* req, long long* id);
+/* Wait up to timeout_s (< 0: no limit) for the request to finish.  WG_OK with st
+ * filled once it is done or failed; WG_ERR_TIMEOUT (st filled) otherwise. */
+int wg_server_wait(wg_server* s, long long id, double timeout_s, wg_request_status* st);
+/* Results of a finished request: phi [nx], n_dg and j [n_el*n_local] (any may be NULL). */
+int wg_server_result(wg_server* s, long long id, double* phi, double* n_dg, double* j);
+/* Forget a finished request (its stored results). */
+int wg_server_release(wg_server* s, long long id);
+int wg_server_stats_get(wg_server* s, wg_server_stats* st);
+/* Finish the queued and running requests, stop the workers, free every handle. */
+int wg_server_destroy(wg_server* s);
 
 /* ---- Allocation-free operator apply ----------------------------------------
  * No counterpart in the reference.  For callers that cannot call cudaMalloc

@@ -25,7 +25,7 @@ class WgParams(C.Structure):
     _fields_ = [("n_el", C.c_int), ("n_local", C.c_int), ("nk", C.c_int), ("n_xi", C.c_int),
                 ("l_xi", C.c_double), ("m_diff", C.c_double), ("mpc", C.c_double), ("precision", C.c_int),
                 ("restart", C.c_int), ("mem_budget_bytes", C.c_double), ("inner_restart", C.c_int),
-                ("inner_tol", C.c_double)]
+                ("inner_tol", C.c_double), ("reorth", C.c_double), ("inner_reorth", C.c_double)]
 
 
 class WgDevice(C.Structure):
@@ -88,6 +88,35 @@ class WgTransientInfo(C.Structure):
 TRANSIENT_METHODS = {"cn": 0, "rk4": 1}
 
 
+class WgServerOpts(C.Structure):
+    _fields_ = [("mem_budget_bytes", C.c_double), ("max_slots", C.c_int), ("precision", C.c_int),
+                ("restart", C.c_int), ("inner_restart", C.c_int), ("inner_tol", C.c_double),
+                ("reorth", C.c_double), ("inner_reorth", C.c_double), ("gummel", WgGummelOpts), ("warm_start", C.c_int), ("idle_release_s", C.c_double)]
+
+
+class WgRequest(C.Structure):
+    _fields_ = [("n_el", C.c_int), ("n_local", C.c_int), ("nk", C.c_int), ("n_xi", C.c_int), ("l_xi", C.c_double),
+                ("m_diff", C.c_double), ("mpc", C.c_double), ("dev", WgDevice), ("rtd", WgRtd1D),
+                ("device_key", C.c_longlong)]
+
+
+class WgRequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int), ("info", WgGummelInfo), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double), ("handle", C.c_int), ("slot", C.c_int), ("warm", C.c_int),
+                ("error", C.c_char * 192)]
+
+
+class WgServerStats(C.Structure):
+    _fields_ = [("handles", C.c_int), ("queued", C.c_int), ("running", C.c_int), ("done", C.c_longlong),
+                ("failed", C.c_longlong), ("device_bytes", C.c_double), ("device_bytes_peak", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+
+
 class WgSolveInfo(C.Structure):
     _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("cycles", C.c_int), ("refinements", C.c_int),
                 ("relres", C.c_double), ("initial_relres", C.c_double), ("rhs_norm", C.c_double)]
@@ -102,6 +131,7 @@ _D = C.POINTER(C.c_double)
 SIGNATURES = {
     "wg_problem_create": ([C.POINTER(WgParams), C.c_int, C.POINTER(_H)], C.c_int),
     "wg_problem_destroy": ([_H], C.c_int),
+    "wg_problem_bytes": ([C.POINTER(WgParams), C.c_int, _D], C.c_int),
     "wg_last_error": ([_H], C.c_char_p),
     "wg_global_error": ([], C.c_char_p),
     "wg_problem_sizes": ([_H, C.POINTER(C.c_longlong), C.POINTER(C.c_int), _D], C.c_int),
@@ -119,6 +149,13 @@ SIGNATURES = {
     "wg_gummel_get": ([_H, C.c_int, _D, _D, _D], C.c_int),
     "wg_transient_set_bias": ([_H, C.c_int, C.c_double], C.c_int),
     "wg_transient_run": ([_H, C.POINTER(WgTransientOpts), _D, _D, C.POINTER(WgTransientInfo)], C.c_int),
+    "wg_server_create": ([C.POINTER(WgServerOpts), C.POINTER(_H)], C.c_int),
+    "wg_server_submit": ([_H, C.POINTER(WgRequest), C.POINTER(C.c_longlong)], C.c_int),
+    "wg_server_wait": ([_H, C.c_longlong, C.c_double, C.POINTER(WgRequestStatus)], C.c_int),
+    "wg_server_result": ([_H, C.c_longlong, _D, _D, _D], C.c_int),
+    "wg_server_release": ([_H, C.c_longlong], C.c_int),
+    "wg_server_stats_get": ([_H, C.POINTER(WgServerStats)], C.c_int),
+    "wg_server_destroy": ([_H], C.c_int),
     "wg_apply_noalloc": ([C.POINTER(WgOperatorView), C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "wg_debug_gemm_bf16": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
                             C.c_int], C.c_int),

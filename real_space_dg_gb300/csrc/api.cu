@@ -8,11 +8,8 @@
 #include <string>
 #include <vector>
 
+#include "kline.cuh"
 #include "problem.h"
-
-struct wg_problem {
-  wg::Problem P;
-};
 
 namespace {
 
@@ -46,7 +43,7 @@ void free_all(wg::Problem& P) {
       e = nullptr;
     }
   wg::gummel_free(P);
-  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
+  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.kmap_a, P.kmap_s, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
                   P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.kused, P.any_active};
   for (void* p : ptrs)
@@ -85,6 +82,17 @@ bool inv_small(const double* A, double* out, int n) {
 }  // namespace
 
 namespace wg {
+
+double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision) {
+  const int nK = s.nK;
+  const double N = (double)s.n_el * nK * s.nk, BN = N * batch, ncols = (double)batch * s.n_el * nK;
+  const double nx = (double)s.n_el * (nK - 1) + 1;
+  double est = 16.0 * BN * (5 + restart + 1) + 16.0 * 2 * s.nxi * ncols +
+               8.0 * batch * s.n_el * nK * nK * (s.nxi + 1) + 16.0 * s.nxi * s.nk;
+  est += 8.0 * batch * (nx * (8 + 2 * kMaxLocal) + 3.0 * s.n_el * nK + 12);   // Gummel state
+  if (precision == WG_PREC_MIXED) est += mixed_bytes(s, batch, restart_inner);
+  return est;
+}
 
 // k-line factors of the flux part of A + sigma I, per problem b and wave number k:
 // D_b(k) = (k K1 + |k| K2 + (sigma / qd_b) I)^-1 and h = D_b(k) * upwind coupling column
@@ -180,6 +188,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   P.restart_inner = prm->inner_restart > 0 ? prm->inner_restart : 40;
   P.restart_max = std::max(P.restart, P.restart_inner);
   P.inner_tol = prm->inner_tol > 0 ? prm->inner_tol : 1e-3;
+  if (prm->reorth != 0) P.reorth_eta = prm->reorth;
+  P.inner_reorth_eta = prm->inner_reorth != 0 ? prm->inner_reorth : -1.0;
   if (P.restart_max > 256) {
     delete h;
     return fail(nullptr, WG_ERR_ARG, "wg_problem_create: restart lengths must be <= 256");
@@ -203,9 +213,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   const int mp1 = P.restart + 1;
   const int pst = P.restart_max + 1;
   // memory estimate before allocating (GmresMemoryLimit analogue)
-  double est = 16.0 * BN * (5 + mp1) + 16.0 * 2 * s.nxi * P.ncols +
-               8.0 * batch * s.n_el * nK * nK * (s.nxi + 1) + 16.0 * s.nxi * s.nk;
-  if (P.precision == WG_PREC_MIXED) est += wg::mixed_bytes(s, batch, P.restart_inner);
+  const double est = wg::estimate_bytes(s, batch, P.restart, P.restart_inner, P.precision);
   if (P.mem_budget > 0 && est > P.mem_budget) {
     delete h;
     return fail(nullptr, WG_ERR_OOM,
@@ -233,6 +241,15 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.betai, (size_t)nK * nK * (s.nxi + 1), bytes));
   A(dalloc(&P.pre_dinv, (size_t)batch * s.nk * nK * nK, bytes));
   A(dalloc(&P.pre_h, (size_t)batch * s.nk * nK, bytes));
+  {
+    const size_t nmap = (size_t)batch * wg::kline::chunk_count(s.n_el) * s.nk;
+    double* a = nullptr;
+    double2* m = nullptr;
+    A(dalloc(&a, nmap, bytes));
+    A(dalloc(&m, nmap, bytes));
+    P.kmap_a = a;
+    P.kmap_s = m;
+  }
   A(dalloc(&P.cosm, (size_t)s.nxi * s.nk, bytes));
   A(dalloc(&P.pinv, (size_t)s.nk * s.nxi, bytes));
   A(dalloc(&P.pp, (size_t)batch * wg::kPP, bytes));
@@ -301,6 +318,14 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   API_CK(&P, cudaMemsetAsync(P.rhs, 0, sizeof(double2) * BN, P.stream));
   API_CK(&P, cudaMemsetAsync(P.x, 0, sizeof(double2) * BN, P.stream));
   API_CK(&P, cudaMemsetAsync(P.beta, 0, sizeof(double) * batch * s.n_el * nK * nK * (s.nxi + 1), P.stream));
+  // a problem never given data is a zero operator with a zero rhs: it is converged and inert
+  API_CK(&P, cudaMemsetAsync(P.qd, 0, sizeof(double) * batch, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.pp, 0, sizeof(double) * batch * wg::kPP, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.flr, 0, sizeof(double) * batch * 2 * s.nk, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.pot_v, 0, sizeof(double) * batch * P.nx, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.pot_x, 0, sizeof(double) * batch * P.nx, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.m_nodes, 0, sizeof(double) * batch * s.n_el * nK, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.xq, 0, sizeof(double) * batch * s.n_el * wg::kNqx, P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
   if (P.precision == WG_PREC_MIXED) {
     const int mr = wg::mixed_alloc(P);
@@ -316,6 +341,17 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   P.h_active.resize(batch);
   P.h_kused.resize(batch);
   *out = h;
+  return WG_OK;
+}
+
+int wg_problem_bytes(const wg_params* prm, int batch, double* bytes) {
+  if (!prm || !bytes || batch < 1) return fail(nullptr, WG_ERR_ARG, "wg_problem_bytes: null argument or batch < 1");
+  wg::Shape s;
+  const std::string e =
+      wg::build_shape_light(s, prm->n_el, prm->n_local, prm->nk, prm->n_xi, prm->l_xi, prm->m_diff, prm->mpc);
+  if (!e.empty()) return fail(nullptr, WG_ERR_ARG, "wg_problem_bytes: " + e);
+  const int restart = prm->restart > 0 ? prm->restart : 50, inner = prm->inner_restart > 0 ? prm->inner_restart : 40;
+  *bytes = wg::estimate_bytes(s, batch, restart, inner, prm->precision);
   return WG_OK;
 }
 

@@ -248,11 +248,11 @@ __global__ void dot_reduce_kernel(const double2* __restrict__ partial, double2* 
 }
 
 // Daniel-Gragg-Kaufman-Stewart test after the first classical Gram-Schmidt pass:
-// problem b is re-orthogonalised only if |w1| < |w| / sqrt(2), where w1 = w - V h
-// and |w|^2 = |w1|^2 + |h|^2 (V orthonormal), i.e. only if |w1|^2 < |h|^2.
+// problem b is re-orthogonalised only if |w1| < eta |w|, where w1 = w - V h and
+// |w|^2 = |w1|^2 + |h|^2 (V orthonormal).
 __global__ void reorth_test_kernel(const double* __restrict__ partial, const double2* __restrict__ hcol,
                                    const int* __restrict__ active, int* __restrict__ reorth, int nblk, int nv,
-                                   int pstride) {
+                                   int pstride, double eta2) {
   const int b = blockIdx.x;
   double w2 = 0, h2 = 0;
   for (int c = threadIdx.x; c < nblk; c += 32) w2 += partial[(long long)b * nblk + c];
@@ -262,7 +262,7 @@ __global__ void reorth_test_kernel(const double* __restrict__ partial, const dou
   }
   w2 = warp_sum(w2);
   h2 = warp_sum(h2);
-  if (threadIdx.x == 0) reorth[b] = (active[b] && w2 < h2) ? 1 : 0;
+  if (threadIdx.x == 0) reorth[b] = (active[b] && w2 < eta2 * (w2 + h2)) ? 1 : 0;
 }
 
 // w -= sum_i V_i hcol_i; with NORM, also nrm_partial[b][blockIdx.x] = sum |w|^2 of the block.
@@ -549,10 +549,13 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   const int nv = k + 1;
   const double sz = (double)sizeof(T), vec = (double)N * B * sz;
   const dim3 gu((unsigned)((N + 255) / 256), B);
-  // classical Gram-Schmidt; the second pass runs only for the problems that fail the
-  // DGKS test (its kernels see P.reorth as their activity mask)
-  for (int pass = 0; pass < 2; ++pass) {
-    const int* mask = pass == 0 ? P.active : P.reorth;
+  // classical Gram-Schmidt; the second pass runs for the problems that fail the DGKS
+  // test (its kernels see P.reorth as their activity mask), for all with eta >= 1,
+  // for none with eta < 0
+  const double eta = sizeof(T) == sizeof(float2) ? P.inner_reorth_eta : P.reorth_eta;
+  const int passes = eta < 0 ? 1 : 2;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int* mask = (pass == 0 || eta >= 1) ? P.active : P.reorth;
     cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B);
     multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, mask, N,
                                                                                       nv, mp1, ps, P.nchunk);
@@ -565,9 +568,10 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
     gs_update_kernel<T, true><<<gu, sizeof(T) == sizeof(float2) ? 128 : 256, 0, P.stream>>>(
         V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1, ps, P.nblk);
     prof_end(P, PROF_GSUPDATE, ev);
-    if (pass == 0) {
+    if (pass == 0 && passes == 2 && eta < 1) {
       ev = prof_begin(P, PROF_KRYLOV);
-      reorth_test_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.hcol, P.active, P.reorth, P.nblk, nv, ps);
+      reorth_test_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.hcol, P.active, P.reorth, P.nblk, nv, ps,
+                                                 eta * eta);
       prof_end(P, PROF_KRYLOV, ev);
     }
   }

@@ -99,13 +99,14 @@ __global__ void observables_batched_kernel(const double2* __restrict__ x, const 
   }
   if (lane == 0) {
     const double m = m_nodes[(long long)b * ncol + col];
+    const double pm = m > 0 ? pref / m : 0.0;   // a problem without data stays zero
     double n, jj;
     if (odd) {
       n = umr;
-      jj = pref / m * (u2i - u1i) / 2 / delta_xi;
+      jj = pm * (u2i - u1i) / 2 / delta_xi;
     } else {
       n = (u1r + u2r) / 2;
-      jj = pref / m * (u2i - u1i) / delta_xi;
+      jj = pm * (u2i - u1i) / delta_xi;
     }
     n_out[(long long)b * ncol + col] = n * scale[b];
     j_out[(long long)b * ncol + col] = jj;
@@ -413,8 +414,146 @@ int gummel_set(Problem& P, int b, const wg_device& dev, const wg_rtd_1d& rtd) {
   return WG_OK;
 }
 
+namespace {
+
+struct LoopOpts {
+  int maxit;
+  double alpha, tol_v, tol_n, tol_p, tol, cap;
+  int transport_maxit;
+  bool inexact;
+};
+
+LoopOpts loop_opts(const wg_gummel_opts& o) {
+  LoopOpts L;
+  L.maxit = o.max_iterations > 0 ? o.max_iterations : 100;
+  L.alpha = o.mixing > 0 ? o.mixing : 0.1;
+  L.tol_v = o.potential_tol > 0 ? o.potential_tol : 5e-4;
+  L.tol_n = o.density_tol > 0 ? o.density_tol : 5e-4;
+  L.tol_p = o.poisson_residual_tol > 0 ? o.poisson_residual_tol : 8e-2;
+  L.tol = o.transport_tol > 0 ? o.transport_tol : 1e-8;
+  L.transport_maxit = o.transport_maxit > 0 ? o.transport_maxit : 50;
+  // Inexact Gummel (opt-in): transport tolerance tied to the potential defect,
+  // tol_b = clamp(factor * defect_b, final tol, cap); convergence is accepted only
+  // after a transport solve at the final tolerance with the same potential.
+  L.inexact = o.inexact_factor > 0;
+  L.cap = o.inexact_cap > 0 ? o.inexact_cap : 1e-4;
+  return L;
+}
+
+double clock_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+int gummel_start(Problem& P, int b, const wg_gummel_opts& o, bool warm, bool from_phi0) {
+  if (!P.gd.phi || !P.gh[b].ready || !P.hp[b].ready) {
+    P.err = "Gummel start: problem " + std::to_string(b) + " lacks wg_set_potential/wg_gummel_set";
+    return WG_ERR_ARG;
+  }
+  const int nx = P.nx, ncol = P.s.n_el * P.s.nK;
+  const LoopOpts L = loop_opts(o);
+  GummelHost& gh = P.gh[b];
+  gh.running = 1;
+  gh.it = 0;
+  gh.tol = L.inexact ? std::max(L.cap, L.tol) : L.tol;
+  gh.t0 = clock_s();
+  std::memset(&gh.info, 0, sizeof(wg_gummel_info));
+  gh.info.status = WG_GUMMEL_ITERATION_LIMIT;
+  gh.info.density_change = INFINITY;
+  GummelDev& G = P.gd;
+  GK(cudaMemsetAsync(G.nprev + (long long)b * ncol, 0, sizeof(double) * ncol, P.stream));
+  if (from_phi0)
+    GK(cudaMemcpyAsync(G.phi + (long long)b * nx, G.phi0 + (long long)b * nx, sizeof(double) * nx,
+                       cudaMemcpyDeviceToDevice, P.stream));
+  if (!warm) GK(cudaMemsetAsync(P.x + (long long)b * P.N, 0, sizeof(double2) * P.N, P.stream));
+  return WG_OK;
+}
+
+int gummel_iterate(Problem& P, const wg_gummel_opts& o, int* still_running) {
+  const int B = P.batch;
+  const LoopOpts L = loop_opts(o);
+  GummelDev& G = P.gd;
+  std::vector<int> active(B, 0), mix(B, 0);
+  int n_run = 0;
+  for (int b = 0; b < B; ++b) {
+    active[b] = P.gh[b].running;
+    n_run += active[b];
+  }
+  *still_running = n_run;
+  if (!n_run) return WG_OK;
+  std::vector<double> diag(8 * B);
+  std::vector<wg_solve_info> sinfo(B);
+  struct TolGuard {
+    Problem& P;
+    ~TolGuard() { P.tol_pp.clear(); }
+  } guard{P};
+  GK(cudaMemcpyAsync(G.active, active.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
+  GK(gummel_potential(P, G.active));
+  GK(launch_potential_update(P, 0, B, G.active));
+  // problems outside their loop keep their state: an unreachable target freezes them
+  P.tol_pp.assign(B, 1e300);
+  for (int b = 0; b < B; ++b)
+    if (active[b]) P.tol_pp[b] = P.gh[b].tol;
+  wg_solve_opts so{};
+  so.tol = L.tol;
+  so.maxit = L.transport_maxit;
+  int rc = solve_dispatch(P, so, /*warm=*/true, sinfo.data());
+  if (rc != WG_OK && rc != WG_NOT_CONVERGED) return rc;
+  GK(gummel_observables(P));
+  GK(gummel_poisson(P, G.active, false));
+  GK(cudaMemcpyAsync(diag.data(), G.diag, sizeof(double) * 8 * B, cudaMemcpyDeviceToHost, P.stream));
+  GK(cudaStreamSynchronize(P.stream));
+  const double tnow = clock_s();
+  for (int b = 0; b < B; ++b) {
+    if (!active[b]) continue;
+    GummelHost& gh = P.gh[b];
+    wg_gummel_info& in = gh.info;
+    const int it = ++gh.it;
+    in.iterations = it;
+    in.seconds = tnow - gh.t0;
+    in.gmres_iterations += sinfo[b].iterations;
+    in.transport_relres = sinfo[b].relres;
+    gh.running = 0;
+    if (sinfo[b].flag != 0 || !std::isfinite(sinfo[b].relres)) {
+      in.status = WG_GUMMEL_TRANSPORT_FAILED;
+      continue;
+    }
+    const double* d = &diag[8 * b];
+    in.potential_defect = d[0];
+    in.density_change = it == 1 ? INFINITY : d[1];
+    in.poisson_relres = d[2];
+    if (d[5] == 0 || !(d[3] < 1e-8)) {
+      in.status = WG_GUMMEL_POISSON_FAILED;
+      continue;
+    }
+    const bool conv = in.potential_defect <= L.tol_v && in.density_change <= L.tol_n && in.poisson_relres <= L.tol_p;
+    if (conv && gh.tol <= L.tol) {
+      in.status = WG_GUMMEL_CONVERGED;
+      continue;
+    }
+    if (it >= L.maxit) continue;  // never hand back a potential newer than the transport state
+    gh.running = 1;
+    if (conv) {
+      // converged on a loose transport solve: re-solve at the final tolerance, same potential
+      gh.tol = L.tol;
+      mix[b] = 2;
+      continue;
+    }
+    if (L.inexact) gh.tol = std::min(L.cap, std::max(L.tol, o.inexact_factor * in.potential_defect));
+    mix[b] = 1;
+  }
+  GK(cudaMemcpyAsync(G.mix, mix.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
+  GK(gummel_mix(P, G.mix, L.alpha));
+  GK(cudaStreamSynchronize(P.stream));   // mix[] is a host vector
+  n_run = 0;
+  for (int b = 0; b < B; ++b) n_run += P.gh[b].running;
+  *still_running = n_run;
+  return WG_OK;
+}
+
 int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
-  const int B = P.batch, nx = P.nx, ncol = P.s.n_el * P.s.nK;
+  const int B = P.batch;
   if (!P.gd.phi) {
     P.err = "wg_gummel_run: wg_gummel_set was not called";
     return WG_ERR_ARG;
@@ -424,102 +563,20 @@ int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info) {
       P.err = "wg_gummel_run: problem " + std::to_string(b) + " lacks wg_set_potential/wg_gummel_set";
       return WG_ERR_ARG;
     }
-  const int maxit = o.max_iterations > 0 ? o.max_iterations : 100;
-  const double alpha = o.mixing > 0 ? o.mixing : 0.1;
-  const double tol_v = o.potential_tol > 0 ? o.potential_tol : 5e-4;
-  const double tol_n = o.density_tol > 0 ? o.density_tol : 5e-4;
-  const double tol_p = o.poisson_residual_tol > 0 ? o.poisson_residual_tol : 8e-2;
-  GummelDev& G = P.gd;
-  std::vector<int> active(B, 1), mix(B, 0);
-  std::vector<double> diag(8 * B);
-  std::vector<wg_solve_info> sinfo(B);
   for (int b = 0; b < B; ++b) {
-    std::memset(&info[b], 0, sizeof(wg_gummel_info));
-    info[b].status = WG_GUMMEL_ITERATION_LIMIT;
-    info[b].density_change = INFINITY;
+    const int rc = gummel_start(P, b, o, o.warm_start != 0, o.restart_from_phi0 != 0);
+    if (rc) return rc;
   }
-  GK(cudaMemsetAsync(G.nprev, 0, sizeof(double) * B * ncol, P.stream));
-  if (o.restart_from_phi0)
-    GK(cudaMemcpyAsync(G.phi, G.phi0, sizeof(double) * B * nx, cudaMemcpyDeviceToDevice, P.stream));
-  const auto t0 = std::chrono::steady_clock::now();
-  auto now_s = [&]() { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); };
-  if (!o.warm_start) GK(cudaMemsetAsync(P.x, 0, sizeof(double2) * P.N * B, P.stream));
-  wg_solve_opts so{};
-  so.tol = o.transport_tol > 0 ? o.transport_tol : 1e-8;
-  so.maxit = o.transport_maxit > 0 ? o.transport_maxit : 50;
-  // Inexact Gummel (opt-in): transport tolerance tied to the potential defect,
-  // tol_b = clamp(factor * defect_b, final tol, cap); convergence is accepted only
-  // after a transport solve at the final tolerance with the same potential.
-  const bool inexact = o.inexact_factor > 0;
-  const double cap = o.inexact_cap > 0 ? o.inexact_cap : 1e-4;
-  std::vector<double> tolb(B, inexact ? std::max(cap, so.tol) : so.tol);
-  struct TolGuard {
-    Problem& P;
-    ~TolGuard() { P.tol_pp.clear(); }
-  } guard{P};
-  for (int it = 1; it <= maxit; ++it) {
-    bool any = false;
-    for (int b = 0; b < B; ++b) any |= active[b] != 0;
-    if (!any) break;
-    GK(cudaMemcpyAsync(G.active, active.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
-    GK(gummel_potential(P, G.active));
-    GK(launch_potential_update(P, 0, B));
-    P.tol_pp = tolb;
-    int rc = solve_dispatch(P, so, /*warm=*/true, sinfo.data());
-    if (rc != WG_OK && rc != WG_NOT_CONVERGED) return rc;
-    GK(gummel_observables(P));
-    GK(gummel_poisson(P, G.active, false));
-    GK(cudaMemcpyAsync(diag.data(), G.diag, sizeof(double) * 8 * B, cudaMemcpyDeviceToHost, P.stream));
-    GK(cudaStreamSynchronize(P.stream));
-    const double tnow = now_s();
-    for (int b = 0; b < B; ++b) {
-      mix[b] = 0;
-      if (!active[b]) continue;
-      wg_gummel_info& in = info[b];
-      in.iterations = it;
-      in.seconds = tnow;
-      in.gmres_iterations += sinfo[b].iterations;
-      in.transport_relres = sinfo[b].relres;
-      if (sinfo[b].flag != 0 || !std::isfinite(sinfo[b].relres)) {
-        in.status = WG_GUMMEL_TRANSPORT_FAILED;
-        active[b] = 0;
-        continue;
-      }
-      const double* d = &diag[8 * b];
-      in.potential_defect = d[0];
-      in.density_change = it == 1 ? INFINITY : d[1];
-      in.poisson_relres = d[2];
-      if (d[5] == 0 || !(d[3] < 1e-8)) {
-        in.status = WG_GUMMEL_POISSON_FAILED;
-        active[b] = 0;
-        continue;
-      }
-      const bool conv = in.potential_defect <= tol_v && in.density_change <= tol_n && in.poisson_relres <= tol_p;
-      if (conv && tolb[b] <= so.tol) {
-        in.status = WG_GUMMEL_CONVERGED;
-        active[b] = 0;
-        continue;
-      }
-      if (it == maxit) {
-        active[b] = 0;  // never hand back a potential newer than the transport state
-        continue;
-      }
-      if (conv) {
-        // converged on a loose transport solve: re-solve at the final tolerance, same potential
-        tolb[b] = so.tol;
-        mix[b] = 2;
-        continue;
-      }
-      if (inexact) tolb[b] = std::min(cap, std::max(so.tol, o.inexact_factor * in.potential_defect));
-      mix[b] = 1;
-    }
-    GK(cudaMemcpyAsync(G.mix, mix.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
-    GK(gummel_mix(P, G.mix, alpha));
+  int running = B;
+  while (running > 0) {
+    const int rc = gummel_iterate(P, o, &running);
+    if (rc) return rc;
   }
-  GK(cudaStreamSynchronize(P.stream));
   int status = WG_OK;
-  for (int b = 0; b < B; ++b)
+  for (int b = 0; b < B; ++b) {
+    info[b] = P.gh[b].info;
     if (info[b].status != WG_GUMMEL_CONVERGED) status = WG_NOT_CONVERGED;
+  }
   return status;
 }
 

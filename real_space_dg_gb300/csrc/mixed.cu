@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "kline.cuh"
 #include "ozaki.cuh"
 #include "problem.h"
 #include "tc_gemm.cuh"
@@ -35,14 +36,15 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
 EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
+  // initialised once, thread-safe (handles may be created from several host threads)
+  static const EncodeTiledFn fn = []() -> EncodeTiledFn {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
+      return reinterpret_cast<EncodeTiledFn>(p);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -103,13 +105,9 @@ void slice_rows_host(const std::vector<double>& A, int M, int K, std::vector<bf1
 template <int EPI>
 cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* ea, const int* eb, double* C, int M,
                          long long Ncol, int K, int* err, cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(oz::gemm_ozaki_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         oz::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static const cudaError_t attr = cudaFuncSetAttribute(oz::gemm_ozaki_kernel<EPI>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, oz::SMEM_BYTES);
+  if (attr != cudaSuccess) return attr;
   dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
   oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err);
   return cudaGetLastError();
@@ -118,13 +116,9 @@ cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* 
 template <int EPI>
 cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, float* D, int M, long long Ncol, int K, int* err,
                         cudaStream_t st) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc::gemm_bf16_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         tc::SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  static const cudaError_t attr = cudaFuncSetAttribute(tc::gemm_bf16_kernel<EPI>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+  if (attr != cudaSuccess) return attr;
   dim3 grid((M + tc::BM - 1) / tc::BM, (unsigned)((Ncol + tc::BN - 1) / tc::BN));
   tc::gemm_bf16_kernel<EPI><<<grid, 128, tc::SMEM_BYTES, st>>>(a, b, D, M, Ncol, K, err);
   return cudaGetLastError();
@@ -247,103 +241,6 @@ __global__ void __launch_bounds__(kFlux32Threads) stencil32_kernel(const float2*
   }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 k-line preconditioner (same chunked affine scan as the FP64 kernel);
-// writes z in FP32 and, optionally, its BF16 copy for GEMM 1.
-// ---------------------------------------------------------------------------
-template <int NK>
-__global__ void precond32_kernel(const float2* __restrict__ r, float2* __restrict__ z, bf162* __restrict__ zb,
-                                 const float* __restrict__ kvec, const float* __restrict__ dinv,
-                                 const float* __restrict__ hvec, const float* __restrict__ qd, int n_el, int nk,
-                                 long long N, long long r_stride) {
-  extern __shared__ float2 shf[];  // [2][P][32]
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-  const int P = blockDim.x >> 5;
-  const int j = blockIdx.x * 32 + lane;
-  const int b = blockIdx.y;
-  const bool valid = j < nk;
-  const int chunk = (n_el + P - 1) / P;
-  const int e_lo = min(n_el, w * chunk), e_hi = min(n_el, (w + 1) * chunk);
-  float D[NK * NK], h[NK];
-  bool fwd = true;
-  float inv_qd = 1.f;
-  const long long bj = (long long)b * nk + j;
-#pragma unroll
-  for (int i = 0; i < NK * NK; ++i) D[i] = valid ? dinv[bj * NK * NK + i] : 0.f;
-#pragma unroll
-  for (int i = 0; i < NK; ++i) h[i] = valid ? hvec[bj * NK + i] : 0.f;
-  if (valid) {
-    fwd = kvec[j] > 0;
-    inv_qd = __frcp_rn(qd[b]);
-  }
-  // row `st` of D and h[st] without dynamic register indexing
-  float Dst[NK];
-  float hst = 0.f;
-#pragma unroll
-  for (int c = 0; c < NK; ++c) Dst[c] = fwd ? D[(NK - 1) * NK + c] : D[c];
-  hst = fwd ? h[NK - 1] : h[0];
-  const float alpha = valid ? -hst : 0.f;
-  const float2* rb = r + (long long)b * r_stride + j;
-  const long long zoff = (long long)b * N + j;
-  const int len = e_hi - e_lo;
-  float2 s = make_float2(0.f, 0.f);
-  float Amul = 1.f;
-  if (valid) {
-    for (int i = 0; i < len; ++i) {
-      const int e = fwd ? e_lo + i : e_hi - 1 - i;
-      const float2* re = rb + (long long)e * NK * nk;
-      float ux = 0.f, uy = 0.f;
-#pragma unroll
-      for (int c = 0; c < NK; ++c) {
-        const float2 rv = re[(long long)c * nk];
-        ux = fmaf(Dst[c], rv.x, ux);
-        uy = fmaf(Dst[c], rv.y, uy);
-      }
-      s = make_float2(ux * inv_qd + alpha * s.x, uy * inv_qd + alpha * s.y);
-      Amul *= alpha;
-    }
-  }
-  shf[(0 * P + w) * 32 + lane] = make_float2(Amul, 0.f);
-  shf[(1 * P + w) * 32 + lane] = s;
-  __syncthreads();
-  if (w == 0 && valid) {
-    float2 acc = make_float2(0.f, 0.f);
-    for (int c = 0; c < P; ++c) {
-      const int cc = fwd ? c : P - 1 - c;
-      const float a = shf[(0 * P + cc) * 32 + lane].x;
-      const float2 bb = shf[(1 * P + cc) * 32 + lane];
-      shf[(1 * P + cc) * 32 + lane] = acc;
-      acc = make_float2(a * acc.x + bb.x, a * acc.y + bb.y);
-    }
-  }
-  __syncthreads();
-  if (!valid) return;
-  s = shf[(1 * P + w) * 32 + lane];
-  for (int i = 0; i < len; ++i) {
-    const int e = fwd ? e_lo + i : e_hi - 1 - i;
-    const float2* re = rb + (long long)e * NK * nk;
-    float2 rv[NK];
-#pragma unroll
-    for (int c = 0; c < NK; ++c) rv[c] = re[(long long)c * nk];
-    float2 snew = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int a = 0; a < NK; ++a) {
-      float ux = 0.f, uy = 0.f;
-#pragma unroll
-      for (int c = 0; c < NK; ++c) {
-        ux = fmaf(D[a * NK + c], rv[c].x, ux);
-        uy = fmaf(D[a * NK + c], rv[c].y, uy);
-      }
-      const float2 zv = make_float2(ux * inv_qd - h[a] * s.x, uy * inv_qd - h[a] * s.y);
-      const long long o = zoff + (long long)(e * NK + a) * nk;
-      z[o] = zv;
-      if (zb) zb[o] = __floats2bfloat162_rn(zv.x, zv.y);
-      if ((fwd && a == NK - 1) || (!fwd && a == 0)) snew = zv;
-    }
-    s = snew;
-  }
-}
 
 __global__ void c2f_kernel(const double2* __restrict__ x, float2* __restrict__ y, long long n) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -396,11 +293,17 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
 
 template <int NK>
 cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb) {
-  const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
-  dim3 grid((P.s.nk + 31) / 32, P.batch);
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 1, (zb ? 20.0 : 16.0) * P.N * P.batch);
-  precond32_kernel<NK><<<grid, 32 * Pw, sizeof(float2) * 2 * Pw * 32, P.stream>>>(
-      r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, P.s.n_el, P.s.nk, P.N, r_stride);
+  const int L = kline::chunk_len(P.s.n_el), nc = kline::chunk_count(P.s.n_el);
+  const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
+  const dim3 block(32, kline::kChunksPerBlock);
+  float* ma = static_cast<float*>(P.kmap_a);
+  float2* ms = static_cast<float2*>(P.kmap_s);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, (zb ? 28.0 : 24.0) * P.N * P.batch);
+  kline::kline_maps_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, ma, ms,
+                                                                    P.s.n_el, P.s.nk, P.N, r_stride, L, nc);
+  kline::kline_apply_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h,
+                                                                     P.mx.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
+                                                                     r_stride, L, nc);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }

@@ -13,6 +13,7 @@
 #include <mutex>
 #include <string>
 
+#include "kline.cuh"
 #include "problem.h"
 
 namespace wg {
@@ -232,105 +233,6 @@ __global__ void __launch_bounds__(kFluxThreads) stencil_kernel(const double2* __
 }
 
 // ---------------------------------------------------------------------------
-// k-line preconditioner: exact inverse of the flux part, per k an upwind
-// block-bidiagonal system over the elements (line operator of
-// get_LineTransversePreconditioner_full2D.m:174-239 in 1D).  The upwind
-// coupling touches one node of the neighbour element, so the sweep carries
-// one complex scalar s_e: s_e = u_e[st] - h[st] s_{e-1}, u_e = D0^-1 r_e / qd.
-// Elements are split into P chunks (one warp each, lanes = k); the affine maps
-// of the chunks are scanned in shared memory, then every chunk re-sweeps.
-// ---------------------------------------------------------------------------
-template <int NK>
-__global__ void precond_kernel(const double2* __restrict__ r, double2* __restrict__ z,
-                               const double* __restrict__ kvec, const double* __restrict__ dinv,
-                               const double* __restrict__ hvec, const double* __restrict__ qd, int n_el, int nk,
-                               long long N, long long r_stride) {
-  extern __shared__ double2 sh[];                 // [2][P][32]
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;
-  const int P = blockDim.x >> 5;
-  const int j = blockIdx.x * 32 + lane;
-  const int b = blockIdx.y;
-  const bool valid = j < nk;
-  const int chunk = (n_el + P - 1) / P;
-  const int e_lo = min(n_el, w * chunk), e_hi = min(n_el, (w + 1) * chunk);
-  double D[NK * NK], h[NK];
-  bool fwd = true;
-  double inv_qd = 1.0;
-  if (valid) {
-    const long long bj = (long long)b * nk + j;
-#pragma unroll
-    for (int i = 0; i < NK * NK; ++i) D[i] = dinv[bj * NK * NK + i];
-#pragma unroll
-    for (int i = 0; i < NK; ++i) h[i] = hvec[bj * NK + i];
-    fwd = kvec[j] > 0;
-    inv_qd = 1.0 / qd[b];
-  }
-  const int st = fwd ? NK - 1 : 0;
-  const double alpha = valid ? -h[st] : 0.0;
-  const double2* rb = r + (long long)b * r_stride + j;
-  double2* zb = z + (long long)b * N + j;
-  const int len = e_hi - e_lo;
-  // phase 1: chunk map with zero input
-  double2 s = make_double2(0.0, 0.0);
-  double Amul = 1.0;
-  if (valid) {
-    for (int i = 0; i < len; ++i) {
-      const int e = fwd ? e_lo + i : e_hi - 1 - i;
-      const double2* re = rb + (long long)e * NK * nk;
-      double2 u = make_double2(0.0, 0.0);
-#pragma unroll
-      for (int c = 0; c < NK; ++c) {
-        const double2 rv = re[(long long)c * nk];
-        u.x += D[st * NK + c] * rv.x;
-        u.y += D[st * NK + c] * rv.y;
-      }
-      s = make_double2(u.x * inv_qd + alpha * s.x, u.y * inv_qd + alpha * s.y);
-      Amul *= alpha;
-    }
-  }
-  sh[(0 * P + w) * 32 + lane] = make_double2(Amul, 0.0);
-  sh[(1 * P + w) * 32 + lane] = s;
-  __syncthreads();
-  if (w == 0 && valid) {
-    // exclusive scan over chunks in sweep order; overwrite B slot with s_in
-    double2 acc = make_double2(0.0, 0.0);
-    for (int c = 0; c < P; ++c) {
-      const int cc = fwd ? c : P - 1 - c;
-      const double a = sh[(0 * P + cc) * 32 + lane].x;
-      const double2 bb = sh[(1 * P + cc) * 32 + lane];
-      sh[(1 * P + cc) * 32 + lane] = acc;
-      acc = make_double2(a * acc.x + bb.x, a * acc.y + bb.y);
-    }
-  }
-  __syncthreads();
-  if (!valid) return;
-  s = sh[(1 * P + w) * 32 + lane];
-  for (int i = 0; i < len; ++i) {
-    const int e = fwd ? e_lo + i : e_hi - 1 - i;
-    const double2* re = rb + (long long)e * NK * nk;
-    double2 rv[NK];
-#pragma unroll
-    for (int c = 0; c < NK; ++c) rv[c] = re[(long long)c * nk];
-    double2* ze = zb + (long long)e * NK * nk;
-    double2 snew = make_double2(0.0, 0.0);
-#pragma unroll
-    for (int a = 0; a < NK; ++a) {
-      double2 u = make_double2(0.0, 0.0);
-#pragma unroll
-      for (int c = 0; c < NK; ++c) {
-        u.x += D[a * NK + c] * rv[c].x;
-        u.y += D[a * NK + c] * rv[c].y;
-      }
-      const double2 zv = make_double2(u.x * inv_qd - h[a] * s.x, u.y * inv_qd - h[a] * s.y);
-      ze[(long long)a * nk] = zv;
-      if (a == st) snew = zv;
-    }
-    s = snew;
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Observables: rho_u(s) = sum_j Phi(s,j) rho_{x,j} at the centre xi rows,
 // n = Re rho_u(centre), j = q hbar / m Im d rho_u / d xi
 // (solve_transport_DG_2D.m:114-156).  One warp per DG node.
@@ -411,12 +313,17 @@ cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
 
 template <int NK>
 cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2* z) {
-  const int Pw = std::max(1, std::min(16, (P.s.n_el + 7) / 8));
-  dim3 grid((P.s.nk + 31) / 32, P.batch);
-  const size_t shm = sizeof(double2) * 2 * Pw * 32;
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 1, 32.0 * P.N * P.batch);
-  precond_kernel<NK><<<grid, 32 * Pw, shm, P.stream>>>(r, z, P.kvec, P.pre_dinv, P.pre_h, P.qd, P.s.n_el, P.s.nk,
-                                                        P.N, r_stride);
+  const int L = kline::chunk_len(P.s.n_el), nc = kline::chunk_count(P.s.n_el);
+  const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
+  const dim3 block(32, kline::kChunksPerBlock);
+  double* ma = static_cast<double*>(P.kmap_a);
+  double2* ms = static_cast<double2*>(P.kmap_s);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, 48.0 * P.N * P.batch);
+  kline::kline_maps_kernel<NK, double><<<grid, block, 0, P.stream>>>(r, P.kvec, P.pre_dinv, P.pre_h, P.qd, ma, ms,
+                                                                     P.s.n_el, P.s.nk, P.N, r_stride, L, nc);
+  kline::kline_apply_kernel<NK, double><<<grid, block, 0, P.stream>>>(r, z, nullptr, P.kvec, P.pre_dinv, P.pre_h,
+                                                                      P.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
+                                                                      r_stride, L, nc);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }

@@ -40,8 +40,10 @@ __device__ double block_reduce(double v, bool is_max) {
   return v;  // valid in warp 0
 }
 
-__global__ void minmax_kernel(const double* __restrict__ pot_v, double* __restrict__ pp, int nx, int b0) {
+__global__ void minmax_kernel(const double* __restrict__ pot_v, double* __restrict__ pp, int nx, int b0,
+                              const int* __restrict__ mask) {
   const int b = b0 + blockIdx.x;
+  if (mask && !mask[b]) return;
   const double* v = pot_v + (long long)b * nx;
   double mx = -INFINITY, mn = INFINITY;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) {
@@ -58,8 +60,10 @@ __global__ void minmax_kernel(const double* __restrict__ pot_v, double* __restri
 
 // f_{L,R}(k_j) = 2/pi dkz sum_z 1/(1 + exp(q (E_{L,R}(k) + E_kz - E_F) / (kB T)))
 __global__ void fermi_kernel(const double* __restrict__ pot_v, const double* __restrict__ pp,
-                             const double* __restrict__ kvec, double* __restrict__ flr, int nx, int nk, int b0) {
+                             const double* __restrict__ kvec, double* __restrict__ flr, int nx, int nk, int b0,
+                             const int* __restrict__ mask) {
   const int j = blockIdx.x, b = b0 + blockIdx.y;
+  if (mask && !mask[b]) return;
   const double* P = pp + b * kPP;
   const double hb = kHV / 2 / kPi;
   const double k = kvec[j];
@@ -88,9 +92,11 @@ __global__ void fermi_kernel(const double* __restrict__ pot_v, const double* __r
 __global__ void inflow_kernel(const double* __restrict__ flr, const double* __restrict__ cosm,
                               const double2* __restrict__ pinv, const double* __restrict__ kvec,
                               const double* __restrict__ pp, double2* __restrict__ rhs, FluxBlocks fb, int nk,
-                              int nxi, int n_el, long long N, double q_diff, double mpc, int b0) {
+                              int nxi, int n_el, long long N, double q_diff, double mpc, int b0,
+                              const int* __restrict__ mask) {
   extern __shared__ double sm[];  // [2][nxi]
   const int b = b0 + blockIdx.x;
+  if (mask && !mask[b]) return;
   const double* fL = flr + (long long)b * 2 * nk;
   const double* fR = fL + nk;
   const double dk = fabs(kvec[1] - kvec[0]);
@@ -150,7 +156,8 @@ template <int NK>
 __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ xq, const double* __restrict__ xi_edge,
                           const double* __restrict__ kap, const double* __restrict__ pot_x,
                           const double* __restrict__ pot_v, const double* __restrict__ pp, int nx, int n_el, int nxi,
-                          double scale, int b0) {
+                          double scale, int b0, const int* __restrict__ mask) {
+  if (mask && !mask[b0 + blockIdx.y]) return;
   const int ne = nxi + 1;
   const int b = b0 + blockIdx.y;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,25 +187,26 @@ __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ 
 
 }  // namespace
 
-cudaError_t launch_potential_update(Problem& P, int b0, int b1) {
+cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask) {
   const int nb = b1 - b0;
   if (nb <= 0) return cudaSuccess;
   const Shape& s = P.s;
   cudaEvent_t ev = prof_begin(P, PROF_OTHER, 4);
-  minmax_kernel<<<nb, 256, 0, P.stream>>>(P.pot_v, P.pp, P.nx, b0);
-  fermi_kernel<<<dim3(s.nk, nb), 128, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr, P.nx, s.nk, b0);
+  minmax_kernel<<<nb, 256, 0, P.stream>>>(P.pot_v, P.pp, P.nx, b0, mask);
+  fermi_kernel<<<dim3(s.nk, nb), 128, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr, P.nx, s.nk, b0, mask);
   inflow_kernel<<<nb, 256, sizeof(double) * 2 * s.nxi, P.stream>>>(P.flr, P.cosm, P.pinv, P.kvec, P.pp, P.rhs, P.fb,
-                                                                   s.nk, s.nxi, s.n_el, P.N, s.q_diff, s.mpc, b0);
+                                                                   s.nk, s.nxi, s.n_el, P.N, s.q_diff, s.mpc, b0,
+                                                                   mask);
   const int ne = s.nxi + 1;
   dim3 g((unsigned)(((long long)s.n_el * ne + 127) / 128), nb);
   const double scale = s.delta_xi / 4 * s.mpc;
   switch (s.nK) {
     case 2: vw_kernel<2><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.pp, P.nx,
-                                                  s.n_el, s.nxi, scale, b0); break;
+                                                  s.n_el, s.nxi, scale, b0, mask); break;
     case 3: vw_kernel<3><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.pp, P.nx,
-                                                  s.n_el, s.nxi, scale, b0); break;
+                                                  s.n_el, s.nxi, scale, b0, mask); break;
     default: vw_kernel<4><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.pp, P.nx,
-                                                   s.n_el, s.nxi, scale, b0); break;
+                                                   s.n_el, s.nxi, scale, b0, mask); break;
   }
   prof_end(P, PROF_OTHER, ev);
   return cudaGetLastError();

@@ -129,6 +129,12 @@ struct GummelHost {
   bool ready = false;
   double bias = 0;
   bool step_pending = false;   // a transient bias step waits for its potential re-solve
+  // state of the problem's Gummel loop
+  int running = 0;             // 1 while the loop iterates
+  int it = 0;                  // iterations done
+  double tol = 0;              // transport tolerance of the next solve
+  double t0 = 0;               // start of the loop [s, steady clock]
+  wg_gummel_info info{};
 };
 
 struct Problem {
@@ -140,6 +146,8 @@ struct Problem {
   int restart_inner = 40;   // inner GMRES length of the mixed form
   int restart_max = 50;     // sizes the Hessenberg storage: max(restart, restart_inner)
   double inner_tol = 1e-3;  // floor of the inner relative tolerance of the mixed form
+  double reorth_eta = 0.7071067811865476;        // DGKS threshold of the FP64 Arnoldi (>= 1 always, < 0 never)
+  double inner_reorth_eta = -1.0;                // the same for the mixed form's inner FP32 Arnoldi
   long long N = 0;          // complex entries per problem
   long long ncols = 0;      // DG nodes in the batch = batch * n_el * nK
   double device_bytes = 0;
@@ -159,6 +167,8 @@ struct Problem {
   double* betai = nullptr;       // [nK*nK][nxi+1] CAP part of the potential weights (imaginary)
   double* pre_dinv = nullptr;    // [B][nk][nK*nK] inverse of k K1 + |k| K2 + shift/qd_b
   double* pre_h = nullptr;       // [B][nk][nK] that inverse times the coupling column
+  void* kmap_a = nullptr;        // [B][n_chunks][nk] k-line chunk maps: factor (double or float)
+  void* kmap_s = nullptr;        // [B][n_chunks][nk] k-line chunk maps: offset (double2 or float2)
   double* cosm = nullptr;        // [nxi][nk] cos(xi_s k_j)
   double2* pinv = nullptr;       // [nk][nxi] pseudo-inverse of Phi
   // per-problem device data
@@ -224,13 +234,16 @@ cudaError_t launch_apply(Problem& P, const double2* x, double2* y);
 cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z);
 // k-line factors of A + sigma I for every problem (sigma = P.shift), uploaded to pre_dinv / pre_h.
 int set_kline_factors(Problem& P);
+// Device bytes of a handle before allocation (the admission estimate of wg_problem_create).
+double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision);
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y);
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh);
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
 cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y);
 int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err);
 // Rebuild potential-dependent data (Vw weights, contact inflow rhs) of problems [b0, b1).
-cudaError_t launch_potential_update(Problem& P, int b0, int b1);
+// mask (device, optional): problems b with mask[b] == 0 are left untouched.
+cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask = nullptr);
 cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j);
 cudaError_t launch_rho_xi(Problem& P, int b, double2* out);
 // Allocation-free operator apply on caller-owned device buffers (operator.cu).
@@ -254,6 +267,11 @@ int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info*
 // Gummel loop (gummel.cu)
 int gummel_set(Problem& P, int b, const wg_device& dev, const wg_rtd_1d& rtd);
 int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info);
+// Problem b's loop from its current state: warm keeps its Wigner function, from_phi0
+// resets the potential to the phi0 of wg_gummel_set.
+int gummel_start(Problem& P, int b, const wg_gummel_opts& o, bool warm, bool from_phi0);
+// One iteration of every running loop (the others keep their state untouched).
+int gummel_iterate(Problem& P, const wg_gummel_opts& o, int* still_running);
 int gummel_get(Problem& P, int b, double* phi, double* n_dg, double* j);
 cudaError_t gummel_observables(Problem& P);                               // ndg, jdg of every problem from x
 cudaError_t gummel_poisson(Problem& P, const int* active_dev, bool linear);  // cand, diag
@@ -264,3 +282,8 @@ int transient_run(Problem& P, const wg_transient_opts& o, double* n_hist, double
 void gummel_free(Problem& P);
 
 }  // namespace wg
+
+// The opaque handle of the C ABI.
+struct wg_problem {
+  wg::Problem P;
+};

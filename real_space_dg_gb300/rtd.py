@@ -30,7 +30,7 @@ from .transport import M0, Problem1D, shape_from_mat
 DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityTolerance=5e-4,
                 poissonResidualTolerance=8e-2, transportTolerance=1e-8, transportMaxCycles=50,
                 fermiOffset=0.05, restart=50, precision="fp64", innerRestart=40, innerTol=1e-3,
-                inexactFactor=0.0, inexactCap=1e-4)
+                inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0)
 
 
 def _opts(options):
@@ -52,7 +52,8 @@ class RTDSweep:
         self.o = _opts(options)
         shp = shape_from_mat(mat)
         self.P = Problem1D(batch=batch, precision=self.o["precision"], restart=self.o["restart"],
-                           inner_restart=self.o["innerRestart"], inner_tol=self.o["innerTol"], **shp)
+                           inner_restart=self.o["innerRestart"], inner_tol=self.o["innerTol"],
+                           reorth=self.o["reorth"], inner_reorth=self.o["innerReorth"], **shp)
         self.lib = self.P.lib
         self.nx = int(mat["Nx"])
         self.dy = float(mat.get("dy_norm_nm") or devices.density_normalisation_nm(mat, self.o["fermiOffset"]))
@@ -69,11 +70,25 @@ class RTDSweep:
     def close(self):
         self.P.close()
 
-    def set(self, b, bias, phi0=None):
-        phi0 = np.ascontiguousarray(bias * self.ramp if phi0 is None else phi0, dtype=float)
-        rtd = _lib.WgRtd1D(_lib.dptr(self.vc), _lib.dptr(self.nd), _lib.dptr(self.eps), _lib.dptr(phi0),
+    def set(self, b, bias, phi0=None, mat=None):
+        """Problem b at ``bias``; ``mat`` (same grid) gives it its own device data."""
+        if mat is None:
+            vc, nd, eps, dev, ramp = self.vc, self.nd, self.eps, self.dev, self.ramp
+        else:
+            if int(mat["Nx"]) != self.nx:
+                raise WignerError(_lib.WG_ERR_ARG, "every problem of a handle needs the same grid")
+            x = np.ascontiguousarray(mat["x"], dtype=float)
+            m = np.ascontiguousarray(np.asarray(mat["me_x"], dtype=float).reshape(-1, self.nx,
+                                                                                  int(mat["Ny"]))[0, :, 0] * M0)
+            vc = np.ascontiguousarray(mat["Vc"], dtype=float)
+            nd = np.ascontiguousarray(mat["Nd"], dtype=float)
+            eps = np.ascontiguousarray(mat["eps"], dtype=float)
+            dev = _lib.WgDevice(self.nx, _lib.dptr(x), _lib.dptr(m), float(mat["me_z_ch"]), float(mat["Temp"]))
+            ramp = np.asarray(mat["ramp"], dtype=float)
+        phi0 = np.ascontiguousarray(bias * ramp if phi0 is None else phi0, dtype=float)
+        rtd = _lib.WgRtd1D(_lib.dptr(vc), _lib.dptr(nd), _lib.dptr(eps), _lib.dptr(phi0),
                            float(bias), float(self.o["fermiOffset"]), self.dy)
-        self.P._check(self.lib.wg_gummel_set(self.P.h, int(b), C.byref(self.dev), C.byref(rtd)))
+        self.P._check(self.lib.wg_gummel_set(self.P.h, int(b), C.byref(dev), C.byref(rtd)))
 
     def run(self, warm_start=False, restart_from_phi0=False):
         o = self.o

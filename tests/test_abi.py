@@ -48,6 +48,12 @@ int main(void) {
   printf("%zu %zu %zu %zu\n", sizeof(wg_params), sizeof(wg_device), sizeof(wg_solve_opts), sizeof(wg_solve_info));
   printf("%zu %zu %zu\n", offsetof(wg_params, l_xi), offsetof(wg_params, precision), offsetof(wg_params, mem_budget_bytes));
   printf("%zu %zu\n", offsetof(wg_solve_info, relres), offsetof(wg_solve_info, rhs_norm));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(wg_rtd_1d), sizeof(wg_gummel_opts), sizeof(wg_gummel_info),
+         sizeof(wg_transient_opts), sizeof(wg_transient_info));
+  printf("%zu %zu %zu %zu %zu\n", sizeof(wg_server_opts), sizeof(wg_request), sizeof(wg_request_status),
+         sizeof(wg_server_stats), sizeof(wg_operator_view));
+  printf("%zu %zu %zu\n", offsetof(wg_server_opts, gummel), offsetof(wg_request, rtd),
+         offsetof(wg_request_status, t_submit));
   return 0;
 }''')
     exe = tmp_path / "probe"
@@ -59,7 +65,12 @@ int main(void) {
     got = list(map(int, out))
     want = [C.sizeof(_lib.WgParams), C.sizeof(_lib.WgDevice), C.sizeof(_lib.WgSolveOpts),
             C.sizeof(_lib.WgSolveInfo), _lib.WgParams.l_xi.offset, _lib.WgParams.precision.offset,
-            _lib.WgParams.mem_budget_bytes.offset, _lib.WgSolveInfo.relres.offset, _lib.WgSolveInfo.rhs_norm.offset]
+            _lib.WgParams.mem_budget_bytes.offset, _lib.WgSolveInfo.relres.offset, _lib.WgSolveInfo.rhs_norm.offset,
+            C.sizeof(_lib.WgRtd1D), C.sizeof(_lib.WgGummelOpts), C.sizeof(_lib.WgGummelInfo),
+            C.sizeof(_lib.WgTransientOpts), C.sizeof(_lib.WgTransientInfo),
+            C.sizeof(_lib.WgServerOpts), C.sizeof(_lib.WgRequest), C.sizeof(_lib.WgRequestStatus),
+            C.sizeof(_lib.WgServerStats), C.sizeof(_lib.WgOperatorView),
+            _lib.WgServerOpts.gummel.offset, _lib.WgRequest.rtd.offset, _lib.WgRequestStatus.t_submit.offset]
     assert got == want
 
 
