@@ -310,7 +310,8 @@ def run_reference(args, rank, world, dist):
                                           "d2h_bytes_per_step": 0}}
 
 
-SERVED = dict(devices=12, biases_per_device=8, rate_hz=20.0, budget_bytes=150e9, max_slots=8, seed=2026)
+SERVED = dict(devices=12, biases_per_device=8, rate_hz=20.0, budget_bytes=150e9, max_slots=8, seed=2026,
+              max_gummel=500)
 
 
 def served_requests(seed):
@@ -343,8 +344,10 @@ def run_served(args):
     g.build()
     from real_space_dg_gb300.serve import Server, serve_sweep
     jobs, arrivals, shapes = served_requests(SERVED["seed"])
-    opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
-                innerTol=args.inner_tol, inexactFactor=args.inexact, reorth=args.reorth, innerReorth=args.inner_reorth)
+    # the C2 loop settings; high-bias points of the stiffer devices need more than 200 damped iterations
+    opts = dict(GUMMEL, maxIterations=SERVED["max_gummel"], precision=args.precision, restart=args.restart,
+                innerRestart=args.inner_restart, innerTol=args.inner_tol, inexactFactor=args.inexact,
+                reorth=args.reorth, innerReorth=args.inner_reorth)
     clocks = ClockSampler()
     clocks.start()
     with Server(opts, mem_budget_bytes=SERVED["budget_bytes"], max_slots=SERVED["max_slots"], warm_start=True) as S:
@@ -368,6 +371,7 @@ def run_served(args):
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "definition": "request arrival to result"},
         "warm_started": int(sum(r["warm"] > 0 for r in res)),
+        "statuses": {k: int(sum(r["status"] == k for r in res)) for k in sorted({r["status"] for r in res})},
         "gummel_iterations_per_point": float(np.mean([r["info"]["iterations"] for r in res])),
         "server": stats, "clocks": clk,
     }
@@ -432,13 +436,39 @@ def run_transient(args):
     }
 
 
+def run_apply(args):
+    """Operator applies/s on the C2 batch: the FP64 operator (plain form), the mixed form's
+    low-precision inner operator and its tensor-core FP64 operator, with per-kernel rooflines."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300.rtd import RTDSweep
+    spec, mat, biases = make_workload(args.batch)
+    S = RTDSweep(mat, args.batch, dict(GUMMEL, precision="mixed"))
+    for b, v in enumerate(biases):
+        S.set(b, v)
+    out = {"metric": "operator applies/s (C2 RTD, batch %d)" % args.batch, "unit": "applies/s",
+           "config": {"workload": "C2 operator, %d problems x 245760 unknowns" % args.batch}, "forms": {}}
+    for which in ("fp64", "lowprec", "fp64_tc"):
+        S.P.apply_time(which, 3)                                    # warm-up
+        ms = S.P.apply_time(which, max(10, args.steps))
+        S.P.profile(on=True, reset=True)
+        S.P.apply_time(which, 5)
+        prof = S.P.profile(on=False, reset=True)
+        roofs = rooflines(prof, "mixed" if which != "fp64" else "fp64")
+        out["forms"][which] = {"ms_per_apply": round(ms, 4), "applies_per_s": round(args.batch * 1000.0 / ms, 1),
+                               "rooflines": roofs}
+    S.close()
+    out["value"] = out["forms"]["lowprec"]["applies_per_s"]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
@@ -466,6 +496,8 @@ def main():
         out = run_served(args) if rank == 0 else None
     elif args.workload == "transient":
         out = run_transient(args) if rank == 0 else None
+    elif args.workload == "apply":
+        out = run_apply(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

@@ -149,7 +149,7 @@ int wg_get_rho_xi(wg_problem* h, int b, double* rho_u);
 /* y = A x for the whole batch (host buffers, batch*N complex each).  FP64 handles
  * use native FP64 arithmetic; mixed handles apply the operator of their FP64
  * refinement residual, whose transforms are FP64 products emulated on the tensor
- * cores (about 1e-14 relative to |Phi| |x|) when 2 N_k and 2 N_xi are at most 512. */
+ * cores (about 1e-14 relative to |Phi| |x|) when 2 N_k and 2 N_xi are at most 1024. */
 int wg_apply(wg_problem* h, const double* x, double* y);
 /* y = A_lo x with the operator of the mixed form's inner solve (BF16 tensor-core
  * transforms, FP32 flux and stencil); mixed handles only.  Host FP64 buffers. */
@@ -357,9 +357,16 @@ int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, i
 /* Diagnostic: C = A * B in FP64 emulated on the tensor cores (6-bit digit slices,
  * exact BF16 products, grouped FP32 accumulation, double-float recombination), the
  * GEMM of the mixed form's FP64 outer residual.  A row-major M x K, B column-major
- * K x N, C column-major M x N, host buffers; 64 <= K <= 512, K % 8 == 0.  No
+ * K x N, C column-major M x N, host buffers; 64 <= K <= 1024, K % 8 == 0.  No
  * counterpart in the reference. */
 int wg_debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K);
+
+/* Diagnostic: apply the operator n times to the resident state on the device and
+ * return the mean time of one apply in *ms.  which = 0: the FP64 operator;
+ * 1: the mixed form's low-precision operator (BF16 transforms, FP32 flux and
+ * stencil); 2: the mixed form's FP64 operator (transforms emulated on the tensor
+ * cores).  No counterpart in the reference (operator applies/s). */
+int wg_apply_repeat(wg_problem* h, int which, int n, double* ms);
 
 /* Kernel-class profiler (the reference's tic/toc solveInfo timings,
  * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).

@@ -45,7 +45,7 @@ void free_all(wg::Problem& P) {
   wg::gummel_free(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.kmap_a, P.kmap_s, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
-                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.kused, P.any_active};
+                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.md_count, P.gs_count, P.kused, P.any_active};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P.stream) cudaStreamDestroy(P.stream);
@@ -282,6 +282,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.target, batch, bytes));
   A(dalloc(&P.active, batch, bytes));
   A(dalloc(&P.reorth, batch, bytes));
+  A(dalloc(&P.md_count, batch, bytes));
+  A(dalloc(&P.gs_count, batch, bytes));
   A(dalloc(&P.kused, batch, bytes));
   A(dalloc(&P.any_active, 1, bytes));
   P.device_bytes = bytes;
@@ -320,6 +322,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   API_CK(&P, cudaMemsetAsync(P.beta, 0, sizeof(double) * batch * s.n_el * nK * nK * (s.nxi + 1), P.stream));
   // a problem never given data is a zero operator with a zero rhs: it is converged and inert
   API_CK(&P, cudaMemsetAsync(P.qd, 0, sizeof(double) * batch, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.md_count, 0, sizeof(int) * batch, P.stream));
+  API_CK(&P, cudaMemsetAsync(P.gs_count, 0, sizeof(int) * batch, P.stream));
   API_CK(&P, cudaMemsetAsync(P.pp, 0, sizeof(double) * batch * wg::kPP, P.stream));
   API_CK(&P, cudaMemsetAsync(P.flr, 0, sizeof(double) * batch * 2 * s.nk, P.stream));
   API_CK(&P, cudaMemsetAsync(P.pot_v, 0, sizeof(double) * batch * P.nx, P.stream));
@@ -616,6 +620,36 @@ int wg_debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int
   std::string err;
   const int rc = wg::debug_gemm_f64_tc(A, B, C, M, N, K, err);
   if (rc) return fail(nullptr, rc, "wg_debug_gemm_f64_tc: " + err);
+  return WG_OK;
+}
+
+int wg_apply_repeat(wg_problem* h, int which, int n, double* ms) {
+  if (!h || !ms || n < 1 || which < 0 || which > 2) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_apply_repeat: bad argument");
+  wg::Problem& P = h->P;
+  if (which > 0 && P.precision != WG_PREC_MIXED)
+    return fail(&P, WG_ERR_ARG, "wg_apply_repeat: the low-precision and tensor-core FP64 operators need a mixed handle");
+  cudaEvent_t a = nullptr, b = nullptr;
+  API_CK(&P, cudaEventCreate(&a));
+  API_CK(&P, cudaEventCreate(&b));
+  cudaError_t e = cudaSuccess;
+  if (which == 1) {
+    e = wg::apply_mixed_repeat(P, P.x, 1);   // conversion and first touch, untimed
+    if (e == cudaSuccess) e = cudaEventRecord(a, P.stream);
+    if (e == cudaSuccess) e = wg::apply_mixed_repeat(P, P.x, n);
+  } else {
+    e = which == 2 ? wg::launch_apply_f64_tc(P, P.x, P.w) : wg::launch_apply(P, P.x, P.w);
+    if (e == cudaSuccess) e = cudaEventRecord(a, P.stream);
+    for (int i = 0; i < n && e == cudaSuccess; ++i)
+      e = which == 2 ? wg::launch_apply_f64_tc(P, P.x, P.w) : wg::launch_apply(P, P.x, P.w);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(b, P.stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(b);
+  float t = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  API_CK(&P, e);
+  *ms = t / n;
   return WG_OK;
 }
 

@@ -135,6 +135,119 @@ __device__ double block_sum1(double v) {
   return r;
 }
 
+// The last block of a problem to finish a grid-wide pass (per-problem ticket
+// counter; the threadFenceReduction pattern: every block fences its partial
+// results, takes a ticket, and the block holding the last ticket reduces them and
+// resets the counter for the next launch on the stream).  No block waits.
+__device__ __forceinline__ bool last_block_of_problem(int* __restrict__ count, int b) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&count[b], 1) == (int)gridDim.x - 1;
+  __syncthreads();
+  if (last) __threadfence();
+  return last;
+}
+
+// hcol[b][i] = sum_c partial[b][i][c] (FP64); H[b][k][i] = (first) or += hcol.  One block.
+__device__ void dot_reduce_block(const double2* __restrict__ partial, double2* __restrict__ hcol,
+                                 float2* __restrict__ hcol32, double2* __restrict__ H, int b, int nv, int k,
+                                 int pstride, int m, int nchunk, int first) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = w; i < nv; i += nw) {
+    double2 acc = make_double2(0, 0);
+    for (int c = lane; c < nchunk; c += 32) {
+      const double2 t = __ldcg(&partial[((long long)b * pstride + i) * nchunk + c]);
+      acc.x += t.x;
+      acc.y += t.y;
+    }
+    acc.x = warp_sum(acc.x);
+    acc.y = warp_sum(acc.y);
+    if (lane == 0) {
+      hcol[b * pstride + i] = acc;
+      if (hcol32) hcol32[b * pstride + i] = make_float2((float)acc.x, (float)acc.y);
+      double2* h = H + (long long)b * pstride * m + (long long)k * pstride + i;
+      if (first) *h = acc;
+      else { h->x += acc.x; h->y += acc.y; }
+    }
+  }
+}
+
+// Givens step k of problem b (one warp): rotate the new Hessenberg column by the
+// previous rotations, make the next rotation, update g and deactivate the problem
+// once the residual estimate |g[k+1]| reaches its target.  H is column-major per
+// problem (H[b][col*(m+1)+row]), cs/sn/g per problem; staging in shared memory.
+__device__ void givens_warp(double2* __restrict__ H, double2* __restrict__ cs, double2* __restrict__ sn,
+                            double2* __restrict__ g, int* __restrict__ active, int* __restrict__ kused,
+                            const double* __restrict__ target, int b, int k, int pstride, int m, double2* col_s,
+                            double2* c_s, double2* s_s) {
+  const int lane = threadIdx.x & 31;
+  double2* col = H + (long long)b * pstride * m + (long long)k * pstride;
+  double2* c = cs + b * m;
+  double2* s = sn + b * m;
+  for (int i = lane; i <= k + 1; i += 32) col_s[i] = col[i];
+  for (int i = lane; i < k; i += 32) {
+    c_s[i] = c[i];
+    s_s[i] = s[i];
+  }
+  __syncwarp();
+  if (lane == 0) {
+    double2* gg = g + b * pstride;
+    double2 hi = col_s[0];
+    for (int i = 0; i < k; ++i) {
+      const double2 hj = col_s[i + 1];
+      const double2 ci = c_s[i], si = s_s[i];
+      col_s[i] = make_double2(ci.x * hi.x - ci.y * hi.y + si.x * hj.x - si.y * hj.y,
+                              ci.x * hi.y + ci.y * hi.x + si.x * hj.y + si.y * hj.x);
+      hi = make_double2(-(si.x * hi.x + si.y * hi.y) + (ci.x * hj.x + ci.y * hj.y),
+                        -(si.x * hi.y - si.y * hi.x) + (ci.x * hj.y - ci.y * hj.x));
+    }
+    const double2 a = hi, bb = col_s[k + 1];
+    const double den = sqrt(a.x * a.x + a.y * a.y + bb.x * bb.x + bb.y * bb.y);
+    double2 cc, ss;
+    if (den == 0.0) {
+      cc = make_double2(1.0, 0.0);
+      ss = make_double2(0.0, 0.0);
+    } else {
+      const double inv = 1.0 / den;
+      cc = make_double2(a.x * inv, -a.y * inv);
+      ss = make_double2(bb.x * inv, -bb.y * inv);
+    }
+    c[k] = cc;
+    s[k] = ss;
+    col_s[k] = make_double2(den, 0.0);
+    col_s[k + 1] = make_double2(0.0, 0.0);
+    const double2 gk = gg[k];
+    gg[k + 1] = make_double2(-(ss.x * gk.x + ss.y * gk.y), -(ss.x * gk.y - ss.y * gk.x));
+    gg[k] = make_double2(cc.x * gk.x - cc.y * gk.y, cc.x * gk.y + cc.y * gk.x);
+    kused[b] = k + 1;
+    const double res = sqrt(gg[k + 1].x * gg[k + 1].x + gg[k + 1].y * gg[k + 1].y);
+    if (!(res > target[b]) || bb.x == 0.0 || !isfinite(res)) active[b] = 0;
+  }
+  __syncwarp();
+  for (int i = lane; i <= k + 1; i += 32) col[i] = col_s[i];
+}
+
+// Arguments of the per-problem tail work done by the last block of a launch.
+struct KrylovTail {
+  int* md_count;       // [B] tickets of the multi-dot
+  int* gs_count;       // [B] tickets of the update
+  double2* partial;    // multi-dot partials
+  double2* hcol;       // FP64 coefficients
+  float2* hcol32;      // FP32 copy (mixed form) or null
+  double2* H;
+  double2 *cs, *sn, *g;
+  int* active;
+  int* kused;
+  int* reorth;
+  const double* target;
+  double* nrm;
+  double* inv64;
+  float* inv32;
+  double eta2;         // DGKS threshold squared
+  int k, pstride, m, first;
+};
+
 // Multi-dot: partial[b][i][c] = sum over chunk c of conj(V_i) . w for every i < nv.
 // One block per (chunk of 256*E elements, problem): w stays in registers, each V_i
 // chunk is read once, warps drop their partial sums in shared memory and the
@@ -143,7 +256,8 @@ constexpr int kMdE = 8;
 template <typename T>
 __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, const T* __restrict__ w,
                                                        double2* __restrict__ partial, const int* __restrict__ active,
-                                                       long long N, int nv, int mp1, int pstride, int nchunk) {
+                                                       long long N, int nv, int mp1, int pstride, int nchunk,
+                                                       KrylovTail tl) {
   extern __shared__ double red[];  // [nv][8 warps][4 doubles]
   const int b = blockIdx.y, c = blockIdx.x;
   if (!active[b]) return;
@@ -219,63 +333,27 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
   __syncthreads();
   for (int i = threadIdx.x; i < nv; i += blockDim.x)
     partial[((long long)b * pstride + i) * nchunk + c] = AccFor<T>::type::combine(red + i * 8 * 4, 8);
+  // the last chunk of problem b reduces the partials into the Hessenberg column
+  if (!last_block_of_problem(tl.md_count, b)) return;
+  dot_reduce_block(partial, tl.hcol, tl.hcol32, tl.H, b, nv, tl.k, pstride, tl.m, nchunk, tl.first);
+  if (threadIdx.x == 0) tl.md_count[b] = 0;
 }
 
-// hcol[b][i] = sum_c partial; H[b][k][i] (+)= hcol          grid (B), block 256
-__global__ void dot_reduce_kernel(const double2* __restrict__ partial, double2* __restrict__ hcol,
-                                  float2* __restrict__ hcol32, double2* __restrict__ H, const int* __restrict__ active,
-                                  int nv, int k, int pstride, int m, int nchunk, int first) {
-  const int b = blockIdx.x;
-  if (!active[b]) return;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = w; i < nv; i += nw) {
-    double2 acc = make_double2(0, 0);
-    for (int c = lane; c < nchunk; c += 32) {
-      const double2 t = partial[((long long)b * pstride + i) * nchunk + c];
-      acc.x += t.x;
-      acc.y += t.y;
-    }
-    acc.x = warp_sum(acc.x);
-    acc.y = warp_sum(acc.y);
-    if (lane == 0) {
-      hcol[b * pstride + i] = acc;
-      if (hcol32) hcol32[b * pstride + i] = make_float2((float)acc.x, (float)acc.y);
-      double2* h = H + (long long)b * pstride * m + (long long)k * pstride + i;
-      if (first) *h = acc;
-      else { h->x += acc.x; h->y += acc.y; }
-    }
-  }
-}
 
-// Daniel-Gragg-Kaufman-Stewart test after the first classical Gram-Schmidt pass:
-// problem b is re-orthogonalised only if |w1| < eta |w|, where w1 = w - V h and
-// |w|^2 = |w1|^2 + |h|^2 (V orthonormal).
-__global__ void reorth_test_kernel(const double* __restrict__ partial, const double2* __restrict__ hcol,
-                                   const int* __restrict__ active, int* __restrict__ reorth, int nblk, int nv,
-                                   int pstride, double eta2) {
-  const int b = blockIdx.x;
-  double w2 = 0, h2 = 0;
-  for (int c = threadIdx.x; c < nblk; c += 32) w2 += partial[(long long)b * nblk + c];
-  for (int i = threadIdx.x; i < nv; i += 32) {
-    const double2 h = hcol[(long long)b * pstride + i];
-    h2 += h.x * h.x + h.y * h.y;
-  }
-  w2 = warp_sum(w2);
-  h2 = warp_sum(h2);
-  if (threadIdx.x == 0) reorth[b] = (active[b] && w2 < eta2 * (w2 + h2)) ? 1 : 0;
-}
 
-// w -= sum_i V_i hcol_i; with NORM, also nrm_partial[b][blockIdx.x] = sum |w|^2 of the block.
-// Grid (ceil(N/256), B): 256 complex values per block, one per thread for FP64 vectors,
-// two per thread (16-byte accesses, 128 threads) for FP32 vectors.  The coefficients
-// are staged in shared memory.
-template <typename T, bool NORM>
+// w -= sum_i V_i hcol_i.  Grid (ceil(N/256), B): 256 complex values per block, one per
+// thread for FP64 vectors, two per thread (16-byte accesses, 128 threads) for FP32
+// vectors; the coefficients are staged in shared memory.
+// MODE 0: update only.  MODE >= 1: also nrm_partial[b][block] = sum |w|^2, and the last
+// block of problem b finishes the step: MODE 1 runs the DGKS test (reorth[b]) and, when
+// no second pass is needed, MODE 2's work: |w|, H[k+1][k], inverse norm, Givens step.
+template <typename T, int MODE>
 __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V, T* __restrict__ w,
-                                                        const T* __restrict__ hcol, const int* __restrict__ active,
+                                                        const T* __restrict__ hcol, const int* __restrict__ mask,
                                                         double* __restrict__ nrm_partial, long long N, int nv, int mp1,
-                                                        int pstride, int nblk) {
+                                                        int pstride, int nblk, KrylovTail tl) {
   const int b = blockIdx.y;
-  if (!active[b]) return;
+  if (!mask[b]) return;
   __shared__ T hs[kMaxRestart + 1];
   for (int i = threadIdx.x; i < nv; i += blockDim.x) hs[i] = hcol[b * pstride + i];
   __syncthreads();
@@ -297,7 +375,7 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
         acc.w = fmaf(-x.z, h.y, fmaf(-x.w, h.x, acc.w));
       }
       *wp = acc;
-      if (NORM) {
+      if (MODE) {
         a.add_norm(make_float2(acc.x, acc.y));
         a.add_norm(make_float2(acc.z, acc.w));
       }
@@ -311,16 +389,49 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
 #pragma unroll 4
       for (int i = 0; i < nv; ++i) cms(acc, v[(long long)i * N], hs[i]);
       w[t] = acc;
-      if (NORM) a.add_norm(acc);
+      if (MODE) a.add_norm(acc);
     }
   }
-  if (NORM) {
+  if constexpr (MODE >= 1) {
     __shared__ double wsum[8 * 4];
     a.warp_reduce();
     if ((threadIdx.x & 31) == 0) a.stage(wsum + (threadIdx.x >> 5) * 4);
     __syncthreads();
     if (threadIdx.x == 0)
       nrm_partial[(long long)b * nblk + blockIdx.x] = AccFor<T>::type::combine(wsum, blockDim.x >> 5).x;
+    if (!last_block_of_problem(tl.gs_count, b)) return;
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      double w2 = 0;
+      for (int c = lane; c < nblk; c += 32) w2 += __ldcg(&nrm_partial[(long long)b * nblk + c]);
+      w2 = warp_sum(w2);
+      bool finish = true;
+      if (MODE == 1) {
+        double h2 = 0;
+        for (int i = lane; i < nv; i += 32) {
+          const double2 h = tl.hcol[(long long)b * pstride + i];
+          h2 += h.x * h.x + h.y * h.y;
+        }
+        h2 = warp_sum(h2);
+        const int re = w2 < tl.eta2 * (w2 + h2) ? 1 : 0;
+        if (lane == 0) tl.reorth[b] = re;
+        finish = !re;
+      }
+      if (finish) {
+        __shared__ double2 col_s[kMaxRestart + 1], c_s[kMaxRestart], s_s[kMaxRestart];
+        if (lane == 0) {
+          const double v = sqrt(w2);
+          tl.nrm[b] = v;
+          if (tl.inv64) tl.inv64[b] = v > 0 ? 1.0 / v : 0.0;
+          if (tl.inv32) tl.inv32[b] = v > 0 ? (float)(1.0 / v) : 0.f;
+          tl.H[(long long)b * pstride * tl.m + (long long)tl.k * pstride + tl.k + 1] = make_double2(v, 0.0);
+        }
+        __syncwarp();
+        givens_warp(tl.H, tl.cs, tl.sn, tl.g, tl.active, tl.kused, tl.target, b, tl.k, pstride, tl.m, col_s, c_s,
+                    s_s);
+      }
+    }
+    if (threadIdx.x == 0) tl.gs_count[b] = 0;
   }
 }
 
@@ -417,84 +528,46 @@ __global__ void cycle_init_kernel(const double* __restrict__ nrm, const double* 
   for (int i = 0; i < pstride; ++i) g[b * pstride + i] = make_double2(i == 0 ? beta : 0.0, 0.0);
 }
 
-// Givens rotations of column k, residual estimate, convergence test.  One warp per
-// problem: the lanes stage the column and the rotations in shared memory, lane 0
-// applies the k previous rotations sequentially there.
-__global__ void givens_kernel(double2* __restrict__ H, double2* __restrict__ cs, double2* __restrict__ sn,
-                              double2* __restrict__ g, int* __restrict__ active, int* __restrict__ kused,
-                              const double* __restrict__ target, int k, int pstride, int m, int batch) {
-  __shared__ double2 col_s[kMaxRestart + 1], c_s[kMaxRestart], s_s[kMaxRestart];
-  const int b = blockIdx.x;
-  const int lane = threadIdx.x;
-  if (b >= batch || !active[b]) return;
-  double2* col = H + (long long)b * pstride * m + (long long)k * pstride;
-  double2* c = cs + b * m;
-  double2* s = sn + b * m;
-  for (int i = lane; i <= k + 1; i += 32) col_s[i] = col[i];
-  for (int i = lane; i < k; i += 32) {
-    c_s[i] = c[i];
-    s_s[i] = s[i];
-  }
-  __syncwarp();
-  if (lane == 0) {
-    double2* gg = g + b * pstride;
-    double2 hi = col_s[0];
-    for (int i = 0; i < k; ++i) {
-      const double2 hj = col_s[i + 1];
-      const double2 ci = c_s[i], si = s_s[i];
-      col_s[i] = make_double2(ci.x * hi.x - ci.y * hi.y + si.x * hj.x - si.y * hj.y,
-                              ci.x * hi.y + ci.y * hi.x + si.x * hj.y + si.y * hj.x);
-      hi = make_double2(-(si.x * hi.x + si.y * hi.y) + (ci.x * hj.x + ci.y * hj.y),
-                        -(si.x * hi.y - si.y * hi.x) + (ci.x * hj.y - ci.y * hj.x));
-    }
-    const double2 a = hi, bb = col_s[k + 1];
-    const double den = sqrt(a.x * a.x + a.y * a.y + bb.x * bb.x + bb.y * bb.y);
-    double2 cc, ss;
-    if (den == 0.0) {
-      cc = make_double2(1.0, 0.0);
-      ss = make_double2(0.0, 0.0);
-    } else {
-      cc = make_double2(a.x / den, -a.y / den);
-      ss = make_double2(bb.x / den, -bb.y / den);
-    }
-    c[k] = cc;
-    s[k] = ss;
-    col_s[k] = make_double2(den, 0.0);
-    col_s[k + 1] = make_double2(0.0, 0.0);
-    const double2 gk = gg[k];
-    gg[k + 1] = make_double2(-(ss.x * gk.x + ss.y * gk.y), -(ss.x * gk.y - ss.y * gk.x));
-    gg[k] = make_double2(cc.x * gk.x - cc.y * gk.y, cc.x * gk.y + cc.y * gk.x);
-    kused[b] = k + 1;
-    const double res = sqrt(gg[k + 1].x * gg[k + 1].x + gg[k + 1].y * gg[k + 1].y);
-    if (!(res > target[b]) || bb.x == 0.0 || !isfinite(res)) active[b] = 0;
-  }
-  __syncwarp();
-  for (int i = lane; i <= k + 1; i += 32) col[i] = col_s[i];
-}
 
+// y = R^-1 g for the rotated Hessenberg matrix R (upper triangular, column-major per
+// problem), one warp per problem: column-oriented back substitution, the lanes update
+// the remaining right-hand side with column i of R while lane 0 divides.
 __global__ void backsolve_kernel(const double2* __restrict__ H, const double2* __restrict__ g,
                                  double2* __restrict__ y, float2* __restrict__ y32, const int* __restrict__ kused,
                                  int pstride, int m, int batch) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ double2 acc[kMaxRestart + 1];
+  const int b = blockIdx.x;
+  const int lane = threadIdx.x;
   if (b >= batch) return;
   const int kk = kused[b];
   const double2* Hb = H + (long long)b * pstride * m;
   double2* yb = y + b * m;
-  for (int i = m - 1; i >= kk; --i) yb[i] = make_double2(0, 0);
-  for (int i = kk - 1; i >= 0; --i) {
-    double2 acc = g[b * pstride + i];
-    for (int c = i + 1; c < kk; ++c) {
-      const double2 t = cmul(Hb[(long long)c * pstride + i], yb[c]);
-      acc.x -= t.x;
-      acc.y -= t.y;
-    }
-    const double2 d = Hb[(long long)i * pstride + i];
-    const double dd = d.x * d.x + d.y * d.y;
-    yb[i] = dd > 0 ? make_double2((acc.x * d.x + acc.y * d.y) / dd, (acc.y * d.x - acc.x * d.y) / dd)
-                   : make_double2(0, 0);
+  for (int i = lane; i < m; i += 32) {
+    acc[i] = i < kk ? g[b * pstride + i] : make_double2(0, 0);
+    if (i >= kk) yb[i] = make_double2(0, 0);
   }
+  __syncwarp();
+  for (int i = kk - 1; i >= 0; --i) {
+    const double2* col = Hb + (long long)i * pstride;
+    const double2 d = col[i];
+    const double dd = d.x * d.x + d.y * d.y;
+    const double2 a = acc[i];
+    const double2 yi = dd > 0 ? make_double2((a.x * d.x + a.y * d.y) / dd, (a.y * d.x - a.x * d.y) / dd)
+                              : make_double2(0, 0);
+    if (lane == 0) yb[i] = yi;
+    for (int j = lane; j < i; j += 32) {
+      const double2 t = cmul(col[j], yi);
+      acc[j].x -= t.x;
+      acc[j].y -= t.y;
+    }
+    __syncwarp();
+  }
+  __syncwarp();
   if (y32)
-    for (int i = 0; i < m; ++i) y32[b * m + i] = make_float2((float)yb[i].x, (float)yb[i].y);
+    for (int i = lane; i < m; i += 32) {
+      const double2 v = i < kk ? yb[i] : make_double2(0, 0);
+      y32[b * m + i] = make_float2((float)v.x, (float)v.y);
+    }
 }
 
 template <typename T>
@@ -551,33 +624,37 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   const dim3 gu((unsigned)((N + 255) / 256), B);
   // classical Gram-Schmidt; the second pass runs for the problems that fail the DGKS
   // test (its kernels see P.reorth as their activity mask), for all with eta >= 1,
-  // for none with eta < 0
+  // for none with eta < 0.  The reductions, the norm and the Givens step run in the
+  // last block of each problem's multi-dot / update launch (KrylovTail).
   const double eta = sizeof(T) == sizeof(float2) ? P.inner_reorth_eta : P.reorth_eta;
   const int passes = eta < 0 ? 1 : 2;
+  KrylovTail tl{P.md_count, P.gs_count, P.partial, P.hcol, coef_col32<T>(P), P.H, P.cs, P.sn, P.g, P.active,
+                P.kused, P.reorth, P.target, P.nrm, sizeof(T) == sizeof(float2) ? nullptr : P.inv64,
+                sizeof(T) == sizeof(float2) ? P.mx.inv : nullptr, eta * eta, k, ps, mm, 1};
+  const unsigned gthreads = sizeof(T) == sizeof(float2) ? 128 : 256;
+  // the DGKS flags are written only for problems that take part in the first pass
+  if (passes == 2 && eta < 1) WG_CK(cudaMemsetAsync(P.reorth, 0, sizeof(int) * B, P.stream));
   for (int pass = 0; pass < passes; ++pass) {
     const int* mask = (pass == 0 || eta >= 1) ? P.active : P.reorth;
+    tl.first = pass == 0;
     cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B);
     multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, mask, N,
-                                                                                      nv, mp1, ps, P.nchunk);
+                                                                                      nv, mp1, ps, P.nchunk, tl);
     prof_end(P, PROF_MULTIDOT, ev);
-    ev = prof_begin(P, PROF_KRYLOV);
-    dot_reduce_kernel<<<B, 256, 0, P.stream>>>(P.partial, P.hcol, coef_col32<T>(P), P.H, mask, nv, k, ps, mm,
-                                               P.nchunk, pass == 0);
-    prof_end(P, PROF_KRYLOV, ev);
     ev = prof_begin(P, PROF_GSUPDATE, 1, (nv + 2) * vec, 8.0 * nv * N * B);
-    gs_update_kernel<T, true><<<gu, sizeof(T) == sizeof(float2) ? 128 : 256, 0, P.stream>>>(
-        V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1, ps, P.nblk);
+    if (pass == passes - 1)
+      gs_update_kernel<T, 2><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
+                                                             ps, P.nblk, tl);
+    else if (eta < 1)
+      gs_update_kernel<T, 1><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
+                                                             ps, P.nblk, tl);
+    else
+      gs_update_kernel<T, 0><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
+                                                             ps, P.nblk, tl);
     prof_end(P, PROF_GSUPDATE, ev);
-    if (pass == 0 && passes == 2 && eta < 1) {
-      ev = prof_begin(P, PROF_KRYLOV);
-      reorth_test_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.hcol, P.active, P.reorth, P.nblk, nv, ps,
-                                                 eta * eta);
-      prof_end(P, PROF_KRYLOV, ev);
-    }
   }
-  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 3, 2 * vec);
-  norm_reduce_kernel<<<B, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, P.H, P.active, P.nblk, k, ps, mm, P.inv64,
-                                             P.mx.inv);
+  // V_{k+1} = w / |w| for the problems still iterating
+  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 1, 2 * vec);
   if (sizeof(T) == sizeof(float2))
     scale_inv_kernel<float2, float><<<blocks_for(tot), 256, 0, P.stream>>>(
         reinterpret_cast<const float2*>(w), reinterpret_cast<float2*>(V) + (long long)(k + 1) * N, P.mx.inv,
@@ -586,7 +663,6 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
     scale_inv_kernel<double2, double><<<blocks_for(tot), 256, 0, P.stream>>>(
         reinterpret_cast<const double2*>(w), reinterpret_cast<double2*>(V) + (long long)(k + 1) * N, P.inv64,
         P.active, N, (long long)mp1 * N, B);
-  givens_kernel<<<B, 32, 0, P.stream>>>(P.H, P.cs, P.sn, P.g, P.active, P.kused, P.target, k, ps, mm, B);
   prof_end(P, PROF_KRYLOV, ev);
   WG_CK(cudaGetLastError());
   return WG_OK;
@@ -690,7 +766,7 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
       }
     }
     P.prof.launches[PROF_OTHER] += 3;
-    backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, nullptr, P.kused, ps, mm, B);
+    backsolve_kernel<<<B, 32, 0, P.stream>>>(P.H, P.g, P.ycoef, nullptr, P.kused, ps, mm, B);
     combine_kernel<double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.V, P.ycoef, P.kused, P.w, N, mp1, mm, B);
     WG_CK(launch_precondition(P, P.w, N, P.z));
     axpy_kernel<double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, P.z, nullptr, N, B);
@@ -751,7 +827,7 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     }
     // d = M^-1 (V y) in FP32, x += |r| d in FP64
     P.prof.launches[PROF_OTHER] += 3;
-    backsolve_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.H, P.g, P.ycoef, M.y, P.kused, ps, mm, B);
+    backsolve_kernel<<<B, 32, 0, P.stream>>>(P.H, P.g, P.ycoef, M.y, P.kused, ps, mm, B);
     combine_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(M.V, M.y, P.kused, M.w, N, mp1, mm, B);
     WG_CK(launch_precondition_mixed(P, M.w, N, M.d, nullptr));
     axpy_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, M.d, P.nrm_keep, N, B);

@@ -28,6 +28,7 @@ namespace {
 constexpr double kQP = 1.602176634e-19;   // solve_Poisson2D_rtd.m:79
 constexpr double kKBP = 1.380649e-23;     // solve_Poisson2D_rtd.m:80
 constexpr double kEps0 = 8.8541878128e-12;  // eval_Poisson2D_rtd.m:28
+constexpr int kPcrMax = 2048;                // Poisson unknowns per problem (block of 256 threads)
 
 __device__ double bmax(double v) {
   __shared__ double sh[32];
@@ -130,8 +131,7 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
   const double* up = di + nx;
   double* ncv = G.ncv + ox;
   double* cand = G.cand + ox;
-  double* wc = G.work + 2 * ox;    // Thomas: modified super-diagonal
-  double* wd = wc + nx;            // Thomas: modified rhs / solution
+  double* wd = G.work + 2 * ox + nx;   // right-hand side -F, then the Newton step
   const double* ndg = G.ndg + (long long)b * ncol;
   const double bias = G.bias[b];
   const double temp = G.temp[b] > 0 ? G.temp[b] : temp_default;
@@ -166,21 +166,63 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
   mf = bmax(mf);
   const double scale = fmax(fmax(mqn, mqd), fmax(mav, kQP));
   __syncthreads();
-  // 3. Thomas solve of J delta = -F over the free nodes 1..nx-2
-  if (threadIdx.x == 0) {
+  // 3. J delta = -F over the free nodes 1..nx-2 by parallel cyclic reduction in shared
+  //    memory (kPcrMax unknowns at most; J is diagonally dominant, so PCR is stable)
+  {
+    extern __shared__ double pcr[];   // a, b, c, d: 4 x n
+    const int n = nx - 2;
+    double* pa = pcr;
+    double* pb = pa + n;
+    double* pc = pb + n;
+    double* pd = pc + n;
     const double g = newton * kQP * kQP / (kKBP * temp);
-    double cprev = 0, dprev = 0;
-    for (int i = 1; i < nx - 1; ++i) {
-      const double a = (i > 1) ? lo[i] : 0.0;
-      const double bb = di[i] - g * ncv[i];
-      const double c = (i < nx - 2) ? up[i] : 0.0;
-      const double den = bb - a * cprev;
-      cprev = c / den;
-      dprev = (wd[i] - a * dprev) / den;
-      wc[i] = cprev;
-      wd[i] = dprev;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+      const int i = q + 1;
+      pa[q] = q > 0 ? lo[i] : 0.0;
+      pb[q] = di[i] - g * ncv[i];
+      pc[q] = q < n - 1 ? up[i] : 0.0;
+      pd[q] = wd[i];
     }
-    for (int i = nx - 3; i >= 1; --i) wd[i] -= wc[i] * wd[i + 1];
+    __syncthreads();
+    constexpr int R = kPcrMax / 256;
+    for (int st = 1; st < n; st <<= 1) {
+      double na[R], nb[R], nc[R], nd2[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int q = threadIdx.x + r * 256;
+        if (q >= n) continue;
+        double a = pa[q], bb = pb[q], c = pc[q], d = pd[q];
+        double an = 0.0, cn = 0.0;
+        if (q - st >= 0) {
+          const double k1 = a / pb[q - st];
+          an = -pa[q - st] * k1;
+          bb -= pc[q - st] * k1;
+          d -= pd[q - st] * k1;
+        }
+        if (q + st < n) {
+          const double k2 = c / pb[q + st];
+          cn = -pc[q + st] * k2;
+          bb -= pa[q + st] * k2;
+          d -= pd[q + st] * k2;
+        }
+        na[r] = an;
+        nb[r] = bb;
+        nc[r] = cn;
+        nd2[r] = d;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int q = threadIdx.x + r * 256;
+        if (q >= n) continue;
+        pa[q] = na[r];
+        pb[q] = nb[r];
+        pc[q] = nc[r];
+        pd[q] = nd2[r];
+      }
+      __syncthreads();
+    }
+    for (int q = threadIdx.x; q < n; q += blockDim.x) wd[q + 1] = pd[q] / pb[q];
   }
   __syncthreads();
   // 4. candidate, defect, linear residual |J delta + F|
@@ -263,9 +305,13 @@ cudaError_t gummel_observables(Problem& P) {
 }
 
 cudaError_t gummel_poisson(Problem& P, const int* active_dev, bool linear) {
+  static const cudaError_t attr = cudaFuncSetAttribute(poisson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       (int)(4 * sizeof(double) * kPcrMax));
+  if (attr != cudaSuccess) return attr;
   P.prof.launches[PROF_OTHER] += 1;
-  poisson_kernel<<<P.batch, 256, 0, P.stream>>>(P.gd, active_dev, P.nx, P.s.n_el * P.s.nK, P.s.nK, 300.0,
-                                                linear ? 0.0 : 1.0);
+  const size_t smem = 4 * sizeof(double) * (size_t)std::max(1, P.nx - 2);
+  poisson_kernel<<<P.batch, 256, smem, P.stream>>>(P.gd, active_dev, P.nx, P.s.n_el * P.s.nK, P.s.nK, 300.0,
+                                                   linear ? 0.0 : 1.0);
   return cudaGetLastError();
 }
 
@@ -340,6 +386,10 @@ int gummel_set(Problem& P, int b, const wg_device& dev, const wg_rtd_1d& rtd) {
   int rc = gummel_alloc(P);
   if (rc) return rc;
   const int nx = P.nx, nK = P.s.nK, n_el = P.s.n_el;
+  if (nx - 2 > kPcrMax || nx < 3) {
+    P.err = "wg_gummel_set: the Poisson grid needs 3 to " + std::to_string(kPcrMax + 2) + " nodes";
+    return WG_ERR_ARG;
+  }
   const double* x = dev.x_nm;
   const double dx = x[1] - x[0];
   for (int i = 1; i < nx; ++i)

@@ -483,6 +483,16 @@ cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162
 }
 
 // y = A_lo x for FP64 device vectors (conversion, mixed apply, conversion back).
+// n low-precision applies of the resident state (x in FP32 once, then M.z -> M.w repeatedly).
+cudaError_t apply_mixed_repeat(Problem& P, const double2* x, int n_apply) {
+  const long long n = P.N * P.batch;
+  cudaError_t e = mixed_sync_weights(P);
+  if (e != cudaSuccess) return e;
+  c2f_kernel<<<(unsigned)((n + 255) / 256), 256, 0, P.stream>>>(x, P.mx.z, n);
+  for (int i = 0; i < n_apply && e == cudaSuccess; ++i) e = launch_apply_mixed(P, P.mx.z, nullptr, P.mx.w);
+  return e;
+}
+
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y) {
   const long long n = P.N * P.batch;
   cudaError_t e = mixed_sync_weights(P);
@@ -583,10 +593,10 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y) {
 }
 
 // Stand-alone digit-sliced FP64 GEMM for diagnostics: C = A B with A row-major M x K,
-// B column-major K x N, C column-major M x N (host FP64 buffers), K <= 512, K % 8 == 0.
+// B column-major K x N, C column-major M x N (host FP64 buffers), K <= 1024, K % 8 == 0.
 int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err) {
   if (M < 1 || N < 1 || K < 64 || K % 8 || K > oz::MAX_K) {
-    err = "debug FP64 GEMM needs 64 <= K <= 512 and K % 8 == 0";
+    err = "debug FP64 GEMM needs 64 <= K <= 1024 and K % 8 == 0";
     return WG_ERR_ARG;
   }
   std::vector<double> a(A, A + (size_t)M * K);

@@ -5,10 +5,10 @@
 // Each row of A and each column of B is scaled by a power of two and rounded to
 // an integer F with |F| <= 2^(6S-1), which is written in S balanced base-64
 // digits: a = 2^e sum_p t_p 2^(-6(p+1)), |t_p| <= 32 (|t_0| <= 33).  The digits
-// are exact in BF16 and a digit product summed over K <= 512 stays below 2^20, so
-// every product A^(p) B^(q) is EXACT in the FP32 tensor-core accumulator.
-// Products of equal weight p+q (at most 8 of them) share one TMEM accumulator
-// (< 2^23, still exact); the S groups of a 128 x 64 output tile use 8 x 64 = 512
+// are exact in BF16 and a digit product summed over K <= 1024 stays below
+// 33^2 * 1024 < 2^21, so every product A^(p) B^(q) is EXACT in the FP32 tensor-core
+// accumulator.  Products of equal weight p+q (at most 8 of them) share one TMEM
+// accumulator (< 8 * 33^2 * 1024 < 2^24, still exact); the S groups of a 128 x 64 output tile use 8 x 64 = 512
 // TMEM columns.  Products of weight p+q >= S are dropped.  The epilogue adds the
 // groups in double-float FP32 arithmetic (exact power-of-two scalings, TwoSum),
 // converts once to FP64 and applies the row and column exponents with integer
@@ -28,7 +28,7 @@ constexpr int A_SLICE = BM * BK * 2;      // 16 KiB
 constexpr int B_SLICE = BN * BK * 2;      // 8 KiB
 constexpr int STAGE = S * (A_SLICE + B_SLICE);
 constexpr int SMEM_BYTES = STAGE + 1024 + 256;
-constexpr int MAX_K = 512;        // exactness bound of the grouped accumulation
+constexpr int MAX_K = 1024;       // exactness bound of the grouped accumulation (8 * 33^2 * K < 2^24)
 
 // Instruction descriptor: D f32, A/B bf16, K-major, M = 128, N = 64.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |

@@ -206,6 +206,8 @@ struct Problem {
   double* target = nullptr;      // [B] absolute residual targets
   int* active = nullptr;         // [B] 1 while iterating in this cycle
   int* reorth = nullptr;         // [B] 1 where the current Arnoldi step re-orthogonalises
+  int* md_count = nullptr;       // [B] last-block tickets of the multi-dot (zero between launches)
+  int* gs_count = nullptr;       // [B] last-block tickets of the Gram-Schmidt update
   int* kused = nullptr;          // [B] iterations used in this cycle
   int* any_active = nullptr;     // [1]
   int nchunk = 0;  // 2048-element chunks of one problem vector (multi-dot partials)
@@ -260,6 +262,7 @@ cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
                                       __nv_bfloat162* zb);
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);
+cudaError_t apply_mixed_repeat(Problem& P, const double2* x, int n_apply);
 int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err);
 int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // FP64 GMRES or the mixed-precision refinement, by P.precision.

@@ -121,6 +121,14 @@ class Problem1D:
                                       y.view(np.float64).ctypes.data_as(_lib._D)))
         return y
 
+    def apply_time(self, which="fp64", n=20):
+        """Mean device time [ms] of one operator apply on the resident state: ``fp64``,
+        ``lowprec`` (mixed inner operator) or ``fp64_tc`` (mixed FP64 operator)."""
+        code = {"fp64": 0, "lowprec": 1, "fp64_tc": 2}[which]
+        ms = C.c_double()
+        self._check(self.lib.wg_apply_repeat(self.h, code, int(n), C.byref(ms)))
+        return ms.value
+
     def apply_lowprec(self, x):
         """The mixed form's inner operator (BF16 tensor-core transforms, FP32 flux)."""
         x = _lib.as_c128(x).reshape(-1)

@@ -46,7 +46,7 @@ def test_tcgen05_bf16_gemm(built_lib, M, N, K):
     assert rel(Cout, ref) < 1e-5
 
 
-@pytest.mark.parametrize("M,N,K", [(256, 300, 512), (200, 150, 512), (128, 64, 64), (40, 37, 72)])
+@pytest.mark.parametrize("M,N,K", [(256, 300, 512), (200, 150, 512), (128, 64, 64), (40, 37, 72), (1024, 130, 1024)])
 def test_fp64_emulated_gemm(built_lib, M, N, K):
     """Digit-sliced FP64 GEMM on the tensor cores against numpy FP64: rows and
     columns spanning many binades, a zero column and a ragged tile edge; the
