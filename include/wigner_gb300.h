@@ -77,6 +77,8 @@ typedef struct {
   double inner_reorth; /* the same for the mixed form's inner FP32 solve; 0 -> never (one classical pass:
                           the inner solve only has to reduce the residual by inner_tol, and the FP64
                           refinement keeps the accuracy; a second pass measured 25% slower, same iterations) */
+  int fp64_tc;       /* FP64 handles: 1 = the two Phi transforms as FP64 products emulated on the tensor cores
+                        (8-digit slices, ~1e-14 of |Phi| |x|, 2 Nk and 2 N_xi <= 1024); 0 = native FP64 (default) */
 } wg_params;
 
 /* One problem's device/material data on the material grid (mat.x, nm). */

@@ -25,7 +25,8 @@ class WgParams(C.Structure):
     _fields_ = [("n_el", C.c_int), ("n_local", C.c_int), ("nk", C.c_int), ("n_xi", C.c_int),
                 ("l_xi", C.c_double), ("m_diff", C.c_double), ("mpc", C.c_double), ("precision", C.c_int),
                 ("restart", C.c_int), ("mem_budget_bytes", C.c_double), ("inner_restart", C.c_int),
-                ("inner_tol", C.c_double), ("reorth", C.c_double), ("inner_reorth", C.c_double)]
+                ("inner_tol", C.c_double), ("reorth", C.c_double), ("inner_reorth", C.c_double),
+                ("fp64_tc", C.c_int)]
 
 
 class WgDevice(C.Structure):

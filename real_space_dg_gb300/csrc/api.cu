@@ -83,7 +83,7 @@ bool inv_small(const double* A, double* out, int n) {
 
 namespace wg {
 
-double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision) {
+double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc) {
   const int nK = s.nK;
   const double N = (double)s.n_el * nK * s.nk, BN = N * batch, ncols = (double)batch * s.n_el * nK;
   const double nx = (double)s.n_el * (nK - 1) + 1;
@@ -91,6 +91,8 @@ double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner,
                8.0 * batch * s.n_el * nK * nK * (s.nxi + 1) + 16.0 * s.nxi * s.nk;
   est += 8.0 * batch * (nx * (8 + 2 * kMaxLocal) + 3.0 * s.n_el * nK + 12);   // Gummel state
   if (precision == WG_PREC_MIXED) est += mixed_bytes(s, batch, restart_inner);
+  if (precision == WG_PREC_MIXED || fp64_tc)   // digit slices of the FP64 emulation
+    est += 2.0 * 8 * ncols * 2 * std::max(s.nk, s.nxi) + 2.0 * 2 * 8 * 4.0 * s.nxi * s.nk;
   return est;
 }
 
@@ -213,7 +215,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   const int mp1 = P.restart + 1;
   const int pst = P.restart_max + 1;
   // memory estimate before allocating (GmresMemoryLimit analogue)
-  const double est = wg::estimate_bytes(s, batch, P.restart, P.restart_inner, P.precision);
+  P.fp64_tc = prm->fp64_tc != 0 && P.precision == WG_PREC_FP64;
+  const double est = wg::estimate_bytes(s, batch, P.restart, P.restart_inner, P.precision, P.fp64_tc);
   if (P.mem_budget > 0 && est > P.mem_budget) {
     delete h;
     return fail(nullptr, WG_ERR_OOM,
@@ -331,8 +334,8 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   API_CK(&P, cudaMemsetAsync(P.m_nodes, 0, sizeof(double) * batch * s.n_el * nK, P.stream));
   API_CK(&P, cudaMemsetAsync(P.xq, 0, sizeof(double) * batch * s.n_el * wg::kNqx, P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
-  if (P.precision == WG_PREC_MIXED) {
-    const int mr = wg::mixed_alloc(P);
+  if (P.precision == WG_PREC_MIXED || P.fp64_tc) {
+    const int mr = P.precision == WG_PREC_MIXED ? wg::mixed_alloc(P) : wg::ozaki_alloc(P);
     if (mr != WG_OK) {
       std::string msg = "wg_problem_create: " + P.err;
       free_all(P);
@@ -355,7 +358,7 @@ int wg_problem_bytes(const wg_params* prm, int batch, double* bytes) {
       wg::build_shape_light(s, prm->n_el, prm->n_local, prm->nk, prm->n_xi, prm->l_xi, prm->m_diff, prm->mpc);
   if (!e.empty()) return fail(nullptr, WG_ERR_ARG, "wg_problem_bytes: " + e);
   const int restart = prm->restart > 0 ? prm->restart : 50, inner = prm->inner_restart > 0 ? prm->inner_restart : 40;
-  *bytes = wg::estimate_bytes(s, batch, restart, inner, prm->precision);
+  *bytes = wg::estimate_bytes(s, batch, restart, inner, prm->precision, prm->fp64_tc != 0);
   return WG_OK;
 }
 
@@ -503,7 +506,7 @@ int wg_apply(wg_problem* h, const double* x, double* y) {
   else API_CK(&P, wg::launch_apply(P, P.z, P.w));
   API_CK(&P, cudaMemcpyAsync(y, P.w, sizeof(double2) * n, cudaMemcpyDeviceToHost, P.stream));
   API_CK(&P, cudaStreamSynchronize(P.stream));
-  if (P.precision == WG_PREC_MIXED) {
+  if (P.mx.err) {
     int herr = 0;
     API_CK(&P, cudaMemcpy(&herr, P.mx.err, sizeof(int), cudaMemcpyDeviceToHost));
     if (herr) return fail(&P, WG_ERR_TIMEOUT, "wg_apply: tensor-core GEMM barrier wait timed out");

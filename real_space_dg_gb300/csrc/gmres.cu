@@ -781,6 +781,14 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
       if (P.h_kused[b] > 0) cycles[b] += 1;
     }
   }
+  if (P.fp64_tc && P.mx.err) {
+    int herr = 0;
+    WG_CK(cudaMemcpy(&herr, P.mx.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (herr) {
+      P.err = "FP64 tensor-core GEMM: bounded barrier wait timed out";
+      return WG_ERR_TIMEOUT;
+    }
+  }
   return solve_end(P, bnorm, tgt, initial, res, iters, cycles, refs, info);
 }
 

@@ -61,7 +61,7 @@ bool make_map(CUtensorMap* m, const void* base, long long rows, int K, int box_r
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// bf16 digit stack [S][rows][K] (K-major), 64 x box_rows x 1 boxes, 128-byte swizzle.
+// bf16 digit stack [S][rows][K] (K-major), BK x box_rows x 1 boxes (64-byte rows), 64-byte swizzle.
 bool make_map3(CUtensorMap* m, const void* base, long long rows, int K, int box_rows) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
@@ -70,7 +70,7 @@ bool make_map3(CUtensorMap* m, const void* base, long long rows, int K, int box_
   cuuint32_t box[3] = {(cuuint32_t)oz::BK, (cuuint32_t)box_rows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -400,7 +400,22 @@ int mixed_alloc(Problem& P) {
     return WG_ERR_CUDA;
   }
   // FP64 outer residual on the tensor cores when the grouped accumulation stays exact
-  M.ozaki = 2 * nk <= oz::MAX_K && 2 * nxi <= oz::MAX_K;
+  return ozaki_alloc(P);
+}
+
+int ozaki_alloc(Problem& P) {
+  MixedBuffers& M = P.mx;
+  const Shape& s = P.s;
+  const int nk = s.nk, nxi = s.nxi;
+  bool ok = true;
+  if (!M.err) {
+    if (cudaMalloc(&M.err, sizeof(int)) != cudaSuccess || cudaMemset(M.err, 0, sizeof(int)) != cudaSuccess) {
+      P.err = "FP64 tensor-core buffers: error flag";
+      return WG_ERR_CUDA;
+    }
+  }
+  // exact grouped accumulation (K <= MAX_K) and 16-byte TMA rows of the digit slices
+  M.ozaki = 2 * nk <= oz::MAX_K && 2 * nxi <= oz::MAX_K && nk % 4 == 0 && nxi % 4 == 0;
   if (M.ozaki) {
     const int kmax = 2 * std::max(nk, nxi);
     std::vector<double> A1((size_t)4 * nxi * nk), A2((size_t)4 * nxi * nk);

@@ -393,6 +393,7 @@ void prof_release(Problem& P) {
 }
 
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
+  if (P.fp64_tc && P.mx.ozaki) return launch_apply_f64_tc(P, x, y);
   switch (P.s.nK) {
     case 2: return apply_nk<2>(P, x, y);
     case 3: return apply_nk<3>(P, x, y);

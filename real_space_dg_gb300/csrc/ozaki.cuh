@@ -22,17 +22,31 @@ namespace oz {
 
 constexpr int S = 8;              // digits per operand
 constexpr int BETA = 6;           // bits per digit
-constexpr int BM = 128, BN = 64, BK = 64;
+// k blocks of 32 (64-byte rows, 64-byte swizzle) so that two stages of all 8 slices fit:
+// the TMA loads of block kb+1 overlap the 72 MMAs of block kb
+constexpr int BM = 128, BN = 64, BK = 32, STAGES = 2;
 constexpr int NGROUP = S;         // weights p+q = 2 .. S+1
-constexpr int A_SLICE = BM * BK * 2;      // 16 KiB
-constexpr int B_SLICE = BN * BK * 2;      // 8 KiB
-constexpr int STAGE = S * (A_SLICE + B_SLICE);
-constexpr int SMEM_BYTES = STAGE + 1024 + 256;
+constexpr int A_SLICE = BM * BK * 2;      // 8 KiB
+constexpr int B_SLICE = BN * BK * 2;      // 4 KiB
+constexpr int STAGE = S * (A_SLICE + B_SLICE);   // 96 KiB
+constexpr int SMEM_BYTES = STAGES * STAGE + 1024 + 256;
 constexpr int MAX_K = 1024;       // exactness bound of the grouped accumulation (8 * 33^2 * K < 2^24)
 
 // Instruction descriptor: D f32, A/B bf16, K-major, M = 128, N = 64.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                             ((uint32_t)(BM >> 4) << 24);
+
+// K-major operand tile with 64-byte rows and the 64-byte swizzle (8-row atoms of 512 bytes).
+__device__ __forceinline__ uint64_t sdesc_sw64(const void* p) {
+  const uint64_t addr = tc::smem_u32(p);
+  uint64_t d = 0;
+  d |= (addr >> 4) & 0x3FFFull;
+  d |= 1ull << 16;                    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;    // stride byte offset: 8 rows x 64 bytes
+  d |= 1ull << 46;                    // descriptor version
+  d |= 4ull << 61;                    // 64-byte swizzle
+  return d;
+}
 
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
                                             uint64_t* bar) {
@@ -74,11 +88,10 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
                                                             int* __restrict__ err) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* sa = smem;                       // [S][BM][BK] bf16
-  uint8_t* sb = smem + S * A_SLICE;         // [S][BN][BK] bf16
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGE);
-  uint64_t* empty = full + 1;
-  uint64_t* done = empty + 1;
+  // stage s: [S][BM][BK] bf16 A slices, then [S][BN][BK] bf16 B slices
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
+  uint64_t* empty = full + STAGES;
+  uint64_t* done = empty + STAGES;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM;
@@ -86,8 +99,10 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
   const int nkb = (K + BK - 1) / BK;
 
   if (threadIdx.x == 0) {
-    tc::mbar_init(full, 1);
-    tc::mbar_init(empty, 1);
+    for (int st = 0; st < STAGES; ++st) {
+      tc::mbar_init(&full[st], 1);
+      tc::mbar_init(&empty[st], 1);
+    }
     tc::mbar_init(done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -99,17 +114,23 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
 
   if (warp == 0 && lane == 0) {
     for (int kb = 0; kb < nkb; ++kb) {
-      if (kb > 0 && !tc::mbar_wait(empty, (kb - 1) & 1, err)) break;
-      tc::mbar_expect_tx(full, STAGE);
+      const int st = kb % STAGES;
+      if (kb >= STAGES && !tc::mbar_wait(&empty[st], ((kb / STAGES) + 1) & 1, err)) break;
+      uint8_t* sa = smem + st * STAGE;
+      uint8_t* sb = sa + S * A_SLICE;
+      tc::mbar_expect_tx(&full[st], STAGE);
       for (int p = 0; p < S; ++p) {
-        tma_load_3d(sa + p * A_SLICE, &tmA, kb * BK, m0, p, full);
-        tma_load_3d(sb + p * B_SLICE, &tmB, kb * BK, (int)n0, p, full);
+        tma_load_3d(sa + p * A_SLICE, &tmA, kb * BK, m0, p, &full[st]);
+        tma_load_3d(sb + p * B_SLICE, &tmB, kb * BK, (int)n0, p, &full[st]);
       }
     }
   } else if (warp == 1 && lane == 0) {
     for (int kb = 0; kb < nkb; ++kb) {
-      if (!tc::mbar_wait(full, kb & 1, err)) break;
+      const int st = kb % STAGES;
+      if (!tc::mbar_wait(&full[st], (kb / STAGES) & 1, err)) break;
       tc::fence_after();
+      const uint8_t* sa = smem + st * STAGE;
+      const uint8_t* sb = sa + S * A_SLICE;
       for (int p = 0; p < S; ++p)
         for (int q = 0; q + p < S; ++q) {        // weight p+q (0-based) <= S-1
           const int g = p + q;
@@ -121,10 +142,10 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
 #pragma unroll
           for (int kk = 0; kk < BK / 16; ++kk) {
             const uint32_t acc = (kb > 0 || kk > 0 || p > 0) ? 1u : 0u;
-            tc::mma_bf16(d, tc::sdesc_sw128(a + kk * 32), tc::sdesc_sw128(b + kk * 32), kIdesc, acc);
+            tc::mma_bf16(d, sdesc_sw64(a + kk * 32), sdesc_sw64(b + kk * 32), kIdesc, acc);
           }
         }
-      tc::mma_commit(empty);
+      tc::mma_commit(&empty[st]);
     }
     tc::mma_commit(done);
   }

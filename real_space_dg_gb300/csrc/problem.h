@@ -154,6 +154,7 @@ struct Problem {
   double mem_budget = 0;
   FluxBlocks fb{};
   double shift = 0;         // sigma of the shifted operator A + sigma I (0: the stationary A)
+  bool fp64_tc = false;     // FP64 handle whose transforms run as FP64 emulated on the tensor cores
   std::string err;
 
   std::vector<HostProblem> hp;
@@ -237,7 +238,7 @@ cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride
 // k-line factors of A + sigma I for every problem (sigma = P.shift), uploaded to pre_dinv / pre_h.
 int set_kline_factors(Problem& P);
 // Device bytes of a handle before allocation (the admission estimate of wg_problem_create).
-double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision);
+double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc = false);
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y);
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh);
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
@@ -256,6 +257,8 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
 std::string mixed_check_shape(const Shape& s);
 double mixed_bytes(const Shape& s, int batch, int restart);
 int mixed_alloc(Problem& P);
+// Digit slices of Phi, state slice buffer and tensor maps of the FP64 emulation (any precision).
+int ozaki_alloc(Problem& P);
 void mixed_free(Problem& P);
 cudaError_t mixed_sync_weights(Problem& P);
 cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y);

@@ -15,7 +15,9 @@
 namespace wg {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 64, STAGES = 4;
+// 3 stages: 97 KiB of shared memory, so two CTAs (2 x 128 TMEM columns) share an SM and
+// one CTA's loads and epilogue overlap the other's MMAs
+constexpr int BM = 128, BN = 128, BK = 64, STAGES = 3;
 constexpr int A_STAGE = BM * BK * 2;         // 16 KiB
 constexpr int B_STAGE = BN * BK * 2;         // 16 KiB
 constexpr int STAGE_BYTES = A_STAGE + B_STAGE;
@@ -128,7 +130,7 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN 
 
 // EPI 0: D = A B.  EPI 1: D += A B.
 template <int EPI>
-__global__ void __launch_bounds__(128, 1) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA,
                                                            const __grid_constant__ CUtensorMap tmB,
                                                            float* __restrict__ D, int M, long long Ncol, int K,
                                                            int* __restrict__ err) {

@@ -30,7 +30,7 @@ from .transport import M0, Problem1D, shape_from_mat
 DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityTolerance=5e-4,
                 poissonResidualTolerance=8e-2, transportTolerance=1e-8, transportMaxCycles=50,
                 fermiOffset=0.05, restart=50, precision="fp64", innerRestart=40, innerTol=1e-3,
-                inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0)
+                inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0, fp64TensorCores=False)
 
 
 def _opts(options):
@@ -53,7 +53,8 @@ class RTDSweep:
         shp = shape_from_mat(mat)
         self.P = Problem1D(batch=batch, precision=self.o["precision"], restart=self.o["restart"],
                            inner_restart=self.o["innerRestart"], inner_tol=self.o["innerTol"],
-                           reorth=self.o["reorth"], inner_reorth=self.o["innerReorth"], **shp)
+                           reorth=self.o["reorth"], inner_reorth=self.o["innerReorth"],
+                           fp64_tc=self.o["fp64TensorCores"], **shp)
         self.lib = self.P.lib
         self.nx = int(mat["Nx"])
         self.dy = float(mat.get("dy_norm_nm") or devices.density_normalisation_nm(mat, self.o["fermiOffset"]))

@@ -3,7 +3,8 @@
 Tolerances: operator apply / rhs / preconditioner 1e-12 relative (FP64,
 different summation order); solution, density and current against the
 oracle's sparse LU: density <= 1e-9, current <= 1e-8 relative L2 (the parity
-bar of the plain form), with GMRES run to a 1e-12 relative residual.
+bar of the plain form), with GMRES run to a 1e-12 relative residual.  The same
+bars hold with the FP64 transforms emulated on the tensor cores (fp64_tc).
 """
 import os
 
@@ -42,14 +43,15 @@ def make_problem(spec, batch=1, **kw):
 CASES = [(12, 32, 2, 0), (10, 16, 1, 20), (8, 24, 3, 0), (9, 20, 2, 26)]
 
 
+@pytest.mark.parametrize("fp64_tc", [False, True])
 @pytest.mark.parametrize("n_el,nk,order,nxi", CASES)
-def test_apply_rhs_precond_match_oracle(lib, n_el, nk, order, nxi):
+def test_apply_rhs_precond_match_oracle(lib, n_el, nk, order, nxi, fp64_tc):
     spec, mat, E, efl, efr, m = small_rtd(n_el=n_el, nk=nk, order=order, n_xi=nxi)
     p = dg1d.init_params(mat, efl, efr, E, m)
     A, rhs = dg1d.get_sysm(mat, p, E)
     op = krylov.Operator1D(mat, p, E)
     pre = krylov.KLinePreconditioner(op, use_drift_diag=False)
-    with make_problem(spec) as P:
+    with make_problem(spec, fp64_tc=fp64_tc) as P:
         P.set_potential(0, mat["x"], E, m, spec.m_rel, spec.temp_k, efl, efr)
         x = det_vec(P.N)
         assert rel(P.apply(x), A @ x) < 1e-12
@@ -57,14 +59,15 @@ def test_apply_rhs_precond_match_oracle(lib, n_el, nk, order, nxi):
         assert rel(P.precondition(x), pre.apply(x)) < 1e-12
 
 
+@pytest.mark.parametrize("fp64_tc", [False, True])
 @pytest.mark.parametrize("n_el,nk,order,nxi", CASES)
-def test_solve_matches_direct_solve(lib, n_el, nk, order, nxi):
+def test_solve_matches_direct_solve(lib, n_el, nk, order, nxi, fp64_tc):
     spec, mat, E, efl, efr, m = small_rtd(n_el=n_el, nk=nk, order=order, n_xi=nxi)
     p = dg1d.init_params(mat, efl, efr, E, m)
     A, rhs = dg1d.get_sysm(mat, p, E)
     ref = spla.spsolve(A.tocsc(), rhs)
     n_ref, j_ref, ru_ref = dg1d.observables(p, ref, dg1d.node_map(p, m))
-    with make_problem(spec) as P:
+    with make_problem(spec, fp64_tc=fp64_tc) as P:
         P.set_potential(0, mat["x"], E, m, spec.m_rel, spec.temp_k, efl, efr)
         st, info = P.solve(tol=1e-12, maxit=60)
         assert st == 0 and info[0]["flag"] == 0 and info[0]["relres"] <= 1e-12
