@@ -6,12 +6,12 @@ RTD, GaAs, 80 nm device with 20 nm contacts at 1e18 cm^-3, Al0.3Ga0.7As double
 barrier 0.27 eV x 3 nm around a 5 nm well; DG p=3, 240 elements, Nk=256 (245,760
 complex unknowns per bias point); Gummel mixing 0.3, potential tolerance 1e-6 V;
 every transport solve to a 1e-8 relative residual.  One step = one batch of
-`--batch` bias points (0.2 V * (1..B)/B) solved from a cold start to the Gummel
+`--batch` (16) bias points (0.2 V * (1..B)/B) solved from a cold start to the Gummel
 fixed point, all points advancing together in one handle.  Default form: mixed
 precision (BF16 tensor-core transforms inside FP64 refinement) with the inexact
-Gummel schedule (transport tolerance tied to the potential defect, every
-accepted state re-solved at 1e-8); ``--precision fp64 --inexact 0`` is the
-plain drop-in form.
+Gummel schedule (transport tolerance 0.3 x the potential defect in V, at most
+1e-3; every accepted state re-solved at 1e-8); ``--precision fp64 --inexact 0``
+is the plain drop-in form.
 
 Arms: default (ours, this library on the GPU) and ``--impl reference`` (the CPU
 restatement of the reference algorithm, timed on a bounded sample).
@@ -183,8 +183,8 @@ def run_ours(args, rank, world, dist):
 
     spec, mat, biases = make_workload(args.batch)
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
-                innerTol=args.inner_tol, inexactFactor=args.inexact, reorth=args.reorth, innerReorth=args.inner_reorth,
-                fp64TensorCores=args.fp64_tc)
+                innerTol=args.inner_tol, inexactFactor=args.inexact, inexactCap=args.inexact_cap, reorth=args.reorth,
+                innerReorth=args.inner_reorth, fp64TensorCores=args.fp64_tc)
     if args.max_gummel:
         opts["maxIterations"] = args.max_gummel      # profiling runs only: points need not converge
     S = RTDSweep(mat, args.batch, opts)
@@ -253,7 +253,7 @@ def run_ours(args, rank, world, dist):
                    "batch_bias_points": args.batch, "biases_v": [round(float(b), 4) for b in biases],
                    "precision": args.precision, "gmres_restart": args.restart,
                    "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
-                   "inexact_gummel_factor": args.inexact, "gummel_mixing": 0.3,
+                   "inexact_gummel_factor": args.inexact, "inexact_cap": args.inexact_cap, "gummel_mixing": 0.3,
                    "reorth": args.reorth, "inner_reorth": args.inner_reorth, "fp64_tensor_cores": args.fp64_tc,
                    "potential_tol_v": 1e-6, "transport_rtol": 1e-8,
                    "l2": "inputs larger than L2 (Krylov basis %.2f GB)" %
@@ -350,6 +350,7 @@ def run_served(args):
     # the C2 loop settings; high-bias points of the stiffer devices need more than 200 damped iterations
     opts = dict(GUMMEL, maxIterations=SERVED["max_gummel"], precision=args.precision, restart=args.restart,
                 innerRestart=args.inner_restart, innerTol=args.inner_tol, inexactFactor=args.inexact,
+                inexactCap=args.inexact_cap,
                 reorth=args.reorth, innerReorth=args.inner_reorth)
     clocks = ClockSampler()
     clocks.start()
@@ -396,7 +397,8 @@ def run_transient(args):
     steps_v = rng.uniform(0.1, 0.4, B)
     base = dict(SPEC, order=TRANSIENT["order"], n_el=TRANSIENT["n_el"], nk=TRANSIENT["nk"])
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
-                innerTol=args.inner_tol, inexactFactor=args.inexact, reorth=args.reorth, innerReorth=args.inner_reorth)
+                innerTol=args.inner_tol, inexactFactor=args.inexact, inexactCap=args.inexact_cap, reorth=args.reorth,
+                innerReorth=args.inner_reorth)
     # one handle; the problems differ in their barrier width (device data per problem)
     mats = []
     for w in widths:
@@ -475,14 +477,16 @@ def main():
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
-    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
     ap.add_argument("--inner-restart", type=int, default=40)
     ap.add_argument("--inner-tol", type=float, default=1e-3)
     ap.add_argument("--max-gummel", type=int, default=0,
                     help="cap on Gummel iterations for profiling runs (0: run to convergence)")
-    ap.add_argument("--inexact", type=float, default=1e-2,
+    ap.add_argument("--inexact", type=float, default=0.3,
                     help="inexact Gummel factor (transport tol = factor * potential defect); 0 = fixed 1e-8")
+    ap.add_argument("--inexact-cap", type=float, default=1e-3,
+                    help="loosest transport tolerance of the inexact Gummel schedule")
     ap.add_argument("--reorth", type=float, default=0.0,
                     help="DGKS re-orthogonalisation threshold of the FP64 Arnoldi (0: 1/sqrt(2), <0 never, >=1 always)")
     ap.add_argument("--inner-reorth", type=float, default=0.0,

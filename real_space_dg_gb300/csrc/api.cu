@@ -43,7 +43,7 @@ void free_all(wg::Problem& P) {
       e = nullptr;
     }
   wg::gummel_free(P);
-  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.kmap_a, P.kmap_s, P.cosm, P.pinv, P.pp, P.flr, P.qd, P.beta, P.xq, P.pot_x,
+  void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.kmap_a, P.kmap_s, P.cosm, P.pinv, P.pp, P.flr, P.fxi, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
                   P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.md_count, P.gs_count, P.kused, P.any_active};
   for (void* p : ptrs)
@@ -257,6 +257,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.pinv, (size_t)s.nk * s.nxi, bytes));
   A(dalloc(&P.pp, (size_t)batch * wg::kPP, bytes));
   A(dalloc(&P.flr, (size_t)batch * 2 * s.nk, bytes));
+  A(dalloc(&P.fxi, (size_t)batch * 2 * s.nxi, bytes));
   A(dalloc(&P.qd, batch, bytes));
   A(dalloc(&P.beta, (size_t)batch * s.n_el * nK * nK * (s.nxi + 1), bytes));
   A(dalloc(&P.xq, (size_t)batch * s.n_el * wg::kNqx, bytes));

@@ -102,6 +102,10 @@ void slice_rows_host(const std::vector<double>& A, int M, int K, std::vector<bf1
   }
 }
 
+unsigned slice_blocks(long long ncol) {
+  return (unsigned)((ncol + oz::kSliceColsPerBlock - 1) / oz::kSliceColsPerBlock);
+}
+
 template <int EPI>
 cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* ea, const int* eb, double* C, int M,
                          long long Ncol, int K, int* err, cudaStream_t st) {
@@ -590,7 +594,8 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y) {
   if (e != cudaSuccess) return e;
   cudaEvent_t ev = prof_begin(P, PROF_GEMM_F64, 2, 8.0 * P.N * P.batch + 16.0 * s.nxi * ncols,
                               8.0 * s.nxi * s.nk * ncols);
-  oz::slice_columns_kernel<<<(unsigned)P.ncols, 256, 0, P.stream>>>(reinterpret_cast<const double*>(x), K1, P.ncols,
+  oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
+      reinterpret_cast<const double*>(x), K1, P.ncols,
                                                                     M.ob, M.eb);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
                       P.stream);
@@ -599,7 +604,8 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y) {
   e = launch_stencil_f64(P, P.xh, P.yh);
   if (e != cudaSuccess) return e;
   ev = prof_begin(P, PROF_GEMM_F64, 2, 16.0 * s.nxi * ncols + 16.0 * P.N * P.batch, 8.0 * s.nxi * s.nk * ncols);
-  oz::slice_columns_kernel<<<(unsigned)P.ncols, 256, 0, P.stream>>>(reinterpret_cast<const double*>(P.yh), K2,
+  oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
+      reinterpret_cast<const double*>(P.yh), K2,
                                                                     P.ncols, M.ob, M.eb);
   e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream);
   prof_end(P, PROF_GEMM_F64, ev);
@@ -639,7 +645,7 @@ int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N,
       err = "cuTensorMapEncodeTiled failed";
       rc = WG_ERR_CUDA;
     } else {
-      oz::slice_columns_kernel<<<N, 256>>>(dB, K, N, db, deb);
+      oz::slice_columns_kernel<<<slice_blocks(N), 32 * oz::kSliceColsPerBlock>>>(dB, K, N, db, deb);
       e = launch_ozaki<0>(ma, mb, dea, deb, dC, M, N, K, derr, 0);
       if (e == cudaSuccess) e = cudaDeviceSynchronize();
       int herr = 0;

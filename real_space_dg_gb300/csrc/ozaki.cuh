@@ -202,48 +202,58 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
 // base-64 digits t_p (p = 0 most significant), x = 2^e sum_p t_p 2^(-6(p+1)) with
 // e = m + 1 written to e_out[c]; t_p goes as bf16 to slices[p][c][k] (K-major).
 // Integer arithmetic on the FP64 bit patterns only.
-__global__ void __launch_bounds__(256) slice_columns_kernel(const double* __restrict__ X, int K, long long Ncol,
-                                                            __nv_bfloat16* __restrict__ slices,
-                                                            int* __restrict__ e_out) {
-  const long long c = blockIdx.x;
-  if (c >= Ncol) return;
-  const double* x = X + c * (long long)K;
-  unsigned long long mx = 0;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    const unsigned long long a = (unsigned long long)__double_as_longlong(x[k]) & 0x7FFFFFFFFFFFFFFFull;
-    mx = a > mx ? a : mx;
+constexpr int kSliceColsPerBlock = 8;   // one warp per column
+
+__device__ __forceinline__ long long round_scaled(long long bits, int m, bool nonzero) {
+  const int ex = (int)((bits >> 52) & 0x7FF);
+  long long F = 0;   // round(|x| 2^(6S-1-m)) <= 2^(6S-1)
+  if (ex != 0 && nonzero) {
+    const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int rs = m - (ex - 1023 - 52) - (BETA * S - 1);   // >= 6 since |x| < 2^m
+    if (rs < 64) F = (long long)((mant + (1ull << (rs - 1))) >> rs);
   }
-  __shared__ unsigned long long smx[8];
+  return bits < 0 ? -F : F;
+}
+
+// One warp per column, two consecutive k per lane (K is even): 4-byte stores per slice.
+__global__ void __launch_bounds__(32 * kSliceColsPerBlock) slice_columns_kernel(const double* __restrict__ X, int K,
+                                                                               long long Ncol,
+                                                                               __nv_bfloat16* __restrict__ slices,
+                                                                               int* __restrict__ e_out) {
+  const int lane = threadIdx.x & 31;
+  const long long c = (long long)blockIdx.x * kSliceColsPerBlock + (threadIdx.x >> 5);
+  if (c >= Ncol) return;
+  const double2* x = reinterpret_cast<const double2*>(X + c * (long long)K);
+  const int K2 = K / 2;
+  unsigned long long mx = 0;
+  for (int k = lane; k < K2; k += 32) {
+    const double2 v = x[k];
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull;
+    mx = a > mx ? a : mx;
+    mx = b > mx ? b : mx;
+  }
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long t = __shfl_xor_sync(0xffffffffu, mx, o);
     mx = t > mx ? t : mx;
   }
-  if ((threadIdx.x & 31) == 0) smx[threadIdx.x >> 5] = mx;
-  __syncthreads();
-  mx = 0;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) mx = smx[w] > mx ? smx[w] : mx;
   const int emax = (int)((mx >> 52) & 0x7FF);
   const int m = mx == 0 ? 0 : emax - 1023 + 1;   // max|x| < 2^m
-  if (threadIdx.x == 0) e_out[c] = m + 1;
+  if (lane == 0) e_out[c] = m + 1;
   const long long slice_stride = Ncol * (long long)K;
-  for (int k = threadIdx.x; k < K; k += blockDim.x) {
-    const long long bits = __double_as_longlong(x[k]);
-    const int ex = (int)((bits >> 52) & 0x7FF);
-    long long F = 0;   // round(|x| 2^(6S-1-m)) <= 2^(6S-1)
-    if (ex != 0 && mx != 0) {
-      const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-      const int rs = m - (ex - 1023 - 52) - (BETA * S - 1);   // >= 6 since |x| < 2^m
-      if (rs < 64) F = (long long)((mant + (1ull << (rs - 1))) >> rs);
-    }
-    if (bits < 0) F = -F;
-    __nv_bfloat16* out = slices + c * (long long)K + k;
+  __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(slices + c * (long long)K);
+  for (int k = lane; k < K2; k += 32) {
+    const double2 v = x[k];
+    long long F0 = round_scaled(__double_as_longlong(v.x), m, mx != 0);
+    long long F1 = round_scaled(__double_as_longlong(v.y), m, mx != 0);
 #pragma unroll
     for (int p = S - 1; p > 0; --p) {
-      const long long d = ((F + 32) & 63) - 32;
-      out[p * slice_stride] = __float2bfloat16_rn((float)d);
-      F = (F - d) >> BETA;
+      const int d0 = (int)(((F0 + 32) & 63) - 32), d1 = (int)(((F1 + 32) & 63) - 32);
+      out[p * (slice_stride / 2) + k] = __floats2bfloat162_rn((float)d0, (float)d1);
+      F0 = (F0 - d0) >> BETA;
+      F1 = (F1 - d1) >> BETA;
     }
-    out[0] = __float2bfloat16_rn((float)F);
+    out[k] = __floats2bfloat162_rn((float)F0, (float)F1);
   }
 }
 

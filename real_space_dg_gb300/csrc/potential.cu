@@ -4,10 +4,11 @@
 //   minmax_kernel   min V (V(x >= Lx) of V_transient.m:6) and max V (kz range of
 //                   verteilung.m:140)
 //   fermi_kernel    f_L(k), f_R(k): Fermi-Dirac occupation integrated over 1001 kz
-//                   (verteilung.m:139-152), one block per (k, problem)
-//   inflow_kernel   cosine transform to the xi cells, least-squares projection on
-//                   Phi (pseudo-inverse, verteilung.m:158-168) and the contact
-//                   inflow blocks of the rhs (get_Diff.m:77-83)
+//                   (verteilung.m:139-152), 16 k per block, kz factors shared
+//   inflow_xi_kernel cosine transform to the xi cells (verteilung.m:158-161)
+//   inflow_kernel   least-squares projection on Phi (pseudo-inverse,
+//                   verteilung.m:167-168) and the contact inflow blocks of the rhs
+//                   (get_Diff.m:77-83)
 //   vw_kernel       Wigner-potential weights beta[e][ab][s] (the Vw(x,k) rebuild of
 //                   get_Drift_accel_trial_permutedShell.m:64-147, contracted with the
 //                   element quadrature)
@@ -59,81 +60,135 @@ __global__ void minmax_kernel(const double* __restrict__ pot_v, double* __restri
 }
 
 // f_{L,R}(k_j) = 2/pi dkz sum_z 1/(1 + exp(q (E_{L,R}(k) + E_kz - E_F) / (kB T)))
-__global__ void fermi_kernel(const double* __restrict__ pot_v, const double* __restrict__ pp,
-                             const double* __restrict__ kvec, double* __restrict__ flr, int nx, int nk, int b0,
-                             const int* __restrict__ mask) {
-  const int j = blockIdx.x, b = b0 + blockIdx.y;
+// 1 / d for d >= 1 by Newton-Raphson from the FP32 reciprocal: two steps take the
+// ~23 correct bits to full double precision (within an ulp or two) without the
+// FP64 divide sequence.
+__device__ __forceinline__ double recip_ge1(double d) {
+  if (!(d < 1e30)) return isinf(d) ? 0.0 : 1.0 / d;   // outside FP32 range (rare): plain division
+  double r = (double)__frcp_rn((float)d);
+  r = r * fma(-d, r, 2.0);
+  r = r * fma(-d, r, 2.0);
+  return r;
+}
+
+// f_L(k_j), f_R(k_j) for kFermiJ consecutive j of problem b.  The Fermi factor of
+// (j, kz) is 1 / (1 + a_j g(kz)) with a_j = exp((E_j - E_F) / kT) and
+// g(kz) = exp(hbar^2 kz^2 / (2 m_z kT)): the kz factors are computed once per block
+// in shared memory, the j factors once per j, instead of one exponential per (j, kz).
+constexpr int kFermiJ = 16;
+__global__ void __launch_bounds__(256) fermi_kernel(const double* __restrict__ pot_v, const double* __restrict__ pp,
+                                                    const double* __restrict__ kvec, double* __restrict__ flr,
+                                                    int nx, int nk, int b0, const int* __restrict__ mask) {
+  __shared__ double g[kNkz];
+  const int b = b0 + blockIdx.y;
   if (mask && !mask[b]) return;
   const double* P = pp + b * kPP;
   const double hb = kHV / 2 / kPi;
-  const double k = kvec[j];
-  const double v0 = pot_v[(long long)b * nx], v1 = pot_v[(long long)b * nx + nx - 1];
-  const double EL = v0 + hb * hb * k * k / 2 / P[PP_M0] / kQV;
-  const double ER = v1 + hb * hb * k * k / 2 / P[PP_M1] / kQV;
   const double me_z = P[PP_MEZ], temp = P[PP_TEMP];
   const double kz_max = sqrt(2 * 2 * kM0V * me_z * kQV * (P[PP_VMAX] + 0.3)) / hb;
   const double dkz = kz_max / (kNkz - 1);
-  double sl = 0, sr = 0;
+  const double inv_kt = kQV / (kKBV * temp);
+  const double cz = hb * hb / 2 / kM0V / me_z / kQV;
   for (int z = threadIdx.x; z < kNkz; z += blockDim.x) {
     const double kz = (z == kNkz - 1) ? kz_max : z * dkz;
-    const double ekz = hb * hb * kz * kz / 2 / kM0V / me_z / kQV;
-    sl += 1.0 / (1.0 + exp(kQV * (EL + ekz - P[PP_EFL]) / (kKBV * temp)));
-    sr += 1.0 / (1.0 + exp(kQV * (ER + ekz - P[PP_EFR]) / (kKBV * temp)));
+    g[z] = exp(cz * kz * kz * inv_kt);
   }
-  sl = block_reduce(sl, false);
-  sr = block_reduce(sr, false);
-  if (threadIdx.x == 0) {
-    flr[((long long)b * 2 + 0) * nk + j] = 2 / kPi * dkz * sl;
-    flr[((long long)b * 2 + 1) * nk + j] = 2 / kPi * dkz * sr;
+  __syncthreads();
+  const double v0 = pot_v[(long long)b * nx], v1 = pot_v[(long long)b * nx + nx - 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int jj = warp; jj < kFermiJ; jj += nw) {
+    const int j = blockIdx.x * kFermiJ + jj;
+    if (j >= nk) break;
+    const double k = kvec[j];
+    const double EL = v0 + hb * hb * k * k / 2 / P[PP_M0] / kQV;
+    const double ER = v1 + hb * hb * k * k / 2 / P[PP_M1] / kQV;
+    const double aL = exp((EL - P[PP_EFL]) * inv_kt), aR = exp((ER - P[PP_EFR]) * inv_kt);
+    double sl = 0, sr = 0;
+    for (int z = lane; z < kNkz; z += 32) {
+      sl += recip_ge1(1.0 + aL * g[z]);
+      sr += recip_ge1(1.0 + aR * g[z]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      sl += __shfl_xor_sync(0xffffffffu, sl, o);
+      sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    }
+    if (lane == 0) {
+      flr[((long long)b * 2 + 0) * nk + j] = 2 / kPi * dkz * sl;
+      flr[((long long)b * 2 + 1) * nk + j] = 2 / kPi * dkz * sr;
+    }
   }
 }
 
 // fLn(s) = sum_j cos(xi_s k_j) f(k_j) dk/(2 pi); fnl = Phi^+ fLn; rhs blocks.
-__global__ void inflow_kernel(const double* __restrict__ flr, const double* __restrict__ cosm,
-                              const double2* __restrict__ pinv, const double* __restrict__ kvec,
-                              const double* __restrict__ pp, double2* __restrict__ rhs, FluxBlocks fb, int nk,
-                              int nxi, int n_el, long long N, double q_diff, double mpc, int b0,
-                              const int* __restrict__ mask) {
-  extern __shared__ double sm[];  // [2][nxi]
-  const int b = b0 + blockIdx.x;
+// Cosine transform of f_L, f_R to the xi cells (verteilung.m:158-161): one warp per
+// (xi cell, problem), lanes over k.  fxi[b][2][nxi].
+__global__ void __launch_bounds__(256) inflow_xi_kernel(const double* __restrict__ flr, const double* __restrict__ cosm,
+                                                        const double* __restrict__ kvec, double* __restrict__ fxi,
+                                                        int nk, int nxi, int b0, const int* __restrict__ mask) {
+  const int b = b0 + blockIdx.y;
   if (mask && !mask[b]) return;
+  const int s = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (s >= nxi) return;
   const double* fL = flr + (long long)b * 2 * nk;
   const double* fR = fL + nk;
-  const double dk = fabs(kvec[1] - kvec[0]);
-  for (int s = threadIdx.x; s < nxi; s += blockDim.x) {
-    double al = 0, ar = 0;
-    const double* c = cosm + (long long)s * nk;
-    for (int j = 0; j < nk; ++j) {
-      al += c[j] * fL[j];
-      ar += c[j] * fR[j];
-    }
-    sm[s] = al * dk / 2 / kPi;
-    sm[nxi + s] = ar * dk / 2 / kPi;
+  const double* c = cosm + (long long)s * nk;
+  double al = 0, ar = 0;
+  for (int j = lane; j < nk; j += 32) {
+    al += c[j] * fL[j];
+    ar += c[j] * fR[j];
   }
-  __syncthreads();
+  for (int o = 16; o > 0; o >>= 1) {
+    al += __shfl_xor_sync(0xffffffffu, al, o);
+    ar += __shfl_xor_sync(0xffffffffu, ar, o);
+  }
+  if (lane == 0) {
+    const double dk = fabs(kvec[1] - kvec[0]);
+    fxi[((long long)b * 2 + 0) * nxi + s] = al * dk / 2 / kPi;
+    fxi[((long long)b * 2 + 1) * nxi + s] = ar * dk / 2 / kPi;
+  }
+}
+
+// Least-squares projection on Phi (pseudo-inverse, verteilung.m:167-168) and the contact
+// inflow blocks of the rhs (get_Diff.m:77-83): one warp per (k, problem), lanes over xi.
+__global__ void __launch_bounds__(256) inflow_kernel(const double* __restrict__ fxi, const double2* __restrict__ pinv,
+                                                     const double* __restrict__ kvec, const double* __restrict__ pp,
+                                                     double2* __restrict__ rhs, FluxBlocks fb, int nk, int nxi,
+                                                     int n_el, long long N, double q_diff, double mpc, int b0,
+                                                     const int* __restrict__ mask) {
+  const int b = b0 + blockIdx.y;
+  if (mask && !mask[b]) return;
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (j >= nk) return;
+  const double* sL = fxi + (long long)b * 2 * nxi;
+  const double* sR = sL + nxi;
+  const double2* pr = pinv + (long long)j * nxi;
+  double2 zl = make_double2(0, 0), zr = make_double2(0, 0);
+  for (int s = lane; s < nxi; s += 32) {
+    const double2 w = pr[s];
+    zl.x += w.x * sL[s];
+    zl.y += w.y * sL[s];
+    zr.x += w.x * sR[s];
+    zr.y += w.y * sR[s];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    zl.x += __shfl_xor_sync(0xffffffffu, zl.x, o);
+    zl.y += __shfl_xor_sync(0xffffffffu, zl.y, o);
+    zr.x += __shfl_xor_sync(0xffffffffu, zr.x, o);
+    zr.y += __shfl_xor_sync(0xffffffffu, zr.y, o);
+  }
   const int nK = fb.nK;
-  const double detJ = pp[b * kPP + PP_LX] / n_el / 2;
-  double2* rfirst = rhs + (long long)b * N;
-  double2* rlast = rfirst + (long long)(n_el - 1) * nK * nk;
-  for (int j = threadIdx.x; j < nk; j += blockDim.x) {
-    double2 zl = make_double2(0, 0), zr = make_double2(0, 0);
-    const double2* pr = pinv + (long long)j * nxi;
-    for (int s = 0; s < nxi; ++s) {
-      const double2 w = pr[s];
-      zl.x += w.x * sm[s];
-      zl.y += w.y * sm[s];
-      zr.x += w.x * sm[nxi + s];
-      zr.y += w.y * sm[nxi + s];
-    }
+  if (lane < nK) {
+    const int a = lane;
+    const double detJ = pp[b * kPP + PP_LX] / n_el / 2;
+    double2* rfirst = rhs + (long long)b * N;
+    double2* rlast = rfirst + (long long)(n_el - 1) * nK * nk;
     const double k = kvec[j], ak = fabs(k);
     const double fl = k > 0 ? 1.0 : 0.0, fr = k < 0 ? 1.0 : 0.0;
-    for (int a = 0; a < nK; ++a) {
-      const double q1 = fb.invM[a * nK + 0] / detJ, q2 = fb.invM[a * nK + nK - 1] / detJ;
-      rfirst[(long long)a * nk + j] =
-          make_double2(mpc * (q_diff * (q1 * (fl * (ak * zl.x)))), mpc * (q_diff * (q1 * (fl * (ak * zl.y)))));
-      rlast[(long long)a * nk + j] =
-          make_double2(mpc * (q_diff * (q2 * (fr * (ak * zr.x)))), mpc * (q_diff * (q2 * (fr * (ak * zr.y)))));
-    }
+    const double q1 = fb.invM[a * nK + 0] / detJ, q2 = fb.invM[a * nK + nK - 1] / detJ;
+    rfirst[(long long)a * nk + j] =
+        make_double2(mpc * (q_diff * (q1 * (fl * (ak * zl.x)))), mpc * (q_diff * (q1 * (fl * (ak * zl.y)))));
+    rlast[(long long)a * nk + j] =
+        make_double2(mpc * (q_diff * (q2 * (fr * (ak * zr.x)))), mpc * (q_diff * (q2 * (fr * (ak * zr.y)))));
   }
 }
 
@@ -141,11 +196,21 @@ __device__ double v_lookup(double x, const double* __restrict__ xg, const double
                            double vmin) {
   if (x < 0) return vg[0];
   if (x >= lx) return vmin;
-  int lo = 0, hi = nx - 1;
+  int hi = nx - 1;
   if (x >= xg[hi]) return vg[hi];
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (xg[mid] <= x) lo = mid; else hi = mid;
+  // the interval [xg[lo], xg[lo+1]) holding x: guessed for a uniform grid, corrected by a few
+  // steps; a binary search when the grid is far from uniform
+  int lo = (int)((x - xg[0]) / (xg[hi] - xg[0]) * (nx - 1));
+  lo = max(0, min(nx - 2, lo));
+  int steps = 0;
+  while (steps < 4 && lo > 0 && xg[lo] > x) { --lo; ++steps; }
+  while (steps < 4 && lo < nx - 2 && xg[lo + 1] <= x) { ++lo; ++steps; }
+  if (xg[lo] > x || xg[lo + 1] <= x) {
+    lo = 0;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (xg[mid] <= x) lo = mid; else hi = mid;
+    }
   }
   const double slope = (vg[lo + 1] - vg[lo]) / (xg[lo + 1] - xg[lo]);
   return slope * (x - xg[lo]) + vg[lo];
@@ -176,13 +241,18 @@ __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ 
     dv[q] = v_lookup(x + 0.5 * xi, xg, vg, nx, lx, vmin) - v_lookup(x - 0.5 * xi, xg, vg, nx, lx, vmin);
   }
   double* be = beta + ((long long)b * n_el + e) * NK * NK * ne;
+  // the weights are symmetric in (a, c) (symmetric inverse mass, products W(q,a) W(q,c)):
+  // one contraction per unordered pair
 #pragma unroll
-  for (int ac = 0; ac < NK * NK; ++ac) {
-    double acc = 0.0;
+  for (int a = 0; a < NK; ++a)
 #pragma unroll
-    for (int q = 0; q < kNqx; ++q) acc += kap[ac * kNqx + q] * dv[q];
-    be[(long long)ac * ne + s] = acc * scale;
-  }
+    for (int c = a; c < NK; ++c) {
+      double acc = 0.0;
+#pragma unroll
+      for (int q = 0; q < kNqx; ++q) acc += kap[(a * NK + c) * kNqx + q] * dv[q];
+      be[(long long)(a * NK + c) * ne + s] = acc * scale;
+      if (c != a) be[(long long)(c * NK + a) * ne + s] = acc * scale;
+    }
 }
 
 }  // namespace
@@ -191,12 +261,14 @@ cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask)
   const int nb = b1 - b0;
   if (nb <= 0) return cudaSuccess;
   const Shape& s = P.s;
-  cudaEvent_t ev = prof_begin(P, PROF_OTHER, 4);
+  cudaEvent_t ev = prof_begin(P, PROF_OTHER, 5);
   minmax_kernel<<<nb, 256, 0, P.stream>>>(P.pot_v, P.pp, P.nx, b0, mask);
-  fermi_kernel<<<dim3(s.nk, nb), 128, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr, P.nx, s.nk, b0, mask);
-  inflow_kernel<<<nb, 256, sizeof(double) * 2 * s.nxi, P.stream>>>(P.flr, P.cosm, P.pinv, P.kvec, P.pp, P.rhs, P.fb,
-                                                                   s.nk, s.nxi, s.n_el, P.N, s.q_diff, s.mpc, b0,
-                                                                   mask);
+  fermi_kernel<<<dim3((s.nk + kFermiJ - 1) / kFermiJ, nb), 256, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr, P.nx,
+                                                                              s.nk, b0, mask);
+  inflow_xi_kernel<<<dim3((s.nxi + 7) / 8, nb), 256, 0, P.stream>>>(P.flr, P.cosm, P.kvec, P.fxi, s.nk, s.nxi, b0,
+                                                                     mask);
+  inflow_kernel<<<dim3((s.nk + 7) / 8, nb), 256, 0, P.stream>>>(P.fxi, P.pinv, P.kvec, P.pp, P.rhs, P.fb, s.nk,
+                                                                  s.nxi, s.n_el, P.N, s.q_diff, s.mpc, b0, mask);
   const int ne = s.nxi + 1;
   dim3 g((unsigned)(((long long)s.n_el * ne + 127) / 128), nb);
   const double scale = s.delta_xi / 4 * s.mpc;

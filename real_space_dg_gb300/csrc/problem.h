@@ -176,6 +176,7 @@ struct Problem {
   double* qd = nullptr;          // [B]
   double* pp = nullptr;          // [B][kPP] per-problem scalars
   double* flr = nullptr;         // [B][2][nk] contact occupations f_L, f_R
+  double* fxi = nullptr;         // [B][2][nxi] their cosine transforms to the xi cells
   double* beta = nullptr;        // [B][n_el][nK*nK][nxi+1] real potential weights
   double* xq = nullptr;          // [B][n_el*10] quadrature x [m]
   double* pot_x = nullptr;       // [B][nx] material grid [m]
