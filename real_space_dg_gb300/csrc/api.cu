@@ -44,7 +44,7 @@ void free_all(wg::Problem& P) {
     }
   wg::gummel_free(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.kmap_a, P.kmap_s, P.cosm, P.pinv, P.pp, P.flr, P.fxi, P.qd, P.beta, P.xq, P.pot_x,
-                  P.pot_v, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
+                  P.pot_v, P.vslope, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
                   P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.md_count, P.gs_count, P.kused, P.any_active};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -231,6 +231,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
     P.fb.K5[i] = s.K5[i];
     P.fb.invM[i] = s.invM[i];
   }
+  wg::finish_flux_blocks(P.fb);
   double bytes = 0;
   cudaError_t ce = cudaSuccess;
   auto A = [&](cudaError_t r) {
@@ -263,6 +264,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.xq, (size_t)batch * s.n_el * wg::kNqx, bytes));
   A(dalloc(&P.pot_x, (size_t)batch * P.nx, bytes));
   A(dalloc(&P.pot_v, (size_t)batch * P.nx, bytes));
+  A(dalloc(&P.vslope, (size_t)batch * P.nx, bytes));
   A(dalloc(&P.m_nodes, (size_t)batch * s.n_el * nK, bytes));
   A(dalloc(&P.rhs, BN, bytes));
   A(dalloc(&P.x, BN, bytes));

@@ -805,8 +805,11 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
   if (rc) return rc;
   std::vector<int> iters(B, 0), cycles(B, 0), refs(B, 0);
   std::vector<double> res = initial, itgt(B), ones(B, 1.0);
-  auto prec = [&](const float2* r, long long stride) { return launch_precondition_mixed(P, r, stride, M.z, M.zb16); };
-  auto apply = [&]() { return launch_apply_mixed(P, M.z, M.zb16, M.w); };
+  // the inner Arnoldi steps skip problems that have converged in this cycle (P.active)
+  auto prec = [&](const float2* r, long long stride) {
+    return launch_precondition_mixed(P, r, stride, M.z, M.zb16, P.active);
+  };
+  auto apply = [&]() { return launch_apply_mixed(P, M.z, M.zb16, M.w, P.active); };
   for (int ref = 0; ref < max_ref; ++ref) {
     bool any = false;
     for (int b = 0; b < B; ++b) any |= (res[b] > tgt[b]) && std::isfinite(res[b]);

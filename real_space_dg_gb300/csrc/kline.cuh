@@ -33,12 +33,12 @@ template <int NK, typename R>
 __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
     const typename Cplx<R>::type* __restrict__ r, const R* __restrict__ kvec, const R* __restrict__ dinv,
     const R* __restrict__ hvec, const R* __restrict__ qd, R* __restrict__ mapA, typename Cplx<R>::type* __restrict__ mapS,
-    int n_el, int nk, long long N, long long r_stride, int L, int nchunk) {
+    int n_el, int nk, long long N, long long r_stride, int L, int nchunk, const int* __restrict__ mask) {
   using T = typename Cplx<R>::type;
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int c = blockIdx.y * kChunksPerBlock + threadIdx.y;
   const int b = blockIdx.z;
-  if (j >= nk || c >= nchunk) return;
+  if (j >= nk || c >= nchunk || (mask && !mask[b])) return;
   const long long bj = (long long)b * nk + j;
   const bool fwd = kvec[j] > R(0);
   const int st = fwd ? NK - 1 : 0;
@@ -78,12 +78,12 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
     __nv_bfloat162* __restrict__ zb, const R* __restrict__ kvec, const R* __restrict__ dinv,
     const R* __restrict__ hvec, const R* __restrict__ qd, const R* __restrict__ mapA,
     const typename Cplx<R>::type* __restrict__ mapS, int n_el, int nk, long long N, long long r_stride, int L,
-    int nchunk) {
+    int nchunk, const int* __restrict__ mask) {
   using T = typename Cplx<R>::type;
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int c = blockIdx.y * kChunksPerBlock + threadIdx.y;
   const int b = blockIdx.z;
-  if (j >= nk || c >= nchunk) return;
+  if (j >= nk || c >= nchunk || (mask && !mask[b])) return;
   const long long bj = (long long)b * nk + j;
   const bool fwd = kvec[j] > R(0);
   const int st = fwd ? NK - 1 : 0;

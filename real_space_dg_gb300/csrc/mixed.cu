@@ -119,12 +119,12 @@ cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* 
 
 template <int EPI>
 cudaError_t launch_gemm(const CUtensorMap& a, const CUtensorMap& b, float* D, int M, long long Ncol, int K, int* err,
-                        cudaStream_t st) {
+                        cudaStream_t st, const int* mask = nullptr, int cols_per_problem = 1) {
   static const cudaError_t attr = cudaFuncSetAttribute(tc::gemm_bf16_kernel<EPI>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
   if (attr != cudaSuccess) return attr;
   dim3 grid((M + tc::BM - 1) / tc::BM, (unsigned)((Ncol + tc::BN - 1) / tc::BN));
-  tc::gemm_bf16_kernel<EPI><<<grid, 128, tc::SMEM_BYTES, st>>>(a, b, D, M, Ncol, K, err);
+  tc::gemm_bf16_kernel<EPI><<<grid, 128, tc::SMEM_BYTES, st>>>(a, b, D, M, Ncol, K, err, mask, cols_per_problem);
   return cudaGetLastError();
 }
 
@@ -142,14 +142,15 @@ __global__ void __launch_bounds__(kFlux32Threads) flux32_kernel(const float2* __
                                                                 bf162* __restrict__ xb,
                                                                 const float* __restrict__ kvec,
                                                                 const float* __restrict__ qd, FluxBlocks32 fb,
-                                                                int n_el, int nk, float shift) {
+                                                                int n_el, int nk, float shift,
+                                                                const int* __restrict__ mask) {
   const int be = blockIdx.x;
   const int j = 2 * (blockIdx.y * kFlux32Threads + threadIdx.x);
   if (j >= nk) return;
   const int b = be / n_el;
+  if (mask && !mask[b]) return;
   const int e = be - b * n_el;
   const float k0 = kvec[j], k1 = kvec[j + 1];
-  const float ak0 = fabsf(k0), ak1 = fabsf(k1);
   const float s = qd[b];
   const long long base = (long long)be * NK * nk + j;
   float4 xv[NK];
@@ -165,44 +166,41 @@ __global__ void __launch_bounds__(kFlux32Threads) flux32_kernel(const float2* __
       *reinterpret_cast<uint2*>(xb + base + (long long)c * nk) = pk;
     }
   }
+  // k K1 + |k| K2 = k (K1 +- K2); the upwind neighbour enters through one node
+  const bool pos = k0 > 0;
   float4 acc[NK];
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
-      const float m0 = k0 * fb.K1[a * NK + c] + ak0 * fb.K2[a * NK + c];
-      const float m1 = k1 * fb.K1[a * NK + c] + ak1 * fb.K2[a * NK + c];
-      v.x = fmaf(m0, xv[c].x, v.x);
-      v.y = fmaf(m0, xv[c].y, v.y);
-      v.z = fmaf(m1, xv[c].z, v.z);
-      v.w = fmaf(m1, xv[c].w, v.w);
+      const float m = pos ? fb.Kp[a * NK + c] : fb.Km[a * NK + c];
+      v.x = fmaf(m, xv[c].x, v.x);
+      v.y = fmaf(m, xv[c].y, v.y);
+      v.z = fmaf(m, xv[c].z, v.z);
+      v.w = fmaf(m, xv[c].w, v.w);
     }
     acc[a] = v;
   }
-  const bool left = k0 > 0 && e > 0, right = k0 < 0 && e < n_el - 1;
+  const bool left = pos && e > 0, right = k0 < 0 && e < n_el - 1;
   if (left || right) {
-    const float* K = left ? fb.K3 : fb.K5;
-    const float w0 = left ? k0 + ak0 : k0 - ak0, w1 = left ? k1 + ak1 : k1 - ak1;
-    const long long nb = base + (left ? -(long long)NK * nk : (long long)NK * nk);
+    const float4 xp = *reinterpret_cast<const float4*>(
+        x + base + (left ? -(long long)NK * nk + (long long)(NK - 1) * nk : (long long)NK * nk));
 #pragma unroll
-    for (int c = 0; c < NK; ++c) {
-      const float4 xp = *reinterpret_cast<const float4*>(x + nb + (long long)c * nk);
-#pragma unroll
-      for (int a = 0; a < NK; ++a) {
-        const float m0 = w0 * K[a * NK + c], m1 = w1 * K[a * NK + c];
-        acc[a].x = fmaf(m0, xp.x, acc[a].x);
-        acc[a].y = fmaf(m0, xp.y, acc[a].y);
-        acc[a].z = fmaf(m1, xp.z, acc[a].z);
-        acc[a].w = fmaf(m1, xp.w, acc[a].w);
-      }
+    for (int a = 0; a < NK; ++a) {
+      const float m = left ? fb.K3c[a] : fb.K5c[a];
+      acc[a].x = fmaf(m, xp.x, acc[a].x);
+      acc[a].y = fmaf(m, xp.y, acc[a].y);
+      acc[a].z = fmaf(m, xp.z, acc[a].z);
+      acc[a].w = fmaf(m, xp.w, acc[a].w);
     }
   }
+  const float s0 = s * k0, s1 = s * k1;
 #pragma unroll
   for (int a = 0; a < NK; ++a)
     *reinterpret_cast<float4*>(y + base + (long long)a * nk) =
-        make_float4(fmaf(s, acc[a].x, shift * xv[a].x), fmaf(s, acc[a].y, shift * xv[a].y),
-                    fmaf(s, acc[a].z, shift * xv[a].z), fmaf(s, acc[a].w, shift * xv[a].w));
+        make_float4(fmaf(s0, acc[a].x, shift * xv[a].x), fmaf(s0, acc[a].y, shift * xv[a].y),
+                    fmaf(s1, acc[a].z, shift * xv[a].z), fmaf(s1, acc[a].w, shift * xv[a].w));
 }
 
 // ---------------------------------------------------------------------------
@@ -213,10 +211,11 @@ template <int NK>
 __global__ void __launch_bounds__(kFlux32Threads) stencil32_kernel(const float2* __restrict__ xh,
                                                                    bf162* __restrict__ yh,
                                                                    const float* __restrict__ betar,
-                                                                   const float* __restrict__ betai, int nxi) {
+                                                                   const float* __restrict__ betai, int nxi,
+                                                                   int n_el, const int* __restrict__ mask) {
   const int be = blockIdx.x;
   const int s = blockIdx.y * kFlux32Threads + threadIdx.x;
-  if (s >= nxi) return;
+  if (s >= nxi || (mask && !mask[be / n_el])) return;
   const int ne = nxi + 1;
   const float2* X = xh + (long long)be * NK * nxi;
   float2 sm[NK], sp[NK];
@@ -262,7 +261,7 @@ __global__ void d2f_kernel(const double* __restrict__ x, float* __restrict__ y, 
 }
 
 template <int NK>
-cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2* y) {
+cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2* y, const int* mask) {
   MixedBuffers& M = P.mx;
   if (xb && xb != M.xin16 && xb != M.zb16) return cudaErrorInvalidValue;
   const Shape& s = P.s;
@@ -275,28 +274,30 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
   cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, (xb_out ? 20.0 : 16.0) * BN);
   const dim3 fgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nk / 2 + kFlux32Threads - 1) / kFlux32Threads));
   flux32_kernel<NK><<<fgrid, kFlux32Threads, 0, P.stream>>>(x, y, xb_out, M.kvec, M.qd, M.fb, s.n_el, s.nk,
-                                                            (float)P.shift);
+                                                            (float)P.shift, mask);
   prof_end(P, PROF_FLUX, ev);
   ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * BN + 8.0 * nxi * ncols, gemm_flops);
   // GEMM 1 reads its B operand through the tensor map of whichever bf16 buffer holds x
+  const int cpp = s.n_el * s.nK;   // GEMM columns per problem
   cudaError_t e = launch_gemm<0>(M.tmA1, xb == M.xin16 ? M.tmB1 : M.tmB1z, reinterpret_cast<float*>(M.xh), 2 * s.nxi,
-                                 P.ncols, 2 * s.nk, M.err, P.stream);
+                                 P.ncols, 2 * s.nk, M.err, P.stream, mask, cpp);
   prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
   ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * NK * NK * (nxi + 1));
   const dim3 sgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nxi + kFlux32Threads - 1) / kFlux32Threads));
   stencil32_kernel<NK><<<sgrid, kFlux32Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16,
-                                                               M.beta, M.betai, s.nxi);
+                                                               M.beta, M.betai, s.nxi, s.n_el, mask);
   prof_end(P, PROF_STENCIL, ev);
   ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops);
-  e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream);
+  e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream, mask,
+                     cpp);
   prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 
 template <int NK>
-cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb) {
+cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb, const int* mask) {
   const int L = kline::chunk_len(P.s.n_el), nc = kline::chunk_count(P.s.n_el);
   const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
   const dim3 block(32, kline::kChunksPerBlock);
@@ -304,10 +305,10 @@ cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, fl
   float2* ms = static_cast<float2*>(P.kmap_s);
   cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, (zb ? 28.0 : 24.0) * P.N * P.batch);
   kline::kline_maps_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, ma, ms,
-                                                                    P.s.n_el, P.s.nk, P.N, r_stride, L, nc);
+                                                                    P.s.n_el, P.s.nk, P.N, r_stride, L, nc, mask);
   kline::kline_apply_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h,
                                                                      P.mx.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
-                                                                     r_stride, L, nc);
+                                                                     r_stride, L, nc, mask);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
@@ -361,12 +362,18 @@ int mixed_alloc(Problem& P) {
     P.err = std::string("mixed-precision buffers: ") + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
   }
+  if (!P.fb.single) {
+    P.err = "the mixed form needs the single-node upwind coupling of the DG flux blocks";
+    return WG_ERR_ARG;
+  }
   M.fb.nK = s.nK;
   for (int i = 0; i < s.nK * s.nK; ++i) {
-    M.fb.K1[i] = (float)s.K1[i];
-    M.fb.K2[i] = (float)s.K2[i];
-    M.fb.K3[i] = (float)s.K3[i];
-    M.fb.K5[i] = (float)s.K5[i];
+    M.fb.Kp[i] = (float)P.fb.Kp[i];
+    M.fb.Km[i] = (float)P.fb.Km[i];
+  }
+  for (int a = 0; a < s.nK; ++a) {
+    M.fb.K3c[a] = (float)P.fb.K3c[a];
+    M.fb.K5c[a] = (float)P.fb.K5c[a];
   }
   P.device_bytes += bytes;
   cudaMemsetAsync(M.err, 0, sizeof(int), P.stream);
@@ -493,11 +500,11 @@ cudaError_t mixed_sync_weights(Problem& P) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y) {
+cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y, const int* mask) {
   switch (P.s.nK) {
-    case 2: return apply_mixed_nk<2>(P, x, xb, y);
-    case 3: return apply_mixed_nk<3>(P, x, xb, y);
-    default: return apply_mixed_nk<4>(P, x, xb, y);
+    case 2: return apply_mixed_nk<2>(P, x, xb, y, mask);
+    case 3: return apply_mixed_nk<3>(P, x, xb, y, mask);
+    default: return apply_mixed_nk<4>(P, x, xb, y, mask);
   }
 }
 
@@ -524,11 +531,11 @@ cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y) {
 }
 
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
-                                      __nv_bfloat162* zb) {
+                                      __nv_bfloat162* zb, const int* mask) {
   switch (P.s.nK) {
-    case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb);
-    case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb);
-    default: return precond_mixed_nk<4>(P, r, r_stride, z, zb);
+    case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb, mask);
+    case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb, mask);
+    default: return precond_mixed_nk<4>(P, r, r_stride, z, zb, mask);
   }
 }
 

@@ -52,6 +52,43 @@ __global__ void __launch_bounds__(kFluxThreads) flux_kernel(const double2* __res
 #pragma unroll
   for (int c = 0; c < NK; ++c) xv[c] = xe[(long long)c * nk];
   double2 acc[NK];
+  if (fb.single) {
+    // k K1 + |k| K2 = k (K1 +- K2); the upwind neighbour enters through one node:
+    // y = qd k [ Kpm x_e + K3c x_{e-1}[nK-1]  (k > 0)  or  K5c x_{e+1}[0]  (k < 0) ] + shift x
+    const bool pos = k > 0;
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NK; ++c) {
+        const double m = pos ? fb.Kp[a * NK + c] : fb.Km[a * NK + c];
+        v.x += m * xv[c].x;
+        v.y += m * xv[c].y;
+      }
+      acc[a] = v;
+    }
+    if (k > 0 && e > 0) {
+      const double2 xn = xe[-(long long)NK * nk + (long long)(NK - 1) * nk];
+#pragma unroll
+      for (int a = 0; a < NK; ++a) {
+        acc[a].x += fb.K3c[a] * xn.x;
+        acc[a].y += fb.K3c[a] * xn.y;
+      }
+    } else if (k < 0 && e < n_el - 1) {
+      const double2 xn = xe[(long long)NK * nk];
+#pragma unroll
+      for (int a = 0; a < NK; ++a) {
+        acc[a].x += fb.K5c[a] * xn.x;
+        acc[a].y += fb.K5c[a] * xn.y;
+      }
+    }
+    const double sk = s * k;
+    double2* ye = y + (long long)be * NK * nk + j;
+#pragma unroll
+    for (int a = 0; a < NK; ++a)
+      ye[(long long)a * nk] = make_double2(sk * acc[a].x + shift * xv[a].x, sk * acc[a].y + shift * xv[a].y);
+    return;
+  }
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
     double2 v = make_double2(0.0, 0.0);
@@ -320,10 +357,11 @@ cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2
   double2* ms = static_cast<double2*>(P.kmap_s);
   cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, 48.0 * P.N * P.batch);
   kline::kline_maps_kernel<NK, double><<<grid, block, 0, P.stream>>>(r, P.kvec, P.pre_dinv, P.pre_h, P.qd, ma, ms,
-                                                                     P.s.n_el, P.s.nk, P.N, r_stride, L, nc);
+                                                                     P.s.n_el, P.s.nk, P.N, r_stride, L, nc,
+                                                                     nullptr);
   kline::kline_apply_kernel<NK, double><<<grid, block, 0, P.stream>>>(r, z, nullptr, P.kvec, P.pre_dinv, P.pre_h,
                                                                       P.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
-                                                                      r_stride, L, nc);
+                                                                      r_stride, L, nc, nullptr);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
@@ -539,6 +577,7 @@ int apply_noalloc(const wg_operator_view& v, const double* x, double* y, void* s
     fb.K3[i] = v.K3[i];
     fb.K5[i] = v.K5[i];
   }
+  finish_flux_blocks(fb);
   const double2* xx = reinterpret_cast<const double2*>(x);
   double2* yy = reinterpret_cast<double2*>(y);
   double2* xh = scratch;

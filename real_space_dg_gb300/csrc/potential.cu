@@ -41,15 +41,19 @@ __device__ double block_reduce(double v, bool is_max) {
   return v;  // valid in warp 0
 }
 
-__global__ void minmax_kernel(const double* __restrict__ pot_v, double* __restrict__ pp, int nx, int b0,
+// min V, max V and the slopes (V[i+1] - V[i]) / (x[i+1] - x[i]) of the linear interpolation.
+__global__ void minmax_kernel(const double* __restrict__ pot_v, const double* __restrict__ pot_x,
+                              double* __restrict__ vslope, double* __restrict__ pp, int nx, int b0,
                               const int* __restrict__ mask) {
   const int b = b0 + blockIdx.x;
   if (mask && !mask[b]) return;
   const double* v = pot_v + (long long)b * nx;
+  const double* x = pot_x + (long long)b * nx;
   double mx = -INFINITY, mn = INFINITY;
   for (int i = threadIdx.x; i < nx; i += blockDim.x) {
     mx = fmax(mx, v[i]);
     mn = fmin(mn, v[i]);
+    if (i < nx - 1) vslope[(long long)b * nx + i] = (v[i + 1] - v[i]) / (x[i + 1] - x[i]);
   }
   mx = block_reduce(mx, true);
   const double mneg = block_reduce(-mn, true);
@@ -192,15 +196,16 @@ __global__ void __launch_bounds__(256) inflow_kernel(const double* __restrict__ 
   }
 }
 
-__device__ double v_lookup(double x, const double* __restrict__ xg, const double* __restrict__ vg, int nx, double lx,
-                           double vmin) {
+// V(x) by linear interpolation on the material grid, V(x < 0) = V(0), V(x >= Lx) = min V
+// (V_transient.m:1-8).  The interval is guessed from a uniform grid (inv_span =
+// (nx-1) / (x[nx-1] - x[0])) and corrected by comparisons; slopes are precomputed.
+__device__ double v_lookup(double x, const double* __restrict__ xg, const double* __restrict__ vg,
+                           const double* __restrict__ slope, int nx, double lx, double vmin, double inv_span) {
   if (x < 0) return vg[0];
   if (x >= lx) return vmin;
   int hi = nx - 1;
   if (x >= xg[hi]) return vg[hi];
-  // the interval [xg[lo], xg[lo+1]) holding x: guessed for a uniform grid, corrected by a few
-  // steps; a binary search when the grid is far from uniform
-  int lo = (int)((x - xg[0]) / (xg[hi] - xg[0]) * (nx - 1));
+  int lo = (int)((x - xg[0]) * inv_span);
   lo = max(0, min(nx - 2, lo));
   int steps = 0;
   while (steps < 4 && lo > 0 && xg[lo] > x) { --lo; ++steps; }
@@ -212,16 +217,16 @@ __device__ double v_lookup(double x, const double* __restrict__ xg, const double
       if (xg[mid] <= x) lo = mid; else hi = mid;
     }
   }
-  const double slope = (vg[lo + 1] - vg[lo]) / (xg[lo + 1] - xg[lo]);
-  return slope * (x - xg[lo]) + vg[lo];
+  return slope[lo] * (x - xg[lo]) + vg[lo];
 }
 
 // beta[b][e][ac][s] = (dxi/4) mpc sum_q kap[ac][q] (V(x_q + xi_s/2) - V(x_q - xi_s/2))
 template <int NK>
 __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ xq, const double* __restrict__ xi_edge,
                           const double* __restrict__ kap, const double* __restrict__ pot_x,
-                          const double* __restrict__ pot_v, const double* __restrict__ pp, int nx, int n_el, int nxi,
-                          double scale, int b0, const int* __restrict__ mask) {
+                          const double* __restrict__ pot_v, const double* __restrict__ vslope,
+                          const double* __restrict__ pp, int nx, int n_el, int nxi, double scale, int b0,
+                          const int* __restrict__ mask) {
   if (mask && !mask[b0 + blockIdx.y]) return;
   const int ne = nxi + 1;
   const int b = b0 + blockIdx.y;
@@ -233,12 +238,15 @@ __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ 
   const double* xg = pot_x + (long long)b * nx;
   const double* vg = pot_v + (long long)b * nx;
   const double lx = pp[b * kPP + PP_LX], vmin = pp[b * kPP + PP_VMIN];
+  const double* sl = vslope + (long long)b * nx;
+  const double inv_span = (nx - 1) / (xg[nx - 1] - xg[0]);
   const double* xqb = xq + (long long)b * n_el * kNqx + e * kNqx;
   double dv[kNqx];
 #pragma unroll
   for (int q = 0; q < kNqx; ++q) {
     const double x = xqb[q];
-    dv[q] = v_lookup(x + 0.5 * xi, xg, vg, nx, lx, vmin) - v_lookup(x - 0.5 * xi, xg, vg, nx, lx, vmin);
+    dv[q] = v_lookup(x + 0.5 * xi, xg, vg, sl, nx, lx, vmin, inv_span) -
+            v_lookup(x - 0.5 * xi, xg, vg, sl, nx, lx, vmin, inv_span);
   }
   double* be = beta + ((long long)b * n_el + e) * NK * NK * ne;
   // the weights are symmetric in (a, c) (symmetric inverse mass, products W(q,a) W(q,c)):
@@ -262,7 +270,7 @@ cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask)
   if (nb <= 0) return cudaSuccess;
   const Shape& s = P.s;
   cudaEvent_t ev = prof_begin(P, PROF_OTHER, 5);
-  minmax_kernel<<<nb, 256, 0, P.stream>>>(P.pot_v, P.pp, P.nx, b0, mask);
+  minmax_kernel<<<nb, 256, 0, P.stream>>>(P.pot_v, P.pot_x, P.vslope, P.pp, P.nx, b0, mask);
   fermi_kernel<<<dim3((s.nk + kFermiJ - 1) / kFermiJ, nb), 256, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr, P.nx,
                                                                               s.nk, b0, mask);
   inflow_xi_kernel<<<dim3((s.nxi + 7) / 8, nb), 256, 0, P.stream>>>(P.flr, P.cosm, P.kvec, P.fxi, s.nk, s.nxi, b0,
@@ -273,12 +281,12 @@ cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask)
   dim3 g((unsigned)(((long long)s.n_el * ne + 127) / 128), nb);
   const double scale = s.delta_xi / 4 * s.mpc;
   switch (s.nK) {
-    case 2: vw_kernel<2><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.pp, P.nx,
-                                                  s.n_el, s.nxi, scale, b0, mask); break;
-    case 3: vw_kernel<3><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.pp, P.nx,
-                                                  s.n_el, s.nxi, scale, b0, mask); break;
-    default: vw_kernel<4><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.pp, P.nx,
-                                                   s.n_el, s.nxi, scale, b0, mask); break;
+    case 2: vw_kernel<2><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.vslope, P.pp,
+                                                  P.nx, s.n_el, s.nxi, scale, b0, mask); break;
+    case 3: vw_kernel<3><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.vslope, P.pp,
+                                                  P.nx, s.n_el, s.nxi, scale, b0, mask); break;
+    default: vw_kernel<4><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.vslope, P.pp,
+                                                   P.nx, s.n_el, s.nxi, scale, b0, mask); break;
   }
   prof_end(P, PROF_OTHER, ev);
   return cudaGetLastError();

@@ -15,21 +15,44 @@ namespace wg {
 // Small constant blocks passed by value to kernels (fits the parameter space).
 struct FluxBlocks {
   int nK;
+  int single;        // 1: K3 couples only the last node of the left element, K5 only the first of the right
   double K1[kMaxLocal * kMaxLocal];
   double K2[kMaxLocal * kMaxLocal];
   double K3[kMaxLocal * kMaxLocal];
   double K5[kMaxLocal * kMaxLocal];
   double invM[kMaxLocal * kMaxLocal];
+  double Kp[kMaxLocal * kMaxLocal];   // K1 + K2: k K1 + |k| K2 = k Kp for k > 0
+  double Km[kMaxLocal * kMaxLocal];   // K1 - K2: ... = k Km for k < 0
+  double K3c[kMaxLocal];              // 2 K3[a][nK-1]: (k + |k|) K3 x_left = k K3c x_left[nK-1]
+  double K5c[kMaxLocal];              // 2 K5[a][0]:    (k - |k|) K5 x_right = k K5c x_right[0]
 };
 
 // FP32 copies of the flux blocks for the mixed form (no FP64 instruction per element).
 struct FluxBlocks32 {
   int nK;
-  float K1[kMaxLocal * kMaxLocal];
-  float K2[kMaxLocal * kMaxLocal];
-  float K3[kMaxLocal * kMaxLocal];
-  float K5[kMaxLocal * kMaxLocal];
+  float Kp[kMaxLocal * kMaxLocal];
+  float Km[kMaxLocal * kMaxLocal];
+  float K3c[kMaxLocal];
+  float K5c[kMaxLocal];
 };
+
+// Fill the derived blocks (Kp, Km, K3c, K5c, single) from K1, K2, K3, K5.
+inline void finish_flux_blocks(FluxBlocks& fb) {
+  const int n = fb.nK;
+  bool single = true;
+  for (int a = 0; a < n; ++a)
+    for (int c = 0; c < n; ++c) {
+      fb.Kp[a * n + c] = fb.K1[a * n + c] + fb.K2[a * n + c];
+      fb.Km[a * n + c] = fb.K1[a * n + c] - fb.K2[a * n + c];
+      if (c != n - 1 && fb.K3[a * n + c] != 0.0) single = false;
+      if (c != 0 && fb.K5[a * n + c] != 0.0) single = false;
+    }
+  for (int a = 0; a < n; ++a) {
+    fb.K3c[a] = 2.0 * fb.K3[a * n + n - 1];
+    fb.K5c[a] = 2.0 * fb.K5[a * n + 0];
+  }
+  fb.single = single ? 1 : 0;
+}
 
 // Per-problem scalar parameters on the device: pp[b * kPP + PP_*].
 constexpr int kPP = 10;
@@ -181,6 +204,7 @@ struct Problem {
   double* xq = nullptr;          // [B][n_el*10] quadrature x [m]
   double* pot_x = nullptr;       // [B][nx] material grid [m]
   double* pot_v = nullptr;       // [B][nx] potential [eV]
+  double* vslope = nullptr;      // [B][nx] slopes of its linear interpolation
   double* m_nodes = nullptr;     // [B][n_el*nK] masses at DG nodes [kg]
   int nx = 0;
   // vectors
@@ -262,9 +286,11 @@ int mixed_alloc(Problem& P);
 int ozaki_alloc(Problem& P);
 void mixed_free(Problem& P);
 cudaError_t mixed_sync_weights(Problem& P);
-cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y);
+// mask (device, optional): problems b with mask[b] == 0 are skipped (their output is left as is).
+cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y,
+                               const int* mask = nullptr);
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
-                                      __nv_bfloat162* zb);
+                                      __nv_bfloat162* zb, const int* mask = nullptr);
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);
 cudaError_t apply_mixed_repeat(Problem& P, const double2* x, int n_apply);
 int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err);

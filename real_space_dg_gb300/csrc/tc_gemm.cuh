@@ -133,7 +133,15 @@ template <int EPI>
 __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA,
                                                            const __grid_constant__ CUtensorMap tmB,
                                                            float* __restrict__ D, int M, long long Ncol, int K,
-                                                           int* __restrict__ err) {
+                                                           int* __restrict__ err, const int* __restrict__ mask,
+                                                           int cols_per_problem) {
+  // a column tile whose problems are all inactive (mask[b] == 0) has nothing to compute
+  if (mask) {
+    const long long c0 = (long long)blockIdx.y * BN, c1 = min(Ncol, c0 + BN) - 1;
+    bool any = false;
+    for (long long b = c0 / cols_per_problem; b <= c1 / cols_per_problem; ++b) any |= mask[b] != 0;
+    if (!any) return;
+  }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
