@@ -437,8 +437,10 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
 
 template <typename T>
 __global__ void __launch_bounds__(256) norm_partial_kernel(const T* __restrict__ v, double* __restrict__ out,
-                                                           long long N, int nchunk) {
+                                                           long long N, int nchunk,
+                                                           const int* __restrict__ mask = nullptr) {
   const int b = blockIdx.y, c = blockIdx.x;
+  if (mask && !mask[b]) return;
   const T* vv = v + (long long)b * N;
   typename AccFor<T>::type a;
   for (long long n = (long long)c * 256 + threadIdx.x; n < N; n += (long long)nchunk * 256) a.add_norm(vv[n]);
@@ -450,8 +452,9 @@ __global__ void __launch_bounds__(256) norm_partial_kernel(const T* __restrict__
 __global__ void norm_reduce_kernel(const double* __restrict__ partial, double* __restrict__ out,
                                    double2* __restrict__ H, const int* __restrict__ active, int nchunk, int k,
                                    int pstride, int m, double* __restrict__ inv64 = nullptr,
-                                   float* __restrict__ inv32 = nullptr) {
+                                   float* __restrict__ inv32 = nullptr, const int* __restrict__ mask = nullptr) {
   const int b = blockIdx.x;
+  if (mask && !mask[b]) return;   // problems outside the mask keep their norm
   double acc = 0;
   for (int c = threadIdx.x; c < nchunk; c += 32) acc += partial[b * nchunk + c];
   acc = warp_sum(acc);
@@ -497,20 +500,23 @@ __global__ void __launch_bounds__(256) scale_inv_kernel(const T* __restrict__ sr
 }
 
 __global__ void __launch_bounds__(256) residual_kernel(const double2* __restrict__ rhs, const double2* __restrict__ ax,
-                                                       double2* __restrict__ r, long long total) {
+                                                       double2* __restrict__ r, long long total, long long N,
+                                                       const int* __restrict__ mask) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= total) return;
+  if (t >= total || (mask && !mask[t / N])) return;
   const double2 a = rhs[t], b = ax[t];
   r[t] = make_double2(a.x - b.x, a.y - b.y);
 }
 
-// x += s[b] * z  (s = nullptr: s = 1)
+// x += s[b] * z  (s = nullptr: s = 1; problems with mask[b] == 0 are left as they are)
 template <typename T>
 __global__ void __launch_bounds__(256) axpy_kernel(double2* __restrict__ x, const T* __restrict__ z,
-                                                   const double* __restrict__ s, long long N, int batch) {
+                                                   const double* __restrict__ s, long long N, int batch,
+                                                   const int* __restrict__ mask = nullptr) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= N * batch) return;
   const int b = (int)(t / N);
+  if (mask && !mask[b]) return;
   const double f = s ? s[b] : 1.0;
   const double2 a = x[t], v = ld2(z[t]);
   x[t] = make_double2(a.x + f * v.x, a.y + f * v.y);
@@ -669,15 +675,19 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
 }
 
 // r = rhs - A x ; nrm[b] = |r_b|  (FP64)
-int true_residual(Problem& P) {
+// r = b - A x and |r| (FP64; the mixed form's transforms on the tensor cores).  mask
+// (device, optional): only problems with mask[b] != 0 are evaluated, the others keep
+// their previous r and |r| (their x has not changed since).
+int true_residual(Problem& P, const int* mask = nullptr) {
   const long long tot = P.N * P.batch;
   P.prof.launches[PROF_OTHER] += 3;
-  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w));
+  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w, mask));
   else WG_CK(launch_apply(P, P.x, P.w));
-  residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot);
-  norm_partial_kernel<double2><<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk);
+  residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot, P.N, mask);
+  norm_partial_kernel<double2><<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk,
+                                                                             mask);
   norm_reduce_kernel<<<P.batch, 32, 0, P.stream>>>(P.nrm_partial, P.nrm, nullptr, P.active, P.nchunk, 0, 0, 0,
-                                                   P.inv64);
+                                                   P.inv64, nullptr, mask);
   WG_CK(cudaGetLastError());
   return WG_OK;
 }
@@ -695,7 +705,15 @@ int solve_begin(Problem& P, double tol, bool warm, std::vector<double>& bnorm, s
   WG_CK(cudaStreamSynchronize(P.stream));
   tgt.resize(B);
   for (int b = 0; b < B; ++b) tgt[b] = (P.tol_pp.empty() ? tol : P.tol_pp[b]) * bnorm[b];
-  int rc = true_residual(P);
+  // problems frozen by an unreachable tolerance keep their residual
+  const int* mask = nullptr;
+  if (!P.tol_pp.empty() && P.precision == WG_PREC_MIXED) {
+    P.h_res_mask.assign(B, 1);
+    for (int b = 0; b < B; ++b) P.h_res_mask[b] = P.tol_pp[b] < 1e299 ? 1 : 0;
+    WG_CK(cudaMemcpyAsync(P.res_mask, P.h_res_mask.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
+    mask = P.res_mask;
+  }
+  int rc = true_residual(P, mask);
   if (rc) return rc;
   res.resize(B);
   WG_CK(cudaMemcpyAsync(res.data(), P.nrm, sizeof(double) * B, cudaMemcpyDeviceToHost, P.stream));
@@ -815,11 +833,14 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     for (int b = 0; b < B; ++b) any |= (res[b] > tgt[b]) && std::isfinite(res[b]);
     if (!any) break;
     // inner target on the normalised residual: reach the outer target, never below inner_tol
+    P.h_res_mask.assign(B, 0);
     for (int b = 0; b < B; ++b) {
       const bool act = (res[b] > tgt[b]) && std::isfinite(res[b]);
       itgt[b] = act ? std::max(P.inner_tol, 0.5 * tgt[b] / res[b]) : INFINITY;
+      P.h_res_mask[b] = act ? 1 : 0;
     }
     WG_CK(cudaMemcpyAsync(P.target, itgt.data(), sizeof(double) * B, cudaMemcpyHostToDevice, P.stream));
+    WG_CK(cudaMemcpyAsync(P.res_mask, P.h_res_mask.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
     // keep |r| for the update, start the inner cycle from the unit-norm residual
     WG_CK(cudaMemcpyAsync(P.nrm_keep, P.nrm, sizeof(double) * B, cudaMemcpyDeviceToDevice, P.stream));
     WG_CK(cudaMemcpyAsync(P.nrm, ones.data(), sizeof(double) * B, cudaMemcpyHostToDevice, P.stream));
@@ -840,10 +861,12 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     P.prof.launches[PROF_OTHER] += 3;
     backsolve_kernel<<<B, 32, 0, P.stream>>>(P.H, P.g, P.ycoef, M.y, P.kused, ps, mm, B);
     combine_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(M.V, M.y, P.kused, M.w, N, mp1, mm, B);
-    WG_CK(launch_precondition_mixed(P, M.w, N, M.d, nullptr));
-    axpy_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, M.d, P.nrm_keep, N, B);
+    WG_CK(launch_precondition_mixed(P, M.w, N, M.d, nullptr, P.res_mask));
+    axpy_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, M.d, P.nrm_keep, N, B, P.res_mask);
     WG_CK(cudaGetLastError());
-    rc = true_residual(P);
+    // problems that did not move this refinement keep r and |r|; the others are re-evaluated
+    WG_CK(cudaMemcpyAsync(P.nrm, P.nrm_keep, sizeof(double) * B, cudaMemcpyDeviceToDevice, P.stream));
+    rc = true_residual(P, P.res_mask);
     if (rc) return rc;
     int herr = 0;
     WG_CK(cudaMemcpyAsync(&herr, M.err, sizeof(int), cudaMemcpyDeviceToHost, P.stream));

@@ -108,12 +108,14 @@ unsigned slice_blocks(long long ncol) {
 
 template <int EPI>
 cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* ea, const int* eb, double* C, int M,
-                         long long Ncol, int K, int* err, cudaStream_t st) {
+                         long long Ncol, int K, int* err, cudaStream_t st, const int* mask = nullptr,
+                         int cols_per_problem = 1) {
   static const cudaError_t attr = cudaFuncSetAttribute(oz::gemm_ozaki_kernel<EPI>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, oz::SMEM_BYTES);
   if (attr != cudaSuccess) return attr;
   dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
-  oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err);
+  oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err, mask,
+                                                                 cols_per_problem);
   return cudaGetLastError();
 }
 
@@ -213,17 +215,27 @@ __global__ void __launch_bounds__(kFlux32Threads) stencil32_kernel(const float2*
                                                                    const float* __restrict__ betar,
                                                                    const float* __restrict__ betai, int nxi,
                                                                    int n_el, const int* __restrict__ mask) {
+  // xi cells along the lanes: the s-1 / s+1 neighbours of x and the s+1 weights come from
+  // the adjacent lanes (shuffles); the warp's edge lanes load theirs
   const int be = blockIdx.x;
+  if (mask && !mask[be / n_el]) return;
   const int s = blockIdx.y * kFlux32Threads + threadIdx.x;
-  if (s >= nxi || (mask && !mask[be / n_el])) return;
+  const int lane = threadIdx.x & 31;
+  const bool valid = s < nxi;
   const int ne = nxi + 1;
   const float2* X = xh + (long long)be * NK * nxi;
   float2 sm[NK], sp[NK];
 #pragma unroll
   for (int c = 0; c < NK; ++c) {
-    const float2 x0 = X[c * nxi + s];
-    const float2 xm = s > 0 ? X[c * nxi + s - 1] : make_float2(0.f, 0.f);
-    const float2 xp = s < nxi - 1 ? X[c * nxi + s + 1] : make_float2(0.f, 0.f);
+    const float2 x0 = valid ? X[c * nxi + s] : make_float2(0.f, 0.f);
+    float2 xm, xp;
+    xm.x = __shfl_up_sync(0xffffffffu, x0.x, 1);
+    xm.y = __shfl_up_sync(0xffffffffu, x0.y, 1);
+    xp.x = __shfl_down_sync(0xffffffffu, x0.x, 1);
+    xp.y = __shfl_down_sync(0xffffffffu, x0.y, 1);
+    if (lane == 0) xm = (valid && s > 0) ? X[c * nxi + s - 1] : make_float2(0.f, 0.f);
+    if (lane == 31 || s == nxi - 1) xp = (valid && s < nxi - 1) ? X[c * nxi + s + 1] : make_float2(0.f, 0.f);
+    if (s == 0) xm = make_float2(0.f, 0.f);
     sm[c] = make_float2(x0.x + xm.x, x0.y + xm.y);
     sp[c] = make_float2(x0.x + xp.x, x0.y + xp.y);
   }
@@ -235,12 +247,16 @@ __global__ void __launch_bounds__(kFlux32Threads) stencil32_kernel(const float2*
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
       const int ac = a * NK + c;
-      const float b0r = br[ac * ne + s], b0i = betai[ac * ne + s];
-      const float b1r = br[ac * ne + s + 1], b1i = betai[ac * ne + s + 1];
+      const float b0r = valid ? br[ac * ne + s] : 0.f, b0i = valid ? betai[ac * ne + s] : 0.f;
+      float b1r = __shfl_down_sync(0xffffffffu, b0r, 1), b1i = __shfl_down_sync(0xffffffffu, b0i, 1);
+      if (lane == 31 || s == nxi - 1) {
+        b1r = valid ? br[ac * ne + s + 1] : 0.f;
+        b1i = valid ? betai[ac * ne + s + 1] : 0.f;
+      }
       vx += b0r * sm[c].x - b0i * sm[c].y + b1r * sp[c].x - b1i * sp[c].y;
       vy += b0r * sm[c].y + b0i * sm[c].x + b1r * sp[c].y + b1i * sp[c].x;
     }
-    Y[a * nxi + s] = __floats2bfloat162_rn(vx, vy);
+    if (valid) Y[a * nxi + s] = __floats2bfloat162_rn(vx, vy);
   }
 }
 
@@ -455,6 +471,9 @@ int ozaki_alloc(Problem& P) {
     C2(cudaMalloc(&M.ea2, sizeof(int) * e2.size()));
     C2(cudaMalloc(&M.ob, sizeof(bf16) * (size_t)oz::S * P.ncols * kmax));
     C2(cudaMalloc(&M.eb, sizeof(int) * (size_t)P.ncols));
+    // columns of masked problems are not re-sliced: keep them finite from the start
+    C2(cudaMemset(M.ob, 0, sizeof(bf16) * (size_t)oz::S * P.ncols * kmax));
+    C2(cudaMemset(M.eb, 0, sizeof(int) * (size_t)P.ncols));
     C2(cudaMemcpy(M.oa1, d1.data(), sizeof(bf16) * d1.size(), cudaMemcpyHostToDevice));
     C2(cudaMemcpy(M.oa2, d2.data(), sizeof(bf16) * d2.size(), cudaMemcpyHostToDevice));
     C2(cudaMemcpy(M.ea1, e1.data(), sizeof(int) * e1.size(), cudaMemcpyHostToDevice));
@@ -591,30 +610,30 @@ int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int 
 
 // FP64 operator apply of the mixed form's outer residual: flux and xi stencil in
 // FP64, both transforms as digit-sliced FP64 GEMMs on the tensor cores.
-cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y) {
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask) {
   MixedBuffers& M = P.mx;
   if (!M.ozaki) return launch_apply(P, x, y);
   const Shape& s = P.s;
   const int K1 = 2 * s.nk, K2 = 2 * s.nxi;
   const double ncols = (double)P.ncols;
-  cudaError_t e = launch_flux_f64(P, x, y);
+  const int cpp = (int)(P.ncols / P.batch);   // columns (element, node) of one problem
+  cudaError_t e = launch_flux_f64(P, x, y, mask);
   if (e != cudaSuccess) return e;
   cudaEvent_t ev = prof_begin(P, PROF_GEMM_F64, 2, 8.0 * P.N * P.batch + 16.0 * s.nxi * ncols,
                               8.0 * s.nxi * s.nk * ncols);
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
-      reinterpret_cast<const double*>(x), K1, P.ncols,
-                                                                    M.ob, M.eb);
+      reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
-                      P.stream);
+                      P.stream, mask, cpp);
   prof_end(P, PROF_GEMM_F64, ev);
   if (e != cudaSuccess) return e;
-  e = launch_stencil_f64(P, P.xh, P.yh);
+  e = launch_stencil_f64(P, P.xh, P.yh, mask);
   if (e != cudaSuccess) return e;
   ev = prof_begin(P, PROF_GEMM_F64, 2, 16.0 * s.nxi * ncols + 16.0 * P.N * P.batch, 8.0 * s.nxi * s.nk * ncols);
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
-      reinterpret_cast<const double*>(P.yh), K2,
-                                                                    P.ncols, M.ob, M.eb);
-  e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream);
+      reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp);
+  e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream,
+                      mask, cpp);
   prof_end(P, PROF_GEMM_F64, ev);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();

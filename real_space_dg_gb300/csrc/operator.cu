@@ -38,11 +38,12 @@ template <int NK>
 __global__ void __launch_bounds__(kFluxThreads) flux_kernel(const double2* __restrict__ x, double2* __restrict__ y,
                                                             const double* __restrict__ kvec,
                                                             const double* __restrict__ qd, FluxBlocks fb, int n_el,
-                                                            int nk, double shift) {
+                                                            int nk, double shift, const int* __restrict__ mask) {
   const int be = blockIdx.x;                  // b * n_el + e
   const int j = blockIdx.y * kFluxThreads + threadIdx.x;
   if (j >= nk) return;
   const int b = be / n_el;
+  if (mask && !mask[b]) return;
   const int e = be - b * n_el;
   const double k = kvec[j];
   const double ak = fabs(k);
@@ -237,11 +238,12 @@ template <int NK>
 __global__ void __launch_bounds__(kFluxThreads) stencil_kernel(const double2* __restrict__ xh,
                                                                double2* __restrict__ yh,
                                                                const double* __restrict__ betar,
-                                                               const double* __restrict__ betai, int nxi) {
+                                                               const double* __restrict__ betai, int nxi,
+                                                               int n_el, const int* __restrict__ mask) {
   // grid (batch * n_el, ceil(nxi / 128)): one block row per element, one thread per xi cell
   const int be = blockIdx.x;
   const int s = blockIdx.y * kFluxThreads + threadIdx.x;
-  if (s >= nxi) return;
+  if (s >= nxi || (mask && !mask[be / n_el])) return;
   const int ne = nxi + 1;
   const double2* X = xh + (long long)be * NK * nxi;
   double2 sm[NK], sp[NK];
@@ -315,16 +317,16 @@ __global__ void observables_kernel(const double2* __restrict__ rho, const double
 
 template <int NK>
 void flux_launch(const double2* x, double2* y, const double* kvec, const double* qd, const FluxBlocks& fb, int batch,
-                 int n_el, int nk, double shift, cudaStream_t st) {
+                 int n_el, int nk, double shift, cudaStream_t st, const int* mask = nullptr) {
   const dim3 grid((unsigned)(batch * n_el), (unsigned)((nk + kFluxThreads - 1) / kFluxThreads));
-  flux_kernel<NK><<<grid, kFluxThreads, 0, st>>>(x, y, kvec, qd, fb, n_el, nk, shift);
+  flux_kernel<NK><<<grid, kFluxThreads, 0, st>>>(x, y, kvec, qd, fb, n_el, nk, shift, mask);
 }
 
 template <int NK>
 void stencil_launch(const double2* xh, double2* yh, const double* beta, const double* betai, int batch, int n_el,
-                    int nxi, cudaStream_t st) {
+                    int nxi, cudaStream_t st, const int* mask = nullptr) {
   const dim3 grid((unsigned)(batch * n_el), (unsigned)((nxi + kFluxThreads - 1) / kFluxThreads));
-  stencil_kernel<NK><<<grid, kFluxThreads, 0, st>>>(xh, yh, beta, betai, nxi);
+  stencil_kernel<NK><<<grid, kFluxThreads, 0, st>>>(xh, yh, beta, betai, nxi, n_el, mask);
 }
 
 template <int NK>
@@ -439,25 +441,25 @@ cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
   }
 }
 
-cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y) {
+cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int* mask) {
   cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * P.N * P.batch);
   switch (P.s.nK) {
-    case 2: flux_launch<2>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream); break;
-    case 3: flux_launch<3>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream); break;
-    default: flux_launch<4>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream); break;
+    case 2: flux_launch<2>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
+    case 3: flux_launch<3>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
+    default: flux_launch<4>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
   }
   prof_end(P, PROF_FLUX, ev);
   return cudaGetLastError();
 }
 
-cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh) {
+cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const int* mask) {
   const int nK = P.s.nK;
   cudaEvent_t ev = prof_begin(P, PROF_STENCIL, 1,
                               32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1));
   switch (nK) {
-    case 2: stencil_launch<2>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream); break;
-    case 3: stencil_launch<3>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream); break;
-    default: stencil_launch<4>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream); break;
+    case 2: stencil_launch<2>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
+    case 3: stencil_launch<3>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
+    default: stencil_launch<4>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
   }
   prof_end(P, PROF_STENCIL, ev);
   return cudaGetLastError();

@@ -85,7 +85,15 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
                                                             const __grid_constant__ CUtensorMap tmB,
                                                             const int* __restrict__ ea, const int* __restrict__ eb,
                                                             double* __restrict__ C, int M, long long Ncol, int K,
-                                                            int* __restrict__ err) {
+                                                            int* __restrict__ err, const int* __restrict__ mask,
+                                                            int cols_per_problem) {
+  // a column tile whose problems are all inactive (mask[b] == 0) has nothing to compute
+  if (mask) {
+    const long long c0 = (long long)blockIdx.y * BN, c1 = min(Ncol, c0 + BN) - 1;
+    bool any = false;
+    for (long long b = c0 / cols_per_problem; b <= c1 / cols_per_problem; ++b) any |= mask[b] != 0;
+    if (!any) return;
+  }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   // stage s: [S][BM][BK] bf16 A slices, then [S][BN][BK] bf16 B slices
@@ -219,10 +227,12 @@ __device__ __forceinline__ long long round_scaled(long long bits, int m, bool no
 __global__ void __launch_bounds__(32 * kSliceColsPerBlock) slice_columns_kernel(const double* __restrict__ X, int K,
                                                                                long long Ncol,
                                                                                __nv_bfloat16* __restrict__ slices,
-                                                                               int* __restrict__ e_out) {
+                                                                               int* __restrict__ e_out,
+                                                                               const int* __restrict__ mask = nullptr,
+                                                                               int cols_per_problem = 1) {
   const int lane = threadIdx.x & 31;
   const long long c = (long long)blockIdx.x * kSliceColsPerBlock + (threadIdx.x >> 5);
-  if (c >= Ncol) return;
+  if (c >= Ncol || (mask && !mask[c / cols_per_problem])) return;
   const double2* x = reinterpret_cast<const double2*>(X + c * (long long)K);
   const int K2 = K / 2;
   unsigned long long mx = 0;

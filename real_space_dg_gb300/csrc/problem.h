@@ -232,6 +232,8 @@ struct Problem {
   double* target = nullptr;      // [B] absolute residual targets
   int* active = nullptr;         // [B] 1 while iterating in this cycle
   int* reorth = nullptr;         // [B] 1 where the current Arnoldi step re-orthogonalises
+  int* res_mask = nullptr;       // [B] problems whose true residual is evaluated
+  std::vector<int> h_res_mask;
   int* md_count = nullptr;       // [B] last-block tickets of the multi-dot (zero between launches)
   int* gs_count = nullptr;       // [B] last-block tickets of the Gram-Schmidt update
   int* kused = nullptr;          // [B] iterations used in this cycle
@@ -264,10 +266,10 @@ cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride
 int set_kline_factors(Problem& P);
 // Device bytes of a handle before allocation (the admission estimate of wg_problem_create).
 double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc = false);
-cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y);
-cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh);
+cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int* mask = nullptr);
+cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const int* mask = nullptr);
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
-cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y);
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask = nullptr);
 int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err);
 // Rebuild potential-dependent data (Vw weights, contact inflow rhs) of problems [b0, b1).
 // mask (device, optional): problems b with mask[b] == 0 are left untouched.
