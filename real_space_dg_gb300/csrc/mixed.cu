@@ -206,60 +206,128 @@ __global__ void __launch_bounds__(kFlux32Threads) flux32_kernel(const float2* __
 }
 
 // ---------------------------------------------------------------------------
-// FP32 xi stencil, output as the BF16 B operand of GEMM 2.
-// Grid (batch * n_el, ceil(nxi / 128)): one block row per element.
+// FP32 xi stencil, output as the BF16 B operand of GEMM 2:
+//   y_a(s) = sum_c beta_ac(s) (x_c(s) + x_c(s-1)) + beta_ac(s+1) (x_c(s) + x_c(s+1)),
+// beta = betar (symmetric in a, c: pairs a <= c stored) + i betai.  Each thread owns
+// four consecutive xi cells (16-byte loads of x, of the weights and of the BF16
+// output); the cells s0-1 and s0+4 come from the neighbouring lanes.  Grid
+// (batch * n_el, ceil(nxi / 256)) of 64 threads; nxi % 4 == 0 (mixed form).
 // ---------------------------------------------------------------------------
+constexpr int kSt4Threads = 64;
+
+__host__ __device__ constexpr int pair_count(int nk) { return nk * (nk + 1) / 2; }
+// index of the pair (a, c), a <= c, in the order (0,0) (0,1) .. (0,nK-1) (1,1) ..
+__host__ __device__ constexpr int pair_index(int nk, int a, int c) { return a * nk - a * (a - 1) / 2 + (c - a); }
+
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+
 template <int NK>
-__global__ void __launch_bounds__(kFlux32Threads) stencil32_kernel(const float2* __restrict__ xh,
-                                                                   bf162* __restrict__ yh,
-                                                                   const float* __restrict__ betar,
-                                                                   const float* __restrict__ betai, int nxi,
-                                                                   int n_el, const int* __restrict__ mask) {
-  // xi cells along the lanes: the s-1 / s+1 neighbours of x and the s+1 weights come from
-  // the adjacent lanes (shuffles); the warp's edge lanes load theirs
+__global__ void __launch_bounds__(kSt4Threads) stencil32_kernel(const float2* __restrict__ xh,
+                                                                bf162* __restrict__ yh,
+                                                                const float* __restrict__ betar,
+                                                                const float* __restrict__ betai, int nxi, int ne4,
+                                                                int n_el, const int* __restrict__ mask) {
   const int be = blockIdx.x;
   if (mask && !mask[be / n_el]) return;
-  const int s = blockIdx.y * kFlux32Threads + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  const bool valid = s < nxi;
-  const int ne = nxi + 1;
+  const int s0 = (blockIdx.y * kSt4Threads + threadIdx.x) * 4;
+  const bool valid = s0 < nxi;             // nxi % 4 == 0: then all four cells are
+  const bool edge = lane == 31 || s0 + 4 >= nxi;   // s0 + 4 not held by the next lane
   const float2* X = xh + (long long)be * NK * nxi;
-  float2 sm[NK], sp[NK];
+  const float2 z2 = make_float2(0.f, 0.f);
+  float2 sm[NK][4], sp[NK][4];
 #pragma unroll
   for (int c = 0; c < NK; ++c) {
-    const float2 x0 = valid ? X[c * nxi + s] : make_float2(0.f, 0.f);
+    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+    if (valid) {
+      lo = *reinterpret_cast<const float4*>(X + c * nxi + s0);
+      hi = *reinterpret_cast<const float4*>(X + c * nxi + s0 + 2);
+    }
+    const float2 x0 = make_float2(lo.x, lo.y), x1 = make_float2(lo.z, lo.w);
+    const float2 x2 = make_float2(hi.x, hi.y), x3 = make_float2(hi.z, hi.w);
     float2 xm, xp;
-    xm.x = __shfl_up_sync(0xffffffffu, x0.x, 1);
-    xm.y = __shfl_up_sync(0xffffffffu, x0.y, 1);
+    xm.x = __shfl_up_sync(0xffffffffu, x3.x, 1);
+    xm.y = __shfl_up_sync(0xffffffffu, x3.y, 1);
     xp.x = __shfl_down_sync(0xffffffffu, x0.x, 1);
     xp.y = __shfl_down_sync(0xffffffffu, x0.y, 1);
-    if (lane == 0) xm = (valid && s > 0) ? X[c * nxi + s - 1] : make_float2(0.f, 0.f);
-    if (lane == 31 || s == nxi - 1) xp = (valid && s < nxi - 1) ? X[c * nxi + s + 1] : make_float2(0.f, 0.f);
-    if (s == 0) xm = make_float2(0.f, 0.f);
-    sm[c] = make_float2(x0.x + xm.x, x0.y + xm.y);
-    sp[c] = make_float2(x0.x + xp.x, x0.y + xp.y);
+    if (lane == 0) xm = (valid && s0 > 0) ? X[c * nxi + s0 - 1] : z2;
+    if (edge) xp = (valid && s0 + 4 < nxi) ? X[c * nxi + s0 + 4] : z2;
+    if (s0 == 0) xm = z2;
+    sm[c][0] = f2add(x0, xm);
+    sm[c][1] = f2add(x1, x0);
+    sm[c][2] = f2add(x2, x1);
+    sm[c][3] = f2add(x3, x2);
+    sp[c][0] = f2add(x0, x1);
+    sp[c][1] = f2add(x1, x2);
+    sp[c][2] = f2add(x2, x3);
+    sp[c][3] = f2add(x3, xp);
   }
-  const float* br = betar + (long long)be * NK * NK * ne;
+  const float* br = betar + (long long)be * pair_count(NK) * ne4;
   bf162* Y = yh + (long long)be * NK * nxi;
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
-    float vx = 0.f, vy = 0.f;
+    float vx[4] = {0.f, 0.f, 0.f, 0.f}, vy[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
-      const int ac = a * NK + c;
-      const float b0r = valid ? br[ac * ne + s] : 0.f, b0i = valid ? betai[ac * ne + s] : 0.f;
-      float b1r = __shfl_down_sync(0xffffffffu, b0r, 1), b1i = __shfl_down_sync(0xffffffffu, b0i, 1);
-      if (lane == 31 || s == nxi - 1) {
-        b1r = valid ? br[ac * ne + s + 1] : 0.f;
-        b1i = valid ? betai[ac * ne + s + 1] : 0.f;
+      const float* rr = br + pair_index(NK, a < c ? a : c, a < c ? c : a) * ne4;
+      const float* ri = betai + (a * NK + c) * ne4;
+      float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), i0 = r0;
+      if (valid) {
+        r0 = *reinterpret_cast<const float4*>(rr + s0);
+        i0 = *reinterpret_cast<const float4*>(ri + s0);
       }
-      vx += b0r * sm[c].x - b0i * sm[c].y + b1r * sp[c].x - b1i * sp[c].y;
-      vy += b0r * sm[c].y + b0i * sm[c].x + b1r * sp[c].y + b1i * sp[c].x;
+      // the weight of edge s0 + 4: the next lane's first, loaded at the warp's edge
+      float r4 = __shfl_down_sync(0xffffffffu, r0.x, 1), i4 = __shfl_down_sync(0xffffffffu, i0.x, 1);
+      if (edge) {
+        r4 = valid ? rr[s0 + 4] : 0.f;
+        i4 = valid ? ri[s0 + 4] : 0.f;
+      }
+      const float b0r[4] = {r0.x, r0.y, r0.z, r0.w}, b0i[4] = {i0.x, i0.y, i0.z, i0.w};
+      const float b1r[4] = {r0.y, r0.z, r0.w, r4}, b1i[4] = {i0.y, i0.z, i0.w, i4};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        vx[j] += b0r[j] * sm[c][j].x - b0i[j] * sm[c][j].y + b1r[j] * sp[c][j].x - b1i[j] * sp[c][j].y;
+        vy[j] += b0r[j] * sm[c][j].y + b0i[j] * sm[c][j].x + b1r[j] * sp[c][j].y + b1i[j] * sp[c][j].x;
+      }
     }
-    if (valid) Y[a * nxi + s] = __floats2bfloat162_rn(vx, vy);
+    if (valid) {
+      uint4 o;
+      bf162 t0 = __floats2bfloat162_rn(vx[0], vy[0]), t1 = __floats2bfloat162_rn(vx[1], vy[1]);
+      bf162 t2 = __floats2bfloat162_rn(vx[2], vy[2]), t3 = __floats2bfloat162_rn(vx[3], vy[3]);
+      o.x = *reinterpret_cast<uint32_t*>(&t0);
+      o.y = *reinterpret_cast<uint32_t*>(&t1);
+      o.z = *reinterpret_cast<uint32_t*>(&t2);
+      o.w = *reinterpret_cast<uint32_t*>(&t3);
+      *reinterpret_cast<uint4*>(Y + a * nxi + s0) = o;
+    }
   }
 }
 
+// FP32 packed copies of the potential weights: out[r][p][s] = beta[r][a*nK+c][s] for the
+// pairs p = (a <= c) (npair = nK(nK+1)/2; npair = nK*nK with all = true copies every
+// (a, c)), rows padded from ne to ne4 with zeros.
+__global__ void pack_weights_kernel(const double* __restrict__ beta, float* __restrict__ out, long long nrows,
+                                    int nk, int npair, bool all, int ne, int ne4) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nrows * npair * ne4) return;
+  const int s = (int)(t % ne4);
+  const long long rp = t / ne4;
+  const int p = (int)(rp % npair);
+  const long long r = rp / npair;
+  int a = 0, c = p;
+  if (all) {
+    a = p / nk;
+    c = p % nk;
+  } else {
+    int rem = p;
+    while (rem >= nk - a) {
+      rem -= nk - a;
+      ++a;
+    }
+    c = a + rem;
+  }
+  out[t] = s < ne ? (float)beta[(r * nk * nk + a * nk + c) * ne + s] : 0.f;
+}
 
 __global__ void c2f_kernel(const double2* __restrict__ x, float2* __restrict__ y, long long n) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -299,10 +367,10 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
                                  P.ncols, 2 * s.nk, M.err, P.stream, mask, cpp);
   prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
-  ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * NK * NK * (nxi + 1));
-  const dim3 sgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nxi + kFlux32Threads - 1) / kFlux32Threads));
-  stencil32_kernel<NK><<<sgrid, kFlux32Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16,
-                                                               M.beta, M.betai, s.nxi, s.n_el, mask);
+  ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * pair_count(NK) * M.ne4);
+  const dim3 sgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nxi + 4 * kSt4Threads - 1) / (4 * kSt4Threads)));
+  stencil32_kernel<NK><<<sgrid, kSt4Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16, M.beta,
+                                                            M.betai, s.nxi, M.ne4, s.n_el, mask);
   prof_end(P, PROF_STENCIL, ev);
   ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops);
   e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream, mask,
@@ -341,7 +409,7 @@ double mixed_bytes(const Shape& s, int batch, int restart) {
   const double BN = (double)s.n_el * s.nK * s.nk * batch;
   const double ncols = (double)batch * s.n_el * s.nK;
   return 2.0 * 2 * (4.0 * s.nxi * s.nk) + 4.0 * BN + 8.0 * ncols * s.nxi + 4.0 * ncols * s.nxi +
-         8.0 * BN * (restart + 1 + 4) + 4.0 * batch * s.n_el * s.nK * s.nK * (s.nxi + 1);
+         8.0 * BN * (restart + 1 + 4) + 4.0 * batch * s.n_el * pair_count(s.nK) * ((s.nxi + 4) & ~3);
 }
 
 int mixed_alloc(Problem& P) {
@@ -364,8 +432,9 @@ int mixed_alloc(Problem& P) {
   alloc((void**)&M.z, sizeof(float2) * BN);
   alloc((void**)&M.r, sizeof(float2) * BN);
   alloc((void**)&M.d, sizeof(float2) * BN);
-  alloc((void**)&M.beta, sizeof(float) * (size_t)P.batch * s.n_el * s.nK * s.nK * (s.nxi + 1));
-  alloc((void**)&M.betai, sizeof(float) * (size_t)s.nK * s.nK * (s.nxi + 1));
+  M.ne4 = (s.nxi + 1 + 3) & ~3;
+  alloc((void**)&M.beta, sizeof(float) * (size_t)P.batch * s.n_el * pair_count(s.nK) * M.ne4);
+  alloc((void**)&M.betai, sizeof(float) * (size_t)s.nK * s.nK * M.ne4);
   alloc((void**)&M.err, sizeof(int));
   alloc((void**)&M.kvec, sizeof(float) * s.nk);
   alloc((void**)&M.qd, sizeof(float) * P.batch);
@@ -506,11 +575,14 @@ void mixed_free(Problem& P) {
 // FP32 copies of the potential weights after every potential update.
 cudaError_t mixed_sync_weights(Problem& P) {
   const Shape& s = P.s;
-  const long long nb = (long long)P.batch * s.n_el * s.nK * s.nK * (s.nxi + 1);
-  const long long ni = (long long)s.nK * s.nK * (s.nxi + 1);
+  const int ne = s.nxi + 1, ne4 = P.mx.ne4, np = pair_count(s.nK);
+  const long long rows = (long long)P.batch * s.n_el;
+  const long long nb = rows * np * ne4, ni = (long long)s.nK * s.nK * ne4;
   P.prof.launches[PROF_OTHER] += 6;
-  d2f_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, P.stream>>>(P.beta, P.mx.beta, nb);
-  d2f_kernel<<<(unsigned)((ni + 255) / 256), 256, 0, P.stream>>>(P.betai, P.mx.betai, ni);
+  pack_weights_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, P.stream>>>(P.beta, P.mx.beta, rows, s.nK, np, false,
+                                                                          ne, ne4);
+  pack_weights_kernel<<<(unsigned)((ni + 255) / 256), 256, 0, P.stream>>>(P.betai, P.mx.betai, 1, s.nK,
+                                                                          s.nK * s.nK, true, ne, ne4);
   d2f_kernel<<<1, 256, 0, P.stream>>>(P.qd, P.mx.qd, P.batch);
   d2f_kernel<<<(unsigned)((s.nk + 255) / 256), 256, 0, P.stream>>>(P.kvec, P.mx.kvec, s.nk);
   const long long nd = (long long)P.batch * s.nk * s.nK * s.nK, nh = (long long)P.batch * s.nk * s.nK;

@@ -9,11 +9,14 @@
 // 33^2 * 1024 < 2^21, so every product A^(p) B^(q) is EXACT in the FP32 tensor-core
 // accumulator.  Products of equal weight p+q (at most 8 of them) share one TMEM
 // accumulator (< 8 * 33^2 * 1024 < 2^24, still exact); the S groups of a 128 x 64 output tile use 8 x 64 = 512
-// TMEM columns.  Products of weight p+q >= S are dropped.  The epilogue adds the
-// groups in double-float FP32 arithmetic (exact power-of-two scalings, TwoSum),
-// converts once to FP64 and applies the row and column exponents with integer
-// arithmetic.  Error: a few 2^(-6S) (S = 8: ~1e-14) relative to |A| |B|,
-// unbiased (rounded split).
+// TMEM columns.  Products of weight p+q >= S are dropped.  The B digit slices lie
+// one after the other in shared memory, so the products of one A slice p with the
+// slices q = q0 .. q0+n-1 are ONE instruction of N = 64 n (n <= 4) whose accumulator
+// starts at group p+q0: 12 MMAs per k step instead of 36, and the A tile is read
+// from shared memory 12 times instead of 36.  The epilogue adds the groups as
+// integers in a 64-bit fixed point (unit 2^-50), rounds once to FP64 and applies
+// the row and column exponents, all with integer instructions.  Error: a few
+// 2^(-6S) (S = 8: ~1e-14) relative to |A| |B|, unbiased (rounded split).
 #pragma once
 #include "tc_gemm.cuh"
 
@@ -32,9 +35,10 @@ constexpr int STAGE = S * (A_SLICE + B_SLICE);   // 96 KiB
 constexpr int SMEM_BYTES = STAGES * STAGE + 1024 + 256;
 constexpr int MAX_K = 1024;       // exactness bound of the grouped accumulation (8 * 33^2 * K < 2^24)
 
-// Instruction descriptor: D f32, A/B bf16, K-major, M = 128, N = 64.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                            ((uint32_t)(BM >> 4) << 24);
+// Instruction descriptor: D f32, A/B bf16, K-major, M = 128, N = n (16 <= n <= 256, n % 16 == 0).
+constexpr uint32_t kIdescM128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BM >> 4) << 24);
+__device__ __forceinline__ uint32_t idesc_n(int n) { return kIdescM128 | ((uint32_t)(n >> 3) << 17); }
+constexpr int kSlicesPerMma = 256 / BN;   // B slices one instruction covers (N <= 256)
 
 // K-major operand tile with 64-byte rows and the 64-byte swizzle (8-row atoms of 512 bytes).
 __device__ __forceinline__ uint64_t sdesc_sw64(const void* p) {
@@ -57,26 +61,40 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
-// (hi, lo) += v exactly-rounded in double-float arithmetic.
-__device__ __forceinline__ void df_add(float& hi, float& lo, float v) {
-  const float s = __fadd_rn(hi, v);
-  const float bb = __fsub_rn(s, hi);
-  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb));
-  const float t = __fadd_rn(lo, e);
-  hi = __fadd_rn(s, t);
-  lo = __fsub_rn(t, __fsub_rn(hi, s));
+// Fixed-point unit of the epilogue: 2^-50.  Group g (weight 2^(-6(g+2))) enters
+// shifted left by 38 - 6g; the last group (g = 7) is rounded by 4 bits.  |sum| <
+// 33^2 * 1024 * 2^38 + ... < 2^59 for K <= 1024.
+constexpr int kFixBits = 50;
+__device__ __forceinline__ long long group_fixed(float v, int g) {
+  const long long t = (long long)__float2int_rn(v);   // exact: an integer below 2^24
+  const int sh = kFixBits - BETA * (g + 2);
+  return sh >= 0 ? (t << sh) : ((t + (1ll << (-sh - 1))) >> -sh);
 }
 
-// x * 2^e for a finite double by exponent arithmetic (no FP64 instruction); zero stays zero.
-__device__ __forceinline__ double scale_pow2(double x, int e) {
-  long long bits = __double_as_longlong(x);
-  const int ex = (int)((bits >> 52) & 0x7FF);
-  if (ex == 0) return 0.0;
-  const int ne = ex + e;
-  if (ne <= 0) return 0.0;
-  if (ne >= 0x7FF) return x > 0 ? INFINITY : -INFINITY;
-  bits = (bits & ~(0x7FFll << 52)) | ((long long)ne << 52);
-  return __longlong_as_double(bits);
+// a * 2^e as the nearest double (ties to even), integer instructions only; results
+// below the normal range flush to zero.
+__device__ __forceinline__ double fixed_to_double(long long a, int e) {
+  if (a == 0) return 0.0;
+  const unsigned long long sign = a < 0 ? 1ull << 63 : 0ull;
+  unsigned long long u = a < 0 ? 0ull - (unsigned long long)a : (unsigned long long)a;
+  int msb = 63 - __clzll((long long)u);
+  unsigned long long mant;
+  if (msb <= 52) {
+    mant = u << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    mant = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    if (mant >> 53) {
+      mant >>= 1;
+      ++msb;
+    }
+  }
+  const int ex = msb + e + 1023;
+  if (ex <= 0) return sign ? -0.0 : 0.0;
+  if (ex >= 0x7FF) return __longlong_as_double((long long)(sign | (0x7FFull << 52)));
+  return __longlong_as_double((long long)(sign | ((unsigned long long)ex << 52) | (mant & 0xFFFFFFFFFFFFFull)));
 }
 
 // EPI 0: C = A B.  EPI 1: C += A B.   ea[row], eb[col]: power-of-two exponents of A's rows and B's columns.
@@ -139,20 +157,20 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
       tc::fence_after();
       const uint8_t* sa = smem + st * STAGE;
       const uint8_t* sb = sa + S * A_SLICE;
-      for (int p = 0; p < S; ++p)
-        for (int q = 0; q + p < S; ++q) {        // weight p+q (0-based) <= S-1
-          const int g = p + q;
-          const uint32_t d = tmem + (uint32_t)(g * BN);
-          // group g is first reached with p == 0 (q == g): that product at the first k block
-          // and k step initialises the accumulator, every other one accumulates
-          const uint8_t* a = sa + p * A_SLICE;
-          const uint8_t* b = sb + q * B_SLICE;
 #pragma unroll
-          for (int kk = 0; kk < BK / 16; ++kk) {
+      for (int kk = 0; kk < BK / 16; ++kk)
+        for (int p = 0; p < S; ++p)
+          for (int q0 = 0; q0 + p < S; q0 += kSlicesPerMma) {   // weights p+q (0-based) <= S-1
+            const int n = min(kSlicesPerMma, S - p - q0);
+            // slices q0 .. q0+n-1 are consecutive 64-row blocks: their accumulators, groups
+            // p+q0 .. p+q0+n-1, are consecutive 64-column blocks of TMEM
+            const uint32_t d = tmem + (uint32_t)((p + q0) * BN);
+            // every group is first reached with p == 0: the p == 0 products of the first k block
+            // and k step initialise the accumulators, every other one accumulates
             const uint32_t acc = (kb > 0 || kk > 0 || p > 0) ? 1u : 0u;
-            tc::mma_bf16(d, sdesc_sw64(a + kk * 32), sdesc_sw64(b + kk * 32), kIdesc, acc);
+            tc::mma_bf16(d, sdesc_sw64(sa + p * A_SLICE + kk * 32), sdesc_sw64(sb + q0 * B_SLICE + kk * 32),
+                         idesc_n(n * BN), acc);
           }
-        }
       tc::mma_commit(&empty[st]);
     }
     tc::mma_commit(done);
@@ -165,18 +183,15 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
     const int er = row < M ? ea[row] : 0;
 #pragma unroll 1
     for (int cb = 0; cb < BN / 32; ++cb) {
-      float hi[32], lo[32];
+      long long fx[32];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) hi[i] = lo[i] = 0.f;
-      // smallest weights first
+      for (int i = 0; i < 32; ++i) fx[i] = 0;
 #pragma unroll 1
-      for (int g = NGROUP - 1; g >= 0; --g) {
+      for (int g = 0; g < NGROUP; ++g) {
         float v[32];
         tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * BN + cb * 32), v);
-        // weight 2^(-6 (g + 2)) with 1-based digits; exact power-of-two scaling
-        const float w = __int_as_float((127 - BETA * (g + 2)) << 23);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) df_add(hi[i], lo[i], v[i] * w);
+        for (int i = 0; i < 32; ++i) fx[i] += group_fixed(v[i], g);
       }
       if (row < M) {
         const long long c0 = n0 + cb * 32;
@@ -190,7 +205,7 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
           if (i < ncb) {
-            const double val = scale_pow2((double)hi[i] + (double)lo[i], er + eb[c0 + i]);
+            const double val = fixed_to_double(fx[i], er + eb[c0 + i] - kFixBits);
             dst[(long long)i * M] = EPI == 1 ? old[i] + val : val;
           }
         }

@@ -80,8 +80,12 @@ struct MixedBuffers {
   float2* z = nullptr;               // [B*N]
   float2* r = nullptr;               // [B*N] normalised outer residual
   float2* d = nullptr;               // [B*N] inner correction
-  float* beta = nullptr;             // fp32 copy of the potential weights
+  // fp32 copies of the potential weights, rows padded to ne4 = (nxi + 1) rounded up to 4:
+  // beta [B][n_el][nK(nK+1)/2][ne4] holds the pairs a <= c only (the weights are symmetric),
+  // betai [nK*nK][ne4] the CAP part
+  float* beta = nullptr;
   float* betai = nullptr;
+  int ne4 = 0;
   float* kvec = nullptr;             // [nk]
   float* qd = nullptr;               // [B]
   float* dinv = nullptr;             // [nk][nK*nK]
