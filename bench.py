@@ -143,6 +143,11 @@ def make_workload(batch):
 
 
 OZAKI_PRODUCTS = 36      # 8 digits per operand, products of weight < 8 (csrc/ozaki.cuh)
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one timed gemm_f64 event of the mixed form (digit
+# slicing + emulated GEMM; the mean of the C = AB and C += AB launches) per state column (element x node), from
+# one ncu capture at batch 8 (7,680 columns; profiles/gemm_ozaki_c2_batch8_mixed.md): slicing 39.6 MB, GEMMs
+# 75.9 and 109.2 MB.  The traffic grows with the columns, so a launch of the bench's batch scales by its columns.
+OZAKI_TRAFFIC_PER_COLUMN = (39.61e6 + 0.5 * (75.94e6 + 109.17e6)) / 7680
 
 
 def rooflines(prof, precision):
@@ -222,6 +227,11 @@ def run_ours(args, rank, world, dist):
     S.run(restart_from_phi0=True)
     prof = S.P.profile(on=False, reset=True)
     roofs = rooflines(prof, args.precision)
+    if args.precision == "mixed" and "gemm_f64" in roofs:
+        ncols = args.batch * SPEC["n_el"] * (SPEC["order"] + 1)
+        roofs["gemm_f64"]["traffic"] = round(OZAKI_TRAFFIC_PER_COLUMN * ncols)
+        roofs["gemm_f64"]["traffic_source"] = ("ncu dram bytes of one slicing + emulated GEMM event at batch 8, "
+                                               "scaled by columns to batch %d" % args.batch)
     roof = max(roofs.values(), key=lambda r: r["share"]) if roofs else None
     # e2e: the public call with host inputs and outputs, every step
     e2e = None
@@ -441,6 +451,96 @@ def run_transient(args):
     }
 
 
+FET = dict(n_gates=32, vg_max=0.6, v_drain=0.4, tol=1e-8, maxit=60)
+
+
+def run_fet(args):
+    """C4: multi-subband FET transport at 32 gate voltages in 0..0.6 V, V_d = 0.4 V.  A gate
+    point is the 8 subband solves (2 valley types x 4 cross-section modes) of
+    solve_transport_DG_2D at a 1e-8 relative residual plus the summed n and j.  One step sets
+    the potentials of every gate point and solves them all from a zero start as one batch
+    (gates x subbands problems in one handle); e2e runs the same sweep through
+    solve_transport_DG_2D one gate point per call (host arrays in, n and j out)."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300 import devices
+    from real_space_dg_gb300.transport import M0, Problem1D, shape_from_mat, solve_transport_DG_2D
+    spec = devices.FETSpec()
+    vgs = np.linspace(0.0, FET["vg_max"], FET["n_gates"])
+    pts = [devices.make_fet(spec, float(vg), FET["v_drain"]) for vg in vgs]
+    mat0 = pts[0][0]
+    shp = shape_from_mat(mat0)
+    nv, nm = int(mat0["n_of_valleys"]), int(mat0["n_of_modes"])
+    nsub = nv * nm
+    B = len(pts) * nsub
+    kw = dict(precision=args.precision, restart=args.restart, inner_restart=args.inner_restart,
+              inner_tol=args.inner_tol, reorth=args.reorth, inner_reorth=args.inner_reorth)
+    P = Problem1D(batch=B, **kw, **shp)
+    x_nm = np.asarray(mat0["x"], dtype=float)
+
+    def step():
+        for gi, (mat, esub, _, efl, efr) in enumerate(pts):
+            for iv in range(nv):
+                m = np.asarray(mat["me_x"], dtype=float)[iv, :, 0] * M0
+                for im in range(nm):
+                    P.set_potential(gi * nsub + iv * nm + im, x_nm, esub[iv, :, im], m, float(mat["me_z_ch"]),
+                                    float(mat["Temp"]), efl, efr)
+        return P.solve(tol=FET["tol"], maxit=FET["maxit"])
+
+    for _ in range(args.warmup):
+        step()
+    clocks = ClockSampler()
+    clocks.start()
+    P.profile(on=False, reset=True)
+    t0 = time.perf_counter()
+    infos = []
+    for _ in range(args.steps):
+        st, info = step()
+        infos.append(info)
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    counted = P.profile(on=False, reset=True)
+    conv = sum(1 for i in infos[-1] if i["relres"] <= FET["tol"])
+    iters = float(np.mean([i["iterations"] for i in infos[-1]]))
+    dev_bytes = P.device_bytes
+    P.close()
+    n_pts = len(pts) * args.steps
+    out = {
+        "metric": "converged gate points/s at 1e-8 transport residual (C4 multi-subband FET, %d subbands per point)"
+                  % nsub,
+        "value": round(n_pts / wall, 4), "unit": "gate_points/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * wall / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "bf16/f32 in f64 refinement",
+        "data": "synthetic UTB Si FET: subbands of a 5 x 5 nm box, compact gate-controlled band profile "
+                "(not self-consistent)",
+        "config": {"workload": "C4 FET 50 nm (15 nm S/D at 1e20 cm^-3), p=2, N_el=200, Nk=256, "
+                               "%d unknowns per subband, %d gate points x %d subbands in one handle"
+                               % (shp["n_el"] * shp["n_local"] * shp["nk"], len(pts), nsub),
+                   "v_drain": FET["v_drain"], "v_gate": [0.0, FET["vg_max"]], "precision": args.precision,
+                   "device_bytes": dev_bytes, "timing": "wall clock, potentials set from the host every step"},
+        "subband_solves_converged": conv, "subband_solves": B, "gmres_iterations_per_subband": iters,
+        "gpu_launches": int(sum(v[2] for v in counted.values())) if counted else None, "clocks": clk,
+    }
+    if not args.no_e2e:
+        Pe = Problem1D(batch=nsub, **kw, **shp)
+        t0 = time.perf_counter()
+        cur = []
+        for mat, esub, vsub, efl, efr in pts:
+            DG = solve_transport_DG_2D(mat, esub, vsub, efl, efr, tol=FET["tol"], maxit=FET["maxit"],
+                                       restart=args.restart, problem=Pe, return_info=False)
+            cur.append(float(np.mean(DG["j"])))          # mean j of the reference's units
+        we = time.perf_counter() - t0
+        Pe.close()
+        nb = pts[0][0]["Nx"] * 8 * (2 + nsub) * len(pts)
+        out["e2e"] = {"value": round(len(pts) / we, 4), "unit": "gate_points/s",
+                      "h2d_bytes_per_step": int(nb), "d2h_bytes_per_step": int(len(pts) * 2 * 8 * shp["n_el"]
+                                                                                  * shp["n_local"] * nsub),
+                      "path": "solve_transport_DG_2D per gate point (batch of its 8 subbands)",
+                      "mean_j_first_last_gate": [cur[0], cur[-1]]}
+    return out
+
+
 def run_apply(args):
     """Operator applies/s on the C2 batch: the FP64 operator (plain form), the mixed form's
     low-precision inner operator and its tensor-core FP64 operator, with per-kernel rooflines."""
@@ -473,9 +573,10 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c4"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
-                         "transient: batched Crank-Nicolson steps of the C5 RTD")
+                         "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
+                         "c4: multi-subband FET gate sweep")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -507,6 +608,8 @@ def main():
         out = run_transient(args) if rank == 0 else None
     elif args.workload == "apply":
         out = run_apply(args) if rank == 0 else None
+    elif args.workload == "c4":
+        out = run_fet(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

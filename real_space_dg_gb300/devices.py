@@ -146,3 +146,122 @@ def contact_fermi_levels(mat: dict, bias: float, offset_ev: float = 0.05):
     (RTD/solve2D_rtd_self_consistent.m:110-111 defaults)."""
     vc = np.asarray(mat["Vc"])
     return float(vc[0] + offset_ev), float(vc[-1] + offset_ev - bias)
+
+
+@dataclass
+class FETSpec:
+    """Gated ultra-thin-body Si FET along x with a square cross-section.
+
+    Subbands: the two valley types of a [100] Si wire (transport mass m_l with the
+    cross-section confined by (m_t, m_t), degeneracy 2; transport mass m_t confined by
+    (m_l, m_t), degeneracy 4) times the ``n_modes`` lowest particle-in-a-box modes of
+    the ``width_nm`` x ``width_nm`` cross-section.  The longitudinal profile is a
+    compact electrostatic model, not a Poisson solution: source at 0 eV, drain at
+    -V_d, channel top at ``barrier_ev - gate_eff * V_g`` lowered towards the drain by
+    ``dibl`` * V_d, joined by logistic steps of width ``step_nm`` at the junctions.
+    """
+    length_nm: float = 50.0
+    sd_nm: float = 15.0               # source and drain extension lengths
+    width_nm: float = 5.0
+    oxide_nm: float = 1.0
+    doping_m3: float = 1e26           # 1e20 cm^-3 in source and drain
+    m_l: float = 0.98
+    m_t: float = 0.19
+    n_modes: int = 4
+    barrier_ev: float = 0.45
+    gate_eff: float = 0.8
+    dibl: float = 0.1
+    step_nm: float = 1.5
+    temp_k: float = 300.0
+    eps_r: float = 11.7
+    order: int = 2
+    n_el: int = 200
+    nk: int = 256
+    n_xi: int = 0
+    l_xi_m: float = 30e-9
+    fermi_offset_ev: float = 0.05
+
+    @property
+    def n_local(self):
+        return self.order + 1
+
+    @property
+    def nx(self):
+        return self.n_el * self.order + 1
+
+    def valleys(self):
+        """[(transport mass, (confinement masses)), ...] in units of m0."""
+        return [(self.m_l, (self.m_t, self.m_t)), (self.m_t, (self.m_l, self.m_t))]
+
+
+def fet_subband_offsets(spec: FETSpec) -> np.ndarray:
+    """Confinement energies [n_valleys x n_modes] in eV: the lowest modes
+    hbar^2 pi^2 (n^2 / m_y + l^2 / m_z) / (2 W^2) of each valley type."""
+    h, m0, q = 6.626e-34, 9.109e-31, 1.602e-19
+    hb = h / 2 / np.pi
+    w = spec.width_nm * 1e-9
+    out = []
+    for _, (my, mz) in spec.valleys():
+        e = sorted(hb ** 2 * np.pi ** 2 * (n * n / (my * m0) + l * l / (mz * m0)) / (2 * w * w) / q
+                   for n in range(1, 5) for l in range(1, 5))
+        out.append(e[:spec.n_modes])
+    return np.asarray(out)
+
+
+def fet_band_profile(spec: FETSpec, x_nm: np.ndarray, v_gate: float, v_drain: float) -> np.ndarray:
+    """Longitudinal potential energy [eV] of the compact FET model (see FETSpec)."""
+    s_src = 1 / (1 + np.exp(-(x_nm - spec.sd_nm) / spec.step_nm))
+    s_drn = 1 / (1 + np.exp(-(x_nm - (spec.length_nm - spec.sd_nm)) / spec.step_nm))
+    ch = spec.length_nm - 2 * spec.sd_nm
+    top = spec.barrier_ev - spec.gate_eff * v_gate
+    top = top - spec.dibl * v_drain * np.clip((x_nm - spec.sd_nm) / ch, 0.0, 1.0)
+    return (1 - s_drn) * s_src * top + s_drn * (-v_drain)
+
+
+def make_fet(spec: FETSpec, v_gate: float, v_drain: float):
+    """(mat, Esub, Vsub, EfL, EfR) of one gate/drain point for ``solve_transport_DG_2D``:
+    n_of_valleys = 2, n_of_modes = spec.n_modes, Ny = 1 (the mode's weight at the
+    cross-section centre taken as 1 / W); E_F,L sits fermi_offset_ev above the
+    source's lowest subband edge, E_F,R = E_F,L - V_d."""
+    nx = spec.nx
+    x = np.linspace(0.0, spec.length_nm, nx)
+    nxi = spec.n_xi or spec.nk
+    vals = spec.valleys()
+    nv, nm = len(vals), spec.n_modes
+    u = fet_band_profile(spec, x, v_gate, v_drain)
+    esub = u[None, :, None] + fet_subband_offsets(spec)[:, None, :]
+    vsub = np.full((nv, nx, nm, 1), 1.0 / np.sqrt(spec.width_nm))
+    nd = np.where((x <= spec.sd_nm) | (x >= spec.length_nm - spec.sd_nm), spec.doping_m3, 0.0)
+    mat = {
+        "type": "UTB-FET-1D-modes",
+        "Nx": nx,
+        "Ny": 1,
+        "dy": spec.width_nm,
+        "dx": spec.length_nm / (nx - 1),
+        "x": x,
+        "L_x": spec.length_nm,
+        "me_x": np.repeat(np.asarray([v[0] for v in vals])[:, None, None], nx, axis=1),
+        "me_z_ch": spec.m_t,
+        "Temp": spec.temp_k,
+        "deg_factor": np.array([2.0, 4.0]),
+        "n_of_valleys": nv,
+        "n_of_modes": nm,
+        "Vc": u,
+        "Nd": nd,
+        "eps": np.full(nx, spec.eps_r),
+        "ramp": np.clip((x - spec.sd_nm) / (spec.length_nm - 2 * spec.sd_nm), 0.0, 1.0),
+        "dg": {"params": {
+            "N_K_chi": spec.n_local,
+            "Xi_solver": "FV",
+            "N_xi": nxi,
+            "N": spec.nk,
+            "Ly": spec.l_xi_m,
+            "Q": "EXP",
+            "permute_shell": True,
+            "MPC": 1.0,
+            "sl": 0,
+            "st_init": False,
+        }},
+    }
+    ef_l = float(esub[:, 0, :].min()) + spec.fermi_offset_ev   # above the source's lowest subband edge
+    return mat, esub, vsub, ef_l, ef_l - v_drain

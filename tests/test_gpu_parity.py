@@ -130,6 +130,23 @@ def test_solve_transport_mirror_matches_oracle(lib):
     assert np.allclose(out["chi"], ref["chi"], rtol=1e-14) and np.allclose(out["xi"], ref["xi"], rtol=1e-14)
 
 
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 1e-12)])
+def test_multi_subband_fet_matches_oracle(lib, precision, tol):
+    """Two valley types x two modes of a small gated FET through the drop-in: every
+    subband is one problem of the batch, n sums the |Vsub|^2-weighted mode densities
+    and j the mode currents (solve_transport_DG_2D.m:47-212)."""
+    from real_space_dg_gb300 import devices, solve_transport_DG_2D
+    spec = devices.FETSpec(length_nm=20.0, sd_nm=6.0, n_el=16, order=2, nk=32, n_modes=2, l_xi_m=12e-9)
+    mat, esub, vsub, efl, efr = devices.make_fet(spec, 0.3, 0.2)
+    ref = dg1d.solve_transport_dg_2d(mat, esub, vsub, efl, efr)
+    out = solve_transport_DG_2D(mat, esub, vsub, efl, efr, tol=tol, maxit=80, precision=precision)
+    assert all(i["flag"] == 0 for i in out["info"]), out["info"]
+    assert out["RHO"].shape == (2, 2, spec.n_el * spec.n_local, spec.nk)
+    assert rel(out["n"], ref["n"]) < 1e-9
+    assert rel(out["j"], ref["j"]) < 1e-8
+    assert rel(out["RHO"], ref["RHO"]) < 1e-9
+
+
 def test_warm_start_and_statuses(lib):
     from real_space_dg_gb300 import WignerError, _lib
     spec, mat, E, efl, efr, m = small_rtd(n_el=10, nk=24, order=2)

@@ -162,3 +162,28 @@ def test_kline_preconditioner_inverts_flux_exactly():
     pre = krylov.KLinePreconditioner(op, use_drift_diag=False)
     x = np.random.default_rng(1).standard_normal(op.N) + 0j
     assert np.linalg.norm(pre.apply(op.apply_flux(x)) - x) <= 1e-10 * np.linalg.norm(x)
+
+
+def test_fet_subbands_and_mode_sum():
+    """The FET builder's subbands (particle-in-a-box levels of the cross-section per
+    valley type) and the oracle's valley x mode loop: n and j of a 2 x 2 subband
+    solve are the sums of the single-subband solves."""
+    from real_space_dg_gb300 import devices
+    spec = devices.FETSpec(length_nm=16.0, sd_nm=5.0, n_el=8, order=1, nk=16, n_modes=2, l_xi_m=10e-9)
+    off = devices.fet_subband_offsets(spec)
+    hb, m0, q = 6.626e-34 / 2 / np.pi, 9.109e-31, 1.602e-19
+    e11 = hb ** 2 * np.pi ** 2 * (1 / (spec.m_t * m0) + 1 / (spec.m_t * m0)) / (2 * (spec.width_nm * 1e-9) ** 2) / q
+    assert abs(off[0, 0] - e11) < 1e-12 and np.all(np.diff(off, axis=1) >= 0)
+    mat, esub, vsub, efl, efr = devices.make_fet(spec, 0.2, 0.1)
+    assert esub.shape == (2, spec.nx, 2) and vsub.shape == (2, spec.nx, 2, 1) and abs(efl - efr - 0.1) < 1e-15
+    full = dg1d.solve_transport_dg_2d(mat, esub, vsub, efl, efr)
+    n_sum, j_sum = 0, 0
+    for iv in range(2):
+        for im in range(2):
+            one = dict(mat, n_of_valleys=1, n_of_modes=1, me_x=mat["me_x"][iv:iv + 1])
+            r = dg1d.solve_transport_dg_2d(one, esub[iv:iv + 1, :, im:im + 1], vsub[iv:iv + 1, :, im:im + 1],
+                                           efl, efr)
+            n_sum = n_sum + r["n"]
+            j_sum = j_sum + r["j"]
+    assert np.allclose(full["n"], n_sum, rtol=1e-13, atol=0)
+    assert np.allclose(full["j"], j_sum, rtol=1e-13, atol=1e-30)
