@@ -121,6 +121,24 @@ const char* wg_global_error(void);
 /* Sizes: N per problem (complex entries), batch, bytes of device memory held. */
 int wg_problem_sizes(const wg_problem* h, long long* n_per_problem, int* batch, double* device_bytes);
 
+/* Runtime state of a handle: the CUDA graphs of its Arnoldi steps (chunks of 4
+ * steps captured once and replayed; WG_CUDA_GRAPHS=0 disables them) and the launch
+ * shapes the autotuner picked on its first solve (WG_AUTOTUNE=0 keeps the defaults).
+ * No reference counterpart (MATLAB's gmres has neither). */
+typedef struct {
+  long long graph_replays;  /* Arnoldi chunks replayed from graphs so far */
+  int graphs_captured;      /* chunk graphs instantiated (both bases) */
+  int graphs_disabled;      /* 1 when a capture failed and the handle launches eagerly */
+  int tuned;                /* 1 once the autotuner ran (or found the shape cached) */
+  int kline_chunk;          /* elements per k-line chunk in use */
+  int stencil_cells;        /* xi cells per thread of the FP32 stencil (mixed form) */
+} wg_runtime_stats;
+int wg_runtime_stats_get(const wg_problem* h, wg_runtime_stats* out);
+/* Pin the launch shapes instead of tuning them (e.g. for results reproducible across
+ * processes): kline_chunk elements per k-line chunk (1 .. n_el, at most 64 chunks),
+ * stencil_cells 2 or 4 (ignored by FP64 handles); 0 keeps the current value. */
+int wg_set_launch_shapes(wg_problem* h, int kline_chunk, int stencil_cells);
+
 /* Set problem b's potential (Esub [eV] on the material grid), masses and the
  * contact Fermi levels.  Rebuilds on the device: the Wigner-potential kernel
  * data Vw(x,k) (get_Drift_accel_trial_permutedShell.m:64-147), the contact

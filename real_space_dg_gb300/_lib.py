@@ -115,6 +115,14 @@ class WgServerStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class WgRuntimeStats(C.Structure):
+    _fields_ = [("graph_replays", C.c_longlong), ("graphs_captured", C.c_int), ("graphs_disabled", C.c_int),
+                ("tuned", C.c_int), ("kline_chunk", C.c_int), ("stencil_cells", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
 
 
@@ -136,6 +144,8 @@ SIGNATURES = {
     "wg_last_error": ([_H], C.c_char_p),
     "wg_global_error": ([], C.c_char_p),
     "wg_problem_sizes": ([_H, C.POINTER(C.c_longlong), C.POINTER(C.c_int), _D], C.c_int),
+    "wg_runtime_stats_get": ([_H, C.POINTER(WgRuntimeStats)], C.c_int),
+    "wg_set_launch_shapes": ([_H, C.c_int, C.c_int], C.c_int),
     "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),
     "wg_solve": ([_H, C.POINTER(WgSolveOpts), _D, C.POINTER(WgSolveInfo)], C.c_int),
     "wg_get_rho": ([_H, C.c_int, _D], C.c_int),

@@ -35,6 +35,11 @@ cudaError_t dalloc(T** p, size_t count, double& bytes) {
 }
 
 void free_all(wg::Problem& P) {
+  for (wg::ArnoldiGraphs& G : P.graphs) {
+    for (cudaGraphExec_t x : G.exec)
+      if (x) cudaGraphExecDestroy(x);
+    G.exec.clear();
+  }
   wg::prof_release(P);
   wg::mixed_free(P);
   for (cudaEvent_t& e : P.ev)
@@ -246,7 +251,9 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.pre_dinv, (size_t)batch * s.nk * nK * nK, bytes));
   A(dalloc(&P.pre_h, (size_t)batch * s.nk * nK, bytes));
   {
-    const size_t nmap = (size_t)batch * wg::kline::chunk_count(s.n_el) * s.nk;
+    // chunk maps for any chunk length the autotuner may pick (at most kMaxChunks chunks)
+    P.kline_L = wg::kline::chunk_len(s.n_el);
+    const size_t nmap = (size_t)batch * std::max(wg::kline::chunk_count(s.n_el), wg::kline::kMaxChunks) * s.nk;
     double* a = nullptr;
     double2* m = nullptr;
     A(dalloc(&a, nmap, bytes));
@@ -380,6 +387,36 @@ int wg_problem_sizes(const wg_problem* h, long long* n_per_problem, int* batch, 
   if (n_per_problem) *n_per_problem = h->P.N;
   if (batch) *batch = h->P.batch;
   if (device_bytes) *device_bytes = h->P.device_bytes;
+  return WG_OK;
+}
+
+int wg_runtime_stats_get(const wg_problem* h, wg_runtime_stats* out) {
+  if (!h || !out) return fail(h ? const_cast<wg::Problem*>(&h->P) : nullptr, WG_ERR_ARG, "wg_runtime_stats_get: null argument");
+  const wg::Problem& P = h->P;
+  wg_runtime_stats r{};
+  for (const wg::ArnoldiGraphs& G : P.graphs) {
+    r.graph_replays += G.replays;
+    for (cudaGraphExec_t x : G.exec) r.graphs_captured += x ? 1 : 0;
+    r.graphs_disabled |= G.disabled ? 1 : 0;
+  }
+  r.tuned = P.tuned ? 1 : 0;
+  r.kline_chunk = P.kline_L;
+  r.stencil_cells = P.st_cells;
+  *out = r;
+  return WG_OK;
+}
+
+int wg_set_launch_shapes(wg_problem* h, int kline_chunk, int stencil_cells) {
+  if (!h) return fail(nullptr, WG_ERR_ARG, "null handle");
+  wg::Problem& P = h->P;
+  if (kline_chunk < 0 || kline_chunk > P.s.n_el ||
+      (kline_chunk > 0 && wg::kline::chunk_count_for(P.s.n_el, kline_chunk) > wg::kline::kMaxChunks))
+    return fail(&P, WG_ERR_ARG, "wg_set_launch_shapes: kline_chunk must give 1 .. 64 chunks of at most n_el elements");
+  if (stencil_cells != 0 && stencil_cells != 2 && stencil_cells != 4)
+    return fail(&P, WG_ERR_ARG, "wg_set_launch_shapes: stencil_cells must be 2 or 4");
+  if (kline_chunk) P.kline_L = kline_chunk;
+  if (stencil_cells) P.st_cells = stencil_cells;
+  P.tuned = true;
   return WG_OK;
 }
 

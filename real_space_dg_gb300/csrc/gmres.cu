@@ -20,6 +20,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <type_traits>
 
@@ -751,6 +752,83 @@ bool all_done(const std::vector<int>& act) {
   return true;
 }
 
+bool graphs_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("WG_CUDA_GRAPHS");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
+void reset_graphs(ArnoldiGraphs& G) {
+  for (cudaGraphExec_t x : G.exec)
+    if (x) cudaGraphExecDestroy(x);
+  G.exec.clear();
+  G.launches.clear();
+  G.eager.clear();
+}
+
+// Arnoldi steps k0 .. k0+3 (fewer at the end of the cycle) of a cycle of length m, run
+// eagerly (`run`) or replayed from the chunk's CUDA graph.  A chunk is captured on its
+// second use, so the launch helpers' one-time set-up has run outside the capture; any
+// failure to capture or instantiate falls back to eager launches for the handle.
+template <typename Run>
+int run_arnoldi_chunk(Problem& P, ArnoldiGraphs& G, int m, int k0, Run run) {
+  if (G.disabled || P.prof.on || !graphs_enabled()) return run();
+  const int nchunk = (m + 3) / 4, c = k0 / 4;
+  if (G.m != m || G.shift != P.shift || G.kline_L != P.kline_L || G.st_cells != P.st_cells ||
+      (int)G.exec.size() != nchunk) {
+    reset_graphs(G);
+    G.m = m;
+    G.shift = P.shift;
+    G.kline_L = P.kline_L;
+    G.st_cells = P.st_cells;
+    G.exec.assign(nchunk, nullptr);
+    G.launches.assign(nchunk, {});
+    G.eager.assign(nchunk, 0);
+  }
+  if (G.exec[c]) {
+    const cudaError_t e = cudaGraphLaunch(G.exec[c], P.stream);
+    if (e != cudaSuccess) {
+      P.err = std::string("CUDA graph launch: ") + cudaGetErrorString(e);
+      return WG_ERR_CUDA;
+    }
+    for (int i = 0; i < PROF_N; ++i) P.prof.launches[i] += G.launches[c][i];
+    ++G.replays;
+    return WG_OK;
+  }
+  if (G.eager[c]++ == 0) return run();
+  std::array<long long, PROF_N> before;
+  for (int i = 0; i < PROF_N; ++i) before[i] = P.prof.launches[i];
+  auto fall_back = [&]() {
+    cudaGetLastError();
+    G.disabled = true;
+    reset_graphs(G);
+    for (int i = 0; i < PROF_N; ++i) P.prof.launches[i] = before[i];
+    return run();
+  };
+  if (cudaStreamBeginCapture(P.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return fall_back();
+  const int rc = run();
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(P.stream, &g);
+  if (rc != WG_OK || ec != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    return fall_back();
+  }
+  cudaGraphExec_t x = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess || !x) return fall_back();
+  G.exec[c] = x;
+  for (int i = 0; i < PROF_N; ++i) G.launches[c][i] = P.prof.launches[i] - before[i];
+  const cudaError_t e = cudaGraphLaunch(x, P.stream);
+  if (e != cudaSuccess) {
+    P.err = std::string("CUDA graph launch: ") + cudaGetErrorString(e);
+    return WG_ERR_CUDA;
+  }
+  return WG_OK;
+}
+
 }  // namespace
 
 int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info) {
@@ -774,14 +852,19 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
     scale_kernel<double2, double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, P.V, P.inv64, P.active, N,
                                                                          (long long)mp1 * N, B);
-    for (int k = 0; k < m; ++k) {
-      rc = arnoldi_step<double2>(P, P.V, P.w, k, m, prec, apply);
+    for (int k0 = 0; k0 < m; k0 += 4) {
+      const int k1 = std::min(m, k0 + 4);
+      rc = run_arnoldi_chunk(P, P.graphs[0], m, k0, [&]() {
+        for (int k = k0; k < k1; ++k) {
+          const int r = arnoldi_step<double2>(P, P.V, P.w, k, m, prec, apply);
+          if (r) return r;
+        }
+        return (int)WG_OK;
+      });
       if (rc) return rc;
-      if ((k & 3) == 3 || k == m - 1) {
-        WG_CK(cudaMemcpyAsync(P.h_active.data(), P.active, sizeof(int) * B, cudaMemcpyDeviceToHost, P.stream));
-        WG_CK(cudaStreamSynchronize(P.stream));
-        if (all_done(P.h_active)) break;
-      }
+      WG_CK(cudaMemcpyAsync(P.h_active.data(), P.active, sizeof(int) * B, cudaMemcpyDeviceToHost, P.stream));
+      WG_CK(cudaStreamSynchronize(P.stream));
+      if (all_done(P.h_active)) break;
     }
     P.prof.launches[PROF_OTHER] += 3;
     backsolve_kernel<<<B, 32, 0, P.stream>>>(P.H, P.g, P.ycoef, nullptr, P.kused, ps, mm, B);
@@ -848,14 +931,19 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
     scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.V, P.inv64, P.active, N,
                                                                         (long long)mp1 * N, B);
-    for (int k = 0; k < m; ++k) {
-      rc = arnoldi_step<float2>(P, M.V, M.w, k, m, prec, apply);
+    for (int k0 = 0; k0 < m; k0 += 4) {
+      const int k1 = std::min(m, k0 + 4);
+      rc = run_arnoldi_chunk(P, P.graphs[1], m, k0, [&]() {
+        for (int k = k0; k < k1; ++k) {
+          const int r = arnoldi_step<float2>(P, M.V, M.w, k, m, prec, apply);
+          if (r) return r;
+        }
+        return (int)WG_OK;
+      });
       if (rc) return rc;
-      if ((k & 3) == 3 || k == m - 1) {
-        WG_CK(cudaMemcpyAsync(P.h_active.data(), P.active, sizeof(int) * B, cudaMemcpyDeviceToHost, P.stream));
-        WG_CK(cudaStreamSynchronize(P.stream));
-        if (all_done(P.h_active)) break;
-      }
+      WG_CK(cudaMemcpyAsync(P.h_active.data(), P.active, sizeof(int) * B, cudaMemcpyDeviceToHost, P.stream));
+      WG_CK(cudaStreamSynchronize(P.stream));
+      if (all_done(P.h_active)) break;
     }
     // d = M^-1 (V y) in FP32, x += |r| d in FP64
     P.prof.launches[PROF_OTHER] += 3;
@@ -891,6 +979,10 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
 }
 
 int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info) {
+  if (!P.tuned) {
+    const int rt = autotune(P);
+    if (rt) return rt;
+  }
   if (P.precision == WG_PREC_MIXED) return gmres_solve_mixed(P, o, warm, info);
   return gmres_solve_fp64(P, o, warm, info);
 }

@@ -17,6 +17,8 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <vector>
+
 namespace wg {
 namespace kline {
 
@@ -145,10 +147,27 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
   }
 }
 
-// Elements per chunk: about 32 chunks per line (the incoming-state fold costs one
-// map read per upwind chunk), at least 4 elements each.
+// Elements per chunk L.  The default: about 32 chunks per line (the incoming-state fold
+// costs one map read per upwind chunk), at least 4 elements each; the autotuner times
+// the candidates below and keeps the fastest per shape.  At most kMaxChunks chunks (the
+// map buffers are sized for that).
+constexpr int kMaxChunks = 64;
 inline int chunk_len(int n_el) { return n_el / 32 > 4 ? (n_el + 31) / 32 : 4; }
-inline int chunk_count(int n_el) { return (n_el + chunk_len(n_el) - 1) / chunk_len(n_el); }
+inline int chunk_count_for(int n_el, int L) { return (n_el + L - 1) / L; }
+inline int chunk_count(int n_el) { return chunk_count_for(n_el, chunk_len(n_el)); }
+inline std::vector<int> chunk_len_candidates(int n_el) {
+  std::vector<int> out;
+  int last = -1;
+  for (int L : {2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128}) {
+    if (L > n_el && !out.empty()) break;
+    const int nc = chunk_count_for(n_el, L);
+    if (nc > kMaxChunks || nc == last) continue;
+    out.push_back(L);
+    last = nc;
+  }
+  if (out.empty()) out.push_back(chunk_len(n_el));
+  return out;
+}
 
 }  // namespace kline
 }  // namespace wg

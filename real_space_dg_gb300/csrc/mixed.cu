@@ -209,9 +209,10 @@ __global__ void __launch_bounds__(kFlux32Threads) flux32_kernel(const float2* __
 // FP32 xi stencil, output as the BF16 B operand of GEMM 2:
 //   y_a(s) = sum_c beta_ac(s) (x_c(s) + x_c(s-1)) + beta_ac(s+1) (x_c(s) + x_c(s+1)),
 // beta = betar (symmetric in a, c: pairs a <= c stored) + i betai.  Each thread owns
-// four consecutive xi cells (16-byte loads of x, of the weights and of the BF16
-// output); the cells s0-1 and s0+4 come from the neighbouring lanes.  Grid
-// (batch * n_el, ceil(nxi / 256)) of 64 threads; nxi % 4 == 0 (mixed form).
+// CELLS (2 or 4, picked per shape by the autotuner) consecutive xi cells: vector loads
+// of x (16 bytes per two cells), of the weights (4 bytes per cell) and vector stores of
+// the BF16 output; the cells s0-1 and s0+CELLS come from the neighbouring lanes.  Grid
+// (batch * n_el, ceil(nxi / (64 CELLS))) of 64 threads; nxi % 4 == 0 (mixed form).
 // ---------------------------------------------------------------------------
 constexpr int kSt4Threads = 64;
 
@@ -221,86 +222,116 @@ __host__ __device__ constexpr int pair_index(int nk, int a, int c) { return a * 
 
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 
-template <int NK>
+// CELLS consecutive floats (CELLS * 4 bytes aligned) into v[0..CELLS)
+template <int CELLS>
+__device__ __forceinline__ void ld_cells(const float* p, float* v) {
+  if constexpr (CELLS == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else {
+    const float2 t = *reinterpret_cast<const float2*>(p);
+    v[0] = t.x; v[1] = t.y;
+  }
+}
+
+template <int NK, int CELLS>
 __global__ void __launch_bounds__(kSt4Threads) stencil32_kernel(const float2* __restrict__ xh,
                                                                 bf162* __restrict__ yh,
                                                                 const float* __restrict__ betar,
                                                                 const float* __restrict__ betai, int nxi, int ne4,
                                                                 int n_el, const int* __restrict__ mask) {
+  static_assert(CELLS == 2 || CELLS == 4, "two or four cells per thread");
   const int be = blockIdx.x;
   if (mask && !mask[be / n_el]) return;
   const int lane = threadIdx.x & 31;
-  const int s0 = (blockIdx.y * kSt4Threads + threadIdx.x) * 4;
-  const bool valid = s0 < nxi;             // nxi % 4 == 0: then all four cells are
-  const bool edge = lane == 31 || s0 + 4 >= nxi;   // s0 + 4 not held by the next lane
+  const int s0 = (blockIdx.y * kSt4Threads + threadIdx.x) * CELLS;
+  const bool valid = s0 < nxi;                       // nxi % 4 == 0: then all CELLS cells are
+  const bool edge = lane == 31 || s0 + CELLS >= nxi;  // s0 + CELLS not held by the next lane
   const float2* X = xh + (long long)be * NK * nxi;
   const float2 z2 = make_float2(0.f, 0.f);
-  float2 sm[NK][4], sp[NK][4];
+  float2 sm[NK][CELLS], sp[NK][CELLS];
 #pragma unroll
   for (int c = 0; c < NK; ++c) {
-    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
-    if (valid) {
-      lo = *reinterpret_cast<const float4*>(X + c * nxi + s0);
-      hi = *reinterpret_cast<const float4*>(X + c * nxi + s0 + 2);
+    float2 x[CELLS];
+#pragma unroll
+    for (int h = 0; h < CELLS / 2; ++h) {
+      float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (valid) t = *reinterpret_cast<const float4*>(X + c * nxi + s0 + 2 * h);
+      x[2 * h] = make_float2(t.x, t.y);
+      x[2 * h + 1] = make_float2(t.z, t.w);
     }
-    const float2 x0 = make_float2(lo.x, lo.y), x1 = make_float2(lo.z, lo.w);
-    const float2 x2 = make_float2(hi.x, hi.y), x3 = make_float2(hi.z, hi.w);
     float2 xm, xp;
-    xm.x = __shfl_up_sync(0xffffffffu, x3.x, 1);
-    xm.y = __shfl_up_sync(0xffffffffu, x3.y, 1);
-    xp.x = __shfl_down_sync(0xffffffffu, x0.x, 1);
-    xp.y = __shfl_down_sync(0xffffffffu, x0.y, 1);
+    xm.x = __shfl_up_sync(0xffffffffu, x[CELLS - 1].x, 1);
+    xm.y = __shfl_up_sync(0xffffffffu, x[CELLS - 1].y, 1);
+    xp.x = __shfl_down_sync(0xffffffffu, x[0].x, 1);
+    xp.y = __shfl_down_sync(0xffffffffu, x[0].y, 1);
     if (lane == 0) xm = (valid && s0 > 0) ? X[c * nxi + s0 - 1] : z2;
-    if (edge) xp = (valid && s0 + 4 < nxi) ? X[c * nxi + s0 + 4] : z2;
+    if (edge) xp = (valid && s0 + CELLS < nxi) ? X[c * nxi + s0 + CELLS] : z2;
     if (s0 == 0) xm = z2;
-    sm[c][0] = f2add(x0, xm);
-    sm[c][1] = f2add(x1, x0);
-    sm[c][2] = f2add(x2, x1);
-    sm[c][3] = f2add(x3, x2);
-    sp[c][0] = f2add(x0, x1);
-    sp[c][1] = f2add(x1, x2);
-    sp[c][2] = f2add(x2, x3);
-    sp[c][3] = f2add(x3, xp);
+#pragma unroll
+    for (int j = 0; j < CELLS; ++j) {
+      sm[c][j] = f2add(x[j], j == 0 ? xm : x[j - 1]);
+      sp[c][j] = f2add(x[j], j == CELLS - 1 ? xp : x[j + 1]);
+    }
   }
   const float* br = betar + (long long)be * pair_count(NK) * ne4;
   bf162* Y = yh + (long long)be * NK * nxi;
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
-    float vx[4] = {0.f, 0.f, 0.f, 0.f}, vy[4] = {0.f, 0.f, 0.f, 0.f};
+    float vx[CELLS], vy[CELLS];
+#pragma unroll
+    for (int j = 0; j < CELLS; ++j) vx[j] = vy[j] = 0.f;
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
       const float* rr = br + pair_index(NK, a < c ? a : c, a < c ? c : a) * ne4;
       const float* ri = betai + (a * NK + c) * ne4;
-      float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), i0 = r0;
-      if (valid) {
-        r0 = *reinterpret_cast<const float4*>(rr + s0);
-        i0 = *reinterpret_cast<const float4*>(ri + s0);
-      }
-      // the weight of edge s0 + 4: the next lane's first, loaded at the warp's edge
-      float r4 = __shfl_down_sync(0xffffffffu, r0.x, 1), i4 = __shfl_down_sync(0xffffffffu, i0.x, 1);
-      if (edge) {
-        r4 = valid ? rr[s0 + 4] : 0.f;
-        i4 = valid ? ri[s0 + 4] : 0.f;
-      }
-      const float b0r[4] = {r0.x, r0.y, r0.z, r0.w}, b0i[4] = {i0.x, i0.y, i0.z, i0.w};
-      const float b1r[4] = {r0.y, r0.z, r0.w, r4}, b1i[4] = {i0.y, i0.z, i0.w, i4};
+      float r0[CELLS], i0[CELLS];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        vx[j] += b0r[j] * sm[c][j].x - b0i[j] * sm[c][j].y + b1r[j] * sp[c][j].x - b1i[j] * sp[c][j].y;
-        vy[j] += b0r[j] * sm[c][j].y + b0i[j] * sm[c][j].x + b1r[j] * sp[c][j].y + b1i[j] * sp[c][j].x;
+      for (int j = 0; j < CELLS; ++j) r0[j] = i0[j] = 0.f;
+      if (valid) {
+        ld_cells<CELLS>(rr + s0, r0);
+        ld_cells<CELLS>(ri + s0, i0);
+      }
+      // the weight of edge s0 + CELLS: the next lane's first, loaded at the warp's edge
+      float rn = __shfl_down_sync(0xffffffffu, r0[0], 1), in = __shfl_down_sync(0xffffffffu, i0[0], 1);
+      if (edge) {
+        rn = valid ? rr[s0 + CELLS] : 0.f;
+        in = valid ? ri[s0 + CELLS] : 0.f;
+      }
+#pragma unroll
+      for (int j = 0; j < CELLS; ++j) {
+        const float b1r = j == CELLS - 1 ? rn : r0[j + 1], b1i = j == CELLS - 1 ? in : i0[j + 1];
+        vx[j] += r0[j] * sm[c][j].x - i0[j] * sm[c][j].y + b1r * sp[c][j].x - b1i * sp[c][j].y;
+        vy[j] += r0[j] * sm[c][j].y + i0[j] * sm[c][j].x + b1r * sp[c][j].y + b1i * sp[c][j].x;
       }
     }
     if (valid) {
-      uint4 o;
-      bf162 t0 = __floats2bfloat162_rn(vx[0], vy[0]), t1 = __floats2bfloat162_rn(vx[1], vy[1]);
-      bf162 t2 = __floats2bfloat162_rn(vx[2], vy[2]), t3 = __floats2bfloat162_rn(vx[3], vy[3]);
-      o.x = *reinterpret_cast<uint32_t*>(&t0);
-      o.y = *reinterpret_cast<uint32_t*>(&t1);
-      o.z = *reinterpret_cast<uint32_t*>(&t2);
-      o.w = *reinterpret_cast<uint32_t*>(&t3);
-      *reinterpret_cast<uint4*>(Y + a * nxi + s0) = o;
+      uint32_t o[CELLS];
+#pragma unroll
+      for (int j = 0; j < CELLS; ++j) {
+        bf162 t = __floats2bfloat162_rn(vx[j], vy[j]);
+        o[j] = *reinterpret_cast<uint32_t*>(&t);
+      }
+      if constexpr (CELLS == 4)
+        *reinterpret_cast<uint4*>(Y + a * nxi + s0) = make_uint4(o[0], o[1], o[2], o[3]);
+      else
+        *reinterpret_cast<uint2*>(Y + a * nxi + s0) = make_uint2(o[0], o[1]);
     }
   }
+}
+
+template <int NK>
+void launch_stencil32(Problem& P, const int* mask) {
+  const Shape& s = P.s;
+  MixedBuffers& M = P.mx;
+  const int cells = P.st_cells == 2 ? 2 : 4;
+  const dim3 grid((unsigned)(P.batch * s.n_el), (unsigned)((s.nxi + cells * kSt4Threads - 1) / (cells * kSt4Threads)));
+  if (cells == 2)
+    stencil32_kernel<NK, 2><<<grid, kSt4Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16,
+                                                                M.beta, M.betai, s.nxi, M.ne4, s.n_el, mask);
+  else
+    stencil32_kernel<NK, 4><<<grid, kSt4Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16,
+                                                                M.beta, M.betai, s.nxi, M.ne4, s.n_el, mask);
 }
 
 // FP32 packed copies of the potential weights: out[r][p][s] = beta[r][a*nK+c][s] for the
@@ -368,9 +399,7 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
   prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
   ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * pair_count(NK) * M.ne4);
-  const dim3 sgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nxi + 4 * kSt4Threads - 1) / (4 * kSt4Threads)));
-  stencil32_kernel<NK><<<sgrid, kSt4Threads, 0, P.stream>>>(reinterpret_cast<const float2*>(M.xh), M.yh16, M.beta,
-                                                            M.betai, s.nxi, M.ne4, s.n_el, mask);
+  launch_stencil32<NK>(P, mask);
   prof_end(P, PROF_STENCIL, ev);
   ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops);
   e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream, mask,
@@ -382,7 +411,7 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
 
 template <int NK>
 cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb, const int* mask) {
-  const int L = kline::chunk_len(P.s.n_el), nc = kline::chunk_count(P.s.n_el);
+  const int L = P.kline_L, nc = kline::chunk_count_for(P.s.n_el, L);
   const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
   const dim3 block(32, kline::kChunksPerBlock);
   float* ma = static_cast<float*>(P.kmap_a);
@@ -618,6 +647,15 @@ cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y) {
   e = launch_apply_mixed(P, P.mx.z, nullptr, P.mx.w);
   if (e != cudaSuccess) return e;
   f2c_kernel<<<(unsigned)((n + 255) / 256), 256, 0, P.stream>>>(P.mx.w, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stencil_mixed(Problem& P) {
+  switch (P.s.nK) {
+    case 2: launch_stencil32<2>(P, nullptr); break;
+    case 3: launch_stencil32<3>(P, nullptr); break;
+    default: launch_stencil32<4>(P, nullptr); break;
+  }
   return cudaGetLastError();
 }
 

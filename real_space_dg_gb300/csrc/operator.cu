@@ -352,7 +352,7 @@ cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
 
 template <int NK>
 cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2* z) {
-  const int L = kline::chunk_len(P.s.n_el), nc = kline::chunk_count(P.s.n_el);
+  const int L = P.kline_L, nc = kline::chunk_count_for(P.s.n_el, L);
   const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
   const dim3 block(32, kline::kChunksPerBlock);
   double* ma = static_cast<double*>(P.kmap_a);

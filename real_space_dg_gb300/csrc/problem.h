@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <array>
 #include <vector>
 
 #include "setup.h"
@@ -129,6 +130,23 @@ struct Profiler {
   std::vector<double> pend_bytes, pend_flops;
 };
 
+// CUDA graphs of the Arnoldi steps: the launches of each chunk of 4 steps (k0 .. k0+3)
+// of one restart cycle are captured once (on the chunk's second use, after the launch
+// helpers' one-time set-up ran eagerly) and replayed in later cycles and refinements.
+// Every kernel argument of a chunk is a device pointer or a per-handle constant except
+// the flux shift, so the graphs are rebuilt when the shift (or the restart length)
+// changes.  Disabled by WG_CUDA_GRAPHS=0 and while the per-launch profiler is on.
+struct ArnoldiGraphs {
+  std::vector<cudaGraphExec_t> exec;               // per chunk, nullptr until captured
+  std::vector<std::array<long long, PROF_N>> launches;   // profiler launch counts of one replay
+  std::vector<int> eager;                          // eager runs of the chunk so far
+  double shift = 0;
+  int m = -1;
+  int kline_L = -1, st_cells = -1;                 // launch shapes the graphs were captured with
+  bool disabled = false;
+  long long replays = 0;
+};
+
 // Device arrays of the Gummel loop (allocated on the first wg_gummel_set).
 struct GummelDev {
   double* vc = nullptr;      // [B][nx] band edge
@@ -237,6 +255,11 @@ struct Problem {
   int* active = nullptr;         // [B] 1 while iterating in this cycle
   int* reorth = nullptr;         // [B] 1 where the current Arnoldi step re-orthogonalises
   int* res_mask = nullptr;       // [B] problems whose true residual is evaluated
+  ArnoldiGraphs graphs[2];       // [0] FP64 basis, [1] the mixed form's FP32 inner basis
+  // launch shapes picked by the autotuner (tune.cu) on the first solve of a shape
+  int kline_L = 4;               // elements per k-line chunk
+  int st_cells = 4;              // xi cells per thread of the FP32 stencil
+  bool tuned = false;
   std::vector<int> h_res_mask;
   int* md_count = nullptr;       // [B] last-block tickets of the multi-dot (zero between launches)
   int* gs_count = nullptr;       // [B] last-block tickets of the Gram-Schmidt update
@@ -297,12 +320,18 @@ cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162
                                const int* mask = nullptr);
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
                                       __nv_bfloat162* zb, const int* mask = nullptr);
+// The FP32 xi stencil alone (M.xh -> M.yh16, every problem), for the autotuner.
+cudaError_t launch_stencil_mixed(Problem& P);
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);
 cudaError_t apply_mixed_repeat(Problem& P, const double2* x, int n_apply);
 int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err);
 int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // FP64 GMRES or the mixed-precision refinement, by P.precision.
 int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
+// Picks the handle's launch shapes (k-line chunk length, FP32 stencil cells per thread)
+// by timing the candidates on the handle's own buffers; the choice is cached per shape
+// (n_el, N_K, Nk, N_xi, precision) for the process.  WG_AUTOTUNE=0 keeps the defaults.
+int autotune(Problem& P);
 // Gummel loop (gummel.cu)
 int gummel_set(Problem& P, int b, const wg_device& dev, const wg_rtd_1d& rtd);
 int gummel_run(Problem& P, const wg_gummel_opts& o, wg_gummel_info* info);

@@ -75,6 +75,17 @@ class Problem1D:
         self._check(self.lib.wg_problem_sizes(self.h, C.byref(n), C.byref(b), C.byref(d)))
         return d.value
 
+    @property
+    def runtime_stats(self):
+        """CUDA-graph replays and the autotuner's launch shapes (wg_runtime_stats_get)."""
+        st = _lib.WgRuntimeStats()
+        self._check(self.lib.wg_runtime_stats_get(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def set_launch_shapes(self, kline_chunk=0, stencil_cells=0):
+        """Pin the k-line chunk length and the FP32 stencil's cells per thread (0 keeps)."""
+        self._check(self.lib.wg_set_launch_shapes(self.h, int(kline_chunk), int(stencil_cells)))
+
     # -- data ------------------------------------------------------------
     def set_potential(self, b, x_nm, esub_ev, m_kg, me_z, temp, ef_l, ef_r):
         x = np.ascontiguousarray(x_nm, dtype=np.float64)

@@ -54,6 +54,7 @@ int main(void) {
          sizeof(wg_server_stats), sizeof(wg_operator_view));
   printf("%zu %zu %zu\n", offsetof(wg_server_opts, gummel), offsetof(wg_request, rtd),
          offsetof(wg_request_status, t_submit));
+  printf("%zu %zu\n", sizeof(wg_runtime_stats), offsetof(wg_runtime_stats, stencil_cells));
   return 0;
 }''')
     exe = tmp_path / "probe"
@@ -70,7 +71,8 @@ int main(void) {
             C.sizeof(_lib.WgTransientOpts), C.sizeof(_lib.WgTransientInfo),
             C.sizeof(_lib.WgServerOpts), C.sizeof(_lib.WgRequest), C.sizeof(_lib.WgRequestStatus),
             C.sizeof(_lib.WgServerStats), C.sizeof(_lib.WgOperatorView),
-            _lib.WgServerOpts.gummel.offset, _lib.WgRequest.rtd.offset, _lib.WgRequestStatus.t_submit.offset]
+            _lib.WgServerOpts.gummel.offset, _lib.WgRequest.rtd.offset, _lib.WgRequestStatus.t_submit.offset,
+            C.sizeof(_lib.WgRuntimeStats), _lib.WgRuntimeStats.stencil_cells.offset]
     assert got == want
 
 
