@@ -541,6 +541,97 @@ def run_fet(args):
     return out
 
 
+FULL2D = dict(length_nm=90.0, width_nm=3.0, nx=361, ny=13, n_el_x=120, nk_x=3, n_el_y=2, nk_y=3, n_rho_x=121,
+              n_rho_y=12, l_rho_x=1e-7, me_x_ch=0.063, quad=5)
+
+
+def full2d_case(cfg=FULL2D):
+    """The Full-2D operator of the shape of the reference's recorded run (2026-10-28_08-47:
+    90 nm x 3 nm RTD, p=2 in X and Y, 120 x 2 elements, 121 x 12 relative cells, periodic Y,
+    upwind fluxes, FV-consistent potential; 3,136,320 complex unknowns) on a seeded synthetic
+    double-barrier potential (0.3 eV barriers, a linear 0.2 V drop, a weak Y modulation)."""
+    x = np.linspace(0.0, cfg["length_nm"], cfg["nx"])
+    y = np.linspace(0.0, cfg["width_nm"], cfg["ny"])
+    prm = dict(N_K_X=cfg["nk_x"], N_K_Y=cfg["nk_y"], N_el_X=cfg["n_el_x"], N_el_Y=cfg["n_el_y"],
+               N_rho_x=cfg["n_rho_x"], N_rho_y=cfg["n_rho_y"], L_rho_x=cfg["l_rho_x"], full2D_X_flux="upwind",
+               full2D_Y_flux="upwind", full2D_Y_boundary="periodic", full2D_potentialQuadratureOrder=cfg["quad"])
+    mat = dict(x=x, y=y, Nx=len(x), Ny=len(y), me_x_ch=cfg["me_x_ch"], dg=dict(params=prm))
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    c = cfg["length_nm"] / 2
+    barrier = 0.3 * (((X > c - 6.5) & (X < c - 2.5)) | ((X > c + 2.5) & (X < c + 6.5)))
+    V = barrier - 0.2 * np.clip((X - 20.0) / (cfg["length_nm"] - 40.0), 0, 1) \
+        + 0.005 * np.cos(2 * np.pi * Y / cfg["width_nm"])
+    return mat, V
+
+
+def full2d_flops(f, n):
+    """Algorithmic FP64 flops of one apply from the host factors (complex MAC = 8 flops,
+    real x complex = 4): centre factors 3 nk per entry and term, relative factors nnz per row,
+    potential interpolation + projection 2 nq n_local per element entry, the vertex stencil."""
+    s = f["shape"]
+    fl = 0.0
+    for axis, nk, nr in ((0, s["nk_x"], s["n_rho_x"]), (1, s["nk_y"], s["n_rho_y"])):
+        for _, _, R in f["terms"][axis]:
+            fl += n * (3 * nk * 4 + 8 * np.count_nonzero(R) / nr)
+    nloc = s["nk_x"] * s["nk_y"]
+    fl += n / nloc * f["nq"] * (2 * nloc * 4 + 4 * 2 + 16 * 2)
+    return fl
+
+
+def run_full2d(args):
+    """Full-2D operator applies/s (a9: applyKronOperator + FV-consistent potential + CAP, FP64)."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300.full2d import Full2DOperator
+    mat, V = full2d_case()
+    op = Full2DOperator(mat, V)
+    n = op.n
+    for _ in range(args.warmup):
+        op.apply_time(1)
+    clocks = ClockSampler()
+    clocks.start()
+    steps = max(10, args.steps)
+    ms, parts = op.apply_time(steps)
+    clk = clocks.stop()
+    fl = full2d_flops(op.factors, n)
+    u = (np.sin(np.arange(n) * 1.3) + 1j * np.cos(np.arange(n) * 0.7)).astype(complex)
+    op.apply(u)
+    t0 = time.perf_counter()
+    ne = 3
+    for _ in range(ne):
+        op.apply(u)
+    e2e_s = (time.perf_counter() - t0) / ne
+    op.close()
+    peak = 1.25
+    out = {"metric": "Full-2D operator applies/s (3,136,320 complex unknowns, FP64)", "value": round(1000.0 / ms, 3),
+           "unit": "applies/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic double-barrier potential on the grid of the reference's recorded Full-2D run",
+           "config": {"workload": "Full-2D apply: X 120 el x p=2, Y 2 el x p=2 periodic, rho 121 x 12, upwind, "
+                                  "FV-consistent potential (5 x 5 quadrature), CAP", "unknowns": n,
+                      "l2": "state 50 MB and intermediates 0.4 GB, larger than L2"},
+           "roofline": {"kernel": "full2d_apply", "bound": "fp64", "achieved": round(fl / ms / 1e9, 3), "peak": peak,
+                        "unit": "TFLOP/s", "frac": round(fl / ms / 1e9 / peak, 4), "traffic": None,
+                        "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)",
+                        "flops_per_apply": fl},
+           "parts_ms": {"transport": round(float(parts[0]), 4), "potential_and_cap": round(float(parts[1]), 4)},
+           "e2e": {"value": round(1.0 / e2e_s, 3), "unit": "applies/s", "h2d_bytes_per_step": 16 * n,
+                   "d2h_bytes_per_step": 16 * n},
+           "gpu_launches": 9, "clocks": clk}
+    if not args.no_cpu:
+        from oracle import full2d as F2
+        t0 = time.perf_counter()
+        p, partsk, dd = F2.system(mat, V)
+        t1 = time.perf_counter()
+        F2.apply_system(p, partsk, dd, u)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"value": round(1.0 / (t2 - t1), 5), "unit": "applies/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "one oracle apply (scipy.sparse Kronecker parts + the "
+                               "element loop of the FV potential) at the full size, %.1f s; set-up %.1f s"
+                               % (t2 - t1, t1 - t0)}
+    return out
+
+
 def run_apply(args):
     """Operator applies/s on the C2 batch: the FP64 operator (plain form), the mixed form's
     low-precision inner operator and its tensor-core FP64 operator, with per-kernel rooflines."""
@@ -573,10 +664,10 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c4"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c4", "full2d"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
-                         "c4: multi-subband FET gate sweep")
+                         "c4: multi-subband FET gate sweep; full2d: Full-2D operator applies/s")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -610,6 +701,8 @@ def main():
         out = run_apply(args) if rank == 0 else None
     elif args.workload == "c4":
         out = run_fet(args) if rank == 0 else None
+    elif args.workload == "full2d":
+        out = run_full2d(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

@@ -407,6 +407,59 @@ int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* laun
 int wg_event_record(wg_problem* h, int slot);
 int wg_event_elapsed(wg_problem* h, int a, int b, double* ms);
 
+/* ------------------------------------------------------------------------------------------------
+ * Full-2D (X, Y, rho_x, rho_y) matrix-free operator: the device-resident apply that
+ * sysInfo.makeGPUApply() returns (DG_code/core/get_SysM_full2D.m:81, 124-139):
+ *   y = sum_parts c (R U) C^T           (applyKronOperator, get_Diff_full2D.m:618-639)
+ *     + CAP + FV-consistent potential   (applyFVConsistentDrift, get_Drift_full2D.m:331-364).
+ * State order F(i_rho_x, i_rho_y, i_X, i_Y), rho_x fastest (complex interleaved FP64).
+ * The host builds the one-dimensional factors once (as the reference does before
+ * makeGPUApply) and hands them over; every apply runs on the device.
+ * ------------------------------------------------------------------------------------------------ */
+typedef struct wg2d_problem wg2d_problem;
+
+typedef struct {
+  int n_el_x, nk_x;         /* centre DG along X: elements, local nodes */
+  int n_el_y, nk_y;         /* centre DG along Y */
+  int n_rho_x, n_rho_y;     /* relative FV cells */
+  int periodic_y;           /* 1: the Y element chain is closed (core/close_PeriodicDGAxis_full2D.m) */
+  int n_quad;               /* potential quadrature points per centre element */
+} wg2d_shape;
+
+int wg2d_create(const wg2d_shape* s, wg2d_problem** out);
+int wg2d_destroy(wg2d_problem* h);
+const char* wg2d_last_error(const wg2d_problem* h);
+
+/* Transport terms of one axis (0: X with rho_x, 1: Y with rho_y): y += sum_t coef[t] (C_t along the
+ * centre axis) (R_t along the relative axis), i.e. the parts kron(I_Y, C_X) x kron(I_rho_y, R_x) and
+ * kron(C_Y, I_X) x kron(R_y, I_rho_x) of get_Diff_full2D.m:76-146.  C_t: element blocks
+ * [n_el][3][nk][nk] (coupling to element e-1, e, e+1; row-major nk x nk; the neighbours of the first
+ * and last element wrap when the axis is periodic and are ignored otherwise).  R_t: CSR
+ * (row_ptr [n_rho+1], col [nnz_t], complex values [nnz_t]) for each term, concatenated.
+ * Replaces the terms of that axis. */
+int wg2d_set_transport(wg2d_problem* h, int axis, int n_terms, const double* coef, const double* center_blocks,
+                       const int* row_ptr, const int* col, const double* val);
+
+/* Potential and CAP (get_Drift_full2D.m:133-300): interp [n_quad][n_local] (DG values at the
+ * element quadrature points), proj [n_quad][n_local] (quadrature weights times the inverse local mass),
+ * the quadrature coordinates xq, yq [n_elements][n_quad] (m), the relative vertex coordinates
+ * vx, vy [n_vert] (m; n_vert = (n_rho_x+1)(n_rho_y+1), or (n_rho_x+1) n_rho_y when periodic),
+ * the complex potential coefficient pot (i Q_drift scale), the real CAP coefficient and profile
+ * cap [n_rho_x n_rho_y]. */
+int wg2d_set_drift(wg2d_problem* h, const double* interp, const double* proj, const double* xq, const double* yq,
+                   const double* vx, const double* vy, const double* pot, double cap_coef, const double* cap);
+
+/* Potential V on the material grid gx [nx] x gy [ny] (m, ascending; V column-major, x fastest):
+ * rebuilds the vertex potential differences V(X + rho/2) - V(X - rho/2) on the device with X clamped
+ * and Y clamped or wrapped (get_Drift_full2D.m:620-666). */
+int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const double* gy, const double* V);
+
+/* y = A x on host buffers (n = n_rho_x n_rho_y n_X n_Y complex entries). */
+int wg2d_apply(wg2d_problem* h, const double* x, double* y);
+/* Diagnostic: n applies to the resident device state; mean time of one apply in *ms, with the time
+ * of its transport and potential kernels in parts_ms[0..1] (may be NULL). */
+int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms);
+
 #ifdef __cplusplus
 }
 #endif

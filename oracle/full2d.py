@@ -1,0 +1,420 @@
+"""CPU restatement of the reference's Full-2D (X, Y, rho_x, rho_y) operator -- ORACLE.
+
+Test infrastructure only: imported by tests/ (and nothing in the product).  It
+restates, with scipy.sparse, how the reference assembles and applies the
+stationary Full-2D Wigner operator A = A_diff + G_drift:
+
+  - grids and element matrices: DG_code/initParams_full2D.m:27-118 (makeRectDGAxis
+    :167-214, makeFVRelativeAxis :216-230), the periodic rho_y derivative :90-96;
+  - transport: DG_code/core/get_Diff_full2D.m:76-146 (operator parts), :206-265
+    (oneDimensionalDGOperators), :268-293 (liftCenterOperators), :295-347
+    (relativeTransportOperators), :718-730 (splitCharacteristicMatrix), :732-755
+    (transportScales), :618-639 (applyKronOperator), :486-493 (assembly),
+    core/close_PeriodicDGAxis_full2D.m (periodic Y seam), core/get_SpecularReflection_full2D.m
+    and get_Diff_full2D.m:433-444 (specular Y walls);
+  - potential and CAP: DG_code/core/get_Drift_full2D.m:133-170 (driftData),
+    :172-209 (addFVConsistentData), :211-300 (centerProjectionData), :331-364
+    (applyFVConsistentDrift), :413-451 (assembly), :620-666 (potential differences
+    with independent clamping / periodic wrapping, linear interpolation),
+    core/get_CAP_full2D.m, core/get_CAP.m.
+
+Scope: the source/drain faces fully open (all contact-mask entries 1, so no
+closed-face reflection parts); Y boundaries 'periodic', 'zero-inflow' or
+'specular'; constant-mass transport; FV-consistent potential.  The reservoir
+right-hand side (get_ContactModeReservoirRho_full2D.m) is not part of the operator.
+"""
+import numpy as np
+import scipy.sparse as sp
+
+from .jacobi import dmatrix1d, jacobi_gl, vandermonde1d
+
+HBAR = 1.054571817e-34
+M0 = 9.1093837015e-31
+QE = 1.602176634e-19
+
+
+def _param(prm, name, default):
+    v = prm.get(name, None)
+    return default if v is None else v
+
+
+def make_rect_dg_axis(coord, n_local, n_elements):
+    """initParams_full2D.m:167-214."""
+    r, w = jacobi_gl(0.0, 0.0, n_local - 1)
+    V = vandermonde1d(n_local - 1, r)
+    invV = np.linalg.inv(V)
+    M = invV.T @ invV
+    Dr = dmatrix1d(n_local - 1, r, V)
+    S = M @ Dr
+    vertices = np.linspace(coord[0], coord[-1], n_elements + 1)
+    jac = (vertices[1:] - vertices[:-1]) / 2
+    nodes = ((vertices[:-1] + vertices[1:])[:, None] / 2 + jac[:, None] * r[None, :]).ravel()
+    return dict(nLocal=n_local, nElements=n_elements, nDof=n_elements * n_local, r=r, w=w, V=V, M=M, Dr=Dr,
+                S=S, vertices=vertices, nodes=nodes, jacobian=jac)
+
+
+def make_fv_relative_axis(n_cells, length):
+    """initParams_full2D.m:216-230: cell centres and the central-difference derivative."""
+    edges = np.linspace(-length / 2, length / 2, n_cells + 1)
+    cells = 0.5 * (edges[:-1] + edges[1:])
+    delta = edges[1] - edges[0]
+    D = sp.diags([-np.ones(n_cells - 1) / (2 * delta), np.ones(n_cells - 1) / (2 * delta)], [-1, 1],
+                 shape=(n_cells, n_cells), format="csr")
+    return dict(nCells=n_cells, length=length, edges=edges, cells=cells, delta=delta, D=D)
+
+
+def init_params_full2d(mat):
+    """The fields of initParams_full2D.m that the operator uses (coordinates in m)."""
+    prm = mat["dg"]["params"]
+    scale = _param(prm, "full2D_coordinate_scale", 1e-9)
+    x = np.asarray(mat["x"], dtype=float) * scale
+    y = np.asarray(mat["y"], dtype=float) * scale
+    nk_def = _param(prm, "N_K_chi", 3)
+    nkx, nky = int(_param(prm, "N_K_X", nk_def)), int(_param(prm, "N_K_Y", nk_def))
+    nex = int(_param(prm, "N_el_X", (len(x) - 1) // (nkx - 1)))
+    ney = int(_param(prm, "N_el_Y", (len(y) - 1) // (nky - 1)))
+    p = {"coordinateScale": scale, "x": x, "y": y}
+    p["X"] = make_rect_dg_axis(x, nkx, nex)
+    p["Y"] = make_rect_dg_axis(y, nky, ney)
+    p["nCenterDof"] = p["X"]["nDof"] * p["Y"]["nDof"]
+    nrx = int(_param(prm, "N_rho_x", _param(prm, "N_xi", 40)))
+    nry = int(_param(prm, "N_rho_y", nrx))
+    ldef = _param(prm, "Ly", max(abs(y[-1] - y[0]), np.finfo(float).eps))
+    lrx = float(_param(prm, "L_rho_x", ldef))
+    lry = float(_param(prm, "L_rho_y", ldef))
+    ytype = y_boundary_type(mat)
+    periodic = ytype == "periodic"
+    if periodic:
+        lry = float(_param(prm, "L_rho_y", 2 * (y[-1] - y[0])))
+    p["rhoX"] = make_fv_relative_axis(nrx, lrx)
+    p["rhoY"] = make_fv_relative_axis(nry, lry)
+    p["rhoY"]["periodic"] = periodic
+    if periodic:                      # initParams_full2D.m:90-96
+        d = p["rhoY"]["delta"]
+        p["rhoY"]["D"] = (p["rhoY"]["D"] + sp.csr_matrix(([-1 / (2 * d), 1 / (2 * d)], ([0, nry - 1], [nry - 1, 0])),
+                                                           shape=(nry, nry))).tocsr()
+    p["nRelative"] = nrx * nry
+    p["nTotal"] = p["nRelative"] * p["nCenterDof"]
+    p["Ax1D"] = -1j * p["rhoX"]["D"]
+    p["Ay1D"] = -1j * p["rhoY"]["D"]
+    p["Ax"] = sp.kron(sp.identity(nry), p["Ax1D"], format="csr")
+    p["Ay"] = sp.kron(p["Ay1D"], sp.identity(nrx), format="csr")
+    p["ytype"] = ytype
+    return p
+
+
+def y_boundary_type(mat):
+    """core/get_YBoundaryType_full2D.m (default 'specular')."""
+    v = str(mat["dg"]["params"].get("full2D_Y_boundary", "specular")).strip().lower()
+    return {"specular-reflection": "specular", "reflection": "specular", "reflecting": "specular",
+            "zero_inflow": "zero-inflow", "zeroinflow": "zero-inflow", "zero": "zero-inflow"}.get(v, v)
+
+
+def one_dimensional_dg_operators(ax):
+    """get_Diff_full2D.m:206-265."""
+    n, ne, nd = ax["nLocal"], ax["nElements"], ax["nDof"]
+    invM = np.linalg.inv(ax["M"])
+    P1 = np.zeros((n, n)); P1[0, 0] = 1
+    P2 = np.zeros((n, n)); P2[0, n - 1] = 1
+    P3 = np.zeros((n, n)); P3[n - 1, n - 1] = 1
+    P4 = np.zeros((n, n)); P4[n - 1, 0] = 1
+    K1 = invM @ (ax["S"] + 0.5 * P1 - 0.5 * P3)
+    K2 = invM @ (0.5 * P1 + 0.5 * P3)
+    K2L = invM @ (0.5 * P1)
+    K2R = invM @ (0.5 * P3)
+    K3 = -0.5 * invM @ P2
+    K4 = K3
+    K5 = 0.5 * invM @ P4
+    K6 = -K5
+    ij = 1.0 / ax["jacobian"]
+    upper = sp.diags([ij[1:]], [1], shape=(ne, ne))       # spdiags(1./jac, 1): (e, e+1) = 1/jac(e+1)
+    lower = sp.diags([ij[1:]], [-1], shape=(ne, ne))
+    diag = sp.diags([ij], [0], shape=(ne, ne))
+    H1 = sp.kron(upper, K5) + sp.kron(lower, K3) + sp.kron(diag, K1)
+    H2 = sp.kron(upper, K6) + sp.kron(lower, K4) + sp.kron(diag, K2)
+    left_el = sp.csr_matrix(([1.0], ([0], [0])), shape=(ne, ne))
+    right_el = sp.csr_matrix(([1.0], ([ne - 1], [ne - 1])), shape=(ne, ne))
+    H2B = sp.kron(left_el @ diag, K2L) + sp.kron(right_el @ diag, K2R)
+    left_lift = np.zeros(nd); left_lift[:n] = invM[:, 0] / ax["jacobian"][0]
+    right_lift = np.zeros(nd); right_lift[nd - n:] = invM[:, n - 1] / ax["jacobian"][-1]
+    left_trace = np.zeros(nd); left_trace[0] = 1
+    right_trace = np.zeros(nd); right_trace[nd - 1] = 1
+    return {"H1": sp.csr_matrix(H1), "H2": sp.csr_matrix(H2), "H2Boundary": sp.csr_matrix(H2B),
+            "H2Interior": sp.csr_matrix(H2 - H2B),
+            "leftBoundary": sp.csr_matrix(np.outer(left_lift, left_trace)),
+            "rightBoundary": sp.csr_matrix(np.outer(right_lift, right_trace)),
+            "leftLift": left_lift, "rightLift": right_lift, "nDof": nd}
+
+
+def close_periodic_dg_axis(ops):
+    """core/close_PeriodicDGAxis_full2D.m."""
+    n = ops["nDof"]
+    left = np.zeros(n); left[0] = 1
+    right = np.zeros(n); right[n - 1] = 1
+    out = dict(ops)
+    out["H1"] = sp.csr_matrix(ops["H1"] - 0.5 * np.outer(ops["leftLift"], right) + 0.5 * np.outer(ops["rightLift"], left))
+    seam = 0.5 * np.outer(ops["leftLift"] - ops["rightLift"], left - right)
+    out["H2Interior"] = sp.csr_matrix(ops["H2Interior"] + seam)
+    out["H2Boundary"] = sp.csr_matrix((n, n))
+    out["H2"] = out["H2Interior"]
+    return out
+
+
+def split_characteristic(A, tol=1e-12):
+    """get_Diff_full2D.m:718-730: A = Phi Lambda Phi^-1, A+ / A- from the signs of Lambda."""
+    lam, Phi = np.linalg.eig(np.asarray(A.todense() if sp.issparse(A) else A))
+    lp = lam.copy(); lp[lp.real <= tol] = 0
+    lm = lam.copy(); lm[lm.real >= -tol] = 0
+    Pinv = np.linalg.solve(Phi, np.eye(Phi.shape[0]))
+    Ap = Phi @ np.diag(lp) @ Pinv
+    Am = Phi @ np.diag(lm) @ Pinv
+    Ap[np.abs(Ap) < 1e-12] = 0
+    Am[np.abs(Am) < 1e-12] = 0
+    return Ap, Am, lam
+
+
+def flux_types(mat):
+    """get_Diff_full2D.m:54-61 with the normalisations of :349-391."""
+    prm = mat["dg"]["params"]
+    general = str(_param(prm, "full2D_fluxType", _param(prm, "rho_flux", _param(prm, "fluxType", "rusanov")))).lower()
+    general = "rusanov" if general in ("lf", "lax-friedrichs", "rusanov-local") else general
+
+    def norm(v):
+        v = str(v).strip().lower()
+        if v in ("lf", "lax-friedrichs", "rusanov-local"):
+            return "rusanov"
+        if v in ("matrix-upwind", "characteristic-upwind"):
+            return "upwind"
+        return v
+    fx = norm(_param(prm, "full2D_X_flux", general))
+    fy = norm(_param(prm, "full2D_Y_flux", fx))
+    return fx, fy
+
+
+def transport_scales(mat):
+    """get_Diff_full2D.m:732-755 (constant mass)."""
+    prm = mat["dg"]["params"]
+
+    def kg(m):
+        mk = m * M0 if abs(m) > 1e-25 else m
+        return mk if mk > 0 else 0.041 * M0
+    mex = mat.get("me_x_ch", 0.041)
+    mey = mat.get("me_y_ch", mex)
+    sx = _param(prm, "full2D_Q_diff_x", _param(prm, "full2D_transportScaleX", HBAR / kg(mex)))
+    sy = _param(prm, "full2D_Q_diff_y", _param(prm, "full2D_transportScaleY", HBAR / kg(mey)))
+    f = _param(prm, "full2D_diff_scale", _param(prm, "rho_diff_scale", 1.0))
+    return f * sx, f * sy
+
+
+def diff_operator_parts(mat, p):
+    """[(name, coefficient, centre matrix, relative matrix)] of get_Diff_full2D.m:76-146."""
+    prm = mat["dg"]["params"]
+    fx, fy = flux_types(mat)
+    ox = one_dimensional_dg_operators(p["X"])
+    oy = one_dimensional_dg_operators(p["Y"])
+    if p["ytype"] == "periodic":
+        oy = close_periodic_dg_axis(oy)
+    IX, IY = sp.identity(p["X"]["nDof"]), sp.identity(p["Y"]["nDof"])
+    nrx, nry = p["rhoX"]["nCells"], p["rhoY"]["nCells"]
+    Irx, Iry = sp.identity(nrx), sp.identity(nry)
+    tol = _param(prm, "full2D_characteristicTol", 1e-12)
+    Apx, Amx, lx = split_characteristic(p["Ax1D"], tol)
+    Apy, Amy, ly = split_characteristic(p["Ay1D"], tol)
+    theta_def = 0.01
+    tx = _param(prm, "full2D_thetaLF_X", _param(prm, "full2D_thetaLF", _param(prm, "thetaLF", theta_def))) \
+        if fx == "rusanov" else 0.0
+    ty = _param(prm, "full2D_thetaLF_Y", _param(prm, "full2D_thetaLF", _param(prm, "thetaLF", theta_def))) \
+        if fy == "rusanov" else 0.0
+    bx = tx * _param(prm, "full2D_alphaLF_X", np.max(np.abs(lx)))
+    by = ty * _param(prm, "full2D_alphaLF_Y", np.max(np.abs(ly)))
+    absx = sp.kron(Iry, sp.csr_matrix(Apx - Amx))
+    absy = sp.kron(sp.csr_matrix(Apy - Amy), Irx)
+    IR = sp.identity(nrx * nry)
+    sx, sy = transport_scales(mat)
+    parts = [("X central", sx, sp.kron(IY, ox["H1"]), p["Ax"])]
+    if fx == "upwind":
+        parts.append(("X interior upwind", sx, sp.kron(IY, ox["H2Interior"]), absx))
+    elif bx != 0:
+        parts.append(("X interior Rusanov", sx, sp.kron(IY, ox["H2Interior"]), bx * IR))
+    parts.append(("X boundary penalty", sx, sp.kron(IY, ox["H2Boundary"]), absx))
+    parts.append(("Y central", sy, sp.kron(oy["H1"], IX), p["Ay"]))
+    if fy == "upwind":
+        parts.append(("Y interior upwind", sy, sp.kron(oy["H2Interior"], IX), absy))
+    elif by != 0:
+        parts.append(("Y interior Rusanov", sy, sp.kron(oy["H2Interior"], IX), by * IR))
+    if p["ytype"] not in ("hard-wall", "periodic"):
+        parts.append(("Y boundary penalty", sy, sp.kron(oy["H2Boundary"], IX), absy))
+    if p["ytype"] == "specular":
+        flip = sp.csr_matrix(np.fliplr(np.eye(nry)))
+        Ry = sp.kron(flip, Irx)
+        parts.append(("Y bottom specular", -sy, sp.kron(oy["leftBoundary"], IX),
+                      sp.kron(sp.csr_matrix(Apy), Irx) @ Ry))
+        parts.append(("Y top specular", sy, sp.kron(oy["rightBoundary"], IX),
+                      sp.kron(sp.csr_matrix(Amy), Irx) @ Ry))
+    return [(n, c, sp.csr_matrix(C), sp.csr_matrix(R)) for n, c, C, R in parts if c != 0 and C.nnz and R.nnz]
+
+
+def apply_kron(parts, u, n_center, n_relative):
+    """applyKronOperator (get_Diff_full2D.m:618-639): Y = sum c (R U) C^T."""
+    U = np.asarray(u).reshape(n_center, n_relative).T        # column-major reshape(u, nRel, nCenter)
+    Y = np.zeros_like(U, dtype=complex)
+    for _, c, C, R in parts:
+        Y += c * (C @ (R @ U).T).T
+    return Y.T.reshape(-1)
+
+
+def assemble_kron(parts, n_center, n_relative):
+    """assembleKronOperator (get_Diff_full2D.m:486-493): sum c kron(C, R)."""
+    A = sp.csr_matrix((n_center * n_relative, n_center * n_relative), dtype=complex)
+    for _, c, C, R in parts:
+        A = A + c * sp.kron(C, R, format="csr")
+    return A
+
+
+# ----------------------------------------------------------------------------- potential and CAP
+
+def cap_profile(p):
+    """core/get_CAP_full2D.m: C_rho = kron(I_y, C_x) + kron(C_y, I_x) (no C_y for periodic rho_y)."""
+    from .dg1d import get_cap
+    wx = get_cap(p["rhoX"]["cells"], p["rhoX"]["length"], p["rhoX"]["delta"])
+    wy = get_cap(p["rhoY"]["cells"], p["rhoY"]["length"], p["rhoY"]["delta"])
+    if p["rhoY"]["periodic"]:
+        wy = np.zeros_like(wy)
+    nrx, nry = len(wx), len(wy)
+    return (np.tile(wx, nry) + np.repeat(wy, nrx)).astype(float)
+
+
+def center_projection_data(mat, p):
+    """get_Drift_full2D.m:211-300."""
+    prm = mat["dg"]["params"]
+    nlx, nly = p["X"]["nLocal"], p["Y"]["nLocal"]
+    common = prm.get("full2D_potentialQuadratureOrder", None)
+    if common is None:
+        nqx = _param(prm, "full2D_potentialQuadratureX", max(4, 2 * nlx - 1))
+        nqy = _param(prm, "full2D_potentialQuadratureY", max(4, 2 * nly - 1))
+    else:
+        nqx = nqy = common
+    nqx, nqy = max(nlx, int(round(nqx))), max(nly, int(round(nqy)))
+    qx, wx = jacobi_gl(0.0, 0.0, nqx - 1)
+    qy, wy = jacobi_gl(0.0, 0.0, nqy - 1)
+    Ix = vandermonde1d(nlx - 1, qx) @ np.linalg.inv(p["X"]["V"])
+    Iy = vandermonde1d(nly - 1, qy) @ np.linalg.inv(p["Y"]["V"])
+    interp = np.kron(Iy, Ix)
+    w = np.kron(wy, wx)
+    MXY = np.kron(p["Y"]["M"], p["X"]["M"])
+    invM = np.linalg.solve(MXY, np.eye(MXY.shape[0]))
+    proj = (interp * w[:, None]) @ invM.T
+    nex, ney = p["X"]["nElements"], p["Y"]["nElements"]
+    ids, XQ, YQ = [], [], []
+    for ey in range(ney):
+        yq = 0.5 * (p["Y"]["vertices"][ey] + p["Y"]["vertices"][ey + 1]) + p["Y"]["jacobian"][ey] * qy
+        yid = ey * nly + np.arange(nly)
+        for ex in range(nex):
+            xq = 0.5 * (p["X"]["vertices"][ex] + p["X"]["vertices"][ex + 1]) + p["X"]["jacobian"][ex] * qx
+            xid = ex * nlx + np.arange(nlx)
+            lx_, ly_ = np.meshgrid(xid, yid, indexing="ij")
+            ids.append((lx_ + ly_ * p["X"]["nDof"]).ravel(order="F"))
+            Xq, Yq = np.meshgrid(xq, yq, indexing="ij")
+            XQ.append(Xq.ravel(order="F"))
+            YQ.append(Yq.ravel(order="F"))
+    return dict(interp=interp, proj=proj, ids=np.array(ids).T, XQ=np.array(XQ).T, YQ=np.array(YQ).T,
+                nq=len(w), nlocal=nlx * nly)
+
+
+def relative_projection(p):
+    """get_Drift_full2D.m:175-196: P = kron(Ey, Ex) sums the cells around each vertex."""
+    nx, ny = p["rhoX"]["nCells"], p["rhoY"]["nCells"]
+    Ex = sp.diags([np.ones(nx), np.ones(nx)], [0, -1], shape=(nx + 1, nx))
+    ey_edges = p["rhoY"]["edges"]
+    if p["rhoY"]["periodic"]:
+        Ey = sp.identity(ny) + sp.csr_matrix((np.ones(ny), (np.arange(ny), np.r_[ny - 1, np.arange(ny - 1)])),
+                                             shape=(ny, ny))
+        ey_edges = ey_edges[:-1]
+    else:
+        Ey = sp.diags([np.ones(ny), np.ones(ny)], [0, -1], shape=(ny + 1, ny))
+    VX, VY = np.meshgrid(p["rhoX"]["edges"], ey_edges, indexing="ij")
+    return sp.csr_matrix(sp.kron(Ey, Ex)), VX.ravel(order="F"), VY.ravel(order="F")
+
+
+def interp_linear_2d(gx, gy, V, qx, qy):
+    """griddedInterpolant({gx, gy}, V, 'linear') inside the grid (queries pre-clamped)."""
+    ix = np.clip(np.searchsorted(gx, qx, side="right") - 1, 0, len(gx) - 2)
+    iy = np.clip(np.searchsorted(gy, qy, side="right") - 1, 0, len(gy) - 2)
+    tx = (qx - gx[ix]) / (gx[ix + 1] - gx[ix])
+    ty = (qy - gy[iy]) / (gy[iy + 1] - gy[iy])
+    return ((1 - tx) * (1 - ty) * V[ix, iy] + tx * (1 - ty) * V[ix + 1, iy] + (1 - tx) * ty * V[ix, iy + 1]
+            + tx * ty * V[ix + 1, iy + 1])
+
+
+def potential_difference(p, V, cpd, vx, vy):
+    """get_Drift_full2D.m:635-666: V(X + rho/2) - V(X - rho/2) at every relative vertex and
+    centre quadrature point, X clamped, Y clamped or wrapped.  [nVert, nq, nElements]."""
+    gx, gy = p["x"], p["y"]
+
+    def ext(qx, qy):
+        qx = np.clip(qx, gx[0], gx[-1])
+        if p["rhoY"]["periodic"]:
+            qy = gy[0] + np.mod(qy - gy[0], gy[-1] - gy[0])
+        else:
+            qy = np.clip(qy, gy[0], gy[-1])
+        return interp_linear_2d(gx, gy, V, qx, qy)
+    X = cpd["XQ"][None, :, :]
+    Y = cpd["YQ"][None, :, :]
+    rx = 0.5 * vx[:, None, None]
+    ry = 0.5 * vy[:, None, None]
+    return ext(X + rx, Y + ry) - ext(X - rx, Y - ry)
+
+
+def drift_data(mat, p, V):
+    """The FV-consistent drift's data (driftData + addFVConsistentData)."""
+    prm = mat["dg"]["params"]
+    qdrift = _param(prm, "full2D_Q_drift", QE / HBAR)
+    dscale = _param(prm, "full2D_drift_scale", 1.0)
+    cscale = _param(prm, "full2D_cap_scale", 1.0)
+    P, vx, vy = relative_projection(p)
+    cpd = center_projection_data(mat, p)
+    return dict(P=P, cpd=cpd, dV=potential_difference(p, np.asarray(V, dtype=float), cpd, vx, vy),
+                pot=1j * dscale * qdrift, capc=dscale * cscale * qdrift, cap=cap_profile(p))
+
+
+def apply_drift(p, dd, u):
+    """applyFVConsistentDrift (get_Drift_full2D.m:331-364)."""
+    nrel, nc = p["nRelative"], p["nCenterDof"]
+    U = np.asarray(u).reshape(nc, nrel).T
+    Y = dd["capc"] * (dd["cap"][:, None] * U)
+    cpd = dd["cpd"]
+    for e in range(cpd["ids"].shape[1]):
+        ids = cpd["ids"][:, e]
+        Uq = U[:, ids] @ cpd["interp"].T                       # [nRel, nq]
+        vert = dd["P"] @ Uq
+        res = dd["P"].T @ (dd["dV"][:, :, e] * vert)
+        res = dd["pot"] * (1.0 / 16) * res
+        Y[:, ids] += res @ cpd["proj"]
+    return Y.T.reshape(-1)
+
+
+def assemble_drift(p, dd):
+    """assembleFVConsistentMatrix (get_Drift_full2D.m:413-451)."""
+    nrel, nc = p["nRelative"], p["nCenterDof"]
+    cpd = dd["cpd"]
+    G = sp.csr_matrix((nrel * nc, nrel * nc), dtype=complex)
+    for e in range(cpd["ids"].shape[1]):
+        local = sp.csr_matrix((nrel * cpd["nlocal"], nrel * cpd["nlocal"]), dtype=complex)
+        for q in range(cpd["nq"]):
+            Crel = dd["pot"] / 16 * (dd["P"].T @ sp.diags(dd["dV"][:, q, e]) @ dd["P"])
+            H = np.outer(cpd["proj"][q, :], cpd["interp"][q, :])
+            local = local + sp.kron(sp.csr_matrix(H), Crel)
+        gid = (np.arange(nrel)[:, None] + cpd["ids"][:, e][None, :] * nrel).ravel(order="F")
+        coo = local.tocoo()
+        G = G + sp.csr_matrix((coo.data, (gid[coo.row], gid[coo.col])), shape=G.shape)
+    return G + sp.diags(np.tile(dd["capc"] * dd["cap"], nc))
+
+
+def system(mat, V):
+    """(p, parts, drift data): A = sum of the parts + G_drift (get_SysM_full2D.m:124-127)."""
+    p = init_params_full2d(mat)
+    return p, diff_operator_parts(mat, p), drift_data(mat, p, V)
+
+
+def apply_system(p, parts, dd, u):
+    return apply_kron(parts, u, p["nCenterDof"], p["nRelative"]) + apply_drift(p, dd, u)

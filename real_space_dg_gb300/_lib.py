@@ -123,6 +123,11 @@ class WgRuntimeStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class Wg2dShape(C.Structure):
+    _fields_ = [("n_el_x", C.c_int), ("nk_x", C.c_int), ("n_el_y", C.c_int), ("nk_y", C.c_int),
+                ("n_rho_x", C.c_int), ("n_rho_y", C.c_int), ("periodic_y", C.c_int), ("n_quad", C.c_int)]
+
+
 REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
 
 
@@ -146,6 +151,14 @@ SIGNATURES = {
     "wg_problem_sizes": ([_H, C.POINTER(C.c_longlong), C.POINTER(C.c_int), _D], C.c_int),
     "wg_runtime_stats_get": ([_H, C.POINTER(WgRuntimeStats)], C.c_int),
     "wg_set_launch_shapes": ([_H, C.c_int, C.c_int], C.c_int),
+    "wg2d_create": ([C.POINTER(Wg2dShape), C.POINTER(_H)], C.c_int),
+    "wg2d_destroy": ([_H], C.c_int),
+    "wg2d_last_error": ([_H], C.c_char_p),
+    "wg2d_set_transport": ([_H, C.c_int, C.c_int, _D, _D, C.POINTER(C.c_int), C.POINTER(C.c_int), _D], C.c_int),
+    "wg2d_set_drift": ([_H, _D, _D, _D, _D, _D, _D, _D, C.c_double, _D], C.c_int),
+    "wg2d_set_potential": ([_H, C.c_int, C.c_int, _D, _D, _D], C.c_int),
+    "wg2d_apply": ([_H, _D, _D], C.c_int),
+    "wg2d_apply_repeat": ([_H, C.c_int, _D, _D], C.c_int),
     "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),
     "wg_solve": ([_H, C.POINTER(WgSolveOpts), _D, C.POINTER(WgSolveInfo)], C.c_int),
     "wg_get_rho": ([_H, C.c_int, _D], C.c_int),

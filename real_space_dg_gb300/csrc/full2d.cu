@@ -1,0 +1,659 @@
+// Full-2D (X, Y, rho_x, rho_y) matrix-free Wigner operator on the device (sm_103a).
+//
+// The device-resident apply of get_SysM_full2D.m:81,124-139 (sysInfo.makeGPUApply):
+//   y = G_drift x + sum_parts c (R U) C^T
+// with U the state reshaped [n_rel x n_center] (rho_x fastest, then rho_y, X, Y).
+//
+// Transport (get_Diff_full2D.m:618-639).  Every part of the reference's operator list
+// acts on one centre axis and the matching relative axis only:
+//   X parts: kron(I_Y, C_X) x kron(I_rho_y, R_x),   Y parts: kron(C_Y, I_X) x kron(R_y, I_rho_x),
+// so an axis is a list of terms (c_t, C_t, R_t) with C_t block-tridiagonal over the DG
+// elements (element blocks, wrapped on a periodic axis) and R_t a small CSR matrix on
+// the FV cells (the central derivative, the dense characteristic |A|, ...).
+//   f2d_center_kernel    G_t = F x_axis C_t for all terms (3 nk real MACs per entry);
+//   f2d_relx_kernel      y += sum_t c_t R_t x_rho_x G_t: a column block of G_t staged in
+//                        shared memory, each thread one rho_x row for 8 columns;
+//   f2d_rely_kernel      the same along rho_y (rows of 12-40 cells: one thread per entry).
+//
+// Potential and CAP (applyFVConsistentDrift, get_Drift_full2D.m:331-364), per centre
+// element e and quadrature point q:
+//   f2d_interp_kernel    Uq[e][q][r] = sum_l W[q][l] U[r, id(e,l)]
+//   f2d_vertex_kernel    Rq[e][q][cell] = sum over the cell's 4 vertices v of dV[e][q][v] x
+//                        (sum of Uq over the <= 4 cells around v)   (P^T diag(dV) P)
+//   f2d_project_kernel   y[r, id(e,l)] = pot/16 sum_q Cp[q][l] Rq[e][q][r] + capc cap[r] U[r, id(e,l)]
+//   f2d_dv_kernel        dV from V on the material grid (bilinear, X clamped, Y clamped or wrapped).
+// All arithmetic FP64 (the plain form).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "wigner_gb300.h"
+
+struct wg2d_problem {
+  wg2d_shape s{};
+  int nX = 0, nY = 0, nrx = 0, nry = 0, nrel = 0, ncen = 0, nel = 0, nloc = 0, nq = 0, nvert = 0;
+  long long n = 0;
+  cudaStream_t stream = nullptr;
+  double2* x = nullptr;
+  double2* y = nullptr;
+  struct Axis {
+    int T = 0;
+    std::vector<double> coef;
+    double* blocks = nullptr;   // [T][n_el][3][nk][nk]
+    int* rp = nullptr;          // [T][n_rho + 1]
+    int* col = nullptr;         // concatenated over the terms
+    double2* val = nullptr;
+    int* offs = nullptr;        // [T] start of term t in col / val
+    double* dcoef = nullptr;    // [T]
+  } ax[2];
+  double2* G = nullptr;         // [Tmax][n] centre-applied state
+  int g_terms = 0;
+  // potential
+  double *interp = nullptr, *proj = nullptr, *xq = nullptr, *yq = nullptr, *vx = nullptr, *vy = nullptr,
+         *cap = nullptr, *dV = nullptr;
+  double2 pot = {0, 0};
+  double capc = 0;
+  double2 *Uq = nullptr, *Rq = nullptr;
+  bool drift_ready = false, potential_ready = false;
+  cudaEvent_t ev[4] = {};
+  std::string err;
+};
+
+namespace {
+
+constexpr int kMaxNK = 4;
+constexpr int kMaxTerms = 6;
+constexpr int kRelxCols = 8;
+
+__device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {   // c + a b
+  c.x = fma(a.x, b.x, fma(-a.y, b.y, c.x));
+  c.y = fma(a.x, b.y, fma(a.y, b.x, c.y));
+  return c;
+}
+
+// G_t[r, X, Y] = sum_{e', b} C_t[e][dir][a][b] F[r, X'(e', b), Y] along X (axis 0) or Y (axis 1).
+// grid (ceil(nrel/256), centre dofs of the other axis, n_el * nk of this axis).
+template <int NK>
+__global__ void __launch_bounds__(256) f2d_center_kernel(const double2* __restrict__ F, double2* __restrict__ G,
+                                                         const double* __restrict__ blocks, int T, int axis,
+                                                         int nrel, int nX, int nY, int n_el, int periodic,
+                                                         long long n) {
+  const int r = blockIdx.x * 256 + threadIdx.x;
+  if (r >= nrel) return;
+  const int other = blockIdx.y;        // Y dof (axis 0) or X dof (axis 1)
+  const int d = blockIdx.z;            // dof along the axis = e * NK + a
+  const int e = d / NK, a = d - e * NK;
+  const int stride = axis == 0 ? nrel : nrel * nX;                     // between dofs of this axis
+  const long long base = axis == 0 ? (long long)other * nX * nrel : (long long)other * nrel;
+  double2 f[3][NK];
+  bool has[3];
+#pragma unroll
+  for (int dir = 0; dir < 3; ++dir) {
+    int en = e + dir - 1;
+    has[dir] = true;
+    if (en < 0 || en >= n_el) {
+      if (periodic) en = (en + n_el) % n_el;
+      else has[dir] = false;
+    }
+#pragma unroll
+    for (int b = 0; b < NK; ++b)
+      f[dir][b] = has[dir] ? F[base + (long long)(en * NK + b) * stride + r] : make_double2(0.0, 0.0);
+  }
+  const long long out = base + (long long)d * stride + r;
+  for (int t = 0; t < T; ++t) {
+    const double* B = blocks + ((long long)t * n_el + e) * 3 * NK * NK;
+    double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir)
+#pragma unroll
+      for (int b = 0; b < NK; ++b) {
+        const double c = B[(dir * NK + a) * NK + b];
+        acc.x = fma(c, f[dir][b].x, acc.x);
+        acc.y = fma(c, f[dir][b].y, acc.y);
+      }
+    G[(long long)t * n + out] = acc;
+  }
+}
+
+// y[rx, col] += sum_t c_t sum_k val_t[k] G_t[col_t[k], col] for kRelxCols columns per block;
+// the G_t columns are staged in shared memory, thread rx owns row rx (blockDim = nrx rounded
+// up to a warp multiple, at most 512).
+__global__ void __launch_bounds__(512) f2d_relx_kernel(const double2* __restrict__ G, double2* __restrict__ y,
+                                                       const int* __restrict__ rp, const int* __restrict__ col,
+                                                       const double2* __restrict__ val, const int* __restrict__ nnz_off,
+                                                       const double* __restrict__ coef, int T, int nrx,
+                                                       long long ncols, long long n) {
+  extern __shared__ double2 sg[];       // [kRelxCols][nrx]
+  const long long c0 = (long long)blockIdx.x * kRelxCols;
+  const int nc = (int)min((long long)kRelxCols, ncols - c0);
+  const int rx = threadIdx.x;
+  double2 acc[kRelxCols];
+#pragma unroll
+  for (int j = 0; j < kRelxCols; ++j) acc[j] = make_double2(0.0, 0.0);
+  for (int t = 0; t < T; ++t) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < kRelxCols * nrx; i += blockDim.x) {
+      const int j = i / nrx, k = i - j * nrx;
+      sg[i] = j < nc ? G[(long long)t * n + (c0 + j) * nrx + k] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    if (rx < nrx) {
+      const double ct = coef[t];
+      const int* rpt = rp + t * (nrx + 1);
+      const int off = nnz_off[t];
+      for (int k = rpt[rx]; k < rpt[rx + 1]; ++k) {
+        const int cidx = col[off + k];
+        double2 v = val[off + k];
+        v.x *= ct;
+        v.y *= ct;
+#pragma unroll
+        for (int j = 0; j < kRelxCols; ++j) acc[j] = cfma(v, sg[j * nrx + cidx], acc[j]);
+      }
+    }
+  }
+  if (rx >= nrx) return;
+#pragma unroll
+  for (int j = 0; j < kRelxCols; ++j) {
+    if (j < nc) {
+      double2* o = y + (c0 + j) * nrx + rx;
+      o->x += acc[j].x;
+      o->y += acc[j].y;
+    }
+  }
+}
+
+// y[rx, ry, c] += sum_t c_t sum_k val_t[k] G_t[rx, col_t[k], c]   (one thread per entry)
+__global__ void __launch_bounds__(256) f2d_rely_kernel(const double2* __restrict__ G, double2* __restrict__ y,
+                                                       const int* __restrict__ rp, const int* __restrict__ col,
+                                                       const double2* __restrict__ val, const int* __restrict__ nnz_off,
+                                                       const double* __restrict__ coef, int T, int nrx, int nry,
+                                                       long long n) {
+  const long long i = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (i >= n) return;
+  const int rx = (int)(i % nrx);
+  const long long q = i / nrx;
+  const int ry = (int)(q % nry);
+  const long long c = q / nry;
+  const long long cbase = c * (long long)nrx * nry + rx;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int t = 0; t < T; ++t) {
+    const int* rpt = rp + t * (nry + 1);
+    const int off = nnz_off[t];
+    double2 s = make_double2(0.0, 0.0);
+    for (int k = rpt[ry]; k < rpt[ry + 1]; ++k)
+      s = cfma(val[off + k], G[(long long)t * n + cbase + (long long)col[off + k] * nrx], s);
+    acc.x = fma(coef[t], s.x, acc.x);
+    acc.y = fma(coef[t], s.y, acc.y);
+  }
+  y[i].x += acc.x;
+  y[i].y += acc.y;
+}
+
+// centre dof of local node l of element e (local order X fastest, elements X fastest)
+__device__ __forceinline__ long long center_id(int e, int l, int nex, int nkx, int nky, int nX) {
+  const int ex = e % nex, ey = e / nex;
+  const int lx = l % nkx, ly = l / nkx;
+  return (long long)(ex * nkx + lx) + (long long)nX * (ey * nky + ly);
+}
+
+// Uq[e][q][r] = sum_l W[q][l] F[r, id(e, l)]; grid (ceil(nrel/128), n_el)
+template <int NL>
+__global__ void __launch_bounds__(128) f2d_interp_kernel(const double2* __restrict__ F, double2* __restrict__ Uq,
+                                                         const double* __restrict__ W, int nq, int nrel, int nex,
+                                                         int nkx, int nky, int nX) {
+  const int r = blockIdx.x * 128 + threadIdx.x;
+  const int e = blockIdx.y;
+  if (r >= nrel) return;
+  double2 u[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) u[l] = F[center_id(e, l, nex, nkx, nky, nX) * nrel + r];
+  double2* out = Uq + (long long)e * nq * nrel + r;
+  for (int q = 0; q < nq; ++q) {
+    double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const double w = W[q * NL + l];
+      s.x = fma(w, u[l].x, s.x);
+      s.y = fma(w, u[l].y, s.y);
+    }
+    out[(long long)q * nrel] = s;
+  }
+}
+
+// sum of Uq over the cells around relative vertex (vi, vj) (cells vi-1..vi, vj-1..vj)
+__device__ __forceinline__ double2 vertex_sum(const double2* __restrict__ U, int vi, int vj, int nrx, int nry,
+                                              bool periodic) {
+  double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+  for (int dj = -1; dj <= 0; ++dj) {
+    int j = vj + dj;
+    if (periodic) j = (j + nry) % nry;
+    else if (j < 0 || j >= nry) continue;
+#pragma unroll
+    for (int di = -1; di <= 0; ++di) {
+      const int i = vi + di;
+      if (i < 0 || i >= nrx) continue;
+      const double2 v = U[j * nrx + i];
+      s.x += v.x;
+      s.y += v.y;
+    }
+  }
+  return s;
+}
+
+// Rq[e][q][cell] = sum_{vertices v of cell} dV[e][q][v] vertex_sum(v); grid (ceil(nrel/128), nq, n_el)
+__global__ void __launch_bounds__(128) f2d_vertex_kernel(const double2* __restrict__ Uq, double2* __restrict__ Rq,
+                                                         const double* __restrict__ dV, int nrx, int nry, int nq,
+                                                         int nvert, int periodic) {
+  const int cell = blockIdx.x * 128 + threadIdx.x;
+  const int nrel = nrx * nry;
+  if (cell >= nrel) return;
+  const int q = blockIdx.y, e = blockIdx.z;
+  const long long slab = ((long long)e * nq + q);
+  const double2* U = Uq + slab * nrel;
+  const double* D = dV + slab * nvert;
+  const int i = cell % nrx, j = cell / nrx;
+  const int nvx = nrx + 1;
+  double2 acc = make_double2(0.0, 0.0);
+#pragma unroll
+  for (int b = 0; b <= 1; ++b) {
+    int vj = j + b;
+    if (periodic) vj %= nry;
+#pragma unroll
+    for (int a = 0; a <= 1; ++a) {
+      const int vi = i + a;
+      const double d = D[vj * nvx + vi];
+      const double2 s = vertex_sum(U, vi, vj, nrx, nry, periodic);
+      acc.x = fma(d, s.x, acc.x);
+      acc.y = fma(d, s.y, acc.y);
+    }
+  }
+  Rq[slab * nrel + cell] = acc;
+}
+
+// y[r, id(e,l)] = pot/16 sum_q Cp[q][l] Rq[e][q][r] + capc cap[r] F[r, id(e,l)]; grid (ceil(nrel/128), n_el)
+template <int NL>
+__global__ void __launch_bounds__(128) f2d_project_kernel(const double2* __restrict__ Rq, const double2* __restrict__ F,
+                                                          double2* __restrict__ y, const double* __restrict__ Cp,
+                                                          const double* __restrict__ cap, double2 pot16, double capc,
+                                                          int nq, int nrel, int nex, int nkx, int nky, int nX) {
+  const int r = blockIdx.x * 128 + threadIdx.x;
+  const int e = blockIdx.y;
+  if (r >= nrel) return;
+  double2 s[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) s[l] = make_double2(0.0, 0.0);
+  const double2* R = Rq + (long long)e * nq * nrel + r;
+  for (int q = 0; q < nq; ++q) {
+    const double2 v = R[(long long)q * nrel];
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const double c = Cp[q * NL + l];
+      s[l].x = fma(c, v.x, s[l].x);
+      s[l].y = fma(c, v.y, s[l].y);
+    }
+  }
+  const double cr = capc * cap[r];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) {
+    const long long idx = center_id(e, l, nex, nkx, nky, nX) * nrel + r;
+    const double2 f = F[idx];
+    double2 o;
+    o.x = pot16.x * s[l].x - pot16.y * s[l].y + cr * f.x;
+    o.y = pot16.x * s[l].y + pot16.y * s[l].x + cr * f.y;
+    y[idx] = o;
+  }
+}
+
+// interval i with g[i] <= v < g[i+1] on an ascending grid (v inside [g0, g_last])
+__device__ __forceinline__ int grid_interval(const double* __restrict__ g, int n, double v) {
+  int lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (g[mid] <= v) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ double v_bilinear(const double* __restrict__ gx, const double* __restrict__ gy,
+                             const double* __restrict__ V, int nx, int ny, double qx, double qy, bool periodic) {
+  qx = fmin(fmax(qx, gx[0]), gx[nx - 1]);
+  if (periodic) {
+    const double w = gy[ny - 1] - gy[0];
+    qy = gy[0] + (qy - gy[0] - w * floor((qy - gy[0]) / w));
+    if (qy > gy[ny - 1]) qy = gy[ny - 1];
+  } else {
+    qy = fmin(fmax(qy, gy[0]), gy[ny - 1]);
+  }
+  const int i = grid_interval(gx, nx, qx), j = grid_interval(gy, ny, qy);
+  const double tx = (qx - gx[i]) / (gx[i + 1] - gx[i]);
+  const double ty = (qy - gy[j]) / (gy[j + 1] - gy[j]);
+  const double v00 = V[i + (long long)nx * j], v10 = V[i + 1 + (long long)nx * j];
+  const double v01 = V[i + (long long)nx * (j + 1)], v11 = V[i + 1 + (long long)nx * (j + 1)];
+  return (1 - tx) * (1 - ty) * v00 + tx * (1 - ty) * v10 + (1 - tx) * ty * v01 + tx * ty * v11;
+}
+
+// dV[e][q][v] = V(X_q + rho_v/2) - V(X_q - rho_v/2); grid (ceil(nvert/128), nq, n_el)
+__global__ void __launch_bounds__(128) f2d_dv_kernel(double* __restrict__ dV, const double* __restrict__ xq,
+                                                     const double* __restrict__ yq, const double* __restrict__ vx,
+                                                     const double* __restrict__ vy, const double* __restrict__ gx,
+                                                     const double* __restrict__ gy, const double* __restrict__ V,
+                                                     int nx, int ny, int nq, int nvert, int periodic) {
+  const int v = blockIdx.x * 128 + threadIdx.x;
+  if (v >= nvert) return;
+  const int q = blockIdx.y, e = blockIdx.z;
+  const double X = xq[(long long)e * nq + q], Y = yq[(long long)e * nq + q];
+  const double hx = 0.5 * vx[v], hy = 0.5 * vy[v];
+  dV[((long long)e * nq + q) * nvert + v] = v_bilinear(gx, gy, V, nx, ny, X + hx, Y + hy, periodic) -
+                                            v_bilinear(gx, gy, V, nx, ny, X - hx, Y - hy, periodic);
+}
+
+int fail(wg2d_problem* h, int code, const std::string& msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+#define F2_CK(expr)                                                         \
+  do {                                                                      \
+    cudaError_t e_ = (expr);                                                \
+    if (e_ != cudaSuccess) return fail(h, WG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #expr); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (n ? n : 1));
+}
+
+void free_axis(wg2d_problem::Axis& a) {
+  cudaFree(a.blocks);
+  cudaFree(a.rp);
+  cudaFree(a.col);
+  cudaFree(a.val);
+  cudaFree(a.offs);
+  cudaFree(a.dcoef);
+  a = wg2d_problem::Axis{};
+}
+
+template <int NK>
+void launch_center(wg2d_problem* h, int axis) {
+  const int nk = axis == 0 ? h->s.nk_x : h->s.nk_y;
+  const int n_el = axis == 0 ? h->s.n_el_x : h->s.n_el_y;
+  const int other = axis == 0 ? h->nY : h->nX;
+  const dim3 grid((unsigned)((h->nrel + 255) / 256), (unsigned)other, (unsigned)(n_el * nk));
+  f2d_center_kernel<NK><<<grid, 256, 0, h->stream>>>(h->x, h->G, h->ax[axis].blocks, h->ax[axis].T, axis, h->nrel,
+                                                     h->nX, h->nY, n_el, axis == 1 ? h->s.periodic_y : 0, h->n);
+}
+
+int apply_transport(wg2d_problem* h, int axis) {
+  wg2d_problem::Axis& a = h->ax[axis];
+  if (a.T == 0) return WG_OK;
+  const int nk = axis == 0 ? h->s.nk_x : h->s.nk_y;
+  switch (nk) {
+    case 2: launch_center<2>(h, axis); break;
+    case 3: launch_center<3>(h, axis); break;
+    default: launch_center<4>(h, axis); break;
+  }
+  const int* nnz_off = a.offs;
+  const double* coef = a.dcoef;
+  if (axis == 0) {
+    const long long ncols = h->n / h->nrx;
+    const size_t smem = sizeof(double2) * kRelxCols * h->nrx;
+    const int threads = (h->nrx + 31) / 32 * 32;
+    f2d_relx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+        h->G, h->y, a.rp, a.col, a.val, nnz_off, coef, a.T, h->nrx, ncols, h->n);
+  } else {
+    f2d_rely_kernel<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(h->G, h->y, a.rp, a.col, a.val, nnz_off,
+                                                                          coef, a.T, h->nrx, h->nry, h->n);
+  }
+  F2_CK(cudaGetLastError());
+  return WG_OK;
+}
+
+template <int NL>
+void launch_drift(wg2d_problem* h) {
+  const wg2d_shape& s = h->s;
+  const dim3 g1((unsigned)((h->nrel + 127) / 128), (unsigned)h->nel);
+  f2d_interp_kernel<NL><<<g1, 128, 0, h->stream>>>(h->x, h->Uq, h->interp, h->nq, h->nrel, s.n_el_x, s.nk_x, s.nk_y,
+                                                   h->nX);
+  const dim3 g2((unsigned)((h->nrel + 127) / 128), (unsigned)h->nq, (unsigned)h->nel);
+  f2d_vertex_kernel<<<g2, 128, 0, h->stream>>>(h->Uq, h->Rq, h->dV, h->nrx, h->nry, h->nq, h->nvert, s.periodic_y);
+  double2 pot16 = make_double2(h->pot.x / 16.0, h->pot.y / 16.0);
+  f2d_project_kernel<NL><<<g1, 128, 0, h->stream>>>(h->Rq, h->x, h->y, h->proj, h->cap, pot16, h->capc, h->nq,
+                                                    h->nrel, s.n_el_x, s.nk_x, s.nk_y, h->nX);
+}
+
+int apply_drift(wg2d_problem* h) {
+  switch (h->nloc) {
+    case 4: launch_drift<4>(h); break;
+    case 6: launch_drift<6>(h); break;
+    case 8: launch_drift<8>(h); break;
+    case 9: launch_drift<9>(h); break;
+    case 12: launch_drift<12>(h); break;
+    default: launch_drift<16>(h); break;
+  }
+  F2_CK(cudaGetLastError());
+  return WG_OK;
+}
+
+bool supported_nloc(int n) { return n == 4 || n == 6 || n == 8 || n == 9 || n == 12 || n == 16; }
+
+}  // namespace
+
+extern "C" {
+
+int wg2d_create(const wg2d_shape* s, wg2d_problem** out) {
+  if (!s || !out) return WG_ERR_ARG;
+  *out = nullptr;
+  if (s->n_el_x < 1 || s->n_el_y < 1 || s->nk_x < 2 || s->nk_x > kMaxNK || s->nk_y < 2 || s->nk_y > kMaxNK ||
+      s->n_rho_x < 2 || s->n_rho_x > 512 || s->n_rho_y < 2 || s->n_quad < 1 || !supported_nloc(s->nk_x * s->nk_y))
+    return WG_ERR_ARG;
+  if (s->periodic_y && (s->n_el_y < 2 || s->n_rho_y < 4)) return WG_ERR_ARG;
+  wg2d_problem* h = new wg2d_problem;
+  h->s = *s;
+  h->nX = s->n_el_x * s->nk_x;
+  h->nY = s->n_el_y * s->nk_y;
+  h->nrx = s->n_rho_x;
+  h->nry = s->n_rho_y;
+  h->nrel = h->nrx * h->nry;
+  h->ncen = h->nX * h->nY;
+  h->nel = s->n_el_x * s->n_el_y;
+  h->nloc = s->nk_x * s->nk_y;
+  h->nq = s->n_quad;
+  h->nvert = (h->nrx + 1) * (s->periodic_y ? h->nry : h->nry + 1);
+  h->n = (long long)h->nrel * h->ncen;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  const size_t slab = (size_t)h->nel * h->nq;
+  if (e == cudaSuccess) e = dalloc(&h->x, h->n);
+  if (e == cudaSuccess) e = dalloc(&h->y, h->n);
+  if (e == cudaSuccess) e = dalloc(&h->Uq, slab * h->nrel);
+  if (e == cudaSuccess) e = dalloc(&h->Rq, slab * h->nrel);
+  if (e == cudaSuccess) e = dalloc(&h->dV, slab * h->nvert);
+  if (e == cudaSuccess) e = dalloc(&h->interp, (size_t)h->nq * h->nloc);
+  if (e == cudaSuccess) e = dalloc(&h->proj, (size_t)h->nq * h->nloc);
+  if (e == cudaSuccess) e = dalloc(&h->xq, slab);
+  if (e == cudaSuccess) e = dalloc(&h->yq, slab);
+  if (e == cudaSuccess) e = dalloc(&h->vx, h->nvert);
+  if (e == cudaSuccess) e = dalloc(&h->vy, h->nvert);
+  if (e == cudaSuccess) e = dalloc(&h->cap, h->nrel);
+  for (cudaEvent_t& ev : h->ev)
+    if (e == cudaSuccess) e = cudaEventCreate(&ev);
+  if (e == cudaSuccess && h->nrx * kRelxCols * sizeof(double2) > 48 * 1024)
+    e = cudaFuncSetAttribute(f2d_relx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(h->nrx * kRelxCols * sizeof(double2)));
+  if (e != cudaSuccess) {
+    wg2d_destroy(h);
+    return e == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
+  }
+  *out = h;
+  return WG_OK;
+}
+
+int wg2d_destroy(wg2d_problem* h) {
+  if (!h) return WG_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (auto& a : h->ax) free_axis(a);
+  void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (cudaEvent_t ev : h->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return WG_OK;
+}
+
+const char* wg2d_last_error(const wg2d_problem* h) { return h ? h->err.c_str() : "null handle"; }
+
+int wg2d_set_transport(wg2d_problem* h, int axis, int n_terms, const double* coef, const double* center_blocks,
+                       const int* row_ptr, const int* col, const double* val) {
+  if (!h) return WG_ERR_ARG;
+  if (axis < 0 || axis > 1 || n_terms < 0 || n_terms > kMaxTerms || (n_terms && (!coef || !center_blocks ||
+                                                                                   !row_ptr || !col || !val)))
+    return fail(h, WG_ERR_ARG, "wg2d_set_transport: axis 0/1, 0 .. 6 terms, non-null arrays");
+  const int nk = axis == 0 ? h->s.nk_x : h->s.nk_y, n_el = axis == 0 ? h->s.n_el_x : h->s.n_el_y;
+  const int nr = axis == 0 ? h->nrx : h->nry;
+  std::vector<int> off(n_terms + 1, 0);
+  for (int t = 0; t < n_terms; ++t) {
+    const int* rp = row_ptr + t * (nr + 1);
+    if (rp[0] != 0) return fail(h, WG_ERR_ARG, "wg2d_set_transport: row_ptr must start at 0");
+    for (int i = 0; i < nr; ++i)
+      if (rp[i + 1] < rp[i]) return fail(h, WG_ERR_ARG, "wg2d_set_transport: row_ptr must not decrease");
+    off[t + 1] = off[t] + rp[nr];
+  }
+  for (int k = 0; k < off[n_terms]; ++k)
+    if (col[k] < 0 || col[k] >= nr) return fail(h, WG_ERR_ARG, "wg2d_set_transport: column index out of range");
+  cudaStreamSynchronize(h->stream);
+  wg2d_problem::Axis& a = h->ax[axis];
+  free_axis(a);
+  a.T = n_terms;
+  a.coef.assign(coef, coef + n_terms);
+  if (n_terms == 0) return WG_OK;
+  const int nrp = n_terms * (nr + 1);
+  const size_t nb = (size_t)n_terms * n_el * 3 * nk * nk;
+  F2_CK(dalloc(&a.blocks, nb));
+  F2_CK(dalloc(&a.rp, nrp));
+  F2_CK(dalloc(&a.col, off[n_terms]));
+  F2_CK(dalloc(&a.val, off[n_terms]));
+  F2_CK(dalloc(&a.offs, n_terms));
+  F2_CK(dalloc(&a.dcoef, n_terms));
+  F2_CK(cudaMemcpy(a.blocks, center_blocks, sizeof(double) * nb, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(a.rp, row_ptr, sizeof(int) * nrp, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(a.offs, off.data(), sizeof(int) * n_terms, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(a.dcoef, coef, sizeof(double) * n_terms, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(a.col, col, sizeof(int) * std::max(1, off[n_terms]), cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(a.val, val, sizeof(double2) * std::max(1, off[n_terms]), cudaMemcpyHostToDevice));
+  const int need = std::max(h->ax[0].T, h->ax[1].T);
+  if (need > h->g_terms) {
+    cudaFree(h->G);
+    h->G = nullptr;
+    h->g_terms = 0;
+    F2_CK(dalloc(&h->G, (size_t)need * h->n));
+    h->g_terms = need;
+  }
+  return WG_OK;
+}
+
+int wg2d_set_drift(wg2d_problem* h, const double* interp, const double* proj, const double* xq, const double* yq,
+                   const double* vx, const double* vy, const double* pot, double cap_coef, const double* cap) {
+  if (!h) return WG_ERR_ARG;
+  if (!interp || !proj || !xq || !yq || !vx || !vy || !pot || !cap || !std::isfinite(cap_coef))
+    return fail(h, WG_ERR_ARG, "wg2d_set_drift: null argument or non-finite coefficient");
+  const size_t nql = (size_t)h->nq * h->nloc, slab = (size_t)h->nel * h->nq;
+  F2_CK(cudaMemcpyAsync(h->interp, interp, sizeof(double) * nql, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(h->proj, proj, sizeof(double) * nql, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(h->xq, xq, sizeof(double) * slab, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(h->yq, yq, sizeof(double) * slab, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(h->vx, vx, sizeof(double) * h->nvert, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(h->vy, vy, sizeof(double) * h->nvert, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(h->cap, cap, sizeof(double) * h->nrel, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  h->pot = make_double2(pot[0], pot[1]);
+  h->capc = cap_coef;
+  h->drift_ready = true;
+  return WG_OK;
+}
+
+int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const double* gy, const double* V) {
+  if (!h) return WG_ERR_ARG;
+  if (!h->drift_ready) return fail(h, WG_ERR_ARG, "wg2d_set_potential: call wg2d_set_drift first");
+  if (nx < 2 || ny < 2 || !gx || !gy || !V) return fail(h, WG_ERR_ARG, "wg2d_set_potential: need a 2 x 2 grid or larger");
+  for (int i = 0; i + 1 < nx; ++i)
+    if (!(gx[i + 1] > gx[i])) return fail(h, WG_ERR_ARG, "wg2d_set_potential: gx must increase");
+  for (int j = 0; j + 1 < ny; ++j)
+    if (!(gy[j + 1] > gy[j])) return fail(h, WG_ERR_ARG, "wg2d_set_potential: gy must increase");
+  for (long long i = 0; i < (long long)nx * ny; ++i)
+    if (!std::isfinite(V[i])) return fail(h, WG_ERR_ARG, "wg2d_set_potential: V must be finite");
+  double *dgx = nullptr, *dgy = nullptr, *dV = nullptr;
+  F2_CK(dalloc(&dgx, nx));
+  F2_CK(dalloc(&dgy, ny));
+  F2_CK(dalloc(&dV, (size_t)nx * ny));
+  F2_CK(cudaMemcpyAsync(dgx, gx, sizeof(double) * nx, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(dgy, gy, sizeof(double) * ny, cudaMemcpyHostToDevice, h->stream));
+  F2_CK(cudaMemcpyAsync(dV, V, sizeof(double) * nx * ny, cudaMemcpyHostToDevice, h->stream));
+  const dim3 g((unsigned)((h->nvert + 127) / 128), (unsigned)h->nq, (unsigned)h->nel);
+  f2d_dv_kernel<<<g, 128, 0, h->stream>>>(h->dV, h->xq, h->yq, h->vx, h->vy, dgx, dgy, dV, nx, ny, h->nq, h->nvert,
+                                         h->s.periodic_y);
+  const cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(h->stream);
+  cudaFree(dgx);
+  cudaFree(dgy);
+  cudaFree(dV);
+  if (e != cudaSuccess) return fail(h, WG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+  h->potential_ready = true;
+  return WG_OK;
+}
+
+static int apply_device(wg2d_problem* h) {
+  if (!h->potential_ready) return fail(h, WG_ERR_ARG, "wg2d_apply: set the drift data and the potential first");
+  int rc = apply_drift(h);
+  if (rc) return rc;
+  rc = apply_transport(h, 0);
+  if (rc) return rc;
+  return apply_transport(h, 1);
+}
+
+int wg2d_apply(wg2d_problem* h, const double* x, double* y) {
+  if (!h || !x || !y) return h ? fail(h, WG_ERR_ARG, "wg2d_apply: null argument") : WG_ERR_ARG;
+  F2_CK(cudaMemcpyAsync(h->x, x, sizeof(double2) * h->n, cudaMemcpyHostToDevice, h->stream));
+  const int rc = apply_device(h);
+  if (rc) return rc;
+  F2_CK(cudaMemcpyAsync(y, h->y, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  return WG_OK;
+}
+
+int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms) {
+  if (!h || n < 1 || !ms) return h ? fail(h, WG_ERR_ARG, "wg2d_apply_repeat: n >= 1 and ms required") : WG_ERR_ARG;
+  int rc = apply_device(h);      // warm-up
+  if (rc) return rc;
+  F2_CK(cudaEventRecord(h->ev[0], h->stream));
+  for (int i = 0; i < n && !rc; ++i) rc = apply_device(h);
+  if (rc) return rc;
+  F2_CK(cudaEventRecord(h->ev[1], h->stream));
+  F2_CK(cudaEventSynchronize(h->ev[1]));
+  float t = 0.f;
+  F2_CK(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
+  *ms = t / n;
+  if (parts_ms) {
+    F2_CK(cudaEventRecord(h->ev[0], h->stream));
+    rc = apply_drift(h);
+    F2_CK(cudaEventRecord(h->ev[1], h->stream));
+    if (!rc) rc = apply_transport(h, 0);
+    if (!rc) rc = apply_transport(h, 1);
+    F2_CK(cudaEventRecord(h->ev[2], h->stream));
+    if (rc) return rc;
+    F2_CK(cudaEventSynchronize(h->ev[2]));
+    float a = 0.f, b = 0.f;
+    F2_CK(cudaEventElapsedTime(&a, h->ev[0], h->ev[1]));
+    F2_CK(cudaEventElapsedTime(&b, h->ev[1], h->ev[2]));
+    parts_ms[0] = b;
+    parts_ms[1] = a;
+  }
+  return WG_OK;
+}
+
+}  // extern "C"

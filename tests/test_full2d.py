@@ -1,0 +1,142 @@
+"""Full-2D (X, Y, rho_x, rho_y) operator: the oracle's invariants, the host-built
+factors against the oracle's literal assembly, and the GPU apply against both.
+
+Tolerances: matrix-free == assembled 1e-13 relative (the reference's own
+full2DDiffOperatorTest bar is 1e-10); the host factors reassemble the oracle's
+transport operator to 1e-13; the GPU apply (FP64) matches the oracle to 1e-12
+relative L2; with a constant potential the drift term reduces to the CAP term up
+to the rounding of the interpolated potential differences (relative 1e-12).
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import full2d as F2
+
+CONFIGS = [
+    dict(yb="periodic", fx="upwind", fy="upwind"),          # the shape of the reference's Sim_Res run
+    dict(yb="zero-inflow", fx="rusanov", fy="central"),
+    dict(yb="specular", fx="upwind", fy="rusanov"),
+]
+
+
+def make_mat(yb="periodic", fx="upwind", fy="upwind", nex=5, ney=2, nkx=3, nky=3, nrx=9, nry=4, nq=5):
+    lx, w = 20.0, 4.0
+    nx, ny = nex * (nkx - 1) + 1, ney * (nky - 1) + 1
+    x, y = np.linspace(0, lx, nx), np.linspace(0, w, ny)
+    prm = dict(N_K_X=nkx, N_K_Y=nky, N_el_X=nex, N_el_Y=ney, N_rho_x=nrx, N_rho_y=nry, L_rho_x=8e-9,
+               full2D_X_flux=fx, full2D_Y_flux=fy, full2D_Y_boundary=yb, full2D_potentialQuadratureOrder=nq)
+    if yb != "periodic":
+        prm["L_rho_y"] = 3e-9
+    mat = dict(x=x, y=y, Nx=nx, Ny=ny, dg=dict(params=prm))
+    X, Y = np.meshgrid(x, y, indexing="ij")
+    V = 0.1 * np.exp(-((X - 10) / 3) ** 2) + 0.02 * np.cos(2 * np.pi * Y / w)
+    return mat, V
+
+
+def det_vec(n):
+    i = np.arange(n, dtype=float)
+    return np.sin(1.3 * i) + 1j * np.cos(0.7 * i)
+
+
+def rel(a, b):
+    return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_oracle_matrix_free_equals_assembled(cfg):
+    mat, V = make_mat(**cfg)
+    p, parts, dd = F2.system(mat, V)
+    u = det_vec(p["nTotal"])
+    A = F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)
+    assert rel(F2.apply_system(p, parts, dd, u), A @ u) < 1e-13
+
+
+def test_oracle_constant_potential_leaves_only_the_cap():
+    mat, V = make_mat()
+    p, parts, dd = F2.system(mat, np.full_like(V, 0.3))
+    u = det_vec(p["nTotal"])
+    cap = np.tile(dd["capc"] * dd["cap"], p["nCenterDof"]) * u
+    assert rel(F2.apply_drift(p, dd, u), cap) < 1e-12
+
+
+def test_oracle_periodic_y_derivative_and_seam():
+    """Periodic Y: the rho_y derivative is circulant and the closed DG chain conserves
+    the discrete mass (columns of H1 sum to zero against the mass-weighted constants)."""
+    mat, V = make_mat()
+    p = F2.init_params_full2d(mat)
+    D = p["rhoY"]["D"].toarray()
+    assert np.allclose(D, -np.roll(np.roll(D, 1, 0), 1, 1)[::-1, ::-1].T) or np.allclose(D + D.T, 0)
+    assert np.allclose(D.sum(axis=1), 0)
+    oy = F2.close_periodic_dg_axis(F2.one_dimensional_dg_operators(p["Y"]))
+    Mg = sp.kron(sp.identity(p["Y"]["nElements"]), p["Y"]["M"] * p["Y"]["jacobian"][0]).toarray()
+    ones = np.ones(p["Y"]["nDof"])
+    assert abs(ones @ Mg @ oy["H1"].toarray() @ ones) < 1e-12 * np.abs(oy["H1"]).sum()
+
+
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_host_factors_reassemble_the_oracle_operator(cfg):
+    from real_space_dg_gb300 import full2d
+    mat, V = make_mat(**cfg)
+    p, parts, dd = F2.system(mat, V)
+    f = full2d.build_factors(mat)
+    nX, nY = p["X"]["nDof"], p["Y"]["nDof"]
+    nrx, nry = p["rhoX"]["nCells"], p["rhoY"]["nCells"]
+    A = sp.csr_matrix((p["nTotal"], p["nTotal"]), dtype=complex)
+    for c, Cm, R in f["terms"][0]:
+        A = A + c * sp.kron(sp.kron(sp.identity(nY), sp.csr_matrix(Cm)), sp.kron(sp.identity(nry), sp.csr_matrix(R)))
+    for c, Cm, R in f["terms"][1]:
+        A = A + c * sp.kron(sp.kron(sp.csr_matrix(Cm), sp.identity(nX)), sp.kron(sp.csr_matrix(R), sp.identity(nrx)))
+    ref = F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"])
+    assert sp.linalg.norm(A - ref) <= 1e-13 * sp.linalg.norm(ref)
+    d, cpd = f["drift"], dd["cpd"]
+    assert np.allclose(d["interp"], cpd["interp"], rtol=0, atol=1e-14)
+    assert np.allclose(d["proj"], cpd["proj"], rtol=1e-13, atol=1e-14)
+    assert np.allclose(d["xq"].T, cpd["XQ"], rtol=1e-15, atol=0) and np.allclose(d["yq"].T, cpd["YQ"], rtol=1e-15, atol=0)
+    _, vx, vy = F2.relative_projection(p)
+    assert np.array_equal(d["vx"], vx) and np.array_equal(d["vy"], vy)
+    assert np.allclose(d["cap"], dd["cap"], rtol=1e-15, atol=0)
+    assert d["capc"] == dd["capc"] and d["pot"] == dd["pot"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg", CONFIGS)
+def test_gpu_apply_matches_oracle(built_lib, cfg):
+    from real_space_dg_gb300.full2d import Full2DOperator
+    mat, V = make_mat(**cfg)
+    p, parts, dd = F2.system(mat, V)
+    u = det_vec(p["nTotal"])
+    with Full2DOperator(mat, V) as op:
+        y = op.apply(u)
+        # a new potential is rebuilt on the device
+        V2 = V * 1.7 + 0.05
+        op.set_potential(V2)
+        y2 = op.apply(u)
+    assert rel(y, F2.apply_system(p, parts, dd, u)) < 1e-12
+    dd2 = F2.drift_data(mat, p, V2)
+    assert rel(y2, F2.apply_system(p, parts, dd2, u)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_apply_larger_orders(built_lib):
+    from real_space_dg_gb300.full2d import Full2DOperator
+    mat, V = make_mat(nex=4, ney=2, nkx=4, nky=2, nrx=12, nry=6, nq=4)
+    p, parts, dd = F2.system(mat, V)
+    u = det_vec(p["nTotal"])
+    with Full2DOperator(mat, V) as op:
+        assert rel(op.apply(u), F2.apply_system(p, parts, dd, u)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_argument_errors(built_lib):
+    from real_space_dg_gb300 import WignerError
+    from real_space_dg_gb300.full2d import Full2DOperator
+    mat, V = make_mat()
+    with Full2DOperator(mat) as op:
+        with pytest.raises(WignerError):
+            op.apply(det_vec(op.n))                 # no potential yet
+        with pytest.raises(WignerError):
+            op.set_potential(V[:, :1])
+        op.set_potential(V)
+        with pytest.raises(WignerError):
+            op.apply(det_vec(op.n - 1))
