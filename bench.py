@@ -566,34 +566,40 @@ def full2d_case(cfg=FULL2D):
 
 def full2d_flops(f, n):
     """Algorithmic FP64 flops of one apply from the host factors (complex MAC = 8 flops,
-    real x complex = 4): centre factors 3 nk per entry and term, relative factors nnz per row,
-    potential interpolation + projection 2 nq n_local per element entry, the vertex stencil."""
+    real x complex = 4), as (transport, potential): centre factors 3 nk per entry and term,
+    relative factors nnz per row; potential interpolation + projection 2 nq n_local per
+    element entry and the vertex stencil."""
     s = f["shape"]
-    fl = 0.0
+    tr = 0.0
     for axis, nk, nr in ((0, s["nk_x"], s["n_rho_x"]), (1, s["nk_y"], s["n_rho_y"])):
         for _, _, R in f["terms"][axis]:
-            fl += n * (3 * nk * 4 + 8 * np.count_nonzero(R) / nr)
+            tr += n * (3 * nk * 4 + 8 * np.count_nonzero(R) / nr)
     nloc = s["nk_x"] * s["nk_y"]
-    fl += n / nloc * f["nq"] * (2 * nloc * 4 + 4 * 2 + 16 * 2)
-    return fl
+    return tr, n / nloc * f["nq"] * (2 * nloc * 4 + 4 * 2 + 16 * 2)
 
 
 def run_full2d(args):
-    """Full-2D operator applies/s (a9: applyKronOperator + FV-consistent potential + CAP, FP64)."""
+    """Full-2D operator applies/s (a9: applyKronOperator + FV-consistent potential + CAP, FP64;
+    the dense characteristic |A_x| factor as FP64 emulated on the tensor cores, and without)."""
     import __graft_entry__ as g
     g.build()
     from real_space_dg_gb300.full2d import Full2DOperator
     mat, V = full2d_case()
-    op = Full2DOperator(mat, V)
-    n = op.n
-    for _ in range(args.warmup):
-        op.apply_time(1)
-    clocks = ClockSampler()
-    clocks.start()
-    steps = max(10, args.steps)
-    ms, parts = op.apply_time(steps)
-    clk = clocks.stop()
-    fl = full2d_flops(op.factors, n)
+    hbm, bf16, src = read_peaks()
+    res = {}
+    for tc in (True, False):
+        op = Full2DOperator(mat, V, tensor_cores=tc)
+        for _ in range(args.warmup):
+            op.apply_time(1)
+        clocks = ClockSampler()
+        clocks.start()
+        steps = max(10, args.steps)
+        ms, parts = op.apply_time(steps)
+        clk = clocks.stop()
+        res[tc] = (ms, parts, clk, op)
+    n = res[True][3].n
+    ms, parts, clk, op = res[True]
+    fl_tr, fl_pot = full2d_flops(op.factors, n)
     u = (np.sin(np.arange(n) * 1.3) + 1j * np.cos(np.arange(n) * 0.7)).astype(complex)
     op.apply(u)
     t0 = time.perf_counter()
@@ -601,23 +607,37 @@ def run_full2d(args):
     for _ in range(ne):
         op.apply(u)
     e2e_s = (time.perf_counter() - t0) / ne
-    op.close()
     peak = 1.25
+    pot = {"kernel": "full2d_potential", "bound": "fp64", "achieved": round(fl_pot / parts[1] / 1e9, 3),
+           "peak": peak, "unit": "TFLOP/s", "frac": round(fl_pot / parts[1] / 1e9 / peak, 4), "traffic": None,
+           "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)", "ms": round(float(parts[1]), 4)}
+    # transport: the dense rho_x factor on the tensor cores counts its 36 BF16 digit products
+    nrx = op.shape["n_rho_x"]
+    dense_fl = sum(2 * (2 * nrx) * (2 * nrx) * (n / nrx) for _, _, R in op.terms[0] if np.count_nonzero(R) * 4 > nrx * nrx)
+    tr = {"kernel": "full2d_transport", "bound": "tensor+fp64", "achieved_fp64_equivalent": round(fl_tr / parts[0] / 1e9, 3),
+          "tensor_tflops_of_digit_products": round(36 * dense_fl / parts[0] / 1e12, 3), "peak": bf16, "unit": "TFLOP/s",
+          "frac": round(36 * dense_fl / parts[0] / 1e12 / bf16, 4), "traffic": None,
+          "peak_source": "bf16_tflops (%s); the whole transport time counted against the digit products" % src,
+          "ms": round(float(parts[0]), 4)}
+    roof = pot if parts[1] >= parts[0] else tr
     out = {"metric": "Full-2D operator applies/s (3,136,320 complex unknowns, FP64)", "value": round(1000.0 / ms, 3),
-           "unit": "applies/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic double-barrier potential on the grid of the reference's recorded Full-2D run",
+           "unit": "applies/s", "n_gpus": 1, "steps": max(10, args.steps), "warmup": args.warmup,
+           "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic double-barrier potential on the grid of the reference's recorded Full-2D run",
            "config": {"workload": "Full-2D apply: X 120 el x p=2, Y 2 el x p=2 periodic, rho 121 x 12, upwind, "
                                   "FV-consistent potential (5 x 5 quadrature), CAP", "unknowns": n,
+                      "dense_rho_x_factor": "FP64 emulated on the tensor cores (8 digits, 36 products)",
                       "l2": "state 50 MB and intermediates 0.4 GB, larger than L2"},
-           "roofline": {"kernel": "full2d_apply", "bound": "fp64", "achieved": round(fl / ms / 1e9, 3), "peak": peak,
-                        "unit": "TFLOP/s", "frac": round(fl / ms / 1e9 / peak, 4), "traffic": None,
-                        "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak)",
-                        "flops_per_apply": fl},
-           "parts_ms": {"transport": round(float(parts[0]), 4), "potential_and_cap": round(float(parts[1]), 4)},
+           "roofline": roof, "rooflines": {"potential": pot, "transport": tr},
+           "flops_per_apply_fp64": fl_tr + fl_pot,
+           "fp64_cuda_cores": {"applies_per_s": round(1000.0 / res[False][0], 3), "ms": round(res[False][0], 4),
+                               "transport_ms": round(float(res[False][1][0]), 4),
+                               "fp64_tflops": round((fl_tr + fl_pot) / res[False][0] / 1e9, 3)},
            "e2e": {"value": round(1.0 / e2e_s, 3), "unit": "applies/s", "h2d_bytes_per_step": 16 * n,
                    "d2h_bytes_per_step": 16 * n},
-           "gpu_launches": 9, "clocks": clk}
+           "gpu_launches": 11, "clocks": clk}
+    for _, (_, _, _, o) in res.items():
+        o.close()
     if not args.no_cpu:
         from oracle import full2d as F2
         t0 = time.perf_counter()

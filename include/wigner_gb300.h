@@ -424,6 +424,8 @@ typedef struct {
   int n_rho_x, n_rho_y;     /* relative FV cells */
   int periodic_y;           /* 1: the Y element chain is closed (core/close_PeriodicDGAxis_full2D.m) */
   int n_quad;               /* potential quadrature points per centre element */
+  int tensor_cores;         /* 1: dense rho_x factors (the characteristic |A_x|) as FP64 GEMMs emulated
+                               on the tensor cores (~1e-14 of |R||G|); 0: FP64 CUDA-core kernels */
 } wg2d_shape;
 
 int wg2d_create(const wg2d_shape* s, wg2d_problem** out);

@@ -125,7 +125,8 @@ class WgRuntimeStats(C.Structure):
 
 class Wg2dShape(C.Structure):
     _fields_ = [("n_el_x", C.c_int), ("nk_x", C.c_int), ("n_el_y", C.c_int), ("nk_y", C.c_int),
-                ("n_rho_x", C.c_int), ("n_rho_y", C.c_int), ("periodic_y", C.c_int), ("n_quad", C.c_int)]
+                ("n_rho_x", C.c_int), ("n_rho_y", C.c_int), ("periodic_y", C.c_int), ("n_quad", C.c_int),
+                ("tensor_cores", C.c_int)]
 
 
 REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}

@@ -30,6 +30,7 @@
 #include <string>
 #include <vector>
 
+#include "ozaki_api.h"
 #include "wigner_gb300.h"
 
 struct wg2d_problem {
@@ -48,7 +49,11 @@ struct wg2d_problem {
     double2* val = nullptr;
     int* offs = nullptr;        // [T] start of term t in col / val
     double* dcoef = nullptr;    // [T]
+    unsigned dense_mask = 0;    // terms applied by the emulated FP64 GEMM (rho_x axis)
+    std::vector<wg::OzakiRowsDev> dense;   // [T] digit slices of c_t R_t (real embedding) for those terms
   } ax[2];
+  wg::OzakiColsDev cols;        // digit slices of the centre-applied state (rho_x columns)
+  int* tc_err = nullptr;        // raised by a timed-out barrier wait of the emulated GEMM
   double2* G = nullptr;         // [Tmax][n] centre-applied state
   int g_terms = 0;
   // potential
@@ -125,7 +130,7 @@ __global__ void __launch_bounds__(512) f2d_relx_kernel(const double2* __restrict
                                                        const int* __restrict__ rp, const int* __restrict__ col,
                                                        const double2* __restrict__ val, const int* __restrict__ nnz_off,
                                                        const double* __restrict__ coef, int T, int nrx,
-                                                       long long ncols, long long n) {
+                                                       long long ncols, long long n, unsigned skip_mask) {
   extern __shared__ double2 sg[];       // [kRelxCols][nrx]
   const long long c0 = (long long)blockIdx.x * kRelxCols;
   const int nc = (int)min((long long)kRelxCols, ncols - c0);
@@ -134,6 +139,7 @@ __global__ void __launch_bounds__(512) f2d_relx_kernel(const double2* __restrict
 #pragma unroll
   for (int j = 0; j < kRelxCols; ++j) acc[j] = make_double2(0.0, 0.0);
   for (int t = 0; t < T; ++t) {
+    if ((skip_mask >> t) & 1u) continue;          // applied on the tensor cores
     __syncthreads();
     for (int i = threadIdx.x; i < kRelxCols * nrx; i += blockDim.x) {
       const int j = i / nrx, k = i - j * nrx;
@@ -369,6 +375,7 @@ cudaError_t dalloc(T** p, size_t n) {
 }
 
 void free_axis(wg2d_problem::Axis& a) {
+  for (wg::OzakiRowsDev& d : a.dense) wg::ozaki_free(d);
   cudaFree(a.blocks);
   cudaFree(a.rp);
   cudaFree(a.col);
@@ -403,8 +410,13 @@ int apply_transport(wg2d_problem* h, int axis) {
     const long long ncols = h->n / h->nrx;
     const size_t smem = sizeof(double2) * kRelxCols * h->nrx;
     const int threads = (h->nrx + 31) / 32 * 32;
-    f2d_relx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
-        h->G, h->y, a.rp, a.col, a.val, nnz_off, coef, a.T, h->nrx, ncols, h->n);
+    if (a.dense_mask != (1u << a.T) - 1u)
+      f2d_relx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+          h->G, h->y, a.rp, a.col, a.val, nnz_off, coef, a.T, h->nrx, ncols, h->n, a.dense_mask);
+    for (int t = 0; t < a.T; ++t)
+      if ((a.dense_mask >> t) & 1u)
+        F2_CK(wg::ozaki_accumulate(a.dense[t], h->cols, reinterpret_cast<const double*>(h->G + (long long)t * h->n),
+                                   reinterpret_cast<double*>(h->y), h->tc_err, h->stream));
   } else {
     f2d_rely_kernel<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(h->G, h->y, a.rp, a.col, a.val, nnz_off,
                                                                           coef, a.T, h->nrx, h->nry, h->n);
@@ -479,6 +491,8 @@ int wg2d_create(const wg2d_shape* s, wg2d_problem** out) {
   if (e == cudaSuccess) e = dalloc(&h->vx, h->nvert);
   if (e == cudaSuccess) e = dalloc(&h->vy, h->nvert);
   if (e == cudaSuccess) e = dalloc(&h->cap, h->nrel);
+  if (e == cudaSuccess) e = dalloc(&h->tc_err, 1);
+  if (e == cudaSuccess) e = cudaMemset(h->tc_err, 0, sizeof(int));
   for (cudaEvent_t& ev : h->ev)
     if (e == cudaSuccess) e = cudaEventCreate(&ev);
   if (e == cudaSuccess && h->nrx * kRelxCols * sizeof(double2) > 48 * 1024)
@@ -496,7 +510,9 @@ int wg2d_destroy(wg2d_problem* h) {
   if (!h) return WG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& a : h->ax) free_axis(a);
-  void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap};
+  wg::ozaki_free(h->cols);
+  void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap,
+                  h->tc_err};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t ev : h->ev)
@@ -546,6 +562,33 @@ int wg2d_set_transport(wg2d_problem* h, int axis, int n_terms, const double* coe
   F2_CK(cudaMemcpy(a.dcoef, coef, sizeof(double) * n_terms, cudaMemcpyHostToDevice));
   F2_CK(cudaMemcpy(a.col, col, sizeof(int) * std::max(1, off[n_terms]), cudaMemcpyHostToDevice));
   F2_CK(cudaMemcpy(a.val, val, sizeof(double2) * std::max(1, off[n_terms]), cudaMemcpyHostToDevice));
+  // dense rho_x factors on the tensor cores: the real embedding of c_t R_t, digit-sliced once
+  a.dense.assign(n_terms, wg::OzakiRowsDev{});
+  a.dense_mask = 0;
+  if (axis == 0 && h->s.tensor_cores) {
+    for (int t = 0; t < n_terms; ++t) {
+      const int nnz = off[t + 1] - off[t];
+      if ((long long)nnz * 4 <= (long long)nr * nr) continue;
+      std::vector<double> A((size_t)4 * nr * nr, 0.0);
+      const int* rp = row_ptr + t * (nr + 1);
+      for (int i = 0; i < nr; ++i)
+        for (int k = rp[i]; k < rp[i + 1]; ++k) {
+          const int j = col[off[t] + k];
+          const double re = coef[t] * val[2 * (off[t] + k)], im = coef[t] * val[2 * (off[t] + k) + 1];
+          A[(size_t)(2 * i) * 2 * nr + 2 * j] += re;
+          A[(size_t)(2 * i) * 2 * nr + 2 * j + 1] += -im;
+          A[(size_t)(2 * i + 1) * 2 * nr + 2 * j] += im;
+          A[(size_t)(2 * i + 1) * 2 * nr + 2 * j + 1] += re;
+        }
+      const int rc = wg::ozaki_rows_upload(A, 2 * nr, 2 * nr, a.dense[t], h->err);
+      if (rc) return rc;
+      a.dense_mask |= 1u << t;
+    }
+    if (a.dense_mask && !h->cols.dig) {
+      const int rc = wg::ozaki_cols_alloc(h->n / nr, 2 * nr, h->cols, h->err);
+      if (rc) return rc;
+    }
+  }
   const int need = std::max(h->ax[0].T, h->ax[1].T);
   if (need > h->g_terms) {
     cudaFree(h->G);
@@ -622,7 +665,10 @@ int wg2d_apply(wg2d_problem* h, const double* x, double* y) {
   const int rc = apply_device(h);
   if (rc) return rc;
   F2_CK(cudaMemcpyAsync(y, h->y, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
+  int flag = 0;
+  F2_CK(cudaMemcpyAsync(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   F2_CK(cudaStreamSynchronize(h->stream));
+  if (flag) return fail(h, WG_ERR_TIMEOUT, "tensor-core GEMM: bounded barrier wait timed out");
   return WG_OK;
 }
 
@@ -638,6 +684,9 @@ int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms) {
   float t = 0.f;
   F2_CK(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
   *ms = t / n;
+  int flag = 0;
+  F2_CK(cudaMemcpy(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag) return fail(h, WG_ERR_TIMEOUT, "tensor-core GEMM: bounded barrier wait timed out");
   if (parts_ms) {
     F2_CK(cudaEventRecord(h->ev[0], h->stream));
     rc = apply_drift(h);

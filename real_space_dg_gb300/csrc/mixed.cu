@@ -22,6 +22,7 @@
 #include "kline.cuh"
 #include "ozaki.cuh"
 #include "problem.h"
+#include "ozaki_api.h"
 #include "tc_gemm.cuh"
 
 namespace wg {
@@ -805,6 +806,82 @@ int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N,
   cudaFree(deb);
   cudaFree(derr);
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Emulated FP64 GEMM as a building block (ozaki_api.h).
+// ---------------------------------------------------------------------------
+int ozaki_rows_upload(const std::vector<double>& A, int M, int K, OzakiRowsDev& out, std::string& err) {
+  if (M < 1 || K < 2 || K > oz::MAX_K || (int)A.size() != M * K) {
+    err = "emulated GEMM: 1 <= M, 2 <= K <= 1024";
+    return WG_ERR_ARG;
+  }
+  const int Kp = (K + 7) / 8 * 8;
+  std::vector<double> Ap((size_t)M * Kp, 0.0);
+  for (int r = 0; r < M; ++r)
+    for (int k = 0; k < K; ++k) Ap[(size_t)r * Kp + k] = A[(size_t)r * K + k];
+  std::vector<bf16> dig;
+  std::vector<int> e;
+  slice_rows_host(Ap, M, Kp, dig, e);
+  cudaError_t ce = cudaMalloc(&out.dig, sizeof(bf16) * dig.size());
+  if (ce == cudaSuccess) ce = cudaMalloc(&out.e, sizeof(int) * e.size());
+  if (ce == cudaSuccess) ce = cudaMemcpy(out.dig, dig.data(), sizeof(bf16) * dig.size(), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemcpy(out.e, e.data(), sizeof(int) * e.size(), cudaMemcpyHostToDevice);
+  if (ce != cudaSuccess) {
+    err = std::string("emulated GEMM rows: ") + cudaGetErrorString(ce);
+    ozaki_free(out);
+    return ce == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
+  }
+  if (!make_map3(&out.map, out.dig, M, Kp, oz::BM)) {
+    err = "emulated GEMM rows: tensor map";
+    ozaki_free(out);
+    return WG_ERR_CUDA;
+  }
+  out.M = M;
+  out.K = K;
+  out.Kp = Kp;
+  return WG_OK;
+}
+
+int ozaki_cols_alloc(long long ncol, int K, OzakiColsDev& out, std::string& err) {
+  const int Kp = (K + 7) / 8 * 8;
+  cudaError_t ce = cudaMalloc(&out.dig, sizeof(bf16) * (size_t)oz::S * ncol * Kp);
+  if (ce == cudaSuccess) ce = cudaMalloc(&out.e, sizeof(int) * (size_t)ncol);
+  if (ce != cudaSuccess) {
+    err = std::string("emulated GEMM columns: ") + cudaGetErrorString(ce);
+    ozaki_free(out);
+    return ce == cudaErrorMemoryAllocation ? WG_ERR_OOM : WG_ERR_CUDA;
+  }
+  if (!make_map3(&out.map, out.dig, ncol, Kp, oz::BN)) {
+    err = "emulated GEMM columns: tensor map";
+    ozaki_free(out);
+    return WG_ERR_CUDA;
+  }
+  out.ncol = ncol;
+  out.Kp = Kp;
+  return WG_OK;
+}
+
+void ozaki_free(OzakiRowsDev& a) {
+  cudaFree(a.dig);
+  cudaFree(a.e);
+  a = OzakiRowsDev{};
+}
+
+void ozaki_free(OzakiColsDev& b) {
+  cudaFree(b.dig);
+  cudaFree(b.e);
+  b = OzakiColsDev{};
+}
+
+cudaError_t ozaki_accumulate(const OzakiRowsDev& A, OzakiColsDev& B, const double* X, double* C, int* err,
+                             cudaStream_t st) {
+  if (B.Kp != A.Kp) return cudaErrorInvalidValue;
+  oz::slice_columns_kernel<<<slice_blocks(B.ncol), 32 * oz::kSliceColsPerBlock, 0, st>>>(X, A.K, B.ncol, B.dig, B.e,
+                                                                                        nullptr, 1, B.Kp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_ozaki<1>(A.map, B.map, A.e, B.e, C, A.M, B.ncol, A.Kp, err, st);
 }
 
 }  // namespace wg

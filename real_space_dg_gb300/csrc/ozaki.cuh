@@ -244,10 +244,13 @@ __global__ void __launch_bounds__(32 * kSliceColsPerBlock) slice_columns_kernel(
                                                                                __nv_bfloat16* __restrict__ slices,
                                                                                int* __restrict__ e_out,
                                                                                const int* __restrict__ mask = nullptr,
-                                                                               int cols_per_problem = 1) {
+                                                                               int cols_per_problem = 1,
+                                                                               int Kout = 0) {
+  // Kout: row length of the slices (>= K, zero-padded; 0: K), for 16-byte TMA rows
   const int lane = threadIdx.x & 31;
   const long long c = (long long)blockIdx.x * kSliceColsPerBlock + (threadIdx.x >> 5);
   if (c >= Ncol || (mask && !mask[c / cols_per_problem])) return;
+  const int Ko = Kout > K ? Kout : K;
   const double2* x = reinterpret_cast<const double2*>(X + c * (long long)K);
   const int K2 = K / 2;
   unsigned long long mx = 0;
@@ -265,8 +268,11 @@ __global__ void __launch_bounds__(32 * kSliceColsPerBlock) slice_columns_kernel(
   const int emax = (int)((mx >> 52) & 0x7FF);
   const int m = mx == 0 ? 0 : emax - 1023 + 1;   // max|x| < 2^m
   if (lane == 0) e_out[c] = m + 1;
-  const long long slice_stride = Ncol * (long long)K;
-  __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(slices + c * (long long)K);
+  const long long slice_stride = Ncol * (long long)Ko;
+  __nv_bfloat162* out = reinterpret_cast<__nv_bfloat162*>(slices + c * (long long)Ko);
+  for (int k = K2 + lane; k < Ko / 2; k += 32)
+#pragma unroll
+    for (int p = 0; p < S; ++p) out[p * (slice_stride / 2) + k] = __floats2bfloat162_rn(0.f, 0.f);
   for (int k = lane; k < K2; k += 32) {
     const double2 v = x[k];
     long long F0 = round_scaled(__double_as_longlong(v.x), m, mx != 0);

@@ -373,9 +373,11 @@ class Full2DOperator:
     ``mat`` carries x, y (nm), dg.params (N_K_X/Y, N_el_X/Y, N_rho_x/y, L_rho_x/y, flux
     and boundary options as in the reference) and optionally me_x_ch; ``V`` is the
     potential [Nx x Ny] on the material grid (V), like get_SysM_full2D(mat, p, Vxy).
+    ``tensor_cores``: the dense characteristic |A_x| factor as an FP64 GEMM emulated on
+    the tensor cores (default) instead of FP64 CUDA-core kernels.
     """
 
-    def __init__(self, mat, V=None):
+    def __init__(self, mat, V=None, tensor_cores=True):
         self.lib = _lib.load()
         f = build_factors(mat)
         self.factors = f
@@ -385,7 +387,8 @@ class Full2DOperator:
         AX, AY = f["axes"]
         periodic = bool(s["periodic_y"])
         nrx, nry = s["n_rho_x"], s["n_rho_y"]
-        st = _lib.Wg2dShape(s["n_el_x"], s["nk_x"], s["n_el_y"], s["nk_y"], nrx, nry, int(periodic), self.nq)
+        st = _lib.Wg2dShape(s["n_el_x"], s["nk_x"], s["n_el_y"], s["nk_y"], nrx, nry, int(periodic), self.nq,
+                            1 if tensor_cores else 0)
         h = C.c_void_p()
         rc = self.lib.wg2d_create(C.byref(st), C.byref(h))
         if rc != _lib.WG_OK:

@@ -100,13 +100,15 @@ def test_host_factors_reassemble_the_oracle_operator(cfg):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("tensor_cores", [False, True])
 @pytest.mark.parametrize("cfg", CONFIGS)
-def test_gpu_apply_matches_oracle(built_lib, cfg):
+def test_gpu_apply_matches_oracle(built_lib, cfg, tensor_cores):
+    """FP64 CUDA-core path and the dense |A_x| factor emulated on the tensor cores."""
     from real_space_dg_gb300.full2d import Full2DOperator
     mat, V = make_mat(**cfg)
     p, parts, dd = F2.system(mat, V)
     u = det_vec(p["nTotal"])
-    with Full2DOperator(mat, V) as op:
+    with Full2DOperator(mat, V, tensor_cores=tensor_cores) as op:
         y = op.apply(u)
         # a new potential is rebuilt on the device
         V2 = V * 1.7 + 0.05
@@ -120,11 +122,12 @@ def test_gpu_apply_matches_oracle(built_lib, cfg):
 @pytest.mark.gpu
 def test_gpu_apply_larger_orders(built_lib):
     from real_space_dg_gb300.full2d import Full2DOperator
-    mat, V = make_mat(nex=4, ney=2, nkx=4, nky=2, nrx=12, nry=6, nq=4)
+    mat, V = make_mat(nex=4, ney=2, nkx=4, nky=2, nrx=37, nry=6, nq=4)
     p, parts, dd = F2.system(mat, V)
     u = det_vec(p["nTotal"])
-    with Full2DOperator(mat, V) as op:
-        assert rel(op.apply(u), F2.apply_system(p, parts, dd, u)) < 1e-12
+    for tc in (False, True):
+        with Full2DOperator(mat, V, tensor_cores=tc) as op:
+            assert rel(op.apply(u), F2.apply_system(p, parts, dd, u)) < 1e-12
 
 
 @pytest.mark.gpu
