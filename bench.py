@@ -615,8 +615,8 @@ def run_full2d(args):
     nrx = op.shape["n_rho_x"]
     dense_fl = sum(2 * (2 * nrx) * (2 * nrx) * (n / nrx) for _, _, R in op.terms[0] if np.count_nonzero(R) * 4 > nrx * nrx)
     tr = {"kernel": "full2d_transport", "bound": "tensor+fp64", "achieved_fp64_equivalent": round(fl_tr / parts[0] / 1e9, 3),
-          "tensor_tflops_of_digit_products": round(36 * dense_fl / parts[0] / 1e12, 3), "peak": bf16, "unit": "TFLOP/s",
-          "frac": round(36 * dense_fl / parts[0] / 1e12 / bf16, 4), "traffic": None,
+          "tensor_tflops_of_digit_products": round(36 * dense_fl / parts[0] / 1e9, 3), "peak": bf16, "unit": "TFLOP/s",
+          "frac": round(36 * dense_fl / parts[0] / 1e9 / bf16, 4), "traffic": None,
           "peak_source": "bf16_tflops (%s); the whole transport time counted against the digit products" % src,
           "ms": round(float(parts[0]), 4)}
     roof = pot if parts[1] >= parts[0] else tr
