@@ -86,7 +86,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = [r for r in self.rows if r[0] == "0"] or self.rows
+        rows = [r for r in self.rows if r[0] == str(PHYS_GPU)] or self.rows
         def num(x):
             try:
                 return float(x)
@@ -100,10 +100,28 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+PHYS_GPU = 0   # index (nvidia-smi numbering) of this rank's GPU
+
+
+def select_device():
+    """One GPU per rank: LOCAL_RANK picks an entry of CUDA_VISIBLE_DEVICES (or that index when
+    unset) and narrows the visible devices to it before the library initialises CUDA, so
+    every rank's handles, streams and server threads run on device 0 of their own view."""
+    global PHYS_GPU
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if int(os.environ.get("WORLD_SIZE", "1")) <= 1:
+        return
+    vis = [v for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    pick = vis[local % len(vis)] if vis else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = pick
+    PHYS_GPU = int(pick) if pick.isdigit() else local
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
+    select_device()
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
@@ -451,6 +469,79 @@ def run_transient(args):
     }
 
 
+C1 = dict(length_nm=60.0, contact_nm=15.0, barrier_ev=0.27, barrier_nm=3.0, well_nm=5.0, doping_m3=1e24, m_rel=0.067,
+          temp_k=300.0, order=2, n_el=120, nk=128, l_xi_m=30e-9, bias=0.1, tol=1e-10, restart=50, batch=64)
+
+
+def run_c1(args):
+    """C1: the reference's CPU-runnable case -- the stationary flat-band RTD (60 nm, p=2, N_el=120,
+    Nk=128, 46,080 unknowns, 0.1 V linear drop, no Poisson), plain FP64, GMRES(50) with the
+    k-line preconditioner to a 1e-10 relative residual, n(x) and J out.  One step solves a batch of
+    64 such problems (the same device at 64 biases in 0..0.1 V) from a zero start; e2e is one solve
+    through solve_transport_DG_2D; the CPU line is the reference's own method, the sparse LU of
+    the assembled system (A\\rhs), in the oracle port on the host cores."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300 import devices
+    from real_space_dg_gb300.transport import Problem1D, shape_from_mat, solve_transport_DG_2D
+    spec = devices.RTDSpec(**{k: v for k, v in C1.items() if k not in ("bias", "tol", "restart", "batch")})
+    mat = devices.make_mat(spec)
+    B = C1["batch"]
+    biases = C1["bias"] * np.arange(1, B + 1) / B
+    m = np.full(mat["Nx"], spec.m_rel * 9.109e-31)
+    P = Problem1D(batch=B, precision="fp64", restart=C1["restart"], **shape_from_mat(mat))
+    for b, v in enumerate(biases):
+        E = devices.flatband_potential(mat, v)
+        efl, efr = devices.contact_fermi_levels(mat, v)
+        P.set_potential(b, mat["x"], E, m, spec.m_rel, spec.temp_k, efl, efr)
+    for _ in range(args.warmup):
+        P.solve(tol=C1["tol"], maxit=100)
+    clocks = ClockSampler()
+    clocks.start()
+    P.profile(on=False, reset=True)
+    P.event(0)
+    infos = []
+    for _ in range(args.steps):
+        st, info = P.solve(tol=C1["tol"], maxit=100)
+        infos.append(info)
+    P.event(1)
+    ms = P.elapsed_ms(0, 1)
+    counted = P.profile(on=False, reset=True)
+    clk = clocks.stop()
+    conv = sum(1 for i in infos[-1] if i["flag"] == 0)
+    iters = float(np.mean([i["iterations"] for i in infos[-1]]))
+    P.close()
+    E = devices.flatband_potential(mat, C1["bias"])
+    efl, efr = devices.contact_fermi_levels(mat, C1["bias"])
+    solve_transport_DG_2D(mat, E, np.ones(mat["Nx"]), efl, efr, tol=C1["tol"], maxit=100)   # warm-up
+    t0 = time.perf_counter()
+    ne = 5
+    for _ in range(ne):
+        DG = solve_transport_DG_2D(mat, E, np.ones(mat["Nx"]), efl, efr, tol=C1["tol"], maxit=100)
+    e2e_s = (time.perf_counter() - t0) / ne
+    out = {"metric": "stationary flat-band RTD solves/s at 1e-10 relative residual (C1, plain FP64)",
+           "value": round(B * args.steps / (ms / 1000.0), 3), "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic RTD of the named shape (C1), 64 biases in 0..0.1 V",
+           "config": {"workload": "C1 flat-band RTD 60 nm, p=2, N_el=120, Nk=128, 46,080 unknowns, GMRES(50), "
+                                  "rtol 1e-10, k-line preconditioner", "batch": B},
+           "solves_converged": conv, "gmres_iterations_per_solve": iters,
+           "e2e": {"value": round(1.0 / e2e_s, 3), "unit": "solves/s", "path": "solve_transport_DG_2D, one problem",
+                   "h2d_bytes_per_step": int(8 * 3 * mat["Nx"]),
+                   "d2h_bytes_per_step": int(DG["RHO"].nbytes + DG["n"].nbytes + DG["j"].nbytes)},
+           "gpu_launches": int(sum(v[2] for v in counted.values())), "clocks": clk}
+    if not args.no_cpu:
+        from oracle import dg1d
+        t0 = time.perf_counter()
+        dg1d.solve_transport_dg_2d(mat, E, np.ones(mat["Nx"]), efl, efr)
+        t1 = time.perf_counter()
+        out["cpu_baseline"] = {"value": round(1.0 / (t1 - t0), 4), "unit": "solves/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "one oracle solve_transport_DG_2D with sparse LU "
+                               "(the reference's A\\rhs) at the C1 size, %.2f s including assembly" % (t1 - t0)}
+    return out
+
+
 FET = dict(n_gates=32, vg_max=0.6, v_drain=0.4, tol=1e-8, maxit=60)
 
 
@@ -684,10 +775,11 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c4", "full2d"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
-                         "c4: multi-subband FET gate sweep; full2d: Full-2D operator applies/s")
+                         "c1: the flat-band C1 solve (plain FP64); c4: multi-subband FET gate sweep; "
+                         "full2d: Full-2D operator applies/s")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -721,6 +813,8 @@ def main():
         out = run_apply(args) if rank == 0 else None
     elif args.workload == "c4":
         out = run_fet(args) if rank == 0 else None
+    elif args.workload == "c1":
+        out = run_c1(args) if rank == 0 else None
     elif args.workload == "full2d":
         out = run_full2d(args) if rank == 0 else None
     else:
