@@ -418,3 +418,107 @@ def system(mat, V):
 
 def apply_system(p, parts, dd, u):
     return apply_kron(parts, u, p["nCenterDof"], p["nRelative"]) + apply_drift(p, dd, u)
+
+
+# ----------------------------------------------------------------------------- line-transverse preconditioner
+
+def transverse_reference(mat, V, ix=0):
+    """transverseReference (get_LineTransversePreconditioner_full2D.m:127-175): the frozen-X
+    transverse transport K and potential V blocks of a 2-cell, 2-element strip at column ix."""
+    prm = dict(mat["dg"]["params"])
+    prm.update(N_rho_x=2, N_K_X=2, N_el_X=2, full2D_Q_diff_x=0.0, full2D_cap_scale=0.0)
+    ref = dict(mat)
+    ref["dg"] = dict(mat["dg"], params=prm)
+    V = np.asarray(V, dtype=float)
+    Vref = np.repeat(V[ix:ix + 1, :], V.shape[0], axis=0)
+    pr = init_params_full2d(ref)
+    parts = diff_operator_parts(ref, pr)
+    dd = drift_data(ref, pr, Vref)
+    Kfull = assemble_kron(parts, pr["nCenterDof"], pr["nRelative"])
+    Vfull = assemble_drift(pr, dd)
+    nry, nX, nY = pr["rhoY"]["nCells"], pr["X"]["nDof"], pr["Y"]["nDof"]
+    ry, Y = np.meshgrid(np.arange(nry), np.arange(nY), indexing="ij")
+    ids = (0 + 2 * (ry + nry * (0 + nX * Y))).ravel(order="F")        # ids(1,:,1,:)(:)
+    K = Kfull[ids][:, ids].toarray()
+    Vt = 2.0 * Vfull[ids][:, ids].toarray()          # the rho_x diagonal of P_x' P_x / 4 is 1/2
+    return K, Vt
+
+
+def x_factors(ax, speeds, sigma):
+    """xFactors (get_LineTransversePreconditioner_full2D.m:177-200): [n, n, modes, elements]."""
+    n = ax["nLocal"]
+    Pl = np.zeros((n, n)); Pl[0, 0] = 1
+    Pr = np.zeros((n, n)); Pr[-1, -1] = 1
+    PfL = np.zeros((n, n)); PfL[0, -1] = 1
+    PfR = np.zeros((n, n)); PfR[-1, 0] = 1
+    K1 = np.linalg.solve(ax["M"], ax["S"] + 0.5 * Pl - 0.5 * Pr)
+    K2 = np.linalg.solve(ax["M"], 0.5 * Pl + 0.5 * Pr)
+    ne, nm = ax["nElements"], len(speeds)
+    inv = np.zeros((n, n, nm, ne), dtype=complex)
+    cpl = np.zeros_like(inv)
+    fwd = speeds >= 0
+    for e in range(ne):
+        for k in range(nm):
+            a = speeds[k] / (sigma * ax["jacobian"][e])
+            inv[:, :, k, e] = np.linalg.solve(np.eye(n) + a * K1 + abs(a) * K2, np.eye(n))
+            cpl[:, :, k, e] = -a * np.linalg.solve(ax["M"], PfL) if fwd[k] else a * np.linalg.solve(ax["M"], PfR)
+    return inv, cpl, fwd
+
+
+def line_transverse(mat, p, V, dd, ix=0):
+    """get_LineTransversePreconditioner_full2D.m:17-113 (dense transverse factors)."""
+    prm = mat["dg"]["params"]
+    nm, nry, nY = p["rhoX"]["nCells"], p["rhoY"]["nCells"], p["Y"]["nDof"]
+    nT = nry * nY
+    lam, U = np.linalg.eigh(p["Ax1D"].toarray())        # Hermitian: real eigenvalues, unitary modes
+    lam = lam.real.copy()
+    lam[np.abs(lam) < 100 * np.spacing(np.max(np.abs(lam)))] = 0
+    K, Vt = transverse_reference(mat, V, ix)
+    wx = dd["cap"][:nm] - (0 if p["rhoY"]["periodic"] else 0)
+    from .dg1d import get_cap
+    wxp = get_cap(p["rhoX"]["cells"], p["rhoX"]["length"], p["rhoX"]["delta"])
+    wyp = get_cap(p["rhoY"]["cells"], p["rhoY"]["length"], p["rhoY"]["delta"])
+    if p["rhoY"]["periodic"]:
+        wyp = np.zeros_like(wyp)
+    capY = np.tile(wyp, nY) * dd["capc"]
+    capX = np.real(np.sum(np.conj(U) * (wxp[:, None] * U), axis=0)) * dd["capc"]
+    Pm = sp.diags([np.ones(nm), np.ones(nm)], [0, -1], shape=(nm + 1, nm)).toarray()
+    pw = np.real(np.sum(np.conj(U) * ((Pm.T @ Pm / 4) @ U), axis=0))
+    sx, _ = transport_scales(mat)
+    x_rate = abs(sx) * np.max(np.abs(lam)) / np.min(p["X"]["jacobian"])
+    t_rate = np.max(np.abs(K).sum(1)) + np.max(np.abs(Vt).sum(1)) + np.max(np.abs(capY)) + np.max(np.abs(capX))
+    sigma = _param(prm, "full2D_lineShift", _param(prm, "full2D_lineRelativeShift", 0.003) * max(x_rate, t_rate,
+                                                                                               np.finfo(float).tiny))
+    xinv, xcpl, fwd = x_factors(p["X"], sx * lam, sigma)
+    Binv = np.zeros((nm, nT, nT), dtype=complex)
+    for k in range(nm):
+        B = K + pw[k] * Vt + np.diag(capY + capX[k])
+        B = B / sigma + np.eye(nT)
+        Binv[k] = np.linalg.solve(B, np.eye(nT))
+    return dict(U=U, lam=lam, sigma=sigma, xinv=xinv, xcpl=xcpl, fwd=fwd, Binv=Binv, K=K, Vt=Vt, pw=pw,
+                capX=capX, capY=capY)
+
+
+def line_transverse_apply(p, d, r):
+    """applyInverse (get_LineTransversePreconditioner_full2D.m:202-238)."""
+    nm, nry, nX, nY = p["rhoX"]["nCells"], p["rhoY"]["nCells"], p["X"]["nDof"], p["Y"]["nDof"]
+    n, ne = p["X"]["nLocal"], p["X"]["nElements"]
+    R = np.asarray(r).reshape(nY, nX, nry, nm)            # C order: [Y][X][ry][mode]
+    W = np.einsum("ik,yxrk->yxri", np.conj(d["U"]).T @ np.eye(nm), R) if False else \
+        np.einsum("ki,yxrk->yxri", np.conj(d["U"]), R)   # w = U^H r along rho_x
+    Wl = W.reshape(nY, ne, n, nry, nm)                      # X = e n + a
+    out = np.zeros_like(Wl)
+    for k in range(nm):
+        order = range(ne) if d["fwd"][k] else range(ne - 1, -1, -1)
+        prev = np.zeros((nY, n, nry), dtype=complex)
+        for e in order:
+            blk = Wl[:, e, :, :, k] - np.einsum("ab,ybr->yar", d["xcpl"][:, :, k, e], prev)
+            prev = np.einsum("ab,ybr->yar", d["xinv"][:, :, k, e], blk)
+            out[:, e, :, :, k] = prev
+    Vv = out.reshape(nY, nX, nry, nm)
+    # transverse solve per mode and X dof over t = ry + nry Y
+    T = np.transpose(Vv, (3, 1, 0, 2)).reshape(nm, nX, nY * nry)   # [k][X][Y][ry] -> t = ry + nry Y
+    T = np.einsum("kst,kxt->kxs", d["Binv"], T)
+    Vv = np.transpose(T.reshape(nm, nX, nY, nry), (2, 1, 3, 0))     # back to [Y][X][ry][k]
+    Z = np.einsum("ik,yxrk->yxri", d["U"], Vv) / d["sigma"]
+    return Z.reshape(-1)
