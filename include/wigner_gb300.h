@@ -458,6 +458,36 @@ int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const 
 
 /* y = A x on host buffers (n = n_rho_x n_rho_y n_X n_Y complex entries). */
 int wg2d_apply(wg2d_problem* h, const double* x, double* y);
+
+/* Line-transverse preconditioner M = (sigma I + X_ref)(sigma I + T_ref) / sigma
+ * (get_LineTransversePreconditioner_full2D.m:17-238), factors built on the host as the reference
+ * does: U [n_rho_x][n_rho_x] complex row-major (column k = eigenmode k of -i D_rho_x), the shift
+ * sigma, the X-line factors x_inverse and x_coupling [n_rho_x][n_el_x][nk_x][nk_x] complex
+ * (row-major blocks), forward [n_rho_x] (1: sweep towards +X), and the inverses of the transverse
+ * blocks t_inverse [n_rho_x][nT][nT] complex with nT = n_rho_y n_Y (t = i_rho_y + n_rho_y i_Y). */
+int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, const double* x_inverse,
+                            const double* x_coupling, const int* forward, const double* t_inverse);
+int wg2d_precondition(wg2d_problem* h, const double* r, double* z);
+
+/* A rho = rhs by restarted GMRES(restart), right-preconditioned, to tol relative to |rhs|, at most
+ * maxit restart cycles (solveStationarySystem / runGmresWithProgress,
+ * solve_transport_DG_full2D.m:132-346, 422-506).  x: the warm start when use_x0 (a correction about
+ * x0, the tolerance still relative to |rhs|), the solution on return.  WG_NOT_CONVERGED is a status. */
+typedef struct {
+  double tol;
+  int maxit;
+  int restart;
+  int use_x0;
+} wg2d_solve_opts;
+typedef struct {
+  int flag;                 /* 0 converged, 1 not */
+  int iterations;           /* inner iterations */
+  int cycles;
+  double relres;            /* true relative residual at exit */
+  double initial_relres;
+  double rhs_norm;
+} wg2d_solve_info;
+int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts, wg2d_solve_info* info);
 /* Diagnostic: n applies to the resident device state; mean time of one apply in *ms, with the time
  * of its transport and potential kernels in parts_ms[0..1] (may be NULL). */
 int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms);

@@ -129,6 +129,18 @@ class Wg2dShape(C.Structure):
                 ("tensor_cores", C.c_int)]
 
 
+class Wg2dSolveOpts(C.Structure):
+    _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("restart", C.c_int), ("use_x0", C.c_int)]
+
+
+class Wg2dSolveInfo(C.Structure):
+    _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("cycles", C.c_int), ("relres", C.c_double),
+                ("initial_relres", C.c_double), ("rhs_norm", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 REQUEST_STATES = {0: "queued", 1: "running", 2: "done", 3: "failed"}
 
 
@@ -160,6 +172,9 @@ SIGNATURES = {
     "wg2d_set_potential": ([_H, C.c_int, C.c_int, _D, _D, _D], C.c_int),
     "wg2d_apply": ([_H, _D, _D], C.c_int),
     "wg2d_apply_repeat": ([_H, C.c_int, _D, _D], C.c_int),
+    "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D], C.c_int),
+    "wg2d_precondition": ([_H, _D, _D], C.c_int),
+    "wg2d_solve": ([_H, _D, _D, C.POINTER(Wg2dSolveOpts), C.POINTER(Wg2dSolveInfo)], C.c_int),
     "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),
     "wg_solve": ([_H, C.POINTER(WgSolveOpts), _D, C.POINTER(WgSolveInfo)], C.c_int),
     "wg_get_rho": ([_H, C.c_int, _D], C.c_int),

@@ -64,6 +64,21 @@ struct wg2d_problem {
   double2 *Uq = nullptr, *Rq = nullptr;
   bool drift_ready = false, potential_ready = false;
   cudaEvent_t ev[4] = {};
+  // line-transverse preconditioner (modes of -i D_rho_x, X lines, dense transverse inverses)
+  bool pre_ready = false;
+  double sigma = 1.0;
+  int nT = 0;
+  wg::OzakiRowsDev UH, Us;        // real embeddings of U^H and U / sigma (tensor-core path)
+  double2 *UHd = nullptr, *Usd = nullptr;   // the same as complex [nrx][nrx] row-major (FP64 path)
+  double2 *xinv = nullptr, *xcpl = nullptr; // [nrx][n_el_x][nk][nk]
+  int* fwd = nullptr;             // [nrx]
+  double2* tinv = nullptr;        // [nrx][nT][nT]
+  double2 *pa = nullptr, *pb = nullptr;     // [n] scratch of the preconditioner
+  // GMRES
+  int vm = 0;                     // basis vectors allocated
+  double2 *V = nullptr, *r = nullptr, *w = nullptr, *z = nullptr, *b = nullptr, *xs = nullptr;
+  double2 *H = nullptr, *g = nullptr, *sn = nullptr, *hc = nullptr, *hp = nullptr, *yc = nullptr;
+  double *cs = nullptr, *partial = nullptr, *nrm = nullptr;
   std::string err;
 };
 
@@ -358,6 +373,289 @@ __global__ void __launch_bounds__(128) f2d_dv_kernel(double* __restrict__ dV, co
                                             v_bilinear(gx, gy, V, nx, ny, X - hx, Y - hy, periodic);
 }
 
+// out[rx, col] = scale sum_j A[rx][j] G[j, col]  (dense complex A [nrx][nrx] row-major; FP64 modal transforms)
+__global__ void __launch_bounds__(512) f2d_dense_rx_kernel(const double2* __restrict__ A, const double2* __restrict__ G,
+                                                           double2* __restrict__ out, int nrx, long long ncols) {
+  extern __shared__ double2 sg[];       // [kRelxCols][nrx]
+  const long long c0 = (long long)blockIdx.x * kRelxCols;
+  const int nc = (int)min((long long)kRelxCols, ncols - c0);
+  for (int i = threadIdx.x; i < kRelxCols * nrx; i += blockDim.x) {
+    const int j = i / nrx, k = i - j * nrx;
+    sg[i] = j < nc ? G[(c0 + j) * nrx + k] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int rx = threadIdx.x;
+  if (rx >= nrx) return;
+  double2 acc[kRelxCols];
+#pragma unroll
+  for (int j = 0; j < kRelxCols; ++j) acc[j] = make_double2(0.0, 0.0);
+  const double2* Ar = A + (long long)rx * nrx;
+  for (int k = 0; k < nrx; ++k) {
+    const double2 a = Ar[k];
+#pragma unroll
+    for (int j = 0; j < kRelxCols; ++j) acc[j] = cfma(a, sg[j * nrx + k], acc[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < kRelxCols; ++j)
+    if (j < nc) out[(c0 + j) * nrx + rx] = acc[j];
+}
+
+// X lines per mode (xFactors / applyInverse of get_LineTransversePreconditioner_full2D.m:177-222):
+// for mode k, transverse (ry, Y): sweep the X elements upwind (forward[k]: e = 0 .. ne-1), each
+// element's nk values: prev = inv[k][e] (w_e - cpl[k][e] prev).  Thread per (k, ry, Y), k fastest.
+template <int NK>
+__global__ void __launch_bounds__(128) f2d_xline_kernel(const double2* __restrict__ W, double2* __restrict__ out,
+                                                        const double2* __restrict__ inv,
+                                                        const double2* __restrict__ cpl, const int* __restrict__ fwd,
+                                                        int nrx, int nry, int nX, int nY, int ne) {
+  const long long t = (long long)blockIdx.x * 128 + threadIdx.x;
+  const long long lines = (long long)nrx * nry * nY;
+  if (t >= lines) return;
+  const int k = (int)(t % nrx);
+  const long long q = t / nrx;
+  const int ry = (int)(q % nry);
+  const int Y = (int)(q / nry);
+  const long long nrel = (long long)nrx * nry;
+  const long long base = k + (long long)nrx * ry + nrel * (long long)nX * Y;
+  const bool f = fwd[k] != 0;
+  double2 prev[NK];
+#pragma unroll
+  for (int a = 0; a < NK; ++a) prev[a] = make_double2(0.0, 0.0);
+  for (int i = 0; i < ne; ++i) {
+    const int e = f ? i : ne - 1 - i;
+    const double2* Ci = cpl + ((long long)k * ne + e) * NK * NK;
+    const double2* Ii = inv + ((long long)k * ne + e) * NK * NK;
+    double2 blk[NK];
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      double2 v = W[base + nrel * (e * NK + a)];
+#pragma unroll
+      for (int b = 0; b < NK; ++b) {
+        const double2 c = Ci[a * NK + b];
+        v.x -= c.x * prev[b].x - c.y * prev[b].y;
+        v.y -= c.x * prev[b].y + c.y * prev[b].x;
+      }
+      blk[a] = v;
+    }
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      double2 v = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int b = 0; b < NK; ++b) v = cfma(Ii[a * NK + b], blk[b], v);
+      prev[a] = v;
+      out[base + nrel * (e * NK + a)] = v;
+    }
+  }
+}
+
+constexpr int kTxTile = 32;
+// transverse solve per mode k and X dof: v[k, t, X] <- Binv[k] v[k, :, X] over t = ry + nry Y.
+// Block (k, tile of kTxTile X dofs); Binv[k] and the tile staged in shared memory.
+__global__ void __launch_bounds__(256) f2d_transverse_kernel(const double2* __restrict__ Vin, double2* __restrict__ Vout,
+                                                             const double2* __restrict__ Binv, int nrx, int nry,
+                                                             int nX, int nY, int nT) {
+  extern __shared__ double2 sm[];       // [nT][nT] then [nT][kTxTile]
+  double2* Bs = sm;
+  double2* Ts = sm + (long long)nT * nT;
+  const int k = blockIdx.y;
+  const int X0 = blockIdx.x * kTxTile;
+  const int nx = min(kTxTile, nX - X0);
+  const long long nrel = (long long)nrx * nry;
+  const double2* Bk = Binv + (long long)k * nT * nT;
+  for (int i = threadIdx.x; i < nT * nT; i += blockDim.x) Bs[i] = Bk[i];
+  for (int i = threadIdx.x; i < nT * kTxTile; i += blockDim.x) {
+    const int s = i / kTxTile, xx = i - s * kTxTile;
+    const int ry = s % nry, Y = s / nry;
+    Ts[i] = xx < nx ? Vin[k + (long long)nrx * ry + nrel * ((long long)(X0 + xx) + (long long)nX * Y)]
+                    : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nT * kTxTile; i += blockDim.x) {
+    const int tt = i / kTxTile, xx = i - tt * kTxTile;
+    if (xx >= nx) continue;
+    double2 acc = make_double2(0.0, 0.0);
+    const double2* Br = Bs + (long long)tt * nT;
+    for (int s2 = 0; s2 < nT; ++s2) acc = cfma(Br[s2], Ts[s2 * kTxTile + xx], acc);
+    const int ry = tt % nry, Y = tt / nry;
+    Vout[k + (long long)nrx * ry + nrel * ((long long)(X0 + xx) + (long long)nX * Y)] = acc;
+  }
+}
+
+// ---------------- GMRES vector kernels (FP64, deterministic two-stage reductions)
+constexpr int kDotBlocks = 1024;
+// partial[(i * kDotBlocks + blk) * 2 + {0,1}] = sum over the block's chunk of conj(V_i) w
+__global__ void __launch_bounds__(256) f2d_dot_partial(const double2* __restrict__ V, long long vstride,
+                                                       const double2* __restrict__ w, double* __restrict__ partial,
+                                                       long long n) {
+  __shared__ double sre[256], sim[256];
+  const int i = blockIdx.y;
+  const double2* v = V + (long long)i * vstride;
+  double re = 0.0, im = 0.0;
+  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n; t += (long long)gridDim.x * 256) {
+    const double2 a = v[t], b = w[t];
+    re = fma(a.x, b.x, fma(a.y, b.y, re));
+    im = fma(a.x, b.y, fma(-a.y, b.x, im));
+  }
+  sre[threadIdx.x] = re;
+  sim[threadIdx.x] = im;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sre[threadIdx.x] += sre[threadIdx.x + o];
+      sim[threadIdx.x] += sim[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[((long long)i * gridDim.x + blockIdx.x) * 2] = sre[0];
+    partial[((long long)i * gridDim.x + blockIdx.x) * 2 + 1] = sim[0];
+  }
+}
+
+// out[i] = sum of the partials of vector i; one block per vector
+__global__ void __launch_bounds__(256) f2d_dot_reduce(const double* __restrict__ partial, double2* __restrict__ out,
+                                                      int nblk, int accumulate) {
+  __shared__ double sre[256], sim[256];
+  const int i = blockIdx.x;
+  double re = 0.0, im = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += 256) {
+    re += partial[((long long)i * nblk + b) * 2];
+    im += partial[((long long)i * nblk + b) * 2 + 1];
+  }
+  sre[threadIdx.x] = re;
+  sim[threadIdx.x] = im;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sre[threadIdx.x] += sre[threadIdx.x + o];
+      sim[threadIdx.x] += sim[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (accumulate) {
+      out[i].x += sre[0];
+      out[i].y += sim[0];
+    } else {
+      out[i] = make_double2(sre[0], sim[0]);
+    }
+  }
+}
+
+// w -= sum_i h[i] V_i
+__global__ void __launch_bounds__(256) f2d_gs_update(const double2* __restrict__ V, long long vstride,
+                                                     double2* __restrict__ w, const double2* __restrict__ h, int nv,
+                                                     long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  double2 acc = w[t];
+  for (int i = 0; i < nv; ++i) {
+    const double2 v = V[(long long)i * vstride + t], c = h[i];
+    acc.x -= c.x * v.x - c.y * v.y;
+    acc.y -= c.x * v.y + c.y * v.x;
+  }
+  w[t] = acc;
+}
+
+// out = a * x (a = 1 / nrm[0] when inv, else a = nrm[0]); x may alias out
+__global__ void __launch_bounds__(256) f2d_scale(const double2* __restrict__ x, double2* __restrict__ out,
+                                                 const double* __restrict__ nrm, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  const double a = nrm[0] > 0 ? 1.0 / nrm[0] : 0.0;
+  out[t] = make_double2(a * x[t].x, a * x[t].y);
+}
+
+// y = x + a z (a complex on the host side as two doubles); r = b - y when residual
+__global__ void __launch_bounds__(256) f2d_axpy(double2* __restrict__ x, const double2* __restrict__ z, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  x[t].x += z[t].x;
+  x[t].y += z[t].y;
+}
+
+__global__ void __launch_bounds__(256) f2d_sub(const double2* __restrict__ b, double2* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  y[t] = make_double2(b[t].x - y[t].x, b[t].y - y[t].y);
+}
+
+// |x|^2 of the dot result (real part) -> nrm[0] = sqrt
+__global__ void f2d_sqrt_real(const double2* __restrict__ d, double* __restrict__ nrm) {
+  nrm[0] = sqrt(fmax(d[0].x, 0.0));
+}
+
+// Hessenberg column j (hc[0..j] from Gram-Schmidt, nrm[0] = |w|): previous Givens rotations, the
+// new one, the rotated right-hand side; g[j+1] is the residual estimate.  One thread.
+__global__ void f2d_givens(double2* __restrict__ H, const double2* __restrict__ hc, const double* __restrict__ nrm,
+                           double* __restrict__ cs, double2* __restrict__ sn, double2* __restrict__ g, int j, int ldh) {
+  double2* col = H + (long long)j * ldh;
+  for (int i = 0; i <= j; ++i) col[i] = hc[i];
+  col[j + 1] = make_double2(nrm[0], 0.0);
+  for (int i = 0; i < j; ++i) {
+    const double c = cs[i];
+    const double2 s = sn[i], a = col[i], b = col[i + 1];
+    // [c s; -conj(s) c] [a; b]
+    col[i] = make_double2(c * a.x + s.x * b.x - s.y * b.y, c * a.y + s.x * b.y + s.y * b.x);
+    col[i + 1] = make_double2(-(s.x * a.x + s.y * a.y) + c * b.x, -(s.x * a.y - s.y * a.x) + c * b.y);
+  }
+  const double2 a = col[j];
+  const double bb = col[j + 1].x;
+  const double aa = hypot(a.x, a.y);
+  const double rho = hypot(aa, bb);
+  double c;
+  double2 s, top;
+  if (rho == 0.0) {
+    c = 1.0;
+    s = make_double2(0.0, 0.0);
+    top = a;
+  } else if (aa == 0.0) {
+    c = 0.0;
+    s = make_double2(1.0, 0.0);
+    top = make_double2(bb, 0.0);
+  } else {
+    c = aa / rho;
+    const double2 ph = make_double2(a.x / aa, a.y / aa);
+    s = make_double2(ph.x * bb / rho, ph.y * bb / rho);        // (a/|a|) conj(b) / rho, b real
+    top = make_double2(ph.x * rho, ph.y * rho);
+  }
+  cs[j] = c;
+  sn[j] = s;
+  col[j] = top;
+  col[j + 1] = make_double2(0.0, 0.0);
+  const double2 gj = g[j];
+  g[j] = make_double2(c * gj.x, c * gj.y);
+  g[j + 1] = make_double2(-(s.x * gj.x + s.y * gj.y), -(s.x * gj.y - s.y * gj.x));
+}
+
+// y = R^-1 g for the leading k x k upper triangle of H; one thread
+__global__ void f2d_backsolve(const double2* __restrict__ H, const double2* __restrict__ g, double2* __restrict__ y,
+                              int k, int ldh) {
+  for (int i = k - 1; i >= 0; --i) {
+    double2 s = g[i];
+    for (int j = i + 1; j < k; ++j) {
+      const double2 h = H[(long long)j * ldh + i], v = y[j];
+      s.x -= h.x * v.x - h.y * v.y;
+      s.y -= h.x * v.y + h.y * v.x;
+    }
+    const double2 d = H[(long long)i * ldh + i];
+    const double den = d.x * d.x + d.y * d.y;
+    y[i] = den > 0 ? make_double2((s.x * d.x + s.y * d.y) / den, (s.y * d.x - s.x * d.y) / den)
+                   : make_double2(0.0, 0.0);
+  }
+}
+
+// u = sum_i y_i V_i
+__global__ void __launch_bounds__(256) f2d_combine(const double2* __restrict__ V, long long vstride,
+                                                   const double2* __restrict__ y, double2* __restrict__ u, int k,
+                                                   long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int i = 0; i < k; ++i) acc = cfma(y[i], V[(long long)i * vstride + t], acc);
+  u[t] = acc;
+}
+
 int fail(wg2d_problem* h, int code, const std::string& msg) {
   if (h) h->err = msg;
   return code;
@@ -457,6 +755,9 @@ bool supported_nloc(int n) { return n == 4 || n == 6 || n == 8 || n == 9 || n ==
 
 extern "C" {
 
+static void free_solver(wg2d_problem* h);
+static void free_preconditioner(wg2d_problem* h);
+
 int wg2d_create(const wg2d_shape* s, wg2d_problem** out) {
   if (!s || !out) return WG_ERR_ARG;
   *out = nullptr;
@@ -510,6 +811,8 @@ int wg2d_destroy(wg2d_problem* h) {
   if (!h) return WG_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);
   for (auto& a : h->ax) free_axis(a);
+  free_solver(h);
+  free_preconditioner(h);
   wg::ozaki_free(h->cols);
   void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap,
                   h->tc_err};
@@ -659,6 +962,85 @@ static int apply_device(wg2d_problem* h) {
   return apply_transport(h, 1);
 }
 
+// out = A in on device buffers (the kernels read h->x and write h->y at launch)
+static int apply_op(wg2d_problem* h, double2* in, double2* out) {
+  double2 *sx = h->x, *sy = h->y;
+  h->x = in;
+  h->y = out;
+  const int rc = apply_device(h);
+  h->x = sx;
+  h->y = sy;
+  return rc;
+}
+
+static unsigned blocks256(long long n) { return (unsigned)((n + 255) / 256); }
+
+// z = M^-1 r (applyInverse of get_LineTransversePreconditioner_full2D.m:202-238)
+static int precondition_device(wg2d_problem* h, const double2* r, double2* z) {
+  if (!h->pre_ready) return fail(h, WG_ERR_ARG, "wg2d: set the preconditioner first");
+  const long long ncols = h->n / h->nrx;
+  const int threads = (h->nrx + 31) / 32 * 32;
+  const size_t smem = sizeof(double2) * kRelxCols * h->nrx;
+  if (h->s.tensor_cores)
+    F2_CK(wg::ozaki_multiply(h->UH, h->cols, reinterpret_cast<const double*>(r), reinterpret_cast<double*>(h->pa),
+                             h->tc_err, h->stream));
+  else
+    f2d_dense_rx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+        h->UHd, r, h->pa, h->nrx, ncols);
+  const long long lines = (long long)h->nrx * h->nry * h->nY;
+  switch (h->s.nk_x) {
+    case 2: f2d_xline_kernel<2><<<(unsigned)((lines + 127) / 128), 128, 0, h->stream>>>(
+        h->pa, h->pb, h->xinv, h->xcpl, h->fwd, h->nrx, h->nry, h->nX, h->nY, h->s.n_el_x); break;
+    case 3: f2d_xline_kernel<3><<<(unsigned)((lines + 127) / 128), 128, 0, h->stream>>>(
+        h->pa, h->pb, h->xinv, h->xcpl, h->fwd, h->nrx, h->nry, h->nX, h->nY, h->s.n_el_x); break;
+    default: f2d_xline_kernel<4><<<(unsigned)((lines + 127) / 128), 128, 0, h->stream>>>(
+        h->pa, h->pb, h->xinv, h->xcpl, h->fwd, h->nrx, h->nry, h->nX, h->nY, h->s.n_el_x); break;
+  }
+  const size_t tsm = sizeof(double2) * ((size_t)h->nT * h->nT + (size_t)h->nT * kTxTile);
+  const dim3 tg((unsigned)((h->nX + kTxTile - 1) / kTxTile), (unsigned)h->nrx);
+  f2d_transverse_kernel<<<tg, 256, tsm, h->stream>>>(h->pb, h->pa, h->tinv, h->nrx, h->nry, h->nX, h->nY, h->nT);
+  if (h->s.tensor_cores)
+    F2_CK(wg::ozaki_multiply(h->Us, h->cols, reinterpret_cast<const double*>(h->pa), reinterpret_cast<double*>(z),
+                             h->tc_err, h->stream));
+  else
+    f2d_dense_rx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+        h->Usd, h->pa, z, h->nrx, ncols);
+  F2_CK(cudaGetLastError());
+  return WG_OK;
+}
+
+// out[0..nv) = V_i^H w (accumulate: out += ...)
+static void dots(wg2d_problem* h, const double2* V, int nv, const double2* w, double2* out, int accumulate) {
+  f2d_dot_partial<<<dim3(kDotBlocks, nv), 256, 0, h->stream>>>(V, h->n, w, h->partial, h->n);
+  f2d_dot_reduce<<<nv, 256, 0, h->stream>>>(h->partial, out, kDotBlocks, accumulate);
+}
+
+static void vnorm(wg2d_problem* h, const double2* w) {
+  dots(h, w, 1, w, h->hp, 0);
+  f2d_sqrt_real<<<1, 1, 0, h->stream>>>(h->hp, h->nrm);
+}
+
+static void free_solver(wg2d_problem* h) {
+  void* ptrs[] = {h->V, h->r, h->w, h->z, h->b, h->xs, h->H, h->g, h->sn, h->hc, h->hp, h->yc, h->cs, h->partial,
+                  h->nrm};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  h->V = h->r = h->w = h->z = h->b = h->xs = h->H = h->g = h->sn = h->hc = h->hp = h->yc = nullptr;
+  h->cs = h->partial = h->nrm = nullptr;
+  h->vm = 0;
+}
+
+static void free_preconditioner(wg2d_problem* h) {
+  wg::ozaki_free(h->UH);
+  wg::ozaki_free(h->Us);
+  void* ptrs[] = {h->UHd, h->Usd, h->xinv, h->xcpl, h->fwd, h->tinv, h->pa, h->pb};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  h->UHd = h->Usd = h->xinv = h->xcpl = h->tinv = h->pa = h->pb = nullptr;
+  h->fwd = nullptr;
+  h->pre_ready = false;
+}
+
 int wg2d_apply(wg2d_problem* h, const double* x, double* y) {
   if (!h || !x || !y) return h ? fail(h, WG_ERR_ARG, "wg2d_apply: null argument") : WG_ERR_ARG;
   F2_CK(cudaMemcpyAsync(h->x, x, sizeof(double2) * h->n, cudaMemcpyHostToDevice, h->stream));
@@ -703,6 +1085,189 @@ int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms) {
     parts_ms[1] = a;
   }
   return WG_OK;
+}
+
+
+// real embedding of a complex row-major n x n matrix scaled by a: [[re, -im], [im, re]] per entry
+static std::vector<double> embed(const double* A, int n, double a, bool conj_transpose) {
+  std::vector<double> E((size_t)4 * n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const size_t src = conj_transpose ? ((size_t)j * n + i) : ((size_t)i * n + j);
+      const double re = a * A[2 * src], im = (conj_transpose ? -a : a) * A[2 * src + 1];
+      E[(size_t)(2 * i) * 2 * n + 2 * j] = re;
+      E[(size_t)(2 * i) * 2 * n + 2 * j + 1] = -im;
+      E[(size_t)(2 * i + 1) * 2 * n + 2 * j] = im;
+      E[(size_t)(2 * i + 1) * 2 * n + 2 * j + 1] = re;
+    }
+  return E;
+}
+
+int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, const double* x_inverse,
+                            const double* x_coupling, const int* forward, const double* t_inverse) {
+  if (!h) return WG_ERR_ARG;
+  if (!U || !x_inverse || !x_coupling || !forward || !t_inverse || !(sigma > 0) || !std::isfinite(sigma))
+    return fail(h, WG_ERR_ARG, "wg2d_set_preconditioner: null argument or sigma not positive and finite");
+  const int nT = h->nry * h->nY;
+  const size_t tsm = sizeof(double2) * ((size_t)nT * nT + (size_t)nT * kTxTile);
+  if (tsm > 220 * 1024)
+    return fail(h, WG_ERR_ARG, "wg2d_set_preconditioner: transverse block n_rho_y * n_Y too large (at most ~104)");
+  cudaStreamSynchronize(h->stream);
+  free_preconditioner(h);
+  h->nT = nT;
+  h->sigma = sigma;
+  const int nr = h->nrx, nk = h->s.nk_x, ne = h->s.n_el_x;
+  const size_t nx = (size_t)nr * ne * nk * nk;
+  F2_CK(dalloc(&h->xinv, nx));
+  F2_CK(dalloc(&h->xcpl, nx));
+  F2_CK(dalloc(&h->fwd, nr));
+  F2_CK(dalloc(&h->tinv, (size_t)nr * nT * nT));
+  F2_CK(dalloc(&h->pa, h->n));
+  F2_CK(dalloc(&h->pb, h->n));
+  F2_CK(cudaMemcpy(h->xinv, x_inverse, sizeof(double2) * nx, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(h->xcpl, x_coupling, sizeof(double2) * nx, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(h->fwd, forward, sizeof(int) * nr, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(h->tinv, t_inverse, sizeof(double2) * nr * nT * nT, cudaMemcpyHostToDevice));
+  F2_CK(cudaFuncSetAttribute(f2d_transverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  if (h->nrx * kRelxCols * sizeof(double2) > 48 * 1024)
+    F2_CK(cudaFuncSetAttribute(f2d_dense_rx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(h->nrx * kRelxCols * sizeof(double2))));
+  if (h->s.tensor_cores) {
+    int rc = wg::ozaki_rows_upload(embed(U, nr, 1.0, true), 2 * nr, 2 * nr, h->UH, h->err);
+    if (!rc) rc = wg::ozaki_rows_upload(embed(U, nr, 1.0 / sigma, false), 2 * nr, 2 * nr, h->Us, h->err);
+    if (!rc && !h->cols.dig) rc = wg::ozaki_cols_alloc(h->n / nr, 2 * nr, h->cols, h->err);
+    if (rc) return rc;
+  } else {
+    std::vector<double> uh((size_t)2 * nr * nr), us((size_t)2 * nr * nr);
+    for (int i = 0; i < nr; ++i)
+      for (int j = 0; j < nr; ++j) {
+        uh[2 * ((size_t)i * nr + j)] = U[2 * ((size_t)j * nr + i)];
+        uh[2 * ((size_t)i * nr + j) + 1] = -U[2 * ((size_t)j * nr + i) + 1];
+        us[2 * ((size_t)i * nr + j)] = U[2 * ((size_t)i * nr + j)] / sigma;
+        us[2 * ((size_t)i * nr + j) + 1] = U[2 * ((size_t)i * nr + j) + 1] / sigma;
+      }
+    F2_CK(dalloc(&h->UHd, (size_t)nr * nr));
+    F2_CK(dalloc(&h->Usd, (size_t)nr * nr));
+    F2_CK(cudaMemcpy(h->UHd, uh.data(), sizeof(double) * uh.size(), cudaMemcpyHostToDevice));
+    F2_CK(cudaMemcpy(h->Usd, us.data(), sizeof(double) * us.size(), cudaMemcpyHostToDevice));
+  }
+  h->pre_ready = true;
+  return WG_OK;
+}
+
+int wg2d_precondition(wg2d_problem* h, const double* r, double* z) {
+  if (!h || !r || !z) return h ? fail(h, WG_ERR_ARG, "wg2d_precondition: null argument") : WG_ERR_ARG;
+  F2_CK(cudaMemcpyAsync(h->x, r, sizeof(double2) * h->n, cudaMemcpyHostToDevice, h->stream));
+  const int rc = precondition_device(h, h->x, h->y);
+  if (rc) return rc;
+  F2_CK(cudaMemcpyAsync(z, h->y, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  return WG_OK;
+}
+
+// Restarted GMRES(m), right-preconditioned with the line-transverse preconditioner, classical
+// Gram-Schmidt with a second pass, FP64 (runGmresWithProgress of solve_transport_DG_full2D.m:422-506
+// with MATLAB's gmres semantics: relative residual of the original system, warm start as x0).
+int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts, wg2d_solve_info* info) {
+  if (!h) return WG_ERR_ARG;
+  if (!rhs || !x || !opts || !info) return fail(h, WG_ERR_ARG, "wg2d_solve: null argument");
+  const int m = opts->restart > 0 ? opts->restart : 40;
+  const int maxit = opts->maxit > 0 ? opts->maxit : 50;
+  const double tol = opts->tol > 0 ? opts->tol : 1e-8;
+  if (m > 256) return fail(h, WG_ERR_ARG, "wg2d_solve: restart at most 256");
+  if (!h->pre_ready || !h->potential_ready) return fail(h, WG_ERR_ARG, "wg2d_solve: set potential and preconditioner first");
+  const long long n = h->n;
+  if (h->vm < m + 1) {
+    free_solver(h);
+    const size_t need = (size_t)(m + 1) * n * sizeof(double2);
+    size_t freeb = 0, total = 0;
+    cudaMemGetInfo(&freeb, &total);
+    if (need + 6 * n * sizeof(double2) > freeb) return fail(h, WG_ERR_OOM, "wg2d_solve: Krylov basis does not fit");
+    F2_CK(dalloc(&h->V, (size_t)(m + 1) * n));
+    F2_CK(dalloc(&h->r, n));
+    F2_CK(dalloc(&h->w, n));
+    F2_CK(dalloc(&h->z, n));
+    F2_CK(dalloc(&h->b, n));
+    F2_CK(dalloc(&h->xs, n));
+    F2_CK(dalloc(&h->H, (size_t)(m + 1) * m));
+    F2_CK(dalloc(&h->g, m + 1));
+    F2_CK(dalloc(&h->sn, m));
+    F2_CK(dalloc(&h->hc, m + 1));
+    F2_CK(dalloc(&h->hp, m + 1));
+    F2_CK(dalloc(&h->yc, m));
+    F2_CK(dalloc(&h->cs, m));
+    F2_CK(dalloc(&h->partial, (size_t)2 * kDotBlocks * (m + 1)));
+    F2_CK(dalloc(&h->nrm, 1));
+    h->vm = m + 1;
+  }
+  std::memset(info, 0, sizeof(*info));
+  F2_CK(cudaMemcpyAsync(h->b, rhs, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  if (opts->use_x0) F2_CK(cudaMemcpyAsync(h->xs, x, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  else F2_CK(cudaMemsetAsync(h->xs, 0, sizeof(double2) * n, h->stream));
+  double bnorm = 0, beta = 0;
+  vnorm(h, h->b);
+  F2_CK(cudaMemcpyAsync(&bnorm, h->nrm, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  auto true_residual = [&]() -> int {
+    int rc = apply_op(h, h->xs, h->r);
+    if (rc) return rc;
+    f2d_sub<<<blocks256(n), 256, 0, h->stream>>>(h->b, h->r, n);
+    vnorm(h, h->r);
+    F2_CK(cudaMemcpyAsync(&beta, h->nrm, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    F2_CK(cudaStreamSynchronize(h->stream));
+    return WG_OK;
+  };
+  int rc = true_residual();
+  if (rc) return rc;
+  info->rhs_norm = bnorm;
+  const double bn = bnorm > 0 ? bnorm : 1.0;
+  info->initial_relres = beta / bn;
+  const double target = tol * bn;
+  const int ldh = m + 1;
+  while (info->cycles < maxit && beta > target && std::isfinite(beta)) {
+    f2d_scale<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->V, h->nrm, n);
+    const double2 g0 = make_double2(beta, 0.0);
+    F2_CK(cudaMemsetAsync(h->g, 0, sizeof(double2) * (m + 1), h->stream));
+    F2_CK(cudaMemcpyAsync(h->g, &g0, sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+    int k = 0;
+    for (int j = 0; j < m; ++j) {
+      double2* Vj = h->V + (long long)j * n;
+      rc = precondition_device(h, Vj, h->z);
+      if (!rc) rc = apply_op(h, h->z, h->w);
+      if (rc) return rc;
+      dots(h, h->V, j + 1, h->w, h->hc, 0);
+      f2d_gs_update<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->w, h->hc, j + 1, n);
+      dots(h, h->V, j + 1, h->w, h->hp, 0);    // second pass
+      f2d_dot_reduce<<<j + 1, 256, 0, h->stream>>>(h->partial, h->hc, kDotBlocks, 1);   // hc += hp
+      f2d_gs_update<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->w, h->hp, j + 1, n);
+      vnorm(h, h->w);
+      f2d_givens<<<1, 1, 0, h->stream>>>(h->H, h->hc, h->nrm, h->cs, h->sn, h->g, j, ldh);
+      f2d_scale<<<blocks256(n), 256, 0, h->stream>>>(h->w, h->V + (long long)(j + 1) * n, h->nrm, n);
+      double2 gj;
+      F2_CK(cudaMemcpyAsync(&gj, h->g + j + 1, sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+      F2_CK(cudaStreamSynchronize(h->stream));
+      k = j + 1;
+      info->iterations += 1;
+      const double est = std::hypot(gj.x, gj.y);
+      if (!(est > target)) break;
+    }
+    f2d_backsolve<<<1, 1, 0, h->stream>>>(h->H, h->g, h->yc, k, ldh);
+    f2d_combine<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->yc, h->w, k, n);
+    rc = precondition_device(h, h->w, h->z);
+    if (rc) return rc;
+    f2d_axpy<<<blocks256(n), 256, 0, h->stream>>>(h->xs, h->z, n);
+    info->cycles += 1;
+    rc = true_residual();
+    if (rc) return rc;
+  }
+  int flag = 0;
+  F2_CK(cudaMemcpyAsync(x, h->xs, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaMemcpyAsync(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  if (flag) return fail(h, WG_ERR_TIMEOUT, "tensor-core GEMM: bounded barrier wait timed out");
+  info->relres = beta / bn;
+  if (!std::isfinite(beta)) return fail(h, WG_ERR_NUMERIC, "wg2d_solve: non-finite residual");
+  info->flag = beta <= target ? 0 : 1;
+  return info->flag ? WG_NOT_CONVERGED : WG_OK;
 }
 
 }  // extern "C"

@@ -884,4 +884,14 @@ cudaError_t ozaki_accumulate(const OzakiRowsDev& A, OzakiColsDev& B, const doubl
   return launch_ozaki<1>(A.map, B.map, A.e, B.e, C, A.M, B.ncol, A.Kp, err, st);
 }
 
+cudaError_t ozaki_multiply(const OzakiRowsDev& A, OzakiColsDev& B, const double* X, double* C, int* err,
+                           cudaStream_t st) {
+  if (B.Kp != A.Kp) return cudaErrorInvalidValue;
+  oz::slice_columns_kernel<<<slice_blocks(B.ncol), 32 * oz::kSliceColsPerBlock, 0, st>>>(X, A.K, B.ncol, B.dig, B.e,
+                                                                                        nullptr, 1, B.Kp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_ozaki<0>(A.map, B.map, A.e, B.e, C, A.M, B.ncol, A.Kp, err, st);
+}
+
 }  // namespace wg

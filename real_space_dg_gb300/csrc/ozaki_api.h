@@ -35,5 +35,8 @@ void ozaki_free(OzakiColsDev& b);
 // C += A X; err: device flag raised when a bounded barrier wait of the GEMM times out.
 cudaError_t ozaki_accumulate(const OzakiRowsDev& A, OzakiColsDev& B, const double* X, double* C, int* err,
                              cudaStream_t st);
+// C = A X (overwrites C).
+cudaError_t ozaki_multiply(const OzakiRowsDev& A, OzakiColsDev& B, const double* X, double* C, int* err,
+                           cudaStream_t st);
 
 }  // namespace wg

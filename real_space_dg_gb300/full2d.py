@@ -312,7 +312,118 @@ def build_factors(mat):
     return dict(shape=dict(n_el_x=nex, nk_x=nkx, n_el_y=ney, nk_y=nky, n_rho_x=nrx, n_rho_y=nry,
                            periodic_y=int(periodic)),
                 n=nrx * nry * nex * nkx * ney * nky, x=x, y=y, terms=(_merge(tx), _merge(ty)), axes=(AX, AY),
-                drift=drift, nq=nq)
+                rel=(RX, RY), scales=(sx, sy), drift=drift, nq=nq)
+
+
+def _bilinear(gx, gy, V, qx, qy, periodic):
+    """V at (qx, qy): X clamped, Y clamped or wrapped, linear in both (get_Drift_full2D.m:650-666)."""
+    qx = np.clip(qx, gx[0], gx[-1])
+    qy = gy[0] + np.mod(qy - gy[0], gy[-1] - gy[0]) if periodic else np.clip(qy, gy[0], gy[-1])
+    ix = np.clip(np.searchsorted(gx, qx, side="right") - 1, 0, len(gx) - 2)
+    iy = np.clip(np.searchsorted(gy, qy, side="right") - 1, 0, len(gy) - 2)
+    tx = (qx - gx[ix]) / (gx[ix + 1] - gx[ix])
+    ty = (qy - gy[iy]) / (gy[iy + 1] - gy[iy])
+    return ((1 - tx) * (1 - ty) * V[ix, iy] + tx * (1 - ty) * V[ix + 1, iy] + (1 - tx) * ty * V[ix, iy + 1]
+            + tx * ty * V[ix + 1, iy + 1])
+
+
+def _transverse_reference(mat, V, ix):
+    """Frozen-X transverse transport K and potential V blocks at material column ix: the
+    (rho_x cell 0, X dof 0) block of a strip with 2 rho_x cells, 2 X elements of 2 nodes, no X
+    transport and no CAP (transverseReference, get_LineTransversePreconditioner_full2D.m:127-175)."""
+    prm = dict(mat["dg"]["params"])
+    prm.update(N_rho_x=2, N_K_X=2, N_el_X=2, full2D_Q_diff_x=0.0, full2D_cap_scale=0.0)
+    strip = dict(mat)
+    strip["dg"] = dict(mat["dg"], params=prm)
+    fs = build_factors(strip)
+    s, (AX, AY), (RX, RY) = fs["shape"], fs["axes"], fs["rel"]
+    nry, nY = s["n_rho_y"], AY["nd"]
+    periodic = bool(s["periodic_y"])
+    K = np.zeros((nry * nY, nry * nY), dtype=complex)
+    for c, Cm, R in fs["terms"][1]:
+        K += c * np.kron(Cm, R)
+    for c, Cm, R in fs["terms"][0]:
+        if c != 0:
+            raise WignerError(_lib.WG_ERR_ARG, "strip with X transport")
+    d = fs["drift"]
+    Vr = np.repeat(np.asarray(V, dtype=float)[ix:ix + 1, :], len(fs["x"]), axis=0)
+    nq, nvx = fs["nq"], RX["n"] + 1
+    nvy = nry if periodic else nry + 1
+    # vertex sums P: (rho_x cell 0 touches vertices 0, 1 in x); cells of rho_y around each vertex
+    Ex = np.zeros((nvx, RX["n"])); Ex[np.arange(RX["n"]), np.arange(RX["n"])] = 1; Ex[np.arange(1, nvx), np.arange(RX["n"])] = 1
+    if periodic:                                      # vertex j touches cells j and j - 1 (mod n)
+        Ey = np.eye(nry); Ey[np.arange(nry), (np.arange(nry) - 1) % nry] += 1
+    else:
+        Ey = np.zeros((nry + 1, nry)); Ey[np.arange(nry), np.arange(nry)] = 1; Ey[np.arange(1, nry + 1), np.arange(nry)] = 1
+    P = np.kron(Ey, Ex)
+    sel = 2 * np.arange(nry)                          # rel = 0 + 2 ry
+    nkx, nky = AX["nl"], AY["nl"]
+    Vb = np.zeros_like(K)
+    for ey in range(AY["ne"]):
+        e = 0 + 2 * ey                                # element (ex = 0, ey)
+        X = d["xq"][e][None, :]
+        Yq = d["yq"][e][None, :]
+        hx, hy = 0.5 * d["vx"][:, None], 0.5 * d["vy"][:, None]
+        dV = _bilinear(fs["x"], fs["y"], Vr, X + hx, Yq + hy, periodic) - \
+            _bilinear(fs["x"], fs["y"], Vr, X - hx, Yq - hy, periodic)          # [n_vert, nq]
+        for ly in range(nky):
+            for ly2 in range(nky):
+                l, l2 = 0 + nkx * ly, 0 + nkx * ly2
+                acc = np.zeros((nry, nry), dtype=complex)
+                for q in range(nq):
+                    Hq = d["proj"][q, l] * d["interp"][q, l2]
+                    if Hq == 0:
+                        continue
+                    C = (P.T * dV[:, q]) @ P
+                    acc += Hq * C[np.ix_(sel, sel)]
+                Y1, Y2 = ey * nky + ly, ey * nky + ly2
+                Vb[Y1 * nry:(Y1 + 1) * nry, Y2 * nry:(Y2 + 1) * nry] += d["pot"] / 16 * acc
+    return K, 2.0 * Vb                                 # the rho_x diagonal of P_x' P_x / 4 is 1/2
+
+
+def build_preconditioner(mat, V, f, ix=0):
+    """Host factors of the line-transverse preconditioner (get_LineTransversePreconditioner_full2D.m:17-113):
+    modes U of -i D_rho_x, the shift sigma, X-line factors per mode and element, dense inverses of
+    the shifted transverse blocks per mode."""
+    prm = mat["dg"]["params"]
+    s, (AX, AY), (RX, RY) = f["shape"], f["axes"], f["rel"]
+    nm, nry, nY = s["n_rho_x"], s["n_rho_y"], AY["nd"]
+    nT = nry * nY
+    lam, U = np.linalg.eigh(-1j * RX["D"])
+    lam = lam.real.copy()
+    lam[np.abs(lam) < 100 * np.spacing(np.max(np.abs(lam)))] = 0
+    K, Vt = _transverse_reference(mat, V, ix)
+    d = f["drift"]
+    wx = cap_1d(RX["cells"], RX["length"], RX["delta"])
+    wy = np.zeros(nry) if s["periodic_y"] else cap_1d(RY["cells"], RY["length"], RY["delta"])
+    capY = np.tile(wy, nY) * d["capc"]
+    capX = np.real(np.sum(np.conj(U) * (wx[:, None] * U), axis=0)) * d["capc"]
+    Pm = np.zeros((nm + 1, nm)); Pm[np.arange(nm), np.arange(nm)] = 1; Pm[np.arange(1, nm + 1), np.arange(nm)] = 1
+    pw = np.real(np.sum(np.conj(U) * ((Pm.T @ Pm / 4) @ U), axis=0))
+    sx = f["scales"][0]
+    x_rate = abs(sx) * np.max(np.abs(lam)) / np.min(AX["jac"])
+    t_rate = np.max(np.abs(K).sum(1)) + np.max(np.abs(Vt).sum(1)) + np.max(np.abs(capY)) + np.max(np.abs(capX))
+    sigma = float(_param(prm, "full2D_lineShift", _param(prm, "full2D_lineRelativeShift", 0.003)
+                         * max(x_rate, t_rate, np.finfo(float).tiny)))
+    n, ne = AX["nl"], AX["ne"]
+    Minv = np.linalg.inv(AX["M"])
+    E = lambda i, j: np.eye(1, n * n, i * n + j).reshape(n, n)
+    K1 = Minv @ (AX["S"] + 0.5 * E(0, 0) - 0.5 * E(n - 1, n - 1))
+    K2 = Minv @ (0.5 * E(0, 0) + 0.5 * E(n - 1, n - 1))
+    speeds = sx * lam
+    fwd = (speeds >= 0).astype(np.int32)
+    xinv = np.zeros((nm, ne, n, n), dtype=complex)
+    xcpl = np.zeros_like(xinv)
+    for e in range(ne):
+        a = speeds / (sigma * AX["jac"][e])
+        for k in range(nm):
+            xinv[k, e] = np.linalg.inv(np.eye(n) + a[k] * K1 + abs(a[k]) * K2)
+            xcpl[k, e] = -a[k] * (Minv @ E(0, n - 1)) if fwd[k] else a[k] * (Minv @ E(n - 1, 0))
+    tinv = np.empty((nm, nT, nT), dtype=complex)
+    for k in range(nm):
+        B = (K + pw[k] * Vt + np.diag(capY + capX[k])) / sigma + np.eye(nT)
+        tinv[k] = np.linalg.inv(B)
+    return dict(U=U, lam=lam, sigma=sigma, xinv=xinv, xcpl=xcpl, fwd=fwd, tinv=tinv)
 
 
 def _merge(terms):
@@ -381,6 +492,8 @@ class Full2DOperator:
         self.lib = _lib.load()
         f = build_factors(mat)
         self.factors = f
+        self.mat = mat
+        self.V = None
         self.x, self.y, self.n, self.nq = f["x"], f["y"], f["n"], f["nq"]
         self.shape, self.terms, self.drift = f["shape"], f["terms"], f["drift"]
         s = f["shape"]
@@ -441,6 +554,43 @@ class Full2DOperator:
         Vc = np.ascontiguousarray(V.ravel(order="F"))
         self._check(self.lib.wg2d_set_potential(self.h, len(self.x), len(self.y), _lib.dptr(self.x),
                                                 _lib.dptr(self.y), _lib.dptr(Vc)))
+        self.V = V
+
+    def set_preconditioner(self, ix=0):
+        """Build the line-transverse preconditioner for the current potential (reference
+        column ix of the material grid) and hand it to the device."""
+        pre = build_preconditioner(self.mat, self.V, self.factors, ix)
+        self.pre = pre
+        U = np.ascontiguousarray(pre["U"], dtype=complex)
+        xi = np.ascontiguousarray(pre["xinv"], dtype=complex)
+        xc = np.ascontiguousarray(pre["xcpl"], dtype=complex)
+        ti = np.ascontiguousarray(pre["tinv"], dtype=complex)
+        fw = np.ascontiguousarray(pre["fwd"], dtype=np.int32)
+        self._check(self.lib.wg2d_set_preconditioner(self.h, _lib.dptr(U.view(np.float64)), float(pre["sigma"]),
+                                                     _lib.dptr(xi.view(np.float64)), _lib.dptr(xc.view(np.float64)),
+                                                     fw.ctypes.data_as(C.POINTER(C.c_int)),
+                                                     _lib.dptr(ti.view(np.float64))))
+
+    def precondition(self, r):
+        r = np.ascontiguousarray(np.asarray(r, dtype=complex).reshape(-1))
+        out = np.empty_like(r)
+        self._check(self.lib.wg2d_precondition(self.h, r.view(np.float64).ctypes.data_as(_lib._D),
+                                               out.view(np.float64).ctypes.data_as(_lib._D)))
+        return out
+
+    def solve(self, rhs, x0=None, tol=1e-8, maxit=50, restart=40):
+        """rho = A \\ rhs by right-preconditioned GMRES(restart) on the device; returns (status, info, rho)."""
+        b = np.ascontiguousarray(np.asarray(rhs, dtype=complex).reshape(-1))
+        x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(np.asarray(x0, dtype=complex).reshape(-1))
+        if b.size != self.n or x.size != self.n:
+            raise WignerError(_lib.WG_ERR_ARG, "rhs and x0 need %d entries" % self.n)
+        opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), int(restart), 0 if x0 is None else 1)
+        info = _lib.Wg2dSolveInfo()
+        st = self.lib.wg2d_solve(self.h, b.view(np.float64).ctypes.data_as(_lib._D),
+                                 x.view(np.float64).ctypes.data_as(_lib._D), C.byref(opts), C.byref(info))
+        if st not in (_lib.WG_OK, _lib.WG_NOT_CONVERGED):
+            self._check(st)
+        return st, info.as_dict(), x
 
     def apply(self, u):
         """y = A u (complex vector in the reference's order rho_x, rho_y, X, Y)."""
