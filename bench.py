@@ -733,7 +733,8 @@ def run_full2d(args):
     rhs = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     op.set_preconditioner()
     t0 = time.perf_counter()
-    st, sinfo, _ = op.solve(rhs, tol=5e-6, maxit=150, restart=40)
+    st, sinfo, _ = op.solve(rhs, tol=5e-6, maxit=args.solve_maxit, restart=40) if args.solve_maxit > 0 else \
+        (0, dict(iterations=0, cycles=0, relres=None), None)
     solve_s = time.perf_counter() - t0
     pre_ms = None
     try:
@@ -822,6 +823,8 @@ def main():
                     help="plain FP64 form with its two transforms as FP64 emulated on the tensor cores")
     ap.add_argument("--cpu-iters", type=int, default=8)
     ap.add_argument("--iters-per-point", type=float, default=ITERS_PER_POINT_FALLBACK)
+    ap.add_argument("--solve-maxit", type=int, default=150,
+                    help="full2d: restart cycles of the timed Full-2D solve (0: skip the solve)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

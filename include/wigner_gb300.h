@@ -380,6 +380,9 @@ int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, i
  * K x N, C column-major M x N, host buffers; 64 <= K <= 1024, K % 8 == 0.  No
  * counterpart in the reference. */
 int wg_debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K);
+/* The same with only the nd (1 .. 8) leading digits of each operand (error ~2^(-6 nd) of |A||B|),
+ * as the mixed form's residual uses for loose tolerances. */
+int wg_debug_gemm_f64_tc_digits(const double* A, const double* B, double* C, int M, int N, int K, int nd);
 
 /* Diagnostic: apply the operator n times to the resident state on the device and
  * return the mean time of one apply in *ms.  which = 0: the FP64 operator;

@@ -200,6 +200,7 @@ SIGNATURES = {
     "wg_debug_gemm_bf16": ([C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int,
                             C.c_int], C.c_int),
     "wg_debug_gemm_f64_tc": ([_D, _D, _D, C.c_int, C.c_int, C.c_int], C.c_int),
+    "wg_debug_gemm_f64_tc_digits": ([_D, _D, _D, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
     "wg_apply_repeat": ([_H, C.c_int, C.c_int, _D], C.c_int),
     "wg_event_record": ([_H, C.c_int], C.c_int),
     "wg_event_elapsed": ([_H, C.c_int, C.c_int, _D], C.c_int),

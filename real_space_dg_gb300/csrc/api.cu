@@ -668,6 +668,14 @@ int wg_debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int
   return WG_OK;
 }
 
+int wg_debug_gemm_f64_tc_digits(const double* A, const double* B, double* C, int M, int N, int K, int nd) {
+  if (!A || !B || !C || nd < 1 || nd > 8) return fail(nullptr, WG_ERR_ARG, "wg_debug_gemm_f64_tc_digits: null argument or nd outside 1 .. 8");
+  std::string err;
+  const int rc = wg::debug_gemm_f64_tc(A, B, C, M, N, K, err, nd);
+  if (rc) return fail(nullptr, rc, "wg_debug_gemm_f64_tc_digits: " + err);
+  return WG_OK;
+}
+
 int wg_apply_repeat(wg_problem* h, int which, int n, double* ms) {
   if (!h || !ms || n < 1 || which < 0 || which > 2) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_apply_repeat: bad argument");
   wg::Problem& P = h->P;

@@ -679,10 +679,10 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
 // r = b - A x and |r| (FP64; the mixed form's transforms on the tensor cores).  mask
 // (device, optional): only problems with mask[b] != 0 are evaluated, the others keep
 // their previous r and |r| (their x has not changed since).
-int true_residual(Problem& P, const int* mask = nullptr) {
+int true_residual(Problem& P, const int* mask = nullptr, int nd = 8) {
   const long long tot = P.N * P.batch;
   P.prof.launches[PROF_OTHER] += 3;
-  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w, mask));
+  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w, mask, nd));
   else WG_CK(launch_apply(P, P.x, P.w));
   residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot, P.N, mask);
   norm_partial_kernel<double2><<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk,
@@ -691,6 +691,27 @@ int true_residual(Problem& P, const int* mask = nullptr) {
                                                    P.inv64, nullptr, mask);
   WG_CK(cudaGetLastError());
   return WG_OK;
+}
+
+// Leading digits of the emulated FP64 transforms for the mixed form's true residual: enough
+// that the residual's error (~2^(-6 nd) |A||x|, with a margin of 2^21 for |A||x| / |b|) stays
+// below the loosest target among the problems it is evaluated for; 8 (the full split) for
+// tolerances of 1e-7 and below.  WG_RESIDUAL_DIGITS (1 .. 8) fixes it.
+int residual_digits(const Problem& P, double tol, const std::vector<int>* hmask) {
+  static const int forced = [] {
+    const char* v = std::getenv("WG_RESIDUAL_DIGITS");
+    const int d = v ? std::atoi(v) : 0;
+    return (d >= 1 && d <= 8) ? d : 0;
+  }();
+  if (forced) return forced;
+  double tmin = INFINITY;
+  for (int b = 0; b < P.batch; ++b) {
+    if (hmask && (int)hmask->size() == P.batch && !(*hmask)[b]) continue;
+    tmin = std::min(tmin, P.tol_pp.empty() ? tol : P.tol_pp[b]);
+  }
+  if (!(tmin > 0) || !(tmin < 1e299)) return 8;
+  const int d = (int)std::ceil((std::log2(1.0 / tmin) + 21.0) / 6.0);
+  return std::max(4, std::min(8, d));
 }
 
 // Shared set-up: |b| per problem, targets, initial true residual.
@@ -708,13 +729,19 @@ int solve_begin(Problem& P, double tol, bool warm, std::vector<double>& bnorm, s
   for (int b = 0; b < B; ++b) tgt[b] = (P.tol_pp.empty() ? tol : P.tol_pp[b]) * bnorm[b];
   // problems frozen by an unreachable tolerance keep their residual
   const int* mask = nullptr;
-  if (!P.tol_pp.empty() && P.precision == WG_PREC_MIXED) {
-    P.h_res_mask.assign(B, 1);
-    for (int b = 0; b < B; ++b) P.h_res_mask[b] = P.tol_pp[b] < 1e299 ? 1 : 0;
-    WG_CK(cudaMemcpyAsync(P.res_mask, P.h_res_mask.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
-    mask = P.res_mask;
+  int nd = 8;
+  if (P.precision == WG_PREC_MIXED) {
+    if (!P.tol_pp.empty()) {
+      P.h_res_mask.assign(B, 1);
+      for (int b = 0; b < B; ++b) P.h_res_mask[b] = P.tol_pp[b] < 1e299 ? 1 : 0;
+      WG_CK(cudaMemcpyAsync(P.res_mask, P.h_res_mask.data(), sizeof(int) * B, cudaMemcpyHostToDevice, P.stream));
+      mask = P.res_mask;
+      nd = residual_digits(P, tol, &P.h_res_mask);
+    } else {
+      nd = residual_digits(P, tol, nullptr);
+    }
   }
-  int rc = true_residual(P, mask);
+  int rc = true_residual(P, mask, nd);
   if (rc) return rc;
   res.resize(B);
   WG_CK(cudaMemcpyAsync(res.data(), P.nrm, sizeof(double) * B, cudaMemcpyDeviceToHost, P.stream));
@@ -954,7 +981,7 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     WG_CK(cudaGetLastError());
     // problems that did not move this refinement keep r and |r|; the others are re-evaluated
     WG_CK(cudaMemcpyAsync(P.nrm, P.nrm_keep, sizeof(double) * B, cudaMemcpyDeviceToDevice, P.stream));
-    rc = true_residual(P, P.res_mask);
+    rc = true_residual(P, P.res_mask, residual_digits(P, tol, &P.h_res_mask));
     if (rc) return rc;
     int herr = 0;
     WG_CK(cudaMemcpyAsync(&herr, M.err, sizeof(int), cudaMemcpyDeviceToHost, P.stream));

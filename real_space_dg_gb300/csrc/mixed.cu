@@ -110,13 +110,14 @@ unsigned slice_blocks(long long ncol) {
 template <int EPI>
 cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* ea, const int* eb, double* C, int M,
                          long long Ncol, int K, int* err, cudaStream_t st, const int* mask = nullptr,
-                         int cols_per_problem = 1) {
+                         int cols_per_problem = 1, int nd = oz::S) {
   static const cudaError_t attr = cudaFuncSetAttribute(oz::gemm_ozaki_kernel<EPI>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, oz::SMEM_BYTES);
   if (attr != cudaSuccess) return attr;
+  if (nd < 1 || nd > oz::S) return cudaErrorInvalidValue;
   dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
   oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err, mask,
-                                                                 cols_per_problem);
+                                                                 cols_per_problem, nd);
   return cudaGetLastError();
 }
 
@@ -721,7 +722,7 @@ int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int 
 
 // FP64 operator apply of the mixed form's outer residual: flux and xi stencil in
 // FP64, both transforms as digit-sliced FP64 GEMMs on the tensor cores.
-cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask) {
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask, int nd) {
   MixedBuffers& M = P.mx;
   if (!M.ozaki) return launch_apply(P, x, y);
   const Shape& s = P.s;
@@ -735,7 +736,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
       reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
-                      P.stream, mask, cpp);
+                      P.stream, mask, cpp, nd);
   prof_end(P, PROF_GEMM_F64, ev);
   if (e != cudaSuccess) return e;
   e = launch_stencil_f64(P, P.xh, P.yh, mask);
@@ -744,7 +745,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
       reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream,
-                      mask, cpp);
+                      mask, cpp, nd);
   prof_end(P, PROF_GEMM_F64, ev);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
@@ -752,7 +753,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
 
 // Stand-alone digit-sliced FP64 GEMM for diagnostics: C = A B with A row-major M x K,
 // B column-major K x N, C column-major M x N (host FP64 buffers), K <= 1024, K % 8 == 0.
-int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err) {
+int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err, int nd) {
   if (M < 1 || N < 1 || K < 64 || K % 8 || K > oz::MAX_K) {
     err = "debug FP64 GEMM needs 64 <= K <= 1024 and K % 8 == 0";
     return WG_ERR_ARG;
@@ -783,7 +784,7 @@ int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N,
       rc = WG_ERR_CUDA;
     } else {
       oz::slice_columns_kernel<<<slice_blocks(N), 32 * oz::kSliceColsPerBlock>>>(dB, K, N, db, deb);
-      e = launch_ozaki<0>(ma, mb, dea, deb, dC, M, N, K, derr, 0);
+      e = launch_ozaki<0>(ma, mb, dea, deb, dC, M, N, K, derr, 0, nullptr, 1, nd);
       if (e == cudaSuccess) e = cudaDeviceSynchronize();
       int herr = 0;
       if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);

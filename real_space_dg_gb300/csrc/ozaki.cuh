@@ -104,8 +104,9 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
                                                             const int* __restrict__ ea, const int* __restrict__ eb,
                                                             double* __restrict__ C, int M, long long Ncol, int K,
                                                             int* __restrict__ err, const int* __restrict__ mask,
-                                                            int cols_per_problem) {
-  // a column tile whose problems are all inactive (mask[b] == 0) has nothing to compute
+                                                            int cols_per_problem, int nd) {
+  // nd (1 .. S): leading digits used of each operand (products of weight < nd); the error grows
+  // to ~2^(-6 nd) of |A||B|.  A column tile whose problems are all inactive has nothing to compute.
   if (mask) {
     const long long c0 = (long long)blockIdx.y * BN, c1 = min(Ncol, c0 + BN) - 1;
     bool any = false;
@@ -144,8 +145,8 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
       if (kb >= STAGES && !tc::mbar_wait(&empty[st], ((kb / STAGES) + 1) & 1, err)) break;
       uint8_t* sa = smem + st * STAGE;
       uint8_t* sb = sa + S * A_SLICE;
-      tc::mbar_expect_tx(&full[st], STAGE);
-      for (int p = 0; p < S; ++p) {
+      tc::mbar_expect_tx(&full[st], (uint32_t)(nd * (A_SLICE + B_SLICE)));
+      for (int p = 0; p < nd; ++p) {
         tma_load_3d(sa + p * A_SLICE, &tmA, kb * BK, m0, p, &full[st]);
         tma_load_3d(sb + p * B_SLICE, &tmB, kb * BK, (int)n0, p, &full[st]);
       }
@@ -159,9 +160,9 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
       const uint8_t* sb = sa + S * A_SLICE;
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk)
-        for (int p = 0; p < S; ++p)
-          for (int q0 = 0; q0 + p < S; q0 += kSlicesPerMma) {   // weights p+q (0-based) <= S-1
-            const int n = min(kSlicesPerMma, S - p - q0);
+        for (int p = 0; p < nd; ++p)
+          for (int q0 = 0; q0 + p < nd; q0 += kSlicesPerMma) {   // weights p+q (0-based) <= nd-1
+            const int n = min(kSlicesPerMma, nd - p - q0);
             // slices q0 .. q0+n-1 are consecutive 64-row blocks: their accumulators, groups
             // p+q0 .. p+q0+n-1, are consecutive 64-column blocks of TMEM
             const uint32_t d = tmem + (uint32_t)((p + q0) * BN);
@@ -187,7 +188,7 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
 #pragma unroll
       for (int i = 0; i < 32; ++i) fx[i] = 0;
 #pragma unroll 1
-      for (int g = 0; g < NGROUP; ++g) {
+      for (int g = 0; g < nd; ++g) {
         float v[32];
         tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * BN + cb * 32), v);
 #pragma unroll

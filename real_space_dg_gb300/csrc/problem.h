@@ -296,8 +296,10 @@ double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner,
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int* mask = nullptr);
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const int* mask = nullptr);
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
-cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask = nullptr);
-int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err);
+// nd: leading digits of the emulated FP64 transforms (8: ~1e-14 of |Phi||x|; fewer for a
+// residual that only has to resolve a loose tolerance, ~2^(-6 nd)).
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask = nullptr, int nd = 8);
+int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err, int nd = 8);
 // Rebuild potential-dependent data (Vw weights, contact inflow rhs) of problems [b0, b1).
 // mask (device, optional): problems b with mask[b] == 0 are left untouched.
 cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask = nullptr);

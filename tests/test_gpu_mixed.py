@@ -68,6 +68,28 @@ def test_fp64_emulated_gemm(built_lib, M, N, K):
     assert np.all(Cout[N // 2] == 0.0)
 
 
+@pytest.mark.parametrize("nd", [3, 4, 5, 6, 7, 8])
+def test_fp64_emulated_gemm_fewer_digits(built_lib, nd):
+    """The emulated GEMM with only nd leading digits per operand (the mixed form's residual at
+    loose tolerances): error within 64 * 2^(-6 nd) of |A| |B| elementwise, and below it the
+    full split is more accurate."""
+    from real_space_dg_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(nd)
+    M, N, K = 256, 150, 512
+    A = rng.standard_normal((M, K)) * np.exp2(rng.integers(-20, 20, (M, 1)))
+    Bt = rng.standard_normal((N, K)) * np.exp2(rng.integers(-20, 20, (N, 1)))
+    Cout = np.zeros((N, M))
+    dp = lambda a: np.ascontiguousarray(a).ctypes.data_as(_lib._D)
+    st = lib.wg_debug_gemm_f64_tc_digits(dp(A), dp(Bt), dp(Cout), M, N, K, nd)
+    assert st == 0, lib.wg_global_error()
+    bound = np.abs(Bt) @ np.abs(A).T
+    err = np.abs(Cout - Bt @ A.T)
+    assert np.all(err <= 64 * 2.0 ** (-6 * nd) * bound)
+    if nd < 8:
+        assert err.max() / bound.max() > 2.0 ** (-6 * (nd + 1)) * 1e-3   # the digits really were dropped
+
+
 def make(spec, precision, batch=1, **kw):
     from real_space_dg_gb300 import Problem1D
     return Problem1D(n_el=spec.n_el, n_local=spec.n_local, nk=spec.nk, n_xi=spec.n_xi or spec.nk,
