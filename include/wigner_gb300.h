@@ -467,9 +467,12 @@ int wg2d_apply(wg2d_problem* h, const double* x, double* y);
  * does: U [n_rho_x][n_rho_x] complex row-major (column k = eigenmode k of -i D_rho_x), the shift
  * sigma, the X-line factors x_inverse and x_coupling [n_rho_x][n_el_x][nk_x][nk_x] complex
  * (row-major blocks), forward [n_rho_x] (1: sweep towards +X), and the inverses of the transverse
- * blocks t_inverse [n_rho_x][nT][nT] complex with nT = n_rho_y n_Y (t = i_rho_y + n_rho_y i_Y). */
+ * blocks t_inverse [n_rho_x][nT][nT] complex with nT = n_rho_y n_Y (t = i_rho_y + n_rho_y i_Y).
+ * fp32 = 1: the preconditioner runs in FP32 (an approximate inverse; wg2d_solve is a flexible GMRES,
+ * so the solve keeps its FP64 accuracy); 0: FP64 (mode transforms on the tensor cores when the
+ * handle was created with tensor_cores). */
 int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, const double* x_inverse,
-                            const double* x_coupling, const int* forward, const double* t_inverse);
+                            const double* x_coupling, const int* forward, const double* t_inverse, int fp32);
 int wg2d_precondition(wg2d_problem* h, const double* r, double* z);
 
 /* A rho = rhs by restarted GMRES(restart), right-preconditioned, to tol relative to |rhs|, at most

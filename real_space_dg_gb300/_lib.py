@@ -172,7 +172,7 @@ SIGNATURES = {
     "wg2d_set_potential": ([_H, C.c_int, C.c_int, _D, _D, _D], C.c_int),
     "wg2d_apply": ([_H, _D, _D], C.c_int),
     "wg2d_apply_repeat": ([_H, C.c_int, _D, _D], C.c_int),
-    "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D], C.c_int),
+    "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D, C.c_int], C.c_int),
     "wg2d_precondition": ([_H, _D, _D], C.c_int),
     "wg2d_solve": ([_H, _D, _D, C.POINTER(Wg2dSolveOpts), C.POINTER(Wg2dSolveInfo)], C.c_int),
     "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),

@@ -50,7 +50,7 @@ void free_all(wg::Problem& P) {
   wg::gummel_free(P);
   void* ptrs[] = {P.phi, P.kvec, P.xi_edge, P.kap, P.betai, P.pre_dinv, P.pre_h, P.kmap_a, P.kmap_s, P.cosm, P.pinv, P.pp, P.flr, P.fxi, P.qd, P.beta, P.xq, P.pot_x,
                   P.pot_v, P.vslope, P.m_nodes, P.rhs, P.tr_b, P.x, P.w, P.z, P.r, P.V, P.xh, P.yh, P.H, P.cs, P.sn, P.g, P.hcol,
-                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.res_mask, P.md_count, P.gs_count, P.kused, P.any_active};
+                  P.ycoef, P.partial, P.nrm_partial, P.nrm, P.nrm_keep, P.inv64, P.target, P.active, P.reorth, P.res_mask, P.res_digits, P.md_count, P.gs_count, P.kused, P.any_active};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (P.stream) cudaStreamDestroy(P.stream);
@@ -296,6 +296,7 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   A(dalloc(&P.active, batch, bytes));
   A(dalloc(&P.reorth, batch, bytes));
   A(dalloc(&P.res_mask, batch, bytes));
+  A(dalloc(&P.res_digits, batch, bytes));
   A(dalloc(&P.md_count, batch, bytes));
   A(dalloc(&P.gs_count, batch, bytes));
   A(dalloc(&P.kused, batch, bytes));

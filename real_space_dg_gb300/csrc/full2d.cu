@@ -74,8 +74,12 @@ struct wg2d_problem {
   int* fwd = nullptr;             // [nrx]
   double2* tinv = nullptr;        // [nrx][nT][nT]
   double2 *pa = nullptr, *pb = nullptr;     // [n] scratch of the preconditioner
+  bool pre32 = false;             // the preconditioner in FP32 (its factors and scratch below)
+  float2 *UH32 = nullptr, *Us32 = nullptr, *xinv32 = nullptr, *xcpl32 = nullptr, *tinv32 = nullptr;
+  float2 *pa32 = nullptr, *pb32 = nullptr;
   // GMRES
   int vm = 0;                     // basis vectors allocated
+  double2* Zb = nullptr;          // [m][n] preconditioned basis (flexible GMRES)
   double2 *V = nullptr, *r = nullptr, *w = nullptr, *z = nullptr, *b = nullptr, *xs = nullptr;
   double2 *H = nullptr, *g = nullptr, *sn = nullptr, *hc = nullptr, *hp = nullptr, *yc = nullptr;
   double *cs = nullptr, *partial = nullptr, *nrm = nullptr;
@@ -93,6 +97,16 @@ __device__ __forceinline__ double2 cfma(double2 a, double2 b, double2 c) {   // 
   c.y = fma(a.x, b.y, fma(a.y, b.x, c.y));
   return c;
 }
+
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+  c.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x));
+  c.y = fmaf(a.x, b.y, fmaf(a.y, b.x, c.y));
+  return c;
+}
+
+template <typename T> __device__ __forceinline__ T czero();
+template <> __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+template <> __device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
 
 // G_t[r, X, Y] = sum_{e', b} C_t[e][dir][a][b] F[r, X'(e', b), Y] along X (axis 0) or Y (axis 1).
 // grid (ceil(nrel/256), centre dofs of the other axis, n_el * nk of this axis).
@@ -374,24 +388,26 @@ __global__ void __launch_bounds__(128) f2d_dv_kernel(double* __restrict__ dV, co
 }
 
 // out[rx, col] = scale sum_j A[rx][j] G[j, col]  (dense complex A [nrx][nrx] row-major; FP64 modal transforms)
-__global__ void __launch_bounds__(512) f2d_dense_rx_kernel(const double2* __restrict__ A, const double2* __restrict__ G,
-                                                           double2* __restrict__ out, int nrx, long long ncols) {
-  extern __shared__ double2 sg[];       // [kRelxCols][nrx]
+template <typename T>
+__global__ void __launch_bounds__(512) f2d_dense_rx_kernel(const T* __restrict__ A, const T* __restrict__ G,
+                                                           T* __restrict__ out, int nrx, long long ncols) {
+  extern __shared__ __align__(16) unsigned char sg_raw[];
+  T* sg = reinterpret_cast<T*>(sg_raw);   // [kRelxCols][nrx]
   const long long c0 = (long long)blockIdx.x * kRelxCols;
   const int nc = (int)min((long long)kRelxCols, ncols - c0);
   for (int i = threadIdx.x; i < kRelxCols * nrx; i += blockDim.x) {
     const int j = i / nrx, k = i - j * nrx;
-    sg[i] = j < nc ? G[(c0 + j) * nrx + k] : make_double2(0.0, 0.0);
+    sg[i] = j < nc ? G[(c0 + j) * nrx + k] : czero<T>();
   }
   __syncthreads();
   const int rx = threadIdx.x;
   if (rx >= nrx) return;
-  double2 acc[kRelxCols];
+  T acc[kRelxCols];
 #pragma unroll
-  for (int j = 0; j < kRelxCols; ++j) acc[j] = make_double2(0.0, 0.0);
-  const double2* Ar = A + (long long)rx * nrx;
+  for (int j = 0; j < kRelxCols; ++j) acc[j] = czero<T>();
+  const T* Ar = A + (long long)rx * nrx;
   for (int k = 0; k < nrx; ++k) {
-    const double2 a = Ar[k];
+    const T a = Ar[k];
 #pragma unroll
     for (int j = 0; j < kRelxCols; ++j) acc[j] = cfma(a, sg[j * nrx + k], acc[j]);
   }
@@ -403,11 +419,11 @@ __global__ void __launch_bounds__(512) f2d_dense_rx_kernel(const double2* __rest
 // X lines per mode (xFactors / applyInverse of get_LineTransversePreconditioner_full2D.m:177-222):
 // for mode k, transverse (ry, Y): sweep the X elements upwind (forward[k]: e = 0 .. ne-1), each
 // element's nk values: prev = inv[k][e] (w_e - cpl[k][e] prev).  Thread per (k, ry, Y), k fastest.
-template <int NK>
-__global__ void __launch_bounds__(128) f2d_xline_kernel(const double2* __restrict__ W, double2* __restrict__ out,
-                                                        const double2* __restrict__ inv,
-                                                        const double2* __restrict__ cpl, const int* __restrict__ fwd,
-                                                        int nrx, int nry, int nX, int nY, int ne) {
+template <int NK, typename T>
+__global__ void __launch_bounds__(128) f2d_xline_kernel(const T* __restrict__ W, T* __restrict__ out,
+                                                        const T* __restrict__ inv, const T* __restrict__ cpl,
+                                                        const int* __restrict__ fwd, int nrx, int nry, int nX, int nY,
+                                                        int ne) {
   const long long t = (long long)blockIdx.x * 128 + threadIdx.x;
   const long long lines = (long long)nrx * nry * nY;
   if (t >= lines) return;
@@ -418,20 +434,20 @@ __global__ void __launch_bounds__(128) f2d_xline_kernel(const double2* __restric
   const long long nrel = (long long)nrx * nry;
   const long long base = k + (long long)nrx * ry + nrel * (long long)nX * Y;
   const bool f = fwd[k] != 0;
-  double2 prev[NK];
+  T prev[NK];
 #pragma unroll
-  for (int a = 0; a < NK; ++a) prev[a] = make_double2(0.0, 0.0);
+  for (int a = 0; a < NK; ++a) prev[a] = czero<T>();
   for (int i = 0; i < ne; ++i) {
     const int e = f ? i : ne - 1 - i;
-    const double2* Ci = cpl + ((long long)k * ne + e) * NK * NK;
-    const double2* Ii = inv + ((long long)k * ne + e) * NK * NK;
-    double2 blk[NK];
+    const T* Ci = cpl + ((long long)k * ne + e) * NK * NK;
+    const T* Ii = inv + ((long long)k * ne + e) * NK * NK;
+    T blk[NK];
 #pragma unroll
     for (int a = 0; a < NK; ++a) {
-      double2 v = W[base + nrel * (e * NK + a)];
+      T v = W[base + nrel * (e * NK + a)];
 #pragma unroll
       for (int b = 0; b < NK; ++b) {
-        const double2 c = Ci[a * NK + b];
+        const T c = Ci[a * NK + b];
         v.x -= c.x * prev[b].x - c.y * prev[b].y;
         v.y -= c.x * prev[b].y + c.y * prev[b].x;
       }
@@ -439,7 +455,7 @@ __global__ void __launch_bounds__(128) f2d_xline_kernel(const double2* __restric
     }
 #pragma unroll
     for (int a = 0; a < NK; ++a) {
-      double2 v = make_double2(0.0, 0.0);
+      T v = czero<T>();
 #pragma unroll
       for (int b = 0; b < NK; ++b) v = cfma(Ii[a * NK + b], blk[b], v);
       prev[a] = v;
@@ -451,34 +467,45 @@ __global__ void __launch_bounds__(128) f2d_xline_kernel(const double2* __restric
 constexpr int kTxTile = 32;
 // transverse solve per mode k and X dof: v[k, t, X] <- Binv[k] v[k, :, X] over t = ry + nry Y.
 // Block (k, tile of kTxTile X dofs); Binv[k] and the tile staged in shared memory.
-__global__ void __launch_bounds__(256) f2d_transverse_kernel(const double2* __restrict__ Vin, double2* __restrict__ Vout,
-                                                             const double2* __restrict__ Binv, int nrx, int nry,
+template <typename T>
+__global__ void __launch_bounds__(256) f2d_transverse_kernel(const T* __restrict__ Vin, T* __restrict__ Vout,
+                                                             const T* __restrict__ Binv, int nrx, int nry,
                                                              int nX, int nY, int nT) {
-  extern __shared__ double2 sm[];       // [nT][nT] then [nT][kTxTile]
-  double2* Bs = sm;
-  double2* Ts = sm + (long long)nT * nT;
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T* Bs = reinterpret_cast<T*>(sm_raw);   // [nT][nT] then [nT][kTxTile]
+  T* Ts = Bs + (long long)nT * nT;
   const int k = blockIdx.y;
   const int X0 = blockIdx.x * kTxTile;
   const int nx = min(kTxTile, nX - X0);
   const long long nrel = (long long)nrx * nry;
-  const double2* Bk = Binv + (long long)k * nT * nT;
+  const T* Bk = Binv + (long long)k * nT * nT;
   for (int i = threadIdx.x; i < nT * nT; i += blockDim.x) Bs[i] = Bk[i];
   for (int i = threadIdx.x; i < nT * kTxTile; i += blockDim.x) {
     const int s = i / kTxTile, xx = i - s * kTxTile;
     const int ry = s % nry, Y = s / nry;
     Ts[i] = xx < nx ? Vin[k + (long long)nrx * ry + nrel * ((long long)(X0 + xx) + (long long)nX * Y)]
-                    : make_double2(0.0, 0.0);
+                    : czero<T>();
   }
   __syncthreads();
   for (int i = threadIdx.x; i < nT * kTxTile; i += blockDim.x) {
     const int tt = i / kTxTile, xx = i - tt * kTxTile;
     if (xx >= nx) continue;
-    double2 acc = make_double2(0.0, 0.0);
-    const double2* Br = Bs + (long long)tt * nT;
+    T acc = czero<T>();
+    const T* Br = Bs + (long long)tt * nT;
     for (int s2 = 0; s2 < nT; ++s2) acc = cfma(Br[s2], Ts[s2 * kTxTile + xx], acc);
     const int ry = tt % nry, Y = tt / nry;
     Vout[k + (long long)nrx * ry + nrel * ((long long)(X0 + xx) + (long long)nX * Y)] = acc;
   }
+}
+
+__global__ void __launch_bounds__(256) f2d_to32(const double2* __restrict__ x, float2* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t < n) y[t] = make_float2((float)x[t].x, (float)x[t].y);
+}
+
+__global__ void __launch_bounds__(256) f2d_to64(const float2* __restrict__ x, double2* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t < n) y[t] = make_double2(x[t].x, x[t].y);
 }
 
 // ---------------- GMRES vector kernels (FP64, deterministic two-stage reductions)
@@ -975,36 +1002,59 @@ static int apply_op(wg2d_problem* h, double2* in, double2* out) {
 
 static unsigned blocks256(long long n) { return (unsigned)((n + 255) / 256); }
 
-// z = M^-1 r (applyInverse of get_LineTransversePreconditioner_full2D.m:202-238)
-static int precondition_device(wg2d_problem* h, const double2* r, double2* z) {
-  if (!h->pre_ready) return fail(h, WG_ERR_ARG, "wg2d: set the preconditioner first");
+// z = M^-1 r (applyInverse of get_LineTransversePreconditioner_full2D.m:202-238): modes along rho_x,
+// X lines per mode, transverse inverses per mode and X dof, back to rho_x.  FP32 (default for the
+// solve: an approximate inverse; the flexible GMRES keeps the solve exact for what was applied) or
+// FP64 with the mode transforms on the tensor cores.
+}  // extern "C"
+
+template <typename T>
+static void precond_stages(wg2d_problem* h, const T* UH, const T* Us, const T* xinv, const T* xcpl, const T* tinv,
+                           const T* r, T* pa, T* pb, T* z) {
   const long long ncols = h->n / h->nrx;
   const int threads = (h->nrx + 31) / 32 * 32;
-  const size_t smem = sizeof(double2) * kRelxCols * h->nrx;
-  if (h->s.tensor_cores)
+  const size_t smem = sizeof(T) * kRelxCols * h->nrx;
+  if (UH)
+    f2d_dense_rx_kernel<T><<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+        UH, r, pa, h->nrx, ncols);
+  const long long lines = (long long)h->nrx * h->nry * h->nY;
+  const unsigned lb = (unsigned)((lines + 127) / 128);
+  switch (h->s.nk_x) {
+    case 2: f2d_xline_kernel<2, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
+                                                             h->nY, h->s.n_el_x); break;
+    case 3: f2d_xline_kernel<3, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
+                                                             h->nY, h->s.n_el_x); break;
+    default: f2d_xline_kernel<4, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
+                                                              h->nY, h->s.n_el_x); break;
+  }
+  const size_t tsm = sizeof(T) * ((size_t)h->nT * h->nT + (size_t)h->nT * kTxTile);
+  const dim3 tg((unsigned)((h->nX + kTxTile - 1) / kTxTile), (unsigned)h->nrx);
+  f2d_transverse_kernel<T><<<tg, 256, tsm, h->stream>>>(pb, pa, tinv, h->nrx, h->nry, h->nX, h->nY, h->nT);
+  if (Us)
+    f2d_dense_rx_kernel<T><<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+        Us, pa, z, h->nrx, ncols);
+}
+
+extern "C" {
+
+static int precondition_device(wg2d_problem* h, const double2* r, double2* z) {
+  if (!h->pre_ready) return fail(h, WG_ERR_ARG, "wg2d: set the preconditioner first");
+  if (h->pre32) {
+    f2d_to32<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(r, h->pb32, h->n);
+    precond_stages<float2>(h, h->UH32, h->Us32, h->xinv32, h->xcpl32, h->tinv32, h->pb32, h->pa32, h->pb32, h->pb32);
+    f2d_to64<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(h->pb32, z, h->n);
+    F2_CK(cudaGetLastError());
+    return WG_OK;
+  }
+  if (h->s.tensor_cores) {
     F2_CK(wg::ozaki_multiply(h->UH, h->cols, reinterpret_cast<const double*>(r), reinterpret_cast<double*>(h->pa),
                              h->tc_err, h->stream));
-  else
-    f2d_dense_rx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
-        h->UHd, r, h->pa, h->nrx, ncols);
-  const long long lines = (long long)h->nrx * h->nry * h->nY;
-  switch (h->s.nk_x) {
-    case 2: f2d_xline_kernel<2><<<(unsigned)((lines + 127) / 128), 128, 0, h->stream>>>(
-        h->pa, h->pb, h->xinv, h->xcpl, h->fwd, h->nrx, h->nry, h->nX, h->nY, h->s.n_el_x); break;
-    case 3: f2d_xline_kernel<3><<<(unsigned)((lines + 127) / 128), 128, 0, h->stream>>>(
-        h->pa, h->pb, h->xinv, h->xcpl, h->fwd, h->nrx, h->nry, h->nX, h->nY, h->s.n_el_x); break;
-    default: f2d_xline_kernel<4><<<(unsigned)((lines + 127) / 128), 128, 0, h->stream>>>(
-        h->pa, h->pb, h->xinv, h->xcpl, h->fwd, h->nrx, h->nry, h->nX, h->nY, h->s.n_el_x); break;
-  }
-  const size_t tsm = sizeof(double2) * ((size_t)h->nT * h->nT + (size_t)h->nT * kTxTile);
-  const dim3 tg((unsigned)((h->nX + kTxTile - 1) / kTxTile), (unsigned)h->nrx);
-  f2d_transverse_kernel<<<tg, 256, tsm, h->stream>>>(h->pb, h->pa, h->tinv, h->nrx, h->nry, h->nX, h->nY, h->nT);
-  if (h->s.tensor_cores)
+    precond_stages<double2>(h, nullptr, nullptr, h->xinv, h->xcpl, h->tinv, r, h->pa, h->pb, z);
     F2_CK(wg::ozaki_multiply(h->Us, h->cols, reinterpret_cast<const double*>(h->pa), reinterpret_cast<double*>(z),
                              h->tc_err, h->stream));
-  else
-    f2d_dense_rx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
-        h->Usd, h->pa, z, h->nrx, ncols);
+  } else {
+    precond_stages<double2>(h, h->UHd, h->Usd, h->xinv, h->xcpl, h->tinv, r, h->pa, h->pb, z);
+  }
   F2_CK(cudaGetLastError());
   return WG_OK;
 }
@@ -1021,11 +1071,11 @@ static void vnorm(wg2d_problem* h, const double2* w) {
 }
 
 static void free_solver(wg2d_problem* h) {
-  void* ptrs[] = {h->V, h->r, h->w, h->z, h->b, h->xs, h->H, h->g, h->sn, h->hc, h->hp, h->yc, h->cs, h->partial,
-                  h->nrm};
+  void* ptrs[] = {h->V, h->Zb, h->r, h->w, h->z, h->b, h->xs, h->H, h->g, h->sn, h->hc, h->hp, h->yc, h->cs,
+                  h->partial, h->nrm};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  h->V = h->r = h->w = h->z = h->b = h->xs = h->H = h->g = h->sn = h->hc = h->hp = h->yc = nullptr;
+  h->V = h->Zb = h->r = h->w = h->z = h->b = h->xs = h->H = h->g = h->sn = h->hc = h->hp = h->yc = nullptr;
   h->cs = h->partial = h->nrm = nullptr;
   h->vm = 0;
 }
@@ -1033,11 +1083,14 @@ static void free_solver(wg2d_problem* h) {
 static void free_preconditioner(wg2d_problem* h) {
   wg::ozaki_free(h->UH);
   wg::ozaki_free(h->Us);
-  void* ptrs[] = {h->UHd, h->Usd, h->xinv, h->xcpl, h->fwd, h->tinv, h->pa, h->pb};
+  void* ptrs[] = {h->UHd, h->Usd, h->xinv, h->xcpl, h->fwd, h->tinv, h->pa, h->pb, h->UH32, h->Us32, h->xinv32,
+                  h->xcpl32, h->tinv32, h->pa32, h->pb32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   h->UHd = h->Usd = h->xinv = h->xcpl = h->tinv = h->pa = h->pb = nullptr;
+  h->UH32 = h->Us32 = h->xinv32 = h->xcpl32 = h->tinv32 = h->pa32 = h->pb32 = nullptr;
   h->fwd = nullptr;
+  h->pre32 = false;
   h->pre_ready = false;
 }
 
@@ -1104,33 +1157,67 @@ static std::vector<double> embed(const double* A, int n, double a, bool conj_tra
 }
 
 int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, const double* x_inverse,
-                            const double* x_coupling, const int* forward, const double* t_inverse) {
+                            const double* x_coupling, const int* forward, const double* t_inverse, int fp32) {
   if (!h) return WG_ERR_ARG;
   if (!U || !x_inverse || !x_coupling || !forward || !t_inverse || !(sigma > 0) || !std::isfinite(sigma))
     return fail(h, WG_ERR_ARG, "wg2d_set_preconditioner: null argument or sigma not positive and finite");
   const int nT = h->nry * h->nY;
-  const size_t tsm = sizeof(double2) * ((size_t)nT * nT + (size_t)nT * kTxTile);
+  const size_t tsm64 = sizeof(double2) * ((size_t)nT * nT + (size_t)nT * kTxTile);
+  const size_t tsm = fp32 ? tsm64 / 2 : tsm64;
   if (tsm > 220 * 1024)
-    return fail(h, WG_ERR_ARG, "wg2d_set_preconditioner: transverse block n_rho_y * n_Y too large (at most ~104)");
+    return fail(h, WG_ERR_ARG, "wg2d_set_preconditioner: transverse block n_rho_y * n_Y too large");
   cudaStreamSynchronize(h->stream);
   free_preconditioner(h);
   h->nT = nT;
   h->sigma = sigma;
   const int nr = h->nrx, nk = h->s.nk_x, ne = h->s.n_el_x;
-  const size_t nx = (size_t)nr * ne * nk * nk;
+  const size_t nx = (size_t)nr * ne * nk * nk, nt = (size_t)nr * nT * nT;
+  F2_CK(dalloc(&h->fwd, nr));
+  F2_CK(cudaMemcpy(h->fwd, forward, sizeof(int) * nr, cudaMemcpyHostToDevice));
+  // U^H and U / sigma as complex [nr][nr] row-major
+  std::vector<double> uh((size_t)2 * nr * nr), us((size_t)2 * nr * nr);
+  for (int i = 0; i < nr; ++i)
+    for (int j = 0; j < nr; ++j) {
+      uh[2 * ((size_t)i * nr + j)] = U[2 * ((size_t)j * nr + i)];
+      uh[2 * ((size_t)i * nr + j) + 1] = -U[2 * ((size_t)j * nr + i) + 1];
+      us[2 * ((size_t)i * nr + j)] = U[2 * ((size_t)i * nr + j)] / sigma;
+      us[2 * ((size_t)i * nr + j) + 1] = U[2 * ((size_t)i * nr + j) + 1] / sigma;
+    }
+  if (fp32) {
+    auto up32 = [&](float2** dst, const double* src, size_t count) -> int {
+      std::vector<float> f(2 * count);
+      for (size_t i = 0; i < 2 * count; ++i) f[i] = (float)src[i];
+      F2_CK(dalloc(dst, count));
+      F2_CK(cudaMemcpy(*dst, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+      return WG_OK;
+    };
+    int rc = up32(&h->xinv32, x_inverse, nx);
+    if (!rc) rc = up32(&h->xcpl32, x_coupling, nx);
+    if (!rc) rc = up32(&h->tinv32, t_inverse, nt);
+    if (!rc) rc = up32(&h->UH32, uh.data(), (size_t)nr * nr);
+    if (!rc) rc = up32(&h->Us32, us.data(), (size_t)nr * nr);
+    if (rc) return rc;
+    F2_CK(dalloc(&h->pa32, h->n));
+    F2_CK(dalloc(&h->pb32, h->n));
+    F2_CK(cudaFuncSetAttribute(f2d_transverse_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+    if (h->nrx * kRelxCols * sizeof(float2) > 48 * 1024)
+      F2_CK(cudaFuncSetAttribute(f2d_dense_rx_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(h->nrx * kRelxCols * sizeof(float2))));
+    h->pre32 = true;
+    h->pre_ready = true;
+    return WG_OK;
+  }
   F2_CK(dalloc(&h->xinv, nx));
   F2_CK(dalloc(&h->xcpl, nx));
-  F2_CK(dalloc(&h->fwd, nr));
-  F2_CK(dalloc(&h->tinv, (size_t)nr * nT * nT));
+  F2_CK(dalloc(&h->tinv, nt));
   F2_CK(dalloc(&h->pa, h->n));
   F2_CK(dalloc(&h->pb, h->n));
   F2_CK(cudaMemcpy(h->xinv, x_inverse, sizeof(double2) * nx, cudaMemcpyHostToDevice));
   F2_CK(cudaMemcpy(h->xcpl, x_coupling, sizeof(double2) * nx, cudaMemcpyHostToDevice));
-  F2_CK(cudaMemcpy(h->fwd, forward, sizeof(int) * nr, cudaMemcpyHostToDevice));
-  F2_CK(cudaMemcpy(h->tinv, t_inverse, sizeof(double2) * nr * nT * nT, cudaMemcpyHostToDevice));
-  F2_CK(cudaFuncSetAttribute(f2d_transverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
+  F2_CK(cudaMemcpy(h->tinv, t_inverse, sizeof(double2) * nt, cudaMemcpyHostToDevice));
+  F2_CK(cudaFuncSetAttribute(f2d_transverse_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm));
   if (h->nrx * kRelxCols * sizeof(double2) > 48 * 1024)
-    F2_CK(cudaFuncSetAttribute(f2d_dense_rx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    F2_CK(cudaFuncSetAttribute(f2d_dense_rx_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(h->nrx * kRelxCols * sizeof(double2))));
   if (h->s.tensor_cores) {
     int rc = wg::ozaki_rows_upload(embed(U, nr, 1.0, true), 2 * nr, 2 * nr, h->UH, h->err);
@@ -1138,14 +1225,6 @@ int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, cons
     if (!rc && !h->cols.dig) rc = wg::ozaki_cols_alloc(h->n / nr, 2 * nr, h->cols, h->err);
     if (rc) return rc;
   } else {
-    std::vector<double> uh((size_t)2 * nr * nr), us((size_t)2 * nr * nr);
-    for (int i = 0; i < nr; ++i)
-      for (int j = 0; j < nr; ++j) {
-        uh[2 * ((size_t)i * nr + j)] = U[2 * ((size_t)j * nr + i)];
-        uh[2 * ((size_t)i * nr + j) + 1] = -U[2 * ((size_t)j * nr + i) + 1];
-        us[2 * ((size_t)i * nr + j)] = U[2 * ((size_t)i * nr + j)] / sigma;
-        us[2 * ((size_t)i * nr + j) + 1] = U[2 * ((size_t)i * nr + j) + 1] / sigma;
-      }
     F2_CK(dalloc(&h->UHd, (size_t)nr * nr));
     F2_CK(dalloc(&h->Usd, (size_t)nr * nr));
     F2_CK(cudaMemcpy(h->UHd, uh.data(), sizeof(double) * uh.size(), cudaMemcpyHostToDevice));
@@ -1165,8 +1244,9 @@ int wg2d_precondition(wg2d_problem* h, const double* r, double* z) {
   return WG_OK;
 }
 
-// Restarted GMRES(m), right-preconditioned with the line-transverse preconditioner, classical
-// Gram-Schmidt with a second pass, FP64 (runGmresWithProgress of solve_transport_DG_full2D.m:422-506
+// Restarted flexible GMRES(m) (Saad's FGMRES: the preconditioned vectors are kept, so an FP32
+// preconditioner does not limit the FP64 accuracy), right-preconditioned with the line-transverse
+// preconditioner, classical Gram-Schmidt with a DGKS-gated second pass, FP64 (runGmresWithProgress of solve_transport_DG_full2D.m:422-506
 // with MATLAB's gmres semantics: relative residual of the original system, warm start as x0).
 int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts, wg2d_solve_info* info) {
   if (!h) return WG_ERR_ARG;
@@ -1179,11 +1259,12 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
   const long long n = h->n;
   if (h->vm < m + 1) {
     free_solver(h);
-    const size_t need = (size_t)(m + 1) * n * sizeof(double2);
+    const size_t need = (size_t)(2 * m + 1) * n * sizeof(double2);
     size_t freeb = 0, total = 0;
     cudaMemGetInfo(&freeb, &total);
     if (need + 6 * n * sizeof(double2) > freeb) return fail(h, WG_ERR_OOM, "wg2d_solve: Krylov basis does not fit");
     F2_CK(dalloc(&h->V, (size_t)(m + 1) * n));
+    F2_CK(dalloc(&h->Zb, (size_t)m * n));
     F2_CK(dalloc(&h->r, n));
     F2_CK(dalloc(&h->w, n));
     F2_CK(dalloc(&h->z, n));
@@ -1223,6 +1304,7 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
   info->initial_relres = beta / bn;
   const double target = tol * bn;
   const int ldh = m + 1;
+  int info_reorth = 0;
   while (info->cycles < maxit && beta > target && std::isfinite(beta)) {
     f2d_scale<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->V, h->nrm, n);
     const double2 g0 = make_double2(beta, 0.0);
@@ -1231,15 +1313,29 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     int k = 0;
     for (int j = 0; j < m; ++j) {
       double2* Vj = h->V + (long long)j * n;
-      rc = precondition_device(h, Vj, h->z);
-      if (!rc) rc = apply_op(h, h->z, h->w);
+      double2* Zj = h->Zb + (long long)j * n;      // flexible GMRES: keep z_j = M^-1 v_j
+      rc = precondition_device(h, Vj, Zj);
+      if (!rc) rc = apply_op(h, Zj, h->w);
       if (rc) return rc;
+      // classical Gram-Schmidt; a second pass only when the first lost more than half of |w|^2
+      // (Daniel-Gragg-Kaufman-Stewart: |w'|^2 < eta^2 (|w'|^2 + |h|^2), eta = 1/sqrt(2))
       dots(h, h->V, j + 1, h->w, h->hc, 0);
       f2d_gs_update<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->w, h->hc, j + 1, n);
-      dots(h, h->V, j + 1, h->w, h->hp, 0);    // second pass
-      f2d_dot_reduce<<<j + 1, 256, 0, h->stream>>>(h->partial, h->hc, kDotBlocks, 1);   // hc += hp
-      f2d_gs_update<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->w, h->hp, j + 1, n);
       vnorm(h, h->w);
+      std::vector<double2> hh(j + 1);
+      double w1 = 0;
+      F2_CK(cudaMemcpyAsync(hh.data(), h->hc, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, h->stream));
+      F2_CK(cudaMemcpyAsync(&w1, h->nrm, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+      F2_CK(cudaStreamSynchronize(h->stream));
+      double h2 = 0;
+      for (const double2& c : hh) h2 += c.x * c.x + c.y * c.y;
+      if (w1 * w1 < 0.5 * (w1 * w1 + h2)) {
+        dots(h, h->V, j + 1, h->w, h->hp, 0);    // second pass
+        f2d_dot_reduce<<<j + 1, 256, 0, h->stream>>>(h->partial, h->hc, kDotBlocks, 1);   // hc += hp
+        f2d_gs_update<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->w, h->hp, j + 1, n);
+        vnorm(h, h->w);
+        info_reorth += 1;
+      }
       f2d_givens<<<1, 1, 0, h->stream>>>(h->H, h->hc, h->nrm, h->cs, h->sn, h->g, j, ldh);
       f2d_scale<<<blocks256(n), 256, 0, h->stream>>>(h->w, h->V + (long long)(j + 1) * n, h->nrm, n);
       double2 gj;
@@ -1251,9 +1347,7 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
       if (!(est > target)) break;
     }
     f2d_backsolve<<<1, 1, 0, h->stream>>>(h->H, h->g, h->yc, k, ldh);
-    f2d_combine<<<blocks256(n), 256, 0, h->stream>>>(h->V, n, h->yc, h->w, k, n);
-    rc = precondition_device(h, h->w, h->z);
-    if (rc) return rc;
+    f2d_combine<<<blocks256(n), 256, 0, h->stream>>>(h->Zb, n, h->yc, h->z, k, n);   // x += Z y
     f2d_axpy<<<blocks256(n), 256, 0, h->stream>>>(h->xs, h->z, n);
     info->cycles += 1;
     rc = true_residual();

@@ -679,10 +679,10 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
 // r = b - A x and |r| (FP64; the mixed form's transforms on the tensor cores).  mask
 // (device, optional): only problems with mask[b] != 0 are evaluated, the others keep
 // their previous r and |r| (their x has not changed since).
-int true_residual(Problem& P, const int* mask = nullptr, int nd = 8) {
+int true_residual(Problem& P, const int* mask = nullptr, int nd = 8, const int* nd_pp = nullptr) {
   const long long tot = P.N * P.batch;
   P.prof.launches[PROF_OTHER] += 3;
-  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w, mask, nd));
+  if (P.precision == WG_PREC_MIXED) WG_CK(launch_apply_f64_tc(P, P.x, P.w, mask, nd, nd_pp));
   else WG_CK(launch_apply(P, P.x, P.w));
   residual_kernel<<<blocks_for(tot), 256, 0, P.stream>>>(P.rhs, P.w, P.r, tot, P.N, mask);
   norm_partial_kernel<double2><<<dim3(P.nchunk, P.batch), 256, 0, P.stream>>>(P.r, P.nrm_partial, P.N, P.nchunk,
@@ -697,6 +697,12 @@ int true_residual(Problem& P, const int* mask = nullptr, int nd = 8) {
 // that the residual's error (~2^(-6 nd) |A||x|, with a margin of 2^21 for |A||x| / |b|) stays
 // below the loosest target among the problems it is evaluated for; 8 (the full split) for
 // tolerances of 1e-7 and below.  WG_RESIDUAL_DIGITS (1 .. 8) fixes it.
+int digits_for(double t) {
+  if (!(t > 0) || !(t < 1e299)) return 8;
+  const int d = (int)std::ceil((std::log2(1.0 / t) + 21.0) / 6.0);
+  return std::max(4, std::min(8, d));
+}
+
 int residual_digits(const Problem& P, double tol, const std::vector<int>* hmask) {
   static const int forced = [] {
     const char* v = std::getenv("WG_RESIDUAL_DIGITS");
@@ -709,9 +715,19 @@ int residual_digits(const Problem& P, double tol, const std::vector<int>* hmask)
     if (hmask && (int)hmask->size() == P.batch && !(*hmask)[b]) continue;
     tmin = std::min(tmin, P.tol_pp.empty() ? tol : P.tol_pp[b]);
   }
-  if (!(tmin > 0) || !(tmin < 1e299)) return 8;
-  const int d = (int)std::ceil((std::log2(1.0 / tmin) + 21.0) / 6.0);
-  return std::max(4, std::min(8, d));
+  return digits_for(tmin);
+}
+
+// Digits per problem (the emulated GEMM's column tiles take the largest of their problems);
+// uploads them and returns the device array, or nullptr when one count serves all.
+const int* residual_digits_pp(Problem& P, double tol) {
+  if (P.tol_pp.empty() || std::getenv("WG_RESIDUAL_DIGITS")) return nullptr;
+  P.h_res_digits.assign(P.batch, 8);
+  for (int b = 0; b < P.batch; ++b) P.h_res_digits[b] = digits_for(P.tol_pp[b]);
+  if (cudaMemcpyAsync(P.res_digits, P.h_res_digits.data(), sizeof(int) * P.batch, cudaMemcpyHostToDevice,
+                      P.stream) != cudaSuccess)
+    return nullptr;
+  return P.res_digits;
 }
 
 // Shared set-up: |b| per problem, targets, initial true residual.
@@ -741,7 +757,7 @@ int solve_begin(Problem& P, double tol, bool warm, std::vector<double>& bnorm, s
       nd = residual_digits(P, tol, nullptr);
     }
   }
-  int rc = true_residual(P, mask, nd);
+  int rc = true_residual(P, mask, nd, P.precision == WG_PREC_MIXED ? residual_digits_pp(P, tol) : nullptr);
   if (rc) return rc;
   res.resize(B);
   WG_CK(cudaMemcpyAsync(res.data(), P.nrm, sizeof(double) * B, cudaMemcpyDeviceToHost, P.stream));
@@ -981,7 +997,7 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     WG_CK(cudaGetLastError());
     // problems that did not move this refinement keep r and |r|; the others are re-evaluated
     WG_CK(cudaMemcpyAsync(P.nrm, P.nrm_keep, sizeof(double) * B, cudaMemcpyDeviceToDevice, P.stream));
-    rc = true_residual(P, P.res_mask, residual_digits(P, tol, &P.h_res_mask));
+    rc = true_residual(P, P.res_mask, residual_digits(P, tol, &P.h_res_mask), residual_digits_pp(P, tol));
     if (rc) return rc;
     int herr = 0;
     WG_CK(cudaMemcpyAsync(&herr, M.err, sizeof(int), cudaMemcpyDeviceToHost, P.stream));

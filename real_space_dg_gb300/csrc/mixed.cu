@@ -110,14 +110,14 @@ unsigned slice_blocks(long long ncol) {
 template <int EPI>
 cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* ea, const int* eb, double* C, int M,
                          long long Ncol, int K, int* err, cudaStream_t st, const int* mask = nullptr,
-                         int cols_per_problem = 1, int nd = oz::S) {
+                         int cols_per_problem = 1, int nd = oz::S, const int* nd_pp = nullptr) {
   static const cudaError_t attr = cudaFuncSetAttribute(oz::gemm_ozaki_kernel<EPI>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, oz::SMEM_BYTES);
   if (attr != cudaSuccess) return attr;
   if (nd < 1 || nd > oz::S) return cudaErrorInvalidValue;
   dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
   oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err, mask,
-                                                                 cols_per_problem, nd);
+                                                                 cols_per_problem, nd, nd_pp);
   return cudaGetLastError();
 }
 
@@ -722,7 +722,8 @@ int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int 
 
 // FP64 operator apply of the mixed form's outer residual: flux and xi stencil in
 // FP64, both transforms as digit-sliced FP64 GEMMs on the tensor cores.
-cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask, int nd) {
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask, int nd,
+                                const int* nd_pp) {
   MixedBuffers& M = P.mx;
   if (!M.ozaki) return launch_apply(P, x, y);
   const Shape& s = P.s;
@@ -736,7 +737,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
       reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
-                      P.stream, mask, cpp, nd);
+                      P.stream, mask, cpp, nd, nd_pp);
   prof_end(P, PROF_GEMM_F64, ev);
   if (e != cudaSuccess) return e;
   e = launch_stencil_f64(P, P.xh, P.yh, mask);
@@ -745,7 +746,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
       reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream,
-                      mask, cpp, nd);
+                      mask, cpp, nd, nd_pp);
   prof_end(P, PROF_GEMM_F64, ev);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();

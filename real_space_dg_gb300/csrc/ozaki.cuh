@@ -104,14 +104,22 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
                                                             const int* __restrict__ ea, const int* __restrict__ eb,
                                                             double* __restrict__ C, int M, long long Ncol, int K,
                                                             int* __restrict__ err, const int* __restrict__ mask,
-                                                            int cols_per_problem, int nd) {
+                                                            int cols_per_problem, int nd,
+                                                            const int* __restrict__ nd_pp) {
   // nd (1 .. S): leading digits used of each operand (products of weight < nd); the error grows
-  // to ~2^(-6 nd) of |A||B|.  A column tile whose problems are all inactive has nothing to compute.
-  if (mask) {
+  // to ~2^(-6 nd) of |A||B|.  nd_pp (optional): digits per problem, the tile takes the largest of
+  // its problems.  A column tile whose problems are all inactive has nothing to compute.
+  if (mask || nd_pp) {
     const long long c0 = (long long)blockIdx.y * BN, c1 = min(Ncol, c0 + BN) - 1;
     bool any = false;
-    for (long long b = c0 / cols_per_problem; b <= c1 / cols_per_problem; ++b) any |= mask[b] != 0;
+    int ndt = 1;
+    for (long long b = c0 / cols_per_problem; b <= c1 / cols_per_problem; ++b) {
+      const bool on = !mask || mask[b] != 0;
+      any |= on;
+      if (nd_pp && on) ndt = max(ndt, min(S, max(1, nd_pp[b])));
+    }
     if (!any) return;
+    if (nd_pp) nd = ndt;
   }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));

@@ -255,6 +255,8 @@ struct Problem {
   int* active = nullptr;         // [B] 1 while iterating in this cycle
   int* reorth = nullptr;         // [B] 1 where the current Arnoldi step re-orthogonalises
   int* res_mask = nullptr;       // [B] problems whose true residual is evaluated
+  int* res_digits = nullptr;     // [B] digits of the emulated FP64 transforms per problem
+  std::vector<int> h_res_digits;
   ArnoldiGraphs graphs[2];       // [0] FP64 basis, [1] the mixed form's FP32 inner basis
   // launch shapes picked by the autotuner (tune.cu) on the first solve of a shape
   int kline_L = 4;               // elements per k-line chunk
@@ -298,7 +300,8 @@ cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
 // nd: leading digits of the emulated FP64 transforms (8: ~1e-14 of |Phi||x|; fewer for a
 // residual that only has to resolve a loose tolerance, ~2^(-6 nd)).
-cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask = nullptr, int nd = 8);
+cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const int* mask = nullptr, int nd = 8,
+                                const int* nd_pp = nullptr);
 int debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K, std::string& err, int nd = 8);
 // Rebuild potential-dependent data (Vw weights, contact inflow rhs) of problems [b0, b1).
 // mask (device, optional): problems b with mask[b] == 0 are left untouched.

@@ -556,9 +556,10 @@ class Full2DOperator:
                                                 _lib.dptr(self.y), _lib.dptr(Vc)))
         self.V = V
 
-    def set_preconditioner(self, ix=0):
+    def set_preconditioner(self, ix=0, fp32=True):
         """Build the line-transverse preconditioner for the current potential (reference
-        column ix of the material grid) and hand it to the device."""
+        column ix of the material grid) and hand it to the device; fp32: apply it in FP32
+        (the flexible GMRES keeps the solve's FP64 accuracy)."""
         pre = build_preconditioner(self.mat, self.V, self.factors, ix)
         self.pre = pre
         U = np.ascontiguousarray(pre["U"], dtype=complex)
@@ -569,7 +570,7 @@ class Full2DOperator:
         self._check(self.lib.wg2d_set_preconditioner(self.h, _lib.dptr(U.view(np.float64)), float(pre["sigma"]),
                                                      _lib.dptr(xi.view(np.float64)), _lib.dptr(xc.view(np.float64)),
                                                      fw.ctypes.data_as(C.POINTER(C.c_int)),
-                                                     _lib.dptr(ti.view(np.float64))))
+                                                     _lib.dptr(ti.view(np.float64)), 1 if fp32 else 0))
 
     def precondition(self, r):
         r = np.ascontiguousarray(np.asarray(r, dtype=complex).reshape(-1))

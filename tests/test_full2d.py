@@ -167,25 +167,29 @@ def test_host_preconditioner_factors_match_oracle(cfg):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("tensor_cores", [False, True])
+@pytest.mark.parametrize("tensor_cores,fp32,tol", [(False, False, 1e-12), (True, False, 1e-12), (True, True, 2e-5)])
 @pytest.mark.parametrize("cfg", CONFIGS)
-def test_gpu_preconditioner_matches_oracle(built_lib, cfg, tensor_cores):
+def test_gpu_preconditioner_matches_oracle(built_lib, cfg, tensor_cores, fp32, tol):
+    """FP64 (CUDA cores, or the mode transforms on the tensor cores): 1e-12; the FP32 form:
+    the single-precision rounding of an approximate inverse (2e-5)."""
     from real_space_dg_gb300.full2d import Full2DOperator
     mat, V = make_mat(**cfg)
     p, parts, dd = F2.system(mat, V)
     ref = F2.line_transverse(mat, p, V, dd)
     r = det_vec(p["nTotal"])
     with Full2DOperator(mat, V, tensor_cores=tensor_cores) as op:
-        op.set_preconditioner()
+        op.set_preconditioner(fp32=fp32)
         z = op.precondition(r)
-    assert rel(z, F2.line_transverse_apply(p, ref, r)) < 1e-12
+    assert rel(z, F2.line_transverse_apply(p, ref, r)) < tol
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("fp32", [True, False])
 @pytest.mark.parametrize("cfg", CONFIGS)
-def test_gpu_solve_matches_direct_solve(built_lib, cfg):
-    """Right-preconditioned GMRES(20) on the device against the oracle's sparse LU; a warm
-    start from the solution needs no iteration."""
+def test_gpu_solve_matches_direct_solve(built_lib, cfg, fp32):
+    """Flexible GMRES(20) on the device, preconditioned in FP32 or FP64, against the oracle's
+    sparse LU (the same FP64 accuracy either way); a warm start from the solution needs no
+    iteration."""
     import scipy.sparse.linalg as spla
     from real_space_dg_gb300.full2d import Full2DOperator
     mat, V = make_mat(**cfg)
@@ -194,7 +198,7 @@ def test_gpu_solve_matches_direct_solve(built_lib, cfg):
     b = det_vec(p["nTotal"])
     ref = spla.spsolve(A, b)
     with Full2DOperator(mat, V) as op:
-        op.set_preconditioner()
+        op.set_preconditioner(fp32=fp32)
         st, info, x = op.solve(b, tol=1e-11, maxit=200, restart=20)
         assert st == 0 and info["flag"] == 0, info
         assert info["relres"] <= 1e-11 and info["iterations"] > 0
