@@ -481,9 +481,12 @@ int wg2d_precondition(wg2d_problem* h, const double* r, double* z);
  * x0, the tolerance still relative to |rhs|), the solution on return.  WG_NOT_CONVERGED is a status. */
 typedef struct {
   double tol;
-  int maxit;
+  int maxit;                /* restart cycles (plain) or refinements (mixed) */
   int restart;
   int use_x0;
+  int mixed;                /* 1: FP64 refinement around FP32 flexible GMRES on the FP32 operator
+                               (needs the FP32 preconditioner); 0: FP64 flexible GMRES */
+  double inner_tol;         /* mixed: floor of each refinement's relative inner tolerance (default 1e-3) */
 } wg2d_solve_opts;
 typedef struct {
   int flag;                 /* 0 converged, 1 not */

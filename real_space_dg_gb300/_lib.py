@@ -130,7 +130,8 @@ class Wg2dShape(C.Structure):
 
 
 class Wg2dSolveOpts(C.Structure):
-    _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("restart", C.c_int), ("use_x0", C.c_int)]
+    _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("restart", C.c_int), ("use_x0", C.c_int),
+                ("mixed", C.c_int), ("inner_tol", C.c_double)]
 
 
 class Wg2dSolveInfo(C.Structure):

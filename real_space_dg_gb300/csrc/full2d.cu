@@ -77,6 +77,14 @@ struct wg2d_problem {
   bool pre32 = false;             // the preconditioner in FP32 (its factors and scratch below)
   float2 *UH32 = nullptr, *Us32 = nullptr, *xinv32 = nullptr, *xcpl32 = nullptr, *tinv32 = nullptr;
   float2 *pa32 = nullptr, *pb32 = nullptr;
+  // FP32 copies of the operator for the mixed solve's inner iterations
+  bool d32_ready = false;
+  float *blocks32[2] = {nullptr, nullptr}, *coef32[2] = {nullptr, nullptr};
+  float2* val32[2] = {nullptr, nullptr};
+  float *interp32 = nullptr, *proj32 = nullptr, *cap32 = nullptr, *dV32 = nullptr;
+  float2 *Uq32 = nullptr, *Rq32 = nullptr, *G32 = nullptr;
+  int vm32 = 0;
+  float2 *V32 = nullptr, *Z32 = nullptr, *w32 = nullptr;
   // GMRES
   int vm = 0;                     // basis vectors allocated
   double2* Zb = nullptr;          // [m][n] preconditioned basis (flexible GMRES)
@@ -110,9 +118,9 @@ template <> __device__ __forceinline__ float2 czero<float2>() { return make_floa
 
 // G_t[r, X, Y] = sum_{e', b} C_t[e][dir][a][b] F[r, X'(e', b), Y] along X (axis 0) or Y (axis 1).
 // grid (ceil(nrel/256), centre dofs of the other axis, n_el * nk of this axis).
-template <int NK>
-__global__ void __launch_bounds__(256) f2d_center_kernel(const double2* __restrict__ F, double2* __restrict__ G,
-                                                         const double* __restrict__ blocks, int T, int axis,
+template <int NK, typename T, typename R>
+__global__ void __launch_bounds__(256) f2d_center_kernel(const T* __restrict__ F, T* __restrict__ G,
+                                                         const R* __restrict__ blocks, int nterm, int axis,
                                                          int nrel, int nX, int nY, int n_el, int periodic,
                                                          long long n) {
   const int r = blockIdx.x * 256 + threadIdx.x;
@@ -122,7 +130,7 @@ __global__ void __launch_bounds__(256) f2d_center_kernel(const double2* __restri
   const int e = d / NK, a = d - e * NK;
   const int stride = axis == 0 ? nrel : nrel * nX;                     // between dofs of this axis
   const long long base = axis == 0 ? (long long)other * nX * nrel : (long long)other * nrel;
-  double2 f[3][NK];
+  T f[3][NK];
   bool has[3];
 #pragma unroll
   for (int dir = 0; dir < 3; ++dir) {
@@ -134,17 +142,17 @@ __global__ void __launch_bounds__(256) f2d_center_kernel(const double2* __restri
     }
 #pragma unroll
     for (int b = 0; b < NK; ++b)
-      f[dir][b] = has[dir] ? F[base + (long long)(en * NK + b) * stride + r] : make_double2(0.0, 0.0);
+      f[dir][b] = has[dir] ? F[base + (long long)(en * NK + b) * stride + r] : czero<T>();
   }
   const long long out = base + (long long)d * stride + r;
-  for (int t = 0; t < T; ++t) {
-    const double* B = blocks + ((long long)t * n_el + e) * 3 * NK * NK;
-    double2 acc = make_double2(0.0, 0.0);
+  for (int t = 0; t < nterm; ++t) {
+    const R* B = blocks + ((long long)t * n_el + e) * 3 * NK * NK;
+    T acc = czero<T>();
 #pragma unroll
     for (int dir = 0; dir < 3; ++dir)
 #pragma unroll
       for (int b = 0; b < NK; ++b) {
-        const double c = B[(dir * NK + a) * NK + b];
+        const R c = B[(dir * NK + a) * NK + b];
         acc.x = fma(c, f[dir][b].x, acc.x);
         acc.y = fma(c, f[dir][b].y, acc.y);
       }
@@ -155,33 +163,35 @@ __global__ void __launch_bounds__(256) f2d_center_kernel(const double2* __restri
 // y[rx, col] += sum_t c_t sum_k val_t[k] G_t[col_t[k], col] for kRelxCols columns per block;
 // the G_t columns are staged in shared memory, thread rx owns row rx (blockDim = nrx rounded
 // up to a warp multiple, at most 512).
-__global__ void __launch_bounds__(512) f2d_relx_kernel(const double2* __restrict__ G, double2* __restrict__ y,
+template <typename T, typename R>
+__global__ void __launch_bounds__(512) f2d_relx_kernel(const T* __restrict__ G, T* __restrict__ y,
                                                        const int* __restrict__ rp, const int* __restrict__ col,
-                                                       const double2* __restrict__ val, const int* __restrict__ nnz_off,
-                                                       const double* __restrict__ coef, int T, int nrx,
+                                                       const T* __restrict__ val, const int* __restrict__ nnz_off,
+                                                       const R* __restrict__ coef, int nterm, int nrx,
                                                        long long ncols, long long n, unsigned skip_mask) {
-  extern __shared__ double2 sg[];       // [kRelxCols][nrx]
+  extern __shared__ __align__(16) unsigned char sgr_raw[];
+  T* sg = reinterpret_cast<T*>(sgr_raw);   // [kRelxCols][nrx]
   const long long c0 = (long long)blockIdx.x * kRelxCols;
   const int nc = (int)min((long long)kRelxCols, ncols - c0);
   const int rx = threadIdx.x;
-  double2 acc[kRelxCols];
+  T acc[kRelxCols];
 #pragma unroll
-  for (int j = 0; j < kRelxCols; ++j) acc[j] = make_double2(0.0, 0.0);
-  for (int t = 0; t < T; ++t) {
+  for (int j = 0; j < kRelxCols; ++j) acc[j] = czero<T>();
+  for (int t = 0; t < nterm; ++t) {
     if ((skip_mask >> t) & 1u) continue;          // applied on the tensor cores
     __syncthreads();
     for (int i = threadIdx.x; i < kRelxCols * nrx; i += blockDim.x) {
       const int j = i / nrx, k = i - j * nrx;
-      sg[i] = j < nc ? G[(long long)t * n + (c0 + j) * nrx + k] : make_double2(0.0, 0.0);
+      sg[i] = j < nc ? G[(long long)t * n + (c0 + j) * nrx + k] : czero<T>();
     }
     __syncthreads();
     if (rx < nrx) {
-      const double ct = coef[t];
+      const R ct = coef[t];
       const int* rpt = rp + t * (nrx + 1);
       const int off = nnz_off[t];
       for (int k = rpt[rx]; k < rpt[rx + 1]; ++k) {
         const int cidx = col[off + k];
-        double2 v = val[off + k];
+        T v = val[off + k];
         v.x *= ct;
         v.y *= ct;
 #pragma unroll
@@ -193,7 +203,7 @@ __global__ void __launch_bounds__(512) f2d_relx_kernel(const double2* __restrict
 #pragma unroll
   for (int j = 0; j < kRelxCols; ++j) {
     if (j < nc) {
-      double2* o = y + (c0 + j) * nrx + rx;
+      T* o = y + (c0 + j) * nrx + rx;
       o->x += acc[j].x;
       o->y += acc[j].y;
     }
@@ -201,10 +211,11 @@ __global__ void __launch_bounds__(512) f2d_relx_kernel(const double2* __restrict
 }
 
 // y[rx, ry, c] += sum_t c_t sum_k val_t[k] G_t[rx, col_t[k], c]   (one thread per entry)
-__global__ void __launch_bounds__(256) f2d_rely_kernel(const double2* __restrict__ G, double2* __restrict__ y,
+template <typename T, typename R>
+__global__ void __launch_bounds__(256) f2d_rely_kernel(const T* __restrict__ G, T* __restrict__ y,
                                                        const int* __restrict__ rp, const int* __restrict__ col,
-                                                       const double2* __restrict__ val, const int* __restrict__ nnz_off,
-                                                       const double* __restrict__ coef, int T, int nrx, int nry,
+                                                       const T* __restrict__ val, const int* __restrict__ nnz_off,
+                                                       const R* __restrict__ coef, int nterm, int nrx, int nry,
                                                        long long n) {
   const long long i = (long long)blockIdx.x * 256 + threadIdx.x;
   if (i >= n) return;
@@ -213,11 +224,11 @@ __global__ void __launch_bounds__(256) f2d_rely_kernel(const double2* __restrict
   const int ry = (int)(q % nry);
   const long long c = q / nry;
   const long long cbase = c * (long long)nrx * nry + rx;
-  double2 acc = make_double2(0.0, 0.0);
-  for (int t = 0; t < T; ++t) {
+  T acc = czero<T>();
+  for (int t = 0; t < nterm; ++t) {
     const int* rpt = rp + t * (nry + 1);
     const int off = nnz_off[t];
-    double2 s = make_double2(0.0, 0.0);
+    T s = czero<T>();
     for (int k = rpt[ry]; k < rpt[ry + 1]; ++k)
       s = cfma(val[off + k], G[(long long)t * n + cbase + (long long)col[off + k] * nrx], s);
     acc.x = fma(coef[t], s.x, acc.x);
@@ -235,22 +246,22 @@ __device__ __forceinline__ long long center_id(int e, int l, int nex, int nkx, i
 }
 
 // Uq[e][q][r] = sum_l W[q][l] F[r, id(e, l)]; grid (ceil(nrel/128), n_el)
-template <int NL>
-__global__ void __launch_bounds__(128) f2d_interp_kernel(const double2* __restrict__ F, double2* __restrict__ Uq,
-                                                         const double* __restrict__ W, int nq, int nrel, int nex,
+template <int NL, typename T, typename R>
+__global__ void __launch_bounds__(128) f2d_interp_kernel(const T* __restrict__ F, T* __restrict__ Uq,
+                                                         const R* __restrict__ W, int nq, int nrel, int nex,
                                                          int nkx, int nky, int nX) {
   const int r = blockIdx.x * 128 + threadIdx.x;
   const int e = blockIdx.y;
   if (r >= nrel) return;
-  double2 u[NL];
+  T u[NL];
 #pragma unroll
   for (int l = 0; l < NL; ++l) u[l] = F[center_id(e, l, nex, nkx, nky, nX) * nrel + r];
-  double2* out = Uq + (long long)e * nq * nrel + r;
+  T* out = Uq + (long long)e * nq * nrel + r;
   for (int q = 0; q < nq; ++q) {
-    double2 s = make_double2(0.0, 0.0);
+    T s = czero<T>();
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
-      const double w = W[q * NL + l];
+      const R w = W[q * NL + l];
       s.x = fma(w, u[l].x, s.x);
       s.y = fma(w, u[l].y, s.y);
     }
@@ -259,9 +270,10 @@ __global__ void __launch_bounds__(128) f2d_interp_kernel(const double2* __restri
 }
 
 // sum of Uq over the cells around relative vertex (vi, vj) (cells vi-1..vi, vj-1..vj)
-__device__ __forceinline__ double2 vertex_sum(const double2* __restrict__ U, int vi, int vj, int nrx, int nry,
+template <typename T>
+__device__ __forceinline__ T vertex_sum(const T* __restrict__ U, int vi, int vj, int nrx, int nry,
                                               bool periodic) {
-  double2 s = make_double2(0.0, 0.0);
+  T s = czero<T>();
 #pragma unroll
   for (int dj = -1; dj <= 0; ++dj) {
     int j = vj + dj;
@@ -271,7 +283,7 @@ __device__ __forceinline__ double2 vertex_sum(const double2* __restrict__ U, int
     for (int di = -1; di <= 0; ++di) {
       const int i = vi + di;
       if (i < 0 || i >= nrx) continue;
-      const double2 v = U[j * nrx + i];
+      const T v = U[j * nrx + i];
       s.x += v.x;
       s.y += v.y;
     }
@@ -280,19 +292,20 @@ __device__ __forceinline__ double2 vertex_sum(const double2* __restrict__ U, int
 }
 
 // Rq[e][q][cell] = sum_{vertices v of cell} dV[e][q][v] vertex_sum(v); grid (ceil(nrel/128), nq, n_el)
-__global__ void __launch_bounds__(128) f2d_vertex_kernel(const double2* __restrict__ Uq, double2* __restrict__ Rq,
-                                                         const double* __restrict__ dV, int nrx, int nry, int nq,
+template <typename T, typename R>
+__global__ void __launch_bounds__(128) f2d_vertex_kernel(const T* __restrict__ Uq, T* __restrict__ Rq,
+                                                         const R* __restrict__ dV, int nrx, int nry, int nq,
                                                          int nvert, int periodic) {
   const int cell = blockIdx.x * 128 + threadIdx.x;
   const int nrel = nrx * nry;
   if (cell >= nrel) return;
   const int q = blockIdx.y, e = blockIdx.z;
   const long long slab = ((long long)e * nq + q);
-  const double2* U = Uq + slab * nrel;
-  const double* D = dV + slab * nvert;
+  const T* U = Uq + slab * nrel;
+  const R* D = dV + slab * nvert;
   const int i = cell % nrx, j = cell / nrx;
   const int nvx = nrx + 1;
-  double2 acc = make_double2(0.0, 0.0);
+  T acc = czero<T>();
 #pragma unroll
   for (int b = 0; b <= 1; ++b) {
     int vj = j + b;
@@ -300,8 +313,8 @@ __global__ void __launch_bounds__(128) f2d_vertex_kernel(const double2* __restri
 #pragma unroll
     for (int a = 0; a <= 1; ++a) {
       const int vi = i + a;
-      const double d = D[vj * nvx + vi];
-      const double2 s = vertex_sum(U, vi, vj, nrx, nry, periodic);
+      const R d = D[vj * nvx + vi];
+      const T s = vertex_sum<T>(U, vi, vj, nrx, nry, periodic);
       acc.x = fma(d, s.x, acc.x);
       acc.y = fma(d, s.y, acc.y);
     }
@@ -310,33 +323,33 @@ __global__ void __launch_bounds__(128) f2d_vertex_kernel(const double2* __restri
 }
 
 // y[r, id(e,l)] = pot/16 sum_q Cp[q][l] Rq[e][q][r] + capc cap[r] F[r, id(e,l)]; grid (ceil(nrel/128), n_el)
-template <int NL>
-__global__ void __launch_bounds__(128) f2d_project_kernel(const double2* __restrict__ Rq, const double2* __restrict__ F,
-                                                          double2* __restrict__ y, const double* __restrict__ Cp,
-                                                          const double* __restrict__ cap, double2 pot16, double capc,
+template <int NL, typename T, typename R>
+__global__ void __launch_bounds__(128) f2d_project_kernel(const T* __restrict__ Rq, const T* __restrict__ F,
+                                                          T* __restrict__ y, const R* __restrict__ Cp,
+                                                          const R* __restrict__ cap, T pot16, R capc,
                                                           int nq, int nrel, int nex, int nkx, int nky, int nX) {
   const int r = blockIdx.x * 128 + threadIdx.x;
   const int e = blockIdx.y;
   if (r >= nrel) return;
-  double2 s[NL];
+  T s[NL];
 #pragma unroll
-  for (int l = 0; l < NL; ++l) s[l] = make_double2(0.0, 0.0);
-  const double2* R = Rq + (long long)e * nq * nrel + r;
+  for (int l = 0; l < NL; ++l) s[l] = czero<T>();
+  const T* Rr = Rq + (long long)e * nq * nrel + r;
   for (int q = 0; q < nq; ++q) {
-    const double2 v = R[(long long)q * nrel];
+    const T v = Rr[(long long)q * nrel];
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
-      const double c = Cp[q * NL + l];
+      const R c = Cp[q * NL + l];
       s[l].x = fma(c, v.x, s[l].x);
       s[l].y = fma(c, v.y, s[l].y);
     }
   }
-  const double cr = capc * cap[r];
+  const R cr = capc * cap[r];
 #pragma unroll
   for (int l = 0; l < NL; ++l) {
     const long long idx = center_id(e, l, nex, nkx, nky, nX) * nrel + r;
-    const double2 f = F[idx];
-    double2 o;
+    const T f = F[idx];
+    T o;
     o.x = pot16.x * s[l].x - pot16.y * s[l].y + cr * f.x;
     o.y = pot16.x * s[l].y + pot16.y * s[l].x + cr * f.y;
     y[idx] = o;
@@ -506,6 +519,87 @@ __global__ void __launch_bounds__(256) f2d_to32(const double2* __restrict__ x, f
 __global__ void __launch_bounds__(256) f2d_to64(const float2* __restrict__ x, double2* __restrict__ y, long long n) {
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
   if (t < n) y[t] = make_double2(x[t].x, x[t].y);
+}
+
+__global__ void __launch_bounds__(256) f2d_to32_scaled(const double2* __restrict__ x, float2* __restrict__ y,
+                                                       const double* __restrict__ nrm, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  const double a = nrm[0] > 0 ? 1.0 / nrm[0] : 0.0;
+  if (t < n) y[t] = make_float2((float)(a * x[t].x), (float)(a * x[t].y));
+}
+
+__global__ void __launch_bounds__(256) f2d_d2f(const double* __restrict__ x, float* __restrict__ y, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t < n) y[t] = (float)x[t];
+}
+
+// FP32 inner products, summed per thread in FP32 and across threads and blocks in FP64
+__global__ void __launch_bounds__(256) f2d_dot_partial32(const float2* __restrict__ V, long long vstride,
+                                                         const float2* __restrict__ w, double* __restrict__ partial,
+                                                         long long n) {
+  __shared__ double sre[256], sim[256];
+  const int i = blockIdx.y;
+  const float2* v = V + (long long)i * vstride;
+  float re = 0.f, im = 0.f;
+  for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n; t += (long long)gridDim.x * 256) {
+    const float2 a = v[t], b = w[t];
+    re = fmaf(a.x, b.x, fmaf(a.y, b.y, re));
+    im = fmaf(a.x, b.y, fmaf(-a.y, b.x, im));
+  }
+  sre[threadIdx.x] = re;
+  sim[threadIdx.x] = im;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      sre[threadIdx.x] += sre[threadIdx.x + o];
+      sim[threadIdx.x] += sim[threadIdx.x + o];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    partial[((long long)i * gridDim.x + blockIdx.x) * 2] = sre[0];
+    partial[((long long)i * gridDim.x + blockIdx.x) * 2 + 1] = sim[0];
+  }
+}
+
+__global__ void __launch_bounds__(256) f2d_gs_update32(const float2* __restrict__ V, long long vstride,
+                                                       float2* __restrict__ w, const double2* __restrict__ h, int nv,
+                                                       long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  float2 acc = w[t];
+  for (int i = 0; i < nv; ++i) {
+    const float2 v = V[(long long)i * vstride + t];
+    const float cx = (float)h[i].x, cy = (float)h[i].y;
+    acc.x -= cx * v.x - cy * v.y;
+    acc.y -= cx * v.y + cy * v.x;
+  }
+  w[t] = acc;
+}
+
+__global__ void __launch_bounds__(256) f2d_scale32(const float2* __restrict__ x, float2* __restrict__ out,
+                                                   const double* __restrict__ nrm, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  const float a = nrm[0] > 0 ? (float)(1.0 / nrm[0]) : 0.f;
+  out[t] = make_float2(a * x[t].x, a * x[t].y);
+}
+
+// x += beta sum_i y_i Z_i (the FP32 correction of one refinement, added in FP64)
+__global__ void __launch_bounds__(256) f2d_correct32(double2* __restrict__ x, const float2* __restrict__ Z,
+                                                     long long zstride, const double2* __restrict__ y, int k,
+                                                     const double* __restrict__ beta, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int i = 0; i < k; ++i) {
+    const float2 z = Z[(long long)i * zstride + t];
+    const double2 c = y[i];
+    acc.x += c.x * z.x - c.y * z.y;
+    acc.y += c.x * z.y + c.y * z.x;
+  }
+  x[t].x += beta[0] * acc.x;
+  x[t].y += beta[0] * acc.y;
 }
 
 // ---------------- GMRES vector kernels (FP64, deterministic two-stage reductions)
@@ -710,68 +804,109 @@ void free_axis(wg2d_problem::Axis& a) {
   a = wg2d_problem::Axis{};
 }
 
-template <int NK>
-void launch_center(wg2d_problem* h, int axis) {
+// Operator data of one precision: FP64 (the handle's own arrays) or the FP32 copies of the mixed solve.
+template <typename T, typename R>
+struct OpData {
+  const R* blocks[2];
+  const T* val[2];
+  const R* coef[2];
+  const R *interp, *proj, *cap, *dV;
+  T *Uq, *Rq, *G;
+  T pot16;
+  R capc;
+};
+
+template <int NK, typename T, typename R>
+void launch_center(wg2d_problem* h, int axis, const T* F, T* G, const R* blocks) {
   const int nk = axis == 0 ? h->s.nk_x : h->s.nk_y;
   const int n_el = axis == 0 ? h->s.n_el_x : h->s.n_el_y;
   const int other = axis == 0 ? h->nY : h->nX;
   const dim3 grid((unsigned)((h->nrel + 255) / 256), (unsigned)other, (unsigned)(n_el * nk));
-  f2d_center_kernel<NK><<<grid, 256, 0, h->stream>>>(h->x, h->G, h->ax[axis].blocks, h->ax[axis].T, axis, h->nrel,
-                                                     h->nX, h->nY, n_el, axis == 1 ? h->s.periodic_y : 0, h->n);
+  f2d_center_kernel<NK, T, R><<<grid, 256, 0, h->stream>>>(F, G, blocks, h->ax[axis].T, axis, h->nrel, h->nX, h->nY,
+                                                           n_el, axis == 1 ? h->s.periodic_y : 0, h->n);
+}
+
+// y += transport terms of one axis; the terms in skip_mask are left to the caller
+template <typename T, typename R>
+void transport_terms(wg2d_problem* h, int axis, const OpData<T, R>& d, const T* F, T* y, unsigned skip_mask) {
+  wg2d_problem::Axis& a = h->ax[axis];
+  const int nk = axis == 0 ? h->s.nk_x : h->s.nk_y;
+  switch (nk) {
+    case 2: launch_center<2, T, R>(h, axis, F, d.G, d.blocks[axis]); break;
+    case 3: launch_center<3, T, R>(h, axis, F, d.G, d.blocks[axis]); break;
+    default: launch_center<4, T, R>(h, axis, F, d.G, d.blocks[axis]); break;
+  }
+  if (axis == 0) {
+    const long long ncols = h->n / h->nrx;
+    const size_t smem = sizeof(T) * kRelxCols * h->nrx;
+    const int threads = (h->nrx + 31) / 32 * 32;
+    if (skip_mask != (1u << a.T) - 1u)
+      f2d_relx_kernel<T, R><<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
+          d.G, y, a.rp, a.col, d.val[0], a.offs, d.coef[0], a.T, h->nrx, ncols, h->n, skip_mask);
+  } else {
+    f2d_rely_kernel<T, R><<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(d.G, y, a.rp, a.col, d.val[1], a.offs,
+                                                                                d.coef[1], a.T, h->nrx, h->nry, h->n);
+  }
+}
+
+OpData<double2, double> op64(wg2d_problem* h) {
+  OpData<double2, double> d;
+  for (int a = 0; a < 2; ++a) {
+    d.blocks[a] = h->ax[a].blocks;
+    d.val[a] = h->ax[a].val;
+    d.coef[a] = h->ax[a].dcoef;
+  }
+  d.interp = h->interp;
+  d.proj = h->proj;
+  d.cap = h->cap;
+  d.dV = h->dV;
+  d.Uq = h->Uq;
+  d.Rq = h->Rq;
+  d.G = h->G;
+  d.pot16 = make_double2(h->pot.x / 16.0, h->pot.y / 16.0);
+  d.capc = h->capc;
+  return d;
 }
 
 int apply_transport(wg2d_problem* h, int axis) {
   wg2d_problem::Axis& a = h->ax[axis];
   if (a.T == 0) return WG_OK;
-  const int nk = axis == 0 ? h->s.nk_x : h->s.nk_y;
-  switch (nk) {
-    case 2: launch_center<2>(h, axis); break;
-    case 3: launch_center<3>(h, axis); break;
-    default: launch_center<4>(h, axis); break;
-  }
-  const int* nnz_off = a.offs;
-  const double* coef = a.dcoef;
-  if (axis == 0) {
-    const long long ncols = h->n / h->nrx;
-    const size_t smem = sizeof(double2) * kRelxCols * h->nrx;
-    const int threads = (h->nrx + 31) / 32 * 32;
-    if (a.dense_mask != (1u << a.T) - 1u)
-      f2d_relx_kernel<<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
-          h->G, h->y, a.rp, a.col, a.val, nnz_off, coef, a.T, h->nrx, ncols, h->n, a.dense_mask);
+  transport_terms<double2, double>(h, axis, op64(h), h->x, h->y, axis == 0 ? a.dense_mask : 0u);
+  if (axis == 0)
     for (int t = 0; t < a.T; ++t)
       if ((a.dense_mask >> t) & 1u)
         F2_CK(wg::ozaki_accumulate(a.dense[t], h->cols, reinterpret_cast<const double*>(h->G + (long long)t * h->n),
                                    reinterpret_cast<double*>(h->y), h->tc_err, h->stream));
-  } else {
-    f2d_rely_kernel<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(h->G, h->y, a.rp, a.col, a.val, nnz_off,
-                                                                          coef, a.T, h->nrx, h->nry, h->n);
-  }
   F2_CK(cudaGetLastError());
   return WG_OK;
 }
 
-template <int NL>
-void launch_drift(wg2d_problem* h) {
+template <int NL, typename T, typename R>
+void launch_drift(wg2d_problem* h, const OpData<T, R>& d, const T* F, T* y) {
   const wg2d_shape& s = h->s;
   const dim3 g1((unsigned)((h->nrel + 127) / 128), (unsigned)h->nel);
-  f2d_interp_kernel<NL><<<g1, 128, 0, h->stream>>>(h->x, h->Uq, h->interp, h->nq, h->nrel, s.n_el_x, s.nk_x, s.nk_y,
-                                                   h->nX);
+  f2d_interp_kernel<NL, T, R><<<g1, 128, 0, h->stream>>>(F, d.Uq, d.interp, h->nq, h->nrel, s.n_el_x, s.nk_x, s.nk_y,
+                                                         h->nX);
   const dim3 g2((unsigned)((h->nrel + 127) / 128), (unsigned)h->nq, (unsigned)h->nel);
-  f2d_vertex_kernel<<<g2, 128, 0, h->stream>>>(h->Uq, h->Rq, h->dV, h->nrx, h->nry, h->nq, h->nvert, s.periodic_y);
-  double2 pot16 = make_double2(h->pot.x / 16.0, h->pot.y / 16.0);
-  f2d_project_kernel<NL><<<g1, 128, 0, h->stream>>>(h->Rq, h->x, h->y, h->proj, h->cap, pot16, h->capc, h->nq,
-                                                    h->nrel, s.n_el_x, s.nk_x, s.nk_y, h->nX);
+  f2d_vertex_kernel<T, R><<<g2, 128, 0, h->stream>>>(d.Uq, d.Rq, d.dV, h->nrx, h->nry, h->nq, h->nvert, s.periodic_y);
+  f2d_project_kernel<NL, T, R><<<g1, 128, 0, h->stream>>>(d.Rq, F, y, d.proj, d.cap, d.pot16, d.capc, h->nq, h->nrel,
+                                                          s.n_el_x, s.nk_x, s.nk_y, h->nX);
+}
+
+template <typename T, typename R>
+void drift_terms(wg2d_problem* h, const OpData<T, R>& d, const T* F, T* y) {
+  switch (h->nloc) {
+    case 4: launch_drift<4, T, R>(h, d, F, y); break;
+    case 6: launch_drift<6, T, R>(h, d, F, y); break;
+    case 8: launch_drift<8, T, R>(h, d, F, y); break;
+    case 9: launch_drift<9, T, R>(h, d, F, y); break;
+    case 12: launch_drift<12, T, R>(h, d, F, y); break;
+    default: launch_drift<16, T, R>(h, d, F, y); break;
+  }
 }
 
 int apply_drift(wg2d_problem* h) {
-  switch (h->nloc) {
-    case 4: launch_drift<4>(h); break;
-    case 6: launch_drift<6>(h); break;
-    case 8: launch_drift<8>(h); break;
-    case 9: launch_drift<9>(h); break;
-    case 12: launch_drift<12>(h); break;
-    default: launch_drift<16>(h); break;
-  }
+  drift_terms<double2, double>(h, op64(h), h->x, h->y);
   F2_CK(cudaGetLastError());
   return WG_OK;
 }
@@ -784,6 +919,7 @@ extern "C" {
 
 static void free_solver(wg2d_problem* h);
 static void free_preconditioner(wg2d_problem* h);
+static void free32(wg2d_problem* h);
 
 int wg2d_create(const wg2d_shape* s, wg2d_problem** out) {
   if (!s || !out) return WG_ERR_ARG;
@@ -824,7 +960,7 @@ int wg2d_create(const wg2d_shape* s, wg2d_problem** out) {
   for (cudaEvent_t& ev : h->ev)
     if (e == cudaSuccess) e = cudaEventCreate(&ev);
   if (e == cudaSuccess && h->nrx * kRelxCols * sizeof(double2) > 48 * 1024)
-    e = cudaFuncSetAttribute(f2d_relx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(f2d_relx_kernel<double2, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(h->nrx * kRelxCols * sizeof(double2)));
   if (e != cudaSuccess) {
     wg2d_destroy(h);
@@ -840,6 +976,7 @@ int wg2d_destroy(wg2d_problem* h) {
   for (auto& a : h->ax) free_axis(a);
   free_solver(h);
   free_preconditioner(h);
+  free32(h);
   wg::ozaki_free(h->cols);
   void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap,
                   h->tc_err};
@@ -875,6 +1012,7 @@ int wg2d_set_transport(wg2d_problem* h, int axis, int n_terms, const double* coe
   cudaStreamSynchronize(h->stream);
   wg2d_problem::Axis& a = h->ax[axis];
   free_axis(a);
+  h->d32_ready = false;
   a.T = n_terms;
   a.coef.assign(coef, coef + n_terms);
   if (n_terms == 0) return WG_OK;
@@ -947,6 +1085,7 @@ int wg2d_set_drift(wg2d_problem* h, const double* interp, const double* proj, co
   h->pot = make_double2(pot[0], pot[1]);
   h->capc = cap_coef;
   h->drift_ready = true;
+  h->d32_ready = false;
   return WG_OK;
 }
 
@@ -977,6 +1116,7 @@ int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const 
   cudaFree(dV);
   if (e != cudaSuccess) return fail(h, WG_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
   h->potential_ready = true;
+  h->d32_ready = false;
   return WG_OK;
 }
 
@@ -1070,6 +1210,16 @@ static void vnorm(wg2d_problem* h, const double2* w) {
   f2d_sqrt_real<<<1, 1, 0, h->stream>>>(h->hp, h->nrm);
 }
 
+static void dots32(wg2d_problem* h, const float2* V, int nv, const float2* w, double2* out, int accumulate) {
+  f2d_dot_partial32<<<dim3(kDotBlocks, nv), 256, 0, h->stream>>>(V, h->n, w, h->partial, h->n);
+  f2d_dot_reduce<<<nv, 256, 0, h->stream>>>(h->partial, out, kDotBlocks, accumulate);
+}
+
+static void vnorm32(wg2d_problem* h, const float2* w) {
+  dots32(h, w, 1, w, h->hp, 0);
+  f2d_sqrt_real<<<1, 1, 0, h->stream>>>(h->hp, h->nrm);
+}
+
 static void free_solver(wg2d_problem* h) {
   void* ptrs[] = {h->V, h->Zb, h->r, h->w, h->z, h->b, h->xs, h->H, h->g, h->sn, h->hc, h->hp, h->yc, h->cs,
                   h->partial, h->nrm};
@@ -1140,6 +1290,99 @@ int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms) {
   return WG_OK;
 }
 
+
+static void free32(wg2d_problem* h) {
+  void* ptrs[] = {h->blocks32[0], h->blocks32[1], h->coef32[0], h->coef32[1], h->val32[0], h->val32[1], h->interp32,
+                  h->proj32, h->cap32, h->dV32, h->Uq32, h->Rq32, h->G32, h->V32, h->Z32, h->w32};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  h->blocks32[0] = h->blocks32[1] = h->coef32[0] = h->coef32[1] = nullptr;
+  h->val32[0] = h->val32[1] = nullptr;
+  h->interp32 = h->proj32 = h->cap32 = h->dV32 = nullptr;
+  h->Uq32 = h->Rq32 = h->G32 = h->V32 = h->Z32 = h->w32 = nullptr;
+  h->vm32 = 0;
+  h->d32_ready = false;
+}
+
+// FP32 copies of the operator (rebuilt after any change of its factors or of the potential)
+static int ensure32(wg2d_problem* h) {
+  if (h->d32_ready) return WG_OK;
+  const int vm = h->vm32;
+  float2 *V = h->V32, *Z = h->Z32, *w = h->w32;
+  h->V32 = h->Z32 = h->w32 = nullptr;
+  free32(h);
+  h->V32 = V;
+  h->Z32 = Z;
+  h->w32 = w;
+  h->vm32 = vm;
+  auto conv = [&](float** dst, const double* src, long long count) -> int {
+    F2_CK(dalloc(dst, count));
+    f2d_d2f<<<(unsigned)((count + 255) / 256), 256, 0, h->stream>>>(src, *dst, count);
+    return WG_OK;
+  };
+  for (int a = 0; a < 2; ++a) {
+    wg2d_problem::Axis& ax = h->ax[a];
+    if (!ax.T) continue;
+    const int nk = a == 0 ? h->s.nk_x : h->s.nk_y, ne = a == 0 ? h->s.n_el_x : h->s.n_el_y;
+    const int nr = a == 0 ? h->nrx : h->nry;
+    int nnz = 0;
+    std::vector<int> rp((size_t)ax.T * (nr + 1));
+    F2_CK(cudaMemcpy(rp.data(), ax.rp, sizeof(int) * rp.size(), cudaMemcpyDeviceToHost));
+    for (int t = 0; t < ax.T; ++t) nnz += rp[(size_t)t * (nr + 1) + nr];
+    int rc = conv(&h->blocks32[a], ax.blocks, (long long)ax.T * ne * 3 * nk * nk);
+    if (!rc) rc = conv(&h->coef32[a], ax.dcoef, ax.T);
+    if (!rc) rc = conv(reinterpret_cast<float**>(&h->val32[a]), reinterpret_cast<const double*>(ax.val), 2LL * nnz);
+    if (rc) return rc;
+  }
+  const long long slab = (long long)h->nel * h->nq;
+  int rc = conv(&h->interp32, h->interp, (long long)h->nq * h->nloc);
+  if (!rc) rc = conv(&h->proj32, h->proj, (long long)h->nq * h->nloc);
+  if (!rc) rc = conv(&h->cap32, h->cap, h->nrel);
+  if (!rc) rc = conv(&h->dV32, h->dV, slab * h->nvert);
+  if (rc) return rc;
+  F2_CK(dalloc(&h->Uq32, slab * h->nrel));
+  F2_CK(dalloc(&h->Rq32, slab * h->nrel));
+  F2_CK(dalloc(&h->G32, (size_t)std::max(1, std::max(h->ax[0].T, h->ax[1].T)) * h->n));
+  if (h->nrx * kRelxCols * sizeof(float2) > 48 * 1024)
+    F2_CK(cudaFuncSetAttribute(f2d_relx_kernel<float2, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(h->nrx * kRelxCols * sizeof(float2))));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  h->d32_ready = true;
+  return WG_OK;
+}
+
+}  // extern "C"
+
+OpData<float2, float> op32(wg2d_problem* h) {
+  OpData<float2, float> d;
+  for (int a = 0; a < 2; ++a) {
+    d.blocks[a] = h->blocks32[a];
+    d.val[a] = h->val32[a];
+    d.coef[a] = h->coef32[a];
+  }
+  d.interp = h->interp32;
+  d.proj = h->proj32;
+  d.cap = h->cap32;
+  d.dV = h->dV32;
+  d.Uq = h->Uq32;
+  d.Rq = h->Rq32;
+  d.G = h->G32;
+  d.pot16 = make_float2((float)(h->pot.x / 16.0), (float)(h->pot.y / 16.0));
+  d.capc = (float)h->capc;
+  return d;
+}
+
+extern "C" {
+
+// out = A in in FP32 (every term on the CUDA cores, the dense abs(A_x) factor included)
+static int apply32(wg2d_problem* h, const float2* in, float2* out) {
+  const OpData<float2, float> d = op32(h);
+  drift_terms<float2, float>(h, d, in, out);
+  for (int a = 0; a < 2; ++a)
+    if (h->ax[a].T) transport_terms<float2, float>(h, a, d, in, out, 0u);
+  F2_CK(cudaGetLastError());
+  return WG_OK;
+}
 
 // real embedding of a complex row-major n x n matrix scaled by a: [[re, -im], [im, re]] per entry
 static std::vector<double> embed(const double* A, int n, double a, bool conj_transpose) {
@@ -1305,7 +1548,73 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
   const double target = tol * bn;
   const int ldh = m + 1;
   int info_reorth = 0;
-  while (info->cycles < maxit && beta > target && std::isfinite(beta)) {
+  if (opts->mixed) {
+    // FP64 iterative refinement around an FP32 flexible GMRES on the FP32 operator: the FP64
+    // residual r = b - A x decides convergence, each refinement solves A d = r / |r| in FP32 to
+    // max(inner_tol, 0.5 target / |r|) and adds |r| d in FP64.
+    if (!h->pre32) return fail(h, WG_ERR_ARG, "wg2d_solve: the mixed form needs the FP32 preconditioner");
+    rc = ensure32(h);
+    if (rc) return rc;
+    const int mi = m;
+    if (h->vm32 < mi + 1) {
+      cudaFree(h->V32);
+      cudaFree(h->Z32);
+      cudaFree(h->w32);
+      h->V32 = h->Z32 = h->w32 = nullptr;
+      h->vm32 = 0;
+      F2_CK(dalloc(&h->V32, (size_t)(mi + 1) * n));
+      F2_CK(dalloc(&h->Z32, (size_t)mi * n));
+      F2_CK(dalloc(&h->w32, n));
+      h->vm32 = mi + 1;
+    }
+    const double inner_tol = opts->inner_tol > 0 ? opts->inner_tol : 1e-3;
+    while (info->cycles < maxit && beta > target && std::isfinite(beta)) {
+      f2d_to32_scaled<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->V32, h->nrm, n);
+      const double2 one = make_double2(1.0, 0.0);
+      F2_CK(cudaMemsetAsync(h->g, 0, sizeof(double2) * (m + 1), h->stream));
+      F2_CK(cudaMemcpyAsync(h->g, &one, sizeof(double2), cudaMemcpyHostToDevice, h->stream));
+      const double itgt = std::max(inner_tol, 0.5 * target / beta);
+      int k = 0;
+      for (int j = 0; j < mi; ++j) {
+        const float2* Vj = h->V32 + (long long)j * n;
+        float2* Zj = h->Z32 + (long long)j * n;
+        precond_stages<float2>(h, h->UH32, h->Us32, h->xinv32, h->xcpl32, h->tinv32, Vj, h->pa32, h->pb32, Zj);
+        rc = apply32(h, Zj, h->w32);
+        if (rc) return rc;
+        dots32(h, h->V32, j + 1, h->w32, h->hc, 0);
+        f2d_gs_update32<<<blocks256(n), 256, 0, h->stream>>>(h->V32, n, h->w32, h->hc, j + 1, n);
+        vnorm32(h, h->w32);
+        std::vector<double2> hh(j + 1);
+        double w1 = 0;
+        F2_CK(cudaMemcpyAsync(hh.data(), h->hc, sizeof(double2) * (j + 1), cudaMemcpyDeviceToHost, h->stream));
+        F2_CK(cudaMemcpyAsync(&w1, h->nrm, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        F2_CK(cudaStreamSynchronize(h->stream));
+        double h2 = 0;
+        for (const double2& c : hh) h2 += c.x * c.x + c.y * c.y;
+        if (w1 * w1 < 0.5 * (w1 * w1 + h2)) {
+          dots32(h, h->V32, j + 1, h->w32, h->hp, 0);
+          f2d_dot_reduce<<<j + 1, 256, 0, h->stream>>>(h->partial, h->hc, kDotBlocks, 1);
+          f2d_gs_update32<<<blocks256(n), 256, 0, h->stream>>>(h->V32, n, h->w32, h->hp, j + 1, n);
+          vnorm32(h, h->w32);
+        }
+        f2d_givens<<<1, 1, 0, h->stream>>>(h->H, h->hc, h->nrm, h->cs, h->sn, h->g, j, ldh);
+        f2d_scale32<<<blocks256(n), 256, 0, h->stream>>>(h->w32, h->V32 + (long long)(j + 1) * n, h->nrm, n);
+        double2 gj;
+        F2_CK(cudaMemcpyAsync(&gj, h->g + j + 1, sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+        F2_CK(cudaStreamSynchronize(h->stream));
+        k = j + 1;
+        info->iterations += 1;
+        if (!(std::hypot(gj.x, gj.y) > itgt)) break;
+      }
+      f2d_backsolve<<<1, 1, 0, h->stream>>>(h->H, h->g, h->yc, k, ldh);
+      F2_CK(cudaMemcpyAsync(h->nrm, &beta, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+      f2d_correct32<<<blocks256(n), 256, 0, h->stream>>>(h->xs, h->Z32, n, h->yc, k, h->nrm, n);
+      info->cycles += 1;
+      rc = true_residual();
+      if (rc) return rc;
+    }
+  }
+  while (!opts->mixed && info->cycles < maxit && beta > target && std::isfinite(beta)) {
     f2d_scale<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->V, h->nrm, n);
     const double2 g0 = make_double2(beta, 0.0);
     F2_CK(cudaMemsetAsync(h->g, 0, sizeof(double2) * (m + 1), h->stream));

@@ -579,13 +579,15 @@ class Full2DOperator:
                                                out.view(np.float64).ctypes.data_as(_lib._D)))
         return out
 
-    def solve(self, rhs, x0=None, tol=1e-8, maxit=50, restart=40):
-        """rho = A \\ rhs by right-preconditioned GMRES(restart) on the device; returns (status, info, rho)."""
+    def solve(self, rhs, x0=None, tol=1e-8, maxit=50, restart=40, mixed=False, inner_tol=1e-3):
+        """rho = A \\ rhs by right-preconditioned flexible GMRES(restart) on the device; mixed: FP64
+        refinement around FP32 inner solves (FP32 preconditioner required).  Returns (status, info, rho)."""
         b = np.ascontiguousarray(np.asarray(rhs, dtype=complex).reshape(-1))
         x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(np.asarray(x0, dtype=complex).reshape(-1))
         if b.size != self.n or x.size != self.n:
             raise WignerError(_lib.WG_ERR_ARG, "rhs and x0 need %d entries" % self.n)
-        opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), int(restart), 0 if x0 is None else 1)
+        opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), int(restart), 0 if x0 is None else 1, 1 if mixed else 0,
+                                  float(inner_tol))
         info = _lib.Wg2dSolveInfo()
         st = self.lib.wg2d_solve(self.h, b.view(np.float64).ctypes.data_as(_lib._D),
                                  x.view(np.float64).ctypes.data_as(_lib._D), C.byref(opts), C.byref(info))
