@@ -775,6 +775,109 @@ def run_full2d(args):
     return out
 
 
+SUBBANDS = dict(n_gates=32, vg_max=0.6, v_drain=0.4, n_modes=8, dy_nm=0.1)
+
+
+def run_subbands(args):
+    """f4: the transverse subband eigensolve of the mode-space set-up (solve_subbands.m) for the
+    C4 gate sweep with the confinement direction resolved: per gate point 2 valleys x 401
+    slices of the 5 nm body between 1 nm oxides (Ny = 71, dy = 0.1 nm), the 8 eigenpairs of
+    smallest magnitude per slice.  One step solves all 32 gate points as one batch (one
+    launch of the slice kernel and one of the sign clean-up) from potentials resident on the
+    device; e2e runs the same batch through SubbandSolver.solve with host arrays (copies in
+    and out timed)."""
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300 import devices
+    from real_space_dg_gb300.subbands import SubbandSolver
+    spec = devices.FETSpec(n_modes=SUBBANDS["n_modes"])
+    vgs = np.linspace(0.0, SUBBANDS["vg_max"], SUBBANDS["n_gates"])
+    secs = [devices.utb_cross_section(spec, float(vg), SUBBANDS["v_drain"], dy_nm=SUBBANDS["dy_nm"]) for vg in vgs]
+    me = secs[0][2]
+    nv, nx, ny = me.shape
+    nm = SUBBANDS["n_modes"]
+    G = len(vgs)
+    dev = torch.device("cuda:0")
+    me_all = np.ascontiguousarray(np.broadcast_to(me[None], (G, nv, nx, ny)))
+    V_all = np.stack([s_[3] for s_ in secs])
+    me_d = torch.tensor(me_all, device=dev)
+    V_d = torch.tensor(V_all, device=dev)
+    E_d = torch.empty((G, nv, nx, nm), dtype=torch.float64, device=dev)
+    Vs_d = torch.empty((G, nv, nx, nm, ny), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    sol = SubbandSolver(nv, nx, ny, nm, batch=G)
+
+    def step():
+        sol.solve_device(SUBBANDS["dy_nm"], me_d.data_ptr(), V_d.data_ptr(), E_d.data_ptr(), Vs_d.data_ptr(),
+                         stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        sol.status(stream.cuda_stream)
+        clocks = ClockSampler()
+        clocks.start()
+        ms = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        clk = clocks.stop()
+        sol.status(stream.cuda_stream)
+    slices = G * nv * nx
+    value = slices * args.steps / (ms / 1000.0)
+    # per slice: Sturm counts of ny entries (2 subtractions, 1 division, 1 compare) -- 1 + the
+    # 32 / nm lanes per candidate x ~54 / log2(32 / nm + 1) multisection steps x nm candidates
+    # (all eigenvalues positive here) -- and the 5 passes of the twisted factorisation per
+    # mode (~14 flops per entry)
+    g = 32 // nm
+    flops_slice = ((1 + int(np.ceil(54 / np.log2(g + 1))) * g * nm) * 4 + 14 * nm) * ny
+    achieved = flops_slice * value / 1e12
+    out = {"metric": "transverse subband eigensolves (slices/s, %d eigenpairs of smallest magnitude per slice)" % nm,
+           "value": round(value, 1), "unit": "slices/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic double-gate UTB Si FET cross-sections",
+           "config": {"workload": "f4 subbands: %d gate points x %d valleys x %d slices, Ny = %d (5 nm body + 2 x 1 nm "
+                                  "oxide, dy = 0.1 nm), %d modes" % (G, nv, nx, ny, nm),
+                      "l2": "256 MB buffer written between timed steps"},
+           "gpu_launches": 2 * args.steps,
+           "roofline": {"bound": "fp64", "achieved": round(achieved, 4), "peak": 1.25, "unit": "TFLOP/s",
+                        "frac": round(achieved / 1.25, 4), "traffic": None,
+                        "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (no measured FP64 peak); flops estimated "
+                                       "from the Sturm counts and eigenvector passes, a division counted as "
+                                       "one (it is ~10 FP64 instructions)"},
+           "clocks": clk}
+    if not args.no_e2e:
+        sol.solve(me_all, V_all, SUBBANDS["dy_nm"])
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            sol.solve(me_all, V_all, SUBBANDS["dy_nm"])
+        we = (time.perf_counter() - t0) / args.steps
+        out["e2e"] = {"value": round(slices / we, 1), "unit": "slices/s",
+                      "h2d_bytes_per_step": int(G * 8 * (nv * nx * ny + nx * ny)),
+                      "d2h_bytes_per_step": int(G * 8 * nv * nx * nm * (1 + ny)),
+                      "path": "SubbandSolver.solve (wg_subbands_solve) of the 32-point batch, host arrays in and out"}
+    sol.close()
+    if not args.no_cpu:
+        from oracle import subbands as S
+        mat = dict(n_of_modes=nm, n_of_valleys=nv, Nx=nx, Ny=ny, dy=SUBBANDS["dy_nm"], me_y=me, V=secs[0][3])
+        t0 = time.perf_counter()
+        S.solve_subbands(mat)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(nv * nx / tc, 2), "unit": "slices/s", "cores": os.cpu_count(),
+                               "kind": "port",
+                               "sample": "one gate point (%d slices) through the oracle: a dense eigensolve of each "
+                                         "slice's Hamiltonian, %.1f s" % (nv * nx, tc)}
+    return out
+
+
 def run_apply(args):
     """Operator applies/s on the C2 batch: the FP64 operator (plain form), the mixed form's
     low-precision inner operator and its tensor-core FP64 operator, with per-kernel rooflines."""
@@ -807,11 +910,12 @@ def main():
     ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d",
+                                                   "subbands"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
                          "c1: the flat-band C1 solve (plain FP64); c4: multi-subband FET gate sweep; "
-                         "full2d: Full-2D operator applies/s")
+                         "full2d: Full-2D operator applies/s; subbands: transverse subband eigensolves/s")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -851,6 +955,8 @@ def main():
         out = run_c1(args) if rank == 0 else None
     elif args.workload == "full2d":
         out = run_full2d(args) if rank == 0 else None
+    elif args.workload == "subbands":
+        out = run_subbands(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

@@ -501,6 +501,33 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
  * of its transport and potential kernels in parts_ms[0..1] (may be NULL). */
 int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms);
 
+/* ------------------------------------------------------------------------------------------------
+ * Transverse subband eigensolve in mode space: replaces [E, V] = solve_subbands(mat)
+ * (solve_subbands.m:1-40 with solve_bandstructure.m:1-33 and eval_transversal_Hamiltonian.m:1-37).
+ * Per valley and x slice: the n_of_modes eigenpairs of smallest magnitude of the Ny x Ny
+ * transverse Hamiltonian, ascending, vectors 2-norm normalised with a positive last entry, then
+ * valley 1's vectors sign-aligned with its first slice.  A handle solves `batch` independent
+ * problems (gate or bias points) at once.  C-order arrays, problem index outermost:
+ *   me_y [batch][nv][nx][ny] (mat.me_y), V [batch][nx][ny] eV (mat.V), dy in nm (mat.dy),
+ *   E [batch][nv][nx][nm] eV, Vsub [batch][nv][nx][nm][ny] -- the Esub / Vsub of solve_transport_DG_2D.
+ * ny in 3..1024, n_modes in 1..min(32, ny).
+ * ------------------------------------------------------------------------------------------------ */
+typedef struct wg_subbands wg_subbands;
+
+int wg_subbands_create(int batch, int n_valleys, int nx, int ny, int n_modes, wg_subbands** out);
+int wg_subbands_destroy(wg_subbands* h);
+const char* wg_subbands_last_error(const wg_subbands* h);
+/* Host buffers in and out; validates the masses (positive) and the potential (finite). */
+int wg_subbands_solve(wg_subbands* h, double dy_nm, const double* me_y, const double* V, double* E, double* Vsub);
+/* Device pointers; enqueued on `stream` (NULL: the handle's), no allocation, no synchronisation. */
+int wg_subbands_solve_device(wg_subbands* h, double dy_nm, const double* me_y, const double* V, double* E,
+                             double* Vsub, void* stream);
+/* Synchronise `stream` (NULL: the handle's) and report a numeric failure of any device solve since
+ * the previous status call (the flag is cleared). */
+int wg_subbands_status(wg_subbands* h, void* stream);
+/* The handle's device buffers for me_y, V, E and Vsub (any pointer may be NULL). */
+int wg_subbands_buffers(wg_subbands* h, double** me_y, double** V, double** E, double** Vsub);
+
 #ifdef __cplusplus
 }
 #endif

@@ -176,6 +176,15 @@ SIGNATURES = {
     "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D, C.c_int], C.c_int),
     "wg2d_precondition": ([_H, _D, _D], C.c_int),
     "wg2d_solve": ([_H, _D, _D, C.POINTER(Wg2dSolveOpts), C.POINTER(Wg2dSolveInfo)], C.c_int),
+    "wg_subbands_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_H)], C.c_int),
+    "wg_subbands_destroy": ([_H], C.c_int),
+    "wg_subbands_last_error": ([_H], C.c_char_p),
+    "wg_subbands_solve": ([_H, C.c_double, _D, _D, _D, _D], C.c_int),
+    "wg_subbands_solve_device": ([_H, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+                                 C.c_int),
+    "wg_subbands_status": ([_H, C.c_void_p], C.c_int),
+    "wg_subbands_buffers": ([_H, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                             C.POINTER(C.c_void_p)], C.c_int),
     "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),
     "wg_solve": ([_H, C.POINTER(WgSolveOpts), _D, C.POINTER(WgSolveInfo)], C.c_int),
     "wg_get_rho": ([_H, C.c_int, _D], C.c_int),

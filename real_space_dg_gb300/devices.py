@@ -265,3 +265,47 @@ def make_fet(spec: FETSpec, v_gate: float, v_drain: float):
     }
     ef_l = float(esub[:, 0, :].min()) + spec.fermi_offset_ev   # above the source's lowest subband edge
     return mat, esub, vsub, ef_l, ef_l - v_drain
+
+
+def utb_cross_section(spec: FETSpec, v_gate: float, v_drain: float, dy_nm: float = 0.1, oxide_offset_ev: float = 3.1,
+                      me_y_ox: float = 0.5, bend_ev: float = 0.05):
+    """Mode-space set-up of a double-gate ultra-thin-body FET with its confinement direction
+    resolved: (x [nm], y [nm], me_y [nv x Nx x Ny], V [Nx x Ny] eV) on the grid
+    y = -t_ox .. W + t_ox step dy, in the layout of the reference's device builders
+    (buildDeviceCMS.m:116-152: the material table mapped onto (x, y), oxide with its
+    own confinement mass and a conduction-band offset).  The body carries the compact
+    longitudinal profile of ``fet_band_profile`` lowered towards both gate interfaces
+    by ``bend_ev`` (a parabola) under the gate; valley v's body mass is its first
+    confinement mass."""
+    x = np.linspace(0.0, spec.length_nm, spec.nx)
+    ny = int(round((spec.width_nm + 2 * spec.oxide_nm) / dy_nm)) + 1
+    y = np.arange(ny) * dy_nm - spec.oxide_nm
+    body = (y >= -1e-12) & (y <= spec.width_nm + 1e-12)
+    u = fet_band_profile(spec, x, v_gate, v_drain)
+    s_src = 1 / (1 + np.exp(-(x - spec.sd_nm) / spec.step_nm))
+    s_drn = 1 / (1 + np.exp(-(x - (spec.length_nm - spec.sd_nm)) / spec.step_nm))
+    gate = s_src * (1 - s_drn)
+    yc = 0.5 * spec.width_nm
+    bend = -bend_ev * gate[:, None] * ((y[None, :] - yc) / yc) ** 2
+    V = np.where(body[None, :], u[:, None] + bend, u[:, None] + oxide_offset_ev)
+    vals = spec.valleys()
+    me_y = np.empty((len(vals), spec.nx, ny))
+    for iv, (_, (my, _)) in enumerate(vals):
+        me_y[iv] = np.where(body, my, me_y_ox)[None, :]
+    return x, y, me_y, V
+
+
+def make_utb_fet(spec: FETSpec, v_gate: float, v_drain: float, solve_subbands=None, dy_nm: float = 0.1, **kw):
+    """(mat, Esub, Vsub, EfL, EfR) of ``make_fet`` with the subbands from the transverse
+    eigensolve of ``utb_cross_section`` (solve_subbands.m:1-40) instead of the box
+    formula: mat gains Ny, dy, y, me_y, V; Vsub is [nv x Nx x nm x Ny].  ``solve_subbands``
+    maps mat -> (E, V) and defaults to the GPU solver."""
+    if solve_subbands is None:
+        from .subbands import solve_subbands
+    mat, _, _, _, _ = make_fet(spec, v_gate, v_drain)
+    x, y, me_y, V = utb_cross_section(spec, v_gate, v_drain, dy_nm=dy_nm, **kw)
+    me_x = np.asarray(mat["me_x"], dtype=float)[:, :, :1]
+    mat.update({"Ny": len(y), "dy": dy_nm, "y": y, "me_y": me_y, "V": V, "me_x": np.repeat(me_x, len(y), axis=2)})
+    esub, vsub = solve_subbands(mat)
+    ef_l = float(esub[:, 0, :].min()) + spec.fermi_offset_ev
+    return mat, esub, vsub, ef_l, ef_l - v_drain
