@@ -878,6 +878,137 @@ def run_subbands(args):
     return out
 
 
+POISSON2D = dict(nx=361, ny=13, dx_nm=0.25, dy_nm=0.25, batch=16, nex=120, ney=2, nk=3)
+
+
+def poisson2d_case(cfg=POISSON2D):
+    """The material grid of the reference's recorded Full-2D run (90 nm x 3 nm: 361 x 13 nodes,
+    periodic Y, Dirichlet source/drain columns) with a seeded double-barrier permittivity and
+    doping layout, and the DG axes of that run (120 x 2 elements, p = 2) for the projection."""
+    nx, ny = cfg["nx"], cfg["ny"]
+    x = np.arange(nx) * cfg["dx_nm"]
+    y = np.arange(ny) * cfg["dy_nm"]
+    eps = np.where(((x > 35) & (x < 40)) | ((x > 50) & (x < 55)), 12.9 * 0.9, 12.9)[:, None] * np.ones((1, ny))
+    nd = np.where((x < 25) | (x > 65), 1e24, 1e21)[:, None] * np.ones((1, ny))
+    prm = dict(N_K_X=cfg["nk"], N_K_Y=cfg["nk"], N_el_X=cfg["nex"], N_el_Y=cfg["ney"], N_rho_x=8, N_rho_y=4,
+               L_rho_x=8e-9, full2D_Y_boundary="periodic")
+    mat = dict(Nx=nx, Ny=ny, dx=cfg["dx_nm"], dy=cfg["dy_nm"], x=x, y=y, eps=eps, Nd=nd, Temp=300.0,
+               dg=dict(params=prm))
+    return mat
+
+
+def run_poisson2d(args):
+    """f3: the Poisson step of the Full-2D Gummel loop (project_DG_density_RTD + the approximate
+    Newton update of solve_Poisson2D_rtd) for 16 bias points on the material grid of the
+    reference's recorded run, one device call per step from nDG resident on the device; e2e
+    through Poisson2D.solve with host arrays; the oracle (scipy sparse LU) as CPU baseline."""
+    import ctypes
+    import torch
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300 import full2d as host2d
+    from real_space_dg_gb300.poisson2d import Poisson2D
+    cfg = POISSON2D
+    mat = poisson2d_case(cfg)
+    B, nx, ny = cfg["batch"], cfg["nx"], cfg["ny"]
+    X = host2d.dg_axis(np.asarray(mat["x"]) * 1e-9, cfg["nk"], cfg["nex"])
+    Y = host2d.dg_axis(np.asarray(mat["y"]) * 1e-9, cfg["nk"], cfg["ney"])
+    p = {"X": X, "Y": Y, "coordinateScale": 1e-9}
+    rng = np.random.default_rng(0)
+    ndx, ndy = X["nd"], Y["nd"]
+    prof = np.where((X["verts"][:-1] < 25e-9) | (X["verts"][:-1] > 65e-9), 1e24, 3e22)
+    nDG = np.repeat(prof, cfg["nk"])[None, :, None] * rng.uniform(0.8, 1.2, (B, ndx, ndy))
+    bias = np.linspace(0.0, 0.3, B)
+    phi0 = np.zeros((B, nx, ny))
+    op = Poisson2D(mat, batch=B)
+    op.set_projection(p, mat)
+    dev = torch.device("cuda:0")
+    src_d = torch.tensor(np.ascontiguousarray(np.swapaxes(nDG, -1, -2)), device=dev)
+    phi0_d = torch.zeros((B, ny, nx), dtype=torch.float64, device=dev)
+    bc = np.empty(B * (ny - 1) * nx)
+    bias_c = np.ascontiguousarray(bias)
+    op.lib.wg_poisson2d_contacts(op.h, bias_c.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None,
+                                 bc.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    bc_d = torch.tensor(bc, device=dev)
+    phi_d = torch.empty((B, ny, nx), dtype=torch.float64, device=dev)
+    n_d = torch.empty((B, ny, nx), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        op.lib.wg_poisson2d_solve_device(op.h, src_d.data_ptr(), 1, phi0_d.data_ptr(), bc_d.data_ptr(), 1, 1.0,
+                                         phi_d.data_ptr(), n_d.data_ptr(), stream.cuda_stream)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        clocks = ClockSampler()
+        clocks.start()
+        ms = 0.0
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            a.record(stream)
+            step()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms += a.elapsed_time(b)
+        clk = clocks.stop()
+    value = B * args.steps / (ms / 1000.0)
+    nu = ny - 1
+    # per bias point: the block sweep (nx Gauss-Jordan inversions of 16 x 16 padded blocks, 2 NU^3
+    # flops each, plus the Schur updates and the two block matvecs) and ~60 flops per node for the
+    # projection, residuals and diagnostics
+    NU = 16
+    flops = nx * (2 * NU ** 3 + 4 * NU * NU) + 60 * nx * ny
+    out = {"metric": "2D Poisson steps/s (DG density projection + approximate-Newton update, %d x %d grid)" % (nx, ny),
+           "value": round(value, 2), "unit": "bias_point_steps/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 4), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic double-barrier permittivity and doping, seeded nDG",
+           "config": {"workload": "f3 Poisson step: %d bias points per call, material grid %d x %d (periodic Y, %d "
+                                  "unique rows), DG axes 120 x 2 elements p=2" % (B, nx, ny, nu),
+                      "l2": "256 MB buffer written between timed steps"},
+           "gpu_launches": args.steps,
+           "roofline": {"bound": "latency", "achieved": round(flops * value / 1e12, 5), "peak": 1.25,
+                        "unit": "TFLOP/s", "frac": round(flops * value / 1e12 / 1.25, 5), "traffic": None,
+                        "peak_source": "nominal GB300 FP64 1.25 TFLOP/s; one warp per bias point runs the "
+                                       "sequential block sweep (latency-bound by construction)"},
+           "clocks": clk}
+    if not args.no_e2e:
+        op.solve(nDG, phi0, bias, method="newton-raphson", dg=True)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            op.solve(nDG, phi0, bias, method="newton-raphson", dg=True)
+        we = (time.perf_counter() - t0) / args.steps
+        out["e2e"] = {"value": round(B / we, 2), "unit": "bias_point_steps/s",
+                      "h2d_bytes_per_step": int(8 * B * (ndx * ndy + nx * ny + nu * nx)),
+                      "d2h_bytes_per_step": int(8 * B * 2 * nx * ny),
+                      "path": "Poisson2D.solve(nDG, ..., dg=True) (wg_poisson2d_solve) for the 16 points"}
+    op.close()
+    if not args.no_cpu:
+        from oracle import poisson2d as P2
+        mat_n = dict(mat, poisson=dict(opt=dict(solve="newton-raphson")))
+        pax = {"X": dict(nLocal=X["nl"], nElements=X["ne"], nDof=X["nd"], r=X["r"], M=X["M"], vertices=X["verts"],
+                         jacobian=X["jac"]),
+               "Y": dict(nLocal=Y["nl"], nElements=Y["ne"], nDof=Y["nd"], r=Y["r"], M=Y["M"], vertices=Y["verts"],
+                         jacobian=Y["jac"]), "coordinateScale": 1e-9}
+        t0 = time.perf_counter()
+        M, num, typ, _ = P2.eval_poisson2d(mat_n)
+        t1 = time.perf_counter()
+        for b in range(4):
+            d, _ = P2.project_dg_density(nDG[b], pax, mat_n, True)
+            P2.solve_poisson2d(M, typ, num, d, mat_n, phi0[b], bias[b])
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"value": round(4 / (t2 - t1), 3), "unit": "bias_point_steps/s", "cores": os.cpu_count(),
+                               "kind": "port", "sample": "4 bias points through the oracle (projection + scipy "
+                               "sparse LU of the Newton system), %.2f s; operator assembly %.2f s once"
+                               % (t2 - t1, t1 - t0)}
+    return out
+
+
 def run_apply(args):
     """Operator applies/s on the C2 batch: the FP64 operator (plain form), the mixed form's
     low-precision inner operator and its tensor-core FP64 operator, with per-kernel rooflines."""
@@ -911,11 +1042,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d",
-                                                   "subbands"],
+                                                   "subbands", "poisson2d"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
                          "c1: the flat-band C1 solve (plain FP64); c4: multi-subband FET gate sweep; "
-                         "full2d: Full-2D operator applies/s; subbands: transverse subband eigensolves/s")
+                         "full2d: Full-2D operator applies/s; subbands: transverse subband eigensolves/s; "
+                         "poisson2d: Full-2D Poisson steps/s")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -957,6 +1089,8 @@ def main():
         out = run_full2d(args) if rank == 0 else None
     elif args.workload == "subbands":
         out = run_subbands(args) if rank == 0 else None
+    elif args.workload == "poisson2d":
+        out = run_poisson2d(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

@@ -528,6 +528,65 @@ int wg_subbands_status(wg_subbands* h, void* stream);
 /* The handle's device buffers for me_y, V, E and Vsub (any pointer may be NULL). */
 int wg_subbands_buffers(wg_subbands* h, double** me_y, double** V, double** E, double** Vsub);
 
+/* ------------------------------------------------------------------------------------------------
+ * 2D Poisson step of the Full-2D Gummel loop: replaces
+ *   [M, node_num, node_type] = eval_Poisson2D_rtd(mat)          (RTD/eval_Poisson2D_rtd.m:1-196)
+ *   n = project_DG_density_RTD(nDG, p, mat, periodicY)          (RTD/project_DG_density_RTD.m:1-37)
+ *   [phi, iter_err, info] = solve_Poisson2D_rtd(M, ..., n, mat, phi0, bias)  (RTD/solve_Poisson2D_rtd.m)
+ * i.e. poissonStep of RTD/make_RTD_poisson_step.m:44-54, for a batch of bias points.  Grid arrays are
+ * [ny][nx] with x fastest (MATLAB's column-major [Nx, Ny], node k = ix + iy nx), in SI units as in the
+ * reference (densities m^-3, potentials V); nDG is [ndof_y][ndof_x] (X fastest).
+ * ------------------------------------------------------------------------------------------------ */
+typedef struct wg_poisson2d wg_poisson2d;
+
+typedef struct {
+  int nx, ny;          /* mat.Nx, mat.Ny (ny - periodic_y <= 32) */
+  double dx_nm, dy_nm; /* mat.dx, mat.dy */
+  int periodic_y;      /* 1: Y endpoints identified (full2D_Y_boundary 'periodic' / mat.poisson.yBoundary) */
+  int neumann_x;       /* 1: mat.poisson.xBoundary = 'neumann' (no Dirichlet nodes; Newton only) */
+  double temp;         /* mat.Temp [K] (Newton screening q^2 n / (kB T)) */
+  int batch;           /* bias points solved per call */
+} wg_poisson2d_desc;
+
+typedef struct {
+  int converged;                     /* the linear update solved to 1e-8 (not self-consistency) */
+  double linear_relres, physical_relres_before, physical_relres_after, physical_residual_before;
+  double residual_scale, unmixed_step, iter_err;
+  double net_charge_per_length, relative_charge_imbalance;
+  double source_integral, target_integral;   /* the projection's conservation check (0 without nDG) */
+} wg_poisson2d_info;
+
+/* eps_r, nd_m3 (mat.Nd), na_m3 (mat.Na, may be NULL) [ny][nx]; boundary [ny][nx] 1 = Dirichlet
+ * (mat.boundary) or NULL for the default (x = first/last column unless neumann_x). */
+int wg_poisson2d_create(const wg_poisson2d_desc* d, const double* eps_r, const unsigned char* boundary,
+                        const double* nd_m3, const double* na_m3, wg_poisson2d** out);
+int wg_poisson2d_destroy(wg_poisson2d* h);
+const char* wg_poisson2d_last_error(const wg_poisson2d* h);
+/* The DG -> dual-volume integration maps (CSR, built by the caller as project_DG_density_RTD.m:39-69
+ * does): Tx [nx x ndof_x], Ty [nu x ndof_y] with the periodic endpoint rows merged, the dual widths
+ * wx [nx], wy [nu] and the element-integral weights src_x [ndof_x], src_y [ndof_y]. */
+int wg_poisson2d_set_projection(wg_poisson2d* h, int ndof_x, const int* tx_rp, const int* tx_col, const double* tx_val,
+                                int ndof_y, const int* ty_rp, const int* ty_col, const double* ty_val,
+                                const double* wx, const double* wy, const double* src_x, const double* src_y);
+/* out = M phi for every problem of the batch (host [batch][ny][nx]). */
+int wg_poisson2d_apply(wg_poisson2d* h, const double* phi, double* out);
+/* Host entry: src = nDG [batch][ndof_y][ndof_x] (src_is_dg = 1) or n [batch][ny][nx] (m^-3);
+ * phi0 [batch][ny][nx]; bias [batch] (bc(end,:) = bias) or vbc [batch][ny][nx] (mat.Vbc);
+ * newton 0 = 'direct', 1 = 'newton-raphson'; alpha in (0, 1].  Out: phi, density [batch][ny][nx],
+ * info [batch]. */
+int wg_poisson2d_solve(wg_poisson2d* h, const double* src, int src_is_dg, const double* phi0, const double* bias,
+                       const double* vbc, int newton, double alpha, double* phi, double* density,
+                       wg_poisson2d_info* info);
+/* Contact potentials on the unique nodes [batch][nu][nx] for the device entry (host arrays). */
+int wg_poisson2d_contacts(wg_poisson2d* h, const double* bias, const double* vbc, double* bc_out);
+/* Device entry: pointers on the device, enqueued on `stream` (NULL: the handle's), no allocation. */
+int wg_poisson2d_solve_device(wg_poisson2d* h, const double* src, int src_is_dg, const double* phi0,
+                              const double* bc, int newton, double alpha, double* phi, double* density, void* stream);
+/* Synchronise `stream` and copy the batch's info to the host. */
+int wg_poisson2d_info_get(wg_poisson2d* h, void* stream, wg_poisson2d_info* info);
+/* The handle's device buffers (src sized for nDG once a projection is set). */
+int wg_poisson2d_buffers(wg_poisson2d* h, double** src, double** phi0, double** bc, double** phi, double** density);
+
 #ifdef __cplusplus
 }
 #endif

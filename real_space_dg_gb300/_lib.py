@@ -154,6 +154,19 @@ class WgSolveInfo(C.Structure):
 
 
 # Every symbol the header declares, with its ctypes signature.
+class WgPoisson2dDesc(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dx_nm", C.c_double), ("dy_nm", C.c_double),
+                ("periodic_y", C.c_int), ("neumann_x", C.c_int), ("temp", C.c_double), ("batch", C.c_int)]
+
+
+class WgPoisson2dInfo(C.Structure):
+    _fields_ = [("converged", C.c_int), ("linear_relres", C.c_double), ("physical_relres_before", C.c_double),
+                ("physical_relres_after", C.c_double), ("physical_residual_before", C.c_double),
+                ("residual_scale", C.c_double), ("unmixed_step", C.c_double), ("iter_err", C.c_double),
+                ("net_charge_per_length", C.c_double), ("relative_charge_imbalance", C.c_double),
+                ("source_integral", C.c_double), ("target_integral", C.c_double)]
+
+
 _H = C.c_void_p
 _D = C.POINTER(C.c_double)
 SIGNATURES = {
@@ -176,6 +189,19 @@ SIGNATURES = {
     "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D, C.c_int], C.c_int),
     "wg2d_precondition": ([_H, _D, _D], C.c_int),
     "wg2d_solve": ([_H, _D, _D, C.POINTER(Wg2dSolveOpts), C.POINTER(Wg2dSolveInfo)], C.c_int),
+    "wg_poisson2d_create": ([C.POINTER(WgPoisson2dDesc), _D, C.POINTER(C.c_ubyte), _D, _D, C.POINTER(_H)], C.c_int),
+    "wg_poisson2d_destroy": ([_H], C.c_int),
+    "wg_poisson2d_last_error": ([_H], C.c_char_p),
+    "wg_poisson2d_set_projection": ([_H, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _D, C.c_int,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_int), _D, _D, _D, _D, _D], C.c_int),
+    "wg_poisson2d_apply": ([_H, _D, _D], C.c_int),
+    "wg_poisson2d_solve": ([_H, _D, C.c_int, _D, _D, _D, C.c_int, C.c_double, _D, _D,
+                            C.POINTER(WgPoisson2dInfo)], C.c_int),
+    "wg_poisson2d_contacts": ([_H, _D, _D, _D], C.c_int),
+    "wg_poisson2d_solve_device": ([_H, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_double,
+                                   C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "wg_poisson2d_info_get": ([_H, C.c_void_p, C.POINTER(WgPoisson2dInfo)], C.c_int),
+    "wg_poisson2d_buffers": ([_H] + [C.POINTER(C.c_void_p)] * 5, C.c_int),
     "wg_subbands_create": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_H)], C.c_int),
     "wg_subbands_destroy": ([_H], C.c_int),
     "wg_subbands_last_error": ([_H], C.c_char_p),

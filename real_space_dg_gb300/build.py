@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libwigner_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "operator.cu", "potential.cu", "mixed.cu", "gmres.cu", "gummel.cu", "transient.cu", "tune.cu", "full2d.cu", "subbands.cu", "api.cu",
+SOURCES = ["setup.cpp", "operator.cu", "potential.cu", "mixed.cu", "gmres.cu", "gummel.cu", "transient.cu", "tune.cu", "full2d.cu", "subbands.cu", "poisson2d.cu", "api.cu",
            "serve.cpp"]
 
 

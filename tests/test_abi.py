@@ -55,6 +55,10 @@ int main(void) {
   printf("%zu %zu %zu\n", offsetof(wg_server_opts, gummel), offsetof(wg_request, rtd),
          offsetof(wg_request_status, t_submit));
   printf("%zu %zu\n", sizeof(wg_runtime_stats), offsetof(wg_runtime_stats, stencil_cells));
+  printf("%zu %zu %zu %zu\n", sizeof(wg2d_shape), sizeof(wg2d_solve_opts), offsetof(wg2d_solve_opts, inner_tol),
+         sizeof(wg2d_solve_info));
+  printf("%zu %zu %zu %zu\n", sizeof(wg_poisson2d_desc), offsetof(wg_poisson2d_desc, temp),
+         sizeof(wg_poisson2d_info), offsetof(wg_poisson2d_info, target_integral));
   return 0;
 }''')
     exe = tmp_path / "probe"
@@ -72,7 +76,11 @@ int main(void) {
             C.sizeof(_lib.WgServerOpts), C.sizeof(_lib.WgRequest), C.sizeof(_lib.WgRequestStatus),
             C.sizeof(_lib.WgServerStats), C.sizeof(_lib.WgOperatorView),
             _lib.WgServerOpts.gummel.offset, _lib.WgRequest.rtd.offset, _lib.WgRequestStatus.t_submit.offset,
-            C.sizeof(_lib.WgRuntimeStats), _lib.WgRuntimeStats.stencil_cells.offset]
+            C.sizeof(_lib.WgRuntimeStats), _lib.WgRuntimeStats.stencil_cells.offset,
+            C.sizeof(_lib.Wg2dShape), C.sizeof(_lib.Wg2dSolveOpts), _lib.Wg2dSolveOpts.inner_tol.offset,
+            C.sizeof(_lib.Wg2dSolveInfo),
+            C.sizeof(_lib.WgPoisson2dDesc), _lib.WgPoisson2dDesc.temp.offset, C.sizeof(_lib.WgPoisson2dInfo),
+            _lib.WgPoisson2dInfo.target_integral.offset]
     assert got == want
 
 
