@@ -655,6 +655,26 @@ def full2d_case(cfg=FULL2D):
     return mat, V
 
 
+def full2d_recorded_case():
+    """The system of the reference's recorded run at its last bias point (0.6 V): the stored
+    potential on the 361 x 13 material grid, the run's DG parameters and its contact-mode
+    reservoirs (E_F,L = 1.474 eV, E_F,R = 0.874 eV inputs; contact-neutrality Fermi levels),
+    from the fixture tests/golden/full2d_reservoir_golden.npz."""
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                             "full2d_reservoir_golden.npz"))
+    prm = {k[4:]: float(g[k]) for k in g.files if k.startswith("prm_")}
+    for k in ("N_K_X", "N_K_Y", "N_el_X", "N_el_Y", "N_rho_x", "N_rho_y", "full2D_contactMode_Nkx",
+              "full2D_contactMode_Nkz"):
+        prm[k] = int(prm[k])
+    prm.update(full2D_Y_boundary="periodic", full2D_reservoirModel="contact-modes", full2D_X_flux="upwind",
+               full2D_Y_flux="upwind", full2D_contactModeFermiModel="contact-neutrality",
+               full2D_potentialQuadratureOrder=5)
+    mat = dict(x=g["x"], y=g["y"], Nx=int(g["Nx"]), Ny=int(g["Ny"]), me_x_ch=float(g["me_x_ch"]),
+               me_y_ch=float(g["me_y_ch"]), me_z_ch=float(g["me_z_ch"]), deg_factor=float(g["deg_factor"]),
+               Temp=float(g["Temp"]), dg=dict(params=prm))
+    return mat, np.asarray(g["potential"]), float(g["ef_input_source"]), float(g["ef_input_drain"])
+
+
 def full2d_flops(f, n):
     """Algorithmic FP64 flops of one apply from the host factors (complex MAC = 8 flops,
     real x complex = 4), as (transport, potential): centre factors 3 nk per entry and term,
@@ -728,9 +748,17 @@ def run_full2d(args):
                    "d2h_bytes_per_step": 16 * n},
            "gpu_launches": 11, "clocks": clk}
     # the Full-2D solve (solve_transport_DG_full2D: GMRES(40), tol 5e-6, at most 150 cycles as in the
-    # recorded run) with the line-transverse preconditioner, on a seeded right-hand side
-    rng = np.random.default_rng(7)
-    rhs = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    # recorded run) with the line-transverse preconditioner, on the recorded run's own system at its
+    # last bias point: stored potential, contact-mode reservoir right-hand side
+    for _, (_, _, _, o) in res.items():
+        o.close()
+    res = {}
+    mat_r, V_r, efl_r, efr_r = full2d_recorded_case()
+    op = Full2DOperator(mat_r, V_r)
+    t0 = time.perf_counter()
+    rhs, inflow = op.reservoir_rhs(efl_r, efr_r)
+    rhs_s = time.perf_counter() - t0
+    res[True] = (None, None, None, op)
     op.set_preconditioner()
     t0 = time.perf_counter()
     st, sinfo, _ = op.solve(rhs, tol=5e-6, maxit=args.solve_maxit, restart=40) if args.solve_maxit > 0 else \
@@ -758,7 +786,9 @@ def run_full2d(args):
                     "cycles": sinfo["cycles"], "relres": sinfo["relres"], "tol": 5e-6, "restart": 40,
                     "ms_per_iteration": round(1000.0 * solve_s / max(1, sinfo["iterations"]), 3),
                     "precondition_host_call_ms": None if pre_ms is None else round(pre_ms, 3),
-                    "rhs": "seeded complex normal vector (the reservoir right-hand side is not built)"}
+                    "rhs": "the recorded run's system at 0.6 V: stored potential, contact-mode reservoirs "
+                           "(contact-neutrality E_F %.6f / %.6f eV), right-hand side built in %.3f s on the host"
+                           % (inflow["source"][1]["fermiLevelUsed"], inflow["drain"][1]["fermiLevelUsed"], rhs_s)}
     for _, (_, _, _, o) in res.items():
         o.close()
     if not args.no_cpu:

@@ -133,8 +133,9 @@ def dg_axis(coord, n_local, n_el):
     M = invV.T @ invV
     Dr = differentiation_matrix(n_local - 1, r, V)
     verts = np.linspace(coord[0], coord[-1], n_el + 1)
-    return dict(nl=n_local, ne=n_el, nd=n_local * n_el, r=r, V=V, M=M, S=M @ Dr, verts=verts,
-                jac=(verts[1:] - verts[:-1]) / 2)
+    jac = (verts[1:] - verts[:-1]) / 2
+    nodes = (0.5 * (verts[:-1] + verts[1:])[:, None] + jac[:, None] * r[None, :]).ravel()
+    return dict(nl=n_local, ne=n_el, nd=n_local * n_el, r=r, V=V, M=M, S=M @ Dr, verts=verts, jac=jac, nodes=nodes)
 
 
 def dg_axis_operators(ax, periodic):
@@ -312,7 +313,8 @@ def build_factors(mat):
     return dict(shape=dict(n_el_x=nex, nk_x=nkx, n_el_y=ney, nk_y=nky, n_rho_x=nrx, n_rho_y=nry,
                            periodic_y=int(periodic)),
                 n=nrx * nry * nex * nkx * ney * nky, x=x, y=y, terms=(_merge(tx), _merge(ty)), axes=(AX, AY),
-                rel=(RX, RY), scales=(sx, sy), drift=drift, nq=nq)
+                rel=(RX, RY), scales=(sx, sy), drift=drift, nq=nq, split=(Apx, Amx, Apy, Amy), ytype=ytype,
+                scale=scale)
 
 
 def _bilinear(gx, gy, V, qx, qy, periodic):
@@ -542,6 +544,18 @@ class Full2DOperator:
         self._check(self.lib.wg2d_set_transport(self.h, axis, len(terms), _lib.dptr(coef), _lib.dptr(blocks),
                                                 rp.ctypes.data_as(C.POINTER(C.c_int)),
                                                 col.ctypes.data_as(C.POINTER(C.c_int)), _lib.dptr(val)))
+
+    def reservoir_rhs(self, EfL, EfR, Vxy=None):
+        """The system's right-hand side from the Source/Drain reservoirs (get_SysM_full2D.m's rhs:
+        get_InflowBoundary_full2D + the inflow parts of get_Diff_full2D.m:405-430), for the model
+        mat.dg.params.full2D_reservoirModel; Vxy defaults to the potential set last.  Returns
+        (rhs, inflow) with inflow[side] = (rhoBoundary, info)."""
+        from . import reservoir
+        V = self.V if Vxy is None else Vxy
+        if V is None:
+            V = self.mat.get("V", np.zeros((len(self.x), len(self.y))))
+        inflow = reservoir.get_InflowBoundary_full2D(self.mat, self.factors, EfL, EfR, V)
+        return reservoir.inflow_rhs(self.factors, inflow), inflow
 
     def set_potential(self, V):
         """Rebuild the potential differences from V [Nx x Ny] on the material grid (device)."""

@@ -1,0 +1,45 @@
+"""Freeze the contact reservoirs of the reference's recorded Full-2D run into a small fixture.
+
+Reads 2026-10-28_08-47/Sim_Res.mat of the reference project (run here, where the reference is
+present; the fixture travels instead): the inputs of the Source/Drain contact-mode reservoirs (the
+material Y grid, the contact-edge potentials of the last bias point, masses, temperature,
+degeneracy and the DG parameters), the whole potential of that bias point (the Full-2D system the
+benchmark solves) and the outputs boundary.physical.XLeft/XRight.rhoBoundary with the mode
+energies and Fermi levels the reference stored beside them.
+
+    python tests/golden/make_reservoir_golden.py /path/to/reference
+"""
+import os
+import sys
+
+import numpy as np
+import scipy.io as sio
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def main(ref_root):
+    d = sio.loadmat(os.path.join(ref_root, "2026-10-28_08-47", "Sim_Res.mat"), squeeze_me=True,
+                    struct_as_record=False)
+    mat = d["mat"]
+    prm = mat.dg.params
+    pot = np.asarray(d["sweep"].potential)[:, :, -1]
+    out = dict(y=np.asarray(mat.y, dtype=float), x=np.asarray(mat.x, dtype=float), Nx=int(mat.Nx), Ny=int(mat.Ny),
+               v_source=pot[0], v_drain=pot[-1], potential=pot, bias=float(np.ravel(d["sweep"].bias)[-1]),
+               me_x_ch=float(mat.me_x_ch), me_y_ch=float(mat.me_y_ch),
+               me_z_ch=float(mat.me_z_ch), deg_factor=float(np.ravel(mat.deg_factor)[0]), Temp=float(mat.Temp))
+    for name in ("N_K_X", "N_K_Y", "N_el_X", "N_el_Y", "N_rho_x", "N_rho_y", "L_rho_x", "L_rho_y",
+                 "full2D_contactMode_Nkx", "full2D_contactMode_Nkz", "full2D_sourceContactSheetDensity",
+                 "full2D_drainContactSheetDensity", "full2D_contactModeIntegrateKz"):
+        out["prm_" + name] = float(getattr(prm, name))
+    for side, key in (("XLeft", "source"), ("XRight", "drain")):
+        s = getattr(d["boundary"].physical, side)
+        out["rho_" + key] = np.asarray(s.rhoBoundary, dtype=float)
+        out["ef_input_" + key] = float(s.fermiLevelInput)
+        out["ef_used_" + key] = float(s.fermiLevel)
+        out["modes_" + key] = np.asarray(s.dataInfo.defaultReservoir.modeEnergy, dtype=float)
+    np.savez_compressed(os.path.join(HERE, "full2d_reservoir_golden.npz"), **out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,139 @@
+"""Full-2D contact reservoirs (get_ContactModeReservoirRho_full2D.m, get_DefaultReservoirRho_full2D.m)
+and the inflow right-hand side (get_Diff_full2D.m:405-430): the oracle and the host module pinned
+to the reservoir data of the reference's recorded run, and the device solve of the resulting
+system against the oracle's sparse LU."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import full2d as F2
+from oracle import reservoir as R
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "full2d_reservoir_golden.npz")
+
+
+def recorded():
+    g = np.load(GOLDEN)
+    prm = {k[4:]: float(g[k]) for k in g.files if k.startswith("prm_")}
+    for k in ("N_K_X", "N_K_Y", "N_el_X", "N_el_Y", "N_rho_x", "N_rho_y", "full2D_contactMode_Nkx",
+              "full2D_contactMode_Nkz"):
+        prm[k] = int(prm[k])
+    prm.update(full2D_Y_boundary="periodic", full2D_reservoirModel="contact-modes", full2D_X_flux="upwind",
+               full2D_Y_flux="upwind", full2D_contactModeFermiModel="contact-neutrality",
+               full2D_potentialQuadratureOrder=5)
+    mat = dict(x=g["x"], y=g["y"], Nx=int(g["Nx"]), Ny=int(g["Ny"]), me_x_ch=float(g["me_x_ch"]),
+               me_y_ch=float(g["me_y_ch"]), me_z_ch=float(g["me_z_ch"]), deg_factor=float(g["deg_factor"]),
+               Temp=float(g["Temp"]), dg=dict(params=prm))
+    return g, mat
+
+
+@pytest.mark.parametrize("side", ["source", "drain"])
+def test_oracle_matches_the_recorded_contact_mode_reservoir(side):
+    g, mat = recorded()
+    p = F2.init_params_full2d(mat)
+    rho, info = R.contact_mode_reservoir(mat, p, side, float(g["ef_input_" + side]), g["potential"])
+    assert np.array_equal(info["modeEnergy"], g["modes_" + side])
+    assert abs(info["fermiLevelUsed"] - float(g["ef_used_" + side])) < 1e-14
+    gold = g["rho_" + side]
+    assert np.abs(rho.imag).max() == 0.0
+    assert np.abs(rho.real - gold).max() <= 1e-14 * np.abs(gold).max()
+
+
+@pytest.mark.parametrize("side", ["source", "drain"])
+def test_host_reservoir_matches_the_recorded_run(side):
+    from real_space_dg_gb300 import full2d as H, reservoir as PR
+    g, mat = recorded()
+    f = H.build_factors(mat)
+    inflow = PR.get_InflowBoundary_full2D(mat, f, float(g["ef_input_source"]), float(g["ef_input_drain"]),
+                                          g["potential"])
+    rho, info = inflow[side]
+    gold = g["rho_" + side]
+    assert abs(info["fermiLevelUsed"] - float(g["ef_used_" + side])) < 1e-14
+    assert np.abs(rho - gold).max() <= 1e-14 * np.abs(gold).max()
+
+
+def test_host_inflow_rhs_matches_oracle():
+    from real_space_dg_gb300 import full2d as H, reservoir as PR
+    g, mat = recorded()
+    p = F2.init_params_full2d(mat)
+    ox = F2.one_dimensional_dg_operators(p["X"])
+    Apx, Amx, _ = F2.split_characteristic(p["Ax1D"])
+    sx, _ = F2.transport_scales(mat)
+    want = R.inflow_rhs(p, g["rho_source"], g["rho_drain"], sx, Apx, Amx, ox["leftLift"], ox["rightLift"])
+    f = H.build_factors(mat)
+    got = PR.inflow_rhs(f, {"source": (g["rho_source"], {}), "drain": (g["rho_drain"], {})})
+    assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+    # only the first and last X element of every Y node row carries inflow
+    nrel = p["rhoX"]["nCells"] * p["rhoY"]["nCells"]
+    touched = np.flatnonzero(np.abs(want).reshape(-1, nrel).max(axis=1)) % p["X"]["nDof"]
+    assert set(touched) <= set(range(3)) | set(range(p["X"]["nDof"] - 3, p["X"]["nDof"]))
+
+
+def small_mat(model, ybc, nrx=9, nry=4):
+    prm = dict(N_K_X=3, N_K_Y=3, N_el_X=5, N_el_Y=2, N_rho_x=nrx, N_rho_y=nry, L_rho_x=8e-9,
+               full2D_X_flux="upwind", full2D_Y_flux="upwind", full2D_Y_boundary=ybc,
+               full2D_potentialQuadratureOrder=5, full2D_reservoirModel=model,
+               full2D_sourceContactSheetDensity=6e15, full2D_drainContactSheetDensity=6e15,
+               full2D_contactMode_Nkx=20, full2D_contactMode_Nkz=31, full2D_contactModeIntegrateKz=1)
+    x, y = np.linspace(0, 20.0, 11), np.linspace(0, 4.0, 5)
+    return dict(x=x, y=y, Nx=11, Ny=5, me_x_ch=0.063, me_y_ch=0.063, me_z_ch=0.063, Temp=300.0, deg_factor=1,
+                dg=dict(params=prm))
+
+
+def test_host_default_reservoir_matches_oracle():
+    from real_space_dg_gb300 import full2d as H, reservoir as PR
+    mat = small_mat("material-default", "zero-inflow")
+    V = 1.424 + 0.1 * np.outer(np.linspace(0, 1, 11), np.ones(5)) + 0.02 * np.random.default_rng(0).normal(size=(11, 5))
+    p = F2.init_params_full2d(mat)
+    f = H.build_factors(mat)
+    for side, ef in (("source", 1.45), ("drain", 1.40)):
+        want = R.default_reservoir(mat, p, side, ef, V)
+        got, _ = PR.default_reservoir(mat, f, side, ef, V)
+        assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_host_reservoir_errors():
+    from real_space_dg_gb300 import WignerError
+    from real_space_dg_gb300 import full2d as H, reservoir as PR
+    mat = small_mat("contact-modes", "zero-inflow")
+    f = H.build_factors(mat)
+    with pytest.raises(WignerError):          # the box contact problem is not restated
+        PR.get_InflowBoundary_full2D(mat, f, 1.45, 1.4, np.full((11, 5), 1.424))
+    mat = small_mat("contact-modes", "periodic")
+    f = H.build_factors(mat)
+    V = np.full((11, 5), 1.424)
+    V[0, 2] = 1.5                              # a Y-dependent contact potential: modes by diagonalisation
+    rho, info = PR.contact_mode_reservoir(mat, f, "source", 1.45, V)
+    p = F2.init_params_full2d(mat)
+    want, winfo = R.contact_mode_reservoir(mat, p, "source", 1.45, V)
+    assert abs(info["fermiLevelUsed"] - winfo["fermiLevelUsed"]) < 1e-12
+    assert np.abs(rho - want).max() <= 1e-12 * np.abs(want).max()
+    V[0, -1] = 1.3                             # endpoints disagree
+    with pytest.raises(WignerError):
+        PR.contact_mode_reservoir(mat, f, "source", 1.45, V)
+    mat = small_mat("material-default", "zero-inflow")
+    mat["dg"]["params"]["full2D_sourceContactMask"] = [1, 1, 0, 1, 1, 1]
+    with pytest.raises(WignerError):
+        PR.get_InflowBoundary_full2D(mat, H.build_factors(mat), 1.45, 1.4, np.full((11, 5), 1.424))
+
+
+@pytest.mark.gpu
+def test_gpu_solve_of_the_reservoir_driven_system(built_lib):
+    """The Full-2D device solve (mixed and FP64) of A rho = rhs with the contact-mode reservoir
+    right-hand side, against the oracle's sparse LU of the same system."""
+    import scipy.sparse.linalg as spla
+    from real_space_dg_gb300.full2d import Full2DOperator
+    mat = small_mat("contact-modes", "periodic")
+    XX, YY = np.meshgrid(mat["x"], mat["y"], indexing="ij")
+    V = 1.424 + 0.15 * np.exp(-((XX - 10) / 3) ** 2) - 0.05 * XX / 20
+    p, parts, dd = F2.system(mat, V)
+    A = F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)
+    with Full2DOperator(mat, V) as op:
+        rhs, inflow = op.reservoir_rhs(1.45, 1.40)
+        want = spla.spsolve(A.tocsc(), rhs)
+        op.set_preconditioner(fp32=True)
+        for mixed in (False, True):
+            st, info, x = op.solve(rhs, tol=1e-11, maxit=200, restart=20, mixed=mixed)
+            assert st == 0
+            assert np.linalg.norm(x - want) <= 1e-8 * np.linalg.norm(want)
