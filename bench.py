@@ -761,13 +761,26 @@ def run_full2d(args):
     res[True] = (None, None, None, op)
     op.set_preconditioner()
     t0 = time.perf_counter()
-    st, sinfo, _ = op.solve(rhs, tol=5e-6, maxit=args.solve_maxit, restart=40) if args.solve_maxit > 0 else \
+    st, sinfo, xs = op.solve(rhs, tol=5e-6, maxit=args.solve_maxit, restart=40) if args.solve_maxit > 0 else \
         (0, dict(iterations=0, cycles=0, relres=None), None)
     solve_s = time.perf_counter() - t0
     t0 = time.perf_counter()
-    stm, minfo, _ = op.solve(rhs, tol=5e-6, maxit=max(args.solve_maxit, 1) * 4, restart=40, mixed=True) \
+    stm, minfo, xm = op.solve(rhs, tol=5e-6, maxit=max(args.solve_maxit, 1) * 4, restart=40, mixed=True) \
         if args.solve_maxit > 0 else (0, dict(iterations=0, cycles=0, relres=None), None)
     mixed_s = time.perf_counter() - t0
+    recorded = {}
+    if xm is not None:
+        # the reference's own transport output for this system (sweep.density / sweep.current of the
+        # recorded run at 0.6 V, solved there to a 4.96e-6 relative residual)
+        g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                 "full2d_reservoir_golden.npz"))
+        for name, x in (("mixed", xm), ("fp64", xs)):
+            if x is None:
+                continue
+            n_o, j_o, _, _ = op.observables(x)
+            recorded[name] = {"density_max_rel_diff": float(np.abs(n_o - g["density"]).max() / np.abs(g["density"]).max()),
+                              "current_max_rel_diff": float(np.abs(j_o - g["current"]).max() / np.abs(g["current"]).max()),
+                              "mean_current": float(np.mean(j_o)), "recorded_mean_current": float(np.mean(g["current"]))}
     pre_ms = None
     try:
         r = rhs.copy()
@@ -778,6 +791,7 @@ def run_full2d(args):
         pre_ms = (time.perf_counter() - t1) / 3 * 1000.0
     except Exception:
         pass
+    out["vs_recorded_run"] = recorded
     out["solve_mixed"] = {"status": int(stm), "seconds": round(mixed_s, 3), "inner_iterations": minfo["iterations"],
                           "refinements": minfo["cycles"], "relres": minfo["relres"], "tol": 5e-6,
                           "ms_per_iteration": round(1000.0 * mixed_s / max(1, minfo["iterations"]), 3),

@@ -522,3 +522,85 @@ def line_transverse_apply(p, d, r):
     Vv = np.transpose(T.reshape(nm, nX, nY, nry), (2, 1, 3, 0))     # back to [Y][X][ry][k]
     Z = np.einsum("ik,yxrk->yxri", d["U"], Vv) / d["sigma"]
     return Z.reshape(-1)
+
+
+# ----------------------------------------------------------------------------- observables
+
+def _zero_weights(cells):
+    """zeroInterpolationWeights (get_Observables_full2D.m:80-103)."""
+    cells = np.asarray(cells, dtype=float)
+    nearest = int(np.argmin(np.abs(cells)))
+    if abs(cells[nearest]) <= max(1e-14, 1e-12 * max(1, np.abs(cells).max())):
+        return [nearest], [1.0]
+    left = np.flatnonzero(cells < 0)
+    right = np.flatnonzero(cells > 0)
+    if left.size and right.size:
+        lo, hi = left[-1], right[0]
+        h = cells[hi] - cells[lo]
+        return [lo, hi], [cells[hi] / h, -cells[lo] / h]
+    return [nearest], [1.0]
+
+
+def _derivative_row(cells, D):
+    """derivativeRowAtZero (get_Observables_full2D.m:105-134) for a grid with a cell at or
+    bracketing zero."""
+    cells = np.asarray(cells, dtype=float)
+    nearest = int(np.argmin(np.abs(cells)))
+    if abs(cells[nearest]) <= max(1e-14, 1e-12 * max(1, np.abs(cells).max())):
+        return np.asarray(D.todense() if sp.issparse(D) else D)[nearest]
+    row = np.zeros(cells.size)
+    lo, hi = np.flatnonzero(cells < 0)[-1], np.flatnonzero(cells > 0)[0]
+    h = cells[hi] - cells[lo]
+    row[lo], row[hi] = -1 / h, 1 / h
+    return row
+
+
+def _project_to_y(values, ydg, target):
+    """projectValuesToY (get_Observables_full2D.m:154-168): columns at the same Y node (element
+    interfaces) averaged, then linear interpolation with extrapolation onto the target Y."""
+    order = np.argsort(ydg, kind="stable")
+    ys, vals = ydg[order], values[:, order]
+    tol = 1e-12 * max(abs(ys[-1] - ys[0]), 1e-300)
+    groups = []
+    for i in range(ys.size):
+        if groups and ys[i] - ys[groups[-1][0]] <= tol:
+            groups[-1].append(i)
+        else:
+            groups.append([i])
+    uy = np.array([ys[g[0]] for g in groups])
+    avg = np.stack([vals[:, g].mean(axis=1) for g in groups], axis=1)
+    if uy.size == 1:
+        return np.repeat(avg, target.size, axis=1)
+    from scipy.interpolate import interp1d
+    return interp1d(uy, avg, axis=1, kind="linear", fill_value="extrapolate")(target)
+
+
+def observables(p, mat, rho):
+    """(n [X nDof x material Ny], j [X nDof], nDG, jxDG) (get_Observables_full2D.m:19-78):
+    n = real(rho) at zero relative separation, j_x = q hbar / m_x imag(d rho / d rho_x) at zero,
+    both projected onto the material Y grid, j integrated over Y (trapezoid, in m)."""
+    nrx, nry = p["rhoX"]["nCells"], p["rhoY"]["nCells"]
+    nX, nY = p["X"]["nDof"], p["Y"]["nDof"]
+    rho = np.asarray(rho).ravel()
+    by_center = rho.reshape(nX * nY, nrx * nry).T                   # reshape(rho, nRel, nCenter)
+    r4 = rho.reshape(nY, nX, nry, nrx).transpose(3, 2, 1, 0)          # rho(iRhoX, iRhoY, iX, iY)
+    ix_ids, ix_w = _zero_weights(p["rhoX"]["cells"])
+    iy_ids, iy_w = _zero_weights(p["rhoY"]["cells"])
+    nDG = np.zeros((nX, nY))
+    for a, wa in zip(ix_ids, ix_w):
+        for b, wb in zip(iy_ids, iy_w):
+            nDG += wa * wb * np.real(r4[a, b])
+    rowx = _derivative_row(p["rhoX"]["cells"], p["rhoX"]["D"])
+    dx = np.zeros(nX * nY, dtype=complex)
+    for b, wb in zip(iy_ids, iy_w):
+        dx += wb * (rowx @ by_center[b * nrx:(b + 1) * nrx, :])
+    mex = mat.get("me_x_ch", 0.041)
+    mkg = mex * M0 if abs(mex) > 1e-25 else mex
+    mkg = mkg if mkg > 0 else 0.041 * M0
+    jxDG = QE * HBAR / mkg * np.imag(dx.reshape(nX, nY, order="F"))
+    target = np.asarray(mat["y"], dtype=float) * p["coordinateScale"]
+    ydg = p["Y"]["nodes"]
+    n = _project_to_y(nDG, ydg, target)
+    jx = _project_to_y(jxDG, ydg, target)
+    trapz = getattr(np, "trapezoid", None) or np.trapz
+    return n, trapz(jx, target, axis=1), nDG, jxDG

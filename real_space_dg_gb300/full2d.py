@@ -545,6 +545,66 @@ class Full2DOperator:
                                                 rp.ctypes.data_as(C.POINTER(C.c_int)),
                                                 col.ctypes.data_as(C.POINTER(C.c_int)), _lib.dptr(val)))
 
+    def observables(self, rho):
+        """(n [X nDof x material Ny] m^-3, j [X nDof], nDG, jxDG) of a state
+        (get_Observables_full2D.m:19-78): n = real(rho) at zero relative separation (the
+        rho_x = 0 cell; the two rho_y cells around 0 weighted linearly), j_x = q hbar / m_x
+        imag(d rho / d rho_x) at zero (the central-difference row), projected onto the material
+        Y grid (DG values at shared interface nodes averaged, linear interpolation), j the
+        trapezoid integral over Y."""
+        f = self.factors
+        RX, RY = f["rel"]
+        AX, AY = f["axes"]
+        nrx, nry, nX, nY = RX["n"], RY["n"], AX["nd"], AY["nd"]
+        r4 = np.asarray(rho).reshape(nY, nX, nry, nrx)                   # [Y, X, rho_y, rho_x]
+
+        def zero(cells):
+            i = int(np.argmin(np.abs(cells)))
+            if abs(cells[i]) <= max(1e-14, 1e-12 * max(1.0, np.abs(cells).max())):
+                return np.array([i]), np.array([1.0])
+            lo, hi = np.flatnonzero(cells < 0)[-1], np.flatnonzero(cells > 0)[0]
+            h = cells[hi] - cells[lo]
+            return np.array([lo, hi]), np.array([cells[hi] / h, -cells[lo] / h])
+        ax_, wx = zero(RX["cells"])
+        ay_, wy = zero(RY["cells"])
+        at0 = np.einsum("yxab,a,b->xy", r4[:, :, ay_][:, :, :, ax_], wy, wx)   # rho at (0, 0)
+        nDG = at0.real
+        ix0 = ax_[0] if ax_.size == 1 else None
+        if ix0 is not None:
+            drow = RX["D"][ix0]
+        else:
+            drow = np.zeros(nrx)
+            h = RX["cells"][ax_[1]] - RX["cells"][ax_[0]]
+            drow[ax_[0]], drow[ax_[1]] = -1 / h, 1 / h
+        d = np.einsum("yxba,a,b->xy", r4[:, :, ay_, :], drow, wy)
+        mex = self.mat.get("me_x_ch", 0.041)
+        mkg = mex * M0 if abs(mex) > 1e-25 else mex
+        mkg = mkg if mkg > 0 else 0.041 * M0
+        jxDG = QE * HBAR / mkg * d.imag
+        target = np.asarray(self.mat["y"], dtype=float) * f["scale"]
+        ydg = AY["nodes"]
+        order = np.argsort(ydg, kind="stable")
+        tol = 1e-12 * max(abs(ydg.max() - ydg.min()), 1e-300)
+        uy, cols = [], []
+        for i in order:
+            if uy and ydg[i] - uy[-1] <= tol:
+                cols[-1].append(i)
+            else:
+                uy.append(ydg[i])
+                cols.append([i])
+        uy = np.asarray(uy)
+
+        def to_y(v):
+            a = np.stack([v[:, c].mean(axis=1) for c in cols], axis=1)
+            if uy.size == 1:
+                return np.repeat(a, target.size, axis=1)
+            k = np.clip(np.searchsorted(uy, target, side="right") - 1, 0, uy.size - 2)
+            t = (target - uy[k]) / (uy[k + 1] - uy[k])
+            return a[:, k] * (1 - t) + a[:, k + 1] * t
+        n, jx = to_y(nDG), to_y(jxDG)
+        j = np.sum(0.5 * (jx[:, 1:] + jx[:, :-1]) * np.diff(target), axis=1) if target.size > 1 else jx[:, 0]
+        return n, j, nDG, jxDG
+
     def reservoir_rhs(self, EfL, EfR, Vxy=None):
         """The system's right-hand side from the Source/Drain reservoirs (get_SysM_full2D.m's rhs:
         get_InflowBoundary_full2D + the inflow parts of get_Diff_full2D.m:405-430), for the model

@@ -4,8 +4,9 @@ Reads 2026-10-28_08-47/Sim_Res.mat of the reference project (run here, where the
 present; the fixture travels instead): the inputs of the Source/Drain contact-mode reservoirs (the
 material Y grid, the contact-edge potentials of the last bias point, masses, temperature,
 degeneracy and the DG parameters), the whole potential of that bias point (the Full-2D system the
-benchmark solves) and the outputs boundary.physical.XLeft/XRight.rhoBoundary with the mode
-energies and Fermi levels the reference stored beside them.
+benchmark solves), the density and current the reference's transport solve returned for it (with
+its GMRES relative residual), and the outputs boundary.physical.XLeft/XRight.rhoBoundary with the
+mode energies and Fermi levels the reference stored beside them.
 
     python tests/golden/make_reservoir_golden.py /path/to/reference
 """
@@ -26,6 +27,9 @@ def main(ref_root):
     pot = np.asarray(d["sweep"].potential)[:, :, -1]
     out = dict(y=np.asarray(mat.y, dtype=float), x=np.asarray(mat.x, dtype=float), Nx=int(mat.Nx), Ny=int(mat.Ny),
                v_source=pot[0], v_drain=pot[-1], potential=pot, bias=float(np.ravel(d["sweep"].bias)[-1]),
+               density=np.asarray(d["sweep"].density, dtype=float)[:, :, -1],
+               current=np.asarray(d["sweep"].current, dtype=float)[:, -1],
+               relres=float(np.ravel(d["sweep"].relres)[-1]),
                me_x_ch=float(mat.me_x_ch), me_y_ch=float(mat.me_y_ch),
                me_z_ch=float(mat.me_z_ch), deg_factor=float(np.ravel(mat.deg_factor)[0]), Temp=float(mat.Temp))
     for name in ("N_K_X", "N_K_Y", "N_el_X", "N_el_Y", "N_rho_x", "N_rho_y", "L_rho_x", "L_rho_y",

@@ -137,3 +137,39 @@ def test_gpu_solve_of_the_reservoir_driven_system(built_lib):
             st, info, x = op.solve(rhs, tol=1e-11, maxit=200, restart=20, mixed=mixed)
             assert st == 0
             assert np.linalg.norm(x - want) <= 1e-8 * np.linalg.norm(want)
+
+
+def test_host_observables_match_oracle():
+    """get_Observables_full2D: density at zero separation and the x current, projected onto the
+    material Y grid (odd and even rho_y counts: the exact cell and the linear bracket)."""
+    from real_space_dg_gb300.full2d import Full2DOperator, build_factors
+    rng = np.random.default_rng(3)
+    for ybc, nry in (("periodic", 4), ("zero-inflow", 5)):
+        mat = small_mat("material-default", ybc, nry=nry)
+        p = F2.init_params_full2d(mat)
+        rho = rng.normal(size=p["nTotal"]) + 1j * rng.normal(size=p["nTotal"])
+        want = F2.observables(p, mat, rho)
+        holder = Full2DOperator.__new__(Full2DOperator)        # the host method only, no device handle
+        holder.factors, holder.mat = build_factors(mat), mat
+        got = holder.observables(rho)
+        for a, b in zip(got, want):
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+
+
+@pytest.mark.gpu
+def test_gpu_recorded_bias_point_reproduces_the_recorded_density_and_current(built_lib):
+    """The recorded run's system at 0.6 V (its stored potential and contact-mode reservoirs) solved
+    on the device with the run's settings (GMRES(40), line-transverse preconditioner, 5e-6)
+    reproduces the density and current the reference stored for it; both solves stop at a ~5e-6
+    relative residual, which bounds the agreement (measured 1.0e-4 / 3.6e-4, mean current 3.6e-5)."""
+    from real_space_dg_gb300.full2d import Full2DOperator
+    g, mat = recorded()
+    with Full2DOperator(mat, g["potential"]) as op:
+        rhs, inflow = op.reservoir_rhs(float(g["ef_input_source"]), float(g["ef_input_drain"]))
+        op.set_preconditioner()
+        st, info, x = op.solve(rhs, tol=5e-6, maxit=600, restart=40, mixed=True)
+        assert st == 0
+        n, j, _, _ = op.observables(x)
+    assert np.abs(n - g["density"]).max() <= 1e-3 * np.abs(g["density"]).max()
+    assert np.abs(j - g["current"]).max() <= 3e-3 * np.abs(g["current"]).max()
+    assert abs(np.mean(j) - np.mean(g["current"])) <= 3e-4 * abs(np.mean(g["current"]))
