@@ -6,7 +6,9 @@ material Y grid, the contact-edge potentials of the last bias point, masses, tem
 degeneracy and the DG parameters), the whole potential of that bias point (the Full-2D system the
 benchmark solves), the density and current the reference's transport solve returned for it (with
 its GMRES relative residual), and the outputs boundary.physical.XLeft/XRight.rhoBoundary with the
-mode energies and Fermi levels the reference stored beside them.
+mode energies and Fermi levels the reference stored beside them; for the sweep's first bias point
+(0 V) the device fields (Vc, eps, Nd, contact lengths), the converged potential and density and
+the Gummel loop's per-iteration history.
 
     python tests/golden/make_reservoir_golden.py /path/to/reference
 """
@@ -36,6 +38,16 @@ def main(ref_root):
                  "full2D_contactMode_Nkx", "full2D_contactMode_Nkz", "full2D_sourceContactSheetDensity",
                  "full2D_drainContactSheetDensity", "full2D_contactModeIntegrateKz"):
         out["prm_" + name] = float(getattr(prm, name))
+    # the self-consistent sweep's first bias point: device fields, the converged potential and the
+    # per-iteration history of the Gummel loop (solve2D_rtd_self_consistent.m)
+    out.update(Vc=np.asarray(mat.Vc, dtype=float), eps=np.asarray(mat.eps, dtype=float),
+               Nd=np.asarray(mat.Nd, dtype=float), Lc1=float(mat.Lc1), Lc2=float(mat.Lc2), dx=float(mat.dx),
+               dy=float(mat.dy), potential0=np.asarray(d["sweep"].potential, dtype=float)[:, :, 0],
+               density0=np.asarray(d["sweep"].density, dtype=float)[:, :, 0],
+               iterations0=int(np.ravel(d["sweep"].iterations)[0]))
+    hist = d["selfConsistency"].history[0]
+    out["history0"] = np.array([[h.gmresIterations, h.potentialDefect, h.densityChange, h.poissonPhysicalRelres]
+                                for h in hist], dtype=float)
     for side, key in (("XLeft", "source"), ("XRight", "drain")):
         s = getattr(d["boundary"].physical, side)
         out["rho_" + key] = np.asarray(s.rhoBoundary, dtype=float)
