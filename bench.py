@@ -1053,6 +1053,54 @@ def run_poisson2d(args):
     return out
 
 
+def run_full2d_sc(args):
+    """The Full-2D self-consistent loop (solve2D_rtd_self_consistent.m) at the first bias point of
+    the reference's recorded run: 0 V on the 90 nm x 3 nm periodic RTD (3,136,320 unknowns), contact-
+    mode reservoirs, approximate-Newton Poisson step, mixing 0.3 (main2D_rtd.m), transport by
+    mixed flexible GMRES(40) to 5e-6, warm-started; compared with the run's stored trajectory,
+    potential and density.  value = self-consistent bias points/s."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300.full2d_sc import solve2D_rtd_self_consistent
+    mat, _, _, _ = full2d_recorded_case()
+    gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                                "full2d_reservoir_golden.npz"))
+    mat.update(Vc=gold["Vc"], eps=gold["eps"], Nd=gold["Nd"], Lc1=float(gold["Lc1"]), Lc2=float(gold["Lc2"]),
+               dx=float(gold["dx"]), dy=float(gold["dy"]), Vdd=np.array([0.0]),
+               poisson=dict(opt=dict(solve="newton-raphson")))
+    mat["dg"]["params"].update(full2D_solverTol=5e-6, full2D_gmresRestart=40, full2D_solverMaxIt=150)
+    hist = []
+    clocks = ClockSampler()
+    clocks.start()
+    t0 = time.perf_counter()
+    res = solve2D_rtd_self_consistent("DG", mat, {"mixing": 0.3}, callback=lambda ib, it, h: hist.append(h))
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    sw = res["sweep"]
+    rec = gold["history0"]
+    m = min(len(hist), rec.shape[0])
+    defect_rel = [abs(hist[i]["potentialDefect"] - rec[i, 1]) / rec[i, 1] for i in range(m)]
+    its = sum(h["gmresIterations"] for h in hist)
+    out = {"metric": "Full-2D self-consistent bias points/s (transport + Poisson Gummel loop to the recorded run's "
+                     "tolerances)", "value": round(1.0 / wall, 5), "unit": "bias_points/s", "n_gpus": 1, "steps": 1,
+           "warmup": 0, "ms_per_step": round(1000 * wall, 1), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "bf16/f32 in f64 refinement (transport), f64 (Poisson)",
+           "data": "the reference's recorded run (Sim_Res.mat fixture): device fields, reservoirs, bias 0 V",
+           "config": {"workload": "Full-2D RTD 90 x 3 nm, 120 x 2 elements p=2, 121 x 12 relative cells, periodic Y, "
+                                  "3,136,320 unknowns; mixing 0.3, Newton Poisson, GMRES(40) 5e-6"},
+           "gummel_iterations": int(sw["iterations"][0]), "recorded_gummel_iterations": int(gold["iterations0"]),
+           "gmres_iterations_total": int(its), "recorded_gmres_iterations_total": int(rec[:, 0].sum()),
+           "status": res["status"],
+           "vs_recorded_run": {
+               "potential_max_abs_diff_V": float(np.abs(sw["potential"][:, :, 0] - gold["potential0"]).max()),
+               "density_max_rel_diff": float(np.abs(sw["density"][:, :, 0] - gold["density0"]).max() /
+                                             np.abs(gold["density0"]).max()),
+               "first_defect_rel_diff": float(defect_rel[0]) if defect_rel else None,
+               "max_defect_rel_diff": float(max(defect_rel)) if defect_rel else None},
+           "clocks": clk}
+    return out
+
+
 def run_apply(args):
     """Operator applies/s on the C2 batch: the FP64 operator (plain form), the mixed form's
     low-precision inner operator and its tensor-core FP64 operator, with per-kernel rooflines."""
@@ -1086,12 +1134,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d",
-                                                   "subbands", "poisson2d"],
+                                                   "full2d_sc", "subbands", "poisson2d"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
                          "c1: the flat-band C1 solve (plain FP64); c4: multi-subband FET gate sweep; "
                          "full2d: Full-2D operator applies/s; subbands: transverse subband eigensolves/s; "
-                         "poisson2d: Full-2D Poisson steps/s")
+                         "poisson2d: Full-2D Poisson steps/s; full2d_sc: the Full-2D self-consistent loop at 0 V")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -1135,6 +1183,8 @@ def main():
         out = run_subbands(args) if rank == 0 else None
     elif args.workload == "poisson2d":
         out = run_poisson2d(args) if rank == 0 else None
+    elif args.workload == "full2d_sc":
+        out = run_full2d_sc(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:
