@@ -8,7 +8,8 @@ benchmark solves), the density and current the reference's transport solve retur
 its GMRES relative residual), and the outputs boundary.physical.XLeft/XRight.rhoBoundary with the
 mode energies and Fermi levels the reference stored beside them; for the sweep's first bias point
 (0 V) the device fields (Vc, eps, Nd, contact lengths), the converged potential and density and
-the Gummel loop's per-iteration history.
+the Gummel loop's per-iteration history; for the whole sweep the bias, the mean current, the Gummel
+iterations and the GMRES iterations of every bias point.
 
     python tests/golden/make_reservoir_golden.py /path/to/reference
 """
@@ -45,6 +46,12 @@ def main(ref_root):
                dy=float(mat.dy), potential0=np.asarray(d["sweep"].potential, dtype=float)[:, :, 0],
                density0=np.asarray(d["sweep"].density, dtype=float)[:, :, 0],
                iterations0=int(np.ravel(d["sweep"].iterations)[0]))
+    # the whole recorded I-V sweep: bias, mean current (results.Id), Gummel iterations per bias
+    out.update(sweep_bias=np.asarray(d["sweep"].bias, dtype=float),
+               sweep_id=np.asarray(d["sweep"].current, dtype=float).mean(axis=0),
+               sweep_iterations=np.asarray(d["sweep"].iterations, dtype=float),
+               sweep_gmres=np.array([sum(h.gmresIterations for h in np.atleast_1d(hb))
+                                     for hb in d["selfConsistency"].history], dtype=float))
     hist = d["selfConsistency"].history[0]
     out["history0"] = np.array([[h.gmresIterations, h.potentialDefect, h.densityChange, h.poissonPhysicalRelres]
                                 for h in hist], dtype=float)
