@@ -251,6 +251,7 @@ def inflow_rhs(f, inflow):
     inc_l = inc_l.reshape(nrx * nry, -1, order="F")
     inc_r = inc_r.reshape(nrx * nry, -1, order="F")
     rhs = np.zeros((AY["nd"], nx, nrx * nry), dtype=complex)                 # [Y dof, X dof, relative]
-    rhs += sx * (lift_l[None, :, None] * inc_l.T[:, None, :])
-    rhs -= sx * (lift_r[None, :, None] * inc_r.T[:, None, :])
+    # the lifts live on the first and last X element only
+    rhs[:, :nl, :] += sx * (lift_l[None, :nl, None] * inc_l.T[:, None, :])
+    rhs[:, nx - nl:, :] -= sx * (lift_r[None, nx - nl:, None] * inc_r.T[:, None, :])
     return rhs.reshape(-1)
