@@ -26,7 +26,9 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -71,6 +73,8 @@ struct wg2d_problem {
   wg::OzakiRowsDev UH, Us;        // real embeddings of U^H and U / sigma (tensor-core path)
   double2 *UHd = nullptr, *Usd = nullptr;   // the same as complex [nrx][nrx] row-major (FP64 path)
   double2 *xinv = nullptr, *xcpl = nullptr; // [nrx][n_el_x][nk][nk]
+  double2* xmaps = nullptr;                  // chunk maps of the X-line sweep [chunk][nk*nk+nk][line]
+  int x_chunk_len = 0, x_chunks = 1;
   int* fwd = nullptr;             // [nrx]
   double2* tinv = nullptr;        // [nrx][nT][nT]
   double2 *pa = nullptr, *pb = nullptr;     // [n] scratch of the preconditioner
@@ -115,6 +119,11 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
 template <typename T> __device__ __forceinline__ T czero();
 template <> __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
 template <> __device__ __forceinline__ float2 czero<float2>() { return make_float2(0.f, 0.f); }
+template <typename T> __device__ __forceinline__ T cone();
+template <> __device__ __forceinline__ double2 cone<double2>() { return make_double2(1.0, 0.0); }
+template <> __device__ __forceinline__ float2 cone<float2>() { return make_float2(1.f, 0.f); }
+__device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
+__device__ __forceinline__ float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
 
 // G_t[r, X, Y] = sum_{e', b} C_t[e][dir][a][b] F[r, X'(e', b), Y] along X (axis 0) or Y (axis 1).
 // grid (ceil(nrel/256), centre dofs of the other axis, n_el * nk of this axis).
@@ -471,6 +480,147 @@ __global__ void __launch_bounds__(128) f2d_xline_kernel(const T* __restrict__ W,
       T v = czero<T>();
 #pragma unroll
       for (int b = 0; b < NK; ++b) v = cfma(Ii[a * NK + b], blk[b], v);
+      prev[a] = v;
+      out[base + nrel * (e * NK + a)] = v;
+    }
+  }
+}
+
+// The same sweep cut into chunks of L elements (sweep order).  The element recurrence is affine in
+// the incoming state, prev_e = -Inv_e Cpl_e prev_{e-1} + Inv_e w_e, so a chunk composes to
+// prev_out = M prev_in + b:
+//   f2d_xline_maps_kernel   (line, chunk): M and b of the chunk from M = I, b = 0;
+//   f2d_xline_apply_kernel  (line, chunk): the incoming state folded from the maps of the chunks
+//                           upwind, then the chunk's elements swept as above, writing out.
+// Threads (line, chunk) with the line fastest; maps stored [chunk][entry][line].
+template <int NK, typename T>
+__global__ void __launch_bounds__(128) f2d_xline_maps_kernel(const T* __restrict__ W, T* __restrict__ maps,
+                                                             const T* __restrict__ inv, const T* __restrict__ cpl,
+                                                             const int* __restrict__ fwd, int nrx, int nry, int nX,
+                                                             int nY, int ne, int L, int nchunk) {
+  const long long lines = (long long)nrx * nry * nY;
+  const long long t = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (t >= lines * nchunk) return;
+  const long long line = t % lines;
+  const int c = (int)(t / lines);
+  const int k = (int)(line % nrx);
+  const long long q = line / nrx;
+  const int ry = (int)(q % nry);
+  const int Y = (int)(q / nry);
+  const long long nrel = (long long)nrx * nry;
+  const long long base = k + (long long)nrx * ry + nrel * (long long)nX * Y;
+  const bool f = fwd[k] != 0;
+  T M[NK][NK], b[NK];
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    b[a] = czero<T>();
+#pragma unroll
+    for (int j = 0; j < NK; ++j) M[a][j] = a == j ? cone<T>() : czero<T>();
+  }
+  const int i1 = min(ne, (c + 1) * L);
+  for (int i = c * L; i < i1; ++i) {
+    const int e = f ? i : ne - 1 - i;
+    const T* Ci = cpl + ((long long)k * ne + e) * NK * NK;
+    const T* Ii = inv + ((long long)k * ne + e) * NK * NK;
+    T CM[NK][NK], r[NK];
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      T v = W[base + nrel * (e * NK + a)];
+#pragma unroll
+      for (int j = 0; j < NK; ++j) {
+        T s = czero<T>();
+#pragma unroll
+        for (int m = 0; m < NK; ++m) s = cfma(Ci[a * NK + m], M[m][j], s);
+        CM[a][j] = s;
+      }
+#pragma unroll
+      for (int m = 0; m < NK; ++m) {
+        const T cc = Ci[a * NK + m];
+        v.x -= cc.x * b[m].x - cc.y * b[m].y;
+        v.y -= cc.x * b[m].y + cc.y * b[m].x;
+      }
+      r[a] = v;
+    }
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      T bb = czero<T>();
+#pragma unroll
+      for (int m = 0; m < NK; ++m) bb = cfma(Ii[a * NK + m], r[m], bb);
+      b[a] = bb;
+#pragma unroll
+      for (int j = 0; j < NK; ++j) {
+        T s = czero<T>();
+#pragma unroll
+        for (int m = 0; m < NK; ++m) s = cfma(Ii[a * NK + m], CM[m][j], s);
+        M[a][j] = cneg(s);
+      }
+    }
+  }
+  T* o = maps + (long long)c * (NK * NK + NK) * lines + line;
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+#pragma unroll
+    for (int j = 0; j < NK; ++j) o[(long long)(a * NK + j) * lines] = M[a][j];
+    o[(long long)(NK * NK + a) * lines] = b[a];
+  }
+}
+
+template <int NK, typename T>
+__global__ void __launch_bounds__(128) f2d_xline_apply_kernel(const T* __restrict__ W, T* __restrict__ out,
+                                                              const T* __restrict__ maps, const T* __restrict__ inv,
+                                                              const T* __restrict__ cpl, const int* __restrict__ fwd,
+                                                              int nrx, int nry, int nX, int nY, int ne, int L,
+                                                              int nchunk) {
+  const long long lines = (long long)nrx * nry * nY;
+  const long long t = (long long)blockIdx.x * 128 + threadIdx.x;
+  if (t >= lines * nchunk) return;
+  const long long line = t % lines;
+  const int c = (int)(t / lines);
+  const int k = (int)(line % nrx);
+  const long long q = line / nrx;
+  const int ry = (int)(q % nry);
+  const int Y = (int)(q / nry);
+  const long long nrel = (long long)nrx * nry;
+  const long long base = k + (long long)nrx * ry + nrel * (long long)nX * Y;
+  const bool f = fwd[k] != 0;
+  T prev[NK];
+#pragma unroll
+  for (int a = 0; a < NK; ++a) prev[a] = czero<T>();
+  for (int cc = 0; cc < c; ++cc) {
+    const T* o = maps + (long long)cc * (NK * NK + NK) * lines + line;
+    T nxt[NK];
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      T s = o[(long long)(NK * NK + a) * lines];
+#pragma unroll
+      for (int j = 0; j < NK; ++j) s = cfma(o[(long long)(a * NK + j) * lines], prev[j], s);
+      nxt[a] = s;
+    }
+#pragma unroll
+    for (int a = 0; a < NK; ++a) prev[a] = nxt[a];
+  }
+  const int i1 = min(ne, (c + 1) * L);
+  for (int i = c * L; i < i1; ++i) {
+    const int e = f ? i : ne - 1 - i;
+    const T* Ci = cpl + ((long long)k * ne + e) * NK * NK;
+    const T* Ii = inv + ((long long)k * ne + e) * NK * NK;
+    T blk[NK];
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      T v = W[base + nrel * (e * NK + a)];
+#pragma unroll
+      for (int m = 0; m < NK; ++m) {
+        const T cc2 = Ci[a * NK + m];
+        v.x -= cc2.x * prev[m].x - cc2.y * prev[m].y;
+        v.y -= cc2.x * prev[m].y + cc2.y * prev[m].x;
+      }
+      blk[a] = v;
+    }
+#pragma unroll
+    for (int a = 0; a < NK; ++a) {
+      T v = czero<T>();
+#pragma unroll
+      for (int m = 0; m < NK; ++m) v = cfma(Ii[a * NK + m], blk[m], v);
       prev[a] = v;
       out[base + nrel * (e * NK + a)] = v;
     }
@@ -1158,14 +1308,31 @@ static void precond_stages(wg2d_problem* h, const T* UH, const T* Us, const T* x
     f2d_dense_rx_kernel<T><<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
         UH, r, pa, h->nrx, ncols);
   const long long lines = (long long)h->nrx * h->nry * h->nY;
-  const unsigned lb = (unsigned)((lines + 127) / 128);
-  switch (h->s.nk_x) {
-    case 2: f2d_xline_kernel<2, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
-                                                             h->nY, h->s.n_el_x); break;
-    case 3: f2d_xline_kernel<3, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
-                                                             h->nY, h->s.n_el_x); break;
-    default: f2d_xline_kernel<4, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
-                                                              h->nY, h->s.n_el_x); break;
+  if (h->x_chunks > 1 && h->xmaps) {
+    T* maps = reinterpret_cast<T*>(h->xmaps);
+    const int L = h->x_chunk_len, C = h->x_chunks, ne = h->s.n_el_x;
+    const unsigned cb = (unsigned)((lines * C + 127) / 128);
+#define WG_XLINE_CHUNKED(NK_)                                                                                \
+  f2d_xline_maps_kernel<NK_, T><<<cb, 128, 0, h->stream>>>(pa, maps, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX, \
+                                                          h->nY, ne, L, C);                                   \
+  f2d_xline_apply_kernel<NK_, T><<<cb, 128, 0, h->stream>>>(pa, pb, maps, xinv, xcpl, h->fwd, h->nrx, h->nry,  \
+                                                           h->nX, h->nY, ne, L, C);
+    switch (h->s.nk_x) {
+      case 2: WG_XLINE_CHUNKED(2) break;
+      case 3: WG_XLINE_CHUNKED(3) break;
+      default: WG_XLINE_CHUNKED(4) break;
+    }
+#undef WG_XLINE_CHUNKED
+  } else {
+    const unsigned lb = (unsigned)((lines + 127) / 128);
+    switch (h->s.nk_x) {
+      case 2: f2d_xline_kernel<2, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
+                                                               h->nY, h->s.n_el_x); break;
+      case 3: f2d_xline_kernel<3, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
+                                                               h->nY, h->s.n_el_x); break;
+      default: f2d_xline_kernel<4, T><<<lb, 128, 0, h->stream>>>(pa, pb, xinv, xcpl, h->fwd, h->nrx, h->nry, h->nX,
+                                                                h->nY, h->s.n_el_x); break;
+    }
   }
   const size_t tsm = sizeof(T) * ((size_t)h->nT * h->nT + (size_t)h->nT * kTxTile);
   const dim3 tg((unsigned)((h->nX + kTxTile - 1) / kTxTile), (unsigned)h->nrx);
@@ -1234,9 +1401,11 @@ static void free_preconditioner(wg2d_problem* h) {
   wg::ozaki_free(h->UH);
   wg::ozaki_free(h->Us);
   void* ptrs[] = {h->UHd, h->Usd, h->xinv, h->xcpl, h->fwd, h->tinv, h->pa, h->pb, h->UH32, h->Us32, h->xinv32,
-                  h->xcpl32, h->tinv32, h->pa32, h->pb32};
+                  h->xcpl32, h->tinv32, h->pa32, h->pb32, h->xmaps};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  h->xmaps = nullptr;
+  h->x_chunks = 1;
   h->UHd = h->Usd = h->xinv = h->xcpl = h->tinv = h->pa = h->pb = nullptr;
   h->UH32 = h->Us32 = h->xinv32 = h->xcpl32 = h->tinv32 = h->pa32 = h->pb32 = nullptr;
   h->fwd = nullptr;
@@ -1415,6 +1584,17 @@ int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, cons
   h->sigma = sigma;
   const int nr = h->nrx, nk = h->s.nk_x, ne = h->s.n_el_x;
   const size_t nx = (size_t)nr * ne * nk * nk, nt = (size_t)nr * nT * nT;
+  // X-line sweep in chunks of L elements (about 16 chunks, at least 4 elements each);
+  // WG_XLINE_CHUNKS=<n> sets the chunk count, 0 or 1 keeps one sequential sweep per line
+  {
+    int C = ne >= 8 ? std::min(16, ne / 4) : 1;
+    if (const char* env = getenv("WG_XLINE_CHUNKS")) C = std::max(1, std::min(atoi(env), ne));
+    const int L = (ne + C - 1) / std::max(1, C);
+    h->x_chunk_len = L;
+    h->x_chunks = C > 1 ? (ne + L - 1) / L : 1;
+    if (h->x_chunks > 1)
+      F2_CK(dalloc(&h->xmaps, (size_t)h->x_chunks * (nk * nk + nk) * ((size_t)nr * h->nry * h->nY)));
+  }
   F2_CK(dalloc(&h->fwd, nr));
   F2_CK(cudaMemcpy(h->fwd, forward, sizeof(int) * nr, cudaMemcpyHostToDevice));
   // U^H and U / sigma as complex [nr][nr] row-major
