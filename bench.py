@@ -752,13 +752,11 @@ def run_full2d(args):
     # last bias point: stored potential, contact-mode reservoir right-hand side
     for _, (_, _, _, o) in res.items():
         o.close()
-    res = {}
     mat_r, V_r, efl_r, efr_r = full2d_recorded_case()
     op = Full2DOperator(mat_r, V_r)
     t0 = time.perf_counter()
     rhs, inflow = op.reservoir_rhs(efl_r, efr_r)
     rhs_s = time.perf_counter() - t0
-    res[True] = (None, None, None, op)
     op.set_preconditioner()
     t0 = time.perf_counter()
     st, sinfo, xs = op.solve(rhs, tol=5e-6, maxit=args.solve_maxit, restart=40) if args.solve_maxit > 0 else \
@@ -803,8 +801,7 @@ def run_full2d(args):
                     "rhs": "the recorded run's system at 0.6 V: stored potential, contact-mode reservoirs "
                            "(contact-neutrality E_F %.6f / %.6f eV), right-hand side built in %.3f s on the host"
                            % (inflow["source"][1]["fermiLevelUsed"], inflow["drain"][1]["fermiLevelUsed"], rhs_s)}
-    for _, (_, _, _, o) in res.items():
-        o.close()
+    op.close()
     if not args.no_cpu:
         from oracle import full2d as F2
         t0 = time.perf_counter()

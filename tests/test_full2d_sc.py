@@ -57,3 +57,21 @@ def test_gpu_recorded_bias_point_reproduced(built_lib):
         assert abs(h["poissonPhysicalRelres"] - r[3]) <= 1e-2 * r[3]
     assert np.abs(sw["potential"][:, :, 0] - g["potential0"]).max() <= 1e-5
     assert np.abs(sw["density"][:, :, 0] - g["density0"]).max() <= 1e-3 * np.abs(g["density0"]).max()
+
+
+@pytest.mark.gpu
+def test_gpu_recorded_sweep_continuation(built_lib):
+    """The first two bias points of the recorded sweep (0 and 0.02 V): the second starts from the
+    first's potential shifted by the bias step and its state (solve2D_rtd_self_consistent.m:91-96,
+    196-198) and needs the recorded 9 Gummel iterations; the mean currents follow the recorded I-V
+    curve."""
+    from real_space_dg_gb300.full2d_sc import solve2D_rtd_self_consistent
+    g, mat = recorded_sc_mat()
+    mat["Vdd"] = np.asarray(g["sweep_bias"])[:2]
+    res = solve2D_rtd_self_consistent("DG", mat, {"mixing": 0.3})
+    sw = res["sweep"]
+    assert res["converged"]
+    assert list(sw["iterations"]) == [int(v) for v in np.asarray(g["sweep_iterations"])[:2]]
+    ids = np.mean(sw["current"], axis=0)
+    scale = np.abs(np.asarray(g["sweep_id"])).max()
+    assert np.abs(ids - np.asarray(g["sweep_id"])[:2]).max() <= 1e-3 * scale
