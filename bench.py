@@ -938,6 +938,33 @@ def poisson2d_case(cfg=POISSON2D):
     return mat
 
 
+def run_full2d_solve(args):
+    """The mixed Full-2D solve alone on the recorded run's 0.6 V system (stored potential, contact-mode
+    reservoirs, line-transverse preconditioner, flexible GMRES(40) with FP64 refinement), to a 1e-12
+    residual for at most --solve-maxit refinements: a fixed amount of inner iterations for timing
+    and for the per-kernel launch list.  value = inner iterations/s."""
+    import __graft_entry__ as g
+    g.build()
+    from real_space_dg_gb300.full2d import Full2DOperator
+    mat_r, V_r, efl_r, efr_r = full2d_recorded_case()
+    with Full2DOperator(mat_r, V_r) as op:
+        rhs, _ = op.reservoir_rhs(efl_r, efr_r)
+        op.set_preconditioner()
+        clocks = ClockSampler()
+        clocks.start()
+        t0 = time.perf_counter()
+        st, info, _ = op.solve(rhs, tol=1e-12, maxit=args.solve_maxit, restart=40, mixed=True)
+        wall = time.perf_counter() - t0
+        clk = clocks.stop()
+    its = info["iterations"]
+    return {"metric": "Full-2D mixed solve inner iterations/s (3,136,320 unknowns)", "value": round(its / wall, 2),
+            "unit": "iterations/s", "n_gpus": 1, "steps": its, "warmup": 0,
+            "ms_per_step": round(1000 * wall / max(1, its), 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 inner, f64 refinement", "data": "the recorded run's 0.6 V system",
+            "config": {"workload": "Full-2D mixed FGMRES(40), %d refinements, line-transverse preconditioner"
+                                   % info["cycles"]}, "relres": info["relres"], "clocks": clk}
+
+
 def run_poisson2d(args):
     """f3: the Poisson step of the Full-2D Gummel loop (project_DG_density_RTD + the approximate
     Newton update of solve_Poisson2D_rtd) for 16 bias points on the material grid of the
@@ -1146,12 +1173,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d",
-                                                   "full2d_sc", "subbands", "poisson2d"],
+                                                   "full2d_sc", "full2d_solve", "subbands", "poisson2d"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
                          "c1: the flat-band C1 solve (plain FP64); c4: multi-subband FET gate sweep; "
                          "full2d: Full-2D operator applies/s; subbands: transverse subband eigensolves/s; "
-                         "poisson2d: Full-2D Poisson steps/s; full2d_sc: the Full-2D self-consistent loop at 0 V")
+                         "poisson2d: Full-2D Poisson steps/s; full2d_sc: the Full-2D self-consistent loop at 0 V; "
+                         "full2d_solve: the mixed Full-2D solve alone (--solve-maxit refinements)")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -1199,6 +1227,8 @@ def main():
         out = run_poisson2d(args) if rank == 0 else None
     elif args.workload == "full2d_sc":
         out = run_full2d_sc(args) if rank == 0 else None
+    elif args.workload == "full2d_solve":
+        out = run_full2d_solve(args) if rank == 0 else None
     else:
         out = run_ours(args, rank, world, dist)
     if rank == 0 and out is not None:

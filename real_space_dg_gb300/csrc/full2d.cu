@@ -739,17 +739,22 @@ __global__ void __launch_bounds__(256) f2d_scale32(const float2* __restrict__ x,
 __global__ void __launch_bounds__(256) f2d_correct32(double2* __restrict__ x, const float2* __restrict__ Z,
                                                      long long zstride, const double2* __restrict__ y, int k,
                                                      const double* __restrict__ beta, long long n) {
+  // The correction sum_i y_i Z_i of the FP32 inner solve is accumulated in FP32 (it is only FP32-
+  // accurate; FP64 products here made the kernel FP64-pipe-bound), then added to the FP64 iterate.
+  __shared__ float2 ys[64];
+  for (int i = threadIdx.x; i < min(k, 64); i += blockDim.x) ys[i] = make_float2((float)y[i].x, (float)y[i].y);
+  __syncthreads();
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
   if (t >= n) return;
-  double2 acc = make_double2(0.0, 0.0);
+  float2 acc = make_float2(0.f, 0.f);
   for (int i = 0; i < k; ++i) {
     const float2 z = Z[(long long)i * zstride + t];
-    const double2 c = y[i];
-    acc.x += c.x * z.x - c.y * z.y;
-    acc.y += c.x * z.y + c.y * z.x;
+    const float2 c = i < 64 ? ys[i] : make_float2((float)y[i].x, (float)y[i].y);
+    acc.x = fmaf(c.x, z.x, fmaf(-c.y, z.y, acc.x));
+    acc.y = fmaf(c.x, z.y, fmaf(c.y, z.x, acc.y));
   }
-  x[t].x += beta[0] * acc.x;
-  x[t].y += beta[0] * acc.y;
+  x[t].x += beta[0] * (double)acc.x;
+  x[t].y += beta[0] * (double)acc.y;
 }
 
 // ---------------- GMRES vector kernels (FP64, deterministic two-stage reductions)
