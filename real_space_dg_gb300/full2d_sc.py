@@ -22,9 +22,13 @@ from ._lib import WignerError
 from .full2d import Full2DOperator
 from .poisson2d import make_RTD_poisson_step
 
+# innerRestart: restart length of the mixed form's FP32 inner FGMRES (each inner cycle ends with an FP64
+# residual refinement); None takes mat.dg.params.full2D_gmresRestart (the reference's GMRES(40)).  20 is
+# faster on the recorded 3.1M-unknown system (3.42 s vs 3.80 s per solve to 5e-6: 7% more iterations, each
+# with less Gram-Schmidt work) and lands on different, equally converged transport states.
 DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityTolerance=5e-4,
                 poissonResidualTolerance=8e-2, chargeNeutralityTolerance=1e-3, poissonMethod="",
-                initialPhi=None, initialRho=None, mixed=True)
+                initialPhi=None, initialRho=None, mixed=True, innerRestart=None)
 
 
 def _options(options):
@@ -102,8 +106,11 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                 efr = (float(mat["EfR"]) if "EfR" in mat else Vc[-1, 0] + 0.05) - bias[ib]
                 op.set_potential(V)
                 rhs, _ = op.reservoir_rhs(efl, efr, V)
-                st, info, rho_new = op.solve(rhs, x0=rho, tol=tol, maxit=maxit if not o["mixed"] else 4 * maxit,
-                                             restart=restart, mixed=bool(o["mixed"]))
+                mixed = bool(o["mixed"])
+                m_in = int(o["innerRestart"] or restart) if mixed else restart
+                st, info, rho_new = op.solve(rhs, x0=rho, tol=tol,
+                                             maxit=maxit if not mixed else maxit * max(1, restart * 4 // m_in),
+                                             restart=m_in, mixed=mixed)
                 h = dict(iteration=it, transportFlag=int(st), transportRelres=info["relres"],
                          gmresIterations=info["iterations"], densityChange=np.inf, potentialDefect=np.inf,
                          poissonConverged=False, poissonPhysicalRelres=np.nan)
