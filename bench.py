@@ -558,7 +558,24 @@ def run_fet(args):
     from real_space_dg_gb300.transport import M0, Problem1D, shape_from_mat, solve_transport_DG_2D
     spec = devices.FETSpec()
     vgs = np.linspace(0.0, FET["vg_max"], FET["n_gates"])
-    pts = [devices.make_fet(spec, float(vg), FET["v_drain"]) for vg in vgs]
+    utb = args.workload == "c4_utb"
+    sub = None
+    if utb:
+        # the confinement direction resolved on a grid (5 nm body between 1 nm oxides, dy = 0.1 nm): every
+        # step solves the subbands of all gate points on the GPU (one batched call) before the transport
+        from real_space_dg_gb300.subbands import SubbandSolver
+        secs = [devices.utb_cross_section(spec, float(vg), FET["v_drain"]) for vg in vgs]
+        me_all = np.stack([c[2] for c in secs])
+        V_all = np.stack([c[3] for c in secs])
+        sub = SubbandSolver(me_all.shape[1], me_all.shape[2], me_all.shape[3], spec.n_modes, batch=len(vgs))
+        E0, _ = sub.solve(me_all, V_all, 0.1)
+        pts = []
+        for gi, vg in enumerate(vgs):
+            mat, _, _, _, _ = devices.make_fet(spec, float(vg), FET["v_drain"])
+            efl = float(E0[gi][:, 0, :].min()) + spec.fermi_offset_ev
+            pts.append((mat, E0[gi], None, efl, efl - FET["v_drain"]))
+    else:
+        pts = [devices.make_fet(spec, float(vg), FET["v_drain"]) for vg in vgs]
     mat0 = pts[0][0]
     shp = shape_from_mat(mat0)
     nv, nm = int(mat0["n_of_valleys"]), int(mat0["n_of_modes"])
@@ -570,6 +587,11 @@ def run_fet(args):
     x_nm = np.asarray(mat0["x"], dtype=float)
 
     def step():
+        if utb:
+            E, _ = sub.solve(me_all, V_all, 0.1)
+            for gi in range(len(pts)):
+                mat, _, _, efl, efr = pts[gi]
+                pts[gi] = (mat, E[gi], None, efl, efr)
         for gi, (mat, esub, _, efl, efr) in enumerate(pts):
             for iv in range(nv):
                 m = np.asarray(mat["me_x"], dtype=float)[iv, :, 0] * M0
@@ -595,6 +617,8 @@ def run_fet(args):
     iters = float(np.mean([i["iterations"] for i in infos[-1]]))
     dev_bytes = P.device_bytes
     P.close()
+    if sub is not None:
+        sub.close()
     n_pts = len(pts) * args.steps
     out = {
         "metric": "converged gate points/s at 1e-8 transport residual (C4 multi-subband FET, %d subbands per point)"
@@ -603,8 +627,11 @@ def run_fet(args):
         "warmup": args.warmup, "ms_per_step": round(1000 * wall / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "bf16/f32 in f64 refinement",
-        "data": "synthetic UTB Si FET: subbands of a 5 x 5 nm box, compact gate-controlled band profile "
-                "(not self-consistent)",
+        "data": ("synthetic double-gate UTB Si FET: subbands from the GPU transverse eigensolve of the resolved "
+                 "5 nm body between 1 nm oxides (solved inside every step), compact gate-controlled band profile "
+                 "(not self-consistent)" if utb else
+                 "synthetic UTB Si FET: subbands of a 5 x 5 nm box, compact gate-controlled band profile "
+                 "(not self-consistent)"),
         "config": {"workload": "C4 FET 50 nm (15 nm S/D at 1e20 cm^-3), p=2, N_el=200, Nk=256, "
                                "%d unknowns per subband, %d gate points x %d subbands in one handle"
                                % (shp["n_el"] * shp["n_local"] * shp["nk"], len(pts), nsub),
@@ -613,7 +640,10 @@ def run_fet(args):
         "subband_solves_converged": conv, "subband_solves": B, "gmres_iterations_per_subband": iters,
         "gpu_launches": int(sum(v[2] for v in counted.values())) if counted else None, "clocks": clk,
     }
-    if not args.no_e2e:
+    if utb:
+        out["metric"] = out["metric"].replace("C4 multi-subband FET", "C4 FET with GPU subband eigensolve")
+        out["config"]["subbands"] = "32 gates x 2 valleys x 401 slices, Ny = 71, 4 modes: one batched device call per step"
+    if not args.no_e2e and not utb:
         Pe = Problem1D(batch=nsub, **kw, **shp)
         t0 = time.perf_counter()
         cur = []
@@ -1173,13 +1203,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c2", "served", "transient", "apply", "c1", "c4", "full2d",
-                                                   "full2d_sc", "full2d_solve", "subbands", "poisson2d"],
+                                                   "full2d_sc", "full2d_solve", "subbands", "poisson2d", "c4_utb"],
                     help="c2: the headline batched C2 sweep; served: mixed-shape requests through the server; "
                          "transient: batched Crank-Nicolson steps of the C5 RTD; apply: operator applies/s; "
                          "c1: the flat-band C1 solve (plain FP64); c4: multi-subband FET gate sweep; "
                          "full2d: Full-2D operator applies/s; subbands: transverse subband eigensolves/s; "
                          "poisson2d: Full-2D Poisson steps/s; full2d_sc: the Full-2D self-consistent loop at 0 V; "
-                         "full2d_solve: the mixed Full-2D solve alone (--solve-maxit refinements)")
+                         "full2d_solve: the mixed Full-2D solve alone (--solve-maxit refinements); "
+                         "c4_utb: the C4 sweep with its subbands from the GPU eigensolve in every step")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
     ap.add_argument("--restart", type=int, default=50)
@@ -1215,7 +1246,7 @@ def main():
         out = run_transient(args) if rank == 0 else None
     elif args.workload == "apply":
         out = run_apply(args) if rank == 0 else None
-    elif args.workload == "c4":
+    elif args.workload in ("c4", "c4_utb"):
         out = run_fet(args) if rank == 0 else None
     elif args.workload == "c1":
         out = run_c1(args) if rank == 0 else None
