@@ -37,6 +37,13 @@
  *    (RK4 kept, Crank-Nicolson added)                -> wg_transient_set_bias / wg_transient_run
  *  - the bias loop of RTD/solve2D_rtd_self_consistent.m, served: requests of
  *    mixed shapes admitted under a device-memory budget -> wg_server_*
+ *  - sysInfo.makeGPUApply() and the Krylov solve of the Full-2D solver
+ *    (DG_code/core/get_SysM_full2D.m:81, DG_code/solve_transport_DG_full2D.m:132-346,
+ *    get_LineTransversePreconditioner_full2D.m)       -> wg2d_*
+ *  - [M,node_num,node_type] = eval_Poisson2D_rtd(mat), project_DG_density_RTD and
+ *    solve_Poisson2D_rtd (RTD/*.m, the poissonStep of make_RTD_poisson_step.m)
+ *                                                     -> wg_poisson2d_*
+ *  - [E,V] = solve_subbands(mat)                      solve_subbands.m:1 -> wg_subbands_*
  */
 #ifndef WIGNER_GB300_H
 #define WIGNER_GB300_H
