@@ -41,7 +41,7 @@
  *    (DG_code/core/get_SysM_full2D.m:81, DG_code/solve_transport_DG_full2D.m:132-346,
  *    get_LineTransversePreconditioner_full2D.m)       -> wg2d_*
  *  - [M,node_num,node_type] = eval_Poisson2D_rtd(mat), project_DG_density_RTD and
- *    solve_Poisson2D_rtd (RTD/*.m, the poissonStep of make_RTD_poisson_step.m)
+ *    solve_Poisson2D_rtd (RTD directory; the poissonStep of make_RTD_poisson_step.m)
  *                                                     -> wg_poisson2d_*
  *  - [E,V] = solve_subbands(mat)                      solve_subbands.m:1 -> wg_subbands_*
  */
