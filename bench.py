@@ -904,12 +904,14 @@ def run_subbands(args):
         sol.status(stream.cuda_stream)
     slices = G * nv * nx
     value = slices * args.steps / (ms / 1000.0)
-    # per slice: Sturm counts of ny entries (2 subtractions, 1 division, 1 compare) -- 1 + the
-    # 32 / nm lanes per candidate x ~54 / log2(32 / nm + 1) multisection steps x nm candidates
-    # (all eigenvalues positive here) -- and the 5 passes of the twisted factorisation per
-    # mode (~14 flops per entry)
+    # per slice, FP64 only: Sturm counts of ny entries (2 subtractions, 1 division, 1 compare) -- 1 + the
+    # 2 bracket checks + 32 / nm lanes per candidate x the multisection steps from the FP32 bracket
+    # (4e-5 of the spectral radius) down to eps x nm candidates (all eigenvalues positive here) -- and
+    # the 5 passes of the twisted factorisation per mode (~14 flops per entry); the coarse FP32
+    # multisection runs on the FP32 pipe and is not counted
     g = 32 // nm
-    flops_slice = ((1 + int(np.ceil(54 / np.log2(g + 1))) * g * nm) * 4 + 14 * nm) * ny
+    steps64 = int(np.ceil(np.log(4e-5 / 2.2e-16) / np.log(g + 1)))
+    flops_slice = ((3 + steps64 * g * nm) * 4 + 14 * nm) * ny
     achieved = flops_slice * value / 1e12
     out = {"metric": "transverse subband eigensolves (slices/s, %d eigenpairs of smallest magnitude per slice)" % nm,
            "value": round(value, 1), "unit": "slices/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,

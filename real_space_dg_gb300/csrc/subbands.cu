@@ -41,7 +41,11 @@ constexpr int kMaxNy = 1024;
 
 struct SliceShared {
   double *a, *b, *b2, *rr, *lam;
+  float *af, *b2f;   // FP32 copies of a and b^2 for the coarse bisection
 };
+
+// per warp: a, b, b2, rr [ny] doubles, lam [2 kMaxModes] doubles, af, b2f [ny] floats
+__host__ __device__ constexpr int slice_doubles(int ny) { return 5 * ny + 2 * kMaxModes; }
 
 __device__ __forceinline__ SliceShared slice_shared(double* base, int ny) {
   SliceShared s;
@@ -50,6 +54,8 @@ __device__ __forceinline__ SliceShared slice_shared(double* base, int ny) {
   s.b2 = base + 2 * ny;
   s.rr = base + 3 * ny;
   s.lam = base + 4 * ny;
+  s.af = reinterpret_cast<float*>(base + 4 * ny + 2 * kMaxModes);
+  s.b2f = s.af + ny;
   return s;
 }
 
@@ -66,6 +72,19 @@ __device__ int sturm_count(const SliceShared& s, int n, double x, double pivmin)
   return c;
 }
 
+// The same count in FP32 (coarse: wrong only within ~ny FP32 ulps of an eigenvalue).
+__device__ int sturm_count32(const SliceShared& s, int n, float x, float pivmin) {
+  float q = s.af[0] - x;
+  q = fabsf(q) < pivmin ? -pivmin : q;
+  int c = q < 0.f;
+  for (int i = 1; i < n; ++i) {
+    q = s.af[i] - x - s.b2f[i - 1] / q;
+    q = fabsf(q) < pivmin ? -pivmin : q;
+    c += q < 0.f;
+  }
+  return c;
+}
+
 __device__ __forceinline__ double hop(double t0, double ma, double mb) { return -2.0 * t0 / (ma + mb); }
 
 __global__ void __launch_bounds__(128) subband_slice_kernel(const double* __restrict__ me_y, const double* __restrict__ pot,
@@ -77,7 +96,7 @@ __global__ void __launch_bounds__(128) subband_slice_kernel(const double* __rest
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int slice = blockIdx.x * (blockDim.x >> 5) + warp;   // slice = (problem * nv + v) * nx + x
   if (slice >= nslice) return;
-  SliceShared s = slice_shared(smem + (size_t)warp * (4 * ny + 2 * kMaxModes), ny);
+  SliceShared s = slice_shared(smem + (size_t)warp * slice_doubles(ny), ny);
   const double* m = me_y + (size_t)slice * ny;
   const double* V = pot + ((size_t)(slice / (nv * nx)) * nx + slice % nx) * ny;
 
@@ -101,6 +120,8 @@ __global__ void __launch_bounds__(128) subband_slice_kernel(const double* __rest
       s.b[i] = 0.0;
       s.rr[i] = 1.0;
     }
+    s.af[i] = (float)s.a[i];
+    s.b2f[i] = (float)s.b2[i];
   }
   if (__any_sync(0xffffffffu, bad)) {
     if (lane == 0) atomicOr(err, 1);
@@ -138,7 +159,37 @@ __global__ void __launch_bounds__(128) subband_slice_kernel(const double* __rest
     const bool mine = c < nc;
     const int k = c0 + (mine ? c : 0);
     const unsigned gmask = (g == 32 ? 0xffffffffu : ((1u << g) - 1u)) << (mine ? c * g : 0);
-    double lo = glo, hi = ghi;
+    // coarse FP32 multisection to ~1e-5 of the spectral radius (FP32 divisions are cheap)
+    const float pivf = FLT_MIN * fmaxf(1.f, (float)bmax), ctol = 1e-5f * (float)gnorm;
+    float flo = (float)glo, fhi = (float)ghi;
+    for (int it = 0; it < 64; ++it) {
+      const bool open = mine && fhi - flo > ctol;
+      if (!__any_sync(0xffffffffu, open)) break;
+      const float step = (fhi - flo) / (g + 1);
+      const float p = flo + (j + 1) * step;
+      const bool above = open && (p >= fhi || (p > flo && sturm_count32(s, ny, p, pivf) > k));
+      const unsigned vote = __ballot_sync(0xffffffffu, above) & gmask;
+      if (open) {
+        const int jf = vote ? __ffs(vote) - 1 - c * g : g;
+        const float nlo = jf == 0 ? flo : fmaxf(flo, flo + jf * step);
+        const float nhi = jf == g ? fhi : fminf(fhi, flo + (jf + 1) * step);
+        if (!(nlo > flo || nhi < fhi)) break;
+        flo = nlo;
+        fhi = nhi;
+      }
+    }
+    // widen by a margin and confirm the bracket with FP64 counts (count(lo) <= k < count(hi)); a
+    // bracket the FP32 counts got wrong falls back to the Gershgorin interval
+    double lo = fmax(glo, (double)flo - 2e-5 * gnorm), hi = fmin(ghi, (double)fhi + 2e-5 * gnorm);
+    {
+      const bool chk = mine && j < 2;
+      const int cnt = chk ? sturm_count(s, ny, j == 0 ? lo : hi, pivmin) : 0;
+      const bool bad = chk && (j == 0 ? cnt > k : cnt <= k);
+      if (__ballot_sync(0xffffffffu, bad) & gmask) {
+        lo = glo;
+        hi = ghi;
+      }
+    }
     for (int it = 0; it < 256; ++it) {
       const bool open = mine && hi - lo > atol + 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi));
       if (!__any_sync(0xffffffffu, open)) break;
@@ -259,7 +310,7 @@ __global__ void __launch_bounds__(256) subband_cleanup_kernel(double* __restrict
     for (int i = lane; i < ny; i += 32) v[i] = -v[i];
 }
 
-size_t slice_smem(int ny) { return (size_t)(4 * ny + 2 * kMaxModes) * sizeof(double); }
+size_t slice_smem(int ny) { return (size_t)slice_doubles(ny) * sizeof(double); }
 
 int warps_per_block(int ny) {
   int w = 4;
