@@ -1153,7 +1153,7 @@ def run_full2d_sc(args):
                                   "3,136,320 unknowns; %d bias points from 0 V in 0.02 V steps; mixing 0.3, Newton "
                                   "Poisson, GMRES(40) 5e-6" % nb, "wall_s": round(wall, 2),
                       "timing": "wall clock of the whole sweep (host set-up of reservoirs and observables included)"},
-           "converged_bias_points": done,
+           "converged_bias_points": done, "phase_seconds": res.get("timing"),
            "gummel_iterations": [int(v) for v in sw["iterations"][:done]],
            "recorded_gummel_iterations": [int(v) for v in np.asarray(gold["sweep_iterations"])[:done]],
            "gmres_iterations_total": int(its),

@@ -15,6 +15,8 @@ Poisson residual at the current potential decide convergence, and phi <- phi + m
 (candidate - phi).  Dirichlet contacts (phi(source) = 0, phi(drain) = bias); the Neumann-contact
 variant (prepare_RTD_neumann_contacts.m) is not built.
 """
+import time
+
 import numpy as np
 
 from . import _lib
@@ -56,7 +58,8 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
     """The self-consistent sweep over mat['Vdd'] (solve2D_rtd_self_consistent.m).  Returns a dict
     with the reference's sweep fields (bias, current [X nDof x nb], density [X nDof x Ny x nb],
     potential V and phi [Nx x Ny x nb], flag, relres, converged, iterations, status) and the
-    per-bias histories (gmresIterations, potentialDefect, densityChange, poissonPhysicalRelres).
+    per-bias histories (gmresIterations, potentialDefect, densityChange, poissonPhysicalRelres) and the
+    wall time per phase (timing: potential, reservoir, transport, observables, poisson seconds).
     ``callback(bias_index, iteration, history_entry)`` is called after every Poisson step."""
     if str(solver).upper() != "DG":
         raise WignerError(_lib.WG_ERR_ARG, "RTD:UnsupportedSolver: the self-consistency loop uses the Full-2D DG solver")
@@ -88,6 +91,8 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                  phi=np.zeros((nx, ny, nb)), flag=np.full(nb, -1), relres=np.full(nb, np.nan),
                  converged=np.zeros(nb, dtype=bool), iterations=np.zeros(nb, dtype=int), status=[])
     histories = []
+    timing = dict(potential_s=0.0, reservoir_s=0.0, transport_s=0.0, observables_s=0.0, poisson_s=0.0)
+    clock = time.perf_counter
     rho = o["initialRho"]
     prev_phi = None
     try:
@@ -104,13 +109,20 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                 V = Vc - phi
                 efl = float(mat["EfL"]) if "EfL" in mat else Vc[0, 0] + 0.05
                 efr = (float(mat["EfR"]) if "EfR" in mat else Vc[-1, 0] + 0.05) - bias[ib]
+                t0 = clock()
                 op.set_potential(V)
+                t1 = clock()
                 rhs, _ = op.reservoir_rhs(efl, efr, V)
+                t2 = clock()
                 mixed = bool(o["mixed"])
                 m_in = int(o["innerRestart"] or restart) if mixed else restart
                 st, info, rho_new = op.solve(rhs, x0=rho, tol=tol,
                                              maxit=maxit if not mixed else maxit * max(1, restart * 4 // m_in),
                                              restart=m_in, mixed=mixed)
+                t3 = clock()
+                timing["potential_s"] += t1 - t0
+                timing["reservoir_s"] += t2 - t1
+                timing["transport_s"] += t3 - t2
                 h = dict(iteration=it, transportFlag=int(st), transportRelres=info["relres"],
                          gmresIterations=info["iterations"], densityChange=np.inf, potentialDefect=np.inf,
                          poissonConverged=False, poissonPhysicalRelres=np.nan)
@@ -118,11 +130,15 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                     history.append(h)
                     status = "transport-not-converged"
                     break
+                t0 = clock()
                 n, j, nDG, _ = op.observables(rho_new)
+                timing["observables_s"] += clock() - t0
                 if prev_n is not None:
                     h["densityChange"] = float(np.linalg.norm(n - prev_n) /
                                                max(np.linalg.norm(n), np.linalg.norm(prev_n), np.finfo(float).tiny))
+                t0 = clock()
                 cand, pinfo = step({"transport": {"nDG": nDG, "p": p_axes}, "phi": phi, "bias": bias[ib]})
+                timing["poisson_s"] += clock() - t0
                 _check_phi(cand, mat, bias[ib], periodic)
                 h["poissonConverged"] = bool(pinfo["converged"])
                 h["potentialDefect"] = float(np.abs(cand - phi).max())
@@ -165,5 +181,6 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
         op.close()
         setup["operator"].close()
     return {"sweep": sweep, "histories": histories, "phi": phi, "status": "self-consistency-" + status,
+            "timing": {k: round(v, 3) for k, v in timing.items()},
             "Id": np.nanmean(sweep["current"], axis=0) if sweep["current"] is not None else None,
             "converged": bool(np.all(sweep["converged"]))}
