@@ -712,26 +712,36 @@ __global__ void __launch_bounds__(256) f2d_dot_partial32(const float2* __restric
   }
 }
 
+// w -= sum_i h_i V_i in FP32.  The coefficients are converted to FP32 once per block into shared memory:
+// converting them per element put every element x vector through the FP64 pipe (98% busy, DRAM at 35%).
+constexpr int kGsStage = 256;
 __global__ void __launch_bounds__(256) f2d_gs_update32(const float2* __restrict__ V, long long vstride,
                                                        float2* __restrict__ w, const double2* __restrict__ h, int nv,
                                                        long long n) {
+  __shared__ float2 hs[kGsStage];
+  for (int i = threadIdx.x; i < min(nv, kGsStage); i += blockDim.x) hs[i] = make_float2((float)h[i].x, (float)h[i].y);
+  __syncthreads();
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
   if (t >= n) return;
   float2 acc = w[t];
   for (int i = 0; i < nv; ++i) {
     const float2 v = V[(long long)i * vstride + t];
-    const float cx = (float)h[i].x, cy = (float)h[i].y;
-    acc.x -= cx * v.x - cy * v.y;
-    acc.y -= cx * v.y + cy * v.x;
+    const float2 c = i < kGsStage ? hs[i] : make_float2((float)h[i].x, (float)h[i].y);
+    acc.x -= c.x * v.x - c.y * v.y;
+    acc.y -= c.x * v.y + c.y * v.x;
   }
   w[t] = acc;
 }
 
 __global__ void __launch_bounds__(256) f2d_scale32(const float2* __restrict__ x, float2* __restrict__ out,
                                                    const double* __restrict__ nrm, long long n) {
+  // the reciprocal once per block (an FP64 division per element made this kernel FP64-bound)
+  __shared__ float sa;
+  if (threadIdx.x == 0) sa = nrm[0] > 0 ? (float)(1.0 / nrm[0]) : 0.f;
+  __syncthreads();
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
   if (t >= n) return;
-  const float a = nrm[0] > 0 ? (float)(1.0 / nrm[0]) : 0.f;
+  const float a = sa;
   out[t] = make_float2(a * x[t].x, a * x[t].y);
 }
 
