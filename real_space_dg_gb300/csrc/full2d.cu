@@ -673,8 +673,11 @@ __global__ void __launch_bounds__(256) f2d_to64(const float2* __restrict__ x, do
 
 __global__ void __launch_bounds__(256) f2d_to32_scaled(const double2* __restrict__ x, float2* __restrict__ y,
                                                        const double* __restrict__ nrm, long long n) {
+  __shared__ double sa;   // the reciprocal once per block
+  if (threadIdx.x == 0) sa = nrm[0] > 0 ? 1.0 / nrm[0] : 0.0;
+  __syncthreads();
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
-  const double a = nrm[0] > 0 ? 1.0 / nrm[0] : 0.0;
+  const double a = sa;
   if (t < n) y[t] = make_float2((float)(a * x[t].x), (float)(a * x[t].y));
 }
 
