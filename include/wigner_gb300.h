@@ -356,16 +356,18 @@ int wg_server_destroy(wg_server* s);
  * No counterpart in the reference.  For callers that cannot call cudaMalloc
  * while they call in: applications that own all device memory through their
  * own allocator (a MEX gateway on gpuArray storage, a framework pool with a
- * hard budget) and code recording a CUDA graph, where allocation is not
- * allowed during stream capture.  y = A x (the FP64 operator of wg_apply) on
- * caller-owned DEVICE buffers; the library allocates nothing.  The transform
- * scratch is a fixed file-scope device array of 2^20 complex doubles (16 MiB)
- * that every GPU loading the library keeps until exit; problems with
- * n_xi*batch*n_el*n_local > 2^19 are rejected with WG_ERR_ARG.  All calls share
- * that array: calls whose kernels overlap on the GPU race and must be
- * serialised by the caller.  The first call on a device looks up the array's
- * device address; make it before any stream capture.  Kernels are enqueued on
- * `stream` (NULL: the default stream) and the call does not synchronise. */
+ * hard budget, an embedding that reserved the whole device up front), where a
+ * library allocation would fail or break the owner's accounting.  y = A x (the
+ * FP64 operator of wg_apply) on caller-owned DEVICE buffers; the library
+ * allocates nothing.  The transform scratch is a fixed file-scope device array
+ * of 2^20 complex doubles (16 MiB) that every GPU loading the library keeps
+ * until exit; problems with n_xi*batch*n_el*n_local > 2^19 are rejected with
+ * WG_ERR_ARG.  All calls share that array: calls whose kernels overlap on the
+ * GPU race and must be serialised by the caller.  The first call on a device
+ * (and the first after a device reset replaced its context) looks up the
+ * array's device address; make it before any stream capture.  Kernels are
+ * enqueued on `stream` (NULL: the default stream) and the call does not
+ * synchronise. */
 typedef struct {
   int n_el, n_local, nk, n_xi, batch;
   const double* phi;    /* device: n_xi x nk complex, row-major (xi row s, k column j), exp(i k_j xi_s)/sqrt(Ly) */
@@ -382,7 +384,8 @@ int wg_apply_noalloc(const wg_operator_view* op, const double* x, double* y, voi
  * M x N, host buffers; K >= 64 and K % 8 == 0.  No counterpart in the reference. */
 int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K);
 /* Diagnostic: C = A * B in FP64 emulated on the tensor cores (6-bit digit slices,
- * exact BF16 products, grouped FP32 accumulation, double-float recombination), the
+ * exact BF16 products, grouped FP32 accumulation, recombination in 64-bit integer
+ * fixed point, one rounding to FP64), the
  * GEMM of the mixed form's FP64 outer residual.  A row-major M x K, B column-major
  * K x N, C column-major M x N, host buffers; 64 <= K <= 1024, K % 8 == 0.  No
  * counterpart in the reference. */
@@ -400,15 +403,19 @@ int wg_apply_repeat(wg_problem* h, int which, int n, double* ms);
 
 /* Kernel-class profiler (the reference's tic/toc solveInfo timings,
  * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).
- * Classes: upwind flux, FP64 transform GEMMs, BF16 tensor-core GEMMs, xi stencil,
- * k-line preconditioner, Gram-Schmidt multi-dot, Gram-Schmidt update, small
- * Krylov kernels (reductions, normalisation, Givens), other. */
+ * Classes: upwind flux, FP64 transform GEMMs on the FP64 pipe, BF16 tensor-core
+ * GEMMs, xi stencil, k-line preconditioner, Gram-Schmidt multi-dot, Gram-Schmidt
+ * update, small Krylov kernels (reductions, normalisation, Givens), other, FP64
+ * transform GEMMs emulated on the tensor cores (digit slicing + slice products). */
 enum { WG_PROF_FLUX = 0, WG_PROF_GEMM_F64, WG_PROF_GEMM_BF16, WG_PROF_STENCIL, WG_PROF_PRECOND, WG_PROF_MULTIDOT,
-       WG_PROF_GSUPDATE, WG_PROF_KRYLOV, WG_PROF_OTHER, WG_PROF_N };
+       WG_PROF_GSUPDATE, WG_PROF_KRYLOV, WG_PROF_OTHER, WG_PROF_GEMM_F64TC, WG_PROF_N };
 int wg_profile_enable(wg_problem* h, int on);
-/* ms[i]: summed event time of class i; timed[i]: timed launches; launches[i]:
- * kernel launches of class i since the last reset (always counted); bytes[i] and
- * flops[i]: algorithmic bytes and flops of the timed launches (any may be NULL). */
+/* Arrays of WG_PROF_N entries.  ms[i]: summed event time of class i; timed[i]:
+ * timed launches; launches[i]: kernel launches of class i since the last reset
+ * (always counted); bytes[i] and flops[i]: algorithmic bytes and flops of the
+ * timed launches (any may be NULL), credited only for the problems each launch
+ * processed (launches skip converged or masked problems); for WG_PROF_GEMM_F64TC
+ * flops count the BF16 digit-slice products the chosen digit counts need. */
 int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* launches, double* bytes, double* flops,
                     int reset);
 

@@ -243,7 +243,8 @@ SIGNATURES = {
     "wg_profile_enable": ([_H, C.c_int], C.c_int),
     "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _D, _D, C.c_int], C.c_int),
 }
-PROF_CLASSES = ["flux", "gemm_f64", "gemm_bf16", "stencil", "precond", "multidot", "gs_update", "krylov_small", "other"]
+PROF_CLASSES = ["flux", "gemm_f64", "gemm_bf16", "stencil", "precond", "multidot", "gs_update", "krylov_small", "other",
+                "gemm_f64_tc"]
 
 _lib = None
 

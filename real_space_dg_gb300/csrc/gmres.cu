@@ -644,11 +644,11 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   for (int pass = 0; pass < passes; ++pass) {
     const int* mask = (pass == 0 || eta >= 1) ? P.active : P.reorth;
     tl.first = pass == 0;
-    cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B);
+    cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B, mask);
     multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, mask, N,
                                                                                       nv, mp1, ps, P.nchunk, tl);
     prof_end(P, PROF_MULTIDOT, ev);
-    ev = prof_begin(P, PROF_GSUPDATE, 1, (nv + 2) * vec, 8.0 * nv * N * B);
+    ev = prof_begin(P, PROF_GSUPDATE, 1, (nv + 2) * vec, 8.0 * nv * N * B, mask);
     if (pass == passes - 1)
       gs_update_kernel<T, 2><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
                                                              ps, P.nblk, tl);
@@ -661,7 +661,7 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
     prof_end(P, PROF_GSUPDATE, ev);
   }
   // V_{k+1} = w / |w| for the problems still iterating
-  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 1, 2 * vec);
+  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 1, 2 * vec, 0, P.active);
   if (sizeof(T) == sizeof(float2))
     scale_inv_kernel<float2, float><<<blocks_for(tot), 256, 0, P.stream>>>(
         reinterpret_cast<const float2*>(w), reinterpret_cast<float2*>(V) + (long long)(k + 1) * N, P.mx.inv,

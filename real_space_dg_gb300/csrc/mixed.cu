@@ -388,22 +388,23 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
   if (!xb) xb = M.xin16;
   const double ncols = (double)P.ncols, nxi = s.nxi, nkd = s.nk;
   const double gemm_flops = 2.0 * (2 * nxi) * (2 * nkd) * ncols;
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, (xb_out ? 20.0 : 16.0) * BN);
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, (xb_out ? 20.0 : 16.0) * BN, 0, mask);
   const dim3 fgrid((unsigned)(P.batch * s.n_el), (unsigned)((s.nk / 2 + kFlux32Threads - 1) / kFlux32Threads));
   flux32_kernel<NK><<<fgrid, kFlux32Threads, 0, P.stream>>>(x, y, xb_out, M.kvec, M.qd, M.fb, s.n_el, s.nk,
                                                             (float)P.shift, mask);
   prof_end(P, PROF_FLUX, ev);
-  ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * BN + 8.0 * nxi * ncols, gemm_flops);
+  ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * BN + 8.0 * nxi * ncols, gemm_flops, mask);
   // GEMM 1 reads its B operand through the tensor map of whichever bf16 buffer holds x
   const int cpp = s.n_el * s.nK;   // GEMM columns per problem
   cudaError_t e = launch_gemm<0>(M.tmA1, xb == M.xin16 ? M.tmB1 : M.tmB1z, reinterpret_cast<float*>(M.xh), 2 * s.nxi,
                                  P.ncols, 2 * s.nk, M.err, P.stream, mask, cpp);
   prof_end(P, PROF_GEMM_BF16, ev);
   if (e != cudaSuccess) return e;
-  ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * pair_count(NK) * M.ne4);
+  ev = prof_begin(P, PROF_STENCIL, 1, 12.0 * nxi * ncols + 4.0 * P.batch * s.n_el * pair_count(NK) * M.ne4, 0,
+                  mask);
   launch_stencil32<NK>(P, mask);
   prof_end(P, PROF_STENCIL, ev);
-  ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops);
+  ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops, mask);
   e = launch_gemm<1>(M.tmA2, M.tmB2, reinterpret_cast<float*>(y), 2 * s.nk, P.ncols, 2 * s.nxi, M.err, P.stream, mask,
                      cpp);
   prof_end(P, PROF_GEMM_BF16, ev);
@@ -418,7 +419,7 @@ cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, fl
   const dim3 block(32, kline::kChunksPerBlock);
   float* ma = static_cast<float*>(P.kmap_a);
   float2* ms = static_cast<float2*>(P.kmap_s);
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, (zb ? 28.0 : 24.0) * P.N * P.batch);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, (zb ? 28.0 : 24.0) * P.N * P.batch, 0, mask);
   kline::kline_maps_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, ma, ms,
                                                                     P.s.n_el, P.s.nk, P.N, r_stride, L, nc, mask);
   kline::kline_apply_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h,
@@ -732,8 +733,11 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   const int cpp = (int)(P.ncols / P.batch);   // columns (element, node) of one problem
   cudaError_t e = launch_flux_f64(P, x, y, mask);
   if (e != cudaSuccess) return e;
-  cudaEvent_t ev = prof_begin(P, PROF_GEMM_F64, 2, 8.0 * P.N * P.batch + 16.0 * s.nxi * ncols,
-                              8.0 * s.nxi * s.nk * ncols);
+  // work of one GEMM: read the FP64 operand (slicing), write the FP64 result; flops of
+  // ONE real-embedded BF16 digit-slice product, weighted by the products the digits need
+  const double prod_flops = 2.0 * (2.0 * s.nxi) * (2.0 * s.nk) * ncols;
+  cudaEvent_t ev = prof_begin(P, PROF_GEMM_F64TC, 2, 8.0 * P.N * P.batch + 16.0 * s.nxi * ncols, prod_flops, mask,
+                              nd, nd_pp);
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
       reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
@@ -742,7 +746,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   if (e != cudaSuccess) return e;
   e = launch_stencil_f64(P, P.xh, P.yh, mask);
   if (e != cudaSuccess) return e;
-  ev = prof_begin(P, PROF_GEMM_F64, 2, 16.0 * s.nxi * ncols + 16.0 * P.N * P.batch, 8.0 * s.nxi * s.nk * ncols);
+  ev = prof_begin(P, PROF_GEMM_F64TC, 2, 16.0 * s.nxi * ncols + 16.0 * P.N * P.batch, prod_flops, mask, nd, nd_pp);
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
       reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream,

@@ -370,14 +370,52 @@ cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2
 
 }  // namespace
 
-cudaEvent_t prof_begin(Problem& P, int cls, int n, double bytes, double flops) {
+// Fraction of the batch a masked launch processes (out[0]) and, for an emulated FP64
+// GEMM with nd > 0 digits (per problem nd_pp[b] when given), its digit-slice products
+// per problem relative to one product (out[1]); out[1] = out[0] without digits.
+__global__ void prof_count_kernel(const int* __restrict__ mask, const int* __restrict__ nd_pp, int nd, int batch,
+                                  double* __restrict__ out) {
+  double act = 0, wt = 0;
+  for (int b = threadIdx.x; b < batch; b += 32) {
+    if (mask && !mask[b]) continue;
+    act += 1.0;
+    const int d = nd_pp ? nd_pp[b] : nd;
+    wt += d > 0 ? 0.5 * d * (d + 1) : 1.0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    act += __shfl_xor_sync(0xffffffffu, act, o);
+    wt += __shfl_xor_sync(0xffffffffu, wt, o);
+  }
+  if (threadIdx.x == 0) {
+    out[0] = act / batch;
+    out[1] = wt / batch;
+  }
+}
+
+cudaEvent_t prof_begin(Problem& P, int cls, int n, double bytes, double flops, const int* mask, int nd,
+                       const int* nd_pp) {
   P.prof.launches[cls] += n;
   if (!P.prof.on) return nullptr;
+  int slot = -1;
+  if (mask || nd > 0 || nd_pp) {
+    if (!P.prof.d_frac && cudaMalloc(&P.prof.d_frac, sizeof(double) * 2 * Profiler::kProfSlots) != cudaSuccess)
+      P.prof.d_frac = nullptr;
+    if (P.prof.d_frac && (int)P.prof.pending.size() < Profiler::kProfSlots) {
+      slot = (int)P.prof.pending.size();
+      prof_count_kernel<<<1, 32, 0, P.stream>>>(mask, nd_pp, nd, P.batch, P.prof.d_frac + 2 * slot);
+    }
+  }
   P.prof.pend_bytes.push_back(bytes);
   P.prof.pend_flops.push_back(flops);
+  P.prof.pend_slot.push_back(slot);
   cudaEvent_t a;
   if (P.prof.pool.empty()) {
-    if (cudaEventCreate(&a) != cudaSuccess) return nullptr;
+    if (cudaEventCreate(&a) != cudaSuccess) {
+      P.prof.pend_bytes.pop_back();
+      P.prof.pend_flops.pop_back();
+      P.prof.pend_slot.pop_back();
+      return nullptr;
+    }
   } else {
     a = P.prof.pool.back();
     P.prof.pool.pop_back();
@@ -394,6 +432,7 @@ void prof_end(Problem& P, int cls, cudaEvent_t a) {
       P.prof.pool.push_back(a);
       P.prof.pend_bytes.pop_back();
       P.prof.pend_flops.pop_back();
+      P.prof.pend_slot.pop_back();
       return;
     }
   } else {
@@ -402,20 +441,29 @@ void prof_end(Problem& P, int cls, cudaEvent_t a) {
   }
   cudaEventRecord(b, P.stream);
   P.prof.pending.push_back({cls, a, b});
-  if (P.prof.pending.size() > 8192) prof_collect(P);
+  if (P.prof.pending.size() >= 8192) prof_collect(P);
 }
 
 cudaError_t prof_collect(Problem& P) {
   if (P.prof.pending.empty()) return cudaSuccess;
   cudaError_t e = cudaStreamSynchronize(P.stream);
+  std::vector<double> frac;
+  bool any = false;
+  for (int s : P.prof.pend_slot) any = any || s >= 0;
+  if (any && e == cudaSuccess) {
+    frac.resize(2 * P.prof.pending.size());
+    e = cudaMemcpy(frac.data(), P.prof.d_frac, sizeof(double) * frac.size(), cudaMemcpyDeviceToHost);
+  }
   for (size_t i = 0; i < P.prof.pending.size(); ++i) {
     const auto& r = P.prof.pending[i];
     float ms = 0;
     if (e == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      const int slot = P.prof.pend_slot[i];
+      const double fb = slot >= 0 ? frac[2 * slot] : 1.0, ff = slot >= 0 ? frac[2 * slot + 1] : 1.0;
       P.prof.ms[r.cls] += ms;
       P.prof.timed[r.cls] += 1;
-      P.prof.bytes[r.cls] += P.prof.pend_bytes[i];
-      P.prof.flops[r.cls] += P.prof.pend_flops[i];
+      P.prof.bytes[r.cls] += fb * P.prof.pend_bytes[i];
+      P.prof.flops[r.cls] += ff * P.prof.pend_flops[i];
     }
     P.prof.pool.push_back(r.a);
     P.prof.pool.push_back(r.b);
@@ -423,6 +471,7 @@ cudaError_t prof_collect(Problem& P) {
   P.prof.pending.clear();
   P.prof.pend_bytes.clear();
   P.prof.pend_flops.clear();
+  P.prof.pend_slot.clear();
   return e;
 }
 
@@ -430,6 +479,8 @@ void prof_release(Problem& P) {
   prof_collect(P);
   for (cudaEvent_t e : P.prof.pool) cudaEventDestroy(e);
   P.prof.pool.clear();
+  if (P.prof.d_frac) cudaFree(P.prof.d_frac);
+  P.prof.d_frac = nullptr;
 }
 
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
@@ -442,7 +493,7 @@ cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
 }
 
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int* mask) {
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * P.N * P.batch);
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * P.N * P.batch, 0, mask);
   switch (P.s.nK) {
     case 2: flux_launch<2>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
     case 3: flux_launch<3>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
@@ -455,7 +506,8 @@ cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int*
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const int* mask) {
   const int nK = P.s.nK;
   cudaEvent_t ev = prof_begin(P, PROF_STENCIL, 1,
-                              32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1));
+                              32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1), 0,
+                              mask);
   switch (nK) {
     case 2: stencil_launch<2>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
     case 3: stencil_launch<3>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
@@ -496,15 +548,15 @@ cudaError_t launch_observables(Problem& P, int b, double* n_dg, double* j) {
 // For callers that must not allocate device memory while they call in: a host
 // application that owns every device allocation through its own pool (a MATLAB
 // MEX gateway working on gpuArray storage, a framework's caching allocator with
-// a hard budget), or code recording a CUDA graph, where cudaMalloc/cudaFree are
-// not allowed inside stream capture.  The caller passes its own device buffers
-// for the operator data, x and y; the only scratch, the transformed state X^ and
-// the stencil output Y^, lives in the file-scope array below.  Its size is fixed
-// (kNoAllocScratch complex doubles, 16 MiB) and every GPU that loads the library
-// keeps it until the process exits.  All calls share it: two calls whose kernels
-// overlap on the GPU (different streams, or devices shared by threads without
-// ordering) race on it and must be serialised by the caller.  Both halves are
-// fully written before they are read in every call, so nothing is cleared.
+// a hard budget, an embedding that has reserved the whole device up front).
+// The caller passes its own device buffers for the operator data, x and y; the
+// only scratch, the transformed state X^ and the stencil output Y^, lives in the
+// file-scope array below.  Its size is fixed (kNoAllocScratch complex doubles,
+// 16 MiB) and every GPU that loads the library keeps it until the process exits.
+// All calls share it: two calls whose kernels overlap on the GPU (different
+// streams, or devices shared by threads without ordering) race on it and must be
+// serialised by the caller.  Both halves are fully written before they are read
+// in every call, so nothing is cleared.
 // ---------------------------------------------------------------------------
 constexpr long long kNoAllocScratch = 1ll << 20;      // complex doubles: two halves for X^ and Y^
 static __device__ __align__(256) double2 g_noalloc_scratch[kNoAllocScratch];
@@ -514,21 +566,53 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 double2* g_noalloc_ptr[kMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kMaxDevices] = {};   // context the cached address belongs to
+
+// Identifier of the current CUDA context (driver entry points loaded once; 0 when
+// no context is current or the driver does not offer them).  A device reset
+// (cudaDeviceReset, MATLAB's reset(gpuDevice)) destroys the primary context, and
+// the context made afterwards has a new identifier.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(p);
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext c = nullptr;
+  if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+  unsigned long long id = 0;
+  return get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
 
 // Device address of the scratch array for the current device.  The first call on
-// a device looks it up (cudaGetSymbolAddress, which does not allocate); make that
-// first call before any stream capture.
+// a device (and the first after a device reset replaced its context) looks it up
+// with cudaGetSymbolAddress, which does not allocate; make that first call before
+// any stream capture.
 cudaError_t noalloc_scratch(double2** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_noalloc_ptr[dev] || ctx == 0 || ctx != g_noalloc_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return e;
     g_noalloc_ptr[dev] = static_cast<double2*>(p);
+    g_noalloc_ctx[dev] = current_context_id();   // the lookup made the primary context current
   }
   *out = g_noalloc_ptr[dev];
   return cudaSuccess;

@@ -110,7 +110,7 @@ struct MixedBuffers {
 
 // Kernel classes timed and counted by the profiler.
 enum ProfClass { PROF_FLUX = 0, PROF_GEMM_F64, PROF_GEMM_BF16, PROF_STENCIL, PROF_PRECOND, PROF_MULTIDOT,
-                 PROF_GSUPDATE, PROF_KRYLOV, PROF_OTHER, PROF_N };
+                 PROF_GSUPDATE, PROF_KRYLOV, PROF_OTHER, PROF_GEMM_F64TC, PROF_N };
 
 // CUDA-event timing of kernel classes on the handle's stream (off by default;
 // launch counts are kept always).
@@ -128,6 +128,14 @@ struct Profiler {
   double bytes[PROF_N] = {};   // algorithmic bytes of the timed launches
   double flops[PROF_N] = {};   // algorithmic flops of the timed launches
   std::vector<double> pend_bytes, pend_flops;
+  // Work actually done by a masked launch: a one-warp kernel enqueued just before the
+  // launch's start event writes, into slot i, the fraction of the batch the launch's
+  // mask lets through and the digit-weighted fraction of an emulated FP64 GEMM (see
+  // prof_begin); the pending bytes / flops (given for the whole batch) are scaled by
+  // them when collected.  Slot -1: an unmasked launch that processes every problem.
+  std::vector<int> pend_slot;
+  double* d_frac = nullptr;    // [kProfSlots][2] on the device (allocated on first use)
+  static constexpr int kProfSlots = 8192 + 16;
 };
 
 // CUDA graphs of the Arnoldi steps: the launches of each chunk of 4 steps (k0 .. k0+3)
@@ -283,7 +291,13 @@ struct Problem {
 
 // Profiler helpers (operator.cu).  prof_begin counts `n` launches of class cls
 // and, when timing is on, records a start event; prof_end records the stop event.
-cudaEvent_t prof_begin(Problem& P, int cls, int n = 1, double bytes = 0, double flops = 0);
+// bytes / flops are the algorithmic work of the launch for all `batch` problems.
+// When the launch skips problems (mask: problems b with mask[b] == 0 do nothing) the
+// work is credited only for the problems it processes; an emulated FP64 GEMM with
+// nd > 0 leading digits (per problem nd_pp[b] when given) is credited with
+// nd (nd + 1) / 2 digit-slice products per problem, `flops` being one product.
+cudaEvent_t prof_begin(Problem& P, int cls, int n = 1, double bytes = 0, double flops = 0,
+                       const int* mask = nullptr, int nd = 0, const int* nd_pp = nullptr);
 void prof_end(Problem& P, int cls, cudaEvent_t a);
 cudaError_t prof_collect(Problem& P);
 void prof_release(Problem& P);
