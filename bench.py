@@ -188,7 +188,8 @@ def rooflines(prof, precision):
             ach, peak, bound, unit = fl / sec / 1e12, bf16, "tensor", "TFLOP/s"
             psrc = "bf16_tflops (%s); achieved counts the BF16 digit-slice products of FP64 emulated on the " \
                    "tensor cores" % src
-        elif cls == "gemm_f64":
+        elif cls in ("gemm_f64", "flux_f64", "stencil_f64") and fl > 0:
+            # FP64 arithmetic on the CUDA cores: the FP64 pipe bounds these on GB300 (1/64 of FP32)
             ach, peak, bound, unit = fl / sec / 1e12, FP64_NOMINAL_TFLOPS, "fp64", "TFLOP/s"
             psrc = "nominal GB300 FP64 %.2f TFLOP/s (no measured FP64 peak)" % FP64_NOMINAL_TFLOPS
         elif by > 0:
@@ -199,6 +200,8 @@ def rooflines(prof, precision):
              "frac": round(ach / peak, 4), "traffic": None, "peak_source": psrc,
              "avg_launch_us": round(1000.0 * ms / n_t, 2), "launches": int(n_t), "share": round(ms / total, 4),
              "per_launch": {"bytes": by / n_t, "flops": fl / n_t}}
+        if bound == "fp64" and by > 0:
+            r["hbm_frac"] = round(by / sec / 1e9 / hbm, 4)
         if ach / peak > 1.05:
             r["flag"] = ("above 1.05 of the peak: operands served from L2 (the class's working set of the "
                          "remaining active problems fits the 129 MB L2) or misattributed work; not an HBM rate")
@@ -365,9 +368,13 @@ def other_forms(args, mat, biases, opts, ours_res, ours_info):
     ms_p, info_p, res_p = _run_form(mat, batch, biases, plain_opts)
     ms_m, info_m, res_m = _run_form(mat, batch, biases, dict(fixed, precision="mixed"))
     # FP64 transport at the headline's final potential: one Gummel iteration from phi0 = that
-    # potential hands back the FP64 density and current of that potential, phi unchanged
-    one = dict(plain_opts, maxIterations=1)
-    _, _, res_t = _run_form(mat, batch, biases, one, phi0=[r[0] for r in ours_res])
+    # potential hands back the FP64 density and current of that potential, phi unchanged; solved
+    # to 1e-12 (the reference solution) and to the same 1e-8 as the headline (the plain form's own
+    # error at that residual)
+    phis = [r[0] for r in ours_res]
+    _, _, res_t = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1, transportTolerance=1e-12,
+                                                     transportMaxCycles=200), phi0=phis)
+    _, _, res_t8 = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1), phi0=phis)
 
     def arm(ms, info, form):
         conv = sum(i["status"] == 0 for i in info)
@@ -384,9 +391,12 @@ def other_forms(args, mat, biases, opts, ours_res, ours_info):
     acc = {"reference": "plain FP64 GPU form (above), same biases",
            "headline_vs_plain_fixed_point": _compare(ours_res, res_p),
            "mixed_exact_vs_plain_fixed_point": _compare(res_m, res_p),
-           "headline_transport_vs_fp64_at_same_potential": _compare(ours_res, res_t),
+           "headline_transport_vs_fp64_1e-12_at_same_potential": _compare(ours_res, res_t),
+           "plain_fp64_1e-8_transport_vs_fp64_1e-12_at_same_potential": _compare(res_t8, res_t),
            "targets": {"terminal_current_rel_transport": 1e-7,
-                       "fixed_point": "set by the Gummel potential tolerance 1e-6 V, the same for both loops"}}
+                       "fixed_point": "set by the Gummel potential tolerance 1e-6 V, the same for both loops",
+                       "note": "a 1e-8 relative residual bounds the current error only to ~cond * 1e-8; the plain "
+                               "FP64 form at 1e-8 is listed beside the headline for that reason"}}
     return plain, mixed_exact, acc
 
 

@@ -167,6 +167,12 @@ int wg_get_rho(wg_problem* h, int b, double* rho);
  * n_dg = Re of the centre-xi value of Phi*rho, j = q hbar/m Im(d rho_u/d xi)
  * (solve_transport_DG_2D.m:114-156). */
 int wg_get_observables(wg_problem* h, int b, double* n_dg, double* j);
+/* Overwrite problem b's resident Wigner function (N complex values, the rho of
+ * wg_get_rho; the INIT.rho of solve_transport_DG_2D_transient_SC_new.m:22) or its
+ * right-hand side (INIT.rhs, :21).  A later wg_set_potential or operator refresh
+ * rebuilds the right-hand side unless the transient keeps it (fixed_rhs). */
+int wg_set_rho(wg_problem* h, int b, const double* rho);
+int wg_set_rhs(wg_problem* h, int b, const double* rhs);
 
 /* Problem b's Wigner function on the xi grid, rho_u = Phi * rho per DG node
  * (solve_transport_DG_2D.m:118, DG.RHO(IV,IM,:,:)): n_el*n_local rows of
@@ -263,6 +269,8 @@ typedef struct {
   double tol;           /* Crank-Nicolson GMRES relative residual per step; 0 -> 1e-10 */
   int maxit;            /* restart cycles per step; 0 -> 20 */
   int record_every;     /* store n and j after every record_every-th step; 0: none */
+  int fixed_rhs;        /* 1: keep the resident right-hand side (the reference's rhs_INIT, never refreshed,
+                           :153-156) and rebuild only the operator at a refresh; 0: rebuild both */
 } wg_transient_opts;
 
 typedef struct {
@@ -403,12 +411,14 @@ int wg_apply_repeat(wg_problem* h, int which, int n, double* ms);
 
 /* Kernel-class profiler (the reference's tic/toc solveInfo timings,
  * solve_transport_DG_full2D.m:182-233, as CUDA events on the handle's stream).
- * Classes: upwind flux, FP64 transform GEMMs on the FP64 pipe, BF16 tensor-core
- * GEMMs, xi stencil, k-line preconditioner, Gram-Schmidt multi-dot, Gram-Schmidt
- * update, small Krylov kernels (reductions, normalisation, Givens), other, FP64
- * transform GEMMs emulated on the tensor cores (digit slicing + slice products). */
+ * Classes: FP32 upwind flux (mixed form), FP64 transform GEMMs on the FP64 pipe,
+ * BF16 tensor-core GEMMs, FP32 xi stencil, k-line preconditioner, Gram-Schmidt
+ * multi-dot, Gram-Schmidt update, small Krylov kernels (reductions, normalisation,
+ * Givens), other, FP64 transform GEMMs emulated on the tensor cores (digit slicing +
+ * slice products), FP64 upwind flux, FP64 xi stencil. */
 enum { WG_PROF_FLUX = 0, WG_PROF_GEMM_F64, WG_PROF_GEMM_BF16, WG_PROF_STENCIL, WG_PROF_PRECOND, WG_PROF_MULTIDOT,
-       WG_PROF_GSUPDATE, WG_PROF_KRYLOV, WG_PROF_OTHER, WG_PROF_GEMM_F64TC, WG_PROF_N };
+       WG_PROF_GSUPDATE, WG_PROF_KRYLOV, WG_PROF_OTHER, WG_PROF_GEMM_F64TC, WG_PROF_FLUX64, WG_PROF_STENCIL64,
+       WG_PROF_N };
 int wg_profile_enable(wg_problem* h, int on);
 /* Arrays of WG_PROF_N entries.  ms[i]: summed event time of class i; timed[i]:
  * timed launches; launches[i]: kernel launches of class i since the last reset
@@ -489,7 +499,8 @@ int wg2d_set_preconditioner(wg2d_problem* h, const double* U, double sigma, cons
                             const double* x_coupling, const int* forward, const double* t_inverse, int fp32);
 int wg2d_precondition(wg2d_problem* h, const double* r, double* z);
 
-/* A rho = rhs by restarted GMRES(restart), right-preconditioned, to tol relative to |rhs|, at most
+/* A rho = rhs by restarted GMRES(restart), right-preconditioned (the identity when no preconditioner
+ * was set; the mixed form needs the FP32 preconditioner), to tol relative to |rhs|, at most
  * maxit restart cycles (solveStationarySystem / runGmresWithProgress,
  * solve_transport_DG_full2D.m:132-346, 422-506).  x: the warm start when use_x0 (a correction about
  * x0, the tolerance still relative to |rhs|), the solution on return.  WG_NOT_CONVERGED is a status. */
@@ -511,6 +522,50 @@ typedef struct {
   double rhs_norm;
 } wg2d_solve_info;
 int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts, wg2d_solve_info* info);
+/* Resident forms of wg2d_solve (the device keeps the right-hand side and the solution between calls, as
+ * the reference keeps DG.rho for the next warm start, solve2D_rtd_self_consistent.m:185,204): rhs = NULL
+ * reuses the right-hand side of the previous solve; x = NULL takes the warm start (when use_x0) from the
+ * resident solution and leaves the result on the device only.  wg2d_get_state copies the resident
+ * solution out (n complex values). */
+int wg2d_get_state(wg2d_problem* h, double* x);
+/* A rho = rhs by preconditioned BiCGSTAB (the full2D_solver = 'bicgstab' branch of solveStationarySystem,
+ * solve_transport_DG_full2D.m:248-272: MATLAB's bicgstab with the preconditioner as M), with the
+ * line-transverse preconditioner when one is set and none otherwise.  opts: tol (relative to |rhs|),
+ * maxit (full iterations), use_x0; restart, mixed and inner_tol are ignored.  rhs / x = NULL as for
+ * wg2d_solve.  info: flag from the final true residual, relres, iterations (full iterations begun),
+ * cycles (half steps done; MATLAB's iter = cycles / 2); wg2d_solve_resvec gives the initial residual
+ * and the norm after every half step.  WG_NOT_CONVERGED (also after a breakdown) is a status. */
+int wg2d_solve_bicgstab(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts,
+                        wg2d_solve_info* info);
+/* Residual history of the last solve (DG.info.solve.resvec of solveStationarySystem,
+ * solve_transport_DG_full2D.m:317-326): the initial true residual norm, then the GMRES estimate
+ * |b - A x_j| after every inner iteration (absolute, in the units of rhs).  Copies
+ * min(cap, count) values to out (out may be NULL) and the count to *count. */
+int wg2d_solve_resvec(wg2d_problem* h, double* out, int cap, int* count);
+
+/* Observables at zero relative separation on the device (get_Observables_full2D.m:19-79):
+ * nDG = real rho(0,0,X,Y), jxDG = scale_x imag(d rho/d rho_x)(0,0,X,Y), jyDG = scale_y
+ * imag(d rho/d rho_y)(0,0,X,Y); n, jx, jy their projections onto the material Y grid (duplicate DG Y
+ * nodes averaged, linear interpolation with extrapolation); j = jx integrated over Y (trapezoid).
+ * The zero of an axis is one cell (weight 1) or two bracketing cells (linear weights), its derivative
+ * row at most 8 nonzeros (zeroInterpolationWeights / derivativeRowAtZero of the same file). */
+typedef struct {
+  int n_zero_x, n_zero_y;          /* 1 or 2 */
+  int zero_x[2], zero_y[2];        /* rho_x / rho_y cell indices (0-based) */
+  double w_zero_x[2], w_zero_y[2];
+  int n_dx, n_dy;                  /* nonzeros of the derivative rows, <= 8 */
+  int dx_idx[8], dy_idx[8];
+  double dx_val[8], dy_val[8];     /* [1/m] */
+  double scale_x, scale_y;         /* q hbar / m_x, q hbar / m_y */
+  int n_target_y;                  /* material Y points */
+} wg2d_observables_desc;
+/* W: [n_target_y][nY] projection weights from the DG Y dofs to the material Y points; wj: [n_target_y]
+ * integration weights over them.  Kept by the handle. */
+int wg2d_set_observables(wg2d_problem* h, const wg2d_observables_desc* d, const double* W, const double* wj);
+/* rho: a host state (n complex values) or NULL for the resident solution.  Outputs (any may be NULL),
+ * row-major with X (the DG X dof) slowest: nDG, jxDG, jyDG [nX][nY]; n, jx, jy [nX][n_target_y]; j [nX]. */
+int wg2d_observables(wg2d_problem* h, const double* rho, double* nDG, double* jxDG, double* jyDG, double* n,
+                     double* jx, double* jy, double* j);
 /* Diagnostic: n applies to the resident device state; mean time of one apply in *ms, with the time
  * of its transport and potential kernels in parts_ms[0..1] (may be NULL). */
 int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms);

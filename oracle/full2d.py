@@ -604,3 +604,24 @@ def observables(p, mat, rho):
     jx = _project_to_y(jxDG, ydg, target)
     trapz = getattr(np, "trapezoid", None) or np.trapz
     return n, trapz(jx, target, axis=1), nDG, jxDG
+
+
+def observables_y(p, mat, rho):
+    """(jy [X nDof x material Ny], jyDG) (get_Observables_full2D.m:47-58): the rho_y derivative at
+    zero relative separation, rho_x interpolated to zero, scaled by q hbar / m_y
+    (me_y_ch, default me_x_ch), projected onto the material Y grid."""
+    nrx, nry = p["rhoX"]["nCells"], p["rhoY"]["nCells"]
+    nX, nY = p["X"]["nDof"], p["Y"]["nDof"]
+    by_center = np.asarray(rho).ravel().reshape(nX * nY, nrx * nry).T
+    ix_ids, ix_w = _zero_weights(p["rhoX"]["cells"])
+    rowy = _derivative_row(p["rhoY"]["cells"], p["rhoY"]["D"])
+    dy = np.zeros(nX * nY, dtype=complex)
+    for a, wa in zip(ix_ids, ix_w):
+        rel_ids = a + np.arange(nry) * nrx
+        dy += wa * (rowy @ by_center[rel_ids, :])
+    mey = mat.get("me_y_ch", mat.get("me_x_ch", 0.041))
+    mkg = mey * M0 if abs(mey) > 1e-25 else mey
+    mkg = mkg if mkg > 0 else 0.041 * M0
+    jyDG = QE * HBAR / mkg * np.imag(dy.reshape(nX, nY, order="F"))
+    target = np.asarray(mat["y"], dtype=float) * p["coordinateScale"]
+    return _project_to_y(jyDG, p["Y"]["nodes"], target), jyDG

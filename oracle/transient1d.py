@@ -64,8 +64,10 @@ def linear_poisson(tri, n_cv, nd, bias):
 
 
 def transient(mat, rho0, phi0, bias, dt, nsteps, *, dy_nm, ef_offset=0.05, method="cn", scale_a=1.0,
-              scale_rhs=1.0, refresh_every=20, refresh_first=50, record_every=1):
-    """Bias-step transient from the state (rho0, phi0) to `bias` at t = 0.
+              scale_rhs=1.0, refresh_every=20, refresh_first=50, record_every=1, fixed_rhs=None):
+    """Bias-step transient from the state (rho0, phi0) to `bias` at t = 0.  fixed_rhs: the
+    reference's INIT.rhs, used at every step instead of the inflow of the rebuilt operator
+    (solve_transport_DG_2D_transient_SC_new.m:21, 153-156).
 
     Returns dict(n=[nrec, ncol], j=[nrec, ncol], phi, rho, steps)."""
     vc = np.asarray(mat["Vc"], dtype=float)
@@ -98,6 +100,8 @@ def transient(mat, rho0, phi0, bias, dt, nsteps, *, dy_nm, ef_offset=0.05, metho
     for t in range(1, nsteps + 1):
         if t == 1 or (refresh_every > 0 and ((t - 1) % refresh_every == 0 or t < refresh_first)):
             p, A, rhs = build(phi)
+            if fixed_rhs is not None:
+                rhs = np.asarray(fixed_rhs, dtype=complex)
             lu = None
         if method == "rk4":
             rho = rk4_step(A, rhs, rho, dt, scale_a, scale_rhs)

@@ -74,7 +74,7 @@ GUMMEL_STATUS = {0: "fixed-point-converged", 1: "iteration-limit", 2: "transport
 class WgTransientOpts(C.Structure):
     _fields_ = [("dt", C.c_double), ("nsteps", C.c_int), ("method", C.c_int), ("scale_a", C.c_double),
                 ("scale_rhs", C.c_double), ("refresh_every", C.c_int), ("refresh_first", C.c_int),
-                ("tol", C.c_double), ("maxit", C.c_int), ("record_every", C.c_int)]
+                ("tol", C.c_double), ("maxit", C.c_int), ("record_every", C.c_int), ("fixed_rhs", C.c_int)]
 
 
 class WgTransientInfo(C.Structure):
@@ -134,6 +134,14 @@ class Wg2dSolveOpts(C.Structure):
                 ("mixed", C.c_int), ("inner_tol", C.c_double)]
 
 
+class Wg2dObservablesDesc(C.Structure):
+    _fields_ = [("n_zero_x", C.c_int), ("n_zero_y", C.c_int), ("zero_x", C.c_int * 2), ("zero_y", C.c_int * 2),
+                ("w_zero_x", C.c_double * 2), ("w_zero_y", C.c_double * 2), ("n_dx", C.c_int), ("n_dy", C.c_int),
+                ("dx_idx", C.c_int * 8), ("dy_idx", C.c_int * 8), ("dx_val", C.c_double * 8),
+                ("dy_val", C.c_double * 8), ("scale_x", C.c_double), ("scale_y", C.c_double),
+                ("n_target_y", C.c_int)]
+
+
 class Wg2dSolveInfo(C.Structure):
     _fields_ = [("flag", C.c_int), ("iterations", C.c_int), ("cycles", C.c_int), ("relres", C.c_double),
                 ("initial_relres", C.c_double), ("rhs_norm", C.c_double)]
@@ -189,6 +197,11 @@ SIGNATURES = {
     "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D, C.c_int], C.c_int),
     "wg2d_precondition": ([_H, _D, _D], C.c_int),
     "wg2d_solve": ([_H, _D, _D, C.POINTER(Wg2dSolveOpts), C.POINTER(Wg2dSolveInfo)], C.c_int),
+    "wg2d_get_state": ([_H, _D], C.c_int),
+    "wg2d_solve_bicgstab": ([_H, _D, _D, C.POINTER(Wg2dSolveOpts), C.POINTER(Wg2dSolveInfo)], C.c_int),
+    "wg2d_solve_resvec": ([_H, _D, C.c_int, C.POINTER(C.c_int)], C.c_int),
+    "wg2d_set_observables": ([_H, C.POINTER(Wg2dObservablesDesc), _D, _D], C.c_int),
+    "wg2d_observables": ([_H, _D, _D, _D, _D, _D, _D, _D, _D], C.c_int),
     "wg_poisson2d_create": ([C.POINTER(WgPoisson2dDesc), _D, C.POINTER(C.c_ubyte), _D, _D, C.POINTER(_H)], C.c_int),
     "wg_poisson2d_destroy": ([_H], C.c_int),
     "wg_poisson2d_last_error": ([_H], C.c_char_p),
@@ -214,6 +227,8 @@ SIGNATURES = {
     "wg_set_potential": ([_H, C.c_int, C.POINTER(WgDevice), _D, C.c_double, C.c_double], C.c_int),
     "wg_solve": ([_H, C.POINTER(WgSolveOpts), _D, C.POINTER(WgSolveInfo)], C.c_int),
     "wg_get_rho": ([_H, C.c_int, _D], C.c_int),
+    "wg_set_rho": ([_H, C.c_int, _D], C.c_int),
+    "wg_set_rhs": ([_H, C.c_int, _D], C.c_int),
     "wg_get_observables": ([_H, C.c_int, _D, _D], C.c_int),
     "wg_get_rho_xi": ([_H, C.c_int, _D], C.c_int),
     "wg_apply": ([_H, _D, _D], C.c_int),
@@ -244,7 +259,7 @@ SIGNATURES = {
     "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _D, _D, C.c_int], C.c_int),
 }
 PROF_CLASSES = ["flux", "gemm_f64", "gemm_bf16", "stencil", "precond", "multidot", "gs_update", "krylov_small", "other",
-                "gemm_f64_tc"]
+                "gemm_f64_tc", "flux_f64", "stencil_f64"]
 
 _lib = None
 
@@ -252,9 +267,9 @@ _lib = None
 class WignerError(RuntimeError):
     """Raised for every non-OK status except WG_NOT_CONVERGED (which is a status)."""
 
-    def __init__(self, status, message):
+    def __init__(self, status, message, identifier=None):
         self.status = status
-        self.identifier = ERROR_IDS.get(status, "DG:Full2D:Error")
+        self.identifier = identifier or ERROR_IDS.get(status, "DG:Full2D:Error")
         super().__init__("%s (%s): %s" % (self.identifier, STATUS_NAMES.get(status, status), message))
 
 

@@ -515,6 +515,25 @@ int wg_get_rho(wg_problem* h, int b, double* rho) {
   return WG_OK;
 }
 
+int wg_set_rho(wg_problem* h, int b, const double* rho) {
+  if (!h || !rho) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_set_rho: null argument");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_set_rho: batch index out of range");
+  API_CK(&P, cudaMemcpyAsync(P.x + (long long)b * P.N, rho, sizeof(double2) * P.N, cudaMemcpyHostToDevice, P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
+int wg_set_rhs(wg_problem* h, int b, const double* rhs) {
+  if (!h || !rhs) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_set_rhs: null argument");
+  wg::Problem& P = h->P;
+  if (b < 0 || b >= P.batch) return fail(&P, WG_ERR_ARG, "wg_set_rhs: batch index out of range");
+  API_CK(&P, cudaMemcpyAsync(P.rhs + (long long)b * P.N, rhs, sizeof(double2) * P.N, cudaMemcpyHostToDevice,
+                             P.stream));
+  API_CK(&P, cudaStreamSynchronize(P.stream));
+  return WG_OK;
+}
+
 int wg_get_observables(wg_problem* h, int b, double* n_dg, double* j) {
   if (!h || !n_dg || !j) return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_get_observables: null argument");
   wg::Problem& P = h->P;

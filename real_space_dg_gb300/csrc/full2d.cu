@@ -95,6 +95,16 @@ struct wg2d_problem {
   double2 *V = nullptr, *r = nullptr, *w = nullptr, *z = nullptr, *b = nullptr, *xs = nullptr;
   double2 *H = nullptr, *g = nullptr, *sn = nullptr, *hc = nullptr, *hp = nullptr, *yc = nullptr;
   double *cs = nullptr, *partial = nullptr, *nrm = nullptr;
+  double2 *bc_rt = nullptr, *bc_p = nullptr, *bc_ph = nullptr, *bc_sh = nullptr;   // BiCGSTAB vectors
+  bool b_ready = false, xs_ready = false;   // resident right-hand side / solution of the last solve
+  std::vector<double> resvec;               // residual norms of the last solve (initial, then per iteration)
+  // observables at zero relative separation (get_Observables_full2D.m): the zero-cell weights and
+  // derivative rows, the projection onto the material Y grid and the trapezoid weights over it
+  wg2d_observables_desc obs{};
+  bool obs_ready = false;
+  double* obs_W = nullptr;    // [nty][nY]
+  double* obs_wj = nullptr;   // [nty]
+  double* obs_out = nullptr;  // nDG, jxDG, jyDG [nX][nY]; n, jx, jy [nX][nty]; j [nX]
   std::string err;
 };
 
@@ -869,6 +879,26 @@ __global__ void __launch_bounds__(256) f2d_sub(const double2* __restrict__ b, do
   y[t] = make_double2(b[t].x - y[t].x, b[t].y - y[t].y);
 }
 
+// BiCGSTAB vector updates (complex scalars by value): p = r + beta (p - omega v); y += a x; y -= a x
+__global__ void __launch_bounds__(256) f2d_bicg_p(double2* __restrict__ p, const double2* __restrict__ r,
+                                                  const double2* __restrict__ v, double2 beta, double2 omega,
+                                                  long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  const double2 pv = p[t], vv = v[t], rv = r[t];
+  const double2 d = make_double2(pv.x - (omega.x * vv.x - omega.y * vv.y), pv.y - (omega.x * vv.y + omega.y * vv.x));
+  p[t] = make_double2(rv.x + beta.x * d.x - beta.y * d.y, rv.y + beta.x * d.y + beta.y * d.x);
+}
+
+__global__ void __launch_bounds__(256) f2d_caxpy(double2* __restrict__ y, const double2* __restrict__ x, double2 a,
+                                                 long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  const double2 xv = x[t];
+  y[t].x += a.x * xv.x - a.y * xv.y;
+  y[t].y += a.x * xv.y + a.y * xv.x;
+}
+
 // |x|^2 of the dot result (real part) -> nrm[0] = sqrt
 __global__ void f2d_sqrt_real(const double2* __restrict__ d, double* __restrict__ nrm) {
   nrm[0] = sqrt(fmax(d[0].x, 0.0));
@@ -1083,6 +1113,69 @@ bool supported_nloc(int n) { return n == 4 || n == 6 || n == 8 || n == 9 || n ==
 
 }  // namespace
 
+namespace {
+
+// Observables at zero relative separation (get_Observables_full2D.m:19-79), one thread per DG X dof:
+// the DG values over the Y dofs, then their projection onto the material Y points and the integral.
+__global__ void __launch_bounds__(128) f2d_observables_kernel(const double2* __restrict__ F, wg2d_observables_desc d,
+                                                              const double* __restrict__ W,
+                                                              const double* __restrict__ wj, int nX, int nY, int nrx,
+                                                              int nry, double* __restrict__ out) {
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= nX) return;
+  const int nty = d.n_target_y;
+  double* nDG = out;
+  double* jxDG = out + (size_t)nX * nY;
+  double* jyDG = out + (size_t)2 * nX * nY;
+  double* n = out + (size_t)3 * nX * nY;
+  double* jx = n + (size_t)nX * nty;
+  double* jy = n + (size_t)2 * nX * nty;
+  double* j = n + (size_t)3 * nX * nty;
+  const long long nrel = (long long)nrx * nry;
+  for (int yd = 0; yd < nY; ++yd) {
+    const double2* c = F + ((long long)yd * nX + X) * nrel;
+    double at0 = 0.0;
+    double2 dx = make_double2(0.0, 0.0), dy = make_double2(0.0, 0.0);
+    for (int a = 0; a < d.n_zero_y; ++a) {
+      const double2* row = c + (long long)d.zero_y[a] * nrx;
+      for (int b = 0; b < d.n_zero_x; ++b) at0 += d.w_zero_y[a] * d.w_zero_x[b] * row[d.zero_x[b]].x;
+      for (int q = 0; q < d.n_dx; ++q) {
+        const double w = d.w_zero_y[a] * d.dx_val[q];
+        const double2 v = row[d.dx_idx[q]];
+        dx.x += w * v.x;
+        dx.y += w * v.y;
+      }
+    }
+    for (int b = 0; b < d.n_zero_x; ++b)
+      for (int q = 0; q < d.n_dy; ++q) {
+        const double w = d.w_zero_x[b] * d.dy_val[q];
+        const double2 v = c[(long long)d.dy_idx[q] * nrx + d.zero_x[b]];
+        dy.x += w * v.x;
+        dy.y += w * v.y;
+      }
+    nDG[(size_t)X * nY + yd] = at0;
+    jxDG[(size_t)X * nY + yd] = d.scale_x * dx.y;
+    jyDG[(size_t)X * nY + yd] = d.scale_y * dy.y;
+  }
+  double jsum = 0.0;
+  for (int t = 0; t < nty; ++t) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int yd = 0; yd < nY; ++yd) {
+      const double w = W[(size_t)t * nY + yd];
+      s0 += w * nDG[(size_t)X * nY + yd];
+      s1 += w * jxDG[(size_t)X * nY + yd];
+      s2 += w * jyDG[(size_t)X * nY + yd];
+    }
+    n[(size_t)X * nty + t] = s0;
+    jx[(size_t)X * nty + t] = s1;
+    jy[(size_t)X * nty + t] = s2;
+    jsum += wj[t] * s1;
+  }
+  j[X] = jsum;
+}
+
+}  // namespace
+
 extern "C" {
 
 static void free_solver(wg2d_problem* h);
@@ -1147,7 +1240,7 @@ int wg2d_destroy(wg2d_problem* h) {
   free32(h);
   wg::ozaki_free(h->cols);
   void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap,
-                  h->tc_err};
+                  h->tc_err, h->obs_W, h->obs_wj, h->obs_out};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t ev : h->ev)
@@ -1407,9 +1500,10 @@ static void vnorm32(wg2d_problem* h, const float2* w) {
 
 static void free_solver(wg2d_problem* h) {
   void* ptrs[] = {h->V, h->Zb, h->r, h->w, h->z, h->b, h->xs, h->H, h->g, h->sn, h->hc, h->hp, h->yc, h->cs,
-                  h->partial, h->nrm};
+                  h->partial, h->nrm, h->bc_rt, h->bc_p, h->bc_ph, h->bc_sh};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  h->bc_rt = h->bc_p = h->bc_ph = h->bc_sh = nullptr;
   h->V = h->Zb = h->r = h->w = h->z = h->b = h->xs = h->H = h->g = h->sn = h->hc = h->hp = h->yc = nullptr;
   h->cs = h->partial = h->nrm = nullptr;
   h->vm = 0;
@@ -1696,10 +1790,19 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
   const int maxit = opts->maxit > 0 ? opts->maxit : 50;
   const double tol = opts->tol > 0 ? opts->tol : 1e-8;
   if (m > 256) return fail(h, WG_ERR_ARG, "wg2d_solve: restart at most 256");
-  if (!h->pre_ready || !h->potential_ready) return fail(h, WG_ERR_ARG, "wg2d_solve: set potential and preconditioner first");
+  if (!h->potential_ready) return fail(h, WG_ERR_ARG, "wg2d_solve: set the potential first");
   const long long n = h->n;
+  if (!rhs && !h->b_ready) return fail(h, WG_ERR_ARG, "wg2d_solve: rhs = NULL needs the right-hand side of a previous solve");
+  if (!x && opts->use_x0 && !h->xs_ready)
+    return fail(h, WG_ERR_ARG, "wg2d_solve: x = NULL with use_x0 needs the resident solution of a previous solve");
   if (h->vm < m + 1) {
+    // the right-hand side and the solution stay resident across a change of the restart length
+    double2* keep_b = h->b;
+    double2* keep_xs = h->xs;
+    h->b = h->xs = nullptr;
     free_solver(h);
+    h->b = keep_b;
+    h->xs = keep_xs;
     const size_t need = (size_t)(2 * m + 1) * n * sizeof(double2);
     size_t freeb = 0, total = 0;
     cudaMemGetInfo(&freeb, &total);
@@ -1709,8 +1812,8 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     F2_CK(dalloc(&h->r, n));
     F2_CK(dalloc(&h->w, n));
     F2_CK(dalloc(&h->z, n));
-    F2_CK(dalloc(&h->b, n));
-    F2_CK(dalloc(&h->xs, n));
+    if (!h->b) F2_CK(dalloc(&h->b, n));
+    if (!h->xs) F2_CK(dalloc(&h->xs, n));
     F2_CK(dalloc(&h->H, (size_t)(m + 1) * m));
     F2_CK(dalloc(&h->g, m + 1));
     F2_CK(dalloc(&h->sn, m));
@@ -1723,9 +1826,18 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     h->vm = m + 1;
   }
   std::memset(info, 0, sizeof(*info));
-  F2_CK(cudaMemcpyAsync(h->b, rhs, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
-  if (opts->use_x0) F2_CK(cudaMemcpyAsync(h->xs, x, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
-  else F2_CK(cudaMemsetAsync(h->xs, 0, sizeof(double2) * n, h->stream));
+  h->resvec.clear();
+  if (rhs) {
+    h->b_ready = false;
+    F2_CK(cudaMemcpyAsync(h->b, rhs, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+    h->b_ready = true;
+  }
+  h->xs_ready = false;
+  if (opts->use_x0) {
+    if (x) F2_CK(cudaMemcpyAsync(h->xs, x, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  } else {
+    F2_CK(cudaMemsetAsync(h->xs, 0, sizeof(double2) * n, h->stream));
+  }
   double bnorm = 0, beta = 0;
   vnorm(h, h->b);
   F2_CK(cudaMemcpyAsync(&bnorm, h->nrm, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -1740,6 +1852,7 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
   };
   int rc = true_residual();
   if (rc) return rc;
+  h->resvec.push_back(beta);
   info->rhs_norm = bnorm;
   const double bn = bnorm > 0 ? bnorm : 1.0;
   info->initial_relres = beta / bn;
@@ -1802,6 +1915,7 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
         F2_CK(cudaStreamSynchronize(h->stream));
         k = j + 1;
         info->iterations += 1;
+        h->resvec.push_back(beta * std::hypot(gj.x, gj.y));
         if (!(std::hypot(gj.x, gj.y) > itgt)) break;
       }
       f2d_backsolve<<<1, 1, 0, h->stream>>>(h->H, h->g, h->yc, k, ldh);
@@ -1821,7 +1935,8 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     for (int j = 0; j < m; ++j) {
       double2* Vj = h->V + (long long)j * n;
       double2* Zj = h->Zb + (long long)j * n;      // flexible GMRES: keep z_j = M^-1 v_j
-      rc = precondition_device(h, Vj, Zj);
+      if (h->pre_ready) rc = precondition_device(h, Vj, Zj);      // no preconditioner set: identity
+      else F2_CK(cudaMemcpyAsync(Zj, Vj, sizeof(double2) * n, cudaMemcpyDeviceToDevice, h->stream));
       if (!rc) rc = apply_op(h, Zj, h->w);
       if (rc) return rc;
       // classical Gram-Schmidt; a second pass only when the first lost more than half of |w|^2
@@ -1851,6 +1966,7 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
       k = j + 1;
       info->iterations += 1;
       const double est = std::hypot(gj.x, gj.y);
+      h->resvec.push_back(est);
       if (!(est > target)) break;
     }
     f2d_backsolve<<<1, 1, 0, h->stream>>>(h->H, h->g, h->yc, k, ldh);
@@ -1861,14 +1977,229 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     if (rc) return rc;
   }
   int flag = 0;
-  F2_CK(cudaMemcpyAsync(x, h->xs, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
+  if (x) F2_CK(cudaMemcpyAsync(x, h->xs, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
   F2_CK(cudaMemcpyAsync(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   F2_CK(cudaStreamSynchronize(h->stream));
   if (flag) return fail(h, WG_ERR_TIMEOUT, "tensor-core GEMM: bounded barrier wait timed out");
+  h->xs_ready = true;
   info->relres = beta / bn;
   if (!std::isfinite(beta)) return fail(h, WG_ERR_NUMERIC, "wg2d_solve: non-finite residual");
   info->flag = beta <= target ? 0 : 1;
   return info->flag ? WG_NOT_CONVERGED : WG_OK;
+}
+
+// Preconditioned BiCGSTAB (van der Vorst), right-preconditioned as MATLAB's bicgstab(A, b, tol, maxit, M)
+// that runBicgstabWithProgress calls (solve_transport_DG_full2D.m:248-272, 367-420): M^-1 is the
+// line-transverse preconditioner when one is set, the identity otherwise.  maxit counts full iterations;
+// convergence is tested after each half step on |s| and |r| against tol |b|, and the final true residual
+// b - A x decides the flag.  info->cycles: half steps done (MATLAB's iter = cycles / 2); info->iterations:
+// full iterations begun.  The resvec holds the initial residual and the norm after every half step.
+int wg2d_solve_bicgstab(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts,
+                        wg2d_solve_info* info) {
+  if (!h) return WG_ERR_ARG;
+  if (!opts || !info) return fail(h, WG_ERR_ARG, "wg2d_solve_bicgstab: null argument");
+  if (!h->potential_ready) return fail(h, WG_ERR_ARG, "wg2d_solve_bicgstab: set the potential first");
+  const int maxit = opts->maxit > 0 ? opts->maxit : 50;
+  const double tol = opts->tol > 0 ? opts->tol : 1e-8;
+  const long long n = h->n;
+  if (!rhs && !h->b_ready) return fail(h, WG_ERR_ARG, "wg2d_solve_bicgstab: rhs = NULL needs a previous right-hand side");
+  if (!x && opts->use_x0 && !h->xs_ready)
+    return fail(h, WG_ERR_ARG, "wg2d_solve_bicgstab: x = NULL with use_x0 needs a resident solution");
+  {
+    size_t freeb = 0, total = 0;
+    cudaMemGetInfo(&freeb, &total);
+    int missing = 0;
+    for (double2* p : {h->r, h->w, h->z, h->b, h->xs, h->bc_rt, h->bc_p, h->bc_ph, h->bc_sh}) missing += p ? 0 : 1;
+    if ((size_t)missing * n * sizeof(double2) > freeb)
+      return fail(h, WG_ERR_OOM, "wg2d_solve_bicgstab: BiCGSTAB vectors do not fit");
+  }
+  for (double2** p : {&h->r, &h->w, &h->z, &h->b, &h->xs, &h->bc_rt, &h->bc_p, &h->bc_ph, &h->bc_sh})
+    if (!*p) F2_CK(dalloc(p, n));
+  if (!h->hc) F2_CK(dalloc(&h->hc, 2));
+  if (!h->hp) F2_CK(dalloc(&h->hp, 2));
+  if (!h->partial) F2_CK(dalloc(&h->partial, (size_t)2 * kDotBlocks * 2));
+  if (!h->nrm) F2_CK(dalloc(&h->nrm, 1));
+  std::memset(info, 0, sizeof(*info));
+  h->resvec.clear();
+  if (rhs) {
+    h->b_ready = false;
+    F2_CK(cudaMemcpyAsync(h->b, rhs, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+    h->b_ready = true;
+  }
+  h->xs_ready = false;
+  if (opts->use_x0) {
+    if (x) F2_CK(cudaMemcpyAsync(h->xs, x, sizeof(double2) * n, cudaMemcpyHostToDevice, h->stream));
+  } else {
+    F2_CK(cudaMemsetAsync(h->xs, 0, sizeof(double2) * n, h->stream));
+  }
+  const unsigned nb = blocks256(n);
+  auto read_dot = [&](const double2* a, const double2* b, double2* out) -> int {
+    dots(h, a, 1, b, h->hc, 0);
+    F2_CK(cudaMemcpyAsync(out, h->hc, sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
+    F2_CK(cudaStreamSynchronize(h->stream));
+    return WG_OK;
+  };
+  auto norm_of = [&](const double2* v, double* out) -> int {
+    vnorm(h, v);
+    F2_CK(cudaMemcpyAsync(out, h->nrm, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    F2_CK(cudaStreamSynchronize(h->stream));
+    return WG_OK;
+  };
+  auto prec = [&](const double2* in, double2* out) -> int {
+    if (h->pre_ready) return precondition_device(h, in, out);
+    F2_CK(cudaMemcpyAsync(out, in, sizeof(double2) * n, cudaMemcpyDeviceToDevice, h->stream));
+    return WG_OK;
+  };
+  double bnorm = 0, beta = 0;
+  int rc = norm_of(h->b, &bnorm);
+  if (rc) return rc;
+  auto true_residual = [&]() -> int {
+    int e = apply_op(h, h->xs, h->r);
+    if (e) return e;
+    f2d_sub<<<nb, 256, 0, h->stream>>>(h->b, h->r, n);
+    return norm_of(h->r, &beta);
+  };
+  rc = true_residual();
+  if (rc) return rc;
+  h->resvec.push_back(beta);
+  info->rhs_norm = bnorm;
+  const double bn = bnorm > 0 ? bnorm : 1.0;
+  info->initial_relres = beta / bn;
+  const double target = tol * bn;
+  if (beta > target && std::isfinite(beta)) {
+    auto cdiv = [](double2 a, double2 b) {
+      const double d = b.x * b.x + b.y * b.y;
+      return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+    };
+    auto cmulh = [](double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+    F2_CK(cudaMemcpyAsync(h->bc_rt, h->r, sizeof(double2) * n, cudaMemcpyDeviceToDevice, h->stream));
+    double2 rho = make_double2(1, 0), alpha = make_double2(1, 0), omega = make_double2(1, 0);
+    for (int it = 1; it <= maxit; ++it) {
+      info->iterations = it;
+      double2 rho1;
+      if ((rc = read_dot(h->bc_rt, h->r, &rho1))) return rc;
+      if (rho1.x == 0.0 && rho1.y == 0.0) break;                     // breakdown: flag stays 1
+      if (it == 1) {
+        F2_CK(cudaMemcpyAsync(h->bc_p, h->r, sizeof(double2) * n, cudaMemcpyDeviceToDevice, h->stream));
+      } else {
+        const double2 bta = cmulh(cdiv(rho1, rho), cdiv(alpha, omega));
+        f2d_bicg_p<<<nb, 256, 0, h->stream>>>(h->bc_p, h->r, h->w, bta, omega, n);
+      }
+      if ((rc = prec(h->bc_p, h->bc_ph))) return rc;
+      if ((rc = apply_op(h, h->bc_ph, h->w))) return rc;              // v
+      double2 rtv;
+      if ((rc = read_dot(h->bc_rt, h->w, &rtv))) return rc;
+      if (rtv.x == 0.0 && rtv.y == 0.0) break;
+      alpha = cdiv(rho1, rtv);
+      f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->r, h->w, make_double2(-alpha.x, -alpha.y), n);   // s = r - alpha v
+      double sn = 0;
+      if ((rc = norm_of(h->r, &sn))) return rc;
+      h->resvec.push_back(sn);
+      info->cycles += 1;
+      if (!(sn > target) || !std::isfinite(sn)) {
+        f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->xs, h->bc_ph, alpha, n);
+        break;
+      }
+      if ((rc = prec(h->r, h->bc_sh))) return rc;
+      if ((rc = apply_op(h, h->bc_sh, h->z))) return rc;             // t
+      double2 tt, ts;
+      if ((rc = read_dot(h->z, h->z, &tt))) return rc;
+      if ((rc = read_dot(h->z, h->r, &ts))) return rc;
+      if (tt.x == 0.0) break;
+      omega = make_double2(ts.x / tt.x, ts.y / tt.x);
+      f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->xs, h->bc_ph, alpha, n);
+      f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->xs, h->bc_sh, omega, n);
+      f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->r, h->z, make_double2(-omega.x, -omega.y), n);   // r = s - omega t
+      double rn = 0;
+      if ((rc = norm_of(h->r, &rn))) return rc;
+      h->resvec.push_back(rn);
+      info->cycles += 1;
+      if (!(rn > target) || !std::isfinite(rn)) break;
+      if (omega.x == 0.0 && omega.y == 0.0) break;
+      rho = rho1;
+    }
+    rc = true_residual();
+    if (rc) return rc;
+  }
+  int flag = 0;
+  if (x) F2_CK(cudaMemcpyAsync(x, h->xs, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaMemcpyAsync(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  if (flag) return fail(h, WG_ERR_TIMEOUT, "tensor-core GEMM: bounded barrier wait timed out");
+  h->xs_ready = true;
+  info->relres = beta / bn;
+  if (!std::isfinite(beta)) return fail(h, WG_ERR_NUMERIC, "wg2d_solve_bicgstab: non-finite residual");
+  info->flag = beta <= target ? 0 : 1;
+  return info->flag ? WG_NOT_CONVERGED : WG_OK;
+}
+
+int wg2d_get_state(wg2d_problem* h, double* x) {
+  if (!h || !x) return h ? fail(h, WG_ERR_ARG, "wg2d_get_state: null argument") : WG_ERR_ARG;
+  if (!h->xs_ready) return fail(h, WG_ERR_ARG, "wg2d_get_state: no resident solution");
+  F2_CK(cudaMemcpyAsync(x, h->xs, sizeof(double2) * h->n, cudaMemcpyDeviceToHost, h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  return WG_OK;
+}
+
+int wg2d_solve_resvec(wg2d_problem* h, double* out, int cap, int* count) {
+  if (!h || !count) return h ? fail(h, WG_ERR_ARG, "wg2d_solve_resvec: null count") : WG_ERR_ARG;
+  *count = (int)h->resvec.size();
+  if (out)
+    for (int i = 0; i < cap && i < *count; ++i) out[i] = h->resvec[i];
+  return WG_OK;
+}
+
+int wg2d_set_observables(wg2d_problem* h, const wg2d_observables_desc* d, const double* W, const double* wj) {
+  if (!h) return WG_ERR_ARG;
+  if (!d || !W || !wj) return fail(h, WG_ERR_ARG, "wg2d_set_observables: null argument");
+  bool ok = d->n_zero_x >= 1 && d->n_zero_x <= 2 && d->n_zero_y >= 1 && d->n_zero_y <= 2 && d->n_dx >= 0 &&
+            d->n_dx <= 8 && d->n_dy >= 0 && d->n_dy <= 8 && d->n_target_y >= 1;
+  for (int i = 0; ok && i < d->n_zero_x; ++i) ok = d->zero_x[i] >= 0 && d->zero_x[i] < h->nrx;
+  for (int i = 0; ok && i < d->n_zero_y; ++i) ok = d->zero_y[i] >= 0 && d->zero_y[i] < h->nry;
+  for (int i = 0; ok && i < d->n_dx; ++i) ok = d->dx_idx[i] >= 0 && d->dx_idx[i] < h->nrx;
+  for (int i = 0; ok && i < d->n_dy; ++i) ok = d->dy_idx[i] >= 0 && d->dy_idx[i] < h->nry;
+  if (!ok) return fail(h, WG_ERR_ARG, "wg2d_set_observables: zero cells or derivative rows out of range");
+  cudaStreamSynchronize(h->stream);
+  void* old[] = {h->obs_W, h->obs_wj, h->obs_out};
+  for (void* p : old)
+    if (p) cudaFree(p);
+  h->obs_W = h->obs_wj = h->obs_out = nullptr;
+  h->obs_ready = false;
+  const size_t nty = d->n_target_y;
+  F2_CK(dalloc(&h->obs_W, nty * h->nY));
+  F2_CK(dalloc(&h->obs_wj, nty));
+  F2_CK(dalloc(&h->obs_out, (size_t)3 * h->nX * h->nY + (size_t)3 * h->nX * nty + h->nX));
+  F2_CK(cudaMemcpy(h->obs_W, W, sizeof(double) * nty * h->nY, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(h->obs_wj, wj, sizeof(double) * nty, cudaMemcpyHostToDevice));
+  h->obs = *d;
+  h->obs_ready = true;
+  return WG_OK;
+}
+
+int wg2d_observables(wg2d_problem* h, const double* rho, double* nDG, double* jxDG, double* jyDG, double* n,
+                     double* jx, double* jy, double* j) {
+  if (!h) return WG_ERR_ARG;
+  if (!h->obs_ready) return fail(h, WG_ERR_ARG, "wg2d_observables: wg2d_set_observables was not called");
+  const double2* F = h->xs;
+  if (rho) {
+    F2_CK(cudaMemcpyAsync(h->x, rho, sizeof(double2) * h->n, cudaMemcpyHostToDevice, h->stream));
+    F = h->x;
+  } else if (!h->xs_ready) {
+    return fail(h, WG_ERR_ARG, "wg2d_observables: no resident solution (pass rho)");
+  }
+  f2d_observables_kernel<<<(h->nX + 127) / 128, 128, 0, h->stream>>>(F, h->obs, h->obs_W, h->obs_wj, h->nX, h->nY,
+                                                                      h->nrx, h->nry, h->obs_out);
+  F2_CK(cudaGetLastError());
+  const size_t g = (size_t)h->nX * h->nY, t = (size_t)h->nX * h->obs.n_target_y;
+  double* outs[] = {nDG, jxDG, jyDG, n, jx, jy, j};
+  const size_t offs[] = {0, g, 2 * g, 3 * g, 3 * g + t, 3 * g + 2 * t, 3 * g + 3 * t};
+  const size_t cnt[] = {g, g, g, t, t, t, (size_t)h->nX};
+  for (int i = 0; i < 7; ++i)
+    if (outs[i])
+      F2_CK(cudaMemcpyAsync(outs[i], h->obs_out + offs[i], sizeof(double) * cnt[i], cudaMemcpyDeviceToHost,
+                            h->stream));
+  F2_CK(cudaStreamSynchronize(h->stream));
+  return WG_OK;
 }
 
 }  // extern "C"

@@ -742,7 +742,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
       reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
                       P.stream, mask, cpp, nd, nd_pp);
-  prof_end(P, PROF_GEMM_F64, ev);
+  prof_end(P, PROF_GEMM_F64TC, ev);
   if (e != cudaSuccess) return e;
   e = launch_stencil_f64(P, P.xh, P.yh, mask);
   if (e != cudaSuccess) return e;
@@ -751,7 +751,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
       reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp);
   e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream,
                       mask, cpp, nd, nd_pp);
-  prof_end(P, PROF_GEMM_F64, ev);
+  prof_end(P, PROF_GEMM_F64TC, ev);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }

@@ -333,16 +333,17 @@ template <int NK>
 cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
   const double BN = (double)P.N * P.batch, ncols = (double)P.ncols, nxi = P.s.nxi, nk = P.s.nk;
   const double gemm_flops = 8.0 * nxi * nk * ncols;
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * BN);
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX64, 1, 32.0 * BN, 8.0 * NK * BN);
   flux_launch<NK>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream);
-  prof_end(P, PROF_FLUX, ev);
+  prof_end(P, PROF_FLUX64, ev);
   dim3 g1((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nxi + GBM - 1) / GBM);
   ev = prof_begin(P, PROF_GEMM_F64, 1, 16.0 * (BN + nxi * ncols), gemm_flops);
   zgemm_kernel<0><<<g1, 256, 0, P.stream>>>(P.phi, P.s.nk, x, P.xh, P.s.nxi, P.s.nk, P.ncols);
   prof_end(P, PROF_GEMM_F64, ev);
-  ev = prof_begin(P, PROF_STENCIL, 1, 32.0 * nxi * ncols + 8.0 * P.batch * P.s.n_el * NK * NK * (nxi + 1));
+  ev = prof_begin(P, PROF_STENCIL64, 1, 32.0 * nxi * ncols + 8.0 * P.batch * P.s.n_el * NK * NK * (nxi + 1),
+                  16.0 * NK * nxi * ncols);
   stencil_launch<NK>(P.xh, P.yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream);
-  prof_end(P, PROF_STENCIL, ev);
+  prof_end(P, PROF_STENCIL64, ev);
   dim3 g2((unsigned)((P.ncols + GBN - 1) / GBN), (P.s.nk + GBM - 1) / GBM);
   ev = prof_begin(P, PROF_GEMM_F64, 1, 16.0 * (2 * BN + nxi * ncols), gemm_flops);
   zgemm_kernel<1><<<g2, 256, 0, P.stream>>>(P.phi, P.s.nk, P.yh, y, P.s.nk, P.s.nxi, P.ncols);
@@ -493,27 +494,27 @@ cudaError_t launch_apply(Problem& P, const double2* x, double2* y) {
 }
 
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int* mask) {
-  cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 32.0 * P.N * P.batch, 0, mask);
+  cudaEvent_t ev = prof_begin(P, PROF_FLUX64, 1, 32.0 * P.N * P.batch, 8.0 * P.s.nK * P.N * P.batch, mask);
   switch (P.s.nK) {
     case 2: flux_launch<2>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
     case 3: flux_launch<3>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
     default: flux_launch<4>(x, y, P.kvec, P.qd, P.fb, P.batch, P.s.n_el, P.s.nk, P.shift, P.stream, mask); break;
   }
-  prof_end(P, PROF_FLUX, ev);
+  prof_end(P, PROF_FLUX64, ev);
   return cudaGetLastError();
 }
 
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const int* mask) {
   const int nK = P.s.nK;
-  cudaEvent_t ev = prof_begin(P, PROF_STENCIL, 1,
-                              32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1), 0,
-                              mask);
+  cudaEvent_t ev = prof_begin(P, PROF_STENCIL64, 1,
+                              32.0 * P.s.nxi * P.ncols + 8.0 * P.batch * P.s.n_el * nK * nK * (P.s.nxi + 1),
+                              16.0 * nK * P.s.nxi * P.ncols, mask);
   switch (nK) {
     case 2: stencil_launch<2>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
     case 3: stencil_launch<3>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
     default: stencil_launch<4>(xh, yh, P.beta, P.betai, P.batch, P.s.n_el, P.s.nxi, P.stream, mask); break;
   }
-  prof_end(P, PROF_STENCIL, ev);
+  prof_end(P, PROF_STENCIL64, ev);
   return cudaGetLastError();
 }
 

@@ -195,7 +195,11 @@ int transient_run(Problem& P, const wg_transient_opts& o, double* n_hist, double
   for (int t = 1; t <= o.nsteps; ++t) {
     if (t == 1 || (E > 0 && ((t - 1) % E == 0 || t < F))) {
       TK(gummel_potential(P, G.active));
+      // the update rebuilds the operator and the inflow; a fixed right-hand side is kept in r
+      // (free between steps) and put back
+      if (o.fixed_rhs) TK(cudaMemcpyAsync(P.r, P.rhs, sizeof(double2) * tot, cudaMemcpyDeviceToDevice, P.stream));
       TK(launch_potential_update(P, 0, B));
+      if (o.fixed_rhs) TK(cudaMemcpyAsync(P.rhs, P.r, sizeof(double2) * tot, cudaMemcpyDeviceToDevice, P.stream));
       for (int b = 0; b < B; ++b) ++info[b].refreshes;
     }
     if (cn) {

@@ -480,6 +480,82 @@ def _drift_setup(prm, AX, AY, RX, RY, periodic):
     return drift, len(w)
 
 
+def _zero_weights(cells):
+    """Cells and weights of the value at zero relative separation (zeroInterpolationWeights of
+    get_Observables_full2D.m:81-103): the cell at zero, else the two bracketing cells linearly,
+    else the nearest cell."""
+    cells = np.asarray(cells, dtype=float)
+    i = int(np.argmin(np.abs(cells)))
+    if abs(cells[i]) <= max(1e-14, 1e-12 * max(1.0, np.abs(cells).max())):
+        return [i], [1.0]
+    neg, pos = np.flatnonzero(cells < 0), np.flatnonzero(cells > 0)
+    if neg.size and pos.size:
+        lo, hi = int(neg[-1]), int(pos[0])
+        h = cells[hi] - cells[lo]
+        return [lo, hi], [cells[hi] / h, -cells[lo] / h]
+    return [i], [1.0]
+
+
+def _derivative_row(cells, D):
+    """The derivative at zero relative separation as a sparse row (derivativeRowAtZero of
+    get_Observables_full2D.m:105-135): the row of D at a zero cell, else a difference of the
+    bracketing (or the nearest one-sided) cells."""
+    cells = np.asarray(cells, dtype=float)
+    n = cells.size
+    i = int(np.argmin(np.abs(cells)))
+    row = np.zeros(n)
+    if abs(cells[i]) <= max(1e-14, 1e-12 * max(1.0, np.abs(cells).max())):
+        row = np.asarray(D[i], dtype=float).ravel().copy()
+    else:
+        neg, pos = np.flatnonzero(cells < 0), np.flatnonzero(cells > 0)
+        if neg.size and pos.size:
+            lo, hi = int(neg[-1]), int(pos[0])
+        elif i == 0:
+            lo, hi = 0, 1
+        elif i == n - 1:
+            lo, hi = n - 2, n - 1
+        else:
+            lo, hi = i - 1, i + 1
+        h = cells[hi] - cells[lo]
+        row[lo], row[hi] = -1 / h, 1 / h
+    nz = np.flatnonzero(row)
+    return [int(k) for k in nz], [float(row[k]) for k in nz]
+
+
+def _y_projection(ydg, target):
+    """W [n_target x nY] with (W v) = v averaged over duplicate DG Y nodes and linearly
+    interpolated (extrapolated) to the target points (projectValuesToY), and the trapezoid
+    weights over the target points (integrateOverY; the single point itself when there is one)."""
+    ydg = np.asarray(ydg, dtype=float)
+    order = np.argsort(ydg, kind="stable")
+    tol = 1e-12 * max(abs(ydg.max() - ydg.min()), 1e-300)
+    uy, cols = [], []
+    for i in order:
+        if uy and ydg[i] - uy[-1] <= tol:
+            cols[-1].append(i)
+        else:
+            uy.append(ydg[i])
+            cols.append([i])
+    uy = np.asarray(uy)
+    A = np.zeros((uy.size, ydg.size))
+    for g, c in enumerate(cols):
+        A[g, c] = 1.0 / len(c)
+    if uy.size == 1:
+        W = np.repeat(A, target.size, axis=0)
+    else:
+        k = np.clip(np.searchsorted(uy, target, side="right") - 1, 0, uy.size - 2)
+        t = (target - uy[k]) / (uy[k + 1] - uy[k])
+        W = A[k] * (1 - t)[:, None] + A[k + 1] * t[:, None]
+    if target.size > 1:
+        d = np.diff(target)
+        wj = np.zeros(target.size)
+        wj[:-1] += 0.5 * d
+        wj[1:] += 0.5 * d
+    else:
+        wj = np.ones(1)
+    return np.ascontiguousarray(W), wj
+
+
 class Full2DOperator:
     """A = A_diff + G_drift of the reference's Full-2D solver, applied on the GPU.
 
@@ -490,9 +566,9 @@ class Full2DOperator:
     the tensor cores (default) instead of FP64 CUDA-core kernels.
     """
 
-    def __init__(self, mat, V=None, tensor_cores=True):
+    def __init__(self, mat, V=None, tensor_cores=True, factors=None):
         self.lib = _lib.load()
-        f = build_factors(mat)
+        f = build_factors(mat) if factors is None else factors
         self.factors = f
         self.mat = mat
         self.V = None
@@ -518,11 +594,47 @@ class Full2DOperator:
                                                 _lib.dptr(d["xq"]), _lib.dptr(d["yq"]), _lib.dptr(d["vx"]),
                                                 _lib.dptr(d["vy"]), _lib.dptr(pot), float(d["capc"]),
                                                 _lib.dptr(d["cap"])))
+            self._set_observables()
             if V is not None:
                 self.set_potential(V)
         except Exception:
             self.close()
             raise
+
+    def _set_observables(self):
+        """Hand the zero-separation weights, derivative rows and the material-Y projection of
+        get_Observables_full2D.m to the device (once per handle)."""
+        f = self.factors
+        RX, RY = f["rel"]
+        AX, AY = f["axes"]
+        d = _lib.Wg2dObservablesDesc()
+        zx, wx = _zero_weights(RX["cells"])
+        zy, wy = _zero_weights(RY["cells"])
+        dxi, dxv = _derivative_row(RX["cells"], RX["D"])
+        dyi, dyv = _derivative_row(RY["cells"], RY["D"])
+        if len(dxi) > 8 or len(dyi) > 8:
+            raise WignerError(_lib.WG_ERR_ARG, "derivative rows with more than 8 nonzeros")
+        d.n_zero_x, d.n_zero_y, d.n_dx, d.n_dy = len(zx), len(zy), len(dxi), len(dyi)
+        for i, (a, w) in enumerate(zip(zx, wx)):
+            d.zero_x[i], d.w_zero_x[i] = a, w
+        for i, (a, w) in enumerate(zip(zy, wy)):
+            d.zero_y[i], d.w_zero_y[i] = a, w
+        for i, (a, v) in enumerate(zip(dxi, dxv)):
+            d.dx_idx[i], d.dx_val[i] = a, v
+        for i, (a, v) in enumerate(zip(dyi, dyv)):
+            d.dy_idx[i], d.dy_val[i] = a, v
+
+        def kg(m):                          # massToKg
+            mk = m * M0 if abs(m) > 1e-25 else m
+            return mk if mk > 0 else 0.041 * M0
+        mex = self.mat.get("me_x_ch", 0.041)
+        d.scale_x = QE * HBAR / kg(mex)
+        d.scale_y = QE * HBAR / kg(self.mat.get("me_y_ch", mex))
+        target = np.asarray(self.mat["y"], dtype=float) * f["scale"]
+        W, wj = _y_projection(AY["nodes"], target)
+        d.n_target_y = target.size
+        self.target_y = target
+        self._check(self.lib.wg2d_set_observables(self.h, C.byref(d), _lib.dptr(W), _lib.dptr(np.ascontiguousarray(wj))))
 
     def _set_axis(self, axis, terms, ax, nr, periodic):
         if not terms:
@@ -545,65 +657,35 @@ class Full2DOperator:
                                                 rp.ctypes.data_as(C.POINTER(C.c_int)),
                                                 col.ctypes.data_as(C.POINTER(C.c_int)), _lib.dptr(val)))
 
-    def observables(self, rho):
-        """(n [X nDof x material Ny] m^-3, j [X nDof], nDG, jxDG) of a state
-        (get_Observables_full2D.m:19-78): n = real(rho) at zero relative separation (the
-        rho_x = 0 cell; the two rho_y cells around 0 weighted linearly), j_x = q hbar / m_x
-        imag(d rho / d rho_x) at zero (the central-difference row), projected onto the material
-        Y grid (DG values at shared interface nodes averaged, linear interpolation), j the
-        trapezoid integral over Y."""
-        f = self.factors
-        RX, RY = f["rel"]
-        AX, AY = f["axes"]
-        nrx, nry, nX, nY = RX["n"], RY["n"], AX["nd"], AY["nd"]
-        r4 = np.asarray(rho).reshape(nY, nX, nry, nrx)                   # [Y, X, rho_y, rho_x]
+    def observables(self, rho=None):
+        """(n [X nDof x material Ny] m^-3, j [X nDof], nDG, jxDG) of a state (get_Observables_full2D.m:19-78),
+        computed on the device: n = real(rho) at zero relative separation (the rho_x = 0 cell; the two
+        rho_y cells around 0 weighted linearly), j_x = q hbar / m_x imag(d rho / d rho_x) at zero (the
+        central-difference row), projected onto the material Y grid (DG values at shared interface
+        nodes averaged, linear interpolation), j the trapezoid integral over Y.  rho = None: the
+        solution resident on the device (no copy of the state crosses to the host)."""
+        o = self.observables_all(rho)
+        return o["n"], o["j"], o["nDG"], o["jxDG"]
 
-        def zero(cells):
-            i = int(np.argmin(np.abs(cells)))
-            if abs(cells[i]) <= max(1e-14, 1e-12 * max(1.0, np.abs(cells).max())):
-                return np.array([i]), np.array([1.0])
-            lo, hi = np.flatnonzero(cells < 0)[-1], np.flatnonzero(cells > 0)[0]
-            h = cells[hi] - cells[lo]
-            return np.array([lo, hi]), np.array([cells[hi] / h, -cells[lo] / h])
-        ax_, wx = zero(RX["cells"])
-        ay_, wy = zero(RY["cells"])
-        at0 = np.einsum("yxab,a,b->xy", r4[:, :, ay_][:, :, :, ax_], wy, wx)   # rho at (0, 0)
-        nDG = at0.real
-        ix0 = ax_[0] if ax_.size == 1 else None
-        if ix0 is not None:
-            drow = RX["D"][ix0]
-        else:
-            drow = np.zeros(nrx)
-            h = RX["cells"][ax_[1]] - RX["cells"][ax_[0]]
-            drow[ax_[0]], drow[ax_[1]] = -1 / h, 1 / h
-        d = np.einsum("yxba,a,b->xy", r4[:, :, ay_, :], drow, wy)
-        mex = self.mat.get("me_x_ch", 0.041)
-        mkg = mex * M0 if abs(mex) > 1e-25 else mex
-        mkg = mkg if mkg > 0 else 0.041 * M0
-        jxDG = QE * HBAR / mkg * d.imag
-        target = np.asarray(self.mat["y"], dtype=float) * f["scale"]
-        ydg = AY["nodes"]
-        order = np.argsort(ydg, kind="stable")
-        tol = 1e-12 * max(abs(ydg.max() - ydg.min()), 1e-300)
-        uy, cols = [], []
-        for i in order:
-            if uy and ydg[i] - uy[-1] <= tol:
-                cols[-1].append(i)
-            else:
-                uy.append(ydg[i])
-                cols.append([i])
-        uy = np.asarray(uy)
-
-        def to_y(v):
-            a = np.stack([v[:, c].mean(axis=1) for c in cols], axis=1)
-            if uy.size == 1:
-                return np.repeat(a, target.size, axis=1)
-            k = np.clip(np.searchsorted(uy, target, side="right") - 1, 0, uy.size - 2)
-            t = (target - uy[k]) / (uy[k + 1] - uy[k])
-            return a[:, k] * (1 - t) + a[:, k + 1] * t
-        n, jx = to_y(nDG), to_y(jxDG)
-        j = np.sum(0.5 * (jx[:, 1:] + jx[:, :-1]) * np.diff(target), axis=1) if target.size > 1 else jx[:, 0]
-        return n, j, nDG, jxDG
+    def observables_all(self, rho=None):
+        """Every observable of get_Observables_full2D.m: n, jx, jy [X nDof x Ny], j, and the DG values
+        nDG, jxDG, jyDG [X nDof x Y nDof], y (the material Y points, m); see observables()."""
+        AX, AY = self.factors["axes"]
+        nX, nY, nty = AX["nd"], AY["nd"], self.target_y.size
+        out = {k: np.empty((nX, nY)) for k in ("nDG", "jxDG", "jyDG")}
+        out.update({k: np.empty((nX, nty)) for k in ("n", "jx", "jy")})
+        out["j"] = np.empty(nX)
+        r = None
+        if rho is not None:
+            r = np.ascontiguousarray(np.asarray(rho, dtype=complex).reshape(-1))
+            if r.size != self.n:
+                raise WignerError(_lib.WG_ERR_ARG, "rho has %d entries, expected %d" % (r.size, self.n),
+                                  "DG:Full2D:InvalidObservableInput")
+        self._check(self.lib.wg2d_observables(self.h, None if r is None else r.view(np.float64).ctypes.data_as(_lib._D),
+                                              *[_lib.dptr(out[k]) for k in ("nDG", "jxDG", "jyDG", "n", "jx", "jy",
+                                                                            "j")]))
+        out["y"] = self.target_y
+        return out
 
     def reservoir_rhs(self, EfL, EfR, Vxy=None):
         """The system's right-hand side from the Source/Drain reservoirs (get_SysM_full2D.m's rhs:
@@ -653,21 +735,73 @@ class Full2DOperator:
                                                out.view(np.float64).ctypes.data_as(_lib._D)))
         return out
 
-    def solve(self, rhs, x0=None, tol=1e-8, maxit=50, restart=40, mixed=False, inner_tol=1e-3):
+    def solve(self, rhs, x0=None, tol=1e-8, maxit=50, restart=40, mixed=False, inner_tol=1e-3, resident=False,
+              warm=False):
         """rho = A \\ rhs by right-preconditioned flexible GMRES(restart) on the device; mixed: FP64
-        refinement around FP32 inner solves (FP32 preconditioner required).  Returns (status, info, rho)."""
-        b = np.ascontiguousarray(np.asarray(rhs, dtype=complex).reshape(-1))
-        x = np.zeros_like(b) if x0 is None else np.ascontiguousarray(np.asarray(x0, dtype=complex).reshape(-1))
-        if b.size != self.n or x.size != self.n:
-            raise WignerError(_lib.WG_ERR_ARG, "rhs and x0 need %d entries" % self.n)
-        opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), int(restart), 0 if x0 is None else 1, 1 if mixed else 0,
-                                  float(inner_tol))
+        refinement around FP32 inner solves (FP32 preconditioner required).  Returns (status, info, rho).
+        resident: the solution stays on the device only (rho is None; observables() and state() read it),
+        warm: the warm start is the resident solution of the previous solve (x0 ignored), rhs = None:
+        the right-hand side of the previous solve."""
+        b = None
+        if rhs is not None:
+            b = np.ascontiguousarray(np.asarray(rhs, dtype=complex).reshape(-1))
+            if b.size != self.n:
+                raise WignerError(_lib.WG_ERR_ARG, "rhs needs %d entries" % self.n)
+        x = None
+        if not warm and (x0 is not None or not resident):
+            x = np.zeros(self.n, dtype=complex)
+            if x0 is not None:
+                x0 = np.asarray(x0, dtype=complex).reshape(-1)
+                if x0.size != self.n:
+                    raise WignerError(_lib.WG_ERR_ARG, "x0 needs %d entries" % self.n)
+                x[:] = x0
+        use_x0 = 1 if (warm or x0 is not None) else 0
+        opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), int(restart), use_x0, 1 if mixed else 0, float(inner_tol))
         info = _lib.Wg2dSolveInfo()
-        st = self.lib.wg2d_solve(self.h, b.view(np.float64).ctypes.data_as(_lib._D),
-                                 x.view(np.float64).ctypes.data_as(_lib._D), C.byref(opts), C.byref(info))
+        st = self.lib.wg2d_solve(self.h, None if b is None else b.view(np.float64).ctypes.data_as(_lib._D),
+                                 None if x is None else x.view(np.float64).ctypes.data_as(_lib._D),
+                                 C.byref(opts), C.byref(info))
         if st not in (_lib.WG_OK, _lib.WG_NOT_CONVERGED):
             self._check(st)
-        return st, info.as_dict(), x
+        if resident:
+            return st, info.as_dict(), None
+        return st, info.as_dict(), (self.state() if x is None else x)
+
+    def solve_bicgstab(self, rhs, x0=None, tol=1e-8, maxit=100, resident=False):
+        """rho = A \\ rhs by preconditioned BiCGSTAB on the device (the line-transverse preconditioner when
+        one is set, none otherwise).  Returns (status, info, rho); info["cycles"] counts half steps."""
+        b = None
+        if rhs is not None:
+            b = np.ascontiguousarray(np.asarray(rhs, dtype=complex).reshape(-1))
+            if b.size != self.n:
+                raise WignerError(_lib.WG_ERR_ARG, "rhs needs %d entries" % self.n)
+        x = None if (resident and x0 is None) else np.zeros(self.n, dtype=complex)
+        if x0 is not None:
+            x[:] = np.asarray(x0, dtype=complex).reshape(-1)
+        opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), 0, 1 if x0 is not None else 0, 0, 0.0)
+        info = _lib.Wg2dSolveInfo()
+        st = self.lib.wg2d_solve_bicgstab(self.h, None if b is None else b.view(np.float64).ctypes.data_as(_lib._D),
+                                          None if x is None else x.view(np.float64).ctypes.data_as(_lib._D),
+                                          C.byref(opts), C.byref(info))
+        if st not in (_lib.WG_OK, _lib.WG_NOT_CONVERGED):
+            self._check(st)
+        return st, info.as_dict(), (None if resident else x)
+
+    def state(self):
+        """The resident solution of the last solve (host copy)."""
+        x = np.empty(self.n, dtype=complex)
+        self._check(self.lib.wg2d_get_state(self.h, x.view(np.float64).ctypes.data_as(_lib._D)))
+        return x
+
+    def resvec(self):
+        """Residual norms of the last solve: the initial true residual, then the GMRES estimate after
+        every inner iteration (DG.info.solve.resvec)."""
+        n = C.c_int()
+        self._check(self.lib.wg2d_solve_resvec(self.h, None, 0, C.byref(n)))
+        out = np.zeros(n.value)
+        if n.value:
+            self._check(self.lib.wg2d_solve_resvec(self.h, _lib.dptr(out), n.value, C.byref(n)))
+        return out
 
     def apply(self, u):
         """y = A u (complex vector in the reference's order rho_x, rho_y, X, Y)."""
@@ -706,3 +840,211 @@ class Full2DOperator:
             self.close()
         except Exception:
             pass
+
+
+_SOLVE_ON = ("true", "yes", "on", "solve", "always")
+_SOLVE_OFF = ("false", "no", "off", "operator-only", "skip", "never")
+
+
+def _should_solve(mode, n, max_auto):
+    """shouldSolve of solve_transport_DG_full2D.m:1249-1279: (solve?, status when skipped)."""
+    if isinstance(mode, (bool, np.bool_)):
+        return bool(mode), "operator-ready-solve-disabled"
+    if isinstance(mode, (int, float, np.number)):
+        return mode != 0, "operator-ready-solve-disabled"
+    m = str(mode).strip().lower()
+    if m == "auto":
+        return n <= max_auto, "operator-ready-solve-skipped-size"
+    if m in _SOLVE_ON:
+        return True, ""
+    if m in _SOLVE_OFF:
+        return False, "operator-ready-solve-disabled"
+    raise WignerError(_lib.WG_ERR_ARG, 'Unknown full2D_solve mode "%s".' % mode, "DG:Full2D:UnknownSolveMode")
+
+
+def _store_rho_array(prm, n):
+    """shouldStoreRHOArray (solve_transport_DG_full2D.m:1309-1330)."""
+    mode = prm.get("full2D_storeRHOArray", "auto")
+    if isinstance(mode, (bool, np.bool_, int, float, np.number)):
+        return bool(mode)
+    m = str(mode).strip().lower()
+    if m == "auto":
+        return n <= float(prm.get("full2D_maxStoredRHOArrayDof", 2e6))
+    if m in ("true", "yes", "on", "store", "always"):
+        return True
+    if m in ("false", "no", "off", "never"):
+        return False
+    raise WignerError(_lib.WG_ERR_ARG, 'Unknown full2D_storeRHOArray mode "%s".' % mode,
+                      "DG:Full2D:UnknownStorageMode")
+
+
+def _initial_rho(rho0, n):
+    """validateInitialRho (solve_transport_DG_full2D.m:508-527)."""
+    if rho0 is None:
+        return None
+    r = np.asarray(rho0)
+    if r.size == 0:
+        return None
+    if r.dtype.kind not in "fc" or (r.ndim > 1 and sum(d > 1 for d in r.shape) > 1) or r.size != n:
+        raise WignerError(_lib.WG_ERR_ARG, "rho0 must be a full single/double vector with %d entries in "
+                          "rho_x,rho_y,X,Y order." % n, "DG:Full2D:InvalidInitialRho")
+    r = r.reshape(-1).astype(complex)
+    if not np.all(np.isfinite(r)):
+        raise WignerError(_lib.WG_ERR_ARG, "rho0 must contain only finite values.", "DG:Full2D:InvalidInitialRho")
+    return r
+
+
+def solve_transport_DG_full2D(mat, Vxy=None, EfL=None, EfR=None, rho0=None):
+    """DG = solve_transport_DG_full2D(mat, Vxy, EfL, EfR, rho0) (DG_code/solve_transport_DG_full2D.m:1-130)
+    with the operator, the preconditioner, the Krylov solve and the observables on the GPU.
+
+    Follows solveStationarySystem (:132-346): the full2D_solve mode (auto: solve up to
+    full2D_maxAutoSolveDof unknowns), full2D_solverTol (default 1e-4) relative to |rhs|,
+    full2D_solverMaxIt (default 1400; restart cycles for GMRES, iterations for BiCGSTAB), the
+    GMRES restart full2D_gmresRestart (default full2D_gpuGmresRestart, 20), the basis-memory guard
+    (DG:Full2D:GmresMemoryLimit, full2D_gmresMaxBasisBytes, default 9 GiB), the warm start rho0 as
+    a right-preconditioned correction (GMRES only, DG:Full2D:InitialRhoSolver otherwise), the
+    independent true-residual check and iterativeStatus.  Solvers: 'gmres' (flexible GMRES,
+    right-preconditioned) and 'bicgstab'; 'auto' selects GMRES with the line-transverse
+    preconditioner (the reference's GPU default is BiCGSTAB with the Jacobi diagonal, which is not
+    built); 'direct' raises DG:Full2D:GPUDirectSolverUnsupported as the reference does on the GPU.
+    Preconditioners: 'line-transverse' (and 'auto'), 'none'; the host-side ones (jacobi, rowabs,
+    blockjacobi) raise DG:Full2D:UnsupportedPreconditioner.  Returns a dict with the reference's
+    DG fields: status, rho, RHO (when stored), n, jx, jy, j, nDG, jxDG, jyDG, y, chi, yDG, rho_x,
+    rho_y, xi, and info.solve (flag, relres, trueRelres, reportedRelres, iterations, resvec,
+    initialGuess, rhsNormalization, tolerance, maxIterations, solver, preconditioner, status, ...).
+    """
+    import time
+    prm = mat["dg"]["params"]
+    V = mat.get("V") if Vxy is None else Vxy
+    if V is None:
+        V = np.zeros((len(np.asarray(mat["x"])), len(np.asarray(mat["y"]))))
+    f = build_factors(mat)
+    n = f["n"]
+    # every argument and option is checked before the device operator is built (validateInitialRho
+    # runs before get_SysM_full2D in the reference)
+    rho0 = _initial_rho(rho0, n)
+    info = dict(requestedMode=prm.get("full2D_solve", "auto"), nTotal=n, matrixAssembled=False,
+                matrixFreeAvailable=True, tolerance=float(prm.get("full2D_solverTol", 1e-4)),
+                maxIterations=int(prm.get("full2D_solverMaxIt", 1400)))
+    do, skip = _should_solve(info["requestedMode"], n, float(prm.get("full2D_maxAutoSolveDof", 1e7)))
+    if do and n > float(prm.get("full2D_maxMatrixFreeSolveDof", 2e7)):
+        do, skip = False, "operator-ready-solve-skipped-matrix-free-limit"
+    solver = pmode = None
+    restart = int(prm.get("full2D_gmresRestart", prm.get("full2D_gpuGmresRestart", 20)))
+    if do:
+        solver = str(prm.get("full2D_solver", "auto")).strip().lower()
+        solver = "gmres" if solver == "auto" else solver
+        if solver == "direct":
+            raise WignerError(_lib.WG_ERR_ARG, "full2D_gpu=true supports full2D_solver='bicgstab' or 'gmres'. "
+                              "Select one of these matrix-free Krylov solvers.", "DG:Full2D:GPUDirectSolverUnsupported")
+        if solver not in ("gmres", "bicgstab"):
+            raise WignerError(_lib.WG_ERR_ARG, 'Unknown full2D_solver "%s". Use auto, direct, bicgstab or gmres.'
+                              % solver, "DG:Full2D:UnknownSolver")
+        if rho0 is not None and solver != "gmres":
+            raise WignerError(_lib.WG_ERR_ARG, "A supplied rho0 currently requires full2D_solver='gmres'.",
+                              "DG:Full2D:InitialRhoSolver")
+        info["solver"] = solver
+        pmode = str(prm.get("full2D_preconditioner", "auto")).strip().lower().replace("_", "-")
+        if pmode in ("auto", "line-transverse", "linetransverse"):
+            pmode = "line-transverse"
+        elif pmode in ("none", "off", "false", "no"):
+            pmode = "none"
+        elif pmode in ("jacobi", "diagonal", "rowabs", "rowsum", "row-sum", "row-scaling", "blockjacobi",
+                       "block-jacobi", "rho-block-jacobi", "relative-block-jacobi", "rho-blockjacobi"):
+            raise WignerError(_lib.WG_ERR_ARG, "full2D_preconditioner '%s' is a host-side preconditioner of the "
+                              "CPU path; the device path offers line-transverse and none" % pmode,
+                              "DG:Full2D:UnsupportedPreconditioner")
+        else:
+            raise WignerError(_lib.WG_ERR_ARG, 'Unknown full2D_preconditioner "%s".' % pmode,
+                              "DG:Full2D:UnknownPreconditioner")
+        if solver == "gmres":
+            info["gmresBasisBytesEstimate"] = 16.0 * n * (min(restart, n) + 1)
+            limit = float(prm.get("full2D_gmresMaxBasisBytes", 9 * 1024 ** 3))
+            if info["gmresBasisBytesEstimate"] > limit:
+                raise WignerError(_lib.WG_ERR_OOM, "Estimated GMRES basis %.3g GiB exceeds full2D_gmresMaxBasisBytes. "
+                                  "Reduce restart or explicitly increase the memory budget."
+                                  % (info["gmresBasisBytesEstimate"] / 1024 ** 3), "DG:Full2D:GmresMemoryLimit")
+            info["gmresRestart"] = restart
+            info["preconditionerSide"] = "right"
+    AX, AY = f["axes"]
+    RX, RY = f["rel"]
+    fx, fy = _flux(prm)
+    DG = dict(basis="rho-full2D", flux=fx, fluxX=fx, fluxY=fy, yBoundaryType=f["ytype"], massModel="constant",
+              coordinates=("rho_x", "rho_y", "X", "Y"), chi=AX["nodes"].copy(), yDG=AY["nodes"].copy(),
+              rho_x=RX["cells"].copy(), rho_y=RY["cells"].copy(), xi=RX["cells"].copy(),
+              arraySize=(RX["n"], RY["n"], AX["nd"], AY["nd"]))
+    op = Full2DOperator(mat, V, tensor_cores=bool(prm.get("full2D_tensorCores", True)), factors=f)
+    try:
+        rho = None
+        if not do:
+            info["status"] = skip
+            info["reason"] = "Operator is ready but no solve was run. nTotal=%d." % n
+        else:
+            t0 = time.perf_counter()
+            fp32 = str(prm.get("full2D_preconditionerPrecision", "single")).lower() in ("single", "fp32", "float")
+            if pmode == "line-transverse":
+                op.set_preconditioner(fp32=fp32)
+            info["preconditioner"] = dict(method=pmode, enabled=pmode != "none", executionDevice="gpu",
+                                          precision="fp32" if fp32 else "fp64")
+            info["preconditionerSetupSeconds"] = time.perf_counter() - t0
+            rhs, inflow = op.reservoir_rhs(EfL, EfR, V)
+            DG["boundary"] = {side: {"rhoBoundary": rb, "info": inf} for side, (rb, inf) in inflow.items()}
+            bnorm = float(np.linalg.norm(rhs))
+            t0 = time.perf_counter()
+            if solver == "gmres":
+                st, sinfo, rho = op.solve(rhs, x0=rho0, tol=info["tolerance"], maxit=info["maxIterations"],
+                                          restart=restart, mixed=bool(prm.get("full2D_mixedPrecision", False)))
+            else:
+                st, sinfo, rho = op.solve_bicgstab(rhs, tol=info["tolerance"], maxit=info["maxIterations"])
+            info["iterationSeconds"] = time.perf_counter() - t0
+            resvec = op.resvec()
+            flag = int(sinfo["flag"])
+            r0 = sinfo["initial_relres"]
+            init = dict(provided=rho0 is not None, used=rho0 is not None, basis="physical-rho",
+                        strategy="zero-start", initialTrueRelres=r0, convergedAtStart=False,
+                        correctionTolerance=float("nan"))
+            if rho0 is not None:
+                if r0 <= info["tolerance"]:
+                    init["convergedAtStart"] = True
+                    init["strategy"] = "native-x0"
+                else:
+                    init["strategy"] = "right-preconditioned-correction"
+                    init["correctionTolerance"] = max(np.finfo(float).tiny, info["tolerance"] / r0)
+            if bnorm == 0:
+                init["used"] = False
+                init["strategy"] = "homogeneous-rhs-zero-solution"
+            info["initialGuess"] = init
+            info["rhsNormalization"] = bnorm if bnorm > 0 else 1.0
+            info["trueRelres"] = sinfo["relres"]
+            info["reportedRelres"] = float(resvec[-1] / bnorm) if bnorm > 0 and resvec.size else sinfo["relres"]
+            info["krylovFlag"] = flag
+            info["flag"] = flag
+            info["relres"] = sinfo["relres"]
+            if solver == "gmres":
+                info["iterations"] = [int(sinfo["cycles"]), int(sinfo["iterations"])]
+            else:
+                info["iterations"] = sinfo["cycles"] / 2.0
+            info["resvec"] = resvec
+            info["status"] = ("solved-" if flag == 0 else "iterative-") + solver + ("" if flag == 0 else
+                                                                                     "-not-converged")
+            info["gpu"] = dict(requested=True, enabled=True, resultGathered=True,
+                               note="operator, preconditioner, Krylov vectors and observables on the GPU")
+        DG["status"] = info["status"]
+        DG["info"] = {"solve": info}
+        DG["rho"] = rho
+        if rho is None:
+            DG.update(n=None, j=None, jx=None, jy=None, RHO=None)
+            return DG
+        o = op.observables_all()
+        DG.update(n=o["n"], jx=o["jx"], jy=o["jy"], j=o["j"], nDG=o["nDG"], jxDG=o["jxDG"], jyDG=o["jyDG"],
+                  y=o["y"])
+        if _store_rho_array(prm, n):
+            DG["RHO"] = rho.reshape(DG["arraySize"], order="F")
+        else:
+            DG["RHO"] = None
+            info["RHONote"] = ("RHO array was not duplicated; use DG.rho and reshape with DG.arraySize, ordered as "
+                               "rho_x,rho_y,X,Y, if needed.")
+        return DG
+    finally:
+        op.close()

@@ -112,13 +112,14 @@ class RTDSweep:
         self.P._check(self.lib.wg_transient_set_bias(self.P.h, int(b), float(bias)))
 
     def transient(self, dt, nsteps, method="cn", scale_a=0.0, scale_rhs=0.0, refresh_every=0, refresh_first=0,
-                  tol=0.0, maxit=0, record_every=1):
-        """Advance every problem by nsteps; returns (status, info, n [nrec, batch, ncol], j)."""
+                  tol=0.0, maxit=0, record_every=1, fixed_rhs=False):
+        """Advance every problem by nsteps; returns (status, info, n [nrec, batch, ncol], j).
+        fixed_rhs: keep the resident right-hand side at every refresh (the reference's rhs_INIT)."""
         if method not in _lib.TRANSIENT_METHODS:
             raise WignerError(_lib.WG_ERR_ARG, "unknown transient method %r" % (method,))
         o = _lib.WgTransientOpts(float(dt), int(nsteps), _lib.TRANSIENT_METHODS[method], float(scale_a),
                                  float(scale_rhs), int(refresh_every), int(refresh_first), float(tol), int(maxit),
-                                 int(record_every))
+                                 int(record_every), 1 if fixed_rhs else 0)
         nrec = nsteps // record_every if record_every > 0 else 0
         n = np.zeros((nrec, self.P.batch, self.P.ncol))
         j = np.zeros((nrec, self.P.batch, self.P.ncol))
@@ -218,3 +219,67 @@ def solve_transient_self_consistent(mat, bias0, steps, options=None, transient=N
     return {"n_over_t": np.transpose(n, (2, 0, 1)), "j_over_t": np.transpose(j, (2, 0, 1)), "t": t, "phi": phi,
             "status": st, "info": info, "stationary": ginfo}
 
+
+
+def solve_transport_DG_2D_transient_SC_new(mat, INIT, options=None, transient=None):
+    """DG = solve_transport_DG_2D_transient_SC_new(mat, INIT) (DG_code/solve_transport_DG_2D_transient_SC_new.m:1-221)
+    for the 1D RTD (one valley, one mode), from a caller-supplied INIT.
+
+    INIT (:18-25): ``rho`` (the initial Wigner function, a vector in the solver's order or a
+    one-entry list of it, INIT.rho{1}), ``rhs`` (INIT.rhs{1}, used as given and never refreshed,
+    :153-156), ``V_total`` (the potential added to the band edge, mat.V + V_total at :132;
+    here phi = -V_total on the material grid), optional ``bias`` (the drain bias the INIT state
+    was computed at, default 0) and ``Ef0`` (unused: the contact Fermi levels follow from the band
+    edge and the bias as in the stationary driver); ``Esub``, ``Vsub``, ``A`` and ``p`` are rebuilt
+    on the device from the potential.  mat: the RTD description of solve_rtd_self_consistent plus
+    ``Nt`` (steps), ``dt`` (s) and ``Vd`` (the drain bias after the step at t = 0).
+
+    The loop follows the reference: d rho/dt = rhs_INIT - 2e-10 A rho with RK4 (:153-158) by
+    default (``transient={"method": "cn"}`` for Crank-Nicolson), the operator rebuilt before step t
+    when (t-1) % 20 == 0 or t < 50 (:131-149), the Poisson problem solved for the density after
+    step t when t % 20 == 0 or t < 50 (:204-211).  Returns n_over_t [Nxdof x Ny x ceil(Nt/50)]
+    (steps 1, 51, ...: n_over_t(:,:,1:50:end)), j_over_t [Nxdof x ceil(Nt/5)] (j_over_t(:,1:5:end)),
+    rho_INIT (the final state, a one-entry list as the reference's cell), chi, xi, the final phi
+    and the per-step solver info.
+    """
+    nm = int(mat.get("n_of_modes", 1)) * int(mat.get("n_of_valleys", 1))
+    if nm != 1:
+        raise WignerError(_lib.WG_ERR_ARG, "the 1D RTD transient mirrors one valley and one mode")
+    T = dict(TRANSIENT_DEFAULTS, method="rk4", scaleRhs=1.0, recordEvery=1, stepTolerance=1e-10)
+    for k, v in (transient or {}).items():
+        if k not in T:
+            raise WignerError(_lib.WG_ERR_ARG, "unknown transient option %s" % k)
+        T[k] = v
+    nt = int(mat["Nt"])
+    dt = float(mat["dt"])
+    rho0 = INIT["rho"]
+    rho0 = rho0[0] if isinstance(rho0, (list, tuple)) else rho0
+    rhs0 = INIT["rhs"]
+    rhs0 = rhs0[0] if isinstance(rhs0, (list, tuple)) else rhs0
+    phi0 = -np.asarray(INIT["V_total"], dtype=float).reshape(-1)
+    S = RTDSweep(mat, 1, options)
+    try:
+        if phi0.size != S.nx:
+            raise WignerError(_lib.WG_ERR_ARG, "INIT.V_total needs %d values on the material grid" % S.nx)
+        S.set(0, float(INIT.get("bias", 0.0)), phi0=phi0)
+        S.P.set_rho(0, rho0)
+        S.P.set_rhs(0, rhs0)
+        S.step_bias(0, float(mat.get("Vd", INIT.get("bias", 0.0))))
+        st, info, n, j = S.transient(dt, nt, T["method"], T["scaleA"], T["scaleRhs"], int(T["refreshEvery"]),
+                                     int(T["refreshFirst"]), T["stepTolerance"], int(T["stepMaxCycles"]), 1,
+                                     fixed_rhs=True)
+        rho_end = S.P.rho(0)
+        phi = S.get(0)[0]
+        shp = shape_from_mat(mat)
+    finally:
+        S.close()
+    n_el, nK = shp["n_el"], shp["n_local"]
+    dx = (float(mat["x"][-1]) - float(mat["x"][0])) * 1e-9 / n_el
+    chi = np.concatenate([np.linspace(e * dx, (e + 1) * dx, nK) for e in range(n_el)])
+    lxi = shp["l_xi"]
+    dxi = lxi / (shp["n_xi"] - 1)
+    xi = np.linspace(-(lxi - dxi) / 2, (lxi - dxi) / 2, shp["n_xi"])
+    n_all = n[:, 0, :].T                                   # [Nxdof x Nt]
+    j_all = j[:, 0, :].T
+    return {"n_over_t": n_all[:, None, 0::50], "j_over_t": j_all[:, 0::5], "rho_INIT": [rho_end], "chi": chi,
+            "xi": xi, "phi": phi, "status": st, "info": info[0], "n_all": n_all, "j_all": j_all}

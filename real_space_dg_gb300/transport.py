@@ -115,6 +115,20 @@ class Problem1D:
         self._check(self.lib.wg_get_rho(self.h, int(b), out.view(np.float64).ctypes.data_as(_lib._D)))
         return out
 
+    def set_rho(self, b, rho):
+        """Overwrite problem b's resident Wigner function (the warm start of the next solve)."""
+        r = np.ascontiguousarray(np.asarray(rho, dtype=np.complex128).reshape(-1))
+        if r.size != self.N:
+            raise WignerError(_lib.WG_ERR_ARG, "rho needs %d entries" % self.N)
+        self._check(self.lib.wg_set_rho(self.h, int(b), r.view(np.float64).ctypes.data_as(_lib._D)))
+
+    def set_rhs(self, b, rhs):
+        """Overwrite problem b's right-hand side (kept until the next potential update)."""
+        r = np.ascontiguousarray(np.asarray(rhs, dtype=np.complex128).reshape(-1))
+        if r.size != self.N:
+            raise WignerError(_lib.WG_ERR_ARG, "rhs needs %d entries" % self.N)
+        self._check(self.lib.wg_set_rhs(self.h, int(b), r.view(np.float64).ctypes.data_as(_lib._D)))
+
     def rho_xi(self, b=0):
         out = np.empty((self.ncol, self.n_xi), dtype=np.complex128)
         self._check(self.lib.wg_get_rho_xi(self.h, int(b), out.view(np.float64).ctypes.data_as(_lib._D)))

@@ -14,7 +14,7 @@ HEADER = os.path.join(ROOT, "include", "wigner_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(wg_[a-z0-9_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(wg(?:2d)?_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_header_declares_the_boundary():
@@ -59,6 +59,8 @@ int main(void) {
          sizeof(wg2d_solve_info));
   printf("%zu %zu %zu %zu\n", sizeof(wg_poisson2d_desc), offsetof(wg_poisson2d_desc, temp),
          sizeof(wg_poisson2d_info), offsetof(wg_poisson2d_info, target_integral));
+  printf("%zu %zu %zu\n", sizeof(wg2d_observables_desc), offsetof(wg2d_observables_desc, dx_val),
+         offsetof(wg2d_observables_desc, n_target_y));
   return 0;
 }''')
     exe = tmp_path / "probe"
@@ -80,7 +82,9 @@ int main(void) {
             C.sizeof(_lib.Wg2dShape), C.sizeof(_lib.Wg2dSolveOpts), _lib.Wg2dSolveOpts.inner_tol.offset,
             C.sizeof(_lib.Wg2dSolveInfo),
             C.sizeof(_lib.WgPoisson2dDesc), _lib.WgPoisson2dDesc.temp.offset, C.sizeof(_lib.WgPoisson2dInfo),
-            _lib.WgPoisson2dInfo.target_integral.offset]
+            _lib.WgPoisson2dInfo.target_integral.offset,
+            C.sizeof(_lib.Wg2dObservablesDesc), _lib.Wg2dObservablesDesc.dx_val.offset,
+            _lib.Wg2dObservablesDesc.n_target_y.offset]
     assert got == want
 
 

@@ -1,0 +1,104 @@
+"""The Full-2D drop-in solve_transport_DG_full2D(mat, Vxy, EfL, EfR, rho0).
+
+CPU: the argument and option checks of solveStationarySystem that come before any device work
+(validateInitialRho, the GPU direct-solver error, rho0 with BiCGSTAB, the GMRES basis-memory
+guard, unknown and host-only preconditioners, full2D_solve = off).
+
+GPU: the solve of a reservoir-driven system through the drop-in (GMRES and BiCGSTAB, with the
+line-transverse preconditioner) against the oracle's sparse LU of the same assembled system:
+rho to 1e-8 relative, density and currents (oracle get_Observables_full2D on the LU solution)
+to 1e-8; the solve info fields (flag, status, trueRelres <= tol, resvec from |b - A x0| down to
+the tolerance); the warm start rho0 = DG.rho converges at the start with no iteration.
+"""
+import numpy as np
+import pytest
+
+from oracle import full2d as F2
+from test_reservoir import small_mat
+
+TOL = 1e-10
+
+
+def _mat(**extra):
+    mat = small_mat("contact-modes", "periodic")
+    XX, YY = np.meshgrid(mat["x"], mat["y"], indexing="ij")
+    mat["V"] = 1.424 + 0.15 * np.exp(-((XX - 10) / 3) ** 2) - 0.05 * XX / 20
+    mat["dg"]["params"].update(full2D_solverTol=TOL, full2D_solverMaxIt=300, full2D_gmresRestart=20, **extra)
+    return mat
+
+
+def _raises(identifier, **extra):
+    from real_space_dg_gb300 import WignerError
+    from real_space_dg_gb300.full2d import solve_transport_DG_full2D
+    mat = _mat(**extra)
+    rho0 = extra.pop("_rho0", None)
+    with pytest.raises(WignerError) as e:
+        solve_transport_DG_full2D(mat, None, 1.45, 1.40, rho0)
+    assert e.value.identifier == identifier, str(e.value)
+
+
+def test_dropin_rejects_bad_initial_rho():
+    from real_space_dg_gb300 import WignerError
+    from real_space_dg_gb300.full2d import solve_transport_DG_full2D
+    mat = _mat()
+    for bad in (np.zeros(7), np.full(F2.init_params_full2d(mat)["nTotal"], np.nan)):
+        with pytest.raises(WignerError) as e:
+            solve_transport_DG_full2D(mat, None, 1.45, 1.40, bad)
+        assert e.value.identifier == "DG:Full2D:InvalidInitialRho"
+
+
+def test_dropin_option_errors_before_device_work():
+    n = F2.init_params_full2d(_mat())["nTotal"]
+    _raises("DG:Full2D:GPUDirectSolverUnsupported", full2D_solver="direct")
+    _raises("DG:Full2D:UnknownSolver", full2D_solver="cgs")
+    _raises("DG:Full2D:GmresMemoryLimit", full2D_gmresMaxBasisBytes=1000.0)
+    _raises("DG:Full2D:UnsupportedPreconditioner", full2D_preconditioner="blockjacobi")
+    _raises("DG:Full2D:UnknownPreconditioner", full2D_preconditioner="ilu0")
+    _raises("DG:Full2D:UnknownSolveMode", full2D_solve="sometimes")
+    from real_space_dg_gb300 import WignerError
+    from real_space_dg_gb300.full2d import solve_transport_DG_full2D
+    mat = _mat(full2D_solver="bicgstab")
+    with pytest.raises(WignerError) as e:
+        solve_transport_DG_full2D(mat, None, 1.45, 1.40, np.zeros(n, dtype=complex))
+    assert e.value.identifier == "DG:Full2D:InitialRhoSolver"
+
+
+@pytest.mark.gpu
+def test_dropin_solve_disabled_returns_the_operator_status(built_lib):
+    from real_space_dg_gb300.full2d import solve_transport_DG_full2D
+    DG = solve_transport_DG_full2D(_mat(full2D_solve="off"), None, 1.45, 1.40)
+    assert DG["status"] == "operator-ready-solve-disabled" and DG["rho"] is None and DG["n"] is None
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("solver", ["gmres", "bicgstab"])
+def test_dropin_matches_sparse_lu(built_lib, solver):
+    import scipy.sparse.linalg as spla
+    from real_space_dg_gb300.full2d import Full2DOperator, solve_transport_DG_full2D
+    mat = _mat(full2D_solver=solver)
+    V = mat["V"]
+    p, parts, dd = F2.system(mat, V)
+    A = (F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)).tocsc()
+    with Full2DOperator(mat, V) as op:
+        rhs, _ = op.reservoir_rhs(1.45, 1.40)
+    want = spla.spsolve(A, rhs)
+    DG = solve_transport_DG_full2D(mat, V, 1.45, 1.40)
+    s = DG["info"]["solve"]
+    assert DG["status"] == "solved-" + solver and s["flag"] == 0, s
+    assert s["trueRelres"] <= TOL and s["relres"] == s["trueRelres"]
+    rv = s["resvec"]
+    assert rv.size >= 3 and abs(rv[0] - np.linalg.norm(rhs)) <= 1e-12 * rv[0] and rv[-1] <= TOL * rv[0]
+    assert np.linalg.norm(DG["rho"] - want) <= 1e-8 * np.linalg.norm(want)
+    n_ref, j_ref, nDG_ref, jx_ref = F2.observables(p, mat, want)
+    jy_ref, _ = F2.observables_y(p, mat, want)
+    assert np.linalg.norm(DG["n"] - n_ref) <= 1e-8 * np.linalg.norm(n_ref)
+    assert np.linalg.norm(DG["j"] - j_ref) <= 1e-8 * np.linalg.norm(j_ref)
+    assert np.linalg.norm(DG["jy"] - jy_ref) <= 1e-8 * max(np.linalg.norm(jy_ref), np.linalg.norm(j_ref))
+    assert DG["RHO"].shape == DG["arraySize"]
+    assert np.array_equal(DG["RHO"].reshape(-1, order="F"), DG["rho"])
+    if solver == "gmres":
+        warm = solve_transport_DG_full2D(mat, V, 1.45, 1.40, DG["rho"])
+        w = warm["info"]["solve"]
+        assert w["initialGuess"]["provided"] and w["initialGuess"]["convergedAtStart"]
+        assert w["iterations"] == [0, 0] and w["flag"] == 0
+        assert np.array_equal(warm["rho"], DG["rho"])

@@ -139,21 +139,36 @@ def test_gpu_solve_of_the_reservoir_driven_system(built_lib):
             assert np.linalg.norm(x - want) <= 1e-8 * np.linalg.norm(want)
 
 
-def test_host_observables_match_oracle():
-    """get_Observables_full2D: density at zero separation and the x current, projected onto the
-    material Y grid (odd and even rho_y counts: the exact cell and the linear bracket)."""
-    from real_space_dg_gb300.full2d import Full2DOperator, build_factors
+@pytest.mark.gpu
+def test_gpu_observables_match_oracle(built_lib):
+    """get_Observables_full2D on the device: density at zero separation, the x and y currents,
+    projected onto the material Y grid (odd and even rho_y counts: the exact cell and the linear
+    bracket), from a host state and from the resident solution of a solve."""
+    from real_space_dg_gb300.full2d import Full2DOperator
     rng = np.random.default_rng(3)
     for ybc, nry in (("periodic", 4), ("zero-inflow", 5)):
         mat = small_mat("material-default", ybc, nry=nry)
         p = F2.init_params_full2d(mat)
         rho = rng.normal(size=p["nTotal"]) + 1j * rng.normal(size=p["nTotal"])
         want = F2.observables(p, mat, rho)
-        holder = Full2DOperator.__new__(Full2DOperator)        # the host method only, no device handle
-        holder.factors, holder.mat = build_factors(mat), mat
-        got = holder.observables(rho)
-        for a, b in zip(got, want):
-            assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+        jy, jyDG = F2.observables_y(p, mat, rho)
+        with Full2DOperator(mat) as op:
+            got = op.observables(rho)
+            for a, b in zip(got, want):
+                assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+            allo = op.observables_all(rho)
+            assert np.abs(allo["jy"] - jy).max() <= 1e-13 * np.abs(jy).max()
+            assert np.abs(allo["jyDG"] - jyDG).max() <= 1e-13 * np.abs(jyDG).max()
+        # the resident solution of a solve gives the observables of the returned state
+        XX, YY = np.meshgrid(mat["x"], mat["y"], indexing="ij")
+        V = 1.424 + 0.1 * np.exp(-((XX - 10) / 3) ** 2)
+        with Full2DOperator(mat, V) as op:
+            op.set_preconditioner(fp32=True)
+            b = rng.normal(size=op.n) + 1j * rng.normal(size=op.n)
+            st, info, x = op.solve(b, tol=1e-10, maxit=100, restart=20)
+            assert st == 0
+            for a, c in zip(op.observables(), F2.observables(p, mat, x)):
+                assert np.abs(a - c).max() <= 1e-13 * np.abs(c).max()
 
 
 @pytest.mark.gpu

@@ -111,3 +111,32 @@ def test_mixed_transient_matches_fp64_and_batch_independence(built_lib):
     assert rel(nmx, n64) < 1e-7 and rel(jmx, j64) < 1e-7
     n1, j1 = out[("fp64", 1)]
     assert rel(n1[:, 0], n64[:, 0]) < 1e-12 and rel(j1[:, 0], j64[:, 0]) < 1e-12
+
+
+@pytest.mark.gpu
+def test_transient_dropin_from_init_matches_oracle(built_lib):
+    """solve_transport_DG_2D_transient_SC_new(mat, INIT): the caller's INIT (rho, the fixed
+    rhs_INIT, V_total) integrated with the reference's RK4 and refresh schedule; n and j after
+    every step, the record strides 1:50:end / 1:5:end and the final rho against the oracle
+    with the same fixed right-hand side (1e-9)."""
+    from real_space_dg_gb300.rtd import solve_transport_DG_2D_transient_SC_new
+    mat, dy, g = _state()
+    vc = np.asarray(mat["Vc"], dtype=float)
+    m = np.full(mat["Nx"], float(np.asarray(mat["me_x"]).ravel()[0]) * dg1d.M0_V)
+    V = vc - g["phi"]
+    p = dg1d.init_params(mat, vc[0] + 0.05, vc[-1] + 0.05 - 0.05, V, m)
+    _, rhs = dg1d.get_sysm(mat, p, V)
+    INIT = dict(rho=[g["rho"]], rhs=[2e-10 * rhs], V_total=-g["phi"], bias=0.05, Ef0=vc[0] + 0.05)
+    nt, dt = 60, 2e-17
+    mat2 = dict(mat, dy_norm_nm=dy, Nt=nt, dt=dt, Vd=0.15)
+    DG = solve_transport_DG_2D_transient_SC_new(mat2, INIT, transient=dict(refreshEvery=5, refreshFirst=8))
+    ref = transient1d.transient(mat, g["rho"], g["phi"], 0.15, dt, nt, dy_nm=dy, method="rk4", scale_a=2e-10,
+                                scale_rhs=1.0, refresh_every=5, refresh_first=8, fixed_rhs=2e-10 * rhs)
+    assert DG["status"] == 0 and DG["info"]["steps"] == nt
+    for t in range(nt):
+        assert rel(DG["n_all"][:, t], ref["n"][t]) < 1e-9, t
+        assert rel(DG["j_all"][:, t], ref["j"][t]) < 1e-9, t
+    assert DG["n_over_t"].shape == (ref["n"].shape[1], 1, 2) and DG["j_over_t"].shape == (ref["j"].shape[1], 12)
+    assert np.array_equal(DG["n_over_t"][:, 0, 1], DG["n_all"][:, 50])
+    assert np.array_equal(DG["j_over_t"][:, 3], DG["j_all"][:, 15])
+    assert rel(DG["rho_INIT"][0], ref["rho"]) < 1e-9
