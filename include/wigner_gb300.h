@@ -220,6 +220,12 @@ typedef struct {
                                   inexact_cap) per problem; convergence is only accepted after a solve at
                                   transport_tol with the same potential.  0: fixed transport_tol (reference) */
   double inexact_cap;          /* loosest transport tolerance of the inexact mode; 0 -> 1e-4 */
+  int defer_final;             /* inexact mode: a problem whose loop converged on a loose solve waits, frozen,
+                                  for its re-solve at transport_tol until no problem of the handle is in its
+                                  loose phase (or at most defer_final iterations), so that the long final
+                                  solves of a batch run together instead of one after another in lockstep
+                                  with the others' short ones.  Every problem's own sequence of iterates is
+                                  unchanged.  0 -> 64; < 0: no waiting */
 } wg_gummel_opts;
 
 enum { WG_GUMMEL_CONVERGED = 0, WG_GUMMEL_ITERATION_LIMIT = 1, WG_GUMMEL_TRANSPORT_FAILED = 2,

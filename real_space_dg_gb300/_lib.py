@@ -55,7 +55,7 @@ class WgGummelOpts(C.Structure):
     _fields_ = [("max_iterations", C.c_int), ("mixing", C.c_double), ("potential_tol", C.c_double),
                 ("density_tol", C.c_double), ("poisson_residual_tol", C.c_double), ("transport_tol", C.c_double),
                 ("transport_maxit", C.c_int), ("warm_start", C.c_int), ("restart_from_phi0", C.c_int),
-                ("inexact_factor", C.c_double), ("inexact_cap", C.c_double)]
+                ("inexact_factor", C.c_double), ("inexact_cap", C.c_double), ("defer_final", C.c_int)]
 
 
 class WgGummelInfo(C.Structure):

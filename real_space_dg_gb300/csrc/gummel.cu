@@ -471,6 +471,7 @@ struct LoopOpts {
   double alpha, tol_v, tol_n, tol_p, tol, cap;
   int transport_maxit;
   bool inexact;
+  int defer;   // iterations a loosely converged problem may wait for the batched final re-solve (0: none)
 };
 
 LoopOpts loop_opts(const wg_gummel_opts& o) {
@@ -487,6 +488,7 @@ LoopOpts loop_opts(const wg_gummel_opts& o) {
   // after a transport solve at the final tolerance with the same potential.
   L.inexact = o.inexact_factor > 0;
   L.cap = o.inexact_cap > 0 ? o.inexact_cap : 1e-4;
+  L.defer = !L.inexact || o.defer_final < 0 ? 0 : (o.defer_final > 0 ? o.defer_final : 64);
   return L;
 }
 
@@ -505,6 +507,7 @@ int gummel_start(Problem& P, int b, const wg_gummel_opts& o, bool warm, bool fro
   const LoopOpts L = loop_opts(o);
   GummelHost& gh = P.gh[b];
   gh.running = 1;
+  gh.waiting = -1;
   gh.it = 0;
   gh.tol = L.inexact ? std::max(L.cap, L.tol) : L.tol;
   gh.t0 = clock_s();
@@ -525,13 +528,20 @@ int gummel_iterate(Problem& P, const wg_gummel_opts& o, int* still_running) {
   const LoopOpts L = loop_opts(o);
   GummelDev& G = P.gd;
   std::vector<int> active(B, 0), mix(B, 0);
-  int n_run = 0;
+  int n_run = 0, n_loose = 0;
+  for (int b = 0; b < B; ++b) n_loose += P.gh[b].running && P.gh[b].waiting < 0;
   for (int b = 0; b < B; ++b) {
-    active[b] = P.gh[b].running;
-    n_run += active[b];
+    GummelHost& gh = P.gh[b];
+    // a problem waiting for its final re-solve runs once no other is in its loose phase or its
+    // wait is over; until then it is frozen (its iterates do not depend on when they run)
+    if (gh.running && gh.waiting >= 0 && (n_loose == 0 || gh.waiting >= L.defer)) gh.waiting = -1;
+    active[b] = gh.running && gh.waiting < 0;
+    n_run += gh.running;
   }
   *still_running = n_run;
   if (!n_run) return WG_OK;
+  for (int b = 0; b < B; ++b)
+    if (P.gh[b].running && P.gh[b].waiting >= 0) ++P.gh[b].waiting;
   std::vector<double> diag(8 * B);
   std::vector<wg_solve_info> sinfo(B);
   struct TolGuard {
@@ -586,8 +596,10 @@ int gummel_iterate(Problem& P, const wg_gummel_opts& o, int* still_running) {
     gh.running = 1;
     if (conv) {
       // converged on a loose transport solve: re-solve at the final tolerance, same potential
+      // (batched with the other problems' final solves when waiting is allowed)
       gh.tol = L.tol;
       mix[b] = 2;
+      if (L.defer > 0) gh.waiting = 0;
       continue;
     }
     if (L.inexact) gh.tol = std::min(L.cap, std::max(L.tol, o.inexact_factor * in.potential_defect));

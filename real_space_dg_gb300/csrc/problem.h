@@ -187,6 +187,7 @@ struct GummelHost {
   int it = 0;                  // iterations done
   double tol = 0;              // transport tolerance of the next solve
   double t0 = 0;               // start of the loop [s, steady clock]
+  int waiting = -1;            // >= 0: iterations spent waiting for the batched final re-solve
   wg_gummel_info info{};
 };
 

@@ -30,7 +30,8 @@ from .transport import M0, Problem1D, shape_from_mat
 DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityTolerance=5e-4,
                 poissonResidualTolerance=8e-2, transportTolerance=1e-8, transportMaxCycles=50,
                 fermiOffset=0.05, restart=50, precision="fp64", innerRestart=40, innerTol=1e-3,
-                inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0, fp64TensorCores=False)
+                inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0, fp64TensorCores=False,
+                deferFinal=0)
 
 
 def _opts(options):
@@ -96,7 +97,8 @@ class RTDSweep:
         go = _lib.WgGummelOpts(int(o["maxIterations"]), float(o["mixing"]), float(o["potentialTolerance"]),
                                float(o["densityTolerance"]), float(o["poissonResidualTolerance"]),
                                float(o["transportTolerance"]), int(o["transportMaxCycles"]), 1 if warm_start else 0,
-                               1 if restart_from_phi0 else 0, float(o["inexactFactor"]), float(o["inexactCap"]))
+                               1 if restart_from_phi0 else 0, float(o["inexactFactor"]), float(o["inexactCap"]),
+                               int(o["deferFinal"]))
         info = (_lib.WgGummelInfo * self.P.batch)()
         st = self.lib.wg_gummel_run(self.P.h, C.byref(go), info)
         self.P._check(st, allow_not_converged=True)

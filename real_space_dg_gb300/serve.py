@@ -24,14 +24,15 @@ def _gummel_opts(o):
     return _lib.WgGummelOpts(int(o["maxIterations"]), float(o["mixing"]), float(o["potentialTolerance"]),
                              float(o["densityTolerance"]), float(o["poissonResidualTolerance"]),
                              float(o["transportTolerance"]), int(o["transportMaxCycles"]), 0, 0,
-                             float(o["inexactFactor"]), float(o["inexactCap"]))
+                             float(o["inexactFactor"]), float(o["inexactCap"]), int(o["deferFinal"]))
 
 
 class Server:
     """Continuous-batching server of self-consistent RTD bias points."""
 
     def __init__(self, options=None, mem_budget_bytes=150e9, max_slots=8, warm_start=True, idle_release_s=0.5):
-        o = dict(DEFAULTS)
+        # a served request waits at most 8 Gummel iterations for its batched final re-solve (latency)
+        o = dict(DEFAULTS, deferFinal=8)
         for k, v in (options or {}).items():
             if k not in o:
                 raise WignerError(_lib.WG_ERR_ARG, "RTD:UnknownSelfConsistencyOption %s" % k)

@@ -93,7 +93,8 @@ def test_dropin_matches_sparse_lu(built_lib, solver):
     jy_ref, _ = F2.observables_y(p, mat, want)
     assert np.linalg.norm(DG["n"] - n_ref) <= 1e-8 * np.linalg.norm(n_ref)
     assert np.linalg.norm(DG["j"] - j_ref) <= 1e-8 * np.linalg.norm(j_ref)
-    assert np.linalg.norm(DG["jy"] - jy_ref) <= 1e-8 * max(np.linalg.norm(jy_ref), np.linalg.norm(j_ref))
+    # the periodic RTD carries no net y current: jy is round-off of the x-current scale on both sides
+    assert np.linalg.norm(DG["jy"] - jy_ref) <= 1e-8 * np.linalg.norm(jx_ref)
     assert DG["RHO"].shape == DG["arraySize"]
     assert np.array_equal(DG["RHO"].reshape(-1, order="F"), DG["rho"])
     if solver == "gmres":

@@ -114,3 +114,29 @@ def test_inexact_gummel_reaches_the_same_fixed_point(built_lib, precision, facto
     assert max(inexact["sweep"]["transport_relres"]) <= 1e-8
     assert np.abs(inexact["sweep"]["phi"] - exact["sweep"]["phi"]).max() < 1e-5
     assert sum(inexact["sweep"]["gmres_iterations"]) < sum(exact["sweep"]["gmres_iterations"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_deferred_final_resolves_keep_every_problems_iterates(built_lib, precision):
+    """Batching the final-tolerance re-solves (a loosely converged problem waits, frozen, until the
+    others leave their loose phase) changes when a problem's iterations run, not what they compute:
+    the same Gummel and GMRES iteration counts per problem and the same fixed point (bit-identical
+    in FP64; the mixed form's emulated residual GEMM shares column tiles between problems, 1e-10 V)."""
+    from real_space_dg_gb300 import devices
+    from real_space_dg_gb300.rtd import solve_rtd_self_consistent
+    spec, mat, E, efl, efr, m = small_rtd(n_el=10, nk=32, order=2)
+    mat = dict(mat, dy_norm_nm=devices.density_normalisation_nm(mat))
+    opts = dict(mixing=0.5, potentialTolerance=1e-6, densityTolerance=1e-5, maxIterations=150,
+                transportTolerance=1e-8, transportMaxCycles=60, precision=precision, inexactFactor=0.3,
+                inexactCap=1e-3)
+    biases = [0.02, 0.1, 0.18, 0.25]
+    now = solve_rtd_self_consistent(mat, biases, dict(opts, deferFinal=-1))
+    deferred = solve_rtd_self_consistent(mat, biases, dict(opts, deferFinal=0))
+    assert now["selfConsistency"]["converged"] and deferred["selfConsistency"]["converged"]
+    if precision == "fp64":
+        assert now["sweep"]["iterations"] == deferred["sweep"]["iterations"]
+        assert now["sweep"]["gmres_iterations"] == deferred["sweep"]["gmres_iterations"]
+        assert np.array_equal(now["sweep"]["phi"], deferred["sweep"]["phi"])
+    else:
+        assert np.abs(now["sweep"]["phi"] - deferred["sweep"]["phi"]).max() < 1e-10
