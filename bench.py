@@ -213,7 +213,7 @@ def run_ours(args, rank, world, dist):
     import __graft_entry__ as g
     g.build()
     from real_space_dg_gb300 import _lib
-    from real_space_dg_gb300.rtd import RTDSweep, solve_rtd_self_consistent
+    from real_space_dg_gb300.rtd import RTDSweep, run_concurrent, solve_rtd_self_consistent
 
     spec, mat, biases = make_workload(args.batch)
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
@@ -221,23 +221,47 @@ def run_ours(args, rank, world, dist):
                 innerReorth=args.inner_reorth, fp64TensorCores=args.fp64_tc)
     if args.max_gummel:
         opts["maxIterations"] = args.max_gummel      # profiling runs only: points need not converge
-    S = RTDSweep(mat, args.batch, opts)
-    for b, v in enumerate(biases):
-        S.set(b, v)
+    K = max(1, min(args.handles, args.batch))
+    sweeps = [RTDSweep(mat, len(range(k, args.batch, K)), opts) for k in range(K)]
+    for i, v in enumerate(biases):
+        sweeps[i % K].set(i // K, v)
+    H0 = sweeps[0].P
+
+    def step():
+        """One step: every handle's Gummel loops from phi0, the handles concurrently on their own
+        streams; device-timed by a pair of events on handle 0's stream that the other streams are
+        fenced against (they start after the first event, the second waits for all of them)."""
+        H0.event(0)
+        for sw in sweeps[1:]:
+            sw.P.wait_event(H0, 0)
+        outs = run_concurrent(sweeps, restart_from_phi0=True)
+        for sw in sweeps[1:]:
+            sw.P.event(15)
+            H0.wait_event(sw.P, 15)
+        H0.event(1)
+        info = [outs[i % K][1][i // K] for i in range(args.batch)]
+        return H0.elapsed_ms(0, 1), info
+
+    def profile(on):
+        merged = {}
+        for sw in sweeps:
+            for cls, v in sw.P.profile(on=on, reset=True).items():
+                a = merged.get(cls, (0.0, 0, 0, 0.0, 0.0))
+                merged[cls] = tuple(x + y for x, y in zip(a, v))
+        return merged
+
     for _ in range(args.warmup):
-        S.run(restart_from_phi0=True)
+        step()
     # the timed region runs without the per-launch event profiler (launches are still counted)
-    S.P.profile(on=False, reset=True)
+    profile(False)
     clocks = ClockSampler()
     clocks.start()
     barrier(dist)
     lat, pts, its, gummel_its, statuses = [], 0, 0, 0, []
     total_ms = 0.0
     for _ in range(args.steps):
-        S.P.event(0)
-        st, info = S.run(restart_from_phi0=True)
-        S.P.event(1)
-        total_ms += S.P.elapsed_ms(0, 1)
+        ms, info = step()
+        total_ms += ms
         for i in info:
             statuses.append(i["status"])
             if i["status"] == 0:
@@ -246,15 +270,15 @@ def run_ours(args, rank, world, dist):
             its += i["gmres_iterations"]
             gummel_its += i["iterations"]
     clk = clocks.stop()
-    counted = S.P.profile(on=False, reset=True)
+    counted = profile(False)
     launches = sum(v[2] for v in counted.values())
     t_max = max_over_ranks(total_ms / 1000.0, dist)
     pts_all = sum_over_ranks(pts, dist)
     value = pts_all / t_max if t_max > 0 else 0.0
     # one more step, untimed, with CUDA events around every launch: per-class rooflines
-    S.P.profile(on=True, reset=True)
-    S.run(restart_from_phi0=True)
-    prof = S.P.profile(on=False, reset=True)
+    profile(True)
+    step()
+    prof = profile(False)
     roofs = rooflines(prof, args.precision)
     if "gemm_f64_tc" in roofs:
         ncols = args.batch * SPEC["n_el"] * (SPEC["order"] + 1)
@@ -266,7 +290,7 @@ def run_ours(args, rank, world, dist):
     e2e = None
     if not args.no_e2e and rank == 0:
         t0 = time.perf_counter()
-        r = solve_rtd_self_consistent(mat, biases, opts, mode="batched")
+        r = solve_rtd_self_consistent(mat, biases, opts, mode="batched", handles=K)
         e2e_s = time.perf_counter() - t0
         nx = int(mat["Nx"])
         ncol = spec.n_el * (spec.order + 1)
@@ -275,9 +299,10 @@ def run_ours(args, rank, world, dist):
                "d2h_bytes_per_step": int(args.batch * (nx + 2 * ncol) * 8),
                "seconds": round(e2e_s, 3)}
     # the timed form's converged state (the profiled step ran the same form from the same start)
-    ours_res = [S.get(b) for b in range(args.batch)]
+    ours_res = [sweeps[i % K].get(i // K) for i in range(args.batch)]
     ours_info = info
-    S.close()
+    for sw in sweeps:
+        sw.close()
     plain = mixed_exact = accuracy = None
     if not args.no_plain and rank == 0:
         plain, mixed_exact, accuracy = other_forms(args, mat, biases, opts, ours_res, ours_info)
@@ -298,6 +323,7 @@ def run_ours(args, rank, world, dist):
         "data": "synthetic RTD device of the named shape (seeded, deterministic)",
         "config": {"workload": "C2 self-consistent RTD 80 nm, p=3, N_el=240, Nk=256, 245760 unknowns/point",
                    "batch_bias_points": args.batch, "biases_v": [round(float(b), 4) for b in biases],
+                   "handles": K, "defer_final": "64 Gummel iterations (inexact mode)",
                    "precision": args.precision, "gmres_restart": args.restart,
                    "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
                    "inexact_gummel_factor": args.inexact, "inexact_cap": args.inexact_cap, "gummel_mixing": 0.3,
@@ -318,21 +344,31 @@ def run_ours(args, rank, world, dist):
     return out
 
 
-def _run_form(mat, batch, biases, opts, phi0=None):
-    """One device-timed Gummel step of `batch` bias points in a fresh handle (untimed by the
-    headline); returns (ms, info, [(phi, n, j)] per point)."""
-    from real_space_dg_gb300.rtd import RTDSweep
-    S = RTDSweep(mat, batch, opts)
+def _run_form(mat, batch, biases, opts, phi0=None, handles=1):
+    """One device-timed Gummel step of `batch` bias points in fresh handles (the batch dealt
+    round-robin to `handles` concurrent handles, as the headline); untimed by the headline.
+    Returns (ms, info, [(phi, n, j)] per point)."""
+    from real_space_dg_gb300.rtd import RTDSweep, run_concurrent
+    K = max(1, min(handles, batch))
+    sweeps = [RTDSweep(mat, len(range(k, batch, K)), opts) for k in range(K)]
     try:
-        for b, v in enumerate(biases):
-            S.set(b, v, phi0=None if phi0 is None else phi0[b])
-        S.P.event(0)
-        st, info = S.run(restart_from_phi0=True)
-        S.P.event(1)
-        ms = S.P.elapsed_ms(0, 1)
-        res = [S.get(b) for b in range(batch)]
+        for i, v in enumerate(biases):
+            sweeps[i % K].set(i // K, v, phi0=None if phi0 is None else phi0[i])
+        H0 = sweeps[0].P
+        H0.event(0)
+        for sw in sweeps[1:]:
+            sw.P.wait_event(H0, 0)
+        outs = run_concurrent(sweeps, restart_from_phi0=True)
+        for sw in sweeps[1:]:
+            sw.P.event(15)
+            H0.wait_event(sw.P, 15)
+        H0.event(1)
+        ms = H0.elapsed_ms(0, 1)
+        info = [outs[i % K][1][i // K] for i in range(batch)]
+        res = [sweeps[i % K].get(i // K) for i in range(batch)]
     finally:
-        S.close()
+        for sw in sweeps:
+            sw.close()
     return ms, info, res
 
 
@@ -365,16 +401,17 @@ def other_forms(args, mat, biases, opts, ours_res, ours_info):
     batch = len(biases)
     fixed = dict(opts, inexactFactor=0.0)
     plain_opts = dict(fixed, precision="fp64", fp64TensorCores=True)
-    ms_p, info_p, res_p = _run_form(mat, batch, biases, plain_opts)
-    ms_m, info_m, res_m = _run_form(mat, batch, biases, dict(fixed, precision="mixed"))
+    K = args.handles
+    ms_p, info_p, res_p = _run_form(mat, batch, biases, plain_opts, handles=K)
+    ms_m, info_m, res_m = _run_form(mat, batch, biases, dict(fixed, precision="mixed"), handles=K)
     # FP64 transport at the headline's final potential: one Gummel iteration from phi0 = that
     # potential hands back the FP64 density and current of that potential, phi unchanged; solved
     # to 1e-12 (the reference solution) and to the same 1e-8 as the headline (the plain form's own
     # error at that residual)
     phis = [r[0] for r in ours_res]
     _, _, res_t = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1, transportTolerance=1e-12,
-                                                     transportMaxCycles=200), phi0=phis)
-    _, _, res_t8 = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1), phi0=phis)
+                                                     transportMaxCycles=200), phi0=phis, handles=K)
+    _, _, res_t8 = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1), phi0=phis, handles=K)
 
     def arm(ms, info, form):
         conv = sum(i["status"] == 0 for i in info)
@@ -1320,6 +1357,8 @@ def main():
                          "c4_utb: the C4 sweep with its subbands from the GPU eigensolve in every step")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--handles", type=int, default=1,
+                    help="c2: the batch dealt round-robin to this many handles run concurrently on their own streams")
     ap.add_argument("--restart", type=int, default=50)
     ap.add_argument("--inner-restart", type=int, default=40)
     ap.add_argument("--inner-tol", type=float, default=1e-3)

@@ -439,6 +439,10 @@ int wg_profile_read(wg_problem* h, double* ms, long long* timed, long long* laun
  * sequence of calls.  wg_event_elapsed waits for slot b. */
 int wg_event_record(wg_problem* h, int slot);
 int wg_event_elapsed(wg_problem* h, int a, int b, double* ms);
+/* The waiter's stream waits (on the device, the host does not block) for event
+ * `slot` last recorded on the signaler's stream: brackets work that several
+ * handles run concurrently on their own streams with one pair of events. */
+int wg_event_wait(wg_problem* waiter, wg_problem* signaler, int slot);
 
 /* ------------------------------------------------------------------------------------------------
  * Full-2D (X, Y, rho_x, rho_y) matrix-free operator: the device-resident apply that

@@ -255,6 +255,7 @@ SIGNATURES = {
     "wg_apply_repeat": ([_H, C.c_int, C.c_int, _D], C.c_int),
     "wg_event_record": ([_H, C.c_int], C.c_int),
     "wg_event_elapsed": ([_H, C.c_int, C.c_int, _D], C.c_int),
+    "wg_event_wait": ([_H, _H, C.c_int], C.c_int),
     "wg_profile_enable": ([_H, C.c_int], C.c_int),
     "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _D, _D, C.c_int], C.c_int),
 }

@@ -734,6 +734,13 @@ int wg_event_record(wg_problem* h, int slot) {
   return WG_OK;
 }
 
+int wg_event_wait(wg_problem* waiter, wg_problem* signaler, int slot) {
+  if (!waiter || !signaler || slot < 0 || slot >= 16 || !signaler->P.ev[slot])
+    return fail(waiter ? &waiter->P : nullptr, WG_ERR_ARG, "wg_event_wait: null handle or unrecorded slot");
+  API_CK(&waiter->P, cudaStreamWaitEvent(waiter->P.stream, signaler->P.ev[slot], 0));
+  return WG_OK;
+}
+
 int wg_event_elapsed(wg_problem* h, int a, int b, double* ms) {
   if (!h || !ms || a < 0 || b < 0 || a >= 16 || b >= 16 || !h->P.ev[a] || !h->P.ev[b])
     return fail(h ? &h->P : nullptr, WG_ERR_ARG, "wg_event_elapsed: unrecorded slot");

@@ -901,7 +901,14 @@ __global__ void __launch_bounds__(256) f2d_caxpy(double2* __restrict__ y, const 
 
 // |x|^2 of the dot result (real part) -> nrm[0] = sqrt
 __global__ void f2d_sqrt_real(const double2* __restrict__ d, double* __restrict__ nrm) {
-  nrm[0] = sqrt(fmax(d[0].x, 0.0));
+  nrm[0] = isnan(d[0].x) ? d[0].x : sqrt(fmax(d[0].x, 0.0));   // a NaN norm stays NaN (never "converged")
+}
+
+__global__ void __launch_bounds__(256) f2d_rscale(double2* __restrict__ v, double s, long long n) {
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  v[t].x *= s;
+  v[t].y *= s;
 }
 
 // Hessenberg column j (hc[0..j] from Gram-Schmidt, nrm[0] = |w|): previous Givens rotations, the
@@ -1785,7 +1792,7 @@ int wg2d_precondition(wg2d_problem* h, const double* r, double* z) {
 // with MATLAB's gmres semantics: relative residual of the original system, warm start as x0).
 int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_opts* opts, wg2d_solve_info* info) {
   if (!h) return WG_ERR_ARG;
-  if (!rhs || !x || !opts || !info) return fail(h, WG_ERR_ARG, "wg2d_solve: null argument");
+  if (!opts || !info) return fail(h, WG_ERR_ARG, "wg2d_solve: null argument");
   const int m = opts->restart > 0 ? opts->restart : 40;
   const int maxit = opts->maxit > 0 ? opts->maxit : 50;
   const double tol = opts->tol > 0 ? opts->tol : 1e-8;
@@ -2059,13 +2066,29 @@ int wg2d_solve_bicgstab(wg2d_problem* h, const double* rhs, double* x, const wg2
     f2d_sub<<<nb, 256, 0, h->stream>>>(h->b, h->r, n);
     return norm_of(h->r, &beta);
   };
+  // the iteration runs on the system scaled by 1/|b| (the FP32 preconditioner would overflow on
+  // the physical magnitudes, cf. the RHS normalisation of solveStationarySystem :299-304); the
+  // resident b and x are scaled back afterwards
+  const double bn = bnorm > 0 ? bnorm : 1.0;
+  f2d_rscale<<<nb, 256, 0, h->stream>>>(h->b, 1.0 / bn, n);
+  f2d_rscale<<<nb, 256, 0, h->stream>>>(h->xs, 1.0 / bn, n);
+  struct Unscale {
+    wg2d_problem* h;
+    double bn;
+    unsigned nb;
+    ~Unscale() {
+      f2d_rscale<<<nb, 256, 0, h->stream>>>(h->b, bn, h->n);
+      f2d_rscale<<<nb, 256, 0, h->stream>>>(h->xs, bn, h->n);
+    }
+  };
   rc = true_residual();
   if (rc) return rc;
-  h->resvec.push_back(beta);
+  h->resvec.push_back(beta * bn);
   info->rhs_norm = bnorm;
-  const double bn = bnorm > 0 ? bnorm : 1.0;
-  info->initial_relres = beta / bn;
-  const double target = tol * bn;
+  info->initial_relres = beta;
+  const double target = tol;
+  {
+  Unscale unscale{h, bn, nb};
   if (beta > target && std::isfinite(beta)) {
     auto cdiv = [](double2 a, double2 b) {
       const double d = b.x * b.x + b.y * b.y;
@@ -2094,7 +2117,7 @@ int wg2d_solve_bicgstab(wg2d_problem* h, const double* rhs, double* x, const wg2
       f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->r, h->w, make_double2(-alpha.x, -alpha.y), n);   // s = r - alpha v
       double sn = 0;
       if ((rc = norm_of(h->r, &sn))) return rc;
-      h->resvec.push_back(sn);
+      h->resvec.push_back(sn * bn);
       info->cycles += 1;
       if (!(sn > target) || !std::isfinite(sn)) {
         f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->xs, h->bc_ph, alpha, n);
@@ -2112,7 +2135,7 @@ int wg2d_solve_bicgstab(wg2d_problem* h, const double* rhs, double* x, const wg2
       f2d_caxpy<<<nb, 256, 0, h->stream>>>(h->r, h->z, make_double2(-omega.x, -omega.y), n);   // r = s - omega t
       double rn = 0;
       if ((rc = norm_of(h->r, &rn))) return rc;
-      h->resvec.push_back(rn);
+      h->resvec.push_back(rn * bn);
       info->cycles += 1;
       if (!(rn > target) || !std::isfinite(rn)) break;
       if (omega.x == 0.0 && omega.y == 0.0) break;
@@ -2121,13 +2144,14 @@ int wg2d_solve_bicgstab(wg2d_problem* h, const double* rhs, double* x, const wg2
     rc = true_residual();
     if (rc) return rc;
   }
+  }   // b and x scaled back
   int flag = 0;
   if (x) F2_CK(cudaMemcpyAsync(x, h->xs, sizeof(double2) * n, cudaMemcpyDeviceToHost, h->stream));
   F2_CK(cudaMemcpyAsync(&flag, h->tc_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   F2_CK(cudaStreamSynchronize(h->stream));
   if (flag) return fail(h, WG_ERR_TIMEOUT, "tensor-core GEMM: bounded barrier wait timed out");
   h->xs_ready = true;
-  info->relres = beta / bn;
+  info->relres = beta;
   if (!std::isfinite(beta)) return fail(h, WG_ERR_NUMERIC, "wg2d_solve_bicgstab: non-finite residual");
   info->flag = beta <= target ? 0 : 1;
   return info->flag ? WG_NOT_CONVERGED : WG_OK;

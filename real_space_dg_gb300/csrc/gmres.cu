@@ -815,10 +815,17 @@ void reset_graphs(ArnoldiGraphs& G) {
 // eagerly (`run`) or replayed from the chunk's CUDA graph.  A chunk is captured on its
 // second use, so the launch helpers' one-time set-up has run outside the capture; any
 // failure to capture or instantiate falls back to eager launches for the handle.
+// Chunks of a cycle: steps [0,1), [1,2), [2,4), then 4 at a time.  The host checks the
+// problems' convergence after every chunk; the short first chunks keep a cycle that
+// converges in one or two steps (loose transport tolerances) from running masked steps.
+int chunk_end(int k0, int m) { return std::min(m, k0 < 2 ? k0 + 1 : (k0 < 4 ? 4 : k0 + 4)); }
+int chunk_index(int k0) { return k0 < 2 ? k0 : (k0 < 4 ? 2 : 2 + k0 / 4); }
+int chunk_count(int m) { return m <= 2 ? m : (m <= 4 ? 3 : 2 + (m + 3) / 4); }
+
 template <typename Run>
 int run_arnoldi_chunk(Problem& P, ArnoldiGraphs& G, int m, int k0, Run run) {
   if (G.disabled || P.prof.on || !graphs_enabled()) return run();
-  const int nchunk = (m + 3) / 4, c = k0 / 4;
+  const int nchunk = chunk_count(m), c = chunk_index(k0);
   if (G.m != m || G.shift != P.shift || G.kline_L != P.kline_L || G.st_cells != P.st_cells ||
       (int)G.exec.size() != nchunk) {
     reset_graphs(G);
@@ -895,8 +902,8 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
     scale_kernel<double2, double2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, P.V, P.inv64, P.active, N,
                                                                          (long long)mp1 * N, B);
-    for (int k0 = 0; k0 < m; k0 += 4) {
-      const int k1 = std::min(m, k0 + 4);
+    for (int k0 = 0; k0 < m; k0 = chunk_end(k0, m)) {
+      const int k1 = chunk_end(k0, m);
       rc = run_arnoldi_chunk(P, P.graphs[0], m, k0, [&]() {
         for (int k = k0; k < k1; ++k) {
           const int r = arnoldi_step<double2>(P, P.V, P.w, k, m, prec, apply);
@@ -974,8 +981,8 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
     scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.V, P.inv64, P.active, N,
                                                                         (long long)mp1 * N, B);
-    for (int k0 = 0; k0 < m; k0 += 4) {
-      const int k1 = std::min(m, k0 + 4);
+    for (int k0 = 0; k0 < m; k0 = chunk_end(k0, m)) {
+      const int k1 = chunk_end(k0, m);
       rc = run_arnoldi_chunk(P, P.graphs[1], m, k0, [&]() {
         for (int k = k0; k < k1; ++k) {
           const int r = arnoldi_step<float2>(P, M.V, M.w, k, m, prec, apply);

@@ -138,8 +138,8 @@ struct Profiler {
   static constexpr int kProfSlots = 8192 + 16;
 };
 
-// CUDA graphs of the Arnoldi steps: the launches of each chunk of 4 steps (k0 .. k0+3)
-// of one restart cycle are captured once (on the chunk's second use, after the launch
+// CUDA graphs of the Arnoldi steps: the launches of each chunk of steps (steps 0, 1, 2-3,
+// then 4 at a time) of one restart cycle are captured once (on the chunk's second use, after the launch
 // helpers' one-time set-up ran eagerly) and replayed in later cycles and refinements.
 // Every kernel argument of a chunk is a device pointer or a per-handle constant except
 // the flux shift, so the graphs are rebuilt when the shift (or the restart length)

@@ -131,25 +131,55 @@ class RTDSweep:
         return st, [i.as_dict() for i in info], n, j
 
 
-def solve_rtd_self_consistent(mat, biases, options=None, mode="batched"):
+def run_concurrent(sweeps, **kw):
+    """Run the Gummel loops of several handles at once, one host thread per handle: each handle
+    works on its own CUDA stream, so the latency-bound launch chains of the handles overlap on the
+    device.  Returns [(status, info)] per handle; an error of any handle is raised."""
+    import threading
+    out = [None] * len(sweeps)
+    errors = []
+
+    def work(k):
+        try:
+            out[k] = sweeps[k].run(**kw)
+        except Exception as e:            # re-raised on the calling thread
+            errors.append(e)
+    if len(sweeps) == 1:
+        work(0)
+    else:
+        threads = [threading.Thread(target=work, args=(k,)) for k in range(len(sweeps))]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+    if errors:
+        raise errors[0]
+    return out
+
+
+def solve_rtd_self_consistent(mat, biases, options=None, mode="batched", handles=1):
     """results = solve2D_rtd_self_consistent('DG', mat, options) for the 1D path.
 
     Returns a dict with ``sweep`` (bias, current [Nxdof x nb], density, potential,
     phi, converged, iterations, status, gmres_iterations), ``Id`` (mean current per
-    bias, results.Id of the reference) and ``selfConsistency``.
+    bias, results.Id of the reference) and ``selfConsistency``.  ``handles`` (batched
+    mode): the biases are dealt round-robin to that many handles that run concurrently
+    on their own streams (each bias' result is the same as in one handle).
     """
     biases = np.atleast_1d(np.asarray(biases, dtype=float))
     nb = len(biases)
-    batch = nb if mode == "batched" else 1
-    S = RTDSweep(mat, batch, options)
+    K = max(1, min(int(handles), nb)) if mode == "batched" else 1
+    sizes = [len(range(k, nb, K)) for k in range(K)] if mode == "batched" else [1]
+    sweeps = [RTDSweep(mat, sz, options) for sz in sizes]
+    S = sweeps[0]
     sweep = {"bias": biases, "current": [], "density": [], "potential": [], "phi": [], "converged": [],
              "iterations": [], "status": [], "gmres_iterations": [], "transport_relres": []}
     try:
         if mode == "batched":
-            for b, v in enumerate(biases):
-                S.set(b, v)
-            st, info = S.run()
-            results = [(info[b], S.get(b)) for b in range(nb)]
+            for i, v in enumerate(biases):
+                sweeps[i % K].set(i // K, v)
+            outs = run_concurrent(sweeps)
+            results = [(outs[i % K][1][i // K], sweeps[i % K].get(i // K)) for i in range(nb)]
         else:
             results = []
             phi_prev = None
@@ -172,7 +202,8 @@ def solve_rtd_self_consistent(mat, biases, options=None, mode="batched"):
             sweep["gmres_iterations"].append(inf["gmres_iterations"])
             sweep["transport_relres"].append(inf["transport_relres"])
     finally:
-        S.close()
+        for sw in sweeps:
+            sw.close()
     for k in ("current", "density", "phi", "potential"):
         sweep[k] = np.array(sweep[k]).T
     Id = sweep["current"].mean(axis=0) if len(sweep["current"]) else np.array([])

@@ -185,6 +185,10 @@ class Problem1D:
         """Record CUDA event `slot` on this handle's stream."""
         self._check(self.lib.wg_event_record(self.h, int(slot)))
 
+    def wait_event(self, other, slot):
+        """This handle's stream waits on the device for event `slot` of handle `other`."""
+        self._check(self.lib.wg_event_wait(self.h, other.h, int(slot)))
+
     def elapsed_ms(self, a, b):
         ms = C.c_double()
         self._check(self.lib.wg_event_elapsed(self.h, int(a), int(b), C.byref(ms)))
