@@ -298,6 +298,7 @@ def run_ours(args, rank, world, dist):
                "h2d_bytes_per_step": int(args.batch * 6 * nx * 8),
                "d2h_bytes_per_step": int(args.batch * (nx + 2 * ncol) * 8),
                "seconds": round(e2e_s, 3)}
+    apply = whole_apply(mat, args) if rank == 0 else None
     # the timed form's converged state (the profiled step ran the same form from the same start)
     ours_res = [sweeps[i % K].get(i // K) for i in range(args.batch)]
     ours_info = info
@@ -336,12 +337,49 @@ def run_ours(args, rank, world, dist):
         "gmres_iterations_per_point": round(iters_per_point, 1),
         "gummel_iterations_per_point": round(gummel_its / max(1, len(statuses)), 2),
         "roofline": roof, "rooflines": roofs, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
-        "plain": plain, "mixed_exact_gummel": mixed_exact, "accuracy": accuracy,
+        "plain": plain, "mixed_exact_gummel": mixed_exact, "accuracy": accuracy, "apply": apply,
         "parity_note": "1D oracle parity unpinned against the reference itself (MATLAB/Octave absent, no 1D golden "
                        "vectors in the reference); pinned to the oracle restatement; the Full-2D path is pinned to "
                        "the reference's recorded Sim_Res.mat run",
     }
     return out
+
+
+def apply_bytes(batch, n_el, n_local, nk, nxi, mixed=True):
+    """Algorithmic bytes of one operator apply: read x and write y (complex, 8 B in FP32 / 16 B
+    in FP64), the potential coefficients B(x_q, xi_e) at the N_el x 10 quadrature points and N_xi + 1
+    cells (4 B BF16 complex / 16 B), and Phi (N_xi x Nk, 4 B / 16 B)."""
+    s_vec, s_coef = (8.0, 4.0) if mixed else (16.0, 16.0)
+    N = n_el * n_local * nk
+    return batch * (2.0 * N * s_vec + n_el * 10 * (nxi + 1) * s_coef) + nxi * nk * s_coef
+
+
+def whole_apply(mat, args, n_apply=50):
+    """The mixed form's inner operator apply on the full batch (all problems active), in the form
+    the Arnoldi step runs it (BF16 copy of x from the preconditioner), against the algorithmic
+    bytes of one apply."""
+    from real_space_dg_gb300.rtd import RTDSweep
+    hbm, _, src = read_peaks()
+    S = RTDSweep(mat, args.batch, dict(GUMMEL, precision="mixed"))
+    try:
+        for b, v in enumerate(0.2 * np.arange(1, args.batch + 1) / args.batch):
+            S.set(b, v)
+        S.P.apply_time("lowprec", 5)
+        ms = S.P.apply_time("lowprec", n_apply)
+        S.P.profile(on=True, reset=True)
+        S.P.apply_time("lowprec", 5)
+        prof = S.P.profile(on=False, reset=True)
+    finally:
+        S.close()
+    by = apply_bytes(args.batch, SPEC["n_el"], SPEC["order"] + 1, SPEC["nk"], SPEC["nk"])
+    launches = {k: int(v[2]) for k, v in prof.items() if v[2]}
+    return {"form": "mixed inner operator: BF16 tensor-core transforms, FP32 flux and xi stencil", "batch": args.batch,
+            "us_per_apply": round(1000.0 * ms, 2), "algorithmic_bytes": round(by),
+            "achieved_gbs": round(by / (ms / 1000.0) / 1e9, 1), "peak_gbs": hbm,
+            "frac": round(by / (ms / 1000.0) / 1e9 / hbm, 4), "peak_source": "hbm_gbs (%s)" % src,
+            "launches_per_apply": round(sum(launches.values()) / 5.0, 2),
+            "bytes_definition": "per problem 2 N x 8 B (x in, y out, FP32 complex) + N_el x 10 x (N_xi + 1) x 4 B "
+                                "(BF16 complex potential coefficients); + N_xi x Nk x 4 B (Phi)"}
 
 
 def _run_form(mat, batch, biases, opts, phi0=None, handles=1):

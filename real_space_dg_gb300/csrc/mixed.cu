@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -118,6 +119,52 @@ cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* 
   dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
   oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err, mask,
                                                                  cols_per_problem, nd, nd_pp);
+  return cudaGetLastError();
+}
+
+// GEMM 1 with the xi stencil in its epilogue (tc::gemm_stencil_kernel): yh16 from x (BF16 via tmB).
+template <int NK>
+cudaError_t launch_gemm_stencil(Problem& P, const CUtensorMap& tmB, const int* mask) {
+  MixedBuffers& M = P.mx;
+  const Shape& s = P.s;
+  static const cudaError_t attr = cudaFuncSetAttribute(tc::gemm_stencil_kernel<NK>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                       tc::ST_SMEM_BYTES);
+  if (attr != cudaSuccess) return attr;
+  constexpr int EPT = tc::BN2 / NK;
+  const long long nel = (long long)P.batch * s.n_el;
+  const unsigned grid = (unsigned)((nel + EPT - 1) / EPT);
+  tc::gemm_stencil_kernel<NK><<<grid, 128, tc::ST_SMEM_BYTES, P.stream>>>(
+      M.tmA1, tmB, M.yh16, M.beta, M.betai, s.nxi, M.ne4, nel, s.n_el, 2 * s.nk, M.err, mask);
+  return cudaGetLastError();
+}
+
+// GEMM 2 with the FP32 flux in its epilogue: y = i Phi^H Y^ + flux(x).
+template <int NK>
+cudaError_t launch_gemm_flux(Problem& P, const float2* x, float2* y, const int* mask) {
+  MixedBuffers& M = P.mx;
+  const Shape& s = P.s;
+  static const cudaError_t attr = cudaFuncSetAttribute(tc::gemm_bf16_kernel<2, NK>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+  if (attr != cudaSuccess) return attr;
+  tc::FluxEpi ep{};
+  ep.x = reinterpret_cast<const float*>(x);
+  ep.kvec = M.kvec;
+  ep.qd = M.qd;
+  for (int i = 0; i < NK * NK; ++i) {
+    ep.kp[i] = M.fb.Kp[i];
+    ep.km[i] = M.fb.Km[i];
+  }
+  for (int a = 0; a < NK; ++a) {
+    ep.k3c[a] = M.fb.K3c[a];
+    ep.k5c[a] = M.fb.K5c[a];
+  }
+  ep.n_el = s.n_el;
+  ep.shift = (float)P.shift;
+  const int Mr = 2 * s.nk;
+  dim3 grid((Mr + tc::BM - 1) / tc::BM, (unsigned)((P.ncols + tc::BN - 1) / tc::BN));
+  tc::gemm_bf16_kernel<2, NK><<<grid, 128, tc::SMEM_BYTES, P.stream>>>(
+      M.tmA2, M.tmB2, reinterpret_cast<float*>(y), Mr, P.ncols, 2 * s.nxi, M.err, mask, s.n_el * NK, ep);
   return cudaGetLastError();
 }
 
@@ -377,12 +424,49 @@ __global__ void d2f_kernel(const double* __restrict__ x, float* __restrict__ y, 
   if (t < n) y[t] = (float)x[t];
 }
 
+__global__ void to_bf16_kernel(const float4* __restrict__ x, uint2* __restrict__ xb, long long n2,
+                               const int* __restrict__ mask, long long n2_per_problem) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n2 || (mask && !mask[t / n2_per_problem])) return;
+  const float4 v = x[t];
+  bf162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+  uint2 pk;
+  pk.x = *reinterpret_cast<uint32_t*>(&lo);
+  pk.y = *reinterpret_cast<uint32_t*>(&hi);
+  xb[t] = pk;
+}
+
 template <int NK>
 cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2* y, const int* mask) {
   MixedBuffers& M = P.mx;
   if (xb && xb != M.xin16 && xb != M.zb16) return cudaErrorInvalidValue;
   const Shape& s = P.s;
   const long long BN = P.N * P.batch;
+  if (M.fused) {
+    // two launches: GEMM 1 + stencil (X^ stays in TMEM), GEMM 2 + flux (y written once)
+    const double ncols = (double)P.ncols, nxi = s.nxi, nkd = s.nk;
+    const double gemm_flops = 2.0 * (2 * nxi) * (2 * nkd) * ncols;
+    if (!xb) {
+      // the BF16 copy of x (the preconditioner writes it in the Arnoldi step)
+      cudaEvent_t ev = prof_begin(P, PROF_FLUX, 1, 12.0 * BN, 0, mask);
+      const long long n2 = BN / 2;
+      to_bf16_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, P.stream>>>(
+          reinterpret_cast<const float4*>(x), reinterpret_cast<uint2*>(M.xin16), n2, mask, P.N / 2);
+      prof_end(P, PROF_FLUX, ev);
+      xb = M.xin16;
+    }
+    cudaEvent_t ev = prof_begin(P, PROF_GEMM_BF16, 1,
+                                4.0 * BN + 4.0 * nxi * ncols + 4.0 * P.batch * s.n_el * pair_count(NK) * M.ne4,
+                                gemm_flops, mask);
+    cudaError_t e = launch_gemm_stencil<NK>(P, xb == M.xin16 ? M.tmB1n : M.tmB1zn, mask);
+    prof_end(P, PROF_GEMM_BF16, ev);
+    if (e != cudaSuccess) return e;
+    ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops, mask);
+    e = launch_gemm_flux<NK>(P, x, y, mask);
+    prof_end(P, PROF_GEMM_BF16, ev);
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+  }
   // without a BF16 copy of x the flux kernel writes one into xin16
   bf162* xb_out = xb ? nullptr : M.xin16;
   if (!xb) xb = M.xin16;
@@ -522,7 +606,15 @@ int mixed_alloc(Problem& P) {
   }
   bool ok = make_map(&M.tmA1, M.phi1, 2 * nxi, 2 * nk, tc::BM) && make_map(&M.tmB1, M.xin16, P.ncols, 2 * nk, tc::BN) &&
             make_map(&M.tmB1z, M.zb16, P.ncols, 2 * nk, tc::BN) && make_map(&M.tmA2, M.phi2, 2 * nk, 2 * nxi, tc::BM) &&
-            make_map(&M.tmB2, M.yh16, P.ncols, 2 * nxi, tc::BN);
+            make_map(&M.tmB2, M.yh16, P.ncols, 2 * nxi, tc::BN) &&
+            make_map(&M.tmB1n, M.xin16, P.ncols, 2 * nk, tc::BN2) && make_map(&M.tmB1zn, M.zb16, P.ncols, 2 * nk, tc::BN2);
+  // the fused apply keeps all 2 N_xi rows of a column tile in TMEM (at most 8 accumulators) and
+  // reads whole 64-wide k blocks; WG_FUSED_APPLY=0 selects the four-launch apply
+  {
+    const char* f = std::getenv("WG_FUSED_APPLY");
+    M.fused = !(f && f[0] == '0') && (2 * nxi) % tc::BM == 0 && 2 * nxi <= tc::BM * tc::ST_MAX_MT &&
+              (2 * nk) % tc::BK == 0;
+  }
   if (!ok) {
     P.err = "cuTensorMapEncodeTiled failed for the BF16 GEMM operands";
     return WG_ERR_CUDA;
@@ -638,7 +730,10 @@ cudaError_t apply_mixed_repeat(Problem& P, const double2* x, int n_apply) {
   cudaError_t e = mixed_sync_weights(P);
   if (e != cudaSuccess) return e;
   c2f_kernel<<<(unsigned)((n + 255) / 256), 256, 0, P.stream>>>(x, P.mx.z, n);
-  for (int i = 0; i < n_apply && e == cudaSuccess; ++i) e = launch_apply_mixed(P, P.mx.z, nullptr, P.mx.w);
+  // the BF16 copy of the input once, as the preconditioner provides it in the Arnoldi step
+  to_bf16_kernel<<<(unsigned)((n / 2 + 255) / 256), 256, 0, P.stream>>>(
+      reinterpret_cast<const float4*>(P.mx.z), reinterpret_cast<uint2*>(P.mx.zb16), n / 2, nullptr, P.N / 2);
+  for (int i = 0; i < n_apply && e == cudaSuccess; ++i) e = launch_apply_mixed(P, P.mx.z, P.mx.zb16, P.mx.w);
   return e;
 }
 

@@ -97,6 +97,8 @@ struct MixedBuffers {
   FluxBlocks32 fb;
   int* err = nullptr;                // raised by a GEMM whose barrier wait timed out
   CUtensorMap tmA1, tmB1, tmB1z, tmA2, tmB2;
+  CUtensorMap tmB1n, tmB1zn;          // the GEMM 1 B operands in 64-column boxes (fused GEMM 1 + stencil)
+  bool fused = false;                // the apply runs as GEMM 1 + stencil and GEMM 2 + flux (two launches)
   // FP64 outer residual on the tensor cores (digit slices, see ozaki.cuh)
   bool ozaki = false;
   __nv_bfloat16* oa1 = nullptr;      // [S][2 N_xi][2 Nk] digits of Phi'

@@ -111,6 +111,26 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 lanes x 4 consecutive fp32 columns of TMEM.
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
+  uint32_t r[4];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 32 lanes x 2 consecutive fp32 columns of TMEM.
+__device__ __forceinline__ void tmem_ld2(uint32_t taddr, float* v) {
+  uint32_t r[2];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0,%1}, [%2];\n" : "=r"(r[0]), "=r"(r[1]) : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  v[0] = __uint_as_float(r[0]);
+  v[1] = __uint_as_float(r[1]);
+}
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
 // 128 B, 8-row core groups 1024 B apart (stride byte offset), sm_100 version bits.
 __device__ __forceinline__ uint64_t sdesc_sw128(const void* p) {
@@ -128,13 +148,28 @@ __device__ __forceinline__ uint64_t sdesc_sw128(const void* p) {
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                             ((uint32_t)(BM >> 4) << 24);
 
-// EPI 0: D = A B.  EPI 1: D += A B.
-template <int EPI>
+// The FP32 upwind flux of the mixed form as the epilogue of GEMM 2 (EPI 2): D = A B + flux(x),
+// x laid out like D (column-major, M = 2 Nk rows interleaving re/im of k, one column per DG
+// node (element e, node a) of a problem of n_el elements with NK nodes each):
+//   flux(x)[n][r] = qd_b k_j (sum_c K(a,c) x[e,c][r] + K3c(a) x[e-1,NK-1][r] (k_j > 0) or
+//                   K5c(a) x[e+1,0][r] (k_j < 0)) + shift x[e,a][r],  j = r / 2,
+// with K = K1 + K2 for k_j > 0 and K1 - K2 for k_j < 0 (the single-node upwind coupling).
+struct FluxEpi {
+  const float* x;
+  const float* kvec;   // [M / 2]
+  const float* qd;     // [problems]
+  float kp[16], km[16], k3c[4], k5c[4];
+  int n_el;
+  float shift;
+};
+
+// EPI 0: D = A B.  EPI 1: D += A B.  EPI 2: D = A B + flux(x) (NK nodes per element).
+template <int EPI, int NK = 0>
 __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA,
                                                            const __grid_constant__ CUtensorMap tmB,
                                                            float* __restrict__ D, int M, long long Ncol, int K,
                                                            int* __restrict__ err, const int* __restrict__ mask,
-                                                           int cols_per_problem) {
+                                                           int cols_per_problem, const FluxEpi ep = FluxEpi{}) {
   // a column tile whose problems are all inactive (mask[b] == 0) has nothing to compute
   if (mask) {
     const long long c0 = (long long)blockIdx.y * BN, c1 = min(Ncol, c0 + BN) - 1;
@@ -207,6 +242,29 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
     for (int cb = 0; cb < BN / 32; ++cb) {
       float v[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, v);
+      if (EPI == 2 && row < M) {
+        // k_j > 0 for j < Nk / 2: the branch is warp-uniform when Nk is a multiple of 32
+        const float kj = ep.kvec[row >> 1];
+        const bool pos = kj > 0.f;
+        const int cpp = cols_per_problem;
+        const long long nb = n0 + cb * 32;
+        const int ncb = (int)min((long long)32, Ncol - nb);
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          if (i >= ncb) continue;
+          const long long n = nb + i;
+          const int b = (int)(n / cpp);
+          const int rem = (int)(n - (long long)b * cpp);
+          const int e = rem / NK, a = rem - e * NK;
+          const float* xc = ep.x + (n - a) * (long long)M + row;   // node 0 of element e
+          float acc = 0.f;
+#pragma unroll
+          for (int c = 0; c < NK; ++c) acc = fmaf(pos ? ep.kp[a * NK + c] : ep.km[a * NK + c], __ldg(xc + c * (long long)M), acc);
+          if (pos && e > 0) acc = fmaf(ep.k3c[a], __ldg(xc - M), acc);
+          else if (!pos && e < ep.n_el - 1) acc = fmaf(ep.k5c[a], __ldg(xc + NK * (long long)M), acc);
+          v[i] += fmaf(ep.qd[b] * kj, acc, ep.shift * __ldg(xc + a * (long long)M));
+        }
+      }
       if (row < M) {
         float* dst = D + (n0 + cb * 32) * (long long)M + row;
         const int ncb = (int)min((long long)32, Ncol - (n0 + cb * 32));
@@ -229,6 +287,189 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
   if (warp == 0) {
     fence_after();
     tmem_dealloc(tmem, BN);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// GEMM 1 with the xi stencil of the mixed form in its epilogue:
+//   X^ = Phi' x (all 2 N_xi rows of a tile of BN2 state columns, MT = 2 N_xi / 128 accumulators
+//   of 128 x BN2 in TMEM), then per element e of the tile, node a, cell s:
+//   Y_a(s) = sum_c beta_ac(s) (X_c(s) + X_c(s-1)) + beta_ac(s+1) (X_c(s) + X_c(s+1)),
+//   beta = betar (pairs a <= c stored) + i betai, written as the BF16 B operand of GEMM 2.
+// A tile holds EPT = BN2 / NK whole elements (columns n0 = tile * EPT * NK ..); its B box of BN2
+// columns may reach into the next tile, those columns are computed and not used.  TMEM lane r of
+// accumulator mt holds row 128 mt + r (row 2 s + o: o = 0 real, 1 imaginary part of cell s); warp
+// w reads lanes 32 w .. 32 w + 31, i.e. cells 16 consecutive cells; the cells at a warp's edges
+// come from the neighbouring warp through shared memory (first pass), the interior ones by
+// shuffles (second pass).  No X^ round trip through global memory.
+// ---------------------------------------------------------------------------------------------
+constexpr int BN2 = 64;
+constexpr int ST_STAGES = 3;
+constexpr int B2_STAGE = BN2 * BK * 2;       // 8 KiB
+constexpr int ST_STAGE_BYTES = A_STAGE + B2_STAGE;
+constexpr int ST_MAX_MT = 8;                  // 2 N_xi <= 1024
+constexpr int ST_EDGE_BYTES = 2 * 4 * ST_MAX_MT * BN2 * 8;
+constexpr int ST_SMEM_BYTES = ST_STAGES * ST_STAGE_BYTES + ST_EDGE_BYTES + 1024 + 256;
+constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN2 >> 3) << 17) |
+                               ((uint32_t)(BM >> 4) << 24);
+
+__host__ __device__ constexpr int st_pair_index(int nk, int a, int c) { return a * nk - a * (a - 1) / 2 + (c - a); }
+
+template <int NK>
+__global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                              const __grid_constant__ CUtensorMap tmB,
+                                                              __nv_bfloat162* __restrict__ Yh,
+                                                              const float* __restrict__ betar,
+                                                              const float* __restrict__ betai, int nxi, int ne4,
+                                                              long long n_elements, int n_el, int K,
+                                                              int* __restrict__ err, const int* __restrict__ mask) {
+  constexpr int EPT = BN2 / NK;
+  constexpr int NP = NK * (NK + 1) / 2;
+  const int MT = (2 * nxi) / BM;
+  const long long be0 = (long long)blockIdx.x * EPT;
+  if (mask) {
+    const long long be1 = min(n_elements, be0 + EPT) - 1;
+    bool any = false;
+    for (long long b = be0 / n_el; b <= be1 / n_el; ++b) any |= mask[b] != 0;
+    if (!any) return;
+  }
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  float2* edge_first = reinterpret_cast<float2*>(smem + ST_STAGES * ST_STAGE_BYTES);   // [4 MT][BN2]
+  float2* edge_last = edge_first + 4 * ST_MAX_MT * BN2;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST_STAGES * ST_STAGE_BYTES + ST_EDGE_BYTES);
+  uint64_t* empty = full + ST_STAGES;
+  uint64_t* done = empty + ST_STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n0 = (int)(be0 * NK);
+  const int nkb = K / BK;
+  const int iters = MT * nkb;
+  const uint32_t ncols_tmem = (uint32_t)(MT * BN2);   // 128, 256 or 512
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < ST_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) tmem_alloc(tmem_slot, ncols_tmem);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0 && lane == 0) {
+    // TMA producer: for every accumulator mt the A rows 128 mt .. and the B tile, k block by k block
+    for (int it = 0; it < iters; ++it) {
+      const int s = it % ST_STAGES, mt = it / nkb, kb = it - mt * nkb;
+      if (it >= ST_STAGES && !mbar_wait(&empty[s], ((it / ST_STAGES) + 1) & 1, err)) break;
+      uint8_t* a = smem + s * ST_STAGE_BYTES;
+      uint8_t* b = a + A_STAGE;
+      mbar_expect_tx(&full[s], ST_STAGE_BYTES);
+      tma_load_2d(a, &tmA, kb * BK, mt * BM, &full[s]);
+      tma_load_2d(b, &tmB, kb * BK, n0, &full[s]);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer: accumulator mt occupies TMEM columns mt * BN2 ..
+    for (int it = 0; it < iters; ++it) {
+      const int s = it % ST_STAGES, mt = it / nkb, kb = it - mt * nkb;
+      if (!mbar_wait(&full[s], (it / ST_STAGES) & 1, err)) break;
+      fence_after();
+      const uint8_t* a = smem + s * ST_STAGE_BYTES;
+      const uint8_t* b = a + A_STAGE;
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk)
+        mma_bf16(tmem + (uint32_t)(mt * BN2), sdesc_sw128(a + kk * 32), sdesc_sw128(b + kk * 32), kIdescN64,
+                 (kb | kk) != 0);
+      mma_commit(&empty[s]);
+    }
+    mma_commit(done);
+  }
+  __syncwarp();
+  const bool ok = mbar_wait(done, 0, err);
+  fence_after();
+  const bool go = ok && !*(volatile int*)err;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+  if (go) {
+    // pass 1: the first and the last cell of every warp's 16 cells, every column
+    for (int mt = 0; mt < MT; ++mt) {
+      float v[BN2];
+      tmem_ld32(tmem + lane_base + mt * BN2, v);
+      tmem_ld32(tmem + lane_base + mt * BN2 + 32, v + 32);
+      const int q = 4 * mt + warp;
+      if (lane < 2 || lane >= 30) {
+        float2* dst = lane < 2 ? edge_first + q * BN2 : edge_last + q * BN2;
+        const int comp = lane & 1;
+#pragma unroll
+        for (int c = 0; c < BN2; ++c) reinterpret_cast<float*>(dst + c)[comp] = v[c];
+      }
+    }
+  }
+  __syncthreads();
+  if (go) {
+    const int comp = lane & 1;
+    for (int mt = 0; mt < MT; ++mt) {
+      const int q = 4 * mt + warp;
+      const int s = (mt * BM + warp * 32 + lane) >> 1;        // this thread's cell
+      const bool first_cell = lane < 2, last_cell = lane >= 30;
+#pragma unroll 1
+      for (int et = 0; et < EPT; ++et) {
+        const long long be = be0 + et;
+        const bool valid = be < n_elements && (!mask || mask[be / n_el]);
+        // X^ of this element's NK columns (a 4-column load for NK = 3 stays inside the tile:
+        // its last element ends at column 62)
+        float v[4];
+        if constexpr (NK == 2) tmem_ld2(tmem + lane_base + mt * BN2 + et * NK, v);
+        else tmem_ld4(tmem + lane_base + mt * BN2 + et * NK, v);
+        float yr[NK], yi[NK];
+#pragma unroll
+        for (int a = 0; a < NK; ++a) yr[a] = yi[a] = 0.f;
+        const float* br = betar + be * NP * (long long)ne4;
+#pragma unroll
+        for (int c = 0; c < NK; ++c) {
+          const int col = et * NK + c;
+          const float own = v[c];
+          const float other = __shfl_xor_sync(0xffffffffu, own, 1);
+          const float xr = comp ? other : own, xi = comp ? own : other;
+          float mr = __shfl_up_sync(0xffffffffu, xr, 2), mi = __shfl_up_sync(0xffffffffu, xi, 2);
+          float pr = __shfl_down_sync(0xffffffffu, xr, 2), pi = __shfl_down_sync(0xffffffffu, xi, 2);
+          if (first_cell) {
+            const float2 t = q > 0 ? edge_last[(q - 1) * BN2 + col] : make_float2(0.f, 0.f);
+            mr = t.x;
+            mi = t.y;
+          }
+          if (last_cell) {
+            const float2 t = q + 1 < 4 * MT ? edge_first[(q + 1) * BN2 + col] : make_float2(0.f, 0.f);
+            pr = t.x;
+            pi = t.y;
+          }
+          const float smr = xr + mr, smi = xi + mi, spr = xr + pr, spi = xi + pi;
+          if (valid) {
+#pragma unroll
+            for (int a = 0; a < NK; ++a) {
+              const float* rr = br + st_pair_index(NK, a < c ? a : c, a < c ? c : a) * (long long)ne4;
+              const float* ri = betai + (a * NK + c) * ne4;
+              const float b0r = __ldg(rr + s), b1r = __ldg(rr + s + 1), b0i = __ldg(ri + s), b1i = __ldg(ri + s + 1);
+              yr[a] += b0r * smr - b0i * smi + b1r * spr - b1i * spi;
+              yi[a] += b0r * smi + b0i * smr + b1r * spi + b1i * spr;
+            }
+          }
+        }
+        if (valid && comp == 0) {
+#pragma unroll
+          for (int a = 0; a < NK; ++a) Yh[(be * NK + a) * nxi + s] = __floats2bfloat162_rn(yr[a], yi[a]);
+        }
+      }
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after();
+    tmem_dealloc(tmem, ncols_tmem);
   }
 }
 
