@@ -236,6 +236,22 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
   // epilogue: every warp drains its 32 TMEM lanes (rows 32w .. 32w+31)
   const bool ok = mbar_wait(done, 0, err);
   fence_after();
+  // EPI 2: the x columns the tile's flux reads (n0 - NK .. n0 + BN + NK - 1, rows m0 .. m0 + BM - 1)
+  // staged in the (now idle) operand ring, coalesced: one 512-byte column per warp access
+  float* xs = reinterpret_cast<float*>(smem);
+  if constexpr (EPI == 2) {
+    static_assert(NK == 0 || (BN + 2 * NK) * BM * 4 <= STAGES * STAGE_BYTES, "x tile must fit the stage ring");
+    __syncthreads();
+    if (ok) {
+      constexpr int NC = BN + 2 * (NK > 0 ? NK : 1);
+      for (int idx = threadIdx.x; idx < NC * BM; idx += blockDim.x) {
+        const int cl = idx / BM, r = idx - cl * BM;
+        const long long n = n0 - NK + cl;
+        xs[idx] = (n >= 0 && n < Ncol && m0 + r < M) ? __ldg(ep.x + n * (long long)M + m0 + r) : 0.f;
+      }
+    }
+    __syncthreads();
+  }
   if (ok && !*(volatile int*)err) {
     const int row = m0 + warp * 32 + lane;
 #pragma unroll 1
@@ -249,6 +265,7 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
         const int cpp = cols_per_problem;
         const long long nb = n0 + cb * 32;
         const int ncb = (int)min((long long)32, Ncol - nb);
+        const int rl = row - m0;
 #pragma unroll
         for (int i = 0; i < 32; ++i) {
           if (i >= ncb) continue;
@@ -256,13 +273,14 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
           const int b = (int)(n / cpp);
           const int rem = (int)(n - (long long)b * cpp);
           const int e = rem / NK, a = rem - e * NK;
-          const float* xc = ep.x + (n - a) * (long long)M + row;   // node 0 of element e
+          // column n - a + c of x is staged at xs[(n - a + c - (n0 - NK)) * BM + rl]
+          const float* xc = xs + (int)(n - a - (n0 - NK)) * BM + rl;   // node 0 of element e
           float acc = 0.f;
 #pragma unroll
-          for (int c = 0; c < NK; ++c) acc = fmaf(pos ? ep.kp[a * NK + c] : ep.km[a * NK + c], __ldg(xc + c * (long long)M), acc);
-          if (pos && e > 0) acc = fmaf(ep.k3c[a], __ldg(xc - M), acc);
-          else if (!pos && e < ep.n_el - 1) acc = fmaf(ep.k5c[a], __ldg(xc + NK * (long long)M), acc);
-          v[i] += fmaf(ep.qd[b] * kj, acc, ep.shift * __ldg(xc + a * (long long)M));
+          for (int c = 0; c < NK; ++c) acc = fmaf(pos ? ep.kp[a * NK + c] : ep.km[a * NK + c], xc[c * BM], acc);
+          if (pos && e > 0) acc = fmaf(ep.k3c[a], xc[-BM], acc);
+          else if (!pos && e < ep.n_el - 1) acc = fmaf(ep.k5c[a], xc[NK * BM], acc);
+          v[i] += fmaf(ep.qd[b] * kj, acc, ep.shift * xc[a * BM]);
         }
       }
       if (row < M) {
@@ -391,7 +409,8 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
   __syncwarp();
   const bool ok = mbar_wait(done, 0, err);
   fence_after();
-  const bool go = ok && !*(volatile int*)err;
+  // block-uniform, since the epilogue synchronises the block between its passes
+  const bool go = __syncthreads_and(ok && !*(volatile int*)err) != 0;
   const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
   if (go) {
     // pass 1: the first and the last cell of every warp's 16 cells, every column
@@ -409,11 +428,32 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
     }
   }
   __syncthreads();
+  // the weights of one accumulator's 64 cells (+1) for the tile's elements, staged in the idle
+  // operand ring: sbr[et][pair][65], sbi[a NK + c][65]
+  constexpr int SW = BM / 2 + 1;
+  static_assert((EPT * NP + NK * NK) * SW * 4 <= ST_STAGES * ST_STAGE_BYTES, "weights must fit the stage ring");
+  float* sbr = reinterpret_cast<float*>(smem);
+  float* sbi = sbr + EPT * NP * SW;
   if (go) {
     const int comp = lane & 1;
     for (int mt = 0; mt < MT; ++mt) {
+      const int s_lo = mt * (BM / 2);
+      for (int idx = threadIdx.x; idx < (EPT * NP + NK * NK) * SW; idx += blockDim.x) {
+        const int row = idx / SW, cs = idx - row * SW;
+        float w = 0.f;
+        if (row < EPT * NP) {
+          const int et = row / NP, p = row - et * NP;
+          const long long be = be0 + et;
+          if (be < n_elements && s_lo + cs < ne4) w = __ldg(betar + (be * NP + p) * (long long)ne4 + s_lo + cs);
+        } else if (s_lo + cs < ne4) {
+          w = __ldg(betai + (row - EPT * NP) * (long long)ne4 + s_lo + cs);
+        }
+        sbr[idx] = w;
+      }
+      __syncthreads();
       const int q = 4 * mt + warp;
       const int s = (mt * BM + warp * 32 + lane) >> 1;        // this thread's cell
+      const int sl = s - s_lo;
       const bool first_cell = lane < 2, last_cell = lane >= 30;
 #pragma unroll 1
       for (int et = 0; et < EPT; ++et) {
@@ -427,7 +467,8 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
         float yr[NK], yi[NK];
 #pragma unroll
         for (int a = 0; a < NK; ++a) yr[a] = yi[a] = 0.f;
-        const float* br = betar + be * NP * (long long)ne4;
+        const float* br = sbr + et * NP * SW + sl;
+        const float* bi = sbi + sl;
 #pragma unroll
         for (int c = 0; c < NK; ++c) {
           const int col = et * NK + c;
@@ -450,9 +491,9 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
           if (valid) {
 #pragma unroll
             for (int a = 0; a < NK; ++a) {
-              const float* rr = br + st_pair_index(NK, a < c ? a : c, a < c ? c : a) * (long long)ne4;
-              const float* ri = betai + (a * NK + c) * ne4;
-              const float b0r = __ldg(rr + s), b1r = __ldg(rr + s + 1), b0i = __ldg(ri + s), b1i = __ldg(ri + s + 1);
+              const float* rr = br + st_pair_index(NK, a < c ? a : c, a < c ? c : a) * SW;
+              const float* ri = bi + (a * NK + c) * SW;
+              const float b0r = rr[0], b1r = rr[1], b0i = ri[0], b1i = ri[1];
               yr[a] += b0r * smr - b0i * smi + b1r * spr - b1i * spi;
               yi[a] += b0r * smi + b0i * smr + b1r * spi + b1i * spr;
             }
@@ -463,6 +504,7 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
           for (int a = 0; a < NK; ++a) Yh[(be * NK + a) * nxi + s] = __floats2bfloat162_rn(yr[a], yi[a]);
         }
       }
+      __syncthreads();   // the next accumulator restages the weights
     }
   }
   fence_before();
