@@ -182,7 +182,10 @@ def rooflines(prof, precision):
         if n_t == 0 or ms <= 0:
             continue
         sec = ms / 1000.0
-        if cls == "gemm_bf16":
+        if cls in ("gemm_stencil", "gemm_flux") and by > 0:
+            # the fused apply kernels stream their operands: HBM-bound by design
+            ach, peak, bound, unit, psrc = by / sec / 1e9, hbm, "hbm", "GB/s", "hbm_gbs (%s)" % src
+        elif cls == "gemm_bf16":
             ach, peak, bound, unit, psrc = fl / sec / 1e12, bf16, "tensor", "TFLOP/s", "bf16_tflops (%s)" % src
         elif cls == "gemm_f64_tc":
             ach, peak, bound, unit = fl / sec / 1e12, bf16, "tensor", "TFLOP/s"
@@ -202,6 +205,8 @@ def rooflines(prof, precision):
              "per_launch": {"bytes": by / n_t, "flops": fl / n_t}}
         if bound == "fp64" and by > 0:
             r["hbm_frac"] = round(by / sec / 1e9 / hbm, 4)
+        if cls in ("gemm_stencil", "gemm_flux"):
+            r["tensor_frac"] = round(fl / sec / 1e12 / bf16, 4)
         if ach / peak > 1.05:
             r["flag"] = ("above 1.05 of the peak: operands served from L2 (the class's working set of the "
                          "remaining active problems fits the 129 MB L2) or misattributed work; not an HBM rate")

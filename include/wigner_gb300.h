@@ -421,10 +421,11 @@ int wg_apply_repeat(wg_problem* h, int which, int n, double* ms);
  * BF16 tensor-core GEMMs, FP32 xi stencil, k-line preconditioner, Gram-Schmidt
  * multi-dot, Gram-Schmidt update, small Krylov kernels (reductions, normalisation,
  * Givens), other, FP64 transform GEMMs emulated on the tensor cores (digit slicing +
- * slice products), FP64 upwind flux, FP64 xi stencil. */
+ * slice products), FP64 upwind flux, FP64 xi stencil, the fused mixed apply's GEMM 1 with the
+ * xi stencil in its epilogue and GEMM 2 with the FP32 flux in its epilogue. */
 enum { WG_PROF_FLUX = 0, WG_PROF_GEMM_F64, WG_PROF_GEMM_BF16, WG_PROF_STENCIL, WG_PROF_PRECOND, WG_PROF_MULTIDOT,
        WG_PROF_GSUPDATE, WG_PROF_KRYLOV, WG_PROF_OTHER, WG_PROF_GEMM_F64TC, WG_PROF_FLUX64, WG_PROF_STENCIL64,
-       WG_PROF_N };
+       WG_PROF_GEMM_STENCIL, WG_PROF_GEMM_FLUX, WG_PROF_N };
 int wg_profile_enable(wg_problem* h, int on);
 /* Arrays of WG_PROF_N entries.  ms[i]: summed event time of class i; timed[i]:
  * timed launches; launches[i]: kernel launches of class i since the last reset

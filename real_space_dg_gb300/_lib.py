@@ -260,7 +260,7 @@ SIGNATURES = {
     "wg_profile_read": ([_H, _D, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _D, _D, C.c_int], C.c_int),
 }
 PROF_CLASSES = ["flux", "gemm_f64", "gemm_bf16", "stencil", "precond", "multidot", "gs_update", "krylov_small", "other",
-                "gemm_f64_tc", "flux_f64", "stencil_f64"]
+                "gemm_f64_tc", "flux_f64", "stencil_f64", "gemm_stencil", "gemm_flux"]
 
 _lib = None
 

@@ -455,15 +455,15 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
       prof_end(P, PROF_FLUX, ev);
       xb = M.xin16;
     }
-    cudaEvent_t ev = prof_begin(P, PROF_GEMM_BF16, 1,
+    cudaEvent_t ev = prof_begin(P, PROF_GEMM_STENCIL, 1,
                                 4.0 * BN + 4.0 * nxi * ncols + 4.0 * P.batch * s.n_el * pair_count(NK) * M.ne4,
                                 gemm_flops, mask);
     cudaError_t e = launch_gemm_stencil<NK>(P, xb == M.xin16 ? M.tmB1n : M.tmB1zn, mask);
-    prof_end(P, PROF_GEMM_BF16, ev);
+    prof_end(P, PROF_GEMM_STENCIL, ev);
     if (e != cudaSuccess) return e;
-    ev = prof_begin(P, PROF_GEMM_BF16, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops, mask);
+    ev = prof_begin(P, PROF_GEMM_FLUX, 1, 4.0 * nxi * ncols + 16.0 * BN, gemm_flops, mask);
     e = launch_gemm_flux<NK>(P, x, y, mask);
-    prof_end(P, PROF_GEMM_BF16, ev);
+    prof_end(P, PROF_GEMM_FLUX, ev);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
   }

@@ -112,7 +112,8 @@ struct MixedBuffers {
 
 // Kernel classes timed and counted by the profiler.
 enum ProfClass { PROF_FLUX = 0, PROF_GEMM_F64, PROF_GEMM_BF16, PROF_STENCIL, PROF_PRECOND, PROF_MULTIDOT,
-                 PROF_GSUPDATE, PROF_KRYLOV, PROF_OTHER, PROF_GEMM_F64TC, PROF_FLUX64, PROF_STENCIL64, PROF_N };
+                 PROF_GSUPDATE, PROF_KRYLOV, PROF_OTHER, PROF_GEMM_F64TC, PROF_FLUX64, PROF_STENCIL64, PROF_GEMM_STENCIL,
+                 PROF_GEMM_FLUX, PROF_N };
 
 // CUDA-event timing of kernel classes on the handle's stream (off by default;
 // launch counts are kept always).
