@@ -134,7 +134,7 @@ cudaError_t launch_gemm_stencil(Problem& P, const CUtensorMap& tmB, const int* m
   constexpr int EPT = tc::BN2 / NK;
   const long long nel = (long long)P.batch * s.n_el;
   const unsigned grid = (unsigned)((nel + EPT - 1) / EPT);
-  tc::gemm_stencil_kernel<NK><<<grid, 128, tc::ST_SMEM_BYTES, P.stream>>>(
+  tc::gemm_stencil_kernel<NK><<<grid, tc::ST_THREADS, tc::ST_SMEM_BYTES, P.stream>>>(
       M.tmA1, tmB, M.yh16, M.beta, M.betai, s.nxi, M.ne4, nel, s.n_el, 2 * s.nk, M.err, mask);
   return cudaGetLastError();
 }
@@ -613,7 +613,7 @@ int mixed_alloc(Problem& P) {
   {
     const char* f = std::getenv("WG_FUSED_APPLY");
     M.fused = !(f && f[0] == '0') && (2 * nxi) % tc::BM == 0 && 2 * nxi <= tc::BM * tc::ST_MAX_MT &&
-              (2 * nk) % tc::BK == 0;
+              (2 * nk) % tc::BM == 0;
   }
   if (!ok) {
     P.err = "cuTensorMapEncodeTiled failed for the BF16 GEMM operands";

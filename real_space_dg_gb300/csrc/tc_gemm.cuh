@@ -122,6 +122,15 @@ __device__ __forceinline__ void tmem_ld4(uint32_t taddr, float* v) {
   for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 16-byte asynchronous global -> shared copy (zero-filled when !valid); many in flight per thread.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, bool valid) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 16 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // 32 lanes x 2 consecutive fp32 columns of TMEM.
 __device__ __forceinline__ void tmem_ld2(uint32_t taddr, float* v) {
   uint32_t r[2];
@@ -243,12 +252,16 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
     static_assert(NK == 0 || (BN + 2 * NK) * BM * 4 <= STAGES * STAGE_BYTES, "x tile must fit the stage ring");
     __syncthreads();
     if (ok) {
+      // 16-byte asynchronous copies, all issued before any is waited for (M % 128 == 0 here)
       constexpr int NC = BN + 2 * (NK > 0 ? NK : 1);
-      for (int idx = threadIdx.x; idx < NC * BM; idx += blockDim.x) {
-        const int cl = idx / BM, r = idx - cl * BM;
+      constexpr int CH = BM / 4;                       // 16-byte chunks per column
+      for (int idx = threadIdx.x; idx < NC * CH; idx += blockDim.x) {
+        const int cl = idx / CH, ch = idx - cl * CH;
         const long long n = n0 - NK + cl;
-        xs[idx] = (n >= 0 && n < Ncol && m0 + r < M) ? __ldg(ep.x + n * (long long)M + m0 + r) : 0.f;
+        const bool v = n >= 0 && n < Ncol;
+        cp_async16(xs + cl * BM + ch * 4, ep.x + (v ? n : 0) * (long long)M + m0 + ch * 4, v);
       }
+      cp_async_wait_all();
     }
     __syncthreads();
   }
@@ -270,8 +283,8 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
         for (int i = 0; i < 32; ++i) {
           if (i >= ncb) continue;
           const long long n = nb + i;
-          const int b = (int)(n / cpp);
-          const int rem = (int)(n - (long long)b * cpp);
+          const int b = (int)n / cpp;                  // 32-bit: a handle's columns fit an int
+          const int rem = (int)n - b * cpp;
           const int e = rem / NK, a = rem - e * NK;
           // column n - a + c of x is staged at xs[(n - a + c - (n0 - NK)) * BM + rl]
           const float* xc = xs + (int)(n - a - (n0 - NK)) * BM + rl;   // node 0 of element e
@@ -333,8 +346,10 @@ constexpr uint32_t kIdescN64 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(
 
 __host__ __device__ constexpr int st_pair_index(int nk, int a, int c) { return a * nk - a * (a - 1) / 2 + (c - a); }
 
+constexpr int ST_THREADS = 512;   // 16 warps: TMEM lane quarter w % 4, element group w / 4
+
 template <int NK>
-__global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(ST_THREADS, 2) gemm_stencil_kernel(const __grid_constant__ CUtensorMap tmA,
                                                               const __grid_constant__ CUtensorMap tmB,
                                                               __nv_bfloat162* __restrict__ Yh,
                                                               const float* __restrict__ betar,
@@ -360,6 +375,8 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
   uint64_t* done = empty + ST_STAGES;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wq = warp & 3, eg = warp >> 2;            // TMEM lane quarter, element group
+  constexpr int NEG = ST_THREADS / 128;               // element groups
   const int n0 = (int)(be0 * NK);
   const int nkb = K / BK;
   const int iters = MT * nkb;
@@ -411,26 +428,28 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
   fence_after();
   // block-uniform, since the epilogue synchronises the block between its passes
   const bool go = __syncthreads_and(ok && !*(volatile int*)err) != 0;
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
-  if (go) {
-    // pass 1: the first and the last cell of every warp's 16 cells, every column
+  const uint32_t lane_base = (uint32_t)(wq * 32) << 16;
+  if (go && eg == 0) {
+    // pass 1: the first and the last cell of every lane quarter's 16 cells, every column
     for (int mt = 0; mt < MT; ++mt) {
-      float v[BN2];
-      tmem_ld32(tmem + lane_base + mt * BN2, v);
-      tmem_ld32(tmem + lane_base + mt * BN2 + 32, v + 32);
-      const int q = 4 * mt + warp;
-      if (lane < 2 || lane >= 30) {
-        float2* dst = lane < 2 ? edge_first + q * BN2 : edge_last + q * BN2;
-        const int comp = lane & 1;
+      const int q = 4 * mt + wq;
+#pragma unroll 1
+      for (int half = 0; half < BN2 / 32; ++half) {
+        float v[32];
+        tmem_ld32(tmem + lane_base + mt * BN2 + half * 32, v);
+        if (lane < 2 || lane >= 30) {
+          float2* dst = (lane < 2 ? edge_first : edge_last) + q * BN2 + half * 32;
+          const int comp = lane & 1;
 #pragma unroll
-        for (int c = 0; c < BN2; ++c) reinterpret_cast<float*>(dst + c)[comp] = v[c];
+          for (int c = 0; c < 32; ++c) reinterpret_cast<float*>(dst + c)[comp] = v[c];
+        }
       }
     }
   }
   __syncthreads();
   // the weights of one accumulator's 64 cells (+1) for the tile's elements, staged in the idle
   // operand ring: sbr[et][pair][65], sbi[a NK + c][65]
-  constexpr int SW = BM / 2 + 1;
+  constexpr int SW = BM / 2 + 4;   // 65 weights (cells s_lo .. s_lo + 64) in 16-byte rows
   static_assert((EPT * NP + NK * NK) * SW * 4 <= ST_STAGES * ST_STAGE_BYTES, "weights must fit the stage ring");
   float* sbr = reinterpret_cast<float*>(smem);
   float* sbi = sbr + EPT * NP * SW;
@@ -438,25 +457,31 @@ __global__ void __launch_bounds__(128, 1) gemm_stencil_kernel(const __grid_const
     const int comp = lane & 1;
     for (int mt = 0; mt < MT; ++mt) {
       const int s_lo = mt * (BM / 2);
-      for (int idx = threadIdx.x; idx < (EPT * NP + NK * NK) * SW; idx += blockDim.x) {
-        const int row = idx / SW, cs = idx - row * SW;
-        float w = 0.f;
+      // rows of ne4 floats (ne4 % 4 == 0, s_lo % 64 == 0, s_lo + SW <= ne4): 16-byte aligned chunks,
+      // asynchronous copies all in flight before the wait
+      constexpr int CH = SW / 4;
+      for (int idx = threadIdx.x; idx < (EPT * NP + NK * NK) * CH; idx += blockDim.x) {
+        const int row = idx / CH, ch = idx - row * CH;
+        const float* src;
+        bool v = true;
         if (row < EPT * NP) {
           const int et = row / NP, p = row - et * NP;
           const long long be = be0 + et;
-          if (be < n_elements && s_lo + cs < ne4) w = __ldg(betar + (be * NP + p) * (long long)ne4 + s_lo + cs);
-        } else if (s_lo + cs < ne4) {
-          w = __ldg(betai + (row - EPT * NP) * (long long)ne4 + s_lo + cs);
+          v = be < n_elements;
+          src = betar + ((v ? be : 0) * NP + p) * (long long)ne4 + s_lo + ch * 4;
+        } else {
+          src = betai + (row - EPT * NP) * (long long)ne4 + s_lo + ch * 4;
         }
-        sbr[idx] = w;
+        cp_async16(sbr + row * SW + ch * 4, src, v);
       }
+      cp_async_wait_all();
       __syncthreads();
-      const int q = 4 * mt + warp;
-      const int s = (mt * BM + warp * 32 + lane) >> 1;        // this thread's cell
+      const int q = 4 * mt + wq;
+      const int s = (mt * BM + wq * 32 + lane) >> 1;          // this thread's cell
       const int sl = s - s_lo;
       const bool first_cell = lane < 2, last_cell = lane >= 30;
 #pragma unroll 1
-      for (int et = 0; et < EPT; ++et) {
+      for (int et = eg; et < EPT; et += NEG) {
         const long long be = be0 + et;
         const bool valid = be < n_elements && (!mask || mask[be / n_el]);
         // X^ of this element's NK columns (a 4-column load for NK = 3 stays inside the tile:
