@@ -144,7 +144,7 @@ template <int NK>
 cudaError_t launch_gemm_flux(Problem& P, const float2* x, float2* y, const int* mask) {
   MixedBuffers& M = P.mx;
   const Shape& s = P.s;
-  static const cudaError_t attr = cudaFuncSetAttribute(tc::gemm_bf16_kernel<2, NK>,
+  static const cudaError_t attr = cudaFuncSetAttribute(tc::gemm_bf16_kernel<2, NK, 256>,
                                                        cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
   if (attr != cudaSuccess) return attr;
   tc::FluxEpi ep{};
@@ -163,7 +163,7 @@ cudaError_t launch_gemm_flux(Problem& P, const float2* x, float2* y, const int* 
   ep.shift = (float)P.shift;
   const int Mr = 2 * s.nk;
   dim3 grid((Mr + tc::BM - 1) / tc::BM, (unsigned)((P.ncols + tc::BN - 1) / tc::BN));
-  tc::gemm_bf16_kernel<2, NK><<<grid, 128, tc::SMEM_BYTES, P.stream>>>(
+  tc::gemm_bf16_kernel<2, NK, 256><<<grid, 256, tc::SMEM_BYTES, P.stream>>>(
       M.tmA2, M.tmB2, reinterpret_cast<float*>(y), Mr, P.ncols, 2 * s.nxi, M.err, mask, s.n_el * NK, ep);
   return cudaGetLastError();
 }

@@ -173,8 +173,9 @@ struct FluxEpi {
 };
 
 // EPI 0: D = A B.  EPI 1: D += A B.  EPI 2: D = A B + flux(x) (NK nodes per element).
-template <int EPI, int NK = 0>
-__global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA,
+// THREADS / 128 warps share each TMEM lane quarter in the epilogue and split its column chunks.
+template <int EPI, int NK = 0, int THREADS = 128>
+__global__ void __launch_bounds__(THREADS, 2) gemm_bf16_kernel(const __grid_constant__ CUtensorMap tmA,
                                                            const __grid_constant__ CUtensorMap tmB,
                                                            float* __restrict__ D, int M, long long Ncol, int K,
                                                            int* __restrict__ err, const int* __restrict__ mask,
@@ -266,11 +267,12 @@ __global__ void __launch_bounds__(128, 2) gemm_bf16_kernel(const __grid_constant
     __syncthreads();
   }
   if (ok && !*(volatile int*)err) {
-    const int row = m0 + warp * 32 + lane;
+    const int wq = warp & 3, cg = warp >> 2;
+    const int row = m0 + wq * 32 + lane;
 #pragma unroll 1
-    for (int cb = 0; cb < BN / 32; ++cb) {
+    for (int cb = cg; cb < BN / 32; cb += THREADS / 128) {
       float v[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + cb * 32, v);
+      tmem_ld32(tmem + ((uint32_t)(wq * 32) << 16) + cb * 32, v);
       if (EPI == 2 && row < M) {
         // k_j > 0 for j < Nk / 2: the branch is warp-uniform when Nk is a multiple of 32
         const float kj = ep.kvec[row >> 1];
