@@ -1400,7 +1400,7 @@ def main():
                          "c4_utb: the C4 sweep with its subbands from the GPU eigensolve in every step")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
     ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--handles", type=int, default=1,
+    ap.add_argument("--handles", type=int, default=8,
                     help="c2: the batch dealt round-robin to this many handles run concurrently on their own streams")
     ap.add_argument("--restart", type=int, default=50)
     ap.add_argument("--inner-restart", type=int, default=40)

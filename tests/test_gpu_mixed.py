@@ -163,3 +163,31 @@ def test_mixed_rejects_unsupported_shapes(built_lib):
     spec, mat, E, efl, efr, m = small_rtd(n_el=10, nk=16, order=2)
     with pytest.raises(WignerError):
         make(spec, "mixed")
+
+
+@pytest.mark.parametrize("order", [1, 2, 3])
+def test_fused_apply_matches_the_four_launch_apply(built_lib, order, monkeypatch):
+    """The opt-in two-launch apply (GEMM 1 with the xi stencil in its TMEM epilogue, GEMM 2 with
+    the flux in its epilogue, WG_FUSED_APPLY=1) computes the same low-precision operator as the
+    four-launch apply (the same BF16 operands and FP32 arithmetic in another order: 1e-3 relative),
+    and the mixed solve built on it reaches the sparse-LU bars (density 1e-8, current 1e-7)."""
+    spec, mat, E, efl, efr, m = small_rtd(n_el=10, nk=128, order=order)
+    p = dg1d.init_params(mat, efl, efr, E, m)
+    A, rhs = dg1d.get_sysm(mat, p, E)
+    rng = np.random.default_rng(order)
+    out = {}
+    for fused in ("0", "1"):
+        monkeypatch.setenv("WG_FUSED_APPLY", fused)
+        with make(spec, "mixed") as P:
+            P.set_potential(0, mat["x"], E, m, spec.m_rel, spec.temp_k, efl, efr)
+            x = rng.standard_normal(P.N) + 1j * rng.standard_normal(P.N) if fused == "0" else out["x"]
+            out["x"] = x
+            out[fused] = P.apply_lowprec(x)
+            if fused == "1":
+                st, info = P.solve(tol=1e-10, maxit=40)
+                assert st == 0 and info[0]["relres"] <= 1e-10
+                n, j = P.observables(0)
+    assert rel(out["1"], out["0"]) < 1e-3
+    ref = spla.spsolve(A.tocsc(), rhs)
+    n_ref, j_ref, _ = dg1d.observables(p, ref, dg1d.node_map(p, m))
+    assert rel(n, n_ref) < 1e-8 and rel(j, j_ref) < 1e-7
