@@ -232,14 +232,19 @@ def run_ours(args, rank, world, dist):
         sweeps[i % K].set(i // K, v)
     H0 = sweeps[0].P
 
-    def step():
+    def step(concurrent=True):
         """One step: every handle's Gummel loops from phi0, the handles concurrently on their own
         streams; device-timed by a pair of events on handle 0's stream that the other streams are
-        fenced against (they start after the first event, the second waits for all of them)."""
+        fenced against (they start after the first event, the second waits for all of them).
+        concurrent=False runs the handles one after another (the per-launch profile, whose event
+        times would otherwise include the other streams' kernels)."""
         H0.event(0)
         for sw in sweeps[1:]:
             sw.P.wait_event(H0, 0)
-        outs = run_concurrent(sweeps, restart_from_phi0=True)
+        if concurrent:
+            outs = run_concurrent(sweeps, restart_from_phi0=True)
+        else:
+            outs = [sw.run(restart_from_phi0=True) for sw in sweeps]
         for sw in sweeps[1:]:
             sw.P.event(15)
             H0.wait_event(sw.P, 15)
@@ -280,16 +285,18 @@ def run_ours(args, rank, world, dist):
     t_max = max_over_ranks(total_ms / 1000.0, dist)
     pts_all = sum_over_ranks(pts, dist)
     value = pts_all / t_max if t_max > 0 else 0.0
-    # one more step, untimed, with CUDA events around every launch: per-class rooflines
+    # one more step, untimed, with CUDA events around every launch and the handles run one after
+    # another: per-class rooflines of the kernels the timed steps run, free of the other streams
     profile(True)
-    step()
+    step(concurrent=False)
     prof = profile(False)
     roofs = rooflines(prof, args.precision)
     if "gemm_f64_tc" in roofs:
-        ncols = args.batch * SPEC["n_el"] * (SPEC["order"] + 1)
+        ncols = len(range(0, args.batch, K)) * SPEC["n_el"] * (SPEC["order"] + 1)
         roofs["gemm_f64_tc"]["traffic"] = round(OZAKI_TRAFFIC_PER_COLUMN * ncols)
         roofs["gemm_f64_tc"]["traffic_source"] = ("ncu dram bytes of one slicing + emulated GEMM event at batch 8, "
-                                                  "scaled by columns to batch %d" % args.batch)
+                                                  "scaled by columns to a handle of %d problems"
+                                                  % len(range(0, args.batch, K)))
     roof = max(roofs.values(), key=lambda r: r["share"]) if roofs else None
     # e2e: the public call with host inputs and outputs, every step
     e2e = None
@@ -330,6 +337,7 @@ def run_ours(args, rank, world, dist):
         "config": {"workload": "C2 self-consistent RTD 80 nm, p=3, N_el=240, Nk=256, 245760 unknowns/point",
                    "batch_bias_points": args.batch, "biases_v": [round(float(b), 4) for b in biases],
                    "handles": K, "defer_final": "64 Gummel iterations (inexact mode)",
+                   "profile": "rooflines from one extra step with per-launch CUDA events, handles run one after another",
                    "precision": args.precision, "gmres_restart": args.restart,
                    "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
                    "inexact_gummel_factor": args.inexact, "inexact_cap": args.inexact_cap, "gummel_mixing": 0.3,

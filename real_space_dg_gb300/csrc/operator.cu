@@ -257,17 +257,25 @@ __global__ void __launch_bounds__(kFluxThreads) stencil_kernel(const double2* __
   }
   const double* br = betar + (long long)be * NK * NK * ne;
   double2* Y = yh + (long long)be * NK * nxi;
+  // beta = betar + i betai with both parts real: Y = R + i I, R = sum betar (.), I = sum betai (.),
+  // 8 FP64 FMAs per (a, c) instead of two complex products; the CAP part betai vanishes outside
+  // the absorbing layers of the xi interval, where its FMAs are skipped (FP64-bound kernel)
 #pragma unroll
   for (int a = 0; a < NK; ++a) {
-    double2 v = make_double2(0.0, 0.0);
+    double2 vr = make_double2(0.0, 0.0), vi = make_double2(0.0, 0.0);
 #pragma unroll
     for (int c = 0; c < NK; ++c) {
       const int ac = a * NK + c;
-      const double2 b0 = make_double2(br[ac * ne + s], betai[ac * ne + s]);
-      const double2 b1 = make_double2(br[ac * ne + s + 1], betai[ac * ne + s + 1]);
-      v = cadd(v, cadd(cmul(b0, sm[c]), cmul(b1, sp[c])));
+      const double r0 = br[ac * ne + s], r1 = br[ac * ne + s + 1];
+      vr.x = fma(r0, sm[c].x, fma(r1, sp[c].x, vr.x));
+      vr.y = fma(r0, sm[c].y, fma(r1, sp[c].y, vr.y));
+      const double i0 = betai[ac * ne + s], i1 = betai[ac * ne + s + 1];
+      if (i0 != 0.0 || i1 != 0.0) {
+        vi.x = fma(i0, sm[c].x, fma(i1, sp[c].x, vi.x));
+        vi.y = fma(i0, sm[c].y, fma(i1, sp[c].y, vi.y));
+      }
     }
-    Y[a * nxi + s] = v;
+    Y[a * nxi + s] = make_double2(vr.x - vi.y, vr.y + vi.x);
   }
 }
 

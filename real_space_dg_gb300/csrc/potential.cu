@@ -220,7 +220,9 @@ __device__ double v_lookup(double x, const double* __restrict__ xg, const double
   return slope[lo] * (x - xg[lo]) + vg[lo];
 }
 
-// beta[b][e][ac][s] = (dxi/4) mpc sum_q kap[ac][q] (V(x_q + xi_s/2) - V(x_q - xi_s/2))
+// beta[b][e][ac][s] = (dxi/4) mpc sum_q kap[ac][q] (V(x_q + xi_s/2) - V(x_q - xi_s/2)).
+// The xi edges are symmetric about 0 (xi_{ne-1-s} = -xi_s up to the rounding of their grid), so
+// the difference is odd in xi: one thread computes the edges s and ne-1-s (FP64-bound kernel).
 template <int NK>
 __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ xq, const double* __restrict__ xi_edge,
                           const double* __restrict__ kap, const double* __restrict__ pot_x,
@@ -228,12 +230,13 @@ __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ 
                           const double* __restrict__ pp, int nx, int n_el, int nxi, double scale, int b0,
                           const int* __restrict__ mask) {
   if (mask && !mask[b0 + blockIdx.y]) return;
-  const int ne = nxi + 1;
+  const int ne = nxi + 1, nh = (ne + 1) / 2;
   const int b = b0 + blockIdx.y;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long long)n_el * ne) return;
-  const int s = (int)(t % ne);
-  const int e = (int)(t / ne);
+  if (t >= (long long)n_el * nh) return;
+  const int s = (int)(t % nh);
+  const int e = (int)(t / nh);
+  const int sm = ne - 1 - s;   // the mirrored edge (== s at the centre of an odd edge count)
   const double xi = xi_edge[s];
   const double* xg = pot_x + (long long)b * nx;
   const double* vg = pot_v + (long long)b * nx;
@@ -258,8 +261,13 @@ __global__ void vw_kernel(double* __restrict__ beta, const double* __restrict__ 
       double acc = 0.0;
 #pragma unroll
       for (int q = 0; q < kNqx; ++q) acc += kap[(a * NK + c) * kNqx + q] * dv[q];
-      be[(long long)(a * NK + c) * ne + s] = acc * scale;
-      if (c != a) be[(long long)(c * NK + a) * ne + s] = acc * scale;
+      acc *= scale;
+      be[(long long)(a * NK + c) * ne + s] = acc;
+      if (c != a) be[(long long)(c * NK + a) * ne + s] = acc;
+      if (sm != s) {
+        be[(long long)(a * NK + c) * ne + sm] = -acc;
+        if (c != a) be[(long long)(c * NK + a) * ne + sm] = -acc;
+      }
     }
 }
 
@@ -278,7 +286,7 @@ cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask)
   inflow_kernel<<<dim3((s.nk + 7) / 8, nb), 256, 0, P.stream>>>(P.fxi, P.pinv, P.kvec, P.pp, P.rhs, P.fb, s.nk,
                                                                   s.nxi, s.n_el, P.N, s.q_diff, s.mpc, b0, mask);
   const int ne = s.nxi + 1;
-  dim3 g((unsigned)(((long long)s.n_el * ne + 127) / 128), nb);
+  dim3 g((unsigned)(((long long)s.n_el * ((ne + 1) / 2) + 127) / 128), nb);
   const double scale = s.delta_xi / 4 * s.mpc;
   switch (s.nK) {
     case 2: vw_kernel<2><<<g, 128, 0, P.stream>>>(P.beta, P.xq, P.xi_edge, P.kap, P.pot_x, P.pot_v, P.vslope, P.pp,
