@@ -483,23 +483,6 @@ __global__ void __launch_bounds__(256) scale_kernel(const S* __restrict__ src, D
   st2(dst[(long long)b * dst_stride + n], make_double2(v.x * inv, v.y * inv));
 }
 
-// dst = src * inv[b]  (inverse norm computed once per problem)
-template <typename T, typename S>
-__global__ void __launch_bounds__(256) scale_inv_kernel(const T* __restrict__ src, T* __restrict__ dst,
-                                                        const S* __restrict__ inv, const int* __restrict__ active,
-                                                        long long N, long long dst_stride, int batch) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= N * batch) return;
-  const int b = (int)(t / N);
-  if (!active[b]) return;
-  const long long n = t - (long long)b * N;
-  const S f = inv[b];
-  T v = src[t];
-  v.x *= f;
-  v.y *= f;
-  dst[(long long)b * dst_stride + n] = v;
-}
-
 __global__ void __launch_bounds__(256) residual_kernel(const double2* __restrict__ rhs, const double2* __restrict__ ax,
                                                        double2* __restrict__ r, long long total, long long N,
                                                        const int* __restrict__ mask) {
@@ -623,8 +606,19 @@ template <> float2* coef_col32<float2>(Problem& P) { return P.mx.hcol; }
 template <typename T, typename Prec, typename Apply>
 int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   const int B = P.batch, mp1 = m + 1, ps = P.restart_max + 1, mm = P.restart_max;
-  const long long N = P.N, tot = N * B;
-  WG_CK(prec(V + (long long)k * N, (long long)mp1 * N));
+  const long long N = P.N;
+  // V_k: step 0 reads the basis vector the cycle start wrote; later steps take the previous
+  // step's w and its inverse norm, and the preconditioner writes V_k = w / |w| as it reads it
+  // (no separate scaling pass per step)
+  if (k == 0) {
+    WG_CK(prec(V, (long long)mp1 * N, nullptr, nullptr));
+  } else {
+    const T* wprev = w;
+    if constexpr (std::is_same<T, float2>::value)
+      WG_CK(prec(wprev, N, P.mx.inv, V + (long long)k * N));
+    else
+      WG_CK(prec(wprev, N, P.inv64, V + (long long)k * N));
+  }
   WG_CK(apply());
   const int nv = k + 1;
   const double sz = (double)sizeof(T), vec = (double)N * B * sz;
@@ -660,17 +654,7 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
                                                              ps, P.nblk, tl);
     prof_end(P, PROF_GSUPDATE, ev);
   }
-  // V_{k+1} = w / |w| for the problems still iterating
-  cudaEvent_t ev = prof_begin(P, PROF_KRYLOV, 1, 2 * vec, 0, P.active);
-  if (sizeof(T) == sizeof(float2))
-    scale_inv_kernel<float2, float><<<blocks_for(tot), 256, 0, P.stream>>>(
-        reinterpret_cast<const float2*>(w), reinterpret_cast<float2*>(V) + (long long)(k + 1) * N, P.mx.inv,
-        P.active, N, (long long)mp1 * N, B);
-  else
-    scale_inv_kernel<double2, double><<<blocks_for(tot), 256, 0, P.stream>>>(
-        reinterpret_cast<const double2*>(w), reinterpret_cast<double2*>(V) + (long long)(k + 1) * N, P.inv64,
-        P.active, N, (long long)mp1 * N, B);
-  prof_end(P, PROF_KRYLOV, ev);
+  // V_{k+1} = w / |w| is written by the next step's preconditioner
   WG_CK(cudaGetLastError());
   return WG_OK;
 }
@@ -892,7 +876,9 @@ int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_inf
   WG_CK(cudaMemcpyAsync(P.target, tgt.data(), sizeof(double) * B, cudaMemcpyHostToDevice, P.stream));
   std::vector<int> iters(B, 0), cycles(B, 0), refs(B, 0);
   std::vector<double> res = initial;
-  auto prec = [&](const double2* r, long long stride) { return launch_precondition(P, r, stride, P.z); };
+  auto prec = [&](const double2* r, long long stride, const double* rscale, double2* rout) {
+    return launch_precondition(P, r, stride, P.z, rscale, rout, (long long)mp1 * N);
+  };
   auto apply = [&]() { return launch_apply(P, P.z, P.w); };
   for (int cyc = 0; cyc < maxit; ++cyc) {
     bool any = false;
@@ -957,8 +943,8 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
   std::vector<int> iters(B, 0), cycles(B, 0), refs(B, 0);
   std::vector<double> res = initial, itgt(B), ones(B, 1.0);
   // the inner Arnoldi steps skip problems that have converged in this cycle (P.active)
-  auto prec = [&](const float2* r, long long stride) {
-    return launch_precondition_mixed(P, r, stride, M.z, M.zb16, P.active);
+  auto prec = [&](const float2* r, long long stride, const float* rscale, float2* rout) {
+    return launch_precondition_mixed(P, r, stride, M.z, M.zb16, P.active, rscale, rout, (long long)mp1 * N);
   };
   auto apply = [&]() { return launch_apply_mixed(P, M.z, M.zb16, M.w, P.active); };
   for (int ref = 0; ref < max_ref; ++ref) {

@@ -13,6 +13,8 @@
 //                       into its incoming s, then sweeps its chunk writing z.
 // Threads: x = 32 consecutive k (coalesced rows), y = 4 chunks; grid
 // (ceil(nk/32), ceil(n_chunks/4), batch) covers every SM even for one problem.
+// Optional: r enters scaled by rscale[b] (the Arnoldi step's w / |w|), and the apply kernel
+// writes the scaled r to rout (the next basis vector), which replaces a separate scaling pass.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -35,7 +37,8 @@ template <int NK, typename R>
 __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
     const typename Cplx<R>::type* __restrict__ r, const R* __restrict__ kvec, const R* __restrict__ dinv,
     const R* __restrict__ hvec, const R* __restrict__ qd, R* __restrict__ mapA, typename Cplx<R>::type* __restrict__ mapS,
-    int n_el, int nk, long long N, long long r_stride, int L, int nchunk, const int* __restrict__ mask) {
+    int n_el, int nk, long long N, long long r_stride, int L, int nchunk, const int* __restrict__ mask,
+    const R* __restrict__ rscale = nullptr) {
   using T = typename Cplx<R>::type;
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int c = blockIdx.y * kChunksPerBlock + threadIdx.y;
@@ -44,6 +47,7 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
   const long long bj = (long long)b * nk + j;
   const bool fwd = kvec[j] > R(0);
   const int st = fwd ? NK - 1 : 0;
+  const R sc = rscale ? rscale[b] : R(1);   // r enters scaled (the basis vector w / |w|)
   R Dst[NK];
 #pragma unroll
   for (int q = 0; q < NK; ++q) Dst[q] = dinv[bj * NK * NK + st * NK + q];
@@ -65,8 +69,8 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
       ux += Dst[q] * rv.x;
       uy += Dst[q] * rv.y;
     }
-    s.x = ux * inv_qd + alpha * s.x;
-    s.y = uy * inv_qd + alpha * s.y;
+    s.x = ux * sc * inv_qd + alpha * s.x;
+    s.y = uy * sc * inv_qd + alpha * s.y;
     A *= alpha;
   }
   const long long m = ((long long)b * nchunk + c) * nk + j;
@@ -80,7 +84,8 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
     __nv_bfloat162* __restrict__ zb, const R* __restrict__ kvec, const R* __restrict__ dinv,
     const R* __restrict__ hvec, const R* __restrict__ qd, const R* __restrict__ mapA,
     const typename Cplx<R>::type* __restrict__ mapS, int n_el, int nk, long long N, long long r_stride, int L,
-    int nchunk, const int* __restrict__ mask) {
+    int nchunk, const int* __restrict__ mask, const R* __restrict__ rscale = nullptr,
+    typename Cplx<R>::type* __restrict__ rout = nullptr, long long rout_stride = 0) {
   using T = typename Cplx<R>::type;
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int c = blockIdx.y * kChunksPerBlock + threadIdx.y;
@@ -117,15 +122,25 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
 #pragma unroll
   for (int q = 0; q < NK; ++q) h[q] = hvec[bj * NK + q];
   const R inv_qd = qd[b] > R(0) ? rcp(qd[b]) : R(0);
+  const R sc = rscale ? rscale[b] : R(1);
   const int e_lo = c * L, e_hi = min(n_el, e_lo + L);
   const T* rb = r + (long long)b * r_stride + j;
   T* zbase = z + (long long)b * N + j;
+  T* obase = rout ? rout + (long long)b * rout_stride + j : nullptr;
   for (int i = 0; i < e_hi - e_lo; ++i) {
     const int e = fwd ? e_lo + i : e_hi - 1 - i;
     const T* re = rb + (long long)e * NK * nk;
     T rv[NK];
 #pragma unroll
-    for (int q = 0; q < NK; ++q) rv[q] = re[(long long)q * nk];
+    for (int q = 0; q < NK; ++q) {
+      rv[q] = re[(long long)q * nk];
+      if (rscale) {
+        rv[q].x *= sc;
+        rv[q].y *= sc;
+      }
+      // the scaled input is the next Krylov basis vector: written here, so no separate pass
+      if (obase) obase[(long long)e * NK * nk + (long long)q * nk] = rv[q];
+    }
     T snew = s;
 #pragma unroll
     for (int a = 0; a < NK; ++a) {

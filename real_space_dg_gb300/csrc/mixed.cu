@@ -497,18 +497,21 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
 }
 
 template <int NK>
-cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb, const int* mask) {
+cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb, const int* mask,
+                             const float* rscale, float2* rout, long long rout_stride) {
   const int L = P.kline_L, nc = kline::chunk_count_for(P.s.n_el, L);
   const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
   const dim3 block(32, kline::kChunksPerBlock);
   float* ma = static_cast<float*>(P.kmap_a);
   float2* ms = static_cast<float2*>(P.kmap_s);
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, (zb ? 28.0 : 24.0) * P.N * P.batch, 0, mask);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, ((zb ? 28.0 : 24.0) + (rout ? 8.0 : 0.0)) * P.N * P.batch, 0, mask);
   kline::kline_maps_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, ma, ms,
-                                                                    P.s.n_el, P.s.nk, P.N, r_stride, L, nc, mask);
+                                                                    P.s.n_el, P.s.nk, P.N, r_stride, L, nc, mask,
+                                                                    rscale);
   kline::kline_apply_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h,
                                                                      P.mx.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
-                                                                     r_stride, L, nc, mask);
+                                                                     r_stride, L, nc, mask, rscale, rout,
+                                                                     rout_stride);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
@@ -761,11 +764,12 @@ cudaError_t launch_stencil_mixed(Problem& P) {
 }
 
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
-                                      __nv_bfloat162* zb, const int* mask) {
+                                      __nv_bfloat162* zb, const int* mask, const float* rscale, float2* rout,
+                                      long long rout_stride) {
   switch (P.s.nK) {
-    case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb, mask);
-    case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb, mask);
-    default: return precond_mixed_nk<4>(P, r, r_stride, z, zb, mask);
+    case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
+    case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
+    default: return precond_mixed_nk<4>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
   }
 }
 

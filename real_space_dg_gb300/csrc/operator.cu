@@ -360,19 +360,21 @@ cudaError_t apply_nk(Problem& P, const double2* x, double2* y) {
 }
 
 template <int NK>
-cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2* z) {
+cudaError_t precond_nk(Problem& P, const double2* r, long long r_stride, double2* z, const double* rscale,
+                       double2* rout, long long rout_stride) {
   const int L = P.kline_L, nc = kline::chunk_count_for(P.s.n_el, L);
   const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
   const dim3 block(32, kline::kChunksPerBlock);
   double* ma = static_cast<double*>(P.kmap_a);
   double2* ms = static_cast<double2*>(P.kmap_s);
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, 48.0 * P.N * P.batch);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, (48.0 + (rout ? 16.0 : 0.0)) * P.N * P.batch);
   kline::kline_maps_kernel<NK, double><<<grid, block, 0, P.stream>>>(r, P.kvec, P.pre_dinv, P.pre_h, P.qd, ma, ms,
                                                                      P.s.n_el, P.s.nk, P.N, r_stride, L, nc,
-                                                                     nullptr);
+                                                                     nullptr, rscale);
   kline::kline_apply_kernel<NK, double><<<grid, block, 0, P.stream>>>(r, z, nullptr, P.kvec, P.pre_dinv, P.pre_h,
                                                                       P.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
-                                                                      r_stride, L, nc, nullptr);
+                                                                      r_stride, L, nc, nullptr, rscale, rout,
+                                                                      rout_stride);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
@@ -526,11 +528,12 @@ cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const
   return cudaGetLastError();
 }
 
-cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z) {
+cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z, const double* rscale,
+                                double2* rout, long long rout_stride) {
   switch (P.s.nK) {
-    case 2: return precond_nk<2>(P, r, r_stride, z);
-    case 3: return precond_nk<3>(P, r, r_stride, z);
-    default: return precond_nk<4>(P, r, r_stride, z);
+    case 2: return precond_nk<2>(P, r, r_stride, z, rscale, rout, rout_stride);
+    case 3: return precond_nk<3>(P, r, r_stride, z, rscale, rout, rout_stride);
+    default: return precond_nk<4>(P, r, r_stride, z, rscale, rout, rout_stride);
   }
 }
 

@@ -308,7 +308,10 @@ void prof_release(Problem& P);
 
 // Kernel launchers (operator.cu)
 cudaError_t launch_apply(Problem& P, const double2* x, double2* y);
-cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z);
+// rscale (device, optional): r enters scaled by rscale[b]; rout (optional): the scaled r is written there
+// (per-problem stride rout_stride), the Arnoldi step's next basis vector.
+cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride, double2* z,
+                                const double* rscale = nullptr, double2* rout = nullptr, long long rout_stride = 0);
 // k-line factors of A + sigma I for every problem (sigma = P.shift), uploaded to pre_dinv / pre_h.
 int set_kline_factors(Problem& P);
 // Device bytes of a handle before allocation (the admission estimate of wg_problem_create).
@@ -342,7 +345,8 @@ cudaError_t mixed_sync_weights(Problem& P);
 cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162* xb, float2* y,
                                const int* mask = nullptr);
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
-                                      __nv_bfloat162* zb, const int* mask = nullptr);
+                                      __nv_bfloat162* zb, const int* mask = nullptr, const float* rscale = nullptr,
+                                      float2* rout = nullptr, long long rout_stride = 0);
 // The FP32 xi stencil alone (M.xh -> M.yh16, every problem), for the autotuner.
 cudaError_t launch_stencil_mixed(Problem& P);
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);
