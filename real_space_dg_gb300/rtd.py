@@ -19,6 +19,7 @@ Two sweep modes:
   * ``batched``: every bias is an independent problem of one handle and all
     Gummel loops advance together on the GPU (initial phi = bias * ramp).
 """
+import atexit
 import ctypes as C
 
 import numpy as np
@@ -31,7 +32,7 @@ DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityT
                 poissonResidualTolerance=8e-2, transportTolerance=1e-8, transportMaxCycles=50,
                 fermiOffset=0.05, restart=50, precision="fp64", innerRestart=40, innerTol=1e-3,
                 inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0, fp64TensorCores=False,
-                deferFinal=0)
+                deferFinal=0, keepHandles=True)
 
 
 def _opts(options):
@@ -45,11 +46,16 @@ def _opts(options):
     return o
 
 
+def _grid_key(mat):
+    """What a handle's device buffers are sized and its operator shape is built from (the node
+    positions, masses and potentials are per problem, set by ``set``)."""
+    return tuple(sorted(shape_from_mat(mat).items())) + (int(mat["Nx"]), int(mat["Ny"]))
+
+
 class RTDSweep:
     """A handle of `batch` RTD problems with their Gummel state resident on the GPU."""
 
     def __init__(self, mat, batch, options=None):
-        self.mat = mat
         self.o = _opts(options)
         shp = shape_from_mat(mat)
         self.P = Problem1D(batch=batch, precision=self.o["precision"], restart=self.o["restart"],
@@ -58,6 +64,15 @@ class RTDSweep:
                            fp64_tc=self.o["fp64TensorCores"], **shp)
         self.lib = self.P.lib
         self.nx = int(mat["Nx"])
+        self.grid = _grid_key(mat)
+        self.bind(mat)
+
+    def bind(self, mat):
+        """The device description (band edge, doping, permittivity, masses, ramp) that ``set``
+        gives every problem without a ``mat`` of its own; ``mat`` has this handle's grid."""
+        if _grid_key(mat) != self.grid:
+            raise WignerError(_lib.WG_ERR_ARG, "bind: the device needs the node count and shape of this handle")
+        self.mat = mat
         self.dy = float(mat.get("dy_norm_nm") or devices.density_normalisation_nm(mat, self.o["fermiOffset"]))
         x = np.ascontiguousarray(mat["x"], dtype=float)
         m = np.ascontiguousarray(np.asarray(mat["me_x"], dtype=float).reshape(-1, self.nx, int(mat["Ny"]))[0, :, 0]
@@ -157,6 +172,30 @@ def run_concurrent(sweeps, **kw):
     return out
 
 
+_KEPT = {"key": None, "sweeps": []}
+
+
+def _take_kept(key):
+    """The kept handles when they match ``key`` (taken out, so that a concurrent call cannot
+    share them), else None."""
+    if _KEPT["key"] != key:
+        return None
+    sweeps = _KEPT["sweeps"]
+    _KEPT.update(key=None, sweeps=[])
+    return sweeps
+
+
+def release_handles():
+    """Close the handles solve_rtd_self_consistent keeps for its next call."""
+    sweeps = _KEPT["sweeps"]
+    _KEPT.update(key=None, sweeps=[])
+    for sw in sweeps:
+        sw.close()
+
+
+atexit.register(release_handles)
+
+
 def solve_rtd_self_consistent(mat, biases, options=None, mode="batched", handles=1):
     """results = solve2D_rtd_self_consistent('DG', mat, options) for the 1D path.
 
@@ -165,12 +204,34 @@ def solve_rtd_self_consistent(mat, biases, options=None, mode="batched", handles
     bias, results.Id of the reference) and ``selfConsistency``.  ``handles`` (batched
     mode): the biases are dealt round-robin to that many handles that run concurrently
     on their own streams (each bias' result is the same as in one handle).
+
+    ``keepHandles`` (option, default on): the handles stay open after the call and serve the
+    next call with the same shape, batch layout and options (another device of the same node
+    count included), which then skips their allocation and set-up; every problem still starts
+    from its own phi0 = bias * ramp with a zero Wigner function, so the results are those of
+    fresh handles.  One set is kept; ``release_handles()`` frees it.
     """
     biases = np.atleast_1d(np.asarray(biases, dtype=float))
     nb = len(biases)
+    o = _opts(options)
     K = max(1, min(int(handles), nb)) if mode == "batched" else 1
     sizes = [len(range(k, nb, K)) for k in range(K)] if mode == "batched" else [1]
-    sweeps = [RTDSweep(mat, sz, options) for sz in sizes]
+    keep = bool(o["keepHandles"])
+    key = (_grid_key(mat), tuple(sizes), repr(sorted((k, v) for k, v in o.items() if k != "keepHandles")))
+    sweeps = _take_kept(key) if keep else None
+    if sweeps is None:
+        release_handles()
+        sweeps = []
+        try:
+            for sz in sizes:
+                sweeps.append(RTDSweep(mat, sz, o))
+        except BaseException:
+            for sw in sweeps:
+                sw.close()
+            raise
+    else:
+        for sw in sweeps:
+            sw.bind(mat)
     S = sweeps[0]
     sweep = {"bias": biases, "current": [], "density": [], "potential": [], "phi": [], "converged": [],
              "iterations": [], "status": [], "gmres_iterations": [], "transport_relres": []}
@@ -201,7 +262,13 @@ def solve_rtd_self_consistent(mat, biases, options=None, mode="batched", handles
             sweep["status"].append(_lib.GUMMEL_STATUS.get(inf["status"], str(inf["status"])))
             sweep["gmres_iterations"].append(inf["gmres_iterations"])
             sweep["transport_relres"].append(inf["transport_relres"])
-    finally:
+    except BaseException:
+        for sw in sweeps:
+            sw.close()
+        raise
+    if keep:
+        _KEPT.update(key=key, sweeps=sweeps)
+    else:
         for sw in sweeps:
             sw.close()
     for k in ("current", "density", "phi", "potential"):

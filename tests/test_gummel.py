@@ -140,3 +140,40 @@ def test_deferred_final_resolves_keep_every_problems_iterates(built_lib, precisi
         assert np.array_equal(now["sweep"]["phi"], deferred["sweep"]["phi"])
     else:
         assert np.abs(now["sweep"]["phi"] - deferred["sweep"]["phi"]).max() < 1e-10
+
+
+@pytest.mark.gpu
+def test_kept_handles_give_the_results_of_fresh_handles(built_lib):
+    """solve_rtd_self_consistent keeps its handles for the next call with the same shape, layout and
+    options; a kept set rebound to another device of the same node count, and back, reproduces the
+    fresh handles' sweep bit for bit (FP64: the same launches on the same inputs)."""
+    from real_space_dg_gb300 import devices, rtd
+    mats = []
+    for barrier in (0.3, 0.2):
+        spec, mat, E, efl, efr, m = small_rtd(n_el=10, nk=32, order=2, barrier_ev=barrier)
+        mats.append(dict(mat, dy_norm_nm=devices.density_normalisation_nm(mat)))
+    opts = dict(mixing=0.5, potentialTolerance=1e-6, densityTolerance=1e-5, maxIterations=150,
+                transportTolerance=1e-8, transportMaxCycles=60, precision="fp64")
+    biases = [0.05, 0.1, 0.2]
+    try:
+        fresh = [rtd.solve_rtd_self_consistent(M, biases, dict(opts, keepHandles=False), handles=2) for M in mats]
+        assert rtd._KEPT["sweeps"] == []
+        first = rtd.solve_rtd_self_consistent(mats[0], biases, opts, handles=2)
+        kept = list(rtd._KEPT["sweeps"])
+        assert len(kept) == 2
+        other = rtd.solve_rtd_self_consistent(mats[1], biases, opts, handles=2)
+        again = rtd.solve_rtd_self_consistent(mats[0], biases, opts, handles=2)
+        assert rtd._KEPT["sweeps"] == kept            # the same handles served all three calls
+        for got, want in ((first, fresh[0]), (other, fresh[1]), (again, fresh[0])):
+            assert got["selfConsistency"]["converged"]
+            assert got["sweep"]["iterations"] == want["sweep"]["iterations"]
+            assert got["sweep"]["gmres_iterations"] == want["sweep"]["gmres_iterations"]
+            for k in ("phi", "density", "current"):
+                assert np.array_equal(got["sweep"][k], want["sweep"][k]), k
+        assert np.abs(fresh[0]["sweep"]["phi"] - fresh[1]["sweep"]["phi"]).max() > 1e-3   # two devices
+        rtd.solve_rtd_self_consistent(mats[0], biases[:2], opts, handles=2)           # another layout
+        assert rtd._KEPT["sweeps"] and all(a is not b for a in rtd._KEPT["sweeps"] for b in kept)
+        assert all(sw.P.h is None for sw in kept)     # the replaced set was closed
+    finally:
+        rtd.release_handles()
+    assert rtd._KEPT["sweeps"] == []
