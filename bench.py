@@ -224,7 +224,8 @@ def run_ours(args, rank, world, dist):
     spec, mat, biases = make_workload(args.batch)
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
                 innerTol=args.inner_tol, inexactFactor=args.inexact, inexactCap=args.inexact_cap, reorth=args.reorth,
-                innerReorth=args.inner_reorth, fp64TensorCores=args.fp64_tc)
+                innerReorth=args.inner_reorth, fp64TensorCores=args.fp64_tc,
+                innerBasisFP32=args.inner_basis_fp32)
     if args.max_gummel:
         opts["maxIterations"] = args.max_gummel      # profiling runs only: points need not converge
     K = max(1, min(args.handles, args.batch))
@@ -286,7 +287,7 @@ def run_ours(args, rank, world, dist):
             its += i["gmres_iterations"]
             gummel_its += i["iterations"]
     clk = clocks.stop()
-    rs = H0.runtime_stats()
+    rs = H0.runtime_stats
     shapes = {"kline_chunk": rs["kline_chunk"], "stencil_cells": rs["stencil_cells"],
               "source": "pinned (--launch-shapes)" if args.launch_shapes else "autotuned"}
     counted = profile(False)
@@ -366,6 +367,7 @@ def run_ours(args, rank, world, dist):
                    "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
                    "inexact_gummel_factor": args.inexact, "inexact_cap": args.inexact_cap, "gummel_mixing": 0.3,
                    "reorth": args.reorth, "inner_reorth": args.inner_reorth, "fp64_tensor_cores": args.fp64_tc,
+                   "inner_basis": "fp32" if args.inner_basis_fp32 else "fp16 storage, fp32 arithmetic",
                    "potential_tol_v": 1e-6, "transport_rtol": 1e-8,
                    "l2": "inputs larger than L2 (Krylov basis %.2f GB)" %
                          (16.0 * (args.restart + 1) * args.batch * spec.n_el * (spec.order + 1) * spec.nk / 1e9)},
@@ -1454,6 +1456,8 @@ def main():
                     help="DGKS re-orthogonalisation threshold of the FP64 Arnoldi (0: 1/sqrt(2), <0 never, >=1 always)")
     ap.add_argument("--inner-reorth", type=float, default=0.0,
                     help="the same for the mixed form's inner FP32 Arnoldi (0: never, one classical pass)")
+    ap.add_argument("--inner-basis-fp32", action="store_true",
+                    help="mixed form: keep the inner Krylov basis in FP32 (default: FP16 storage, FP32 arithmetic)")
     ap.add_argument("--fp64-tc", action="store_true",
                     help="plain FP64 form with its two transforms as FP64 emulated on the tensor cores")
     ap.add_argument("--cpu-iters", type=int, default=8)

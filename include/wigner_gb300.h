@@ -86,6 +86,10 @@ typedef struct {
                           refinement keeps the accuracy; a second pass measured 25% slower, same iterations) */
   int fp64_tc;       /* FP64 handles: 1 = the two Phi transforms as FP64 products emulated on the tensor cores
                         (8-digit slices, ~1e-14 of |Phi| |x|, 2 Nk and 2 N_xi <= 1024); 0 = native FP64 (default) */
+  int inner_basis_fp32; /* mixed form: 1 keeps the inner Krylov basis in FP32; 0 (default) stores it in FP16
+                           with FP32 arithmetic (the preconditioner works on the stored FP16 vector; the FP64
+                           refinement keeps the accuracy; C2: the same inner iteration counts, half the basis
+                           traffic of the Gram-Schmidt kernels) */
 } wg_params;
 
 /* One problem's device/material data on the material grid (mat.x, nm). */
@@ -493,6 +497,15 @@ int wg2d_set_drift(wg2d_problem* h, const double* interp, const double* proj, co
  * rebuilds the vertex potential differences V(X + rho/2) - V(X - rho/2) on the device with X clamped
  * and Y clamped or wrapped (get_Drift_full2D.m:620-666). */
 int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const double* gy, const double* V);
+
+/* Hard-wall Y boundary (full2D_Y_boundary = 'hard-wall'; replaces constrain_HardWall_full2D.m:1-44 with
+ * get_HardWallGeometry_full2D.m:15-48): every apply becomes T A (mask u) + scale (u - mask u).
+ * active [nY][n_rho_y] (1: the sample's two particle coordinates Y +- rho_y/2 lie inside the Y
+ * interval); projection [n_el_y][n_rho_y][nk_y][nk_y] row-major: per Y element and rho_y cell the
+ * exact-DG-mass projection M(keep,keep)^-1 M(keep,:) on the element's nodes (zero rows for inactive
+ * nodes); scale: the weight of the constraint rows.  The transport terms must not carry the Y
+ * boundary penalty (the reference drops it for hard walls).  active = NULL removes the wall. */
+int wg2d_set_hard_wall(wg2d_problem* h, const unsigned char* active, const double* projection, double scale);
 
 /* y = A x on host buffers (n = n_rho_x n_rho_y n_X n_Y complex entries). */
 int wg2d_apply(wg2d_problem* h, const double* x, double* y);

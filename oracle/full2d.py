@@ -19,8 +19,10 @@ stationary Full-2D Wigner operator A = A_diff + G_drift:
     core/get_CAP_full2D.m, core/get_CAP.m.
 
 Scope: the source/drain faces fully open (all contact-mask entries 1, so no
-closed-face reflection parts); Y boundaries 'periodic', 'zero-inflow' or
-'specular'; constant-mass transport; FV-consistent potential.  The reservoir
+closed-face reflection parts); Y boundaries 'periodic', 'zero-inflow',
+'specular' or 'hard-wall' (core/get_HardWallGeometry_full2D.m,
+core/constrain_HardWall_full2D.m: the two-point Dirichlet constraint of the
+complete operator); constant-mass transport; FV-consistent potential.  The reservoir
 right-hand side (get_ContactModeReservoirRho_full2D.m) is not part of the operator.
 """
 import numpy as np
@@ -107,7 +109,8 @@ def y_boundary_type(mat):
     """core/get_YBoundaryType_full2D.m (default 'specular')."""
     v = str(mat["dg"]["params"].get("full2D_Y_boundary", "specular")).strip().lower()
     return {"specular-reflection": "specular", "reflection": "specular", "reflecting": "specular",
-            "zero_inflow": "zero-inflow", "zeroinflow": "zero-inflow", "zero": "zero-inflow"}.get(v, v)
+            "zero_inflow": "zero-inflow", "zeroinflow": "zero-inflow", "zero": "zero-inflow",
+            "hardwall": "hard-wall", "hard_wall": "hard-wall", "dirichlet": "hard-wall"}.get(v, v)
 
 
 def one_dimensional_dg_operators(ax):
@@ -420,6 +423,86 @@ def apply_system(p, parts, dd, u):
     return apply_kron(parts, u, p["nCenterDof"], p["nRelative"]) + apply_drift(p, dd, u)
 
 
+# ----------------------------------------------------------------------------- hard-wall Y boundary
+
+def hard_wall_geometry(p, scales):
+    """core/get_HardWallGeometry_full2D.m:15-48 and constrain_HardWall_full2D.m:10-18.
+
+    active [N_rho_y, nYdof]: the samples whose two particle coordinates Y +- rho_y/2 lie strictly
+    inside the Y interval (64 ulp of the largest coordinate as margin); T: per Y element and rho_y
+    cell, the exact-DG-mass projection M(keep,keep)^-1 M(keep,:) onto the element's active nodes
+    (rows of inactive nodes zero), on the (rho_y fastest, Y node) index; scale: the constraint
+    row weight max(1, |Qx| / (min dX * d_rho_x) + |Qy| / (min dY * d_rho_y))."""
+    rho = p["rhoY"]["cells"]
+    Y = p["Y"]["nodes"]
+    y0, y1 = p["y"][0], p["y"][-1]
+    big = max(abs(y0), abs(y1), float(np.max(np.abs(rho))))
+    tol = 64 * np.spacing(big)
+    dist = np.minimum(Y - y0, y1 - Y)
+    active = np.abs(rho)[:, None] / 2 < dist[None, :] - tol
+    if not active.any():
+        raise ValueError("DG:Full2D:HardWallEmptyDomain")
+    nr, ny, nl = len(rho), len(Y), p["Y"]["nLocal"]
+    M = p["Y"]["M"]
+    T = sp.lil_matrix((nr * ny, nr * ny))
+    for e in range(p["Y"]["nElements"]):
+        yids = e * nl + np.arange(nl)
+        for ir in range(nr):
+            keep = active[ir, yids]
+            if keep.any():
+                ids = ir + nr * yids
+                T[np.ix_(ids[keep], ids)] = np.linalg.solve(M[np.ix_(keep, keep)], M[keep, :])
+    sx, sy = scales
+    g = max(1.0, abs(sx) / (np.min(np.diff(p["X"]["vertices"])) * p["rhoX"]["delta"])
+            + abs(sy) / (np.min(np.diff(p["Y"]["vertices"])) * p["rhoY"]["delta"]))
+    return dict(active=active, T=sp.csr_matrix(T), scale=g)
+
+
+def _wall_order(p):
+    """Permutation taking the global index (rho_x, rho_y, X, Y) to (rho_y, Y) x (rho_x, X) blocks."""
+    nrx, nry = p["rhoX"]["nCells"], p["rhoY"]["nCells"]
+    nx, ny = p["X"]["nDof"], p["Y"]["nDof"]
+    idx = np.arange(nrx * nry * nx * ny).reshape(ny, nx, nry, nrx)     # C order: rho_x fastest
+    # rows (X, rho_x) with rho_x fastest, columns (Y, rho_y) with rho_y fastest (T's index)
+    return idx.transpose(1, 3, 0, 2).reshape(nx * nrx, ny * nry)
+
+
+def wall_active_mask(p, wall):
+    """The active flag of every global unknown (maskInput of constrain_HardWall_full2D.m:46-50)."""
+    nrx, nx = p["rhoX"]["nCells"], p["X"]["nDof"]
+    nry, ny = p["rhoY"]["nCells"], p["Y"]["nDof"]
+    m = np.broadcast_to(wall["active"].T[:, None, :, None], (ny, nx, nry, nrx))
+    return m.reshape(-1).astype(float)
+
+
+def wall_project(p, wall, u):
+    """applyTransverse (constrain_HardWall_full2D.m:52-57): T on the (rho_y, Y) index of u."""
+    order = _wall_order(p)
+    U = np.asarray(u)[order]                           # [(rho_x, X), (rho_y, Y)]
+    out = np.empty_like(np.asarray(u), dtype=complex)
+    out[order] = (wall["T"] @ U.T).T
+    return out
+
+
+def apply_hard_wall(p, wall, apply_base, u):
+    """constrainedApply (constrain_HardWall_full2D.m:40-44): T A (mask u) + scale (u - mask u)."""
+    act = wall_active_mask(p, wall)
+    um = np.asarray(u) * act
+    return wall_project(p, wall, apply_base(um)) + wall["scale"] * (np.asarray(u) - um)
+
+
+def constrain_hard_wall(p, wall, A):
+    """constrainedMatrix (constrain_HardWall_full2D.m:65-72): T A P + scale (I - P), T lifted."""
+    n = p["nTotal"]
+    act = wall_active_mask(p, wall)
+    order = _wall_order(p)
+    nb = order.shape[0]
+    Tl = sp.kron(wall["T"], sp.identity(nb), format="coo")        # index (rho_y,Y) * nb + (rho_x,X)
+    flat = order.T.reshape(-1)                                       # position (rho_y,Y)*nb + (rho_x,X)
+    T = sp.csr_matrix((Tl.data, (flat[Tl.row], flat[Tl.col])), shape=(n, n))
+    return (T @ A @ sp.diags(act) + wall["scale"] * sp.diags(1 - act)).tocsr()
+
+
 # ----------------------------------------------------------------------------- line-transverse preconditioner
 
 def transverse_reference(mat, V, ix=0):
@@ -490,9 +573,13 @@ def line_transverse(mat, p, V, dd, ix=0):
     sigma = _param(prm, "full2D_lineShift", _param(prm, "full2D_lineRelativeShift", 0.003) * max(x_rate, t_rate,
                                                                                                np.finfo(float).tiny))
     xinv, xcpl, fwd = x_factors(p["X"], sx * lam, sigma)
+    wall = hard_wall_geometry(p, transport_scales(mat)) if p["ytype"] == "hard-wall" else None
     Binv = np.zeros((nm, nT, nT), dtype=complex)
     for k in range(nm):
         B = K + pw[k] * Vt + np.diag(capY + capX[k])
+        if wall is not None:            # get_LineTransversePreconditioner_full2D.m:84-88
+            act = wall["active"].T.reshape(-1).astype(float)        # (rho_y fastest, Y) index
+            B = wall["T"].toarray() @ B @ np.diag(act) + wall["scale"] * np.diag(1 - act)
         B = B / sigma + np.eye(nT)
         Binv[k] = np.linalg.solve(B, np.eye(nT))
     return dict(U=U, lam=lam, sigma=sigma, xinv=xinv, xcpl=xcpl, fwd=fwd, Binv=Binv, K=K, Vt=Vt, pw=pw,

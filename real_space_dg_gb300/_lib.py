@@ -26,7 +26,7 @@ class WgParams(C.Structure):
                 ("l_xi", C.c_double), ("m_diff", C.c_double), ("mpc", C.c_double), ("precision", C.c_int),
                 ("restart", C.c_int), ("mem_budget_bytes", C.c_double), ("inner_restart", C.c_int),
                 ("inner_tol", C.c_double), ("reorth", C.c_double), ("inner_reorth", C.c_double),
-                ("fp64_tc", C.c_int)]
+                ("fp64_tc", C.c_int), ("inner_basis_fp32", C.c_int)]
 
 
 class WgDevice(C.Structure):
@@ -192,6 +192,7 @@ SIGNATURES = {
     "wg2d_set_transport": ([_H, C.c_int, C.c_int, _D, _D, C.POINTER(C.c_int), C.POINTER(C.c_int), _D], C.c_int),
     "wg2d_set_drift": ([_H, _D, _D, _D, _D, _D, _D, _D, C.c_double, _D], C.c_int),
     "wg2d_set_potential": ([_H, C.c_int, C.c_int, _D, _D, _D], C.c_int),
+    "wg2d_set_hard_wall": ([_H, C.c_void_p, _D, C.c_double], C.c_int),
     "wg2d_apply": ([_H, _D, _D], C.c_int),
     "wg2d_apply_repeat": ([_H, C.c_int, _D, _D], C.c_int),
     "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D, C.c_int], C.c_int),

@@ -88,14 +88,15 @@ bool inv_small(const double* A, double* out, int n) {
 
 namespace wg {
 
-double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc) {
+double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc,
+                      bool basis16) {
   const int nK = s.nK;
   const double N = (double)s.n_el * nK * s.nk, BN = N * batch, ncols = (double)batch * s.n_el * nK;
   const double nx = (double)s.n_el * (nK - 1) + 1;
   double est = 16.0 * BN * (5 + restart + 1) + 16.0 * 2 * s.nxi * ncols +
                8.0 * batch * s.n_el * nK * nK * (s.nxi + 1) + 16.0 * s.nxi * s.nk;
   est += 8.0 * batch * (nx * (8 + 2 * kMaxLocal) + 3.0 * s.n_el * nK + 12);   // Gummel state
-  if (precision == WG_PREC_MIXED) est += mixed_bytes(s, batch, restart_inner);
+  if (precision == WG_PREC_MIXED) est += mixed_bytes(s, batch, restart_inner, basis16);
   if (precision == WG_PREC_MIXED || fp64_tc)   // digit slices of the FP64 emulation
     est += 2.0 * 8 * ncols * 2 * std::max(s.nk, s.nxi) + 2.0 * 2 * 8 * 4.0 * s.nxi * s.nk;
   return est;
@@ -221,7 +222,9 @@ int wg_problem_create(const wg_params* prm, int batch, wg_problem** out) {
   const int pst = P.restart_max + 1;
   // memory estimate before allocating (GmresMemoryLimit analogue)
   P.fp64_tc = prm->fp64_tc != 0 && P.precision == WG_PREC_FP64;
-  const double est = wg::estimate_bytes(s, batch, P.restart, P.restart_inner, P.precision, P.fp64_tc);
+  P.inner_basis16 = prm->inner_basis_fp32 == 0;
+  const double est = wg::estimate_bytes(s, batch, P.restart, P.restart_inner, P.precision, P.fp64_tc,
+                                        P.inner_basis16);
   if (P.mem_budget > 0 && est > P.mem_budget) {
     delete h;
     return fail(nullptr, WG_ERR_OOM,
@@ -371,7 +374,8 @@ int wg_problem_bytes(const wg_params* prm, int batch, double* bytes) {
       wg::build_shape_light(s, prm->n_el, prm->n_local, prm->nk, prm->n_xi, prm->l_xi, prm->m_diff, prm->mpc);
   if (!e.empty()) return fail(nullptr, WG_ERR_ARG, "wg_problem_bytes: " + e);
   const int restart = prm->restart > 0 ? prm->restart : 50, inner = prm->inner_restart > 0 ? prm->inner_restart : 40;
-  *bytes = wg::estimate_bytes(s, batch, restart, inner, prm->precision, prm->fp64_tc != 0);
+  *bytes = wg::estimate_bytes(s, batch, restart, inner, prm->precision, prm->fp64_tc != 0,
+                              prm->inner_basis_fp32 == 0);
   return WG_OK;
 }
 

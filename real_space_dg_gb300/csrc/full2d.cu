@@ -105,6 +105,15 @@ struct wg2d_problem {
   double* obs_W = nullptr;    // [nty][nY]
   double* obs_wj = nullptr;   // [nty]
   double* obs_out = nullptr;  // nDG, jxDG, jyDG [nX][nY]; n, jx, jy [nX][nty]; j [nX]
+  // hard-wall Y boundary (constrain_HardWall_full2D.m): active (rho_y cell, Y node) samples, the
+  // exact-mass projection per (Y element, rho_y cell) and the weight of the constraint rows
+  bool wall = false;
+  double wall_scale = 0;
+  unsigned char* wall_act = nullptr;   // [nY][nry]
+  double* wall_T = nullptr;            // [n_el_y][nry][nk_y][nk_y] row-major
+  float* wall_T32 = nullptr;
+  double2* wall_u = nullptr;           // [n] masked input
+  float2* wall_u32 = nullptr;
   std::string err;
 };
 
@@ -681,6 +690,65 @@ __global__ void __launch_bounds__(256) f2d_to64(const float2* __restrict__ x, do
   if (t < n) y[t] = make_double2(x[t].x, x[t].y);
 }
 
+// Hard-wall Y boundary (constrain_HardWall_full2D.m:40-50): um = u on the active samples, 0 on the
+// others.  Index g = rho_x + nrx (rho_y + nry (X + nX Y)); the flag is act[Y * nry + rho_y].
+template <typename T>
+__global__ void __launch_bounds__(256) f2d_wall_mask_kernel(const T* __restrict__ u, T* __restrict__ um,
+                                                            const unsigned char* __restrict__ act, int nrx, int nry,
+                                                            int nX, long long n) {
+  const long long g = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (g >= n) return;
+  const long long t = g / nrx;
+  const int ry = (int)(t % nry);
+  const long long Y = t / ((long long)nry * nX);
+  T v = u[g];
+  if (!act[Y * nry + ry]) v = czero<T>();
+  um[g] = v;
+}
+
+// y <- T y on the Y nodes of each (rho_x, rho_y, X, Y element) group, and scale * u on the
+// inactive samples (applyTransverse + the constraint rows of constrainedApply, :40-57).  One thread
+// per group, rho_x fastest (coalesced); the group's NK nodes are NK Y dofs apart.
+template <typename T, typename R, int NK>
+__global__ void __launch_bounds__(256) f2d_wall_project_kernel(T* __restrict__ y, const T* __restrict__ u,
+                                                               const unsigned char* __restrict__ act,
+                                                               const R* __restrict__ Tb, R scale, int nrx, int nry,
+                                                               int nX, int ney) {
+  const long long q = (long long)blockIdx.x * 256 + threadIdx.x;
+  const long long ngroups = (long long)nrx * nry * nX * ney;
+  if (q >= ngroups) return;
+  const int rx = (int)(q % nrx);
+  long long t = q / nrx;
+  const int ry = (int)(t % nry);
+  t /= nry;
+  const int X = (int)(t % nX);
+  const int e = (int)(t / nX);
+  const long long nrel = (long long)nrx * nry, ystride = nrel * nX;
+  const long long base = rx + (long long)nrx * ry + nrel * X + ystride * ((long long)e * NK);
+  T v[NK];
+#pragma unroll
+  for (int j = 0; j < NK; ++j) v[j] = y[base + ystride * j];
+  const R* Te = Tb + ((long long)e * nry + ry) * NK * NK;
+#pragma unroll
+  for (int a = 0; a < NK; ++a) {
+    const long long g = base + ystride * a;
+    T o;
+    if (act[(long long)(e * NK + a) * nry + ry]) {
+      o = czero<T>();
+#pragma unroll
+      for (int j = 0; j < NK; ++j) {
+        o.x += Te[a * NK + j] * v[j].x;
+        o.y += Te[a * NK + j] * v[j].y;
+      }
+    } else {
+      const T uu = u[g];
+      o.x = scale * uu.x;
+      o.y = scale * uu.y;
+    }
+    y[g] = o;
+  }
+}
+
 __global__ void __launch_bounds__(256) f2d_to32_scaled(const double2* __restrict__ x, float2* __restrict__ y,
                                                        const double* __restrict__ nrm, long long n) {
   __shared__ double sa;   // the reciprocal once per block
@@ -1247,7 +1315,8 @@ int wg2d_destroy(wg2d_problem* h) {
   free32(h);
   wg::ozaki_free(h->cols);
   void* ptrs[] = {h->x, h->y, h->G, h->Uq, h->Rq, h->dV, h->interp, h->proj, h->xq, h->yq, h->vx, h->vy, h->cap,
-                  h->tc_err, h->obs_W, h->obs_wj, h->obs_out};
+                  h->tc_err, h->obs_W, h->obs_wj, h->obs_out, h->wall_act, h->wall_T, h->wall_T32, h->wall_u,
+                  h->wall_u32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t ev : h->ev)
@@ -1388,13 +1457,42 @@ int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const 
   return WG_OK;
 }
 
+}  // extern "C"
+
+// The hard-wall constraint around an apply: mask the input before, project the output after.
+template <typename T, typename R>
+static int wall_project(wg2d_problem* h, T* y, const T* u, const R* Tb) {
+  const long long groups = (long long)h->nrx * h->nry * h->nX * h->s.n_el_y;
+  const unsigned nb = (unsigned)((groups + 255) / 256);
+  const R sc = (R)h->wall_scale;
+  switch (h->s.nk_y) {
+    case 2: f2d_wall_project_kernel<T, R, 2><<<nb, 256, 0, h->stream>>>(y, u, h->wall_act, Tb, sc, h->nrx, h->nry,
+                                                                         h->nX, h->s.n_el_y); break;
+    case 3: f2d_wall_project_kernel<T, R, 3><<<nb, 256, 0, h->stream>>>(y, u, h->wall_act, Tb, sc, h->nrx, h->nry,
+                                                                         h->nX, h->s.n_el_y); break;
+    default: f2d_wall_project_kernel<T, R, 4><<<nb, 256, 0, h->stream>>>(y, u, h->wall_act, Tb, sc, h->nrx, h->nry,
+                                                                          h->nX, h->s.n_el_y); break;
+  }
+  F2_CK(cudaGetLastError());
+  return WG_OK;
+}
+
+extern "C" {
+
 static int apply_device(wg2d_problem* h) {
   if (!h->potential_ready) return fail(h, WG_ERR_ARG, "wg2d_apply: set the drift data and the potential first");
+  double2* u = h->x;
+  if (h->wall) {
+    f2d_wall_mask_kernel<double2><<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(u, h->wall_u, h->wall_act,
+                                                                                     h->nrx, h->nry, h->nX, h->n);
+    h->x = h->wall_u;
+  }
   int rc = apply_drift(h);
-  if (rc) return rc;
-  rc = apply_transport(h, 0);
-  if (rc) return rc;
-  return apply_transport(h, 1);
+  if (!rc) rc = apply_transport(h, 0);
+  if (!rc) rc = apply_transport(h, 1);
+  h->x = u;
+  if (rc || !h->wall) return rc;
+  return wall_project<double2, double>(h, h->y, u, h->wall_T);
 }
 
 // out = A in on device buffers (the kernels read h->x and write h->y at launch)
@@ -1532,6 +1630,38 @@ static void free_preconditioner(wg2d_problem* h) {
   h->pre_ready = false;
 }
 
+int wg2d_set_hard_wall(wg2d_problem* h, const unsigned char* active, const double* projection, double scale) {
+  if (!h) return WG_ERR_ARG;
+  cudaStreamSynchronize(h->stream);
+  void* old[] = {h->wall_act, h->wall_T, h->wall_T32, h->wall_u, h->wall_u32};
+  for (void* p : old)
+    if (p) cudaFree(p);
+  h->wall_act = nullptr;
+  h->wall_T = nullptr;
+  h->wall_T32 = nullptr;
+  h->wall_u = nullptr;
+  h->wall_u32 = nullptr;
+  h->wall = false;
+  if (!active) return WG_OK;
+  if (!projection || !(scale > 0) || !std::isfinite(scale))
+    return fail(h, WG_ERR_ARG, "wg2d_set_hard_wall: projection required and scale positive and finite");
+  if (h->s.periodic_y) return fail(h, WG_ERR_ARG, "wg2d_set_hard_wall: the Y axis is periodic");
+  const long long na = (long long)h->nY * h->nry;
+  const long long nt = (long long)h->s.n_el_y * h->nry * h->s.nk_y * h->s.nk_y;
+  std::vector<float> t32(projection, projection + nt);
+  F2_CK(cudaMalloc(&h->wall_act, na));
+  F2_CK(dalloc(&h->wall_T, nt));
+  F2_CK(dalloc(&h->wall_T32, nt));
+  F2_CK(dalloc(&h->wall_u, h->n));
+  F2_CK(dalloc(&h->wall_u32, h->n));
+  F2_CK(cudaMemcpy(h->wall_act, active, na, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(h->wall_T, projection, sizeof(double) * nt, cudaMemcpyHostToDevice));
+  F2_CK(cudaMemcpy(h->wall_T32, t32.data(), sizeof(float) * nt, cudaMemcpyHostToDevice));
+  h->wall_scale = scale;
+  h->wall = true;
+  return WG_OK;
+}
+
 int wg2d_apply(wg2d_problem* h, const double* x, double* y) {
   if (!h || !x || !y) return h ? fail(h, WG_ERR_ARG, "wg2d_apply: null argument") : WG_ERR_ARG;
   F2_CK(cudaMemcpyAsync(h->x, x, sizeof(double2) * h->n, cudaMemcpyHostToDevice, h->stream));
@@ -1665,10 +1795,18 @@ extern "C" {
 // out = A in in FP32 (every term on the CUDA cores, the dense abs(A_x) factor included)
 static int apply32(wg2d_problem* h, const float2* in, float2* out) {
   const OpData<float2, float> d = op32(h);
-  drift_terms<float2, float>(h, d, in, out);
+  const float2* src = in;
+  if (h->wall) {
+    f2d_wall_mask_kernel<float2><<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(in, h->wall_u32,
+                                                                                    h->wall_act, h->nrx, h->nry,
+                                                                                    h->nX, h->n);
+    src = h->wall_u32;
+  }
+  drift_terms<float2, float>(h, d, src, out);
   for (int a = 0; a < 2; ++a)
-    if (h->ax[a].T) transport_terms<float2, float>(h, a, d, in, out, 0u);
+    if (h->ax[a].T) transport_terms<float2, float>(h, a, d, src, out, 0u);
   F2_CK(cudaGetLastError());
+  if (h->wall) return wall_project<float2, float>(h, out, in, h->wall_T32);
   return WG_OK;
 }
 

@@ -37,6 +37,21 @@ __device__ __forceinline__ double2 ld2(const float2& v) { return make_double2(v.
 __device__ __forceinline__ void st2(double2& d, double2 v) { d = v; }
 __device__ __forceinline__ void st2(float2& d, double2 v) { d = make_float2((float)v.x, (float)v.y); }
 
+// Basis loads of the FP32 inner solve: two consecutive complex values (16 bytes of an FP32
+// basis, 8 bytes of an FP16 one) as one float4; one complex value as float2.
+__device__ __forceinline__ float4 ld_pair(const float2* v, long long n4) {
+  return reinterpret_cast<const float4*>(v)[n4];
+}
+__device__ __forceinline__ float4 ld_pair(const __half2* v, long long n4) {
+  const uint2 u = reinterpret_cast<const uint2*>(v)[n4];
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ float2 ld_one(const float2& v) { return v; }
+__device__ __forceinline__ double2 ld_one(const double2& v) { return v; }
+__device__ __forceinline__ float2 ld_one(const __half2& v) { return __half22float2(v); }
+
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -254,8 +269,8 @@ struct KrylovTail {
 // chunk is read once, warps drop their partial sums in shared memory and the
 // block adds them at the end (no block barrier per coefficient).
 constexpr int kMdE = 8;
-template <typename T>
-__global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, const T* __restrict__ w,
+template <typename T, typename VB = T>
+__global__ void __launch_bounds__(256) multidot_kernel(const VB* __restrict__ V, const T* __restrict__ w,
                                                        double2* __restrict__ partial, const int* __restrict__ active,
                                                        long long N, int nv, int mp1, int pstride, int nchunk,
                                                        KrylovTail tl) {
@@ -276,14 +291,14 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
     }
     int i = 0;
     for (; i + 1 < nv; i += 2) {
-      const float4* v0 = reinterpret_cast<const float4*>(V + ((long long)b * mp1 + i) * N);
-      const float4* v1 = v0 + N4;
+      const VB* v0 = V + ((long long)b * mp1 + i) * N;
+      const VB* v1 = v0 + N;
       float4 a0[E4], a1[E4];
 #pragma unroll
       for (int j = 0; j < E4; ++j) {
         const long long n = base4 + (long long)j * 256;
-        a0[j] = n < N4 ? v0[n] : make_float4(0.f, 0.f, 0.f, 0.f);
-        a1[j] = n < N4 ? v1[n] : make_float4(0.f, 0.f, 0.f, 0.f);
+        a0[j] = n < N4 ? ld_pair(v0, n) : make_float4(0.f, 0.f, 0.f, 0.f);
+        a1[j] = n < N4 ? ld_pair(v1, n) : make_float4(0.f, 0.f, 0.f, 0.f);
       }
       AccF32 s0, s1;
 #pragma unroll
@@ -299,12 +314,12 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
       }
     }
     if (i < nv) {
-      const float4* v0 = reinterpret_cast<const float4*>(V + ((long long)b * mp1 + i) * N);
+      const VB* v0 = V + ((long long)b * mp1 + i) * N;
       AccF32 s0;
 #pragma unroll
       for (int j = 0; j < E4; ++j) {
         const long long n = base4 + (long long)j * 256;
-        if (n < N4) s0.add_cdot4(v0[n], wv[j]);
+        if (n < N4) s0.add_cdot4(ld_pair(v0, n), wv[j]);
       }
       s0.warp_reduce();
       if (lane == 0) s0.stage(red + (i * 8 + warp) * 4);
@@ -320,7 +335,7 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
       else { wv[j].x = 0; wv[j].y = 0; }
     }
     for (int i = 0; i < nv; ++i) {
-      const T* v = V + ((long long)b * mp1 + i) * N;
+      const VB* v = V + ((long long)b * mp1 + i) * N;
       typename AccFor<T>::type a;
 #pragma unroll
       for (int j = 0; j < kMdE; ++j) {
@@ -348,8 +363,8 @@ __global__ void __launch_bounds__(256) multidot_kernel(const T* __restrict__ V, 
 // MODE 0: update only.  MODE >= 1: also nrm_partial[b][block] = sum |w|^2, and the last
 // block of problem b finishes the step: MODE 1 runs the DGKS test (reorth[b]) and, when
 // no second pass is needed, MODE 2's work: |w|, H[k+1][k], inverse norm, Givens step.
-template <typename T, int MODE>
-__global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V, T* __restrict__ w,
+template <typename T, int MODE, typename VB = T>
+__global__ void __launch_bounds__(256) gs_update_kernel(const VB* __restrict__ V, T* __restrict__ w,
                                                         const T* __restrict__ hcol, const int* __restrict__ mask,
                                                         double* __restrict__ nrm_partial, long long N, int nv, int mp1,
                                                         int pstride, int nblk, KrylovTail tl) {
@@ -365,10 +380,10 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
     if (n4 < N4) {
       float4* wp = reinterpret_cast<float4*>(w + (long long)b * N) + n4;
       float4 acc = *wp;
-      const float4* v = reinterpret_cast<const float4*>(V + (long long)b * mp1 * N) + n4;
+      const VB* v = V + (long long)b * mp1 * N;
 #pragma unroll 4
       for (int i = 0; i < nv; ++i) {
-        const float4 x = v[(long long)i * N4];
+        const float4 x = ld_pair(v, (long long)i * N4 + n4);
         const float2 h = hs[i];
         acc.x = fmaf(-x.x, h.x, fmaf(x.y, h.y, acc.x));
         acc.y = fmaf(-x.x, h.y, fmaf(-x.y, h.x, acc.y));
@@ -386,7 +401,7 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const T* __restrict__ V,
     if (n < N) {
       const long long t = (long long)b * N + n;
       T acc = w[t];
-      const T* v = V + (long long)b * mp1 * N + n;
+      const VB* v = V + (long long)b * mp1 * N + n;
 #pragma unroll 4
       for (int i = 0; i < nv; ++i) cms(acc, v[(long long)i * N], hs[i]);
       w[t] = acc;
@@ -560,8 +575,8 @@ __global__ void backsolve_kernel(const double2* __restrict__ H, const double2* _
     }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) combine_kernel(const T* __restrict__ V, const T* __restrict__ y,
+template <typename T, typename VB = T>
+__global__ void __launch_bounds__(256) combine_kernel(const VB* __restrict__ V, const T* __restrict__ y,
                                                       const int* __restrict__ kused, T* __restrict__ u, long long N,
                                                       int mp1, int m, int batch) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -572,12 +587,12 @@ __global__ void __launch_bounds__(256) combine_kernel(const T* __restrict__ V, c
   T acc;
   acc.x = 0;
   acc.y = 0;
-  const T* v = V + (long long)b * mp1 * N + n;
+  const VB* v = V + (long long)b * mp1 * N + n;
   for (int i = 0; i < kk; ++i) {
     T h = y[b * m + i];
     h.x = -h.x;
     h.y = -h.y;
-    cms(acc, v[(long long)i * N], h);   // acc += v y
+    cms(acc, ld_one(v[(long long)i * N]), h);   // acc += v y
   }
   u[t] = acc;
 }
@@ -603,15 +618,17 @@ template <typename T> float2* coef_col32(Problem& P);
 template <> float2* coef_col32<double2>(Problem&) { return nullptr; }
 template <> float2* coef_col32<float2>(Problem& P) { return P.mx.hcol; }
 
-template <typename T, typename Prec, typename Apply>
-int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
+template <typename T, typename VB = T, typename Prec, typename Apply>
+int arnoldi_step(Problem& P, VB* V, T* w, int k, int m, Prec prec, Apply apply) {
   const int B = P.batch, mp1 = m + 1, ps = P.restart_max + 1, mm = P.restart_max;
   const long long N = P.N;
   // V_k: step 0 reads the basis vector the cycle start wrote; later steps take the previous
   // step's w and its inverse norm, and the preconditioner writes V_k = w / |w| as it reads it
-  // (no separate scaling pass per step)
+  // (no separate scaling pass per step).  An FP16 basis: the cycle start leaves V_0 in FP32
+  // in w, and the preconditioner stores its FP16 rounding as V_0.
   if (k == 0) {
-    WG_CK(prec(V, (long long)mp1 * N, nullptr, nullptr));
+    if constexpr (std::is_same<VB, T>::value) WG_CK(prec(V, (long long)mp1 * N, nullptr, nullptr));
+    else WG_CK(prec(w, N, nullptr, V));
   } else {
     const T* wprev = w;
     if constexpr (std::is_same<T, float2>::value)
@@ -621,7 +638,7 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   }
   WG_CK(apply());
   const int nv = k + 1;
-  const double sz = (double)sizeof(T), vec = (double)N * B * sz;
+  const double vec = (double)N * B * sizeof(T), vecb = (double)N * B * sizeof(VB);
   const dim3 gu((unsigned)((N + 255) / 256), B);
   // classical Gram-Schmidt; the second pass runs for the problems that fail the DGKS
   // test (its kernels see P.reorth as their activity mask), for all with eta >= 1,
@@ -638,20 +655,21 @@ int arnoldi_step(Problem& P, T* V, T* w, int k, int m, Prec prec, Apply apply) {
   for (int pass = 0; pass < passes; ++pass) {
     const int* mask = (pass == 0 || eta >= 1) ? P.active : P.reorth;
     tl.first = pass == 0;
-    cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, (nv + 1) * vec, 8.0 * nv * N * B, mask);
-    multidot_kernel<T><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, mask, N,
-                                                                                      nv, mp1, ps, P.nchunk, tl);
+    cudaEvent_t ev = prof_begin(P, PROF_MULTIDOT, 1, nv * vecb + vec, 8.0 * nv * N * B, mask);
+    multidot_kernel<T, VB><<<dim3(P.nchunk, B), 256, sizeof(double) * 32 * nv, P.stream>>>(V, w, P.partial, mask,
+                                                                                          N, nv, mp1, ps, P.nchunk,
+                                                                                          tl);
     prof_end(P, PROF_MULTIDOT, ev);
-    ev = prof_begin(P, PROF_GSUPDATE, 1, (nv + 2) * vec, 8.0 * nv * N * B, mask);
+    ev = prof_begin(P, PROF_GSUPDATE, 1, nv * vecb + 2 * vec, 8.0 * nv * N * B, mask);
     if (pass == passes - 1)
-      gs_update_kernel<T, 2><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
-                                                             ps, P.nblk, tl);
+      gs_update_kernel<T, 2, VB><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv,
+                                                                 mp1, ps, P.nblk, tl);
     else if (eta < 1)
-      gs_update_kernel<T, 1><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
-                                                             ps, P.nblk, tl);
+      gs_update_kernel<T, 1, VB><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv,
+                                                                 mp1, ps, P.nblk, tl);
     else
-      gs_update_kernel<T, 0><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv, mp1,
-                                                             ps, P.nblk, tl);
+      gs_update_kernel<T, 0, VB><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv,
+                                                                 mp1, ps, P.nblk, tl);
     prof_end(P, PROF_GSUPDATE, ev);
   }
   // V_{k+1} = w / |w| is written by the next step's preconditioner
@@ -946,6 +964,9 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
   auto prec = [&](const float2* r, long long stride, const float* rscale, float2* rout) {
     return launch_precondition_mixed(P, r, stride, M.z, M.zb16, P.active, rscale, rout, (long long)mp1 * N);
   };
+  auto prec_h = [&](const float2* r, long long stride, const float* rscale, __half2* rout) {
+    return launch_precondition_mixed_h(P, r, stride, M.z, M.zb16, P.active, rscale, rout, (long long)mp1 * N);
+  };
   auto apply = [&]() { return launch_apply_mixed(P, M.z, M.zb16, M.w, P.active); };
   for (int ref = 0; ref < max_ref; ++ref) {
     bool any = false;
@@ -965,13 +986,18 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     WG_CK(cudaMemcpyAsync(P.nrm, ones.data(), sizeof(double) * B, cudaMemcpyHostToDevice, P.stream));
     P.prof.launches[PROF_OTHER] += 2;
     cycle_init_kernel<<<(B + 127) / 128, 128, 0, P.stream>>>(P.nrm, P.target, P.g, P.active, P.kused, ps, B);
-    scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.V, P.inv64, P.active, N,
-                                                                        (long long)mp1 * N, B);
+    // V_0 = r / |r| (an FP16 basis: in FP32 in w, stored by the first step's preconditioner)
+    if (M.basis16)
+      scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.w, P.inv64, P.active, N, N, B);
+    else
+      scale_kernel<double2, float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.r, M.V, P.inv64, P.active, N,
+                                                                          (long long)mp1 * N, B);
     for (int k0 = 0; k0 < m; k0 = chunk_end(k0, m)) {
       const int k1 = chunk_end(k0, m);
       rc = run_arnoldi_chunk(P, P.graphs[1], m, k0, [&]() {
         for (int k = k0; k < k1; ++k) {
-          const int r = arnoldi_step<float2>(P, M.V, M.w, k, m, prec, apply);
+          const int r = M.basis16 ? arnoldi_step<float2, __half2>(P, M.Vh, M.w, k, m, prec_h, apply)
+                                  : arnoldi_step<float2>(P, M.V, M.w, k, m, prec, apply);
           if (r) return r;
         }
         return (int)WG_OK;
@@ -984,7 +1010,10 @@ int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_in
     // d = M^-1 (V y) in FP32, x += |r| d in FP64
     P.prof.launches[PROF_OTHER] += 3;
     backsolve_kernel<<<B, 32, 0, P.stream>>>(P.H, P.g, P.ycoef, M.y, P.kused, ps, mm, B);
-    combine_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(M.V, M.y, P.kused, M.w, N, mp1, mm, B);
+    if (M.basis16)
+      combine_kernel<float2, __half2><<<blocks_for(tot), 256, 0, P.stream>>>(M.Vh, M.y, P.kused, M.w, N, mp1, mm, B);
+    else
+      combine_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(M.V, M.y, P.kused, M.w, N, mp1, mm, B);
     WG_CK(launch_precondition_mixed(P, M.w, N, M.d, nullptr, P.res_mask));
     axpy_kernel<float2><<<blocks_for(tot), 256, 0, P.stream>>>(P.x, M.d, P.nrm_keep, N, B, P.res_mask);
     WG_CK(cudaGetLastError());

@@ -15,9 +15,14 @@
 // (ceil(nk/32), ceil(n_chunks/4), batch) covers every SM even for one problem.
 // Optional: r enters scaled by rscale[b] (the Arnoldi step's w / |w|), and the apply kernel
 // writes the scaled r to rout (the next basis vector), which replaces a separate scaling pass.
+// With an FP16 basis (rout of type __half2) both kernels round the scaled r to FP16 before
+// they use it, so z is the preconditioned image of exactly the stored basis vector.
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include <vector>
 
@@ -33,7 +38,21 @@ template <> struct Cplx<float> { using type = float2; };
 __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
 __device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
 
-template <int NK, typename R>
+// r value as the basis stores it: unchanged, or rounded to FP16 (RH)
+template <bool RH, typename T>
+__device__ __forceinline__ T basis_round(T v) {
+  if constexpr (RH) {
+    const float2 f = __half22float2(__floats2half2_rn((float)v.x, (float)v.y));
+    v.x = f.x;
+    v.y = f.y;
+  }
+  return v;
+}
+__device__ __forceinline__ void basis_store(float2& d, float2 v) { d = v; }
+__device__ __forceinline__ void basis_store(double2& d, double2 v) { d = v; }
+__device__ __forceinline__ void basis_store(__half2& d, float2 v) { d = __floats2half2_rn(v.x, v.y); }
+
+template <int NK, typename R, bool RH = false>
 __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
     const typename Cplx<R>::type* __restrict__ r, const R* __restrict__ kvec, const R* __restrict__ dinv,
     const R* __restrict__ hvec, const R* __restrict__ qd, R* __restrict__ mapA, typename Cplx<R>::type* __restrict__ mapS,
@@ -65,12 +84,18 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
     R ux = R(0), uy = R(0);
 #pragma unroll
     for (int q = 0; q < NK; ++q) {
-      const T rv = re[(long long)q * nk];
+      T rv = re[(long long)q * nk];
+      if constexpr (RH) {
+        rv.x *= sc;
+        rv.y *= sc;
+        rv = basis_round<RH>(rv);
+      }
       ux += Dst[q] * rv.x;
       uy += Dst[q] * rv.y;
     }
-    s.x = ux * sc * inv_qd + alpha * s.x;
-    s.y = uy * sc * inv_qd + alpha * s.y;
+    const R scm = RH ? R(1) : sc;   // RH: the scale is already in rv
+    s.x = ux * scm * inv_qd + alpha * s.x;
+    s.y = uy * scm * inv_qd + alpha * s.y;
     A *= alpha;
   }
   const long long m = ((long long)b * nchunk + c) * nk + j;
@@ -78,15 +103,16 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
   mapS[m] = s;
 }
 
-template <int NK, typename R>
+template <int NK, typename R, typename O = typename Cplx<R>::type>
 __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
     const typename Cplx<R>::type* __restrict__ r, typename Cplx<R>::type* __restrict__ z,
     __nv_bfloat162* __restrict__ zb, const R* __restrict__ kvec, const R* __restrict__ dinv,
     const R* __restrict__ hvec, const R* __restrict__ qd, const R* __restrict__ mapA,
     const typename Cplx<R>::type* __restrict__ mapS, int n_el, int nk, long long N, long long r_stride, int L,
     int nchunk, const int* __restrict__ mask, const R* __restrict__ rscale = nullptr,
-    typename Cplx<R>::type* __restrict__ rout = nullptr, long long rout_stride = 0) {
+    O* __restrict__ rout = nullptr, long long rout_stride = 0) {
   using T = typename Cplx<R>::type;
+  constexpr bool RH = std::is_same<O, __half2>::value;
   const int j = blockIdx.x * 32 + threadIdx.x;
   const int c = blockIdx.y * kChunksPerBlock + threadIdx.y;
   const int b = blockIdx.z;
@@ -126,7 +152,7 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
   const int e_lo = c * L, e_hi = min(n_el, e_lo + L);
   const T* rb = r + (long long)b * r_stride + j;
   T* zbase = z + (long long)b * N + j;
-  T* obase = rout ? rout + (long long)b * rout_stride + j : nullptr;
+  O* obase = rout ? rout + (long long)b * rout_stride + j : nullptr;
   for (int i = 0; i < e_hi - e_lo; ++i) {
     const int e = fwd ? e_lo + i : e_hi - 1 - i;
     const T* re = rb + (long long)e * NK * nk;
@@ -138,8 +164,9 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
         rv[q].x *= sc;
         rv[q].y *= sc;
       }
+      rv[q] = basis_round<RH>(rv[q]);
       // the scaled input is the next Krylov basis vector: written here, so no separate pass
-      if (obase) obase[(long long)e * NK * nk + (long long)q * nk] = rv[q];
+      if (obase) basis_store(obase[(long long)e * NK * nk + (long long)q * nk], rv[q]);
     }
     T snew = s;
 #pragma unroll

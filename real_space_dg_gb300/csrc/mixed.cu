@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "kline.cuh"
@@ -496,22 +497,24 @@ cudaError_t apply_mixed_nk(Problem& P, const float2* x, const bf162* xb, float2*
   return cudaGetLastError();
 }
 
-template <int NK>
+template <int NK, typename O>
 cudaError_t precond_mixed_nk(Problem& P, const float2* r, long long r_stride, float2* z, bf162* zb, const int* mask,
-                             const float* rscale, float2* rout, long long rout_stride) {
+                             const float* rscale, O* rout, long long rout_stride) {
+  constexpr bool RH = std::is_same<O, __half2>::value;
   const int L = P.kline_L, nc = kline::chunk_count_for(P.s.n_el, L);
   const dim3 grid((P.s.nk + 31) / 32, (nc + kline::kChunksPerBlock - 1) / kline::kChunksPerBlock, P.batch);
   const dim3 block(32, kline::kChunksPerBlock);
   float* ma = static_cast<float*>(P.kmap_a);
   float2* ms = static_cast<float2*>(P.kmap_s);
-  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2, ((zb ? 28.0 : 24.0) + (rout ? 8.0 : 0.0)) * P.N * P.batch, 0, mask);
-  kline::kline_maps_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, ma, ms,
-                                                                    P.s.n_el, P.s.nk, P.N, r_stride, L, nc, mask,
-                                                                    rscale);
-  kline::kline_apply_kernel<NK, float><<<grid, block, 0, P.stream>>>(r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h,
-                                                                     P.mx.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
-                                                                     r_stride, L, nc, mask, rscale, rout,
-                                                                     rout_stride);
+  cudaEvent_t ev = prof_begin(P, PROF_PRECOND, 2,
+                              ((zb ? 28.0 : 24.0) + (rout ? (double)sizeof(O) : 0.0)) * P.N * P.batch, 0, mask);
+  kline::kline_maps_kernel<NK, float, RH><<<grid, block, 0, P.stream>>>(r, P.mx.kvec, P.mx.dinv, P.mx.h, P.mx.qd, ma,
+                                                                        ms, P.s.n_el, P.s.nk, P.N, r_stride, L, nc,
+                                                                        mask, rscale);
+  kline::kline_apply_kernel<NK, float, O><<<grid, block, 0, P.stream>>>(r, z, zb, P.mx.kvec, P.mx.dinv, P.mx.h,
+                                                                        P.mx.qd, ma, ms, P.s.n_el, P.s.nk, P.N,
+                                                                        r_stride, L, nc, mask, rscale, rout,
+                                                                        rout_stride);
   prof_end(P, PROF_PRECOND, ev);
   return cudaGetLastError();
 }
@@ -524,11 +527,12 @@ std::string mixed_check_shape(const Shape& s) {
   return "";
 }
 
-double mixed_bytes(const Shape& s, int batch, int restart) {
+double mixed_bytes(const Shape& s, int batch, int restart, bool basis16) {
   const double BN = (double)s.n_el * s.nK * s.nk * batch;
   const double ncols = (double)batch * s.n_el * s.nK;
   return 2.0 * 2 * (4.0 * s.nxi * s.nk) + 4.0 * BN + 8.0 * ncols * s.nxi + 4.0 * ncols * s.nxi +
-         8.0 * BN * (restart + 1 + 4) + 4.0 * batch * s.n_el * pair_count(s.nK) * ((s.nxi + 4) & ~3);
+         (basis16 ? 4.0 : 8.0) * BN * (restart + 1) + 8.0 * BN * 4 +
+         4.0 * batch * s.n_el * pair_count(s.nK) * ((s.nxi + 4) & ~3);
 }
 
 int mixed_alloc(Problem& P) {
@@ -546,7 +550,9 @@ int mixed_alloc(Problem& P) {
   alloc((void**)&M.zb16, sizeof(bf162) * BN);
   alloc((void**)&M.yh16, sizeof(bf162) * (size_t)s.nxi * P.ncols);
   alloc((void**)&M.xh, sizeof(float2) * (size_t)s.nxi * P.ncols);
-  alloc((void**)&M.V, sizeof(float2) * BN * mp1);
+  M.basis16 = P.inner_basis16;
+  if (M.basis16) alloc((void**)&M.Vh, sizeof(__half2) * BN * mp1);
+  else alloc((void**)&M.V, sizeof(float2) * BN * mp1);
   alloc((void**)&M.w, sizeof(float2) * BN);
   alloc((void**)&M.z, sizeof(float2) * BN);
   alloc((void**)&M.r, sizeof(float2) * BN);
@@ -695,8 +701,8 @@ int ozaki_alloc(Problem& P) {
 
 void mixed_free(Problem& P) {
   MixedBuffers& M = P.mx;
-  void* ptrs[] = {M.phi1, M.phi2, M.xin16, M.zb16, M.yh16, M.xh, M.V, M.w, M.z, M.r, M.d, M.beta, M.betai, M.err,
-                  M.kvec, M.qd, M.dinv, M.h, M.hcol, M.y, M.inv, M.oa1, M.oa2, M.ea1, M.ea2, M.ob, M.eb};
+  void* ptrs[] = {M.phi1, M.phi2, M.xin16, M.zb16, M.yh16, M.xh, M.V, M.Vh, M.w, M.z, M.r, M.d, M.beta, M.betai,
+                  M.err, M.kvec, M.qd, M.dinv, M.h, M.hcol, M.y, M.inv, M.oa1, M.oa2, M.ea1, M.ea2, M.ob, M.eb};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   M = MixedBuffers{};
@@ -766,6 +772,16 @@ cudaError_t launch_stencil_mixed(Problem& P) {
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
                                       __nv_bfloat162* zb, const int* mask, const float* rscale, float2* rout,
                                       long long rout_stride) {
+  switch (P.s.nK) {
+    case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
+    case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
+    default: return precond_mixed_nk<4>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
+  }
+}
+
+cudaError_t launch_precondition_mixed_h(Problem& P, const float2* r, long long r_stride, float2* z,
+                                        __nv_bfloat162* zb, const int* mask, const float* rscale, __half2* rout,
+                                        long long rout_stride) {
   switch (P.s.nK) {
     case 2: return precond_mixed_nk<2>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);
     case 3: return precond_mixed_nk<3>(P, r, r_stride, z, zb, mask, rscale, rout, rout_stride);

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -77,6 +78,8 @@ struct MixedBuffers {
   __nv_bfloat162* yh16 = nullptr;    // [ncols][N_xi] bf16 stencil output (GEMM 2 B operand)
   float2* xh = nullptr;              // [ncols][N_xi] fp32 GEMM 1 output
   float2* V = nullptr;               // [B][m_inner+1][N] fp32 Krylov basis
+  __half2* Vh = nullptr;             // the same basis stored in FP16 (basis16; V is then unused)
+  bool basis16 = false;              // inner basis stored in FP16, arithmetic in FP32
   float2* w = nullptr;               // [B*N]
   float2* z = nullptr;               // [B*N]
   float2* r = nullptr;               // [B*N] normalised outer residual
@@ -212,6 +215,7 @@ struct Problem {
   FluxBlocks fb{};
   double shift = 0;         // sigma of the shifted operator A + sigma I (0: the stationary A)
   bool fp64_tc = false;     // FP64 handle whose transforms run as FP64 emulated on the tensor cores
+  bool inner_basis16 = true;  // mixed form: the inner Krylov basis stored in FP16
   std::string err;
 
   std::vector<HostProblem> hp;
@@ -315,7 +319,8 @@ cudaError_t launch_precondition(Problem& P, const double2* r, long long r_stride
 // k-line factors of A + sigma I for every problem (sigma = P.shift), uploaded to pre_dinv / pre_h.
 int set_kline_factors(Problem& P);
 // Device bytes of a handle before allocation (the admission estimate of wg_problem_create).
-double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc = false);
+double estimate_bytes(const Shape& s, int batch, int restart, int restart_inner, int precision, bool fp64_tc = false,
+                      bool basis16 = true);
 cudaError_t launch_flux_f64(Problem& P, const double2* x, double2* y, const int* mask = nullptr);
 cudaError_t launch_stencil_f64(Problem& P, const double2* xh, double2* yh, const int* mask = nullptr);
 // FP64 operator apply with the transforms emulated on the tensor cores (mixed form only).
@@ -335,7 +340,7 @@ int apply_noalloc(const wg_operator_view& v, const double* x, double* y, void* s
 int gmres_solve_fp64(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // Mixed form (mixed.cu)
 std::string mixed_check_shape(const Shape& s);
-double mixed_bytes(const Shape& s, int batch, int restart);
+double mixed_bytes(const Shape& s, int batch, int restart, bool basis16);
 int mixed_alloc(Problem& P);
 // Digit slices of Phi, state slice buffer and tensor maps of the FP64 emulation (any precision).
 int ozaki_alloc(Problem& P);
@@ -347,6 +352,11 @@ cudaError_t launch_apply_mixed(Problem& P, const float2* x, const __nv_bfloat162
 cudaError_t launch_precondition_mixed(Problem& P, const float2* r, long long r_stride, float2* z,
                                       __nv_bfloat162* zb, const int* mask = nullptr, const float* rscale = nullptr,
                                       float2* rout = nullptr, long long rout_stride = 0);
+// The same with the (scaled) input rounded to FP16 first and written to rout, an FP16 basis
+// vector: the preconditioner works on exactly the vector the basis stores.
+cudaError_t launch_precondition_mixed_h(Problem& P, const float2* r, long long r_stride, float2* z,
+                                        __nv_bfloat162* zb, const int* mask, const float* rscale, __half2* rout,
+                                        long long rout_stride);
 // The FP32 xi stencil alone (M.xh -> M.yh16, every problem), for the autotuner.
 cudaError_t launch_stencil_mixed(Problem& P);
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);

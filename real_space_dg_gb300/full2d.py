@@ -12,8 +12,11 @@ runs on the GPU (``wg2d_*`` in libwigner_gb300.so):
   - potential and CAP, get_Drift_full2D.m:133-364 (FV-consistent form): the vertex
     potential differences are rebuilt on the device from V on the material grid.
 
-Supported: source/drain faces fully open, Y boundaries 'periodic', 'zero-inflow' and
-'specular', X/Y fluxes 'upwind', 'rusanov', 'central', constant mass.
+Supported: source/drain faces fully open, Y boundaries 'periodic', 'zero-inflow',
+'specular' and 'hard-wall' (the two-point Dirichlet constraint of
+constrain_HardWall_full2D.m on the complete operator, its right-hand side and the
+preconditioner's transverse blocks), X/Y fluxes 'upwind', 'rusanov', 'central',
+constant mass.
 """
 import ctypes as C
 import math
@@ -223,7 +226,8 @@ def _flux(prm):
 def _ytype(prm):
     v = str(prm.get("full2D_Y_boundary", "specular")).strip().lower()
     return {"specular-reflection": "specular", "reflection": "specular", "reflecting": "specular",
-            "zero_inflow": "zero-inflow", "zeroinflow": "zero-inflow", "zero": "zero-inflow"}.get(v, v)
+            "zero_inflow": "zero-inflow", "zeroinflow": "zero-inflow", "zero": "zero-inflow",
+            "hardwall": "hard-wall", "hard_wall": "hard-wall", "dirichlet": "hard-wall"}.get(v, v)
 
 
 def _blocks(Cm, nl, ne, periodic):
@@ -261,8 +265,9 @@ def build_factors(mat):
     nex = int(_param(prm, "N_el_X", (len(x) - 1) // (nkx - 1)))
     ney = int(_param(prm, "N_el_Y", (len(y) - 1) // (nky - 1)))
     ytype = _ytype(prm)
-    if ytype not in ("periodic", "zero-inflow", "specular"):
-        raise WignerError(_lib.WG_ERR_ARG, "Full-2D Y boundary %r is not supported on the GPU" % ytype)
+    if ytype not in ("periodic", "zero-inflow", "specular", "hard-wall"):
+        raise WignerError(_lib.WG_ERR_ARG, 'Unknown full2D_Y_boundary "%s". Use "specular" or "zero-inflow", '
+                          '"hard-wall" or "periodic".' % ytype, "DG:Full2D:UnknownYBoundaryType")
     periodic = ytype == "periodic"
     nrx = int(_param(prm, "N_rho_x", _param(prm, "N_xi", 40)))
     nry = int(_param(prm, "N_rho_y", nrx))
@@ -303,18 +308,55 @@ def build_factors(mat):
         ty.append((sy, oy["HI"], absy))
     elif by != 0:
         ty.append((sy, oy["HI"], by * np.eye(nry)))
-    if ytype != "periodic":
+    if ytype not in ("periodic", "hard-wall"):
         ty.append((sy, oy["HB"], absy))
     if ytype == "specular":
         flip = np.fliplr(np.eye(nry))
         ty.append((-sy, oy["lb"], Apy @ flip))
         ty.append((sy, oy["rb"], Amy @ flip))
     drift, nq = _drift_setup(prm, AX, AY, RX, RY, periodic)
+    wall = _hard_wall(AX, AY, RX, RY, y, (sx, sy)) if ytype == "hard-wall" else None
     return dict(shape=dict(n_el_x=nex, nk_x=nkx, n_el_y=ney, nk_y=nky, n_rho_x=nrx, n_rho_y=nry,
                            periodic_y=int(periodic)),
                 n=nrx * nry * nex * nkx * ney * nky, x=x, y=y, terms=(_merge(tx), _merge(ty)), axes=(AX, AY),
                 rel=(RX, RY), scales=(sx, sy), drift=drift, nq=nq, split=(Apx, Amx, Apy, Amy), ytype=ytype,
-                scale=scale)
+                scale=scale, wall=wall)
+
+
+def wall_project(f, v):
+    """T v: the hard-wall projection on the (rho_y, Y) index of a state (applyTransverse of
+    constrain_HardWall_full2D.m:52-57)."""
+    s = f["shape"]
+    ne, nl, nX = s["n_el_y"], s["nk_y"], s["n_el_x"] * s["nk_x"]
+    v5 = np.asarray(v, dtype=complex).reshape(ne, nl, nX, s["n_rho_y"], s["n_rho_x"])
+    return np.einsum("erAj,ejxrq->eAxrq", f["wall"]["blocks"], v5).reshape(-1)
+
+
+def _hard_wall(AX, AY, RX, RY, y, scales):
+    """Hard-wall geometry (get_HardWallGeometry_full2D.m:15-48, constrain_HardWall_full2D.m:10-18):
+    active [n_rho_y, nY] (both particle coordinates Y +- rho_y/2 strictly inside [y0, y1], 64 ulp
+    of the largest coordinate as margin), the exact-DG-mass projection per (Y element, rho_y cell)
+    as blocks [n_el_y, n_rho_y, nk_y, nk_y] (zero rows for inactive nodes) and the weight of the
+    constraint rows."""
+    rho, Y = RY["cells"], AY["nodes"]
+    big = max(abs(y[0]), abs(y[-1]), float(np.max(np.abs(rho))))
+    dist = np.minimum(Y - y[0], y[-1] - Y)
+    active = np.abs(rho)[:, None] / 2 < dist[None, :] - 64 * np.spacing(big)
+    if not active.any():
+        raise WignerError(_lib.WG_ERR_ARG, "No Y/rho_y samples lie inside the hard walls. Refine these grids.",
+                          "DG:Full2D:HardWallEmptyDomain")
+    nl, ne, nr = AY["nl"], AY["ne"], len(rho)
+    M = AY["M"]
+    blocks = np.zeros((ne, nr, nl, nl))
+    for e in range(ne):
+        for ir in range(nr):
+            keep = active[ir, e * nl:(e + 1) * nl]
+            if keep.any():
+                blocks[e, ir][keep] = np.linalg.solve(M[np.ix_(keep, keep)], M[keep, :])
+    sx, sy = scales
+    g = max(1.0, abs(sx) / (np.min(np.diff(AX["verts"])) * RX["delta"])
+            + abs(sy) / (np.min(np.diff(AY["verts"])) * RY["delta"]))
+    return dict(active=active, blocks=blocks, scale=g)
 
 
 def _bilinear(gx, gy, V, qx, qy, periodic):
@@ -421,10 +463,21 @@ def build_preconditioner(mat, V, f, ix=0):
         for k in range(nm):
             xinv[k, e] = np.linalg.inv(np.eye(n) + a[k] * K1 + abs(a[k]) * K2)
             xcpl[k, e] = -a[k] * (Minv @ E(0, n - 1)) if fwd[k] else a[k] * (Minv @ E(n - 1, 0))
+    wall = f.get("wall")
+    if wall is not None:       # get_LineTransversePreconditioner_full2D.m:84-88: T B P + scale (I - P)
+        act = wall["active"].T.reshape(-1).astype(float)           # index rho_y + n_rho_y Y
+        Tm = np.zeros((nT, nT))
+        nl = AY["nl"]
+        for e in range(AY["ne"]):
+            for ir in range(nry):
+                ids = ir + nry * (e * nl + np.arange(nl))
+                Tm[np.ix_(ids, ids)] = wall["blocks"][e, ir]
     tinv = np.empty((nm, nT, nT), dtype=complex)
     for k in range(nm):
-        B = (K + pw[k] * Vt + np.diag(capY + capX[k])) / sigma + np.eye(nT)
-        tinv[k] = np.linalg.inv(B)
+        B = K + pw[k] * Vt + np.diag(capY + capX[k])
+        if wall is not None:
+            B = (Tm @ B) * act[None, :] + np.diag(wall["scale"] * (1 - act))
+        tinv[k] = np.linalg.inv(B / sigma + np.eye(nT))
     return dict(U=U, lam=lam, sigma=sigma, xinv=xinv, xcpl=xcpl, fwd=fwd, tinv=tinv)
 
 
@@ -594,6 +647,12 @@ class Full2DOperator:
                                                 _lib.dptr(d["xq"]), _lib.dptr(d["yq"]), _lib.dptr(d["vx"]),
                                                 _lib.dptr(d["vy"]), _lib.dptr(pot), float(d["capc"]),
                                                 _lib.dptr(d["cap"])))
+            w = f.get("wall")
+            if w is not None:
+                act = np.ascontiguousarray(w["active"].T, dtype=np.uint8)          # [nY][n_rho_y]
+                blk = np.ascontiguousarray(w["blocks"], dtype=float)
+                self._check(self.lib.wg2d_set_hard_wall(self.h, act.ctypes.data_as(C.c_void_p), _lib.dptr(blk),
+                                                        float(w["scale"])))
             self._set_observables()
             if V is not None:
                 self.set_potential(V)
@@ -697,7 +756,10 @@ class Full2DOperator:
         if V is None:
             V = self.mat.get("V", np.zeros((len(self.x), len(self.y))))
         inflow = reservoir.get_InflowBoundary_full2D(self.mat, self.factors, EfL, EfR, V)
-        return reservoir.inflow_rhs(self.factors, inflow), inflow
+        rhs = reservoir.inflow_rhs(self.factors, inflow)
+        if self.factors.get("wall") is not None:
+            rhs = wall_project(self.factors, rhs)      # the constrained system's rhs, T b
+        return rhs, inflow
 
     def set_potential(self, V):
         """Rebuild the potential differences from V [Nx x Ny] on the material grid (device)."""

@@ -228,6 +228,12 @@ def get_InflowBoundary_full2D(mat, f, EfL, EfR, Vxy=None):
             out[side] = (np.zeros((RX["n"] * RY["n"], f["axes"][1]["nd"])), {"model": "none"})
         else:
             raise WignerError(_lib.WG_ERR_ARG, "unknown full2D_reservoirModel %r" % model)
+    if f.get("wall") is not None:
+        # hard walls: the face data only on the active (rho_y, Y) samples (get_InflowBoundary_full2D.m:36-43)
+        mask = np.repeat(f["wall"]["active"], f["rel"][0]["n"], axis=0)
+        for side in out:
+            rho, info = out[side]
+            out[side] = (rho * mask, dict(info, hardWallSupportApplied=True))
     return out
 
 

@@ -32,7 +32,7 @@ DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityT
                 poissonResidualTolerance=8e-2, transportTolerance=1e-8, transportMaxCycles=50,
                 fermiOffset=0.05, restart=50, precision="fp64", innerRestart=40, innerTol=1e-3,
                 inexactFactor=0.0, inexactCap=1e-4, reorth=0.0, innerReorth=0.0, fp64TensorCores=False,
-                deferFinal=0, keepHandles=True)
+                deferFinal=0, keepHandles=True, innerBasisFP32=False)
 
 
 def _opts(options):
@@ -61,7 +61,7 @@ class RTDSweep:
         self.P = Problem1D(batch=batch, precision=self.o["precision"], restart=self.o["restart"],
                            inner_restart=self.o["innerRestart"], inner_tol=self.o["innerTol"],
                            reorth=self.o["reorth"], inner_reorth=self.o["innerReorth"],
-                           fp64_tc=self.o["fp64TensorCores"], **shp)
+                           fp64_tc=self.o["fp64TensorCores"], inner_basis_fp32=self.o["innerBasisFP32"], **shp)
         self.lib = self.P.lib
         self.nx = int(mat["Nx"])
         self.grid = _grid_key(mat)

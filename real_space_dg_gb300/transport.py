@@ -29,12 +29,12 @@ class Problem1D:
 
     def __init__(self, n_el, n_local, nk, n_xi=None, l_xi=30e-9, batch=1, precision="fp64", restart=50,
                  m_diff=0.0, mpc=1.0, mem_budget_bytes=0.0, inner_restart=0, inner_tol=0.0, reorth=0.0,
-                 inner_reorth=0.0, fp64_tc=False):
+                 inner_reorth=0.0, fp64_tc=False, inner_basis_fp32=False):
         self.lib = _lib.load()
         prm = _lib.WgParams(int(n_el), int(n_local), int(nk), int(n_xi or nk), float(l_xi), float(m_diff),
                             float(mpc), PRECISIONS[precision] if isinstance(precision, str) else int(precision),
                             int(restart), float(mem_budget_bytes), int(inner_restart), float(inner_tol),
-                            float(reorth), float(inner_reorth), 1 if fp64_tc else 0)
+                            float(reorth), float(inner_reorth), 1 if fp64_tc else 0, 1 if inner_basis_fp32 else 0)
         h = C.c_void_p()
         st = self.lib.wg_problem_create(C.byref(prm), int(batch), C.byref(h))
         if st != _lib.WG_OK:

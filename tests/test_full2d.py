@@ -17,6 +17,7 @@ CONFIGS = [
     dict(yb="periodic", fx="upwind", fy="upwind"),          # the shape of the reference's Sim_Res run
     dict(yb="zero-inflow", fx="rusanov", fy="central"),
     dict(yb="specular", fx="upwind", fy="rusanov"),
+    dict(yb="hard-wall", fx="upwind", fy="upwind"),         # constrain_HardWall_full2D.m
 ]
 
 
@@ -32,6 +33,21 @@ def make_mat(yb="periodic", fx="upwind", fy="upwind", nex=5, ney=2, nkx=3, nky=3
     X, Y = np.meshgrid(x, y, indexing="ij")
     V = 0.1 * np.exp(-((X - 10) / 3) ** 2) + 0.02 * np.cos(2 * np.pi * Y / w)
     return mat, V
+
+
+def oracle_apply(mat, p, parts, dd, u):
+    """The oracle's A u; with hard walls the constrained apply T A (mask u) + scale (u - mask u)."""
+    if p["ytype"] != "hard-wall":
+        return F2.apply_system(p, parts, dd, u)
+    wall = F2.hard_wall_geometry(p, F2.transport_scales(mat))
+    return F2.apply_hard_wall(p, wall, lambda v: F2.apply_system(p, parts, dd, v), u)
+
+
+def oracle_matrix(mat, p, parts, dd):
+    A = (F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)).tocsr()
+    if p["ytype"] == "hard-wall":
+        A = F2.constrain_hard_wall(p, F2.hard_wall_geometry(p, F2.transport_scales(mat)), A)
+    return A
 
 
 def det_vec(n):
@@ -114,9 +130,9 @@ def test_gpu_apply_matches_oracle(built_lib, cfg, tensor_cores):
         V2 = V * 1.7 + 0.05
         op.set_potential(V2)
         y2 = op.apply(u)
-    assert rel(y, F2.apply_system(p, parts, dd, u)) < 1e-12
+    assert rel(y, oracle_apply(mat, p, parts, dd, u)) < 1e-12
     dd2 = F2.drift_data(mat, p, V2)
-    assert rel(y2, F2.apply_system(p, parts, dd2, u)) < 1e-12
+    assert rel(y2, oracle_apply(mat, p, parts, dd2, u)) < 1e-12
 
 
 @pytest.mark.gpu
@@ -194,7 +210,7 @@ def test_gpu_solve_matches_direct_solve(built_lib, cfg, fp32, mixed):
     from real_space_dg_gb300.full2d import Full2DOperator
     mat, V = make_mat(**cfg)
     p, parts, dd = F2.system(mat, V)
-    A = (F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)).tocsc()
+    A = oracle_matrix(mat, p, parts, dd).tocsc()
     b = det_vec(p["nTotal"])
     ref = spla.spsolve(A, b)
     with Full2DOperator(mat, V) as op:
@@ -206,3 +222,51 @@ def test_gpu_solve_matches_direct_solve(built_lib, cfg, fp32, mixed):
         st2, info2, x2 = op.solve(b, x0=x, tol=1e-10, maxit=5, restart=20)
         assert st2 == 0 and info2["iterations"] == 0 and info2["cycles"] == 0
         assert np.array_equal(x2, x)
+
+
+def test_oracle_hard_wall_geometry_and_constraint():
+    """get_HardWallGeometry_full2D.m: the active samples form the diamond |rho_y|/2 < distance to
+    the nearer wall; T is a projection (T T = T) that keeps every function supported on the
+    element's active nodes; the matrix-free constrained apply equals the constrained matrix, and
+    its constraint rows are scale * u."""
+    mat, V = make_mat(yb="hard-wall")
+    p, parts, dd = F2.system(mat, V)
+    wall = F2.hard_wall_geometry(p, F2.transport_scales(mat))
+    Y, rho = p["Y"]["nodes"], p["rhoY"]["cells"]
+    dist = np.minimum(Y - p["y"][0], p["y"][-1] - Y)
+    assert np.array_equal(wall["active"], np.abs(rho)[:, None] / 2 < dist[None, :] - 1e-20)
+    assert wall["active"].any() and not wall["active"].all()
+    T = wall["T"].toarray()
+    assert np.abs(T @ T - T).max() < 1e-13
+    act = wall["active"].T.reshape(-1).astype(float)
+    v = np.cos(np.arange(act.size)) * act
+    assert np.abs(T @ v - v).max() < 1e-13
+    u = det_vec(p["nTotal"])
+    A = oracle_matrix(mat, p, parts, dd)
+    y = oracle_apply(mat, p, parts, dd, u)
+    assert rel(y, A @ u) < 1e-13
+    m = F2.wall_active_mask(p, wall)
+    assert np.array_equal(y[m == 0], wall["scale"] * u[m == 0])
+
+
+def test_host_hard_wall_matches_oracle():
+    """The product's host wall data (geometry, projection blocks, scale, the rhs projection)
+    against the oracle's restatement; an empty diamond is the reference's error."""
+    from real_space_dg_gb300 import WignerError, full2d
+    mat, V = make_mat(yb="hard-wall")
+    p = F2.init_params_full2d(mat)
+    wall = F2.hard_wall_geometry(p, F2.transport_scales(mat))
+    f = full2d.build_factors(mat)
+    assert np.array_equal(f["wall"]["active"], wall["active"])
+    assert f["wall"]["scale"] == pytest.approx(wall["scale"], rel=1e-14)
+    u = det_vec(p["nTotal"])
+    assert rel(full2d.wall_project(f, u), F2.wall_project(p, wall, u)) < 1e-14
+    thin, _ = make_mat(yb="hard-wall", ney=1, nky=2)
+    thin["dg"]["params"]["L_rho_y"] = 40e-9
+    with pytest.raises(WignerError) as e:
+        full2d.build_factors(thin)
+    assert e.value.identifier == "DG:Full2D:HardWallEmptyDomain"
+    bad, _ = make_mat(yb="sticky")
+    with pytest.raises(WignerError) as e:
+        full2d.build_factors(bad)
+    assert e.value.identifier == "DG:Full2D:UnknownYBoundaryType"

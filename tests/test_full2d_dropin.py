@@ -103,3 +103,33 @@ def test_dropin_matches_sparse_lu(built_lib, solver):
         assert w["initialGuess"]["provided"] and w["initialGuess"]["convergedAtStart"]
         assert w["iterations"] == [0, 0] and w["flag"] == 0
         assert np.array_equal(warm["rho"], DG["rho"])
+
+
+@pytest.mark.gpu
+def test_dropin_hard_wall_matches_sparse_lu(built_lib):
+    """full2D_Y_boundary = 'hard-wall' through the drop-in (material-default reservoirs): the face data
+    only on the active samples, the constrained system T A P + scale (I - P) with rhs T b
+    (constrain_HardWall_full2D.m), solved by GMRES with the constrained line-transverse
+    preconditioner; against the sparse LU of the oracle's constrained matrix, 1e-8; the solution
+    vanishes on the constrained samples."""
+    import scipy.sparse.linalg as spla
+    from real_space_dg_gb300.full2d import Full2DOperator, solve_transport_DG_full2D
+    mat = small_mat("material-default", "hard-wall", nry=8)
+    XX, YY = np.meshgrid(mat["x"], mat["y"], indexing="ij")
+    mat["V"] = 1.424 + 0.15 * np.exp(-((XX - 10) / 3) ** 2) - 0.05 * XX / 20
+    mat["dg"]["params"].update(L_rho_y=8e-9, full2D_solverTol=TOL, full2D_solverMaxIt=300, full2D_gmresRestart=20)
+    V = mat["V"]
+    p, parts, dd = F2.system(mat, V)
+    wall = F2.hard_wall_geometry(p, F2.transport_scales(mat))
+    A = F2.constrain_hard_wall(p, wall, (F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"])
+                                         + F2.assemble_drift(p, dd)).tocsr()).tocsc()
+    with Full2DOperator(mat, V) as op:
+        rhs, inflow = op.reservoir_rhs(1.45, 1.40)
+    act = F2.wall_active_mask(p, wall)
+    assert np.abs(rhs[act == 0]).max() == 0 and inflow["source"][1]["hardWallSupportApplied"]
+    want = spla.spsolve(A, rhs)
+    DG = solve_transport_DG_full2D(mat, V, 1.45, 1.40)
+    s = DG["info"]["solve"]
+    assert DG["status"] == "solved-gmres" and s["flag"] == 0 and s["trueRelres"] <= TOL, s
+    assert np.linalg.norm(DG["rho"] - want) <= 1e-8 * np.linalg.norm(want)
+    assert np.abs(DG["rho"][act == 0]).max() <= 1e-12 * np.abs(want).max()

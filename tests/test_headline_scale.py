@@ -47,13 +47,18 @@ def c1_reference():
     return spec, mat, E, efl, efr, m, rho, n_ref, j_ref
 
 
-@pytest.mark.parametrize("precision,fp64_tc,tol_n,tol_j", [("fp64", False, 1e-9, 1e-8), ("fp64", True, 1e-9, 1e-8),
-                                                           ("mixed", False, 1e-8, 1e-7)])
-def test_c1_solve_matches_sparse_lu(built_lib, c1_reference, precision, fp64_tc, tol_n, tol_j):
+@pytest.mark.parametrize("precision,fp64_tc,basis16,tol_n,tol_j", [("fp64", False, False, 1e-9, 1e-8),
+                                                                   ("fp64", True, False, 1e-9, 1e-8),
+                                                                   ("mixed", False, False, 1e-8, 1e-7),
+                                                                   ("mixed", False, True, 1e-8, 1e-7)])
+def test_c1_solve_matches_sparse_lu(built_lib, c1_reference, precision, fp64_tc, basis16, tol_n, tol_j):
+    """basis16: the mixed form's inner Krylov basis stored in FP16 (the default) or in FP32; the
+    FP64 refinement holds the same bars either way."""
     from real_space_dg_gb300.transport import Problem1D, shape_from_mat
     spec, mat, E, efl, efr, m, rho, n_ref, j_ref = c1_reference
     assert spec.n_el * spec.n_local * spec.nk == 46080
-    with Problem1D(batch=1, precision=precision, restart=50, fp64_tc=fp64_tc, **shape_from_mat(mat)) as P:
+    with Problem1D(batch=1, precision=precision, restart=50, fp64_tc=fp64_tc, inner_basis_fp32=not basis16,
+                   **shape_from_mat(mat)) as P:
         P.set_potential(0, mat["x"], E, m, spec.m_rel, spec.temp_k, efl, efr)
         st, info = P.solve(tol=1e-10, maxit=200)
         assert st == 0 and info[0]["flag"] == 0 and info[0]["relres"] <= 1e-10, info
