@@ -12,8 +12,12 @@ Host driver of RTD/solve2D_rtd_self_consistent.m:1-222 around the device pieces:
 with the reference's fixed-point logic: phi starts from bias x ramp (or the previous bias point
 shifted by the bias step), the unmixed potential defect, the relative density change and the
 Poisson residual at the current potential decide convergence, and phi <- phi + mixing
-(candidate - phi).  Dirichlet contacts (phi(source) = 0, phi(drain) = bias); the Neumann-contact
-variant (prepare_RTD_neumann_contacts.m) is not built.
+(candidate - phi).  Dirichlet contacts (phi(source) = 0, phi(drain) = bias) or Neumann contacts
+(options.poissonXBoundary / mat.poisson.xBoundary = 'neumann', periodic Y and contact-mode
+reservoirs): the contact modes are calibrated once to charge neutrality at the flat bands
+(prepare_RTD_neumann_contacts.m), mu_S is held at the source's neutral level and mu_D = mu_S - bias,
+phi starts from (bias + built-in voltage) x ramp, the Poisson step is the approximate Newton one
+and convergence also asks the global charge balance (chargeNeutralityTolerance).
 """
 import time
 
@@ -30,7 +34,7 @@ from .poisson2d import make_RTD_poisson_step
 # with less Gram-Schmidt work) and lands on different, equally converged transport states.
 DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityTolerance=5e-4,
                 poissonResidualTolerance=8e-2, chargeNeutralityTolerance=1e-3, poissonMethod="",
-                initialPhi=None, initialRho=None, mixed=True, innerRestart=None)
+                poissonXBoundary="", initialPhi=None, initialRho=None, mixed=True, innerRestart=None)
 
 
 def _options(options):
@@ -44,14 +48,72 @@ def _options(options):
     return o
 
 
-def _check_phi(phi, mat, bias, periodic):
+def _check_phi(phi, mat, bias, periodic, neumann=False):
     tol = 1e-10 * max(1.0, abs(bias))
     if not np.all(np.isfinite(phi)) or phi.shape != (int(mat["Nx"]), int(mat["Ny"])):
         raise WignerError(_lib.WG_ERR_ARG, "RTD:InvalidPoissonPotential")
-    if np.abs(phi[0]).max() > tol or np.abs(phi[-1] - bias).max() > tol:
+    if not neumann and (np.abs(phi[0]).max() > tol or np.abs(phi[-1] - bias).max() > tol):
         raise WignerError(_lib.WG_ERR_ARG, "RTD:PoissonContactPotential: phi(source) = 0, phi(drain) = bias")
     if periodic and np.abs(phi[:, 0] - phi[:, -1]).max() > tol:
         raise WignerError(_lib.WG_ERR_ARG, "RTD:NonperiodicPoissonPotential")
+
+
+def rtd_doping_si(mat):
+    """(Nd, Na) [Nx x Ny] in m^-3 (RTD/get_RTD_doping_SI.m): mat.Nd / mat.Na in SI, or the legacy
+    N_d / N_a in cm^-3; both given must agree."""
+    nx, ny = int(mat["Nx"]), int(mat["Ny"])
+
+    def field(si, legacy, required):
+        if si not in mat and legacy not in mat:
+            if required:
+                raise WignerError(_lib.WG_ERR_ARG, "Provide mat.Nd [m^-3] or mat.N_d [cm^-3].", "RTD:MissingDoping")
+            return np.zeros((nx, ny))
+        v = np.asarray(mat[si] if si in mat else np.asarray(mat[legacy], dtype=float) * 1e6, dtype=float)
+        if v.shape != (nx, ny) or not np.all(np.isfinite(v)) or (v < 0).any():
+            raise WignerError(_lib.WG_ERR_ARG, "mat.%s must be a finite nonnegative Nx x Ny array" % si,
+                              "RTD:MissingDoping")
+        if si in mat and legacy in mat and \
+                np.abs(v - np.asarray(mat[legacy], dtype=float) * 1e6).max() > 1e-12 * max(1.0, v.max()):
+            raise WignerError(_lib.WG_ERR_ARG, "mat.%s and mat.%s disagree after cm^-3 to m^-3 conversion."
+                              % (si, legacy), "RTD:InconsistentDopingUnits")
+        return v
+    return field("Nd", "N_d", True), field("Na", "N_a", False)
+
+
+def prepare_RTD_neumann_contacts(mat):
+    """(mat, reference) (RTD/prepare_RTD_neumann_contacts.m): calibrate the contact modes of both
+    contacts once to charge neutrality (sheet densities from the contact columns' net doping,
+    flat bands V = Vc as the energy reference), then fix the Fermi levels ('external' model).
+    reference: sourceMuEV, neutralDrainMuEV, builtInVoltage = mu_D - mu_S."""
+    from . import full2d, reservoir
+    prm = mat["dg"]["params"]
+    model = str(prm.get("full2D_reservoirModel", "material-default")).strip().lower().replace("_", "-")
+    if full2d._ytype(prm) != "periodic" or model not in ("contact-modes", "contact-mode", "modes"):
+        raise WignerError(_lib.WG_ERR_ARG, "Neumann RTD requires periodic Y and contact-modes reservoirs.",
+                          "RTD:NeumannContactModel")
+    Nd, Na = rtd_doping_si(mat)
+    dy = np.diff(np.asarray(mat["y"], dtype=float) * 1e-9)
+
+    def sheet(v):                            # trapz(y, v) over the contact column
+        return float(0.5 * np.sum((v[1:] + v[:-1]) * dy))
+    cal = dict(prm, full2D_contactModeFermiModel="contact-neutrality", full2D_contactModeIntegrateKz=True,
+               full2D_sourceContactSheetDensity=sheet(Nd[0] - Na[0]),
+               full2D_drainContactSheetDensity=sheet(Nd[-1] - Na[-1]))
+    mcal = dict(mat, dg=dict(mat["dg"], params=cal))
+    f = full2d.build_factors(mcal)
+    Vc = np.asarray(mat["Vc"], dtype=float).reshape(int(mat["Nx"]), int(mat["Ny"]))
+    _, src = reservoir.contact_mode_reservoir(mcal, f, "source", None, Vc)
+    _, drn = reservoir.contact_mode_reservoir(mcal, f, "drain", None, Vc)
+    mu_s, mu_d = float(src["fermiLevelUsed"]), float(drn["fermiLevelUsed"])
+    if not (np.isfinite(mu_s) and np.isfinite(mu_d)):
+        raise WignerError(_lib.WG_ERR_ARG, "Both contact-mode neutrality calibrations must converge.",
+                          "RTD:ReservoirCalibration")
+    reference = dict(sourceMuEV=mu_s, neutralDrainMuEV=mu_d, builtInVoltage=mu_d - mu_s,
+                     sourceSheetDensity=cal["full2D_sourceContactSheetDensity"],
+                     drainSheetDensity=cal["full2D_drainContactSheetDensity"])
+    out = dict(mcal, dg=dict(mcal["dg"], params=dict(cal, full2D_contactModeFermiModel="external")),
+               reservoirReference=reference)
+    return out, reference
 
 
 def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
@@ -67,8 +129,24 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
     prm = mat["dg"]["params"]
     if str(prm.get("full2D_solver", "gmres")).lower() != "gmres":
         raise WignerError(_lib.WG_ERR_ARG, "RTD:SelfConsistencyNeedsGmres")
-    if str(mat.get("poisson", {}).get("xBoundary", "dirichlet")).lower() == "neumann":
-        raise WignerError(_lib.WG_ERR_ARG, "Neumann RTD contacts (prepare_RTD_neumann_contacts) are not built")
+    if o["poissonXBoundary"]:
+        mat = dict(mat, poisson=dict(mat.get("poisson", {}), xBoundary=o["poissonXBoundary"]))
+    xbc = str(mat.get("poisson", {}).get("xBoundary", "dirichlet")).strip().lower()
+    if xbc not in ("dirichlet", "neumann"):
+        raise WignerError(_lib.WG_ERR_ARG, "poisson.xBoundary must be 'dirichlet' or 'neumann'",
+                          "RTD:PoissonXBoundary")
+    neumann = xbc == "neumann"
+    reference, builtin = None, 0.0
+    if neumann:
+        if str(prm.get("full2D_Y_boundary", "")).lower() != "periodic":
+            raise WignerError(_lib.WG_ERR_ARG, "Neumann RTD contacts require periodic Y.",
+                              "RTD:PoissonBoundaryMismatch")
+        if str(mat.get("poisson", {}).get("yBoundary", "periodic")).lower() != "periodic":
+            raise WignerError(_lib.WG_ERR_ARG, "Neumann RTD contacts require periodic Poisson Y.",
+                              "RTD:PoissonBoundaryMismatch")
+        mat = dict(mat, poisson=dict(mat.get("poisson", {}), yBoundary="periodic"))
+        mat, reference = prepare_RTD_neumann_contacts(mat)
+        builtin = reference["builtInVoltage"]
     nx, ny = int(mat["Nx"]), int(mat["Ny"])
     Vc = np.asarray(mat["Vc"], dtype=float).reshape(nx, ny)
     bias = np.atleast_1d(np.asarray(mat["Vdd"], dtype=float))
@@ -78,7 +156,8 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
         raise WignerError(_lib.WG_ERR_ARG, "RTD:ContactGeometry")
     ramp = np.repeat(np.clip((x - float(mat["Lc1"])) / ramp_len, 0.0, 1.0)[:, None], ny, axis=1)
     periodic = str(prm.get("full2D_Y_boundary", "")).lower() == "periodic"
-    method = o["poissonMethod"] or mat.get("poisson", {}).get("opt", {}).get("solve", "direct")
+    method = o["poissonMethod"] or mat.get("poisson", {}).get("opt", {}).get(
+        "solve", "newton-raphson" if neumann else "direct")
     step, setup = make_RTD_poisson_step(mat, method)
     tol = float(prm.get("full2D_solverTol", 1e-6))
     restart = int(prm.get("full2D_gmresRestart", 40))
@@ -100,10 +179,11 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
     try:
         for ib in range(nb):
             if ib == 0:
-                phi = bias[0] * ramp if o["initialPhi"] is None else np.asarray(o["initialPhi"], dtype=float)
+                phi = (bias[0] + builtin) * ramp if o["initialPhi"] is None else \
+                    np.asarray(o["initialPhi"], dtype=float)
             else:
                 phi = prev_phi + (bias[ib] - bias[ib - 1]) * ramp
-            _check_phi(phi, mat, bias[ib], periodic)
+            _check_phi(phi, mat, bias[ib], periodic, neumann)
             prev_n = None
             history = []
             status, converged = "iteration-limit", False
@@ -111,6 +191,9 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                 V = Vc - phi
                 efl = float(mat["EfL"]) if "EfL" in mat else Vc[0, 0] + 0.05
                 efr = (float(mat["EfR"]) if "EfR" in mat else Vc[-1, 0] + 0.05) - bias[ib]
+                if neumann:                   # the calibrated source level, mu_S - mu_D = bias
+                    efl = reference["sourceMuEV"]
+                    efr = efl - bias[ib]
                 t0 = clock()
                 op.set_potential(V)
                 t1 = clock()
@@ -132,7 +215,7 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                 timing["transport_s"] += t3 - t2
                 h = dict(iteration=it, transportFlag=int(st), transportRelres=info["relres"],
                          gmresIterations=info["iterations"], densityChange=np.inf, potentialDefect=np.inf,
-                         poissonConverged=False, poissonPhysicalRelres=np.nan)
+                         poissonConverged=False, poissonPhysicalRelres=np.nan, relativeChargeImbalance=np.nan)
                 if st != 0 or not np.isfinite(info["relres"]) or info["relres"] > tol:
                     history.append(h)
                     status = "transport-not-converged"
@@ -146,10 +229,15 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                 t0 = clock()
                 cand, pinfo = step({"transport": {"nDG": nDG, "p": p_axes}, "phi": phi, "bias": bias[ib]})
                 timing["poisson_s"] += clock() - t0
-                _check_phi(cand, mat, bias[ib], periodic)
+                _check_phi(cand, mat, bias[ib], periodic, neumann)
                 h["poissonConverged"] = bool(pinfo["converged"])
                 h["potentialDefect"] = float(np.abs(cand - phi).max())
                 h["poissonPhysicalRelres"] = float(pinfo["physical_relres_before"])
+                balance_ok = True
+                if neumann:
+                    h["relativeChargeImbalance"] = float(pinfo["relative_charge_imbalance"])
+                    balance_ok = bool(np.isfinite(h["relativeChargeImbalance"])
+                                      and h["relativeChargeImbalance"] <= o["chargeNeutralityTolerance"])
                 history.append(h)
                 if callback is not None:
                     callback(ib, it, h)
@@ -157,7 +245,7 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                     status = "poisson-not-converged"
                     break
                 if h["potentialDefect"] <= o["potentialTolerance"] and h["densityChange"] <= o["densityTolerance"] \
-                        and h["poissonPhysicalRelres"] <= o["poissonResidualTolerance"]:
+                        and h["poissonPhysicalRelres"] <= o["poissonResidualTolerance"] and balance_ok:
                     status, converged = "fixed-point-converged", True
                     break
                 if it == int(o["maxIterations"]):
@@ -184,7 +272,11 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
     finally:
         op.close()
         setup["operator"].close()
+    if neumann:
+        sweep["reservoirMuEV"] = np.vstack([np.full(nb, reference["sourceMuEV"]),
+                                            reference["sourceMuEV"] - bias])
     return {"sweep": sweep, "histories": histories, "phi": phi, "status": "self-consistency-" + status,
+            "poissonXBoundary": xbc, "reservoirReference": reference,
             "timing": {k: round(v, 3) for k, v in timing.items()},
             "Id": np.nanmean(sweep["current"], axis=0) if sweep["current"] is not None else None,
             "converged": bool(np.all(sweep["converged"]))}
