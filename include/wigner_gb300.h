@@ -401,6 +401,12 @@ int wg_apply_noalloc(const wg_operator_view* op, const double* x, double* y, voi
  * form, FP32 accumulation.  A row-major M x K, B column-major K x N, C column-major
  * M x N, host buffers; K >= 64 and K % 8 == 0.  No counterpart in the reference. */
 int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K);
+/* Diagnostic of the failure path of the tensor-core kernels: one thread waits on an mbarrier that
+ * nothing arrives at, with the bounded wait of those kernels limited to spin_limit polls (1 .. 2^24).
+ * Returns WG_ERR_TIMEOUT with "bounded barrier wait timed out" when the wait gave up and raised its
+ * error flag, as a GEMM whose copies never land would; the context stays usable.  No counterpart in
+ * the reference. */
+int wg_debug_wait_timeout(long long spin_limit);
 /* Diagnostic: C = A * B in FP64 emulated on the tensor cores (6-bit digit slices,
  * exact BF16 products, grouped FP32 accumulation, recombination in 64-bit integer
  * fixed point, one rounding to FP64), the

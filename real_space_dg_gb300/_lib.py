@@ -178,6 +178,7 @@ class WgPoisson2dInfo(C.Structure):
 _H = C.c_void_p
 _D = C.POINTER(C.c_double)
 SIGNATURES = {
+    "wg_debug_wait_timeout": ([C.c_longlong], C.c_int),
     "wg_problem_create": ([C.POINTER(WgParams), C.c_int, C.POINTER(_H)], C.c_int),
     "wg_problem_destroy": ([_H], C.c_int),
     "wg_problem_bytes": ([C.POINTER(WgParams), C.c_int, _D], C.c_int),

@@ -684,6 +684,15 @@ int wg_debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, i
   return WG_OK;
 }
 
+int wg_debug_wait_timeout(long long spin_limit) {
+  if (spin_limit < 1 || spin_limit > (1ll << 24))
+    return fail(nullptr, WG_ERR_ARG, "wg_debug_wait_timeout: spin_limit must be in 1 .. 2^24");
+  std::string err;
+  const int rc = wg::debug_wait_timeout(spin_limit, err);
+  if (rc) return fail(nullptr, rc, "wg_debug_wait_timeout: " + err);
+  return WG_OK;
+}
+
 int wg_debug_gemm_f64_tc(const double* A, const double* B, double* C, int M, int N, int K) {
   if (!A || !B || !C) return fail(nullptr, WG_ERR_ARG, "wg_debug_gemm_f64_tc: null argument");
   std::string err;

@@ -789,6 +789,39 @@ cudaError_t launch_precondition_mixed_h(Problem& P, const float2* r, long long r
   }
 }
 
+// One thread waits on an mbarrier that nothing arrives at: the bounded wait of the GEMM kernels
+// must give up after `limit` polls, raise err and return.
+__global__ void stuck_wait_kernel(int* err, long long limit) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    tc::mbar_wait_limit(&bar, 0, err, limit);
+  }
+}
+
+int debug_wait_timeout(long long limit, std::string& err) {
+  int* d = nullptr;
+  int flag = 0;
+  cudaError_t e = cudaMalloc(&d, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, sizeof(int));
+  if (e == cudaSuccess) {
+    stuck_wait_kernel<<<1, 32>>>(d, limit);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(&flag, d, sizeof(int), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  if (e != cudaSuccess) {
+    err = std::string("CUDA: ") + cudaGetErrorString(e);
+    return WG_ERR_CUDA;
+  }
+  if (flag) {
+    err = "bounded barrier wait timed out";
+    return WG_ERR_TIMEOUT;
+  }
+  return WG_OK;
+}
+
 // Stand-alone BF16 GEMM for diagnostics: C = bf16(A) bf16(B), A row-major M x K,
 // B column-major K x N, C column-major M x N (fp32 host buffers).
 int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err) {

@@ -362,6 +362,7 @@ cudaError_t launch_stencil_mixed(Problem& P);
 cudaError_t apply_mixed_f64(Problem& P, const double2* x, double2* y);
 cudaError_t apply_mixed_repeat(Problem& P, const double2* x, int n_apply);
 int debug_gemm_bf16(const float* A, const float* B, float* C, int M, int N, int K, std::string& err);
+int debug_wait_timeout(long long limit, std::string& err);
 int gmres_solve_mixed(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);
 // FP64 GMRES or the mixed-precision refinement, by P.precision.
 int solve_dispatch(Problem& P, const wg_solve_opts& o, bool warm, wg_solve_info* info);

@@ -103,3 +103,6 @@ def test_errors_without_handle_are_statuses(built_lib):
     prm = _lib.WgParams(8, 3, 16, 16, 30e-9, 0.0, 1.0, 0, 0, 1.0)    # 1-byte budget -> OOM status
     assert lib.wg_problem_create(C.byref(prm), 1, C.byref(h)) == _lib.WG_ERR_OOM
     assert b"budget" in lib.wg_global_error()
+    # the bounded-wait diagnostic checks its limit before any CUDA call
+    assert lib.wg_debug_wait_timeout(0) == _lib.WG_ERR_ARG
+    assert b"spin_limit" in lib.wg_global_error()

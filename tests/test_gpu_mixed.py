@@ -31,6 +31,18 @@ def rel(a, b):
     return np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b))
 
 
+def test_bounded_barrier_wait_gives_up_and_leaves_the_context_usable(built_lib):
+    """The failure path of the tensor-core kernels without a GPU fault: an mbarrier wait that nothing
+    completes gives up after its poll limit, raises the error flag the host reads (WG_ERR_TIMEOUT,
+    the GEMMs' "bounded barrier wait timed out"), and the same context then runs the tcgen05 GEMM
+    correctly."""
+    from real_space_dg_gb300 import _lib
+    lib = _lib.load()
+    assert lib.wg_debug_wait_timeout(1 << 14) == _lib.WG_ERR_TIMEOUT
+    assert b"bounded barrier wait timed out" in lib.wg_global_error()
+    test_tcgen05_bf16_gemm(built_lib, 128, 64, 64)
+
+
 @pytest.mark.parametrize("M,N,K", [(256, 300, 128), (128, 64, 64), (512, 1000, 512), (40, 37, 64)])
 def test_tcgen05_bf16_gemm(built_lib, M, N, K):
     from real_space_dg_gb300 import _lib
