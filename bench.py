@@ -489,6 +489,13 @@ def other_forms(args, mat, biases, opts, ours_res, ours_info):
     _, _, res_t = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1, transportTolerance=1e-12,
                                                      transportMaxCycles=200), phi0=phis, handles=K)
     _, _, res_t8 = _run_form(mat, batch, biases, dict(plain_opts, maxIterations=1), phi0=phis, handles=K)
+    # the mixed transport at a 1e-10 residual at the same potential, and the headline form with its final
+    # re-solves at 1e-10: what the benchmark spec's 1e-7 current bar costs at C2's conditioning
+    _, _, res_m10 = _run_form(mat, batch, biases, dict(opts, maxIterations=1, transportTolerance=1e-10,
+                                                       inexactFactor=0.0, transportMaxCycles=200),
+                              phi0=phis, handles=K)
+    ms_10, info_10, res_10 = _run_form(mat, batch, biases, dict(opts, transportTolerance=1e-10,
+                                                                transportMaxCycles=200), handles=K)
 
     def arm(ms, info, form):
         conv = sum(i["status"] == 0 for i in info)
@@ -502,11 +509,15 @@ def other_forms(args, mat, biases, opts, ours_res, ours_info):
                               "as FP64 emulated on the tensor cores" % args.restart)
     mixed_exact = arm(ms_m, info_m, "mixed (BF16 transforms, FP32 flux/preconditioner, FP64 refinement), fixed 1e-8 "
                                     "transport schedule")
+    tight = arm(ms_10, info_10, "the headline form with every accepted transport solve at 1e-10 (inexact "
+                                "Gummel, final re-solves at 1e-10)")
     acc = {"reference": "plain FP64 GPU form (above), same biases",
            "headline_vs_plain_fixed_point": _compare(ours_res, res_p),
            "mixed_exact_vs_plain_fixed_point": _compare(res_m, res_p),
            "headline_transport_vs_fp64_1e-12_at_same_potential": _compare(ours_res, res_t),
            "plain_fp64_1e-8_transport_vs_fp64_1e-12_at_same_potential": _compare(res_t8, res_t),
+           "mixed_1e-10_transport_vs_fp64_1e-12_at_same_potential": _compare(res_m10, res_t),
+           "headline_at_1e-10": dict(tight, vs_plain_fixed_point=_compare(res_10, res_p)),
            "targets": {"terminal_current_rel_transport": 1e-7,
                        "fixed_point": "set by the Gummel potential tolerance 1e-6 V, the same for both loops",
                        "note": "a 1e-8 relative residual bounds the current error only to ~cond * 1e-8; the plain "
