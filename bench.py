@@ -1459,9 +1459,11 @@ def main():
     ap.add_argument("--inner-tol", type=float, default=1e-3)
     ap.add_argument("--max-gummel", type=int, default=0,
                     help="cap on Gummel iterations for profiling runs (0: run to convergence)")
-    ap.add_argument("--inexact", type=float, default=0.3,
-                    help="inexact Gummel factor (transport tol = factor * potential defect); 0 = fixed 1e-8")
-    ap.add_argument("--inexact-cap", type=float, default=1e-3,
+    ap.add_argument("--inexact", type=float, default=0.5,
+                    help="inexact Gummel factor (transport tol = factor * potential defect); 0 = fixed 1e-8 "
+                         "(C2 sweep, points/s: 0.1 23.4, 0.3 31.3, 0.5 37.5-38.0, 0.7 41.8, 1.0 45.5 at cap 1e-2; "
+                         "3.0 and 10.0 do not converge)")
+    ap.add_argument("--inexact-cap", type=float, default=1e-2,
                     help="loosest transport tolerance of the inexact Gummel schedule")
     ap.add_argument("--reorth", type=float, default=0.0,
                     help="DGKS re-orthogonalisation threshold of the FP64 Arnoldi (0: 1/sqrt(2), <0 never, >=1 always)")
