@@ -21,6 +21,7 @@ Two sweep modes:
 """
 import atexit
 import ctypes as C
+import threading
 
 import numpy as np
 
@@ -150,7 +151,6 @@ def run_concurrent(sweeps, **kw):
     """Run the Gummel loops of several handles at once, one host thread per handle: each handle
     works on its own CUDA stream, so the latency-bound launch chains of the handles overlap on the
     device.  Returns [(status, info)] per handle; an error of any handle is raised."""
-    import threading
     out = [None] * len(sweeps)
     errors = []
 
@@ -173,22 +173,34 @@ def run_concurrent(sweeps, **kw):
 
 
 _KEPT = {"key": None, "sweeps": []}
+_KEPT_LOCK = threading.Lock()
 
 
 def _take_kept(key):
-    """The kept handles when they match ``key`` (taken out, so that a concurrent call cannot
-    share them), else None."""
-    if _KEPT["key"] != key:
-        return None
-    sweeps = _KEPT["sweeps"]
-    _KEPT.update(key=None, sweeps=[])
+    """The kept handles when they match ``key`` (taken out under the lock, so that a concurrent
+    call cannot share them), else None."""
+    with _KEPT_LOCK:
+        if _KEPT["key"] != key:
+            return None
+        sweeps = _KEPT["sweeps"]
+        _KEPT.update(key=None, sweeps=[])
     return sweeps
+
+
+def _keep(key, sweeps):
+    """Keep ``sweeps`` for the next call; a set kept meanwhile by another thread is closed."""
+    with _KEPT_LOCK:
+        old = _KEPT["sweeps"]
+        _KEPT.update(key=key, sweeps=sweeps)
+    for sw in old:
+        sw.close()
 
 
 def release_handles():
     """Close the handles solve_rtd_self_consistent keeps for its next call."""
-    sweeps = _KEPT["sweeps"]
-    _KEPT.update(key=None, sweeps=[])
+    with _KEPT_LOCK:
+        sweeps = _KEPT["sweeps"]
+        _KEPT.update(key=None, sweeps=[])
     for sw in sweeps:
         sw.close()
 
@@ -267,7 +279,7 @@ def solve_rtd_self_consistent(mat, biases, options=None, mode="batched", handles
             sw.close()
         raise
     if keep:
-        _KEPT.update(key=key, sweeps=sweeps)
+        _keep(key, sweeps)
     else:
         for sw in sweeps:
             sw.close()
