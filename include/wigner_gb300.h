@@ -504,6 +504,14 @@ int wg2d_set_drift(wg2d_problem* h, const double* interp, const double* proj, co
  * and Y clamped or wrapped (get_Drift_full2D.m:620-666). */
 int wg2d_set_potential(wg2d_problem* h, int nx, int ny, const double* gx, const double* gy, const double* V);
 
+/* Y masks of the rho_x-axis transport terms set by wg2d_set_transport (axis 0): masks[t][iY] = 1 where
+ * term t acts.  The closed (masked-off) pieces of the outer X faces take the rho_x-reflected interior
+ * state as their incoming characteristics (get_Diff_full2D.m:393-423, with centre factor
+ * kron(diag(closed), leftBoundary / rightBoundary) and relative factor A+- R_x); the caller sets those
+ * corrections as terms with their closed Y dofs as mask.  masks = NULL: every term acts everywhere.
+ * Must follow wg2d_set_transport (which clears the masks). */
+int wg2d_set_transport_masks(wg2d_problem* h, int axis, int n_terms, const unsigned char* masks);
+
 /* Hard-wall Y boundary (full2D_Y_boundary = 'hard-wall'; replaces constrain_HardWall_full2D.m:1-44 with
  * get_HardWallGeometry_full2D.m:15-48): every apply becomes T A (mask u) + scale (u - mask u).
  * active [nY][n_rho_y] (1: the sample's two particle coordinates Y +- rho_y/2 lie inside the Y

@@ -18,8 +18,8 @@ stationary Full-2D Wigner operator A = A_diff + G_drift:
     with independent clamping / periodic wrapping, linear interpolation),
     core/get_CAP_full2D.m, core/get_CAP.m.
 
-Scope: the source/drain faces fully open (all contact-mask entries 1, so no
-closed-face reflection parts); Y boundaries 'periodic', 'zero-inflow',
+Scope: the source/drain faces with their contact masks (core/get_ContactMask_full2D.m;
+the closed pieces reflect rho_x, get_Diff_full2D.m:393-423); Y boundaries 'periodic', 'zero-inflow',
 'specular' or 'hard-wall' (core/get_HardWallGeometry_full2D.m,
 core/constrain_HardWall_full2D.m: the two-point Dirichlet constraint of the
 complete operator); constant-mass transport; FV-consistent potential.  The reservoir
@@ -209,8 +209,73 @@ def transport_scales(mat):
     return f * sx, f * sy
 
 
+def _nearest(values, grid, target):
+    """interp1(grid, values, target, 'nearest', 'extrap'): the value of the nearest grid point (a
+    target halfway between two points takes the upper one)."""
+    grid = np.asarray(grid, dtype=float)
+    i = np.clip(np.searchsorted(grid, target, side="right") - 1, 0, len(grid) - 1)
+    j = np.minimum(i + 1, len(grid) - 1)
+    up = (j > i) & (target - grid[i] >= grid[j] - target)
+    return np.asarray(values)[np.where(up, j, i)]
+
+
+def contact_mask(mat, p, side):
+    """get_ContactMask_full2D.m:14-120: the face Y dofs that receive Source/Drain inflow (the rest
+    of the outer X face is closed).  Explicit full2D_<side>ContactMask (per face dof or per material
+    y point), else the doping at the X edge above full2D_contactNdThreshold, else the material gap
+    (Eg below the middle of Eg_c and Eg_ox) or the W_c / W_cy geometry, else the whole face; an empty
+    mask falls back to the material/geometry rule."""
+    prm = mat["dg"]["params"]
+    scale = p["coordinateScale"]
+    y_face = p["Y"]["nodes"]
+    grid = np.asarray(mat["y"], dtype=float) * scale
+    nx, ny = int(mat["Nx"]), int(mat["Ny"])
+    ix = 0 if side == "source" else nx - 1
+
+    def xy(field):
+        a = np.squeeze(np.asarray(field, dtype=float))
+        if a.shape == (nx, ny):
+            return a
+        if a.shape == (ny, nx):
+            return a.T
+        if a.ndim == 1 and a.size == nx:
+            return np.repeat(a[:, None], ny, axis=1)
+        if a.ndim == 1 and a.size == ny:
+            return np.repeat(a[None, :], nx, axis=0)
+        raise ValueError("DG:Full2D:InvalidMaterialField")
+
+    def material():
+        if mat.get("Eg") is not None and mat.get("Eg_ox") is not None:
+            eg = xy(mat["Eg"])
+            thr = 0.5 * (float(mat.get("Eg_c", eg.min())) + float(mat["Eg_ox"]))
+            return _nearest(eg[ix] < thr, grid, y_face).astype(bool)
+        for wo, wc in (("W_ox", "W_c"), ("W_oxy", "W_cy")):
+            if wo in mat and wc in mat:
+                return (y_face >= 0) & (y_face <= float(mat[wc]) * scale)
+        return np.ones(y_face.size, dtype=bool)
+
+    explicit = prm.get("full2D_%sContactMask" % side)
+    if explicit is not None and np.size(explicit) > 0:
+        m = np.ravel(np.asarray(explicit))
+        if m.size == y_face.size:
+            mask = m.astype(bool)
+        elif m.size == ny:
+            mask = _nearest(m.astype(float), grid, y_face) > 0.5
+        else:
+            raise ValueError("DG:Full2D:InvalidContactMask")
+    elif mat.get("Nd") is not None and np.size(mat["Nd"]) > 0:
+        thr = float(prm.get("full2D_contactNdThreshold", 0.0) or 0.0)
+        mask = _nearest((xy(mat["Nd"])[ix] > thr).astype(float), grid, y_face) > 0.5
+    else:
+        mask = material()
+    if not mask.any():
+        mask = material()
+    return np.asarray(mask, dtype=bool)
+
+
 def diff_operator_parts(mat, p):
-    """[(name, coefficient, centre matrix, relative matrix)] of get_Diff_full2D.m:76-146."""
+    """[(name, coefficient, centre matrix, relative matrix)] of get_Diff_full2D.m:76-146, with the
+    closed-face reflection parts of :393-423 on the masked-off Y dofs of the outer X faces."""
     prm = mat["dg"]["params"]
     fx, fy = flux_types(mat)
     ox = one_dimensional_dg_operators(p["X"])
@@ -240,6 +305,14 @@ def diff_operator_parts(mat, p):
     elif bx != 0:
         parts.append(("X interior Rusanov", sx, sp.kron(IY, ox["H2Interior"]), bx * IR))
     parts.append(("X boundary penalty", sx, sp.kron(IY, ox["H2Boundary"]), absx))
+    # closed pieces of the outer X faces reflect rho_x -> -rho_x (R_x = I_rho_y kron Flip_rho_x)
+    Rx = sp.kron(Iry, sp.csr_matrix(np.fliplr(np.eye(nrx))))
+    for side, sign, lift, Ach in (("source", -1.0, ox["leftBoundary"], Apx), ("drain", 1.0, ox["rightBoundary"], Amx)):
+        closed = ~contact_mask(mat, p, side)
+        if closed.any():
+            parts.append(("X-%s closed-face reflection correction" % ("left" if side == "source" else "right"),
+                          sign * sx, sp.kron(sp.diags(closed.astype(float)), lift),
+                          sp.kron(Iry, sp.csr_matrix(Ach)) @ Rx))
     parts.append(("Y central", sy, sp.kron(oy["H1"], IX), p["Ay"]))
     if fy == "upwind":
         parts.append(("Y interior upwind", sy, sp.kron(oy["H2Interior"], IX), absy))

@@ -194,6 +194,7 @@ SIGNATURES = {
     "wg2d_set_drift": ([_H, _D, _D, _D, _D, _D, _D, _D, C.c_double, _D], C.c_int),
     "wg2d_set_potential": ([_H, C.c_int, C.c_int, _D, _D, _D], C.c_int),
     "wg2d_set_hard_wall": ([_H, C.c_void_p, _D, C.c_double], C.c_int),
+    "wg2d_set_transport_masks": ([_H, C.c_int, C.c_int, C.c_void_p], C.c_int),
     "wg2d_apply": ([_H, _D, _D], C.c_int),
     "wg2d_apply_repeat": ([_H, C.c_int, _D, _D], C.c_int),
     "wg2d_set_preconditioner": ([_H, _D, C.c_double, _D, _D, C.POINTER(C.c_int), _D, C.c_int], C.c_int),

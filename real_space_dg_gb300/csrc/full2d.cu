@@ -52,6 +52,7 @@ struct wg2d_problem {
     int* offs = nullptr;        // [T] start of term t in col / val
     double* dcoef = nullptr;    // [T]
     unsigned dense_mask = 0;    // terms applied by the emulated FP64 GEMM (rho_x axis)
+    unsigned char* ymask = nullptr;   // rho_x axis: [T][nY] 1 where term t acts (closed X-face pieces); null: all
     std::vector<wg::OzakiRowsDev> dense;   // [T] digit slices of c_t R_t (real embedding) for those terms
   } ax[2];
   wg::OzakiColsDev cols;        // digit slices of the centre-applied state (rho_x columns)
@@ -196,7 +197,9 @@ __global__ void __launch_bounds__(512) f2d_relx_kernel(const T* __restrict__ G, 
                                                        const int* __restrict__ rp, const int* __restrict__ col,
                                                        const T* __restrict__ val, const int* __restrict__ nnz_off,
                                                        const R* __restrict__ coef, int nterm, int nrx,
-                                                       long long ncols, long long n, unsigned skip_mask) {
+                                                       long long ncols, long long n, unsigned skip_mask,
+                                                       const unsigned char* __restrict__ ymask = nullptr,
+                                                       long long cols_per_y = 1, int nY = 1) {
   extern __shared__ __align__(16) unsigned char sgr_raw[];
   T* sg = reinterpret_cast<T*>(sgr_raw);   // [kRelxCols][nrx]
   const long long c0 = (long long)blockIdx.x * kRelxCols;
@@ -210,7 +213,9 @@ __global__ void __launch_bounds__(512) f2d_relx_kernel(const T* __restrict__ G, 
     __syncthreads();
     for (int i = threadIdx.x; i < kRelxCols * nrx; i += blockDim.x) {
       const int j = i / nrx, k = i - j * nrx;
-      sg[i] = j < nc ? G[(long long)t * n + (c0 + j) * nrx + k] : czero<T>();
+      // a masked term (a closed X-face piece) acts only on its own Y dofs
+      const bool on = j < nc && (!ymask || ymask[(long long)t * nY + (c0 + j) / cols_per_y]);
+      sg[i] = on ? G[(long long)t * n + (c0 + j) * nrx + k] : czero<T>();
     }
     __syncthreads();
     if (rx < nrx) {
@@ -1074,6 +1079,7 @@ void free_axis(wg2d_problem::Axis& a) {
   cudaFree(a.val);
   cudaFree(a.offs);
   cudaFree(a.dcoef);
+  cudaFree(a.ymask);
   a = wg2d_problem::Axis{};
 }
 
@@ -1115,7 +1121,8 @@ void transport_terms(wg2d_problem* h, int axis, const OpData<T, R>& d, const T* 
     const int threads = (h->nrx + 31) / 32 * 32;
     if (skip_mask != (1u << a.T) - 1u)
       f2d_relx_kernel<T, R><<<(unsigned)((ncols + kRelxCols - 1) / kRelxCols), threads, smem, h->stream>>>(
-          d.G, y, a.rp, a.col, d.val[0], a.offs, d.coef[0], a.T, h->nrx, ncols, h->n, skip_mask);
+          d.G, y, a.rp, a.col, d.val[0], a.offs, d.coef[0], a.T, h->nrx, ncols, h->n, skip_mask, a.ymask,
+          (long long)h->nry * h->nX, h->nY);
   } else {
     f2d_rely_kernel<T, R><<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(d.G, y, a.rp, a.col, d.val[1], a.offs,
                                                                                 d.coef[1], a.T, h->nrx, h->nry, h->n);
@@ -1628,6 +1635,30 @@ static void free_preconditioner(wg2d_problem* h) {
   h->fwd = nullptr;
   h->pre32 = false;
   h->pre_ready = false;
+}
+
+int wg2d_set_transport_masks(wg2d_problem* h, int axis, int n_terms, const unsigned char* masks) {
+  if (!h) return WG_ERR_ARG;
+  if (axis != 0) return fail(h, WG_ERR_ARG, "wg2d_set_transport_masks: only the rho_x axis (0) takes Y masks");
+  wg2d_problem::Axis& a = h->ax[0];
+  if (n_terms != a.T) return fail(h, WG_ERR_ARG, "wg2d_set_transport_masks: n_terms must equal the terms set");
+  cudaStreamSynchronize(h->stream);
+  cudaFree(a.ymask);
+  a.ymask = nullptr;
+  if (!masks) return WG_OK;
+  const size_t nm = (size_t)n_terms * h->nY;
+  F2_CK(cudaMalloc(&a.ymask, nm));
+  F2_CK(cudaMemcpy(a.ymask, masks, nm, cudaMemcpyHostToDevice));
+  // a masked term leaves the dense tensor-core path (which applies a term on every column)
+  for (int t = 0; t < n_terms; ++t) {
+    bool all = true;
+    for (int i = 0; i < h->nY; ++i) all = all && masks[(size_t)t * h->nY + i];
+    if (!all && ((a.dense_mask >> t) & 1u)) {
+      wg::ozaki_free(a.dense[t]);
+      a.dense_mask &= ~(1u << t);
+    }
+  }
+  return WG_OK;
 }
 
 int wg2d_set_hard_wall(wg2d_problem* h, const unsigned char* active, const double* projection, double scale) {

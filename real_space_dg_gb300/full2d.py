@@ -316,11 +316,83 @@ def build_factors(mat):
         ty.append((sy, oy["rb"], Amy @ flip))
     drift, nq = _drift_setup(prm, AX, AY, RX, RY, periodic)
     wall = _hard_wall(AX, AY, RX, RY, y, (sx, sy)) if ytype == "hard-wall" else None
+    # closed pieces of the outer X faces (get_Diff_full2D.m:393-423): the incoming characteristics there
+    # are the rho_x-reflected interior state, a correction on the masked-off Y dofs only
+    masks = {side: contact_mask(mat, AY, y, side, scale) for side in ("source", "drain")}
+    flip = np.fliplr(np.eye(nrx))
+    closed = []
+    for side, sign, lift, Ach in (("source", -1.0, ox["lb"], Apx), ("drain", 1.0, ox["rb"], Amx)):
+        if not masks[side].all() and sx != 0:
+            closed.append((sign * sx, lift, Ach @ flip, ~masks[side]))
     return dict(shape=dict(n_el_x=nex, nk_x=nkx, n_el_y=ney, nk_y=nky, n_rho_x=nrx, n_rho_y=nry,
                            periodic_y=int(periodic)),
                 n=nrx * nry * nex * nkx * ney * nky, x=x, y=y, terms=(_merge(tx), _merge(ty)), axes=(AX, AY),
                 rel=(RX, RY), scales=(sx, sy), drift=drift, nq=nq, split=(Apx, Amx, Apy, Amy), ytype=ytype,
-                scale=scale, wall=wall)
+                scale=scale, wall=wall, contact_masks=masks, closed_terms=closed)
+
+
+def _nearest(values, grid, target):
+    """interp1(grid, values, target, 'nearest', 'extrap'), a target halfway between two grid points
+    taking the upper one."""
+    grid = np.asarray(grid, dtype=float)
+    target = np.asarray(target, dtype=float)
+    lo = np.clip(np.searchsorted(grid, target, side="right") - 1, 0, len(grid) - 1)
+    hi = np.minimum(lo + 1, len(grid) - 1)
+    up = (hi > lo) & (target - grid[lo] >= grid[hi] - target)
+    return np.asarray(values)[np.where(up, hi, lo)]
+
+
+def contact_mask(mat, AY, y, side, scale):
+    """The Y dofs of the outer X face at ``side`` that receive reservoir inflow
+    (get_ContactMask_full2D.m:14-120); the others are closed.  In order: an explicit
+    full2D_<side>ContactMask (per face dof, or per material y point taken to the nearest), the
+    doping of the edge column above full2D_contactNdThreshold, the material gap (Eg below the middle
+    of Eg_c and Eg_ox) or the W_c / W_cy geometry, the whole face; an empty mask falls back to the
+    material / geometry rule."""
+    prm = mat["dg"]["params"]
+    y_face = AY["nodes"]
+    nx, ny = int(mat["Nx"]), int(mat["Ny"])
+    ix = 0 if side == "source" else nx - 1
+
+    def xy(field):
+        a = np.squeeze(np.asarray(field, dtype=float))
+        if a.shape == (nx, ny):
+            return a
+        if a.shape == (ny, nx):
+            return a.T
+        if a.ndim == 1 and a.size in (nx, ny):
+            return np.repeat(a[:, None], ny, axis=1) if a.size == nx else np.repeat(a[None, :], nx, axis=0)
+        raise WignerError(_lib.WG_ERR_ARG, "Cannot interpret material field with size %s as an X/Y field."
+                          % (a.shape,), "DG:Full2D:InvalidMaterialField")
+
+    def material():
+        if mat.get("Eg") is not None and mat.get("Eg_ox") is not None:
+            eg = xy(mat["Eg"])
+            thr = 0.5 * (float(mat.get("Eg_c", eg.min())) + float(mat["Eg_ox"]))
+            return _nearest(eg[ix] < thr, y, y_face).astype(bool)
+        for wo, wc in (("W_ox", "W_c"), ("W_oxy", "W_cy")):
+            if wo in mat and wc in mat:
+                return (y_face >= 0) & (y_face <= float(mat[wc]) * scale)
+        return np.ones(y_face.size, dtype=bool)
+
+    explicit = prm.get("full2D_%sContactMask" % side)
+    if explicit is not None and np.size(explicit) > 0:
+        m = np.ravel(np.asarray(explicit))
+        if m.size == y_face.size:
+            mask = m.astype(bool)
+        elif m.size == ny:
+            mask = _nearest(m.astype(float), y, y_face) > 0.5
+        else:
+            raise WignerError(_lib.WG_ERR_ARG, "Contact mask has %d entries, expected %d face DOFs or mat.Ny "
+                              "entries." % (m.size, y_face.size), "DG:Full2D:InvalidContactMask")
+    elif mat.get("Nd") is not None and np.size(mat["Nd"]) > 0:
+        thr = float(prm.get("full2D_contactNdThreshold", 0.0) or 0.0)
+        mask = _nearest((xy(mat["Nd"])[ix] > thr).astype(float), y, y_face) > 0.5
+    else:
+        mask = material()
+    if not mask.any():
+        mask = material()
+    return np.asarray(mask, dtype=bool)
 
 
 def wall_project(f, v):
@@ -639,8 +711,17 @@ class Full2DOperator:
             raise WignerError(rc, "wg2d_create failed")
         self.h = h
         try:
-            for axis, (terms, ax, nr) in enumerate(((self.terms[0], AX, nrx), (self.terms[1], AY, nry))):
+            closed = f.get("closed_terms") or []
+            xterms = list(self.terms[0]) + [t[:3] for t in closed]
+            for axis, (terms, ax, nr) in enumerate(((xterms, AX, nrx), (self.terms[1], AY, nry))):
                 self._set_axis(axis, terms, ax, nr, periodic and axis == 1)
+            if closed:       # the closed-face corrections act on their masked-off Y dofs only
+                masks = np.ones((len(xterms), AY["nd"]), dtype=np.uint8)
+                for i, t in enumerate(closed):
+                    masks[len(self.terms[0]) + i] = t[3].astype(np.uint8)
+                masks = np.ascontiguousarray(masks)
+                self._check(self.lib.wg2d_set_transport_masks(self.h, 0, len(xterms),
+                                                              masks.ctypes.data_as(C.c_void_p)))
             d = self.drift
             pot = np.array([d["pot"].real, d["pot"].imag])
             self._check(self.lib.wg2d_set_drift(self.h, _lib.dptr(d["interp"]), _lib.dptr(d["proj"]),

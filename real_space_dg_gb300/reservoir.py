@@ -213,10 +213,10 @@ def get_InflowBoundary_full2D(mat, f, EfL, EfR, Vxy=None):
     if Vxy is None:
         Vxy = mat.get("V", np.zeros((int(mat["Nx"]), int(mat["Ny"]))))
     model = str(_p(prm, "full2D_reservoirModel", "material-default")).strip().lower().replace("_", "-")
-    for name in ("full2D_sourceContactMask", "full2D_drainContactMask"):
-        m = prm.get(name)
-        if m is not None and not np.all(np.asarray(m, dtype=bool)):
-            raise WignerError(_lib.WG_ERR_ARG, "closed X-face segments (contact masks) are not built on the device")
+    masks = f.get("contact_masks") or {}
+    if f.get("ytype") == "periodic" and not all(np.all(m) for m in masks.values()):
+        raise WignerError(_lib.WG_ERR_ARG, "Periodic two-point contacts currently require full-width Source/Drain "
+                          "masks.", "DG:Full2D:PeriodicContactMask")
     out = {}
     for side, ef in (("source", EfL), ("drain", EfR)):
         if model in ("contact-modes", "contact-mode", "modes"):
@@ -228,6 +228,12 @@ def get_InflowBoundary_full2D(mat, f, EfL, EfR, Vxy=None):
             out[side] = (np.zeros((RX["n"] * RY["n"], f["axes"][1]["nd"])), {"model": "none"})
         else:
             raise WignerError(_lib.WG_ERR_ARG, "unknown full2D_reservoirModel %r" % model)
+    for side in out:
+        # reservoir data only on the contact pieces of the face (applyContactMask, get_InflowBoundary_full2D.m:23-24)
+        m = masks.get(side)
+        if m is not None and not np.all(m):
+            rho, info = out[side]
+            out[side] = (rho * m[None, :], dict(info, contactMask=np.asarray(m, dtype=bool)))
     if f.get("wall") is not None:
         # hard walls: the face data only on the active (rho_y, Y) samples (get_InflowBoundary_full2D.m:36-43)
         mask = np.repeat(f["wall"]["active"], f["rel"][0]["n"], axis=0)

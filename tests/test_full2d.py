@@ -18,15 +18,19 @@ CONFIGS = [
     dict(yb="zero-inflow", fx="rusanov", fy="central"),
     dict(yb="specular", fx="upwind", fy="rusanov"),
     dict(yb="hard-wall", fx="upwind", fy="upwind"),         # constrain_HardWall_full2D.m
+    dict(yb="zero-inflow", fx="upwind", fy="upwind", masks=True),   # closed X-face pieces (contact masks)
 ]
 
 
-def make_mat(yb="periodic", fx="upwind", fy="upwind", nex=5, ney=2, nkx=3, nky=3, nrx=9, nry=4, nq=5):
+def make_mat(yb="periodic", fx="upwind", fy="upwind", nex=5, ney=2, nkx=3, nky=3, nrx=9, nry=4, nq=5, masks=False):
     lx, w = 20.0, 4.0
     nx, ny = nex * (nkx - 1) + 1, ney * (nky - 1) + 1
     x, y = np.linspace(0, lx, nx), np.linspace(0, w, ny)
     prm = dict(N_K_X=nkx, N_K_Y=nky, N_el_X=nex, N_el_Y=ney, N_rho_x=nrx, N_rho_y=nry, L_rho_x=8e-9,
                full2D_X_flux=fx, full2D_Y_flux=fy, full2D_Y_boundary=yb, full2D_potentialQuadratureOrder=nq)
+    if masks:     # contacts on part of each outer X face (per material y point); the rest is closed
+        prm["full2D_sourceContactMask"] = (y > 0.5) & (y < 3.5)
+        prm["full2D_drainContactMask"] = y < 2.5
     if yb != "periodic":
         prm["L_rho_y"] = 3e-9
     mat = dict(x=x, y=y, Nx=nx, Ny=ny, dg=dict(params=prm))
@@ -101,6 +105,9 @@ def test_host_factors_reassemble_the_oracle_operator(cfg):
     A = sp.csr_matrix((p["nTotal"], p["nTotal"]), dtype=complex)
     for c, Cm, R in f["terms"][0]:
         A = A + c * sp.kron(sp.kron(sp.identity(nY), sp.csr_matrix(Cm)), sp.kron(sp.identity(nry), sp.csr_matrix(R)))
+    for c, Cm, R, m in f["closed_terms"]:      # closed X-face pieces: only their Y dofs
+        A = A + c * sp.kron(sp.kron(sp.diags(m.astype(float)), sp.csr_matrix(Cm)),
+                            sp.kron(sp.identity(nry), sp.csr_matrix(R)))
     for c, Cm, R in f["terms"][1]:
         A = A + c * sp.kron(sp.kron(sp.csr_matrix(Cm), sp.identity(nX)), sp.kron(sp.csr_matrix(R), sp.identity(nrx)))
     ref = F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"])
@@ -270,3 +277,43 @@ def test_host_hard_wall_matches_oracle():
     with pytest.raises(WignerError) as e:
         full2d.build_factors(bad)
     assert e.value.identifier == "DG:Full2D:UnknownYBoundaryType"
+
+
+def test_contact_masks_match_oracle_and_close_the_face():
+    """get_ContactMask_full2D.m: the explicit per-y masks taken to the face dofs by nearest
+    neighbour, the doping-edge rule with its threshold, and the whole face without data; the host's
+    masks equal the oracle's; the closed pieces add the reflected-characteristic parts (the assembled
+    operators differ exactly there)."""
+    from real_space_dg_gb300 import full2d
+    mat, V = make_mat(yb="zero-inflow", masks=True)
+    p = F2.init_params_full2d(mat)
+    f = full2d.build_factors(mat)
+    for side in ("source", "drain"):
+        want = F2.contact_mask(mat, p, side)
+        assert np.array_equal(f["contact_masks"][side], want)
+        assert want.any() and not want.all()
+    assert len(f["closed_terms"]) == 2
+    nd_mat, _ = make_mat(yb="zero-inflow")
+    Nd = np.full((nd_mat["Nx"], nd_mat["Ny"]), 1e24)
+    Nd[:, 0] = 0.0
+    nd_mat["Nd"] = Nd
+    pn = F2.init_params_full2d(nd_mat)
+    m = F2.contact_mask(nd_mat, pn, "drain")
+    assert not m[0] and m[1:].all()
+    assert np.array_equal(full2d.build_factors(nd_mat)["contact_masks"]["drain"], m)
+    nd_mat["dg"]["params"]["full2D_contactNdThreshold"] = 2e24          # nothing above: whole face
+    assert F2.contact_mask(nd_mat, pn, "source").all()
+    open_mat, _ = make_mat(yb="zero-inflow")
+    p0, parts0, dd0 = F2.system(open_mat, V)
+    p1, parts1, dd1 = F2.system(mat, V)
+    extra = [q for q in parts1 if "closed-face" in q[0]]
+    assert len(extra) == 2 and len(parts1) == len(parts0) + 2
+
+
+def test_periodic_contacts_need_full_masks():
+    from real_space_dg_gb300 import WignerError, full2d, reservoir
+    mat, V = make_mat(yb="periodic", masks=True)
+    f = full2d.build_factors(mat)
+    with pytest.raises(WignerError) as e:
+        reservoir.get_InflowBoundary_full2D(mat, f, 1.45, 1.40, V)
+    assert e.value.identifier == "DG:Full2D:PeriodicContactMask"

@@ -133,3 +133,36 @@ def test_dropin_hard_wall_matches_sparse_lu(built_lib):
     assert DG["status"] == "solved-gmres" and s["flag"] == 0 and s["trueRelres"] <= TOL, s
     assert np.linalg.norm(DG["rho"] - want) <= 1e-8 * np.linalg.norm(want)
     assert np.abs(DG["rho"][act == 0]).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.gpu
+def test_dropin_contact_masks_match_sparse_lu(built_lib):
+    """Source and drain contacts on part of the outer X faces (full2D_<side>ContactMask): the reservoir
+    data only on the contact pieces, the closed pieces reflecting rho_x (get_Diff_full2D.m:393-423,
+    get_InflowBoundary_full2D.m:23-24); the drop-in's GMRES solve against the sparse LU of the
+    oracle's operator with those parts, 1e-8."""
+    import scipy.sparse.linalg as spla
+    from real_space_dg_gb300.full2d import Full2DOperator, solve_transport_DG_full2D
+    mat = small_mat("material-default", "zero-inflow")
+    y = np.asarray(mat["y"], dtype=float)
+    XX, YY = np.meshgrid(mat["x"], y, indexing="ij")
+    mat["V"] = 1.424 + 0.15 * np.exp(-((XX - 10) / 3) ** 2) - 0.05 * XX / 20
+    mat["dg"]["params"].update(full2D_solverTol=TOL, full2D_solverMaxIt=300, full2D_gmresRestart=20,
+                               full2D_sourceContactMask=(y > 0.5) & (y < 3.5), full2D_drainContactMask=y < 2.5)
+    V = mat["V"]
+    p, parts, dd = F2.system(mat, V)
+    assert sum("closed-face" in q[0] for q in parts) == 2
+    A = (F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)).tocsc()
+    with Full2DOperator(mat, V) as op:
+        rhs, inflow = op.reservoir_rhs(1.45, 1.40)
+        u = np.sin(np.arange(p["nTotal"])) + 1j * np.cos(0.3 * np.arange(p["nTotal"]))
+        assert np.linalg.norm(op.apply(u) - A @ u) <= 1e-12 * np.linalg.norm(A @ u)
+    for side in ("source", "drain"):
+        rho_b, info = inflow[side]
+        closed = ~F2.contact_mask(mat, p, side)
+        assert np.abs(rho_b[:, closed]).max() == 0 and np.abs(rho_b[:, ~closed]).max() > 0
+    want = spla.spsolve(A, rhs)
+    DG = solve_transport_DG_full2D(mat, V, 1.45, 1.40)
+    s = DG["info"]["solve"]
+    assert DG["status"] == "solved-gmres" and s["flag"] == 0 and s["trueRelres"] <= TOL, s
+    assert np.linalg.norm(DG["rho"] - want) <= 1e-8 * np.linalg.norm(want)

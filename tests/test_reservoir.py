@@ -113,9 +113,15 @@ def test_host_reservoir_errors():
     with pytest.raises(WignerError):
         PR.contact_mode_reservoir(mat, f, "source", 1.45, V)
     mat = small_mat("material-default", "zero-inflow")
-    mat["dg"]["params"]["full2D_sourceContactMask"] = [1, 1, 0, 1, 1, 1]
-    with pytest.raises(WignerError):
-        PR.get_InflowBoundary_full2D(mat, H.build_factors(mat), 1.45, 1.4, np.full((11, 5), 1.424))
+    mat["dg"]["params"]["full2D_sourceContactMask"] = [1, 1, 0, 1, 1, 1]     # per face dof: one closed
+    out = PR.get_InflowBoundary_full2D(mat, H.build_factors(mat), 1.45, 1.4, np.full((11, 5), 1.424))
+    src = out["source"][0]
+    assert np.abs(src[:, 2]).max() == 0 and np.abs(src[:, [0, 1, 3, 4, 5]]).min(axis=0).max() >= 0
+    assert np.abs(out["drain"][0]).max() > 0
+    mat["dg"]["params"]["full2D_sourceContactMask"] = [1, 0, 1, 1]           # neither face dofs nor Ny
+    with pytest.raises(WignerError) as e:
+        H.build_factors(mat)
+    assert e.value.identifier == "DG:Full2D:InvalidContactMask"
 
 
 @pytest.mark.gpu
