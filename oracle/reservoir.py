@@ -4,8 +4,9 @@ infrastructure only).
 Restates in NumPy the reservoir data that the reference feeds into the Full-2D transport solve:
 
   contact_mode_reservoir    DG_code/core/get_ContactModeReservoirRho_full2D.m:1-151 on a periodic
-                            Y cell: the Fourier-Galerkin contact modes of
-                            get_PeriodicContactModes_full2D.m:1-70, the contact-neutrality Fermi
+                            Y cell (the Fourier-Galerkin contact modes of
+                            get_PeriodicContactModes_full2D.m:1-70) or on a box (the transverse
+                            contact problem of :153-302, :343-367), the contact-neutrality Fermi
                             level (:407-467, :483-621: bracket + bisection on the k_z-integrated
                             sheet density of the modes), the k_z window (:649-702), the
                             longitudinal occupation and its cosine transform (:304-329), the
@@ -163,13 +164,92 @@ def longitudinal_occupation(kx, e_mode, mx, mz, ef, temp, deg, kz):
     return 2 * deg * trapz(fermi, kz, axis=1) / np.pi
 
 
+def box_contact_modes(mat, p, side, Vxy):
+    """The non-periodic contact problem (get_ContactModeReservoirRho_full2D.m:153-302): the transverse
+    Hamiltonian on the sorted material Y grid of the contact column (interior three-point rows with
+    harmonic-mean masses; the first and last rows copy their neighbour's diagonal and outer coupling,
+    the mode vanishing one step beyond the grid), or with hard walls the interior unknowns only (the
+    mode vanishing at the walls); the nModes eigenpairs of smallest magnitude in ascending order,
+    normalised to a unit trapezoid integral over y, the last grid value made nonnegative.  Constant
+    masses.  Returns (energy, modes [nY x nModes] on the grid, grid, hard_wall)."""
+    prm = mat["dg"]["params"]
+    raw = np.asarray(mat["y"], dtype=float) * p["coordinateScale"]
+    order = np.argsort(raw, kind="stable")
+    grid = raw[order]
+    nx, ny = int(mat["Nx"]), int(mat["Ny"])
+    V = np.asarray(Vxy, dtype=float).reshape(nx, ny)[0 if side == "source" else nx - 1][order]
+    my = _constant_mass(mat, "y")
+    n = grid.size
+    if n < 3:
+        raise ValueError("DG:Full2D:ContactModeGridTooSmall")
+    dy = np.mean(np.diff(grid))
+    t0 = HBAR ** 2 / (2 * M0 * QE * dy ** 2)
+    H = np.zeros((n, n))
+    for i in range(1, n - 1):
+        left, right = -2 * t0 / (my + my), -2 * t0 / (my + my)
+        H[i, i - 1], H[i, i], H[i, i + 1] = left, -left - right + V[i], right
+    H[0, 0], H[0, 1] = H[1, 1], H[1, 2]
+    H[n - 1, n - 1], H[n - 1, n - 2] = H[n - 2, n - 2], H[n - 2, n - 3]
+    hard = p.get("ytype") == "hard-wall"
+    active = np.arange(n)
+    if hard:
+        tol = 64 * np.spacing(np.max(np.abs(grid)))
+        if max(abs(grid[0] - p["y"][0]), abs(grid[-1] - p["y"][-1])) > tol:
+            raise ValueError("DG:Full2D:HardWallContactDomainMismatch")
+        active = np.arange(1, n - 1)
+        H = H[np.ix_(active, active)]
+    ngrid = H.shape[0]
+    nm = int(mat["n_of_modes"]) if mat.get("n_of_modes") is not None else min(4, ngrid - 1)
+    nm = int(round(_param(prm, "full2D_contactModeCount", nm)))
+    nm = max(1, min(nm, ngrid))
+    w, vec = np.linalg.eig(H)
+    if nm < ngrid:                        # eigs(H, nModes, 'sm'): the smallest magnitudes
+        keep = np.argsort(np.abs(w), kind="stable")[:nm]
+        w, vec = w[keep], vec[:, keep]
+    ids = np.argsort(np.real(w), kind="stable")[:nm]
+    energy = np.real(w[ids])
+    modes = np.zeros((n, nm))
+    modes[active, :] = np.real(vec[:, ids])
+    wts = np.zeros(n)
+    wts[1:] += 0.5 * np.diff(grid)
+    wts[:-1] += 0.5 * np.diff(grid)
+    for im in range(nm):
+        norm = np.sqrt(np.sum(wts * modes[:, im] ** 2))
+        if norm > 0:
+            modes[:, im] /= norm
+        if modes[-1, im] < 0:
+            modes[:, im] = -modes[:, im]
+    return energy, modes, grid, hard
+
+
+def box_mode_density(mode, grid, hard, yface, rho_y):
+    """transverseModeDensity (:343-360): phi(Y + rho_y/2) phi(Y - rho_y/2) by linear interpolation,
+    zero outside; the box modes continue to zero ghost nodes one grid step beyond the edges."""
+    if hard:
+        g, v = grid, mode
+    else:
+        dy = np.mean(np.diff(grid))
+        g = np.concatenate([[grid[0] - dy], grid, [grid[-1] + dy]])
+        v = np.concatenate([[0.0], mode, [0.0]])
+    out = np.zeros((rho_y.size, yface.size))
+    for iy in range(yface.size):
+        plus = np.interp(yface[iy] + 0.5 * rho_y, g, v, left=0.0, right=0.0)
+        minus = np.interp(yface[iy] - 0.5 * rho_y, g, v, left=0.0, right=0.0)
+        out[:, iy] = plus * minus
+    return out
+
+
 def contact_mode_reservoir(mat, p, side, ef_input, Vxy):
-    """(rhoBoundary [nRel x nYnodes], info) for a periodic Y cell
-    (get_ContactModeReservoirRho_full2D.m:35-151 with the periodic branch)."""
+    """(rhoBoundary [nRel x nYnodes], info) (get_ContactModeReservoirRho_full2D.m:35-151): the periodic
+    branch on a periodic Y cell, the box contact problem otherwise."""
     prm = mat["dg"]["params"]
     temp = float(mat.get("Temp", 300))
     deg = float(np.ravel(mat.get("deg_factor", [1]))[0])
-    energy, coef, kw, gridY, width = periodic_contact_modes(mat, p, side, Vxy)
+    periodic = p.get("ytype", "periodic") == "periodic"
+    if periodic:
+        energy, coef, kw, gridY, width = periodic_contact_modes(mat, p, side, Vxy)
+    else:
+        energy, modes, gridY, hard = box_contact_modes(mat, p, side, Vxy)
     nm = energy.size
     mx = _constant_mass(mat, "x") * M0 * np.ones(nm)     # constant mass: the harmonic mode average
     mz = _constant_mass(mat, "z") * M0 * np.ones(nm)
@@ -192,9 +272,12 @@ def contact_mode_reservoir(mat, p, side, ef_input, Vxy):
     for im in range(nm):
         fkx = longitudinal_occupation(kx, energy[im], mx[im], mz[im], ef, temp, deg, kz)
         rx = cosX @ fkx * dkx / (2 * np.pi)
-        php = np.exp(1j * np.outer(ypl.ravel(order="F") - gridY[0], kw)) @ coef[:, im] / np.sqrt(width)
-        phm = np.exp(1j * np.outer(ymi.ravel(order="F") - gridY[0], kw)) @ coef[:, im] / np.sqrt(width)
-        ry = (php * np.conj(phm)).reshape(ypl.shape, order="F")
+        if periodic:
+            php = np.exp(1j * np.outer(ypl.ravel(order="F") - gridY[0], kw)) @ coef[:, im] / np.sqrt(width)
+            phm = np.exp(1j * np.outer(ymi.ravel(order="F") - gridY[0], kw)) @ coef[:, im] / np.sqrt(width)
+            ry = (php * np.conj(phm)).reshape(ypl.shape, order="F")
+        else:
+            ry = box_mode_density(modes[:, im], gridY, hard, yface, rho_y)
         for iy in range(yface.size):
             rho[:, iy] += np.outer(rx, ry[:, iy]).ravel(order="F")
     # the +/- k plane waves of one energy pair up into real cosines; the stored data are real

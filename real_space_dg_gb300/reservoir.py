@@ -13,9 +13,10 @@ its right-hand side:
       distribution of the contact edge, cosine-transformed)
   inflow_rhs(f, inflow)                               get_Diff_full2D.m:405-430, :609-615
 
-``f`` is ``full2d.build_factors(mat)``.  Contacts must span the whole X face (the device
-operator has no closed-face reflection parts); the non-periodic contact-mode box problem is
-not restated (periodic Y, or the material-default model, are).
+``f`` is ``full2d.build_factors(mat)``.  Contact modes: the Fourier-Galerkin modes of a periodic Y
+cell, or the box contact problem (get_ContactModeReservoirRho_full2D.m:153-302) for the other Y
+boundaries, with constant masses.  Contacts on part of an X face keep their data on the contact
+pieces only (the operator closes the rest).
 """
 import numpy as np
 
@@ -125,14 +126,84 @@ def _neutral_fermi(E, mx, mz, target, temp, deg, prm, guess):
     return 0.5 * (lo + hi)
 
 
-def contact_mode_reservoir(mat, f, side, Ef, Vxy):
-    """(rhoBoundary [N_rho_x N_rho_y x N_Y_nodes], info) (get_ContactModeReservoirRho_full2D.m)."""
+def _box_modes(mat, f, side, Vxy):
+    """The transverse contact problem of a non-periodic Y face (get_ContactModeReservoirRho_full2D.m:
+    153-302): H on the sorted material Y grid of the contact column, three-point interior rows with
+    the harmonic-mean mass, boundary rows repeating their neighbour's diagonal and outer coupling
+    (the mode vanishes one step beyond the grid), or with hard walls the interior unknowns alone (it
+    vanishes at the walls); the n modes of smallest |E| in ascending order, unit trapezoid norm over
+    y, last grid value nonnegative.  Returns (E, modes [nY x n], grid, hard)."""
+    for key in ("me_x", "me_y", "me_z"):
+        if mat.get(key) is not None and np.size(mat[key]) > 1:
+            raise WignerError(_lib.WG_ERR_ARG, "position-dependent contact masses (the variable-mass model) are "
+                              "not built", "DG:Full2D:ContactModeMass")
     prm = mat["dg"]["params"]
-    if f.get("ytype") != "periodic":
-        raise WignerError(_lib.WG_ERR_ARG, "contact-mode reservoirs are built for a periodic Y cell only")
+    raw = np.asarray(mat["y"], dtype=float) * f["scale"]
+    order = np.argsort(raw, kind="stable")
+    grid = raw[order]
+    n = grid.size
+    if n < 3:
+        raise WignerError(_lib.WG_ERR_ARG, "Contact-mode reservoir needs at least three Y grid points.",
+                          "DG:Full2D:ContactModeGridTooSmall")
+    v = _edge(mat, Vxy, side)[order]
+    my = _rel_mass(mat, "y")
+    t0 = HBAR ** 2 / (2 * M0 * QE * np.mean(np.diff(grid)) ** 2)
+    off = -2 * t0 / (2 * my)                       # -2 t0 / (m_i + m_j), constant mass
+    diag = np.empty(n)
+    diag[1:-1] = -2 * off + v[1:-1]
+    diag[0], diag[-1] = diag[1], diag[-2]
+    H = np.diag(diag) + np.diag(np.full(n - 1, off), 1) + np.diag(np.full(n - 1, off), -1)
+    hard = f.get("ytype") == "hard-wall"
+    lo, hi = 0, n
+    if hard:
+        if max(abs(grid[0] - f["y"][0]), abs(grid[-1] - f["y"][-1])) > 64 * np.spacing(np.abs(grid).max()):
+            raise WignerError(_lib.WG_ERR_ARG, "Hard-wall contact modes require the material and DG Y bounds to "
+                              "agree.", "DG:Full2D:HardWallContactDomainMismatch")
+        lo, hi = 1, n - 1
+    Hs = H[lo:hi, lo:hi]
+    ng = Hs.shape[0]
+    nm = int(mat["n_of_modes"]) if mat.get("n_of_modes") is not None else min(4, ng - 1)
+    nm = max(1, min(int(round(_p(prm, "full2D_contactModeCount", nm))), ng))
+    w, vec = np.linalg.eigh(Hs)                  # constant mass: H is symmetric
+    if nm < ng:
+        pick = np.sort(np.argsort(np.abs(w), kind="stable")[:nm])
+        w, vec = w[pick], vec[:, pick]
+    modes = np.zeros((n, nm))
+    modes[lo:hi] = vec[:, :nm]
+    wts = np.concatenate([[0.0], 0.5 * np.diff(grid)]) + np.concatenate([0.5 * np.diff(grid), [0.0]])
+    modes /= np.sqrt(wts @ modes ** 2)[None, :]
+    modes *= np.where(modes[-1] < 0, -1.0, 1.0)[None, :]
+    return w[:nm], modes, grid, hard
+
+
+def _box_density(modes, grid, hard, yn, rho_y):
+    """phi_n(Y + rho_y/2) phi_n(Y - rho_y/2) [rho_y, node, mode], linear between the grid values and
+    zero beyond (transverseModeDensity, :343-367)."""
+    if not hard:
+        d = np.mean(np.diff(grid))
+        grid = np.concatenate([[grid[0] - d], grid, [grid[-1] + d]])
+        modes = np.vstack([np.zeros((1, modes.shape[1])), modes, np.zeros((1, modes.shape[1]))])
+    yp = (yn[None, :] + 0.5 * rho_y[:, None]).ravel()
+    ym = (yn[None, :] - 0.5 * rho_y[:, None]).ravel()
+    out = np.empty((rho_y.size, yn.size, modes.shape[1]))
+    for m in range(modes.shape[1]):
+        a = np.interp(yp, grid, modes[:, m], left=0.0, right=0.0)
+        b = np.interp(ym, grid, modes[:, m], left=0.0, right=0.0)
+        out[:, :, m] = (a * b).reshape(rho_y.size, yn.size)
+    return out
+
+
+def contact_mode_reservoir(mat, f, side, Ef, Vxy):
+    """(rhoBoundary [N_rho_x N_rho_y x N_Y_nodes], info) (get_ContactModeReservoirRho_full2D.m): the
+    Fourier-Galerkin contact modes of a periodic Y cell, or the box contact problem."""
+    prm = mat["dg"]["params"]
     temp = float(mat.get("Temp", 300))
     deg = float(np.ravel(mat.get("deg_factor", [1]))[0])
-    E, coef, kw, gy, width = _periodic_modes(mat, f, side, Vxy)
+    periodic = f.get("ytype") == "periodic"
+    if periodic:
+        E, coef, kw, gy, width = _periodic_modes(mat, f, side, Vxy)
+    else:
+        E, modes, grid, hard = _box_modes(mat, f, side, Vxy)
     mx, mz = _rel_mass(mat, "x") * M0, _rel_mass(mat, "z") * M0
     RX, RY = f["rel"]
     kx, dkx = _k_grid(_p(prm, "full2D_contactMode_Nkx", _p(prm, "full2D_reservoir_Nkx", RX["n"])), RX["length"])
@@ -161,11 +232,14 @@ def contact_mode_reservoir(mat, f, side, Ef, Vxy):
         fk = 2 * deg / (1.0 + np.exp(arg))
     rx = (np.cos(np.outer(RX["cells"], kx)) @ fk.T) * dkx / (2 * np.pi)          # [rho_x, mode]
     yn = f["axes"][1]["nodes"]
-    yp = (yn[None, :] + 0.5 * RY["cells"][:, None]) - gy[0]                       # [rho_y, node]
-    ym = (yn[None, :] - 0.5 * RY["cells"][:, None]) - gy[0]
-    php = np.exp(1j * yp[..., None] * kw) @ coef / np.sqrt(width)                # [rho_y, node, mode]
-    phm = np.exp(1j * ym[..., None] * kw) @ coef / np.sqrt(width)
-    ry = php * np.conj(phm)
+    if periodic:
+        yp = (yn[None, :] + 0.5 * RY["cells"][:, None]) - gy[0]                   # [rho_y, node]
+        ym = (yn[None, :] - 0.5 * RY["cells"][:, None]) - gy[0]
+        php = np.exp(1j * yp[..., None] * kw) @ coef / np.sqrt(width)            # [rho_y, node, mode]
+        phm = np.exp(1j * ym[..., None] * kw) @ coef / np.sqrt(width)
+        ry = php * np.conj(phm)
+    else:
+        ry = _box_density(modes, grid, hard, yn, RY["cells"])
     rho = np.einsum("am,bnm->abn", rx, ry)                                         # [rho_x, rho_y, node]
     rho = rho.reshape(RX["n"] * RY["n"], yn.size, order="F")
     return rho.real if np.abs(rho.imag).max() <= 1e-12 * max(np.abs(rho.real).max(), 1e-300) else rho, \

@@ -166,3 +166,31 @@ def test_dropin_contact_masks_match_sparse_lu(built_lib):
     s = DG["info"]["solve"]
     assert DG["status"] == "solved-gmres" and s["flag"] == 0 and s["trueRelres"] <= TOL, s
     assert np.linalg.norm(DG["rho"] - want) <= 1e-8 * np.linalg.norm(want)
+
+
+@pytest.mark.gpu
+def test_dropin_box_contact_modes_match_sparse_lu(built_lib):
+    """Contact-mode reservoirs on a non-periodic Y face (the box contact problem) through the drop-in:
+    the reservoir right-hand side from the host's box modes, GMRES on the device, against the sparse
+    LU of the oracle's operator; the face data are those of the oracle's restatement."""
+    import scipy.sparse.linalg as spla
+    from oracle import reservoir as R
+    from real_space_dg_gb300.full2d import Full2DOperator, solve_transport_DG_full2D
+    mat = small_mat("contact-modes", "zero-inflow", nry=8)
+    XX, YY = np.meshgrid(mat["x"], mat["y"], indexing="ij")
+    mat["V"] = 1.424 + 0.15 * np.exp(-((XX - 10) / 3) ** 2) - 0.05 * XX / 20
+    mat["dg"]["params"].update(L_rho_y=6e-9, full2D_contactModeCount=3, full2D_solverTol=TOL,
+                               full2D_solverMaxIt=300, full2D_gmresRestart=20)
+    V = mat["V"]
+    p, parts, dd = F2.system(mat, V)
+    A = (F2.assemble_kron(parts, p["nCenterDof"], p["nRelative"]) + F2.assemble_drift(p, dd)).tocsc()
+    with Full2DOperator(mat, V) as op:
+        rhs, inflow = op.reservoir_rhs(1.45, 1.40)
+    for side, ef in (("source", 1.45), ("drain", 1.40)):
+        want_b, _ = R.contact_mode_reservoir(mat, p, side, ef, V)
+        assert np.abs(inflow[side][0] - want_b).max() <= 1e-12 * np.abs(want_b).max()
+    want = spla.spsolve(A, rhs)
+    DG = solve_transport_DG_full2D(mat, V, 1.45, 1.40)
+    s = DG["info"]["solve"]
+    assert DG["status"] == "solved-gmres" and s["flag"] == 0 and s["trueRelres"] <= TOL, s
+    assert np.linalg.norm(DG["rho"] - want) <= 1e-8 * np.linalg.norm(want)

@@ -96,10 +96,6 @@ def test_host_default_reservoir_matches_oracle():
 def test_host_reservoir_errors():
     from real_space_dg_gb300 import WignerError
     from real_space_dg_gb300 import full2d as H, reservoir as PR
-    mat = small_mat("contact-modes", "zero-inflow")
-    f = H.build_factors(mat)
-    with pytest.raises(WignerError):          # the box contact problem is not restated
-        PR.get_InflowBoundary_full2D(mat, f, 1.45, 1.4, np.full((11, 5), 1.424))
     mat = small_mat("contact-modes", "periodic")
     f = H.build_factors(mat)
     V = np.full((11, 5), 1.424)
@@ -194,3 +190,30 @@ def test_gpu_recorded_bias_point_reproduces_the_recorded_density_and_current(bui
     assert np.abs(n - g["density"]).max() <= 1e-3 * np.abs(g["density"]).max()
     assert np.abs(j - g["current"]).max() <= 3e-3 * np.abs(g["current"]).max()
     assert abs(np.mean(j) - np.mean(g["current"])) <= 3e-4 * abs(np.mean(g["current"]))
+
+
+@pytest.mark.parametrize("ybc", ["zero-inflow", "hard-wall", "specular"])
+def test_host_box_contact_modes_match_oracle(ybc):
+    """The non-periodic contact problem (get_ContactModeReservoirRho_full2D.m:153-367): the transverse
+    Hamiltonian of the contact column (ghost-node closure, or the hard-wall interior), the modes of
+    smallest |E|, their density matrix by linear interpolation, the contact-neutrality level; host
+    against the oracle's literal restatement, with a Y-dependent contact potential."""
+    from real_space_dg_gb300 import full2d as H, reservoir as PR
+    mat = small_mat("contact-modes", ybc, nry=8)
+    mat["dg"]["params"].update(L_rho_y=6e-9, full2D_contactModeCount=3)
+    V = np.full((11, 5), 1.424)
+    V[0] += 0.02 * np.sin(np.linspace(0, np.pi, 5))
+    V[-1] -= 0.01 * np.linspace(0, 1, 5)
+    f = H.build_factors(mat)
+    p = F2.init_params_full2d(mat)
+    for side, ef in (("source", 1.45), ("drain", 1.40)):
+        rho, info = PR.contact_mode_reservoir(mat, f, side, ef, V)
+        want, winfo = R.contact_mode_reservoir(mat, p, side, ef, V)
+        assert np.allclose(info["modeEnergy"], winfo["modeEnergy"], rtol=1e-13, atol=0)
+        assert abs(info["fermiLevelUsed"] - winfo["fermiLevelUsed"]) < 1e-12
+        assert np.abs(rho - want).max() <= 1e-12 * np.abs(want).max() and np.abs(want).max() > 0
+    # box modes vanish beyond the grid: no density where both particle coordinates leave the face
+    Eb, modes, grid, hard = PR._box_modes(mat, f, "source", V)
+    assert modes.shape == (5, 3) and np.all(np.diff(Eb) > 0)
+    if ybc == "hard-wall":
+        assert hard and np.all(modes[[0, -1]] == 0)
