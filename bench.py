@@ -225,7 +225,7 @@ def run_ours(args, rank, world, dist):
     opts = dict(GUMMEL, precision=args.precision, restart=args.restart, innerRestart=args.inner_restart,
                 innerTol=args.inner_tol, inexactFactor=args.inexact, inexactCap=args.inexact_cap, reorth=args.reorth,
                 innerReorth=args.inner_reorth, fp64TensorCores=args.fp64_tc,
-                innerBasisFP32=args.inner_basis_fp32)
+                innerBasisFP32=args.inner_basis_fp32, deferFinal=args.defer_final)
     if args.max_gummel:
         opts["maxIterations"] = args.max_gummel      # profiling runs only: points need not converge
     K = max(1, min(args.handles, args.batch))
@@ -361,7 +361,8 @@ def run_ours(args, rank, world, dist):
                    "batch_bias_points": args.batch, "biases_v": [round(float(b), 4) for b in biases],
                    "handles": K, "handles_run": "one after another" if args.serial_handles else "concurrently",
                    "launch_shapes": shapes,
-                   "defer_final": "64 Gummel iterations (inexact mode)",
+                   "defer_final": "none" if args.defer_final < 0 else
+                   "%d Gummel iterations (inexact mode)" % (args.defer_final or 64),
                    "profile": "rooflines from one extra step with per-launch CUDA events, handles run one after another",
                    "precision": args.precision, "gmres_restart": args.restart,
                    "inner_restart": args.inner_restart, "inner_tol": args.inner_tol,
@@ -1469,6 +1470,9 @@ def main():
                     help="DGKS re-orthogonalisation threshold of the FP64 Arnoldi (0: 1/sqrt(2), <0 never, >=1 always)")
     ap.add_argument("--inner-reorth", type=float, default=0.0,
                     help="the same for the mixed form's inner FP32 Arnoldi (0: never, one classical pass)")
+    ap.add_argument("--defer-final", type=int, default=0,
+                    help="Gummel iterations a loosely converged point may wait for the batched final re-solve "
+                         "(0: the library's 64; -1: none)")
     ap.add_argument("--inner-basis-fp32", action="store_true",
                     help="mixed form: keep the inner Krylov basis in FP32 (default: FP16 storage, FP32 arithmetic)")
     ap.add_argument("--fp64-tc", action="store_true",

@@ -13,9 +13,10 @@
 //  - gmres_solve_fp64:  FP64 basis and operator (the drop-in plain form);
 //  - gmres_solve_mixed: FP64 iterative refinement.  The outer residual
 //    r = b - A x is FP64; each correction solves A d = r/|r| with one GMRES cycle
-//    whose basis is FP32 and whose operator runs the BF16 tensor-core transforms
-//    and the FP32 flux / preconditioner.  Inner products and norms are combined
-//    in FP64 (see AccF32), Givens rotations and the Hessenberg solve are FP64.
+//    whose basis is stored in FP16 (FP32 with inner_basis_fp32), with FP32
+//    arithmetic, and whose operator runs the BF16 tensor-core transforms and the
+//    FP32 flux / preconditioner.  Inner products and norms are combined in FP64
+//    (see AccF32), Givens rotations and the Hessenberg solve are FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
