@@ -79,8 +79,10 @@ __device__ __forceinline__ double recip_ge1(double d) {
 // (j, kz) is 1 / (1 + a_j g(kz)) with a_j = exp((E_j - E_F) / kT) and
 // g(kz) = exp(hbar^2 kz^2 / (2 m_z kT)): the kz factors are computed once per block
 // in shared memory, the j factors once per j, instead of one exponential per (j, kz).
-constexpr int kFermiJ = 16;
-__global__ void __launch_bounds__(256) fermi_kernel(const double* __restrict__ pot_v, const double* __restrict__ pp,
+// Four j per block, one warp each: a small batch still spreads over the SMs (16 j per block left
+// 32 blocks for a 2-problem handle at Nk = 256).
+constexpr int kFermiJ = 4;
+__global__ void __launch_bounds__(32 * kFermiJ) fermi_kernel(const double* __restrict__ pot_v, const double* __restrict__ pp,
                                                     const double* __restrict__ kvec, double* __restrict__ flr,
                                                     int nx, int nk, int b0, const int* __restrict__ mask) {
   __shared__ double g[kNkz];
@@ -279,8 +281,8 @@ cudaError_t launch_potential_update(Problem& P, int b0, int b1, const int* mask)
   const Shape& s = P.s;
   cudaEvent_t ev = prof_begin(P, PROF_OTHER, 5);
   minmax_kernel<<<nb, 256, 0, P.stream>>>(P.pot_v, P.pot_x, P.vslope, P.pp, P.nx, b0, mask);
-  fermi_kernel<<<dim3((s.nk + kFermiJ - 1) / kFermiJ, nb), 256, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr, P.nx,
-                                                                              s.nk, b0, mask);
+  fermi_kernel<<<dim3((s.nk + kFermiJ - 1) / kFermiJ, nb), 32 * kFermiJ, 0, P.stream>>>(P.pot_v, P.pp, P.kvec, P.flr,
+                                                                                       P.nx, s.nk, b0, mask);
   inflow_xi_kernel<<<dim3((s.nxi + 7) / 8, nb), 256, 0, P.stream>>>(P.flr, P.cosm, P.kvec, P.fxi, s.nk, s.nxi, b0,
                                                                      mask);
   inflow_kernel<<<dim3((s.nk + 7) / 8, nb), 256, 0, P.stream>>>(P.fxi, P.pinv, P.kvec, P.pp, P.rhs, P.fb, s.nk,
