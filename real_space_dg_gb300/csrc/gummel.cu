@@ -28,8 +28,7 @@ namespace {
 constexpr double kQP = 1.602176634e-19;   // solve_Poisson2D_rtd.m:79
 constexpr double kKBP = 1.380649e-23;     // solve_Poisson2D_rtd.m:80
 constexpr double kEps0 = 8.8541878128e-12;  // eval_Poisson2D_rtd.m:28
-constexpr int kPcrMax = 2048;                // Poisson unknowns per problem
-constexpr int kPoissonThreads = 1024;        // one block per problem: two unknowns per thread at kPcrMax
+constexpr int kPcrMax = 2048;                // Poisson unknowns per problem (block of 256 threads)
 
 __device__ double bmax(double v) {
   __shared__ double sh[32];
@@ -120,8 +119,7 @@ __global__ void observables_batched_kernel(const double2* __restrict__ x, const 
 // newton = 1: approximate-Newton step of the Gummel loop; newton = 0: the linear
 // Poisson problem A v = q (n - N_D) of the transient (solve_Poisson2D_transient.m),
 // solved exactly by the same step with J = A.
-__global__ void __launch_bounds__(kPoissonThreads) poisson_kernel(const GummelDev G, const int* __restrict__ active,
-                                                                  int nx,
+__global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const int* __restrict__ active, int nx,
                                                       int ncol, int nK, double temp_default, double newton) {
   const int b = blockIdx.x;
   if (!active[b]) return;
@@ -186,12 +184,12 @@ __global__ void __launch_bounds__(kPoissonThreads) poisson_kernel(const GummelDe
       pd[q] = wd[i];
     }
     __syncthreads();
-    constexpr int R = kPcrMax / kPoissonThreads;
+    constexpr int R = kPcrMax / 256;
     for (int st = 1; st < n; st <<= 1) {
       double na[R], nb[R], nc[R], nd2[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const int q = threadIdx.x + r * kPoissonThreads;
+        const int q = threadIdx.x + r * 256;
         if (q >= n) continue;
         double a = pa[q], bb = pb[q], c = pc[q], d = pd[q];
         double an = 0.0, cn = 0.0;
@@ -215,7 +213,7 @@ __global__ void __launch_bounds__(kPoissonThreads) poisson_kernel(const GummelDe
       __syncthreads();
 #pragma unroll
       for (int r = 0; r < R; ++r) {
-        const int q = threadIdx.x + r * kPoissonThreads;
+        const int q = threadIdx.x + r * 256;
         if (q >= n) continue;
         pa[q] = na[r];
         pb[q] = nb[r];
@@ -312,8 +310,8 @@ cudaError_t gummel_poisson(Problem& P, const int* active_dev, bool linear) {
   if (attr != cudaSuccess) return attr;
   P.prof.launches[PROF_OTHER] += 1;
   const size_t smem = 4 * sizeof(double) * (size_t)std::max(1, P.nx - 2);
-  poisson_kernel<<<P.batch, kPoissonThreads, smem, P.stream>>>(P.gd, active_dev, P.nx, P.s.n_el * P.s.nK, P.s.nK,
-                                                               300.0, linear ? 0.0 : 1.0);
+  poisson_kernel<<<P.batch, 256, smem, P.stream>>>(P.gd, active_dev, P.nx, P.s.n_el * P.s.nK, P.s.nK, 300.0,
+                                                   linear ? 0.0 : 1.0);
   return cudaGetLastError();
 }
 
