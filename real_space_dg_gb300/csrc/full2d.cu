@@ -23,6 +23,7 @@
 //   f2d_project_kernel   y[r, id(e,l)] = pot/16 sum_q Cp[q][l] Rq[e][q][r] + capc cap[r] U[r, id(e,l)]
 //   f2d_dv_kernel        dV from V on the material grid (bilinear, X clamped, Y clamped or wrapped).
 // All arithmetic FP64 (the plain form).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -90,6 +91,9 @@ struct wg2d_problem {
   float2 *Uq32 = nullptr, *Rq32 = nullptr, *G32 = nullptr;
   int vm32 = 0;
   float2 *V32 = nullptr, *Z32 = nullptr, *w32 = nullptr;
+  __half2* Vh32 = nullptr;    // the inner basis stored in FP16 (V32 unused then)
+  float2* vj32 = nullptr;     // FP32 copy of the current FP16 basis vector (the preconditioner's input)
+  bool vbasis16 = false;      // the inner basis allocated in FP16
   // GMRES
   int vm = 0;                     // basis vectors allocated
   double2* Zb = nullptr;          // [m][n] preconditioned basis (flexible GMRES)
@@ -764,21 +768,54 @@ __global__ void __launch_bounds__(256) f2d_to32_scaled(const double2* __restrict
   if (t < n) y[t] = make_float2((float)(a * x[t].x), (float)(a * x[t].y));
 }
 
+// FP16 basis: the scaled vector rounded to FP16 is the basis vector; its FP32 value (exactly the
+// stored one) also goes to `copy`, the preconditioner's input, so z = M^-1 v for the stored v.
+__global__ void __launch_bounds__(256) f2d_to16_scaled(const double2* __restrict__ x, __half2* __restrict__ y,
+                                                       float2* __restrict__ copy, const double* __restrict__ nrm,
+                                                       long long n) {
+  __shared__ double sa;
+  if (threadIdx.x == 0) sa = nrm[0] > 0 ? 1.0 / nrm[0] : 0.0;
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  const __half2 v = __floats2half2_rn((float)(sa * x[t].x), (float)(sa * x[t].y));
+  y[t] = v;
+  copy[t] = __half22float2(v);
+}
+
+__global__ void __launch_bounds__(256) f2d_scale16(const float2* __restrict__ x, __half2* __restrict__ out,
+                                                   float2* __restrict__ copy, const double* __restrict__ nrm,
+                                                   long long n) {
+  __shared__ float sa;
+  if (threadIdx.x == 0) sa = nrm[0] > 0 ? (float)(1.0 / nrm[0]) : 0.f;
+  __syncthreads();
+  const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
+  if (t >= n) return;
+  const __half2 v = __floats2half2_rn(sa * x[t].x, sa * x[t].y);
+  out[t] = v;
+  copy[t] = __half22float2(v);
+}
+
 __global__ void __launch_bounds__(256) f2d_d2f(const double* __restrict__ x, float* __restrict__ y, long long n) {
   const long long t = (long long)blockIdx.x * 256 + threadIdx.x;
   if (t < n) y[t] = (float)x[t];
 }
 
-// FP32 inner products, summed per thread in FP32 and across threads and blocks in FP64
-__global__ void __launch_bounds__(256) f2d_dot_partial32(const float2* __restrict__ V, long long vstride,
+__device__ __forceinline__ float2 f2d_ld(const float2& v) { return v; }
+__device__ __forceinline__ float2 f2d_ld(const __half2& v) { return __half22float2(v); }
+
+// FP32 inner products, summed per thread in FP32 and across threads and blocks in FP64; the basis
+// vectors V in FP32 or FP16 storage
+template <typename VB>
+__global__ void __launch_bounds__(256) f2d_dot_partial32(const VB* __restrict__ V, long long vstride,
                                                          const float2* __restrict__ w, double* __restrict__ partial,
                                                          long long n) {
   __shared__ double sre[256], sim[256];
   const int i = blockIdx.y;
-  const float2* v = V + (long long)i * vstride;
+  const VB* v = V + (long long)i * vstride;
   float re = 0.f, im = 0.f;
   for (long long t = (long long)blockIdx.x * 256 + threadIdx.x; t < n; t += (long long)gridDim.x * 256) {
-    const float2 a = v[t], b = w[t];
+    const float2 a = f2d_ld(v[t]), b = w[t];
     re = fmaf(a.x, b.x, fmaf(a.y, b.y, re));
     im = fmaf(a.x, b.y, fmaf(-a.y, b.x, im));
   }
@@ -801,7 +838,8 @@ __global__ void __launch_bounds__(256) f2d_dot_partial32(const float2* __restric
 // w -= sum_i h_i V_i in FP32.  The coefficients are converted to FP32 once per block into shared memory:
 // converting them per element put every element x vector through the FP64 pipe (98% busy, DRAM at 35%).
 constexpr int kGsStage = 256;
-__global__ void __launch_bounds__(256) f2d_gs_update32(const float2* __restrict__ V, long long vstride,
+template <typename VB>
+__global__ void __launch_bounds__(256) f2d_gs_update32(const VB* __restrict__ V, long long vstride,
                                                        float2* __restrict__ w, const double2* __restrict__ h, int nv,
                                                        long long n) {
   __shared__ float2 hs[kGsStage];
@@ -811,7 +849,7 @@ __global__ void __launch_bounds__(256) f2d_gs_update32(const float2* __restrict_
   if (t >= n) return;
   float2 acc = w[t];
   for (int i = 0; i < nv; ++i) {
-    const float2 v = V[(long long)i * vstride + t];
+    const float2 v = f2d_ld(V[(long long)i * vstride + t]);
     const float2 c = i < kGsStage ? hs[i] : make_float2((float)h[i].x, (float)h[i].y);
     acc.x -= c.x * v.x - c.y * v.y;
     acc.y -= c.x * v.y + c.y * v.x;
@@ -1600,10 +1638,15 @@ static void vnorm(wg2d_problem* h, const double2* w) {
   f2d_sqrt_real<<<1, 1, 0, h->stream>>>(h->hp, h->nrm);
 }
 
-static void dots32(wg2d_problem* h, const float2* V, int nv, const float2* w, double2* out, int accumulate) {
-  f2d_dot_partial32<<<dim3(kDotBlocks, nv), 256, 0, h->stream>>>(V, h->n, w, h->partial, h->n);
+}  // extern "C"
+
+template <typename VB>
+static void dots32(wg2d_problem* h, const VB* V, int nv, const float2* w, double2* out, int accumulate) {
+  f2d_dot_partial32<VB><<<dim3(kDotBlocks, nv), 256, 0, h->stream>>>(V, h->n, w, h->partial, h->n);
   f2d_dot_reduce<<<nv, 256, 0, h->stream>>>(h->partial, out, kDotBlocks, accumulate);
 }
+
+extern "C" {
 
 static void vnorm32(wg2d_problem* h, const float2* w) {
   dots32(h, w, 1, w, h->hp, 0);
@@ -1742,13 +1785,14 @@ int wg2d_apply_repeat(wg2d_problem* h, int n, double* ms, double* parts_ms) {
 
 static void free32(wg2d_problem* h) {
   void* ptrs[] = {h->blocks32[0], h->blocks32[1], h->coef32[0], h->coef32[1], h->val32[0], h->val32[1], h->interp32,
-                  h->proj32, h->cap32, h->dV32, h->Uq32, h->Rq32, h->G32, h->V32, h->Z32, h->w32};
+                  h->proj32, h->cap32, h->dV32, h->Uq32, h->Rq32, h->G32, h->V32, h->Z32, h->w32, h->Vh32, h->vj32};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   h->blocks32[0] = h->blocks32[1] = h->coef32[0] = h->coef32[1] = nullptr;
   h->val32[0] = h->val32[1] = nullptr;
   h->interp32 = h->proj32 = h->cap32 = h->dV32 = nullptr;
-  h->Uq32 = h->Rq32 = h->G32 = h->V32 = h->Z32 = h->w32 = nullptr;
+  h->Uq32 = h->Rq32 = h->G32 = h->V32 = h->Z32 = h->w32 = h->vj32 = nullptr;
+  h->Vh32 = nullptr;
   h->vm32 = 0;
   h->d32_ready = false;
 }
@@ -1757,12 +1801,16 @@ static void free32(wg2d_problem* h) {
 static int ensure32(wg2d_problem* h) {
   if (h->d32_ready) return WG_OK;
   const int vm = h->vm32;
-  float2 *V = h->V32, *Z = h->Z32, *w = h->w32;
-  h->V32 = h->Z32 = h->w32 = nullptr;
+  float2 *V = h->V32, *Z = h->Z32, *w = h->w32, *vj = h->vj32;
+  __half2* Vh = h->Vh32;
+  h->V32 = h->Z32 = h->w32 = h->vj32 = nullptr;
+  h->Vh32 = nullptr;
   free32(h);
   h->V32 = V;
   h->Z32 = Z;
   h->w32 = w;
+  h->vj32 = vj;
+  h->Vh32 = Vh;
   h->vm32 = vm;
   auto conv = [&](float** dst, const double* src, long long count) -> int {
     F2_CK(dalloc(dst, count));
@@ -2043,33 +2091,53 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     rc = ensure32(h);
     if (rc) return rc;
     const int mi = m;
-    if (h->vm32 < mi + 1) {
-      cudaFree(h->V32);
-      cudaFree(h->Z32);
-      cudaFree(h->w32);
-      h->V32 = h->Z32 = h->w32 = nullptr;
+    // the inner basis in FP16 (default; FP32 arithmetic) or FP32 (inner_basis_fp32)
+    const bool b16 = opts->inner_basis_fp32 == 0;
+    if (h->vm32 < mi + 1 || h->vbasis16 != b16) {
+      for (void* p : {(void*)h->V32, (void*)h->Vh32, (void*)h->vj32, (void*)h->Z32, (void*)h->w32})
+        if (p) cudaFree(p);
+      h->V32 = h->Z32 = h->w32 = h->vj32 = nullptr;
+      h->Vh32 = nullptr;
       h->vm32 = 0;
-      F2_CK(dalloc(&h->V32, (size_t)(mi + 1) * n));
+      if (b16) {
+        F2_CK(dalloc(&h->Vh32, (size_t)(mi + 1) * n));
+        F2_CK(dalloc(&h->vj32, n));
+      } else {
+        F2_CK(dalloc(&h->V32, (size_t)(mi + 1) * n));
+      }
       F2_CK(dalloc(&h->Z32, (size_t)mi * n));
       F2_CK(dalloc(&h->w32, n));
       h->vm32 = mi + 1;
+      h->vbasis16 = b16;
     }
     const double inner_tol = opts->inner_tol > 0 ? opts->inner_tol : 1e-3;
     while (info->cycles < maxit && beta > target && std::isfinite(beta)) {
-      f2d_to32_scaled<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->V32, h->nrm, n);
+      if (b16) f2d_to16_scaled<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->Vh32, h->vj32, h->nrm, n);
+      else f2d_to32_scaled<<<blocks256(n), 256, 0, h->stream>>>(h->r, h->V32, h->nrm, n);
       const double2 one = make_double2(1.0, 0.0);
       F2_CK(cudaMemsetAsync(h->g, 0, sizeof(double2) * (m + 1), h->stream));
       F2_CK(cudaMemcpyAsync(h->g, &one, sizeof(double2), cudaMemcpyHostToDevice, h->stream));
       const double itgt = std::max(inner_tol, 0.5 * target / beta);
-      int k = 0;
+      int k = 0, j_cur = 0;
+      // the basis as the Gram-Schmidt kernels read it
+      auto gs_dots = [&](double2* out) {
+        if (b16) dots32(h, h->Vh32, j_cur + 1, h->w32, out, 0);
+        else dots32(h, h->V32, j_cur + 1, h->w32, out, 0);
+      };
+      auto gs_update = [&](const double2* coef) {
+        if (b16) f2d_gs_update32<<<blocks256(n), 256, 0, h->stream>>>(h->Vh32, n, h->w32, coef, j_cur + 1, n);
+        else f2d_gs_update32<<<blocks256(n), 256, 0, h->stream>>>(h->V32, n, h->w32, coef, j_cur + 1, n);
+      };
       for (int j = 0; j < mi; ++j) {
-        const float2* Vj = h->V32 + (long long)j * n;
+        j_cur = j;
+        // the preconditioner works on the basis vector as stored (its FP32 copy with an FP16 basis)
+        const float2* Vj = b16 ? h->vj32 : h->V32 + (long long)j * n;
         float2* Zj = h->Z32 + (long long)j * n;
         precond_stages<float2>(h, h->UH32, h->Us32, h->xinv32, h->xcpl32, h->tinv32, Vj, h->pa32, h->pb32, Zj);
         rc = apply32(h, Zj, h->w32);
         if (rc) return rc;
-        dots32(h, h->V32, j + 1, h->w32, h->hc, 0);
-        f2d_gs_update32<<<blocks256(n), 256, 0, h->stream>>>(h->V32, n, h->w32, h->hc, j + 1, n);
+        gs_dots(h->hc);
+        gs_update(h->hc);
         vnorm32(h, h->w32);
         std::vector<double2> hh(j + 1);
         double w1 = 0;
@@ -2079,13 +2147,17 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
         double h2 = 0;
         for (const double2& c : hh) h2 += c.x * c.x + c.y * c.y;
         if (w1 * w1 < 0.5 * (w1 * w1 + h2)) {
-          dots32(h, h->V32, j + 1, h->w32, h->hp, 0);
+          gs_dots(h->hp);
           f2d_dot_reduce<<<j + 1, 256, 0, h->stream>>>(h->partial, h->hc, kDotBlocks, 1);
-          f2d_gs_update32<<<blocks256(n), 256, 0, h->stream>>>(h->V32, n, h->w32, h->hp, j + 1, n);
+          gs_update(h->hp);
           vnorm32(h, h->w32);
         }
         f2d_givens<<<1, 1, 0, h->stream>>>(h->H, h->hc, h->nrm, h->cs, h->sn, h->g, j, ldh);
-        f2d_scale32<<<blocks256(n), 256, 0, h->stream>>>(h->w32, h->V32 + (long long)(j + 1) * n, h->nrm, n);
+        if (b16)
+          f2d_scale16<<<blocks256(n), 256, 0, h->stream>>>(h->w32, h->Vh32 + (long long)(j + 1) * n, h->vj32,
+                                                           h->nrm, n);
+        else
+          f2d_scale32<<<blocks256(n), 256, 0, h->stream>>>(h->w32, h->V32 + (long long)(j + 1) * n, h->nrm, n);
         double2 gj;
         F2_CK(cudaMemcpyAsync(&gj, h->g + j + 1, sizeof(double2), cudaMemcpyDeviceToHost, h->stream));
         F2_CK(cudaStreamSynchronize(h->stream));
