@@ -1216,8 +1216,7 @@ def run_full2d_solve(args):
         clocks = ClockSampler()
         clocks.start()
         t0 = time.perf_counter()
-        st, info, _ = op.solve(rhs, tol=1e-12, maxit=args.solve_maxit, restart=40, mixed=True,
-                               inner_basis_fp32=args.inner_basis_fp32)
+        st, info, _ = op.solve(rhs, tol=1e-12, maxit=args.solve_maxit, restart=40, mixed=True)
         wall = time.perf_counter() - t0
         clk = clocks.stop()
     its = info["iterations"]
@@ -1364,7 +1363,7 @@ def run_full2d_sc(args):
     clocks = ClockSampler()
     clocks.start()
     t0 = time.perf_counter()
-    res = solve2D_rtd_self_consistent("DG", mat, {"mixing": 0.3, "innerBasisFP32": args.inner_basis_fp32},
+    res = solve2D_rtd_self_consistent("DG", mat, {"mixing": 0.3},
                                       callback=lambda ib, it, h: hist.append(h) if ib == 0 else None)
     wall = time.perf_counter() - t0
     clk = clocks.stop()

@@ -550,8 +550,9 @@ typedef struct {
   int mixed;                /* 1: FP64 refinement around FP32 flexible GMRES on the FP32 operator
                                (needs the FP32 preconditioner); 0: FP64 flexible GMRES */
   double inner_tol;         /* mixed: floor of each refinement's relative inner tolerance (default 1e-3) */
-  int inner_basis_fp32;     /* mixed: 1 keeps the inner basis in FP32; 0 (default) stores it in FP16 with FP32
-                               arithmetic (the preconditioner works on the stored vector) */
+  int inner_basis_fp16;     /* mixed: 1 stores the inner basis in FP16 with FP32 arithmetic (the preconditioner
+                               works on the stored vector); 0 (default) keeps it in FP32.  At the recorded run's
+                               shape and 5e-6 target FP16 needed 9% more inner iterations for a 1% faster one */
 } wg2d_solve_opts;
 typedef struct {
   int flag;                 /* 0 converged, 1 not */

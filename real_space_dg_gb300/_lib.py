@@ -131,7 +131,7 @@ class Wg2dShape(C.Structure):
 
 class Wg2dSolveOpts(C.Structure):
     _fields_ = [("tol", C.c_double), ("maxit", C.c_int), ("restart", C.c_int), ("use_x0", C.c_int),
-                ("mixed", C.c_int), ("inner_tol", C.c_double), ("inner_basis_fp32", C.c_int)]
+                ("mixed", C.c_int), ("inner_tol", C.c_double), ("inner_basis_fp16", C.c_int)]
 
 
 class Wg2dObservablesDesc(C.Structure):

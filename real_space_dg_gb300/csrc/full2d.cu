@@ -2091,8 +2091,8 @@ int wg2d_solve(wg2d_problem* h, const double* rhs, double* x, const wg2d_solve_o
     rc = ensure32(h);
     if (rc) return rc;
     const int mi = m;
-    // the inner basis in FP16 (default; FP32 arithmetic) or FP32 (inner_basis_fp32)
-    const bool b16 = opts->inner_basis_fp32 == 0;
+    // the inner basis in FP32 (default) or FP16 storage with FP32 arithmetic (inner_basis_fp16)
+    const bool b16 = opts->inner_basis_fp16 != 0;
     if (h->vm32 < mi + 1 || h->vbasis16 != b16) {
       for (void* p : {(void*)h->V32, (void*)h->Vh32, (void*)h->vj32, (void*)h->Z32, (void*)h->w32})
         if (p) cudaFree(p);

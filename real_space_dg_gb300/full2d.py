@@ -879,10 +879,10 @@ class Full2DOperator:
         return out
 
     def solve(self, rhs, x0=None, tol=1e-8, maxit=50, restart=40, mixed=False, inner_tol=1e-3, resident=False,
-              warm=False, inner_basis_fp32=False):
+              warm=False, inner_basis_fp16=False):
         """rho = A \\ rhs by right-preconditioned flexible GMRES(restart) on the device; mixed: FP64
-        refinement around FP32 inner solves (FP32 preconditioner required; the inner basis stored in FP16
-        unless inner_basis_fp32).  Returns (status, info, rho).
+        refinement around FP32 inner solves (FP32 preconditioner required; the inner basis in FP32, or
+        stored in FP16 with inner_basis_fp16).  Returns (status, info, rho).
         resident: the solution stays on the device only (rho is None; observables() and state() read it),
         warm: the warm start is the resident solution of the previous solve (x0 ignored), rhs = None:
         the right-hand side of the previous solve."""
@@ -901,7 +901,7 @@ class Full2DOperator:
                 x[:] = x0
         use_x0 = 1 if (warm or x0 is not None) else 0
         opts = _lib.Wg2dSolveOpts(float(tol), int(maxit), int(restart), use_x0, 1 if mixed else 0, float(inner_tol),
-                                  1 if inner_basis_fp32 else 0)
+                                  1 if inner_basis_fp16 else 0)
         info = _lib.Wg2dSolveInfo()
         st = self.lib.wg2d_solve(self.h, None if b is None else b.view(np.float64).ctypes.data_as(_lib._D),
                                  None if x is None else x.view(np.float64).ctypes.data_as(_lib._D),

@@ -35,7 +35,7 @@ from .poisson2d import make_RTD_poisson_step
 DEFAULTS = dict(maxIterations=100, mixing=0.1, potentialTolerance=5e-4, densityTolerance=5e-4,
                 poissonResidualTolerance=8e-2, chargeNeutralityTolerance=1e-3, poissonMethod="",
                 poissonXBoundary="", initialPhi=None, initialRho=None, mixed=True, innerRestart=None,
-                innerBasisFP32=False)
+                innerBasisFP16=False)
 
 
 def _options(options):
@@ -208,7 +208,7 @@ def solve2D_rtd_self_consistent(solver, mat, options=None, callback=None):
                 m_in = int(o["innerRestart"] or restart) if mixed else restart
                 st, info, _ = op.solve(rhs, x0=None if resident else rho, warm=resident, resident=True, tol=tol,
                                        maxit=maxit if not mixed else maxit * max(1, restart * 4 // m_in),
-                                       restart=m_in, mixed=mixed, inner_basis_fp32=bool(o["innerBasisFP32"]))
+                                       restart=m_in, mixed=mixed, inner_basis_fp16=bool(o["innerBasisFP16"]))
                 resident = True
                 t3 = clock()
                 timing["potential_s"] += t1 - t0

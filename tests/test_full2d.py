@@ -207,12 +207,12 @@ def test_gpu_preconditioner_matches_oracle(built_lib, cfg, tensor_cores, fp32, t
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("fp32,mixed,basis32", [(True, False, False), (False, False, False), (True, True, False),
+@pytest.mark.parametrize("fp32,mixed,basis16", [(True, False, False), (False, False, False), (True, True, False),
                                                  (True, True, True)])
 @pytest.mark.parametrize("cfg", CONFIGS)
-def test_gpu_solve_matches_direct_solve(built_lib, cfg, fp32, mixed, basis32):
+def test_gpu_solve_matches_direct_solve(built_lib, cfg, fp32, mixed, basis16):
     """Flexible GMRES(20) on the device, preconditioned in FP32 or FP64, and the mixed form (FP64
-    refinement around FP32 inner solves, inner basis in FP16 or FP32), against the oracle's sparse LU
+    refinement around FP32 inner solves, inner basis in FP32 or FP16), against the oracle's sparse LU
     (the same FP64 accuracy every way); a warm start from the solution needs no iteration."""
     import scipy.sparse.linalg as spla
     from real_space_dg_gb300.full2d import Full2DOperator
@@ -223,7 +223,7 @@ def test_gpu_solve_matches_direct_solve(built_lib, cfg, fp32, mixed, basis32):
     ref = spla.spsolve(A, b)
     with Full2DOperator(mat, V) as op:
         op.set_preconditioner(fp32=fp32)
-        st, info, x = op.solve(b, tol=1e-11, maxit=200, restart=20, mixed=mixed, inner_basis_fp32=basis32)
+        st, info, x = op.solve(b, tol=1e-11, maxit=200, restart=20, mixed=mixed, inner_basis_fp16=basis16)
         assert st == 0 and info["flag"] == 0, info
         assert info["relres"] <= 1e-11 and info["iterations"] > 0
         assert rel(x, ref) < 1e-8
