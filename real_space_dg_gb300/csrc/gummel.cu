@@ -169,17 +169,22 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
   // 3. J delta = -F over the free nodes 1..nx-2 by parallel cyclic reduction in shared
   //    memory (kPcrMax unknowns at most; J is diagonally dominant, so PCR is stable)
   {
-    extern __shared__ double pcr[];   // a, b, c, d: 4 x n
+    // a, b, c, d and 1/b: 5 x n.  Each row's owner keeps the reciprocal of its diagonal, so a
+    // reduction step divides once per row instead of once per (row, neighbour) pair (FP64
+    // divisions on one SM are this kernel's cost)
+    extern __shared__ double pcr[];
     const int n = nx - 2;
     double* pa = pcr;
     double* pb = pa + n;
     double* pc = pb + n;
     double* pd = pc + n;
+    double* pi = pd + n;
     const double g = newton * kQP * kQP / (kKBP * temp);
     for (int q = threadIdx.x; q < n; q += blockDim.x) {
       const int i = q + 1;
       pa[q] = q > 0 ? lo[i] : 0.0;
       pb[q] = di[i] - g * ncv[i];
+      pi[q] = 1.0 / pb[q];
       pc[q] = q < n - 1 ? up[i] : 0.0;
       pd[q] = wd[i];
     }
@@ -194,13 +199,13 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
         double a = pa[q], bb = pb[q], c = pc[q], d = pd[q];
         double an = 0.0, cn = 0.0;
         if (q - st >= 0) {
-          const double k1 = a / pb[q - st];
+          const double k1 = a * pi[q - st];
           an = -pa[q - st] * k1;
           bb -= pc[q - st] * k1;
           d -= pd[q - st] * k1;
         }
         if (q + st < n) {
-          const double k2 = c / pb[q + st];
+          const double k2 = c * pi[q + st];
           cn = -pc[q + st] * k2;
           bb -= pa[q + st] * k2;
           d -= pd[q + st] * k2;
@@ -217,6 +222,7 @@ __global__ void __launch_bounds__(256) poisson_kernel(const GummelDev G, const i
         if (q >= n) continue;
         pa[q] = na[r];
         pb[q] = nb[r];
+        pi[q] = 1.0 / nb[r];
         pc[q] = nc[r];
         pd[q] = nd2[r];
       }
@@ -306,10 +312,10 @@ cudaError_t gummel_observables(Problem& P) {
 
 cudaError_t gummel_poisson(Problem& P, const int* active_dev, bool linear) {
   static const cudaError_t attr = cudaFuncSetAttribute(poisson_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                       (int)(4 * sizeof(double) * kPcrMax));
+                                                       (int)(5 * sizeof(double) * kPcrMax));
   if (attr != cudaSuccess) return attr;
   P.prof.launches[PROF_OTHER] += 1;
-  const size_t smem = 4 * sizeof(double) * (size_t)std::max(1, P.nx - 2);
+  const size_t smem = 5 * sizeof(double) * (size_t)std::max(1, P.nx - 2);
   poisson_kernel<<<P.batch, 256, smem, P.stream>>>(P.gd, active_dev, P.nx, P.s.n_el * P.s.nK, P.s.nK, 300.0,
                                                    linear ? 0.0 : 1.0);
   return cudaGetLastError();

@@ -118,7 +118,7 @@ cudaError_t launch_ozaki(const CUtensorMap& a, const CUtensorMap& b, const int* 
   if (attr != cudaSuccess) return attr;
   if (nd < 1 || nd > oz::S) return cudaErrorInvalidValue;
   dim3 grid((M + oz::BM - 1) / oz::BM, (unsigned)((Ncol + oz::BN - 1) / oz::BN));
-  oz::gemm_ozaki_kernel<EPI><<<grid, 128, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err, mask,
+  oz::gemm_ozaki_kernel<EPI><<<grid, oz::THREADS, oz::SMEM_BYTES, st>>>(a, b, ea, eb, C, M, Ncol, K, err, mask,
                                                                  cols_per_problem, nd, nd_pp);
   return cudaGetLastError();
 }
@@ -890,7 +890,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   cudaEvent_t ev = prof_begin(P, PROF_GEMM_F64TC, 2, 8.0 * P.N * P.batch + 16.0 * s.nxi * ncols, prod_flops, mask,
                               nd, nd_pp);
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
-      reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp);
+      reinterpret_cast<const double*>(x), K1, P.ncols, M.ob, M.eb, mask, cpp, 0, nd, nd_pp);
   e = launch_ozaki<0>(M.tmOA1, M.tmOB1, M.ea1, M.eb, reinterpret_cast<double*>(P.xh), K2, P.ncols, K1, M.err,
                       P.stream, mask, cpp, nd, nd_pp);
   prof_end(P, PROF_GEMM_F64TC, ev);
@@ -899,7 +899,7 @@ cudaError_t launch_apply_f64_tc(Problem& P, const double2* x, double2* y, const 
   if (e != cudaSuccess) return e;
   ev = prof_begin(P, PROF_GEMM_F64TC, 2, 16.0 * s.nxi * ncols + 16.0 * P.N * P.batch, prod_flops, mask, nd, nd_pp);
   oz::slice_columns_kernel<<<slice_blocks(P.ncols), 32 * oz::kSliceColsPerBlock, 0, P.stream>>>(
-      reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp);
+      reinterpret_cast<const double*>(P.yh), K2, P.ncols, M.ob, M.eb, mask, cpp, 0, nd, nd_pp);
   e = launch_ozaki<1>(M.tmOA2, M.tmOB2, M.ea2, M.eb, reinterpret_cast<double*>(y), K1, P.ncols, K2, M.err, P.stream,
                       mask, cpp, nd, nd_pp);
   prof_end(P, PROF_GEMM_F64TC, ev);

@@ -270,7 +270,8 @@ __global__ void __launch_bounds__(kFluxThreads) stencil_kernel(const double2* __
       vr.x = fma(r0, sm[c].x, fma(r1, sp[c].x, vr.x));
       vr.y = fma(r0, sm[c].y, fma(r1, sp[c].y, vr.y));
       const double i0 = betai[ac * ne + s], i1 = betai[ac * ne + s + 1];
-      if (i0 != 0.0 || i1 != 0.0) {
+      // i0 != 0 || i1 != 0 tested on the bit patterns: an FP64 compare would take the FP64 pipe
+      if ((((unsigned long long)__double_as_longlong(i0) | (unsigned long long)__double_as_longlong(i1)) << 1) != 0) {
         vi.x = fma(i0, sm[c].x, fma(i1, sp[c].x, vi.x));
         vi.y = fma(i0, sm[c].y, fma(i1, sp[c].y, vi.y));
       }

@@ -25,14 +25,20 @@ namespace oz {
 
 constexpr int S = 8;              // digits per operand
 constexpr int BETA = 6;           // bits per digit
-// k blocks of 32 (64-byte rows, 64-byte swizzle) so that two stages of all 8 slices fit:
-// the TMA loads of block kb+1 overlap the 72 MMAs of block kb
-constexpr int BM = 128, BN = 64, BK = 32, STAGES = 2;
+// k blocks of 32 (64-byte rows, 64-byte swizzle).  A stage holds the nd A and nd B slices
+// the launch uses, so the 192 KiB ring has two stages at 7 or 8 digits and more with fewer
+// digits (three at 5, four at 4): the TMA loads run further ahead of the MMAs
+constexpr int BM = 128, BN = 64, BK = 32, STAGES = 2, MAX_STAGES = 8;
+constexpr int THREADS = 256;      // warp 0 TMA, warp 1 MMA, all 8 drain TMEM (two warps per lane quarter)
 constexpr int NGROUP = S;         // weights p+q = 2 .. S+1
 constexpr int A_SLICE = BM * BK * 2;      // 8 KiB
 constexpr int B_SLICE = BN * BK * 2;      // 4 KiB
-constexpr int STAGE = S * (A_SLICE + B_SLICE);   // 96 KiB
-constexpr int SMEM_BYTES = STAGES * STAGE + 1024 + 256;
+constexpr int STAGE = S * (A_SLICE + B_SLICE);   // 96 KiB (all 8 digits)
+constexpr int RING = STAGES * STAGE;              // 192 KiB
+constexpr int SMEM_BYTES = RING + 1024 + 256;
+__host__ __device__ constexpr int stages_for(int nd) {
+  return RING / (nd * (A_SLICE + B_SLICE)) < MAX_STAGES ? RING / (nd * (A_SLICE + B_SLICE)) : MAX_STAGES;
+}
 constexpr int MAX_K = 1024;       // exactness bound of the grouped accumulation (8 * 33^2 * K < 2^24)
 
 // Instruction descriptor: D f32, A/B bf16, K-major, M = 128, N = n (16 <= n <= 256, n % 16 == 0).
@@ -99,7 +105,7 @@ __device__ __forceinline__ double fixed_to_double(long long a, int e) {
 
 // EPI 0: C = A B.  EPI 1: C += A B.   ea[row], eb[col]: power-of-two exponents of A's rows and B's columns.
 template <int EPI>
-__global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ void __launch_bounds__(THREADS, 1) gemm_ozaki_kernel(const __grid_constant__ CUtensorMap tmA,
                                                             const __grid_constant__ CUtensorMap tmB,
                                                             const int* __restrict__ ea, const int* __restrict__ eb,
                                                             double* __restrict__ C, int M, long long Ncol, int K,
@@ -123,10 +129,12 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
   }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  // stage s: [S][BM][BK] bf16 A slices, then [S][BN][BK] bf16 B slices
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE);
-  uint64_t* empty = full + STAGES;
-  uint64_t* done = empty + STAGES;
+  // stage s: [nd][BM][BK] bf16 A slices, then [nd][BN][BK] bf16 B slices
+  const int ns = stages_for(nd);
+  const int stage = nd * (A_SLICE + B_SLICE);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + RING);
+  uint64_t* empty = full + MAX_STAGES;
+  uint64_t* done = empty + MAX_STAGES;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * BM;
@@ -134,7 +142,7 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
   const int nkb = (K + BK - 1) / BK;
 
   if (threadIdx.x == 0) {
-    for (int st = 0; st < STAGES; ++st) {
+    for (int st = 0; st < ns; ++st) {
       tc::mbar_init(&full[st], 1);
       tc::mbar_init(&empty[st], 1);
     }
@@ -149,10 +157,10 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
 
   if (warp == 0 && lane == 0) {
     for (int kb = 0; kb < nkb; ++kb) {
-      const int st = kb % STAGES;
-      if (kb >= STAGES && !tc::mbar_wait(&empty[st], ((kb / STAGES) + 1) & 1, err)) break;
-      uint8_t* sa = smem + st * STAGE;
-      uint8_t* sb = sa + S * A_SLICE;
+      const int st = kb % ns;
+      if (kb >= ns && !tc::mbar_wait(&empty[st], ((kb / ns) + 1) & 1, err)) break;
+      uint8_t* sa = smem + st * stage;
+      uint8_t* sb = sa + nd * A_SLICE;
       tc::mbar_expect_tx(&full[st], (uint32_t)(nd * (A_SLICE + B_SLICE)));
       for (int p = 0; p < nd; ++p) {
         tma_load_3d(sa + p * A_SLICE, &tmA, kb * BK, m0, p, &full[st]);
@@ -161,11 +169,11 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
     }
   } else if (warp == 1 && lane == 0) {
     for (int kb = 0; kb < nkb; ++kb) {
-      const int st = kb % STAGES;
-      if (!tc::mbar_wait(&full[st], (kb / STAGES) & 1, err)) break;
+      const int st = kb % ns;
+      if (!tc::mbar_wait(&full[st], (kb / ns) & 1, err)) break;
       tc::fence_after();
-      const uint8_t* sa = smem + st * STAGE;
-      const uint8_t* sb = sa + S * A_SLICE;
+      const uint8_t* sa = smem + st * stage;
+      const uint8_t* sb = sa + nd * A_SLICE;
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk)
         for (int p = 0; p < nd; ++p)
@@ -188,17 +196,19 @@ __global__ void __launch_bounds__(128, 1) gemm_ozaki_kernel(const __grid_constan
   const bool ok = tc::mbar_wait(done, 0, err);
   tc::fence_after();
   if (ok && !*(volatile int*)err) {
-    const int row = m0 + warp * 32 + lane;
+    // warp w reads TMEM lanes 32 (w % 4) .. +31 (rows) and the 32-column block w / 4
+    const int wq = warp & 3;
+    const int row = m0 + wq * 32 + lane;
     const int er = row < M ? ea[row] : 0;
 #pragma unroll 1
-    for (int cb = 0; cb < BN / 32; ++cb) {
+    for (int cb = warp >> 2; cb < BN / 32; cb += THREADS / 128) {
       long long fx[32];
 #pragma unroll
       for (int i = 0; i < 32; ++i) fx[i] = 0;
 #pragma unroll 1
       for (int g = 0; g < nd; ++g) {
         float v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(g * BN + cb * 32), v);
+        tc::tmem_ld32(tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(g * BN + cb * 32), v);
 #pragma unroll
         for (int i = 0; i < 32; ++i) fx[i] += group_fixed(v[i], g);
       }
@@ -254,11 +264,21 @@ __global__ void __launch_bounds__(32 * kSliceColsPerBlock) slice_columns_kernel(
                                                                                int* __restrict__ e_out,
                                                                                const int* __restrict__ mask = nullptr,
                                                                                int cols_per_problem = 1,
-                                                                               int Kout = 0) {
-  // Kout: row length of the slices (>= K, zero-padded; 0: K), for 16-byte TMA rows
+                                                                               int Kout = 0, int nd = S,
+                                                                               const int* __restrict__ nd_pp = nullptr) {
+  // Kout: row length of the slices (>= K, zero-padded; 0: K), for 16-byte TMA rows.
+  // nd, nd_pp: the digits gemm_ozaki_kernel reads for the column's 64-column tile (the same
+  // rule: nd_pp's largest over the tile's active problems, else nd); only those are written
   const int lane = threadIdx.x & 31;
   const long long c = (long long)blockIdx.x * kSliceColsPerBlock + (threadIdx.x >> 5);
   if (c >= Ncol || (mask && !mask[c / cols_per_problem])) return;
+  int ndt = nd < 1 ? 1 : (nd > S ? S : nd);
+  if (nd_pp) {
+    const long long c0 = c / BN * BN, c1 = min(Ncol, c0 + BN) - 1;
+    ndt = 1;
+    for (long long b = c0 / cols_per_problem; b <= c1 / cols_per_problem; ++b)
+      if (!mask || mask[b] != 0) ndt = max(ndt, min(S, max(1, nd_pp[b])));
+  }
   const int Ko = Kout > K ? Kout : K;
   const double2* x = reinterpret_cast<const double2*>(X + c * (long long)K);
   const int K2 = K / 2;
@@ -289,7 +309,7 @@ __global__ void __launch_bounds__(32 * kSliceColsPerBlock) slice_columns_kernel(
 #pragma unroll
     for (int p = S - 1; p > 0; --p) {
       const int d0 = (int)(((F0 + 32) & 63) - 32), d1 = (int)(((F1 + 32) & 63) - 32);
-      out[p * (slice_stride / 2) + k] = __floats2bfloat162_rn((float)d0, (float)d1);
+      if (p < ndt) out[p * (slice_stride / 2) + k] = __floats2bfloat162_rn((float)d0, (float)d1);
       F0 = (F0 - d0) >> BETA;
       F1 = (F1 - d1) >> BETA;
     }
