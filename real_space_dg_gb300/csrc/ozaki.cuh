@@ -29,7 +29,9 @@ constexpr int BETA = 6;           // bits per digit
 // the launch uses, so the 192 KiB ring has two stages at 7 or 8 digits and more with fewer
 // digits (three at 5, four at 4): the TMA loads run further ahead of the MMAs
 constexpr int BM = 128, BN = 64, BK = 32, STAGES = 2, MAX_STAGES = 8;
-constexpr int THREADS = 256;      // warp 0 TMA, warp 1 MMA, all 8 drain TMEM (two warps per lane quarter)
+constexpr int THREADS = 512;      // warp 0 TMA, warp 1 MMA, all 16 drain TMEM (four warps per lane quarter)
+constexpr int EPI_COLS = BN / (THREADS / 128);   // 16 output columns per epilogue warp
+static_assert(EPI_COLS == 16, "the epilogue drains 16 TMEM columns per warp");
 constexpr int NGROUP = S;         // weights p+q = 2 .. S+1
 constexpr int A_SLICE = BM * BK * 2;      // 8 KiB
 constexpr int B_SLICE = BN * BK * 2;      // 4 KiB
@@ -65,6 +67,20 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
           "r"(tc::smem_u32(dst)),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(tc::smem_u32(bar))
       : "memory");
+}
+
+// 32 lanes x 16 consecutive fp32 columns of TMEM into 16 registers per thread.
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 // Fixed-point unit of the epilogue: 2^-50.  Group g (weight 2^(-6(g+2))) enters
@@ -196,33 +212,33 @@ __global__ void __launch_bounds__(THREADS, 1) gemm_ozaki_kernel(const __grid_con
   const bool ok = tc::mbar_wait(done, 0, err);
   tc::fence_after();
   if (ok && !*(volatile int*)err) {
-    // warp w reads TMEM lanes 32 (w % 4) .. +31 (rows) and the 32-column block w / 4
-    const int wq = warp & 3;
+    // warp w reads TMEM lanes 32 (w % 4) .. +31 (rows) and the 16-column block w / 4
+    constexpr int EC = EPI_COLS;
+    const int wq = warp & 3, cb = warp >> 2;
     const int row = m0 + wq * 32 + lane;
     const int er = row < M ? ea[row] : 0;
-#pragma unroll 1
-    for (int cb = warp >> 2; cb < BN / 32; cb += THREADS / 128) {
-      long long fx[32];
+    {
+      long long fx[EC];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) fx[i] = 0;
+      for (int i = 0; i < EC; ++i) fx[i] = 0;
 #pragma unroll 1
       for (int g = 0; g < nd; ++g) {
-        float v[32];
-        tc::tmem_ld32(tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(g * BN + cb * 32), v);
+        float v[EC];
+        tmem_ld16(tmem + ((uint32_t)(wq * 32) << 16) + (uint32_t)(g * BN + cb * EC), v);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) fx[i] += group_fixed(v[i], g);
+        for (int i = 0; i < EC; ++i) fx[i] += group_fixed(v[i], g);
       }
       if (row < M) {
-        const long long c0 = n0 + cb * 32;
-        const int ncb = (int)min((long long)32, Ncol - c0);
+        const long long c0 = n0 + cb * EC;
+        const int ncb = (int)max(0ll, min((long long)EC, Ncol - c0));
         double* dst = C + c0 * (long long)M + row;
-        double old[32];
+        double old[EC];
         if (EPI == 1) {
 #pragma unroll
-          for (int i = 0; i < 32; ++i) old[i] = i < ncb ? dst[(long long)i * M] : 0.0;
+          for (int i = 0; i < EC; ++i) old[i] = i < ncb ? dst[(long long)i * M] : 0.0;
         }
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
+        for (int i = 0; i < EC; ++i) {
           if (i < ncb) {
             const double val = fixed_to_double(fx[i], er + eb[c0 + i] - kFixBits);
             dst[(long long)i * M] = EPI == 1 ? old[i] + val : val;
