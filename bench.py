@@ -376,7 +376,8 @@ def run_ours(args, rank, world, dist):
         "converged_points": int(pts_all), "points_attempted": len(statuses) * world,
         "gmres_iterations_per_point": round(iters_per_point, 1),
         "gummel_iterations_per_point": round(gummel_its / max(1, len(statuses)), 2),
-        "roofline": roof, "rooflines": roofs, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clk,
+        "roofline": roof, "rooflines": roofs, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+        "gpu_launches_by_class": {c: int(v[2]) for c, v in counted.items() if v[2]}, "clocks": clk,
         "plain": plain, "mixed_exact_gummel": mixed_exact, "accuracy": accuracy, "apply": apply,
         "parity_note": "1D oracle parity unpinned against the reference itself (MATLAB/Octave absent, no 1D golden "
                        "vectors in the reference); pinned to the oracle restatement; the Full-2D path is pinned to "

@@ -137,15 +137,16 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Sum over a block of up to 256 threads; the result is valid in warp 0.
 __device__ double block_sum1(double v) {
   __shared__ double s[8];
   v = warp_sum(v);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
   if (lane == 0) s[w] = v;
   __syncthreads();
   double r = 0;
   if (threadIdx.x < 32) {
-    r = lane < 8 ? s[lane] : 0.0;
+    r = lane < nw ? s[lane] : 0.0;
     r = warp_sum(r);
   }
   __syncthreads();
@@ -170,22 +171,39 @@ __device__ __forceinline__ bool last_block_of_problem(int* __restrict__ count, i
 __device__ void dot_reduce_block(const double2* __restrict__ partial, double2* __restrict__ hcol,
                                  float2* __restrict__ hcol32, double2* __restrict__ H, int b, int nv, int k,
                                  int pstride, int m, int nchunk, int first) {
+  // warp w takes the coefficients w, w + nw, w + 2 nw, w + 3 nw together, so that the loads
+  // of four partial rows are in flight at once (this tail runs after the grid's last block)
+  constexpr int U = 4;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = w; i < nv; i += nw) {
-    double2 acc = make_double2(0, 0);
+  for (int i0 = w; i0 < nv; i0 += U * nw) {
+    double2 acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc[u] = make_double2(0, 0);
+#pragma unroll 2
     for (int c = lane; c < nchunk; c += 32) {
-      const double2 t = __ldcg(&partial[((long long)b * pstride + i) * nchunk + c]);
-      acc.x += t.x;
-      acc.y += t.y;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int i = i0 + u * nw;
+        if (i < nv) {
+          const double2 t = __ldcg(&partial[((long long)b * pstride + i) * nchunk + c]);
+          acc[u].x += t.x;
+          acc[u].y += t.y;
+        }
+      }
     }
-    acc.x = warp_sum(acc.x);
-    acc.y = warp_sum(acc.y);
-    if (lane == 0) {
-      hcol[b * pstride + i] = acc;
-      if (hcol32) hcol32[b * pstride + i] = make_float2((float)acc.x, (float)acc.y);
-      double2* h = H + (long long)b * pstride * m + (long long)k * pstride + i;
-      if (first) *h = acc;
-      else { h->x += acc.x; h->y += acc.y; }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * nw;
+      if (i >= nv) continue;   // warp-uniform
+      acc[u].x = warp_sum(acc[u].x);
+      acc[u].y = warp_sum(acc[u].y);
+      if (lane == 0) {
+        hcol[b * pstride + i] = acc[u];
+        if (hcol32) hcol32[b * pstride + i] = make_float2((float)acc[u].x, (float)acc[u].y);
+        double2* h = H + (long long)b * pstride * m + (long long)k * pstride + i;
+        if (first) *h = acc[u];
+        else { h->x += acc[u].x; h->y += acc[u].y; }
+      }
     }
   }
 }
@@ -291,6 +309,28 @@ __global__ void __launch_bounds__(256) multidot_kernel(const VB* __restrict__ V,
       wv[j] = n < N4 ? wb[n] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     int i = 0;
+    // four basis vectors per pass: 16 loads in flight per thread between two reductions
+    for (; i + 3 < nv; i += 4) {
+      const VB* v0 = V + ((long long)b * mp1 + i) * N;
+      float4 a[4][E4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int j = 0; j < E4; ++j) {
+          const long long n = base4 + (long long)j * 256;
+          a[u][j] = n < N4 ? ld_pair(v0 + (long long)u * N, n) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      AccF32 s4[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int j = 0; j < E4; ++j) s4[u].add_cdot4(a[u][j], wv[j]);
+        s4[u].warp_reduce();
+      }
+      if (lane == 0)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) s4[u].stage(red + ((i + u) * 8 + warp) * 4);
+    }
     for (; i + 1 < nv; i += 2) {
       const VB* v0 = V + ((long long)b * mp1 + i) * N;
       const VB* v1 = v0 + N;
@@ -358,12 +398,13 @@ __global__ void __launch_bounds__(256) multidot_kernel(const VB* __restrict__ V,
 
 
 
-// w -= sum_i V_i hcol_i.  Grid (ceil(N/256), B): 256 complex values per block, one per
-// thread for FP64 vectors, two per thread (16-byte accesses, 128 threads) for FP32
-// vectors; the coefficients are staged in shared memory.
+// w -= sum_i V_i hcol_i.  FP64 vectors: grid (ceil(N/256), B), one complex value per
+// thread; FP32 vectors: grid (ceil(N/(256 kGsPairs)), B), 128 threads of kGsPairs 16-byte
+// accesses (two complex values each); the coefficients are staged in shared memory.
 // MODE 0: update only.  MODE >= 1: also nrm_partial[b][block] = sum |w|^2, and the last
 // block of problem b finishes the step: MODE 1 runs the DGKS test (reorth[b]) and, when
 // no second pass is needed, MODE 2's work: |w|, H[k+1][k], inverse norm, Givens step.
+constexpr int kGsPairs = 2;
 template <typename T, int MODE, typename VB = T>
 __global__ void __launch_bounds__(256) gs_update_kernel(const VB* __restrict__ V, T* __restrict__ w,
                                                         const T* __restrict__ hcol, const int* __restrict__ mask,
@@ -376,25 +417,42 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const VB* __restrict__ V
   __syncthreads();
   typename AccFor<T>::type a;
   if constexpr (std::is_same<T, float2>::value) {
+    // kGsPairs float4 (two complex values each) per thread, 128 apart: the grid of a handle
+    // fits one wave of resident blocks and every basis pass has kGsPairs loads per thread
     const long long N4 = N / 2;
-    const long long n4 = (long long)blockIdx.x * 128 + threadIdx.x;
-    if (n4 < N4) {
-      float4* wp = reinterpret_cast<float4*>(w + (long long)b * N) + n4;
-      float4 acc = *wp;
-      const VB* v = V + (long long)b * mp1 * N;
+    const long long n40 = (long long)blockIdx.x * (128 * kGsPairs) + threadIdx.x;
+    float4* wp = reinterpret_cast<float4*>(w + (long long)b * N);
+    float4 acc[kGsPairs];
+#pragma unroll
+    for (int g = 0; g < kGsPairs; ++g) {
+      const long long n4 = n40 + 128 * g;
+      acc[g] = n4 < N4 ? wp[n4] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const VB* v = V + (long long)b * mp1 * N;
 #pragma unroll 4
-      for (int i = 0; i < nv; ++i) {
-        const float4 x = ld_pair(v, (long long)i * N4 + n4);
-        const float2 h = hs[i];
-        acc.x = fmaf(-x.x, h.x, fmaf(x.y, h.y, acc.x));
-        acc.y = fmaf(-x.x, h.y, fmaf(-x.y, h.x, acc.y));
-        acc.z = fmaf(-x.z, h.x, fmaf(x.w, h.y, acc.z));
-        acc.w = fmaf(-x.z, h.y, fmaf(-x.w, h.x, acc.w));
+    for (int i = 0; i < nv; ++i) {
+      const float2 h = hs[i];
+#pragma unroll
+      for (int g = 0; g < kGsPairs; ++g) {
+        const long long n4 = n40 + 128 * g;
+        if (n4 < N4) {
+          const float4 x = ld_pair(v, (long long)i * N4 + n4);
+          acc[g].x = fmaf(-x.x, h.x, fmaf(x.y, h.y, acc[g].x));
+          acc[g].y = fmaf(-x.x, h.y, fmaf(-x.y, h.x, acc[g].y));
+          acc[g].z = fmaf(-x.z, h.x, fmaf(x.w, h.y, acc[g].z));
+          acc[g].w = fmaf(-x.z, h.y, fmaf(-x.w, h.x, acc[g].w));
+        }
       }
-      *wp = acc;
-      if (MODE) {
-        a.add_norm(make_float2(acc.x, acc.y));
-        a.add_norm(make_float2(acc.z, acc.w));
+    }
+#pragma unroll
+    for (int g = 0; g < kGsPairs; ++g) {
+      const long long n4 = n40 + 128 * g;
+      if (n4 < N4) {
+        wp[n4] = acc[g];
+        if (MODE) {
+          a.add_norm(make_float2(acc[g].x, acc[g].y));
+          a.add_norm(make_float2(acc[g].z, acc[g].w));
+        }
       }
     }
   } else {
@@ -417,11 +475,14 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const VB* __restrict__ V
     if (threadIdx.x == 0)
       nrm_partial[(long long)b * nblk + blockIdx.x] = AccFor<T>::type::combine(wsum, blockDim.x >> 5).x;
     if (!last_block_of_problem(tl.gs_count, b)) return;
+    // the whole last block adds the partial norms (independent loads), warp 0 finishes the step
+    double w2p = 0;
+#pragma unroll 8
+    for (int c = threadIdx.x; c < nblk; c += blockDim.x) w2p += __ldcg(&nrm_partial[(long long)b * nblk + c]);
+    const double w2b = block_sum1(w2p);
     if (threadIdx.x < 32) {
       const int lane = threadIdx.x;
-      double w2 = 0;
-      for (int c = lane; c < nblk; c += 32) w2 += __ldcg(&nrm_partial[(long long)b * nblk + c]);
-      w2 = warp_sum(w2);
+      const double w2 = w2b;
       bool finish = true;
       if (MODE == 1) {
         double h2 = 0;
@@ -537,11 +598,15 @@ __global__ void cycle_init_kernel(const double* __restrict__ nrm, const double* 
 
 // y = R^-1 g for the rotated Hessenberg matrix R (upper triangular, column-major per
 // problem), one warp per problem: column-oriented back substitution, the lanes update
-// the remaining right-hand side with column i of R while lane 0 divides.
+// the remaining right-hand side with column i of R.  The inverse diagonal is formed for
+// all rows at once first, and column i - 1 is loaded into registers while column i is
+// applied, so the serial sweep waits on neither a division nor a load per row.
 __global__ void backsolve_kernel(const double2* __restrict__ H, const double2* __restrict__ g,
                                  double2* __restrict__ y, float2* __restrict__ y32, const int* __restrict__ kused,
                                  int pstride, int m, int batch) {
+  constexpr int JT = kMaxRestart / 32;   // column entries per lane
   __shared__ double2 acc[kMaxRestart + 1];
+  __shared__ double2 dinv[kMaxRestart];
   const int b = blockIdx.x;
   const int lane = threadIdx.x;
   if (b >= batch) return;
@@ -552,21 +617,38 @@ __global__ void backsolve_kernel(const double2* __restrict__ H, const double2* _
     acc[i] = i < kk ? g[b * pstride + i] : make_double2(0, 0);
     if (i >= kk) yb[i] = make_double2(0, 0);
   }
+  for (int i = lane; i < kk; i += 32) {
+    const double2 d = Hb[(long long)i * pstride + i];
+    const double dd = d.x * d.x + d.y * d.y;
+    dinv[i] = dd > 0 ? make_double2(d.x / dd, -d.y / dd) : make_double2(0, 0);
+  }
+  double2 cur[JT], nxt[JT];
+#pragma unroll
+  for (int t = 0; t < JT; ++t) {
+    const int j = lane + 32 * t;
+    cur[t] = (kk > 0 && j < kk - 1) ? Hb[(long long)(kk - 1) * pstride + j] : make_double2(0, 0);
+  }
   __syncwarp();
   for (int i = kk - 1; i >= 0; --i) {
-    const double2* col = Hb + (long long)i * pstride;
-    const double2 d = col[i];
-    const double dd = d.x * d.x + d.y * d.y;
-    const double2 a = acc[i];
-    const double2 yi = dd > 0 ? make_double2((a.x * d.x + a.y * d.y) / dd, (a.y * d.x - a.x * d.y) / dd)
-                              : make_double2(0, 0);
+#pragma unroll
+    for (int t = 0; t < JT; ++t) {
+      const int j = lane + 32 * t;
+      nxt[t] = (i > 0 && j < i - 1) ? Hb[(long long)(i - 1) * pstride + j] : make_double2(0, 0);
+    }
+    const double2 yi = cmul(acc[i], dinv[i]);
     if (lane == 0) yb[i] = yi;
-    for (int j = lane; j < i; j += 32) {
-      const double2 t = cmul(col[j], yi);
-      acc[j].x -= t.x;
-      acc[j].y -= t.y;
+#pragma unroll
+    for (int t = 0; t < JT; ++t) {
+      const int j = lane + 32 * t;
+      if (j < i) {
+        const double2 u = cmul(cur[t], yi);
+        acc[j].x -= u.x;
+        acc[j].y -= u.y;
+      }
     }
     __syncwarp();
+#pragma unroll
+    for (int t = 0; t < JT; ++t) cur[t] = nxt[t];
   }
   __syncwarp();
   if (y32)
@@ -640,7 +722,10 @@ int arnoldi_step(Problem& P, VB* V, T* w, int k, int m, Prec prec, Apply apply) 
   WG_CK(apply());
   const int nv = k + 1;
   const double vec = (double)N * B * sizeof(T), vecb = (double)N * B * sizeof(VB);
-  const dim3 gu((unsigned)((N + 255) / 256), B);
+  // the FP32 update covers 256 kGsPairs complex values per block of 128 threads
+  const long long per_blk = sizeof(T) == sizeof(float2) ? 256LL * kGsPairs : 256LL;
+  const dim3 gu((unsigned)((N + per_blk - 1) / per_blk), B);
+  const int nblk = (int)gu.x;
   // classical Gram-Schmidt; the second pass runs for the problems that fail the DGKS
   // test (its kernels see P.reorth as their activity mask), for all with eta >= 1,
   // for none with eta < 0.  The reductions, the norm and the Givens step run in the
@@ -664,13 +749,13 @@ int arnoldi_step(Problem& P, VB* V, T* w, int k, int m, Prec prec, Apply apply) 
     ev = prof_begin(P, PROF_GSUPDATE, 1, nv * vecb + 2 * vec, 8.0 * nv * N * B, mask);
     if (pass == passes - 1)
       gs_update_kernel<T, 2, VB><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv,
-                                                                 mp1, ps, P.nblk, tl);
+                                                                 mp1, ps, nblk, tl);
     else if (eta < 1)
       gs_update_kernel<T, 1, VB><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv,
-                                                                 mp1, ps, P.nblk, tl);
+                                                                 mp1, ps, nblk, tl);
     else
       gs_update_kernel<T, 0, VB><<<gu, gthreads, 0, P.stream>>>(V, w, coef_col<T>(P), mask, P.nrm_partial, N, nv,
-                                                                 mp1, ps, P.nblk, tl);
+                                                                 mp1, ps, nblk, tl);
     prof_end(P, PROF_GSUPDATE, ev);
   }
   // V_{k+1} = w / |w| is written by the next step's preconditioner
