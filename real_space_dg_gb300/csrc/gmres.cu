@@ -429,18 +429,28 @@ __global__ void __launch_bounds__(256) gs_update_kernel(const VB* __restrict__ V
       acc[g] = n4 < N4 ? wp[n4] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
     const VB* v = V + (long long)b * mp1 * N;
-#pragma unroll 4
-    for (int i = 0; i < nv; ++i) {
-      const float2 h = hs[i];
+    // the loads of four basis vectors are issued before their updates are applied
+    constexpr int U = 4;
+    for (int i0 = 0; i0 < nv; i0 += U) {
+      float4 x[U][kGsPairs];
 #pragma unroll
-      for (int g = 0; g < kGsPairs; ++g) {
-        const long long n4 = n40 + 128 * g;
-        if (n4 < N4) {
-          const float4 x = ld_pair(v, (long long)i * N4 + n4);
-          acc[g].x = fmaf(-x.x, h.x, fmaf(x.y, h.y, acc[g].x));
-          acc[g].y = fmaf(-x.x, h.y, fmaf(-x.y, h.x, acc[g].y));
-          acc[g].z = fmaf(-x.z, h.x, fmaf(x.w, h.y, acc[g].z));
-          acc[g].w = fmaf(-x.z, h.y, fmaf(-x.w, h.x, acc[g].w));
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int g = 0; g < kGsPairs; ++g) {
+          const long long n4 = n40 + 128 * g;
+          x[u][g] = (i0 + u < nv && n4 < N4) ? ld_pair(v, (long long)(i0 + u) * N4 + n4)
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        // past nv the coefficient is zero and the (zero) loads change nothing
+        const float2 h = i0 + u < nv ? hs[i0 + u] : make_float2(0.f, 0.f);
+#pragma unroll
+        for (int g = 0; g < kGsPairs; ++g) {
+          acc[g].x = fmaf(-x[u][g].x, h.x, fmaf(x[u][g].y, h.y, acc[g].x));
+          acc[g].y = fmaf(-x[u][g].x, h.y, fmaf(-x[u][g].y, h.x, acc[g].y));
+          acc[g].z = fmaf(-x[u][g].z, h.x, fmaf(x[u][g].w, h.y, acc[g].z));
+          acc[g].w = fmaf(-x[u][g].z, h.y, fmaf(-x[u][g].w, h.x, acc[g].w));
         }
       }
     }
