@@ -163,9 +163,10 @@ def make_workload(batch):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one timed gemm_f64_tc event of the mixed form (digit
 # slicing + emulated GEMM; the mean of the C = AB and C += AB launches) per state column (element x node), from
-# one ncu capture at batch 8 (7,680 columns; profiles/gemm_ozaki_c2_batch8_mixed.md): slicing 39.6 MB, GEMMs
-# 75.9 and 109.2 MB.  The traffic grows with the columns, so a launch of the bench's batch scales by its columns.
-OZAKI_TRAFFIC_PER_COLUMN = (39.61e6 + 0.5 * (75.94e6 + 109.17e6)) / 7680
+# ncu captures of residuals at 5 digits (profiles/gemm_ozaki_c2_batch8_mixed.md): the GEMMs at batch 8 (7,680
+# columns) 44.5 and 75.8 MB, the slicing at a 2-problem handle (1,920 columns) 7.9 MB (its digit writes stay in
+# L2).  The traffic grows with the columns, so a launch of the bench's batch scales by its columns.
+OZAKI_TRAFFIC_PER_COLUMN = 7.89e6 / 1920 + 0.5 * (44.53e6 + 75.75e6) / 7680
 FP64_NOMINAL_TFLOPS = 1.25   # no FP64 peak is measured on this machine: nominal GB300 FP64 (CUDA cores)
 
 
