@@ -78,8 +78,6 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_maps_kernel(
   T s;
   s.x = R(0);
   s.y = R(0);
-  // unrolled so that the loads of the next elements (independent of the recurrence) issue early
-#pragma unroll 4
   for (int i = 0; i < e_hi - e_lo; ++i) {
     const int e = fwd ? e_lo + i : e_hi - 1 - i;
     const T* re = rb + (long long)e * NK * nk;
@@ -155,7 +153,6 @@ __global__ void __launch_bounds__(32 * kChunksPerBlock) kline_apply_kernel(
   const T* rb = r + (long long)b * r_stride + j;
   T* zbase = z + (long long)b * N + j;
   O* obase = rout ? rout + (long long)b * rout_stride + j : nullptr;
-#pragma unroll 4
   for (int i = 0; i < e_hi - e_lo; ++i) {
     const int e = fwd ? e_lo + i : e_hi - 1 - i;
     const T* re = rb + (long long)e * NK * nk;
